@@ -1,0 +1,203 @@
+// Test infrastructure: NOT part of the product.
+//
+// Driver that runs the reference implementation (IMSRG++ compiled from its own
+// sources by oracle/ref_build.mk) on operators read from binary "arena" files
+// and writes the results in the same arena layout.  It is only used in the
+// build container to produce the golden fixtures under tests/golden/ and to pin
+// the C oracle (oracle/imsrg_oracle.c) against the reference itself.
+//
+// Arena layout (doubles, shared with the product and the C oracle):
+//   [0]                ZeroBody
+//   [32 .. 32+N*N)     OneBody, N x N column-major (N = number of orbits)
+//   then, for each two-body channel ch = 6J + 2(Tz+1) + parity in index order,
+//   an n_ch x n_ch column-major block (local ket order of TwoBodyChannel),
+//   every block starting on a multiple of 32 doubles.
+//
+// usage: ref_harness <emax> <X.bin> <Y.bin> <W.bin> <outdir>
+//   X hermitian, Y anti-hermitian, W hermitian.  Writes
+//     tables.txt                      orbits and channel ket lists
+//     <case>_<term>.bin               term applied to a zeroed Z
+//     <case>_full.bin                 Commutator::CommutatorScalarScalar
+//   for the cases  xy = [X,Y] (Z hermitian), yx = [Y,X] (Z hermitian),
+//   xw = [X,W] (Z anti-hermitian), and
+//     bch.bin                         BCH::BCH_Transform(X, 0.25*Y/|Y|)
+//     norms.txt                       Operator::Norm of the inputs
+
+#include "ModelSpace.hh"
+#include "Operator.hh"
+#include "Commutator.hh"
+#include "BCH.hh"
+
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <string>
+#include <vector>
+
+static size_t round32(size_t x) { return (x + 31) / 32 * 32; }
+
+struct ArenaLayout {
+  size_t n_orb = 0;
+  std::vector<size_t> off2;  // per channel
+  std::vector<size_t> dim2;
+  size_t total = 0;
+};
+
+static ArenaLayout make_layout(ModelSpace& ms) {
+  ArenaLayout L;
+  L.n_orb = ms.GetNumberOrbits();
+  size_t cur = round32(32 + L.n_orb * L.n_orb);
+  int nch = ms.GetNumberTwoBodyChannels();
+  for (int ch = 0; ch < nch; ++ch) {
+    size_t n = ms.GetTwoBodyChannel(ch).GetNumberKets();
+    L.off2.push_back(cur);
+    L.dim2.push_back(n);
+    cur = round32(cur + n * n);
+  }
+  L.total = cur;
+  return L;
+}
+
+static std::vector<double> read_file(const std::string& path, size_t expect) {
+  std::vector<double> v(expect, 0.0);
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) { std::cerr << "cannot open " << path << "\n"; std::exit(2); }
+  size_t got = std::fread(v.data(), sizeof(double), expect, f);
+  std::fclose(f);
+  if (got != expect) { std::cerr << path << ": expected " << expect << " doubles, got " << got << "\n"; std::exit(2); }
+  return v;
+}
+
+static void write_file(const std::string& path, const std::vector<double>& v) {
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) { std::cerr << "cannot write " << path << "\n"; std::exit(2); }
+  std::fwrite(v.data(), sizeof(double), v.size(), f);
+  std::fclose(f);
+}
+
+static void load(Operator& op, const std::vector<double>& a, const ArenaLayout& L) {
+  op.ZeroBody = a[0];
+  for (size_t c = 0; c < L.n_orb; ++c)
+    for (size_t r = 0; r < L.n_orb; ++r) op.OneBody(r, c) = a[32 + c * L.n_orb + r];
+  for (size_t ch = 0; ch < L.off2.size(); ++ch) {
+    size_t n = L.dim2[ch];
+    if (n == 0) continue;
+    arma::mat& M = op.TwoBody.GetMatrix(ch, ch);
+    for (size_t c = 0; c < n; ++c)
+      for (size_t r = 0; r < n; ++r) M(r, c) = a[L.off2[ch] + c * n + r];
+  }
+}
+
+static std::vector<double> store(const Operator& op, const ArenaLayout& L) {
+  std::vector<double> a(L.total, 0.0);
+  a[0] = op.ZeroBody;
+  for (size_t c = 0; c < L.n_orb; ++c)
+    for (size_t r = 0; r < L.n_orb; ++r) a[32 + c * L.n_orb + r] = op.OneBody(r, c);
+  for (size_t ch = 0; ch < L.off2.size(); ++ch) {
+    size_t n = L.dim2[ch];
+    if (n == 0) continue;
+    const arma::mat& M = op.TwoBody.GetMatrix(ch, ch);
+    for (size_t c = 0; c < n; ++c)
+      for (size_t r = 0; r < n; ++r) a[L.off2[ch] + c * n + r] = M(r, c);
+  }
+  return a;
+}
+
+static void dump_tables(ModelSpace& ms, const std::string& path) {
+  std::ofstream out(path);
+  int norb = ms.GetNumberOrbits();
+  out << "orbits " << norb << "\n";
+  for (int i = 0; i < norb; ++i) {
+    Orbit& o = ms.GetOrbit(i);
+    out << i << " " << o.n << " " << o.l << " " << o.j2 << " " << o.tz2 << " " << std::setprecision(17) << o.occ << "\n";
+  }
+  int nch = ms.GetNumberTwoBodyChannels();
+  out << "channels " << nch << "\n";
+  for (int ch = 0; ch < nch; ++ch) {
+    TwoBodyChannel& tbc = ms.GetTwoBodyChannel(ch);
+    int n = tbc.GetNumberKets();
+    out << ch << " " << tbc.J << " " << tbc.parity << " " << tbc.Tz << " " << n;
+    for (int i = 0; i < n; ++i) out << " " << tbc.GetKet(i).p << " " << tbc.GetKet(i).q;
+    out << "\n";
+    out << "pp " << tbc.GetKetIndex_pp().n_elem;
+    for (auto x : tbc.GetKetIndex_pp()) out << " " << x;
+    out << "\nhh " << tbc.GetKetIndex_hh().n_elem;
+    for (auto x : tbc.GetKetIndex_hh()) out << " " << x;
+    out << "\nph " << tbc.GetKetIndex_ph().n_elem;
+    for (auto x : tbc.GetKetIndex_ph()) out << " " << x;
+    out << "\n";
+  }
+  out << "cc_channels " << nch << "\n";
+  for (int ch = 0; ch < nch; ++ch) {
+    TwoBodyChannel_CC& tbc = ms.GetTwoBodyChannel_CC(ch);
+    int n = tbc.GetNumberKets();
+    out << ch << " " << tbc.J << " " << tbc.parity << " " << tbc.Tz << " " << n;
+    for (int i = 0; i < n; ++i) out << " " << tbc.GetKet(i).p << " " << tbc.GetKet(i).q;
+    out << "\n";
+    out << "hh " << tbc.GetKetIndex_hh().n_elem;
+    for (auto x : tbc.GetKetIndex_hh()) out << " " << x;
+    out << "\nph " << tbc.GetKetIndex_ph().n_elem;
+    for (auto x : tbc.GetKetIndex_ph()) out << " " << x;
+    out << "\n";
+  }
+}
+
+typedef void (*term_fn)(const Operator&, const Operator&, Operator&);
+
+int main(int argc, char** argv) {
+  if (argc != 6) {
+    std::cerr << "usage: ref_harness <emax> <X.bin> <Y.bin> <W.bin> <outdir>\n";
+    return 1;
+  }
+  int emax = std::atoi(argv[1]);
+  std::string outdir = argv[5];
+  ModelSpace ms(emax, "O16", "O16");
+  ArenaLayout L = make_layout(ms);
+  dump_tables(ms, outdir + "/tables.txt");
+
+  Operator X(ms, 0, 0, 0, 2), Y(ms, 0, 0, 0, 2), W(ms, 0, 0, 0, 2);
+  X.SetHermitian();
+  Y.SetAntiHermitian();
+  W.SetHermitian();
+  load(X, read_file(argv[2], L.total), L);
+  load(Y, read_file(argv[3], L.total), L);
+  load(W, read_file(argv[4], L.total), L);
+
+  {
+    std::ofstream nf(outdir + "/norms.txt");
+    nf << std::setprecision(17) << X.Norm() << " " << Y.Norm() << " " << W.Norm() << "\n";
+  }
+
+  struct Term { const char* name; term_fn fn; };
+  const Term terms[] = {
+      {"comm110ss", Commutator::comm110ss},
+      {"comm220ss", Commutator::comm220ss},
+      {"comm111ss", Commutator::comm111ss},
+      {"comm121ss", Commutator::comm121ss},
+      {"comm122ss", Commutator::comm122ss},
+      {"comm222_pp_hh_221ss", Commutator::comm222_pp_hh_221ss},
+      {"comm222_pp_hhss", Commutator::comm222_pp_hhss},
+      {"comm221ss", Commutator::comm221ss},
+      {"comm222_phss", Commutator::comm222_phss},
+  };
+  struct Case { const char* name; const Operator* a; const Operator* b; bool z_herm; };
+  const Case cases[] = {{"xy", &X, &Y, true}, {"yx", &Y, &X, true}, {"xw", &X, &W, false}};
+
+  for (const Case& cs : cases) {
+    for (const Term& t : terms) {
+      Operator Z(ms, 0, 0, 0, 2);
+      if (cs.z_herm) Z.SetHermitian(); else Z.SetAntiHermitian();
+      t.fn(*cs.a, *cs.b, Z);
+      write_file(outdir + "/" + cs.name + "_" + t.name + ".bin", store(Z, L));
+    }
+    Operator Zf = Commutator::CommutatorScalarScalar(*cs.a, *cs.b);
+    write_file(outdir + "/" + cs.name + "_full.bin", store(Zf, L));
+  }
+
+  Operator Omega = Y * (0.25 / Y.Norm());
+  Operator Hs = BCH::BCH_Transform(X, Omega);
+  write_file(outdir + "/bch.bin", store(Hs, L));
+  return 0;
+}

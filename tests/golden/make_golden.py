@@ -1,0 +1,125 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Runs the reference IMSRG++ commutator code, compiled from its own sources by
+oracle/ref_build.mk into oracle/_ref/ref_harness, on seeded random operators
+and stores inputs and outputs as compressed .npz files.  Needs the reference
+sources (build container only):
+
+    make -f oracle/ref_build.mk -j8
+    python tests/golden/make_golden.py
+
+Fixtures (arena layout: see oracle/modelspace_ref.py):
+  golden_emax2.npz   X (hermitian), Y (anti-hermitian), W (hermitian); for the
+                     cases xy=[X,Y], yx=[Y,X], xw=[X,W]: every IMSRG(2) term on a
+                     zeroed Z and the full CommutatorScalarScalar; the
+                     BCH_Transform of X with Omega = 0.25 Y/|Y|; the reference's
+                     channel tables; Operator::Norm of the inputs.
+  golden_emax3.npz   the same for the case xy only, plus bch.
+  sixj_exact.npz     6j symbols {j1 j2 J3; j4 j5 J6} for half-integer
+                     j <= 9/2 and integer J <= 9, evaluated in exact rational
+                     arithmetic (Racah formula with Python integers), the pin for
+                     every 6j implementation in this repository.
+"""
+
+import os
+import subprocess
+import sys
+import tempfile
+from fractions import Fraction
+from math import factorial, isqrt
+from decimal import Decimal, getcontext
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+from modelspace_ref import RefModelSpace  # noqa: E402
+
+TERMS = ["comm110ss", "comm220ss", "comm111ss", "comm121ss", "comm122ss",
+         "comm222_pp_hh_221ss", "comm222_pp_hhss", "comm221ss", "comm222_phss", "full"]
+
+
+def run_reference(emax, cases):
+    ms = RefModelSpace(emax)
+    X = ms.random_operator(1000 + emax, hermitian=True)
+    Y = ms.random_operator(2000 + emax, hermitian=False)
+    W = ms.random_operator(3000 + emax, hermitian=True)
+    harness = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+    with tempfile.TemporaryDirectory() as td:
+        for name, a in (("X", X), ("Y", Y), ("W", W)):
+            a.tofile(os.path.join(td, name + ".bin"))
+        subprocess.run([harness, str(emax), os.path.join(td, "X.bin"), os.path.join(td, "Y.bin"),
+                        os.path.join(td, "W.bin"), td], check=True, stdout=subprocess.DEVNULL,
+                       env=dict(os.environ, OMP_NUM_THREADS="1"))
+        out = {"X": X, "Y": Y, "W": W, "emax": np.array(emax)}
+        for cs in cases:
+            for t in TERMS:
+                out["%s_%s" % (cs, t)] = np.fromfile(os.path.join(td, "%s_%s.bin" % (cs, t)))
+        out["bch"] = np.fromfile(os.path.join(td, "bch.bin"))
+        with open(os.path.join(td, "tables.txt")) as f:
+            out["tables"] = np.array(f.read())
+        with open(os.path.join(td, "norms.txt")) as f:
+            out["norms"] = np.array([float(x) for x in f.read().split()])
+    return out
+
+
+def _delta2(a, b, c):
+    # a, b, c doubled
+    return Fraction(factorial((a + b - c) // 2) * factorial((a - b + c) // 2) * factorial((-a + b + c) // 2),
+                    factorial((a + b + c) // 2 + 1))
+
+
+def _triad(a, b, c):
+    return (a + b + c) % 2 == 0 and abs(a - b) <= c <= a + b
+
+
+def sixj_exact(ja, jb, jc, jd, je, jf):
+    """6j with doubled arguments, exact: Racah single sum in rationals, then
+    sign * sqrt(prefactor^2) * |sum| rounded to double via 40-digit Decimal."""
+    if not (_triad(ja, jb, jc) and _triad(ja, je, jf) and _triad(jd, jb, jf) and _triad(jd, je, jc)):
+        return 0.0
+    a1, a2, a3, a4 = (ja + jb + jc) // 2, (ja + je + jf) // 2, (jd + jb + jf) // 2, (jd + je + jc) // 2
+    b1, b2, b3 = (ja + jb + jd + je) // 2, (ja + jc + jd + jf) // 2, (jb + jc + je + jf) // 2
+    s = Fraction(0)
+    for t in range(max(a1, a2, a3, a4), min(b1, b2, b3) + 1):
+        den = (factorial(t - a1) * factorial(t - a2) * factorial(t - a3) * factorial(t - a4)
+               * factorial(b1 - t) * factorial(b2 - t) * factorial(b3 - t))
+        s += Fraction((-1) ** t * factorial(t + 1), den)
+    if s == 0:
+        return 0.0
+    pre2 = _delta2(ja, jb, jc) * _delta2(ja, je, jf) * _delta2(jd, jb, jf) * _delta2(jd, je, jc)
+    val2 = pre2 * s * s
+    getcontext().prec = 40
+    v = (Decimal(val2.numerator) / Decimal(val2.denominator)).sqrt()
+    return float(v) if s > 0 else -float(v)
+
+
+def make_sixj_table(jj1max=9, jmax=9):
+    rows = []
+    for ja in range(1, jj1max + 1, 2):
+        for jb in range(1, jj1max + 1, 2):
+            for J3 in range(0, jmax + 1):
+                for jd in range(1, jj1max + 1, 2):
+                    for je in range(1, jj1max + 1, 2):
+                        for J6 in range(0, jmax + 1):
+                            v = sixj_exact(ja, jb, 2 * J3, jd, je, 2 * J6)
+                            if v != 0.0:
+                                rows.append((ja, jb, J3, jd, je, J6, v))
+    arr = np.array(rows)
+    return arr[:, :6].astype(np.int16), arr[:, 6].copy()
+
+
+def main():
+    g2 = run_reference(2, ["xy", "yx", "xw"])
+    np.savez_compressed(os.path.join(HERE, "golden_emax2.npz"), **g2)
+    g3 = run_reference(3, ["xy"])
+    np.savez_compressed(os.path.join(HERE, "golden_emax3.npz"), **g3)
+    keys, vals = make_sixj_table()
+    np.savez_compressed(os.path.join(HERE, "sixj_exact.npz"), keys=keys, values=vals)
+    for f in ("golden_emax2.npz", "golden_emax3.npz", "sixj_exact.npz"):
+        print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
+
+
+if __name__ == "__main__":
+    main()
