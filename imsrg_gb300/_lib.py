@@ -1,0 +1,106 @@
+"""ctypes binding of the C ABI (include/imsrg_gb300.h).
+
+Loads imsrg_gb300/_build/libimsrg_gb300.so, building it first if the sources
+are newer.  There is no fallback: if the library cannot be built or loaded,
+importing raises.
+"""
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+OK = 0
+ERR_ARG = 1
+ERR_CUDA = 2
+ERR_UNSUPPORTED = 3
+ERR_NOMEM = 4
+ERR_KERNEL = 5
+PREC_FP64 = 0
+PREC_SPLIT = 1
+
+_lock = threading.Lock()
+_lib = None
+
+P = ctypes.c_void_p
+I = ctypes.c_int
+IP = ctypes.POINTER(ctypes.c_int)
+D = ctypes.c_double
+DP = ctypes.POINTER(ctypes.c_double)
+LL = ctypes.c_longlong
+LLP = ctypes.POINTER(ctypes.c_longlong)
+
+# name -> (restype, argtypes); every function declared in include/imsrg_gb300.h
+SIGNATURES = {
+    "imsrg_last_error": (ctypes.c_char_p, []),
+    "imsrg_space_create": (I, [I, I, IP, IP, IP, IP, DP, ctypes.POINTER(P)]),
+    "imsrg_space_create_reference": (I, [I, I, I, ctypes.POINTER(P)]),
+    "imsrg_space_destroy": (None, [P]),
+    "imsrg_space_sizes": (I, [P, IP, IP, LLP]),
+    "imsrg_space_orbit": (I, [P, I, IP, IP, IP, IP, DP]),
+    "imsrg_space_channel": (I, [P, I, IP, IP, IP, IP, LLP]),
+    "imsrg_space_channel_kets": (I, [P, I, IP, IP]),
+    "imsrg_space_cc_channel": (I, [P, I, IP, IP, IP, IP, IP, IP]),
+    "imsrg_space_sixj": (I, [P, I, I, I, I, I, I, DP]),
+    "imsrg_op_create": (I, [P, I, ctypes.POINTER(P)]),
+    "imsrg_op_destroy": (None, [P]),
+    "imsrg_op_hermiticity": (I, [P, IP]),
+    "imsrg_op_set_hermiticity": (I, [P, I]),
+    "imsrg_op_upload": (I, [P, DP, P]),
+    "imsrg_op_download": (I, [P, DP, P]),
+    "imsrg_op_device_arena": (I, [P, ctypes.POINTER(P)]),
+    "imsrg_op_zero": (I, [P, P]),
+    "imsrg_op_copy": (I, [P, P, P]),
+    "imsrg_op_scale": (I, [P, D, P]),
+    "imsrg_op_axpy": (I, [P, D, P, P]),
+    "imsrg_op_norm": (I, [P, DP, P]),
+    "imsrg_op_fill_random": (I, [P, ctypes.c_ulonglong, P]),
+    "imsrg_comm110ss": (I, [P, P, P, P]),
+    "imsrg_comm220ss": (I, [P, P, P, P]),
+    "imsrg_comm111ss": (I, [P, P, P, P]),
+    "imsrg_comm121ss": (I, [P, P, P, P]),
+    "imsrg_comm122ss": (I, [P, P, P, P]),
+    "imsrg_comm221ss": (I, [P, P, P, P]),
+    "imsrg_comm222_pp_hhss": (I, [P, P, P, I, P]),
+    "imsrg_comm222_pp_hh_221ss": (I, [P, P, P, I, P]),
+    "imsrg_comm222_phss": (I, [P, P, P, I, P]),
+    "imsrg_commutator_scalar_scalar": (I, [P, P, P, I, P]),
+    "imsrg_set_term": (I, [ctypes.c_char_p, I]),
+    "imsrg_get_term": (I, [ctypes.c_char_p, IP]),
+    "imsrg_set_default_precision": (I, [I]),
+    "imsrg_get_default_precision": (I, [IP]),
+    "imsrg_bch_transform": (I, [P, P, P, D, I, IP, P]),
+}
+
+
+class IMSRGError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("imsrg_gb300 error %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib():
+    """The loaded library (built on first use)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = _build.build()
+            L = ctypes.CDLL(path)
+            for name, (res, args) in SIGNATURES.items():
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+            _lib = L
+    return _lib
+
+
+def library_path():
+    return _build.LIB
+
+
+def check(rc):
+    if rc != OK:
+        msg = lib().imsrg_last_error()
+        raise IMSRGError(rc, msg.decode() if msg else "")
+    return rc

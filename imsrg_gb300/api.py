@@ -1,0 +1,401 @@
+"""Python mirror of the reference's operator / commutator interface on the
+GB300 kernels.
+
+Names, argument meaning and error behaviour follow the reference's pybind11
+module (src/pyIMSRG.cc:649-706 Commutator, :738-747 BCH) so code written
+against pyIMSRG reads the same:
+
+    ms = ModelSpace(6, "O16", "O16")
+    X = Operator(ms, 0, 0, 0, 2); X.SetHermitian()
+    Y = Operator(ms, 0, 0, 0, 2); Y.SetAntiHermitian()
+    Z = Commutator.Commutator(X, Y)            # CommutatorScalarScalar
+    Commutator.comm222_phss(X, Y, Z)           # accumulate one term into Z
+    Hs = BCH.BCH_Transform(H, Omega)
+
+Operator keeps its data on the host in the arena layout (numpy); every call
+uploads the operands, runs the CUDA kernels and downloads the result.
+DeviceOperator keeps an operator resident in HBM for chained device work
+(the BCH series, benchmarks).
+"""
+
+import ctypes
+import re
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+
+_ELEMENTS = ("n H He Li Be B C N O F Ne Na Mg Al Si P S Cl Ar K Ca Sc Ti V Cr Mn Fe Co Ni Cu Zn Ga Ge As Se "
+             "Br Kr Rb Sr Y Zr Nb Mo Tc Ru Rh Pd Ag Cd In Sn Sb Te I Xe Cs Ba La Ce Pr Nd Pm Sm Eu Gd Tb Dy Ho "
+             "Er Tm Yb Lu Hf Ta W Re Os Ir Pt Au Hg Tl Pb Bi Po At Rn").split()
+
+
+def parse_reference(ref):
+    """'O16' -> (A=16, Z=8), as ModelSpace::GetAZfromString."""
+    m = re.fullmatch(r"([A-Za-z]+)(\d+)", ref.strip())
+    if not m:
+        raise ValueError("cannot parse reference %r" % ref)
+    sym, A = m.group(1), int(m.group(2))
+    sym = sym[0].upper() + sym[1:].lower()
+    if sym not in _ELEMENTS:
+        raise ValueError("unknown element %r" % sym)
+    return A, _ELEMENTS.index(sym)
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class ModelSpace:
+    """ModelSpace(emax, reference, valence) for a single reference (the
+    valence argument must name the same nucleus: no valence space)."""
+
+    def __init__(self, emax, reference="O16", valence=None, orbits=None):
+        L = _lib.lib()
+        h = ctypes.c_void_p()
+        if orbits is not None:
+            n, l, j2, tz2, occ = (np.ascontiguousarray(x) for x in orbits)
+            n, l, j2, tz2 = (np.asarray(x, dtype=np.int32) for x in (n, l, j2, tz2))
+            occ = np.asarray(occ, dtype=np.float64)
+            check(L.imsrg_space_create(emax, len(n), _ip(n), _ip(l), _ip(j2), _ip(tz2), _dp(occ), ctypes.byref(h)))
+        else:
+            if valence is not None and valence != reference:
+                raise NotImplementedError("valence spaces are outside the IMSRG(2) commutator scope")
+            A, Z = parse_reference(reference)
+            check(L.imsrg_space_create_reference(emax, A, Z, ctypes.byref(h)))
+        self._h = h
+        self._L = L
+        self.emax = emax
+        norb, nch, arena = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+        check(L.imsrg_space_sizes(h, ctypes.byref(norb), ctypes.byref(nch), ctypes.byref(arena)))
+        self.norb, self.nch, self.arena_size = norb.value, nch.value, arena.value
+        self.orbits = []
+        for i in range(self.norb):
+            v = [ctypes.c_int() for _ in range(4)]
+            o = ctypes.c_double()
+            check(L.imsrg_space_orbit(h, i, *[ctypes.byref(x) for x in v], ctypes.byref(o)))
+            self.orbits.append((v[0].value, v[1].value, v[2].value, v[3].value, o.value))
+        self.channels = []
+        for ch in range(self.nch):
+            J, par, Tz, nk = (ctypes.c_int() for _ in range(4))
+            off = ctypes.c_longlong()
+            check(L.imsrg_space_channel(h, ch, ctypes.byref(J), ctypes.byref(par), ctypes.byref(Tz), ctypes.byref(nk),
+                                        ctypes.byref(off)))
+            p = np.zeros(max(nk.value, 1), dtype=np.int32)
+            q = np.zeros(max(nk.value, 1), dtype=np.int32)
+            if nk.value:
+                check(L.imsrg_space_channel_kets(h, ch, _ip(p), _ip(q)))
+            self.channels.append(dict(J=J.value, parity=par.value, Tz=Tz.value, nkets=nk.value, offset=off.value,
+                                      kets=list(zip(p[:nk.value].tolist(), q[:nk.value].tolist()))))
+
+    def __del__(self):
+        try:
+            self._L.imsrg_space_destroy(self._h)
+        except Exception:
+            pass
+
+    def GetNumberOrbits(self):
+        return self.norb
+
+    def GetNumberTwoBodyChannels(self):
+        return self.nch
+
+    def cc_channel(self, ch):
+        J, par, Tz, nk = (ctypes.c_int() for _ in range(4))
+        check(self._L.imsrg_space_cc_channel(self._h, ch, ctypes.byref(J), ctypes.byref(par), ctypes.byref(Tz),
+                                             ctypes.byref(nk), None, None))
+        p = np.zeros(max(nk.value, 1), dtype=np.int32)
+        q = np.zeros(max(nk.value, 1), dtype=np.int32)
+        check(self._L.imsrg_space_cc_channel(self._h, ch, None, None, None, None, _ip(p), _ip(q)))
+        return dict(J=J.value, parity=par.value, Tz=Tz.value, nkets=nk.value,
+                    kets=list(zip(p[:nk.value].tolist(), q[:nk.value].tolist())))
+
+    def GetSixJ(self, j1, j2, j3, j4, j5, j6):
+        """{j1 j2 j3; j4 j5 j6} with j1, j2, j4, j5 half-integer and j3, j6
+        integer (ModelSpace::GetCachedSixJ argument convention doubled)."""
+        out = ctypes.c_double()
+        check(self._L.imsrg_space_sixj(self._h, int(round(2 * j1)), int(round(2 * j2)), int(j3), int(round(2 * j4)),
+                                       int(round(2 * j5)), int(j6), ctypes.byref(out)))
+        return out.value
+
+
+class _TwoBody:
+    def __init__(self, op):
+        self._op = op
+
+    def GetMatrix(self, ch_bra, ch_ket=None):
+        if ch_ket is not None and ch_ket != ch_bra:
+            raise KeyError("scalar operators only store diagonal channel blocks")
+        ms = self._op.modelspace
+        c = ms.channels[ch_bra]
+        n, o = c["nkets"], c["offset"]
+        return self._op.arena[o:o + n * n].reshape(n, n, order="F")
+
+
+class Operator:
+    """Scalar operator (J=0, parity +, Tz=0, particle rank 2) in the arena
+    layout, host resident.  Operator(ms, 0, 0, 0, 2) as in the reference."""
+
+    def __init__(self, ms, jrank=0, trank=0, parity=0, particle_rank=2, arena=None, hermitian=True):
+        if (jrank, trank, parity) != (0, 0, 0) or particle_rank != 2:
+            raise NotImplementedError("only scalar particle-rank-2 operators are on the GPU path")
+        self.modelspace = ms
+        self.arena = np.zeros(ms.arena_size) if arena is None else np.ascontiguousarray(arena, dtype=np.float64)
+        if self.arena.shape != (ms.arena_size,):
+            raise ValueError("arena has the wrong length")
+        self.hermitian = 1 if hermitian else -1
+        self.TwoBody = _TwoBody(self)
+
+    # hermiticity
+    def SetHermitian(self):
+        self.hermitian = 1
+
+    def SetAntiHermitian(self):
+        self.hermitian = -1
+
+    def IsHermitian(self):
+        return self.hermitian == 1
+
+    def IsAntiHermitian(self):
+        return self.hermitian == -1
+
+    @property
+    def ZeroBody(self):
+        return float(self.arena[0])
+
+    @ZeroBody.setter
+    def ZeroBody(self, v):
+        self.arena[0] = v
+
+    @property
+    def OneBody(self):
+        N = self.modelspace.norb
+        return self.arena[32:32 + N * N].reshape(N, N, order="F")
+
+    def copy(self):
+        return Operator(self.modelspace, arena=self.arena.copy(), hermitian=self.hermitian == 1)
+
+    def Erase(self):
+        self.arena[:] = 0
+
+    def Norm(self):
+        with DeviceOperator.from_host(self) as d:
+            return d.norm()
+
+    def __iadd__(self, other):
+        self.arena += other.arena
+        return self
+
+    def __isub__(self, other):
+        self.arena -= other.arena
+        return self
+
+    def __imul__(self, a):
+        self.arena *= a
+        return self
+
+    def __mul__(self, a):
+        out = self.copy()
+        out.arena *= a
+        return out
+
+    __rmul__ = __mul__
+
+
+class DeviceOperator:
+    """Operator resident in device memory (imsrg_op)."""
+
+    def __init__(self, ms, hermiticity=1):
+        self.modelspace = ms
+        self._L = _lib.lib()
+        self._h = ctypes.c_void_p()
+        check(self._L.imsrg_op_create(ms._h, int(hermiticity), ctypes.byref(self._h)))
+
+    @classmethod
+    def from_host(cls, op, stream=None):
+        d = cls(op.modelspace, op.hermitian)
+        d.upload(op.arena, stream)
+        return d
+
+    def close(self):
+        if self._h:
+            self._L.imsrg_op_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def hermiticity(self):
+        h = ctypes.c_int()
+        check(self._L.imsrg_op_hermiticity(self._h, ctypes.byref(h)))
+        return h.value
+
+    @hermiticity.setter
+    def hermiticity(self, h):
+        check(self._L.imsrg_op_set_hermiticity(self._h, int(h)))
+
+    def upload(self, arena, stream=None):
+        a = np.ascontiguousarray(arena, dtype=np.float64)
+        assert a.shape == (self.modelspace.arena_size,)
+        check(self._L.imsrg_op_upload(self._h, _dp(a), stream))
+        if stream is not None:
+            self._keep = a
+
+    def download(self, out=None, stream=None):
+        if out is None:
+            out = np.empty(self.modelspace.arena_size)
+        check(self._L.imsrg_op_download(self._h, _dp(out), stream))
+        return out
+
+    def to_host(self):
+        return Operator(self.modelspace, arena=self.download(), hermitian=self.hermiticity == 1)
+
+    def device_ptr(self):
+        p = ctypes.c_void_p()
+        check(self._L.imsrg_op_device_arena(self._h, ctypes.byref(p)))
+        return p.value
+
+    def zero(self, stream=None):
+        check(self._L.imsrg_op_zero(self._h, stream))
+
+    def copy_from(self, other, stream=None):
+        check(self._L.imsrg_op_copy(self._h, other._h, stream))
+
+    def scale(self, a, stream=None):
+        check(self._L.imsrg_op_scale(self._h, float(a), stream))
+
+    def axpy(self, a, x, stream=None):
+        check(self._L.imsrg_op_axpy(self._h, float(a), x._h, stream))
+
+    def norm(self, stream=None):
+        out = ctypes.c_double()
+        check(self._L.imsrg_op_norm(self._h, ctypes.byref(out), stream))
+        return out.value
+
+    def fill_random(self, seed, stream=None):
+        check(self._L.imsrg_op_fill_random(self._h, int(seed), stream))
+
+
+def _precision(p):
+    if p is None:
+        v = ctypes.c_int()
+        check(_lib.lib().imsrg_get_default_precision(ctypes.byref(v)))
+        return v.value
+    if isinstance(p, str):
+        return {"fp64": _lib.PREC_FP64, "split": _lib.PREC_SPLIT}[p.lower()]
+    return int(p)
+
+
+class _CommutatorNamespace:
+    """Commutator:: free functions (src/Commutator.hh:57-87)."""
+
+    _TERMS_3 = ("comm110ss", "comm220ss", "comm111ss", "comm121ss", "comm122ss", "comm221ss")
+    _TERMS_P = ("comm222_pp_hhss", "comm222_pp_hh_221ss", "comm222_phss")
+
+    def TurnOnTerm(self, name):
+        check(_lib.lib().imsrg_set_term(name.encode(), 1))
+
+    def TurnOffTerm(self, name):
+        check(_lib.lib().imsrg_set_term(name.encode(), 0))
+
+    def IsTermOn(self, name):
+        v = ctypes.c_int()
+        check(_lib.lib().imsrg_get_term(name.encode(), ctypes.byref(v)))
+        return bool(v.value)
+
+    def SetPrecision(self, p):
+        check(_lib.lib().imsrg_set_default_precision(_precision(p)))
+
+    def GetPrecision(self):
+        return _precision(None)
+
+    def _run_term(self, name, X, Y, Z, precision=None):
+        L = _lib.lib()
+        with DeviceOperator.from_host(X) as dx, DeviceOperator.from_host(Y) as dy, \
+                DeviceOperator.from_host(Z) as dz:
+            fn = getattr(L, "imsrg_" + name)
+            if name in self._TERMS_P:
+                check(fn(dx._h, dy._h, dz._h, _precision(precision), None))
+            else:
+                check(fn(dx._h, dy._h, dz._h, None))
+            dz.download(Z.arena)
+
+    def CommutatorScalarScalar(self, X, Y, precision=None):
+        ms = X.modelspace
+        Z = Operator(ms)
+        with DeviceOperator.from_host(X) as dx, DeviceOperator.from_host(Y) as dy, DeviceOperator(ms) as dz:
+            check(_lib.lib().imsrg_commutator_scalar_scalar(dx._h, dy._h, dz._h, _precision(precision), None))
+            dz.download(Z.arena)
+            Z.hermitian = dz.hermiticity
+        return Z
+
+    Commutator = CommutatorScalarScalar
+
+    def device_commutator(self, dX, dY, dZ, precision=None, stream=None):
+        """[X,Y] on device-resident operators (Z overwritten)."""
+        check(_lib.lib().imsrg_commutator_scalar_scalar(dX._h, dY._h, dZ._h, _precision(precision), stream))
+
+    def device_term(self, name, dX, dY, dZ, precision=None, stream=None):
+        fn = getattr(_lib.lib(), "imsrg_" + name)
+        if name in self._TERMS_P:
+            check(fn(dX._h, dY._h, dZ._h, _precision(precision), stream))
+        else:
+            check(fn(dX._h, dY._h, dZ._h, stream))
+
+
+def _make_term(name):
+    def f(self, X, Y, Z, precision=None):
+        self._run_term(name, X, Y, Z, precision)
+    f.__name__ = name
+    f.__doc__ = "Commutator::%s(X, Y, Z): accumulate the term into Z." % name
+    return f
+
+
+for _n in _CommutatorNamespace._TERMS_3 + _CommutatorNamespace._TERMS_P:
+    setattr(_CommutatorNamespace, _n, _make_term(_n))
+
+Commutator = _CommutatorNamespace()
+
+
+class _BCHNamespace:
+    """BCH:: free functions (src/BCH.hh:22-25)."""
+
+    def __init__(self):
+        self.bch_transform_threshold = 1e-9
+
+    def Set_BCH_Transform_Threshold(self, x):
+        self.bch_transform_threshold = float(x)
+
+    def BCH_Transform(self, OpIn, Omega, precision=None):
+        ms = OpIn.modelspace
+        out = Operator(ms)
+        with DeviceOperator.from_host(OpIn) as di, DeviceOperator.from_host(Omega) as dom, \
+                DeviceOperator(ms) as do:
+            self.last_n_nested = self.device_transform(di, dom, do, precision)
+            do.download(out.arena)
+            out.hermitian = do.hermiticity
+        return out
+
+    def device_transform(self, dIn, dOmega, dOut, precision=None, stream=None):
+        n = ctypes.c_int()
+        check(_lib.lib().imsrg_bch_transform(dIn._h, dOmega._h, dOut._h, self.bch_transform_threshold,
+                                             _precision(precision), ctypes.byref(n), stream))
+        return n.value
+
+
+BCH = _BCHNamespace()

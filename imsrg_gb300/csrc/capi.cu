@@ -1,0 +1,856 @@
+// extern "C" boundary (include/imsrg_gb300.h): model spaces, device-resident
+// operators, the IMSRG(2) terms, CommutatorScalarScalar and the BCH transform.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <exception>
+#include <map>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/imsrg_gb300.h"
+#include "kernels.cuh"
+#include "space.hpp"
+
+using namespace imsrg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg)
+{
+  g_err = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                  \
+  do {                                                                                  \
+    cudaError_t _e = (expr);                                                            \
+    if (_e != cudaSuccess)                                                              \
+      return fail(IMSRG_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+enum Term { T110 = 0, T220, T111, T121, T122, T221, T222PPHH, T222PH, NTERMS };
+const char* kTermNames[NTERMS] = {"comm110ss", "comm220ss",      "comm111ss",   "comm121ss",
+                                  "comm122ss", "comm221ss", "comm222_pp_hhss", "comm222_phss"};
+std::mutex g_mu;
+bool g_term_on[NTERMS] = {true, true, true, true, true, true, true, true};
+int g_default_precision = IMSRG_PREC_FP64;
+
+template <class T>
+T* dmalloc(size_t count)
+{
+  void* p = nullptr;
+  if (cudaMalloc(&p, std::max<size_t>(1, count) * sizeof(T)) != cudaSuccess) throw std::runtime_error("cudaMalloc");
+  return (T*)p;
+}
+
+template <class T>
+T* dcopy(const std::vector<T>& v)
+{
+  T* p = dmalloc<T>(v.size());
+  if (!v.empty() && cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+    throw std::runtime_error("cudaMemcpy");
+  return p;
+}
+
+}  // namespace
+
+struct imsrg_space {
+  Space* s = nullptr;
+  bool dev_ready = false;
+  std::mutex mu;
+  std::vector<void*> allocs;
+  int* d_holes = nullptr;
+  // FP64 symmetrised products
+  GemmJobDev* d_ladder_jobs = nullptr;
+  int* d_ladder_pairs = nullptr;
+  int n_ladder_pairs = 0;
+  std::vector<GemmJobDev> ladder_jobs, zbar_jobs;
+  GemmJobDev* d_zbar_jobs = nullptr;
+  int* d_zbar_pairs = nullptr;
+  int n_zbar_pairs = 0;
+  // other tile lists
+  int* d_sym122 = nullptr;
+  int n_sym122 = 0;
+  int* d_pfwd = nullptr;
+  int n_pfwd = 0;
+  int* d_pinv = nullptr;
+  int n_pinv = 0;
+  std::vector<std::pair<int64_t, int64_t>> zbar_zero;  // Zbar regions with no ph kets
+  // norm chunks
+  long long* d_norm_off = nullptr;
+  int* d_norm_len = nullptr;
+  double* d_norm_w = nullptr;
+  int n_norm = 0;
+  double* d_norm_partial = nullptr;
+  std::vector<double> h_norm_partial;
+  // scratch
+  double *d_xb = nullptr, *d_yt = nullptr, *d_yf = nullptr, *d_zb = nullptr, *d_w2 = nullptr;
+  int* d_status = nullptr;
+  // split-precision plans
+  SplitPlan* split_ladder = nullptr;
+  SplitPlan* split_zbar = nullptr;
+  // BCH work operators
+  double *d_nested = nullptr, *d_next = nullptr;
+
+  template <class T>
+  T* track(T* p)
+  {
+    allocs.push_back((void*)p);
+    return p;
+  }
+  ~imsrg_space()
+  {
+    if (split_ladder) split_plan_destroy(split_ladder);
+    if (split_zbar) split_plan_destroy(split_zbar);
+    for (void* p : allocs) cudaFree(p);
+    delete s;
+  }
+};
+
+struct imsrg_op {
+  imsrg_space* sp = nullptr;
+  double* d = nullptr;
+  int herm = 1;
+};
+
+namespace {
+
+std::vector<int> tile_pairs(const std::vector<GemmJobDev>& jobs, int tile)
+{
+  // jobs in decreasing size order so the big tiles start first
+  std::vector<int> order(jobs.size());
+  for (size_t i = 0; i < jobs.size(); ++i) order[i] = (int)i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return jobs[a].m > jobs[b].m; });
+  std::vector<int> out;
+  for (int j : order) {
+    int nt = (jobs[j].m + tile - 1) / tile;
+    for (int a = 0; a < nt; ++a)
+      for (int b = a; b < nt; ++b) {
+        out.push_back(j);
+        out.push_back(a);
+        out.push_back(b);
+      }
+  }
+  return out;
+}
+
+GemmJobDev to_dev(const SymGemmJob& j, int bsel, int sign, int accumulate)
+{
+  GemmJobDev d{};
+  d.a_off = j.a_off;
+  d.b_off = j.b_off;
+  d.out_off = j.out_off;
+  d.m = j.m;
+  d.K = j.K;
+  d.lda = j.lda;
+  d.ldb = j.ldb;
+  d.ldo = j.ldo;
+  d.kidx_off = j.kidx_off;
+  d.w_off = j.w_off;
+  d.phase_off = j.phase_off;
+  d.bsel = bsel;
+  d.sign = sign;
+  d.accumulate = accumulate;
+  d.bscale = 1.0;
+  return d;
+}
+
+void setup_device_lists(imsrg_space* sp)
+{
+  Space& s = *sp->s;
+  upload_space(s);
+  sp->d_holes = sp->track(dcopy(s.holes));
+  // ladder: bscale = hY (launch), sign = hZ (launch), accumulate into Z
+  for (const SymGemmJob& j : s.ladder_jobs) sp->ladder_jobs.push_back(to_dev(j, 0, 0, 1));
+  sp->d_ladder_jobs = sp->track(dcopy(sp->ladder_jobs));
+  std::vector<int> lp = tile_pairs(sp->ladder_jobs, symgemm_fp64_tile());
+  sp->n_ladder_pairs = (int)lp.size() / 3;
+  sp->d_ladder_pairs = sp->track(dcopy(lp));
+  // Zbar: head (B = Ybar^T, sign = hZ), tail (B = Yflip^T, sign +1, phases), overwrite
+  for (size_t t = 0; t < s.zbar_jobs.size(); ++t) {
+    bool tail = (t % 2) == 1;
+    sp->zbar_jobs.push_back(to_dev(s.zbar_jobs[t], tail ? 1 : 0, tail ? 1 : 0, 0));
+  }
+  sp->d_zbar_jobs = sp->track(dcopy(sp->zbar_jobs));
+  std::vector<int> zp = tile_pairs(sp->zbar_jobs, symgemm_fp64_tile());
+  sp->n_zbar_pairs = (int)zp.size() / 3;
+  sp->d_zbar_pairs = sp->track(dcopy(zp));
+  // comm122 symmetrisation tiles (all 32x32 tiles of every block)
+  std::vector<int> t122, tinv, tfwd;
+  for (int c = 0; c < s.nch; ++c) {
+    int n = s.ch[c].n();
+    int nt = (n + 31) / 32;
+    for (int a = 0; a < nt; ++a)
+      for (int b = 0; b < nt; ++b) {
+        t122.push_back(c);
+        t122.push_back(a);
+        t122.push_back(b);
+      }
+    int n16 = (n + 15) / 16;
+    for (int a = 0; a < n16; ++a)
+      for (int b = a; b < n16; ++b) {
+        tinv.push_back(c);
+        tinv.push_back(a);
+        tinv.push_back(b);
+      }
+  }
+  for (int c = 0; c < s.nch; ++c) {
+    int ncc = s.cc[c].n();
+    int K = 2 * s.cc_nph[c];
+    if (ncc == 0) continue;
+    if (K == 0) {
+      sp->zbar_zero.push_back({s.zb_off[c], (int64_t)ncc * 2 * ncc});
+      continue;
+    }
+    for (int r0 = 0; r0 < ncc; r0 += 64)
+      for (int t0 = 0; t0 < K; t0 += 4) {
+        tfwd.push_back(c);
+        tfwd.push_back(r0);
+        tfwd.push_back(t0);
+      }
+  }
+  sp->n_sym122 = (int)t122.size() / 3;
+  sp->d_sym122 = sp->track(dcopy(t122));
+  sp->n_pinv = (int)tinv.size() / 3;
+  sp->d_pinv = sp->track(dcopy(tinv));
+  sp->n_pfwd = (int)tfwd.size() / 3;
+  sp->d_pfwd = sp->track(dcopy(tfwd));
+  // norm chunks: every 2b block in pieces of <= 65536 elements, weight (2J+1)^2
+  std::vector<long long> no;
+  std::vector<int> nl;
+  std::vector<double> nw;
+  for (int c = 0; c < s.nch; ++c) {
+    long long nn = (long long)s.ch[c].n() * s.ch[c].n();
+    double w = (double)(2 * s.ch[c].J + 1) * (2 * s.ch[c].J + 1);
+    for (long long o = 0; o < nn; o += 65536) {
+      no.push_back(s.ch[c].off + o);
+      nl.push_back((int)std::min<long long>(65536, nn - o));
+      nw.push_back(w);
+    }
+  }
+  sp->n_norm = (int)no.size();
+  sp->d_norm_off = sp->track(dcopy(no));
+  sp->d_norm_len = sp->track(dcopy(nl));
+  sp->d_norm_w = sp->track(dcopy(nw));
+  sp->d_norm_partial = sp->track(dmalloc<double>(sp->n_norm + 1));
+  sp->h_norm_partial.resize(sp->n_norm + 1);
+  sp->d_status = sp->track(dmalloc<int>(16));
+  cudaMemset(sp->d_status, 0, 16 * sizeof(int));
+}
+
+// device tables are built on first device use, so a space can be created and
+// queried on a machine without a GPU
+int ensure_device(imsrg_space* sp)
+{
+  std::lock_guard<std::mutex> g(sp->mu);
+  if (sp->dev_ready) return IMSRG_OK;
+  try {
+    setup_device_lists(sp);
+  } catch (std::exception& e) {
+    return fail(IMSRG_ERR_CUDA, std::string("device tables: ") + e.what());
+  }
+  sp->dev_ready = true;
+  return IMSRG_OK;
+}
+
+// lazily allocated scratch of a space
+int ensure_scratch(imsrg_space* sp, bool pandya, bool w2)
+{
+  try {
+    Space& s = *sp->s;
+    if (pandya && !sp->d_zb) {
+      sp->d_xb = sp->track(dmalloc<double>(s.xb_total));
+      sp->d_yt = sp->track(dmalloc<double>(s.xb_total));
+      sp->d_yf = sp->track(dmalloc<double>(s.xb_total));
+      sp->d_zb = sp->track(dmalloc<double>(s.zb_total));
+    }
+    if (w2 && !sp->d_w2) sp->d_w2 = sp->track(dmalloc<double>(s.arena));
+  } catch (std::exception& e) {
+    return fail(IMSRG_ERR_NOMEM, std::string("scratch allocation failed: ") + e.what());
+  }
+  return IMSRG_OK;
+}
+
+int check_ops(const imsrg_op* X, const imsrg_op* Y, const imsrg_op* Z)
+{
+  if (!X || !Y || !Z) return fail(IMSRG_ERR_ARG, "null operator");
+  if (X->sp != Y->sp || X->sp != Z->sp) return fail(IMSRG_ERR_ARG, "operators belong to different model spaces");
+  if ((X->herm != 1 && X->herm != -1) || (Y->herm != 1 && Y->herm != -1))
+    return fail(IMSRG_ERR_UNSUPPORTED, "X and Y must be hermitian or anti-hermitian");
+  if (Z->herm != 1 && Z->herm != -1) return fail(IMSRG_ERR_UNSUPPORTED, "Z must be hermitian or anti-hermitian");
+  return IMSRG_OK;
+}
+
+cudaStream_t S_(void* st) { return (cudaStream_t)st; }
+
+// ---------------------------------------------------------------- the terms
+int do_111_110(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, bool do111, bool do110, cudaStream_t st)
+{
+  // comm110ss returns early when X and Y have the same hermiticity (src/Commutator.cc:567-570)
+  if (do110 && X->herm == Y->herm) do110 = false;
+  if (!do111 && !do110) return IMSRG_OK;
+  CUDA_TRY(launch_comm111_110(*X->sp->s, X->d, Y->d, Z->d, do111, do110, st));
+  return IMSRG_OK;
+}
+
+int do_220(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
+{
+  if (X->herm == Y->herm) return IMSRG_OK;  // src/Commutator.cc:606-609
+  CUDA_TRY(launch_comm220(*X->sp->s, X->d, Y->d, Z->d, X->herm, st));
+  return IMSRG_OK;
+}
+
+int do_121(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
+{
+  CUDA_TRY(launch_comm121(*X->sp->s, X->sp->d_holes, X->d, Y->d, Z->d, Z->herm, st));
+  return IMSRG_OK;
+}
+
+int do_122(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
+{
+  imsrg_space* sp = X->sp;
+  int rc = ensure_scratch(sp, false, true);
+  if (rc) return rc;
+  CUDA_TRY(launch_comm122(*sp->s, X->d, Y->d, Z->d, sp->d_w2, Z->herm, sp->d_sym122, sp->n_sym122, st));
+  return IMSRG_OK;
+}
+
+int do_221_1b(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
+{
+  CUDA_TRY(launch_comm221_1b(*X->sp->s, X->d, Y->d, Z->d, X->herm, Z->herm, st));
+  return IMSRG_OK;
+}
+
+int check_status(imsrg_space* sp, cudaStream_t st)
+{
+  int h = 0;
+  CUDA_TRY(cudaMemcpyAsync(&h, sp->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (h != 0) {
+    cudaMemsetAsync(sp->d_status, 0, sizeof(int), st);
+    return fail(IMSRG_ERR_KERNEL, "a kernel reported error status " + std::to_string(h));
+  }
+  return IMSRG_OK;
+}
+
+int ensure_split(imsrg_space* sp)
+{
+  try {
+    if (!sp->split_ladder) sp->split_ladder = split_plan_create(*sp->s, sp->ladder_jobs, 0);
+    if (!sp->split_zbar) sp->split_zbar = split_plan_create(*sp->s, sp->zbar_jobs, 1);
+  } catch (std::exception& e) {
+    return fail(IMSRG_ERR_NOMEM, std::string("split-precision plan: ") + e.what());
+  }
+  return IMSRG_OK;
+}
+
+int do_ladder(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStream_t st)
+{
+  imsrg_space* sp = X->sp;
+  Space& s = *sp->s;
+  if (prec == IMSRG_PREC_SPLIT) {
+    int rc = ensure_split(sp);
+    if (rc) return rc;
+    CUDA_TRY(launch_symgemm_split(sp->split_ladder, X->d, Y->d, Y->d, Z->d, s.work.kidx, s.work.kweight,
+                                  s.work.phase_tab, sp->d_status, st));
+    return IMSRG_OK;
+  }
+  if (prec != IMSRG_PREC_FP64) return fail(IMSRG_ERR_ARG, "unknown precision");
+  CUDA_TRY(launch_symgemm_fp64(sp->d_ladder_jobs, sp->d_ladder_pairs, sp->n_ladder_pairs, X->d, Y->d, Y->d, Z->d,
+                               s.work.kidx, s.work.kweight, s.work.phase_tab, Z->herm, (double)Y->herm, st));
+  return IMSRG_OK;
+}
+
+int do_ph(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStream_t st)
+{
+  imsrg_space* sp = X->sp;
+  Space& s = *sp->s;
+  int rc = ensure_scratch(sp, true, false);
+  if (rc) return rc;
+  CUDA_TRY(launch_pandya_fwd(s, X->d, Y->d, Y->herm, sp->d_xb, sp->d_yt, sp->d_yf, sp->d_pfwd, sp->n_pfwd, st));
+  for (auto& zr : sp->zbar_zero) CUDA_TRY(cudaMemsetAsync(sp->d_zb + zr.first, 0, zr.second * sizeof(double), st));
+  if (prec == IMSRG_PREC_SPLIT) {
+    rc = ensure_split(sp);
+    if (rc) return rc;
+    CUDA_TRY(launch_symgemm_split(sp->split_zbar, sp->d_xb, sp->d_yt, sp->d_yf, sp->d_zb, s.work.kidx,
+                                  s.work.kweight, s.work.phase_tab, sp->d_status, st));
+  } else if (prec == IMSRG_PREC_FP64) {
+    CUDA_TRY(launch_symgemm_fp64(sp->d_zbar_jobs, sp->d_zbar_pairs, sp->n_zbar_pairs, sp->d_xb, sp->d_yt, sp->d_yf,
+                                 sp->d_zb, s.work.kidx, s.work.kweight, s.work.phase_tab, Z->herm, 1.0, st));
+  } else {
+    return fail(IMSRG_ERR_ARG, "unknown precision");
+  }
+  CUDA_TRY(launch_pandya_inv(s, sp->d_zb, Z->d, Z->herm, sp->d_pinv, sp->n_pinv, st));
+  return IMSRG_OK;
+}
+
+int z_herm(int hx, int hy) { return (hx == hy) ? -1 : 1; }
+
+int commutator_impl(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStream_t st)
+{
+  if (!X || !Y || !Z) return fail(IMSRG_ERR_ARG, "null operator");
+  if (Z == X || Z == Y) return fail(IMSRG_ERR_ARG, "Z must not alias X or Y");
+  Z->herm = z_herm(X->herm, Y->herm);
+  int rc = check_ops(X, Y, Z);
+  if (rc) return rc;
+  bool on[NTERMS];
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    std::copy(g_term_on, g_term_on + NTERMS, on);
+  }
+  CUDA_TRY(cudaMemsetAsync(Z->d, 0, X->sp->s->arena * sizeof(double), st));
+  if ((rc = do_111_110(X, Y, Z, on[T111], on[T110], st))) return rc;
+  if (on[T220] && (rc = do_220(X, Y, Z, st))) return rc;
+  if (on[T121] && (rc = do_121(X, Y, Z, st))) return rc;
+  if (on[T122] && (rc = do_122(X, Y, Z, st))) return rc;
+  if (on[T222PPHH] && (rc = do_ladder(X, Y, Z, prec, st))) return rc;
+  if (on[T221] && (rc = do_221_1b(X, Y, Z, st))) return rc;
+  if (on[T222PH] && (rc = do_ph(X, Y, Z, prec, st))) return rc;
+  return IMSRG_OK;
+}
+
+int norm_impl(const imsrg_op* op, double* out, cudaStream_t st)
+{
+  imsrg_space* sp = op->sp;
+  CUDA_TRY(launch_norm(*sp->s, op->d, sp->d_norm_off, sp->d_norm_len, sp->d_norm_w, sp->n_norm, sp->d_norm_partial,
+                       st));
+  CUDA_TRY(cudaMemcpyAsync(sp->h_norm_partial.data(), sp->d_norm_partial, (sp->n_norm + 1) * sizeof(double),
+                           cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  double n2 = 0.0;
+  for (int i = 0; i < sp->n_norm; ++i) n2 += sp->h_norm_partial[i];
+  *out = std::sqrt(sp->h_norm_partial[sp->n_norm] + n2);
+  return IMSRG_OK;
+}
+
+// splitmix64 -> uniform [-1, 1)
+struct Rng {
+  uint64_t s;
+  uint64_t next()
+  {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  }
+  double uniform() { return (double)(next() >> 11) * (2.0 / 9007199254740992.0) - 1.0; }
+};
+
+}  // namespace
+
+// ======================================================================= ABI
+extern "C" {
+
+const char* imsrg_last_error(void) { return g_err.c_str(); }
+
+int imsrg_space_create(int emax, int norb, const int* n, const int* l, const int* j2, const int* tz2,
+                       const double* occ, imsrg_space** out)
+{
+  if (!out || norb <= 0 || !n || !l || !j2 || !tz2 || !occ || emax < 0) return fail(IMSRG_ERR_ARG, "bad arguments");
+  *out = nullptr;
+  imsrg_space* sp = new imsrg_space();
+  try {
+    sp->s = build_space(emax, std::vector<int>(n, n + norb), std::vector<int>(l, l + norb),
+                        std::vector<int>(j2, j2 + norb), std::vector<int>(tz2, tz2 + norb),
+                        std::vector<double>(occ, occ + norb));
+  } catch (std::exception& e) {
+    delete sp;
+    return fail(IMSRG_ERR_ARG, std::string("model space: ") + e.what());
+  }
+  *out = sp;
+  return IMSRG_OK;
+}
+
+int imsrg_space_create_reference(int emax, int A, int Z, imsrg_space** out)
+{
+  if (emax < 0 || A < 0 || Z < 0 || Z > A) return fail(IMSRG_ERR_ARG, "bad emax / A / Z");
+  std::vector<int> n, l, j2, tz2;
+  std::vector<double> occ;
+  try {
+    reference_orbits(emax, A, Z, n, l, j2, tz2, occ);
+  } catch (std::exception& e) {
+    return fail(IMSRG_ERR_ARG, e.what());
+  }
+  return imsrg_space_create(emax, (int)n.size(), n.data(), l.data(), j2.data(), tz2.data(), occ.data(), out);
+}
+
+void imsrg_space_destroy(imsrg_space* s) { delete s; }
+
+int imsrg_space_sizes(const imsrg_space* sp, int* norb, int* nch, long long* arena_len)
+{
+  if (!sp) return fail(IMSRG_ERR_ARG, "null space");
+  if (norb) *norb = sp->s->norb;
+  if (nch) *nch = sp->s->nch;
+  if (arena_len) *arena_len = sp->s->arena;
+  return IMSRG_OK;
+}
+
+int imsrg_space_orbit(const imsrg_space* sp, int i, int* n, int* l, int* j2, int* tz2, double* occ)
+{
+  if (!sp || i < 0 || i >= sp->s->norb) return fail(IMSRG_ERR_ARG, "bad orbit index");
+  const Space& s = *sp->s;
+  if (n) *n = s.n[i];
+  if (l) *l = s.l[i];
+  if (j2) *j2 = s.j2[i];
+  if (tz2) *tz2 = s.tz2[i];
+  if (occ) *occ = s.occ[i];
+  return IMSRG_OK;
+}
+
+int imsrg_space_channel(const imsrg_space* sp, int ch, int* J, int* parity, int* Tz, int* nkets, long long* offset)
+{
+  if (!sp || ch < 0 || ch >= sp->s->nch) return fail(IMSRG_ERR_ARG, "bad channel index");
+  const Chan& C = sp->s->ch[ch];
+  if (J) *J = C.J;
+  if (parity) *parity = C.parity;
+  if (Tz) *Tz = C.Tz;
+  if (nkets) *nkets = C.n();
+  if (offset) *offset = C.off;
+  return IMSRG_OK;
+}
+
+int imsrg_space_channel_kets(const imsrg_space* sp, int ch, int* p, int* q)
+{
+  if (!sp || ch < 0 || ch >= sp->s->nch || !p || !q) return fail(IMSRG_ERR_ARG, "bad arguments");
+  const Chan& C = sp->s->ch[ch];
+  std::copy(C.p.begin(), C.p.end(), p);
+  std::copy(C.q.begin(), C.q.end(), q);
+  return IMSRG_OK;
+}
+
+int imsrg_space_cc_channel(const imsrg_space* sp, int ch, int* J, int* parity, int* Tz, int* nkets, int* p, int* q)
+{
+  if (!sp || ch < 0 || ch >= sp->s->nch) return fail(IMSRG_ERR_ARG, "bad channel index");
+  const Chan& C = sp->s->cc[ch];
+  if (J) *J = C.J;
+  if (parity) *parity = C.parity;
+  if (Tz) *Tz = C.Tz;
+  if (nkets) *nkets = C.n();
+  if (p) std::copy(C.p.begin(), C.p.end(), p);
+  if (q) std::copy(C.q.begin(), C.q.end(), q);
+  return IMSRG_OK;
+}
+
+int imsrg_space_sixj(const imsrg_space* sp, int jj1, int jj2, int j3, int jj4, int jj5, int j6, double* out)
+{
+  if (!sp || !out) return fail(IMSRG_ERR_ARG, "bad arguments");
+  *out = sixj_lookup(*sp->s, jj1, jj2, j3, jj4, jj5, j6);
+  return IMSRG_OK;
+}
+
+int imsrg_op_create(imsrg_space* sp, int hermiticity, imsrg_op** out)
+{
+  if (!sp || !out) return fail(IMSRG_ERR_ARG, "bad arguments");
+  if (hermiticity != 1 && hermiticity != -1) return fail(IMSRG_ERR_UNSUPPORTED, "hermiticity must be +1 or -1");
+  *out = nullptr;
+  int rc = ensure_device(sp);
+  if (rc) return rc;
+  imsrg_op* op = new imsrg_op();
+  op->sp = sp;
+  op->herm = hermiticity;
+  if (cudaMalloc(&op->d, sp->s->arena * sizeof(double)) != cudaSuccess) {
+    delete op;
+    cudaGetLastError();
+    return fail(IMSRG_ERR_NOMEM, "operator arena allocation failed");
+  }
+  if (cudaMemset(op->d, 0, sp->s->arena * sizeof(double)) != cudaSuccess) {
+    cudaFree(op->d);
+    delete op;
+    return fail(IMSRG_ERR_CUDA, "operator arena memset failed");
+  }
+  *out = op;
+  return IMSRG_OK;
+}
+
+void imsrg_op_destroy(imsrg_op* op)
+{
+  if (!op) return;
+  cudaFree(op->d);
+  delete op;
+}
+
+int imsrg_op_hermiticity(const imsrg_op* op, int* h)
+{
+  if (!op || !h) return fail(IMSRG_ERR_ARG, "bad arguments");
+  *h = op->herm;
+  return IMSRG_OK;
+}
+
+int imsrg_op_set_hermiticity(imsrg_op* op, int h)
+{
+  if (!op) return fail(IMSRG_ERR_ARG, "null operator");
+  if (h != 1 && h != -1) return fail(IMSRG_ERR_UNSUPPORTED, "hermiticity must be +1 or -1");
+  op->herm = h;
+  return IMSRG_OK;
+}
+
+int imsrg_op_upload(imsrg_op* op, const double* host, void* stream)
+{
+  if (!op || !host) return fail(IMSRG_ERR_ARG, "bad arguments");
+  CUDA_TRY(cudaMemcpyAsync(op->d, host, op->sp->s->arena * sizeof(double), cudaMemcpyHostToDevice, S_(stream)));
+  return IMSRG_OK;
+}
+
+int imsrg_op_download(const imsrg_op* op, double* host, void* stream)
+{
+  if (!op || !host) return fail(IMSRG_ERR_ARG, "bad arguments");
+  CUDA_TRY(cudaMemcpyAsync(host, op->d, op->sp->s->arena * sizeof(double), cudaMemcpyDeviceToHost, S_(stream)));
+  CUDA_TRY(cudaStreamSynchronize(S_(stream)));
+  return IMSRG_OK;
+}
+
+int imsrg_op_device_arena(const imsrg_op* op, double** dptr)
+{
+  if (!op || !dptr) return fail(IMSRG_ERR_ARG, "bad arguments");
+  *dptr = op->d;
+  return IMSRG_OK;
+}
+
+int imsrg_op_zero(imsrg_op* op, void* stream)
+{
+  if (!op) return fail(IMSRG_ERR_ARG, "null operator");
+  CUDA_TRY(cudaMemsetAsync(op->d, 0, op->sp->s->arena * sizeof(double), S_(stream)));
+  return IMSRG_OK;
+}
+
+int imsrg_op_copy(imsrg_op* dst, const imsrg_op* src, void* stream)
+{
+  if (!dst || !src || dst->sp != src->sp) return fail(IMSRG_ERR_ARG, "bad arguments");
+  if (dst == src) return IMSRG_OK;
+  CUDA_TRY(cudaMemcpyAsync(dst->d, src->d, src->sp->s->arena * sizeof(double), cudaMemcpyDeviceToDevice,
+                           S_(stream)));
+  dst->herm = src->herm;
+  return IMSRG_OK;
+}
+
+int imsrg_op_scale(imsrg_op* op, double a, void* stream)
+{
+  if (!op) return fail(IMSRG_ERR_ARG, "null operator");
+  CUDA_TRY(launch_scale(op->d, a, op->sp->s->arena, S_(stream)));
+  return IMSRG_OK;
+}
+
+int imsrg_op_axpy(imsrg_op* y, double a, const imsrg_op* x, void* stream)
+{
+  if (!y || !x || y->sp != x->sp) return fail(IMSRG_ERR_ARG, "bad arguments");
+  CUDA_TRY(launch_axpy(y->d, x->d, a, y->sp->s->arena, S_(stream)));
+  return IMSRG_OK;
+}
+
+int imsrg_op_norm(const imsrg_op* op, double* out, void* stream)
+{
+  if (!op || !out) return fail(IMSRG_ERR_ARG, "bad arguments");
+  return norm_impl(op, out, S_(stream));
+}
+
+int imsrg_op_fill_random(imsrg_op* op, unsigned long long seed, void* stream)
+{
+  if (!op) return fail(IMSRG_ERR_ARG, "null operator");
+  const Space& s = *op->sp->s;
+  std::vector<double> a((size_t)s.arena, 0.0);
+  Rng rng{seed * 0x2545F4914F6CDD1Dull + 0x1234567ull};
+  double sg = op->herm == 1 ? 1.0 : -1.0;
+  a[0] = op->herm == 1 ? rng.uniform() : 0.0;
+  int N = s.norb;
+  double f1 = 0.0;
+  for (int i = 0; i < N; ++i)
+    for (int k = 0; k < s.ob_count[i]; ++k) {
+      int j = s.ob_list[s.ob_start[i] + k];
+      if (j < i) continue;
+      double v = rng.uniform();
+      if (i == j) v = (op->herm == 1) ? v : 0.0;
+      a[32 + (size_t)j * N + i] = v;
+      a[32 + (size_t)i * N + j] = (i == j) ? v : sg * v;
+      f1 += (i == j ? 1.0 : 2.0) * v * v;
+    }
+  if (f1 > 0)
+    for (int t = 0; t < N * N; ++t) a[32 + t] /= std::sqrt(f1);
+  for (int c = 0; c < s.nch; ++c) {
+    int n = s.ch[c].n();
+    double* b = a.data() + s.ch[c].off;
+    double f = 0.0;
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i <= j; ++i) {
+        double v = rng.uniform();
+        if (i == j && op->herm != 1) v = 0.0;
+        b[(size_t)j * n + i] = v;
+        b[(size_t)i * n + j] = (i == j) ? v : sg * v;
+        f += (i == j ? 1.0 : 2.0) * v * v;
+      }
+    if (f > 0) {
+      double r = 1.0 / std::sqrt(f);
+      for (size_t t = 0; t < (size_t)n * n; ++t) b[t] *= r;
+    }
+  }
+  CUDA_TRY(cudaMemcpyAsync(op->d, a.data(), s.arena * sizeof(double), cudaMemcpyHostToDevice, S_(stream)));
+  CUDA_TRY(cudaStreamSynchronize(S_(stream)));
+  return IMSRG_OK;
+}
+
+#define TERM_PROLOGUE                        \
+  int rc = check_ops(X, Y, Z);               \
+  if (rc) return rc;                         \
+  cudaStream_t st = S_(stream);
+
+int imsrg_comm110ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream)
+{
+  TERM_PROLOGUE
+  return do_111_110(X, Y, Z, false, true, st);
+}
+
+int imsrg_comm220ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream)
+{
+  TERM_PROLOGUE
+  return do_220(X, Y, Z, st);
+}
+
+int imsrg_comm111ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream)
+{
+  TERM_PROLOGUE
+  return do_111_110(X, Y, Z, true, false, st);
+}
+
+int imsrg_comm121ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream)
+{
+  TERM_PROLOGUE
+  return do_121(X, Y, Z, st);
+}
+
+int imsrg_comm122ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream)
+{
+  TERM_PROLOGUE
+  return do_122(X, Y, Z, st);
+}
+
+int imsrg_comm221ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream)
+{
+  TERM_PROLOGUE
+  return do_221_1b(X, Y, Z, st);
+}
+
+int imsrg_comm222_pp_hhss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream)
+{
+  TERM_PROLOGUE
+  rc = do_ladder(X, Y, Z, precision, st);
+  if (rc == IMSRG_OK && precision == IMSRG_PREC_SPLIT) rc = check_status(X->sp, st);
+  return rc;
+}
+
+int imsrg_comm222_pp_hh_221ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream)
+{
+  TERM_PROLOGUE
+  if ((rc = do_ladder(X, Y, Z, precision, st))) return rc;
+  if ((rc = do_221_1b(X, Y, Z, st))) return rc;
+  if (precision == IMSRG_PREC_SPLIT) rc = check_status(X->sp, st);
+  return rc;
+}
+
+int imsrg_comm222_phss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream)
+{
+  TERM_PROLOGUE
+  rc = do_ph(X, Y, Z, precision, st);
+  if (rc == IMSRG_OK && precision == IMSRG_PREC_SPLIT) rc = check_status(X->sp, st);
+  return rc;
+}
+
+int imsrg_commutator_scalar_scalar(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream)
+{
+  int rc = commutator_impl(X, Y, Z, precision, S_(stream));
+  if (rc == IMSRG_OK && precision == IMSRG_PREC_SPLIT) rc = check_status(X->sp, S_(stream));
+  return rc;
+}
+
+int imsrg_set_term(const char* name, int on)
+{
+  if (!name) return fail(IMSRG_ERR_ARG, "null name");
+  std::lock_guard<std::mutex> g(g_mu);
+  for (int t = 0; t < NTERMS; ++t)
+    if (std::strcmp(name, kTermNames[t]) == 0) {
+      g_term_on[t] = on != 0;
+      return IMSRG_OK;
+    }
+  return fail(IMSRG_ERR_ARG, std::string("unknown term ") + name);
+}
+
+int imsrg_get_term(const char* name, int* on)
+{
+  if (!name || !on) return fail(IMSRG_ERR_ARG, "bad arguments");
+  std::lock_guard<std::mutex> g(g_mu);
+  for (int t = 0; t < NTERMS; ++t)
+    if (std::strcmp(name, kTermNames[t]) == 0) {
+      *on = g_term_on[t] ? 1 : 0;
+      return IMSRG_OK;
+    }
+  return fail(IMSRG_ERR_ARG, std::string("unknown term ") + name);
+}
+
+int imsrg_set_default_precision(int precision)
+{
+  if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_SPLIT) return fail(IMSRG_ERR_ARG, "bad precision");
+  std::lock_guard<std::mutex> g(g_mu);
+  g_default_precision = precision;
+  return IMSRG_OK;
+}
+
+int imsrg_get_default_precision(int* precision)
+{
+  if (!precision) return fail(IMSRG_ERR_ARG, "null pointer");
+  std::lock_guard<std::mutex> g(g_mu);
+  *precision = g_default_precision;
+  return IMSRG_OK;
+}
+
+int imsrg_bch_transform(const imsrg_op* OpIn, const imsrg_op* Omega, imsrg_op* OpOut, double threshold,
+                        int precision, int* n_nested, void* stream)
+{
+  if (!OpIn || !Omega || !OpOut) return fail(IMSRG_ERR_ARG, "null operator");
+  if (OpIn->sp != Omega->sp || OpIn->sp != OpOut->sp) return fail(IMSRG_ERR_ARG, "different model spaces");
+  if (OpOut == Omega) return fail(IMSRG_ERR_ARG, "OpOut must not alias Omega");
+  cudaStream_t st = S_(stream);
+  imsrg_space* sp = OpIn->sp;
+  if (n_nested) *n_nested = 0;
+  int rc;
+  double nx = 0, ny = 0;
+  if ((rc = norm_impl(OpIn, &nx, st))) return rc;
+  if ((rc = norm_impl(Omega, &ny, st))) return rc;
+  if ((rc = imsrg_op_copy(OpOut, OpIn, stream))) return rc;
+  if (!(nx > threshold)) return IMSRG_OK;
+  try {
+    if (!sp->d_nested) sp->d_nested = sp->track(dmalloc<double>(sp->s->arena));
+    if (!sp->d_next) sp->d_next = sp->track(dmalloc<double>(sp->s->arena));
+  } catch (std::exception&) {
+    return fail(IMSRG_ERR_NOMEM, "BCH work operators");
+  }
+  imsrg_op nested, next;
+  nested.sp = next.sp = sp;
+  nested.d = sp->d_nested;
+  next.d = sp->d_next;
+  CUDA_TRY(cudaMemcpyAsync(nested.d, OpOut->d, sp->s->arena * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  nested.herm = OpOut->herm;
+  double epsilon = nx * std::exp(-2 * ny) * threshold / (2 * ny);
+  double fden = 1.0;
+  for (int i = 1; i <= 40; ++i) {
+    if ((rc = commutator_impl(Omega, &nested, &next, precision, st))) return rc;
+    std::swap(nested.d, next.d);
+    std::swap(nested.herm, next.herm);
+    fden /= i;
+    CUDA_TRY(launch_axpy(OpOut->d, nested.d, fden, sp->s->arena, st));
+    if (n_nested) *n_nested = i;
+    epsilon *= i + 1;
+    double nn = 0;
+    if ((rc = norm_impl(&nested, &nn, st))) return rc;
+    if (precision == IMSRG_PREC_SPLIT && (rc = check_status(sp, st))) return rc;
+    if (nn < epsilon) break;
+  }
+  return IMSRG_OK;
+}
+
+}  // extern "C"

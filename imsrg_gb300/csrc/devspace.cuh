@@ -1,0 +1,112 @@
+// Device view of a model space: flat tables the kernels read, passed by value.
+#pragma once
+
+#include <cstdint>
+
+#ifdef __CUDACC__
+#define IMSRG_HD __host__ __device__ __forceinline__
+#else
+#define IMSRG_HD inline
+#endif
+
+namespace imsrg {
+
+struct DevSpace {
+  int norb, nch, nkets, NJ, d1;
+  const int* l;
+  const int* j2;
+  const int* tz2;
+  const double* occ;
+  const int* ob_start;  // one-body channel of each orbit: ob_list[ob_start[i] .. +ob_count[i])
+  const int* ob_count;
+  const int* ob_list;
+  const int* ketJ_loc;  // [ket * NJ + J] -> local index in the 2b channel (J, parity, Tz of the ket)
+  const int* ccJ_loc;   // [ket * NJ + J] -> local index in the CC channel (J, parity, |dTz|)
+  const int* ch_n;      // kets per 2b channel
+  const long long* ch_off;  // arena offset per 2b channel
+  const int* ch_kofs;   // start of the channel's kets in ket_p / ket_q
+  const int* ket_p;
+  const int* ket_q;
+  const int* cc_n;
+  const int* cc_kofs;
+  const int* cc_p;
+  const int* cc_q;
+  const int* sixj_base;  // [((a*d1+b)*d1+c)*d1+d] -> offset into sixj_val
+  const double* sixj_val;
+};
+
+// Device copies of the per-kernel work lists (built once per space).
+struct DevWork {
+  const double* ket_wpp;  // flat over 2b channel kets (ch_kofs order)
+  const double* ket_nn;
+  const int* hh_off;      // per channel, into hh_list
+  const int* hh_list;
+  const int* items220; int n220;
+  const int* pairs1b; int npairs1b;
+  const int* items221; int n221;
+  const int* cols122; int ncols122;
+  const int* it122_loc;
+  const int* it122_a;
+  const int* it122_src;
+  const double* it122_f;
+  const int* kidx;        // ladder gather lists
+  const double* kweight;
+  const int* phase_tab;
+  const int* cc_nph;      // Pandya
+  const int* cc_ph_off;
+  const int* cc_ph;
+  const long long* xb_off;
+  const long long* zb_off;
+  const int* cc_phase_off;
+};
+
+// global index of ket (p, q), p <= q: ModelSpace::Index2 (src/ModelSpace.cc:1108-1118)
+IMSRG_HD int ket_index(int norb, int p, int q) { return p * (2 * norb - 1 - p) / 2 + q; }
+
+IMSRG_HD int chan_index(int J, int parity, int Tz) { return 6 * J + 2 * (Tz + 1) + parity; }
+
+IMSRG_HD int iphase(int x) { return (x & 1) ? -1 : 1; }
+
+// compact 6j lookup {jj1/2 jj2/2 J3; jj4/2 jj5/2 J6}; 0 outside the triads
+IMSRG_HD int sixj_slot(int d1, const int* base, int jj1, int jj2, int J3, int jj4, int jj5, int J6)
+{
+  int J3min = (jj1 > jj2 ? jj1 - jj2 : jj2 - jj1) >> 1, J3max = (jj1 + jj2) >> 1;
+  int t1 = jj1 > jj5 ? jj1 - jj5 : jj5 - jj1, t2 = jj4 > jj2 ? jj4 - jj2 : jj2 - jj4;
+  int J6min = (t1 > t2 ? t1 : t2) >> 1;
+  int s1 = jj1 + jj5, s2 = jj4 + jj2;
+  int J6max = (s1 < s2 ? s1 : s2) >> 1;
+  if (J3 < J3min || J3 > J3max || J6 < J6min || J6 > J6max) return -1;
+  int a = (jj1 - 1) >> 1, b = (jj2 - 1) >> 1, c = (jj4 - 1) >> 1, d = (jj5 - 1) >> 1;
+  return base[((a * d1 + b) * d1 + c) * d1 + d] + (J3 - J3min) * (J6max - J6min + 1) + (J6 - J6min);
+}
+
+#ifdef __CUDACC__
+__device__ __forceinline__ double dev_sixj(const DevSpace& S, int jj1, int jj2, int J3, int jj4, int jj5, int J6)
+{
+  int s = sixj_slot(S.d1, S.sixj_base, jj1, jj2, J3, jj4, jj5, J6);
+  return s < 0 ? 0.0 : __ldg(S.sixj_val + s);
+}
+
+// Normalised J-coupled matrix element of a scalar operator arena, with the
+// swap phases of TwoBodyME::GetTBME_J_norm (src/TwoBodyME.cc:132-153,339-356).
+__device__ __forceinline__ double dev_tbme_J_norm(const DevSpace& S, const double* op, int J, int a, int b, int c,
+                                                  int d)
+{
+  int la = __ldg(S.l + a), lb = __ldg(S.l + b), lc = __ldg(S.l + c), ld = __ldg(S.l + d);
+  int ta = __ldg(S.tz2 + a), tb = __ldg(S.tz2 + b), tc = __ldg(S.tz2 + c), td = __ldg(S.tz2 + d);
+  if (((la + lb + lc + ld) & 1) || (ta + tb != tc + td)) return 0.0;
+  int kb = ket_index(S.norb, a < b ? a : b, a < b ? b : a);
+  int kk = ket_index(S.norb, c < d ? c : d, c < d ? d : c);
+  int bi = __ldg(S.ketJ_loc + kb * S.NJ + J);
+  int ki = __ldg(S.ketJ_loc + kk * S.NJ + J);
+  if (bi < 0 || ki < 0) return 0.0;
+  int ch = chan_index(J, (la + lb) & 1, (ta + tb) / 2);
+  int n = __ldg(S.ch_n + ch);
+  double ph = 1.0;
+  if (a > b) ph *= iphase(((__ldg(S.j2 + a) + __ldg(S.j2 + b)) >> 1) + 1 + J);
+  if (c > d) ph *= iphase(((__ldg(S.j2 + c) + __ldg(S.j2 + d)) >> 1) + 1 + J);
+  return ph * op[__ldg(S.ch_off + ch) + (long long)ki * n + bi];
+}
+#endif
+
+}  // namespace imsrg

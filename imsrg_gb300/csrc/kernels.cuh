@@ -1,0 +1,54 @@
+// Kernel launchers of the GB300 IMSRG(2) commutator (host-callable).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "space.hpp"
+
+namespace imsrg {
+
+// device copy of a SymGemmJob (see space.hpp)
+struct GemmJobDev {
+  long long a_off, b_off, out_off;
+  int m, K, lda, ldb, ldo;
+  int kidx_off, w_off, phase_off;
+  int bsel;        // 0: B0, 1: B1
+  int sign;        // +-1, or 0: the launch's sign
+  int accumulate;  // 1: Out += ..., 0: Out = ...
+  double bscale;   // times the launch's scale
+};
+
+// kernels_terms.cu
+cudaError_t launch_comm111_110(const Space& s, const double* X, const double* Y, double* Z, bool do111, bool do110,
+                               cudaStream_t st);
+cudaError_t launch_comm220(const Space& s, const double* X, const double* Y, double* Z, int hX, cudaStream_t st);
+cudaError_t launch_comm121(const Space& s, const int* dev_holes, const double* X, const double* Y, double* Z, int hZ,
+                           cudaStream_t st);
+cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, double* Z, int hX, int hZ,
+                              cudaStream_t st);
+cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, double* Z, double* W2, int hZ,
+                           const int* sym_tiles, int nsym_tiles, cudaStream_t st);
+cudaError_t launch_pandya_fwd(const Space& s, const double* X, const double* Y, int hY, double* Xb, double* Yt,
+                              double* Yf, const int* tiles, int ntiles, cudaStream_t st);
+cudaError_t launch_pandya_inv(const Space& s, const double* Zb, double* Z, int hZ, const int* tiles, int ntiles,
+                              cudaStream_t st);
+cudaError_t launch_axpy(double* y, const double* x, double a, long long n, cudaStream_t st);
+cudaError_t launch_scale(double* y, double a, long long n, cudaStream_t st);
+cudaError_t launch_norm(const Space& s, const double* A, const long long* chunk_off, const int* chunk_len,
+                        const double* chunk_w, int nchunks, double* partial, cudaStream_t st);
+
+// kernels_gemm.cu
+int symgemm_fp64_tile();
+cudaError_t launch_symgemm_fp64(const GemmJobDev* jobs, const int* pairs, int npairs, const double* A,
+                                const double* B0, const double* B1, double* O, const int* kidx, const double* kw,
+                                const int* phase, int gsign, double gbscale, cudaStream_t st);
+
+// kernels_split.cu (Ozaki-style sliced BF16 products on tcgen05)
+struct SplitPlan;
+SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs, int family);
+void split_plan_destroy(SplitPlan* p);
+cudaError_t launch_symgemm_split(SplitPlan* p, const double* A, const double* B0, const double* B1, double* O,
+                                 const int* kidx, const double* kw, const int* phase, int* dev_status,
+                                 cudaStream_t st);
+
+}  // namespace imsrg

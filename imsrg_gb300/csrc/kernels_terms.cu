@@ -1,0 +1,546 @@
+// FP64 kernels of the scalar IMSRG(2) commutator terms other than the dense
+// channel products: comm110ss, comm111ss, comm220ss, comm121ss, the one-body
+// part of comm221ss, comm122ss, the forward and inverse Pandya
+// transformations of comm222_phss, and the operator algebra of the BCH series.
+// Each kernel states the reference lines it reproduces.
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+
+namespace imsrg {
+
+static constexpr double kSqrt2 = 1.4142135623730950488;
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------- 111 + 110
+// Z1 += X1 Y1 - Y1 X1  (comm111ss, src/Commutator.cc:644-649) and
+// Z0 += sum_a (2j_a+1) n_a (X1 Y1 - Y1 X1)_aa over holes (comm110ss, :564-581)
+__global__ void k_comm111_110(DevSpace S, const double* __restrict__ X, const double* __restrict__ Y,
+                              double* __restrict__ Z, int do111, int do110)
+{
+  int N = S.norb;
+  int i = blockIdx.x;
+  const double* X1 = X + 32;
+  const double* Y1 = Y + 32;
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    double xy = 0.0, yx = 0.0;
+    for (int b = 0; b < N; ++b) {
+      xy = fma(X1[(size_t)b * N + i], Y1[(size_t)j * N + b], xy);
+      yx = fma(Y1[(size_t)b * N + i], X1[(size_t)j * N + b], yx);
+    }
+    double v = xy - yx;
+    if (do111) Z[32 + (size_t)j * N + i] += v;
+    if (do110 && j == i) {
+      double oc = S.occ[i];
+      if (oc >= 1e-6) atomicAdd(Z, (S.j2[i] + 1) * oc * v);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------- 220
+// Z0 += 2 sum_ch (2J+1) sum_{h in hh} n_h n_h' (X_{h,nbar} (nbar nbar) Y_{nbar,h})
+// (comm220ss, src/Commutator.cc:601-631); one warp per hh ket.
+__global__ void k_comm220(DevSpace S, DevWork W, const double* __restrict__ X, const double* __restrict__ Y,
+                          double* __restrict__ Z, int hX)
+{
+  int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  if (item >= W.n220) return;
+  int ch = W.items220[2 * item], h = W.items220[2 * item + 1];
+  int n = S.ch_n[ch];
+  long long off = S.ch_off[ch];
+  const double* xc = X + off + (long long)h * n;  // X(h,k) = hX X(k,h)
+  const double* yc = Y + off + (long long)h * n;  // Y(k,h)
+  const double* w = W.ket_wpp + S.ch_kofs[ch];
+  double d = 0.0;
+  for (int k = lane; k < n; k += 32) d = fma(xc[k] * w[k], yc[k], d);
+  d = warp_sum(d);
+  if (lane == 0) {
+    int J = ch / 6;
+    double nn = W.ket_nn[S.ch_kofs[ch] + h];
+    atomicAdd(Z, 2.0 * (2 * J + 1) * hX * d * nn);
+  }
+}
+
+// ---------------------------------------------------------------------- 121
+// TwoBodyME::GetTBMEmonopole (src/TwoBodyME.cc:615-682)
+__device__ double dev_monopole(const DevSpace& S, const double* op, int a, int b, int c, int d)
+{
+  int pab = (S.l[a] + S.l[b]) & 1, pcd = (S.l[c] + S.l[d]) & 1;
+  if (pab != pcd) return 0.0;
+  if (S.tz2[a] + S.tz2[b] != S.tz2[c] + S.tz2[d]) return 0.0;
+  int ja = S.j2[a], jb = S.j2[b];
+  int jmin = abs(ja - jb) / 2, jmax = (ja + jb) / 2;
+  double mon = 0.0;
+  for (int J = jmin; J <= jmax; ++J) mon += (2 * J + 1) * dev_tbme_J_norm(S, op, J, a, b, c, d);
+  mon /= (double)((ja + 1) * (jb + 1));
+  if (a == b) mon *= kSqrt2;
+  if (c == d) mon *= kSqrt2;
+  return mon;
+}
+
+// comm121ss, src/Commutator.cc:670-728: one warp per (i <= j) pair, lanes over
+// (hole a, b in the one-body channel of a).
+__global__ void k_comm121(DevSpace S, DevWork W, const int* __restrict__ holes, int nholes,
+                          const double* __restrict__ X, const double* __restrict__ Y, double* __restrict__ Z, int hZ)
+{
+  int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  if (item >= W.npairs1b) return;
+  int i = W.pairs1b[2 * item], j = W.pairs1b[2 * item + 1];
+  int N = S.norb;
+  const double* X1 = X + 32;
+  const double* Y1 = Y + 32;
+  double z = 0.0;
+  // enumerate (a, b) pairs: a = holes[ia], b = ob_list[ob_start[a] + ib]
+  int total = 0;
+  for (int ia = 0; ia < nholes; ++ia) total += S.ob_count[holes[ia]];
+  for (int t = lane; t < total; t += 32) {
+    int ia = 0, rem = t;
+    while (rem >= S.ob_count[holes[ia]]) {
+      rem -= S.ob_count[holes[ia]];
+      ++ia;
+    }
+    int a = holes[ia];
+    int b = S.ob_list[S.ob_start[a] + rem];
+    double nanb = S.occ[a] * (1.0 - S.occ[b]);
+    if (fabs(nanb) < 1e-6) continue;
+    int jja = S.j2[a], jjb = S.j2[b];
+    double ybiaj = dev_monopole(S, Y, b, i, a, j);
+    double yaibj = dev_monopole(S, Y, a, i, b, j);
+    z += (jjb + 1) * nanb * X1[(size_t)b * N + a] * ybiaj;
+    z -= (jja + 1) * nanb * X1[(size_t)a * N + b] * yaibj;
+    z -= (jjb + 1) * nanb * Y1[(size_t)b * N + a] * dev_monopole(S, X, b, i, a, j);
+    z += (jja + 1) * nanb * Y1[(size_t)a * N + b] * dev_monopole(S, X, a, i, b, j);
+  }
+  z = warp_sum(z);
+  if (lane == 0) {
+    Z[32 + (size_t)j * N + i] += z;
+    if (i != j) Z[32 + (size_t)i * N + j] += hZ * z;
+  }
+}
+
+// -------------------------------------------------------------- 221 (1b)
+// One-body part of comm222_pp_hh_221ss / comm221ss (src/Commutator.cc:1250-1294):
+// Z1_ij += 1/(2j_i+1) sum_c sum_J (2J+1) [n_c Mpp^J_{ci,cj} + nbar_c Mhh^J_{ci,cj}],
+// with the needed elements of the symmetrised intermediates
+// Mpp = X P Y + hZ (X P Y)^T, Mhh = X (nn) Y + hZ (...)^T (ConstructScalarMpp_Mhh,
+// src/Commutator.cc:1170-1194) evaluated as dot products.  One warp per (i, j, c).
+__device__ __forceinline__ double warp_dot_w(const double* a, const double* b, const double* w, int n, int lane)
+{
+  double d = 0.0;
+  for (int k = lane; k < n; k += 32) d = fma(a[k] * w[k], b[k], d);
+  return warp_sum(d);
+}
+
+__device__ __forceinline__ double warp_dot_list(const double* a, const double* b, const double* w, const int* idx,
+                                                int m, int lane)
+{
+  double d = 0.0;
+  for (int t = lane; t < m; t += 32) {
+    int k = idx[t];
+    d = fma(a[k] * w[k], b[k], d);
+  }
+  return warp_sum(d);
+}
+
+__global__ void k_comm221_1b(DevSpace S, DevWork W, const double* __restrict__ X, const double* __restrict__ Y,
+                             double* __restrict__ Z, int hX, int hZ)
+{
+  int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  if (item >= W.n221) return;
+  int i = W.items221[3 * item], j = W.items221[3 * item + 1], c = W.items221[3 * item + 2];
+  int N = S.norb;
+  double nc = S.occ[c], nbarc = 1.0 - nc;
+  int jc = S.j2[c], ji = S.j2[i], jj = S.j2[j];
+  int Jmin = max(abs(jc - ji), abs(jc - jj)) / 2;
+  int Jmax = (jc + min(ji, jj)) / 2;
+  int par = (S.l[c] + S.l[i]) & 1, tz = (S.tz2[c] + S.tz2[i]) / 2;
+  int kci = ket_index(N, min(c, i), max(c, i)), kcj = ket_index(N, min(c, j), max(c, j));
+  double z = 0.0;
+  for (int J = Jmin; J <= Jmax; ++J) {
+    int r = S.ketJ_loc[kci * S.NJ + J], s = S.ketJ_loc[kcj * S.NJ + J];
+    if (r < 0 || s < 0) continue;
+    int ch = chan_index(J, par, tz);
+    int n = S.ch_n[ch];
+    long long off = S.ch_off[ch];
+    const double* xr = X + off + (long long)r * n;
+    const double* xs = X + off + (long long)s * n;
+    const double* yr = Y + off + (long long)r * n;
+    const double* ys = Y + off + (long long)s * n;
+    double ph = 1.0;
+    if (c > i) ph *= iphase((jc + ji) / 2 + 1 + J);
+    if (c > j) ph *= iphase((jc + jj) / 2 + 1 + J);
+    double nrm = 1.0;
+    if (c == i) nrm *= kSqrt2;
+    if (c == j) nrm *= kSqrt2;
+    double fac = (2 * J + 1) * ph * nrm;
+    if (fabs(nc) > 1e-9) {
+      const double* w = W.ket_wpp + S.ch_kofs[ch];
+      double m_rs = hX * warp_dot_w(xr, ys, w, n, lane);
+      double m_sr = (r == s) ? m_rs : hX * warp_dot_w(xs, yr, w, n, lane);
+      z += fac * nc * (m_rs + hZ * m_sr);
+    }
+    if (fabs(nbarc) > 1e-9) {
+      const double* w = W.ket_nn + S.ch_kofs[ch];
+      const int* hh = W.hh_list + W.hh_off[ch];
+      int nhh = W.hh_off[ch + 1] - W.hh_off[ch];
+      double m_rs = hX * warp_dot_list(xr, ys, w, hh, nhh, lane);
+      double m_sr = (r == s) ? m_rs : hX * warp_dot_list(xs, yr, w, hh, nhh, lane);
+      z += fac * nbarc * (m_rs + hZ * m_sr);
+    }
+  }
+  if (lane == 0 && z != 0.0) {
+    double v = z / (ji + 1.0);
+    atomicAdd(Z + 32 + (size_t)j * N + i, v);
+    if (i != j) atomicAdd(Z + 32 + (size_t)i * N + j, hZ * v);
+  }
+}
+
+// ---------------------------------------------------------------------- 122
+// comm122ss, src/Commutator.cc:837-932.  W2(:, ij) = sum_items f (Y2(:,loc) X1(a,src)
+// - X2(:,loc) Y1(a,src)); one block per column, threads over rows.
+__global__ void k_comm122_w(DevSpace S, DevWork W, const double* __restrict__ X, const double* __restrict__ Y,
+                            double* __restrict__ W2)
+{
+  int col = blockIdx.x;
+  if (col >= W.ncols122) return;
+  int ch = W.cols122[4 * col], ij = W.cols122[4 * col + 1];
+  int first = W.cols122[4 * col + 2], cnt = W.cols122[4 * col + 3];
+  int n = S.ch_n[ch];
+  long long off = S.ch_off[ch];
+  int N = S.norb;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    double w = 0.0;
+    for (int t = 0; t < cnt; ++t) {
+      int loc = W.it122_loc[first + t];
+      int a = W.it122_a[first + t], src = W.it122_src[first + t];
+      double f = W.it122_f[first + t];
+      double x1 = X[32 + (size_t)src * N + a] * f;
+      double y1 = Y[32 + (size_t)src * N + a] * f;
+      w = fma(Y[off + (long long)loc * n + r], x1, w);
+      w = fma(-X[off + (long long)loc * n + r], y1, w);
+    }
+    W2[off + (long long)ij * n + r] = w;
+  }
+}
+
+// Z2 -= W2 + hZ W2^T, per channel in 32x32 tiles
+__global__ void k_sym_subtract(DevSpace S, const double* __restrict__ W2, double* __restrict__ Z, int hZ,
+                               const int* __restrict__ tiles, int ntiles)
+{
+  __shared__ double tt[32][33];
+  int t = blockIdx.x;
+  if (t >= ntiles) return;
+  int ch = tiles[3 * t], ti = tiles[3 * t + 1], tj = tiles[3 * t + 2];
+  int n = S.ch_n[ch];
+  long long off = S.ch_off[ch];
+  int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  // load W2 tile (tj, ti) transposed: rows tj*32+.., cols ti*32+..
+  for (int yy = ty; yy < 32; yy += 8) {
+    int r = tj * 32 + tx, c = ti * 32 + yy;
+    tt[yy][tx] = (r < n && c < n) ? W2[off + (long long)c * n + r] : 0.0;
+  }
+  __syncthreads();
+  for (int yy = ty; yy < 32; yy += 8) {
+    int r = ti * 32 + tx, c = tj * 32 + yy;
+    if (r < n && c < n) {
+      // W2^T(r, c) = W2(c, r) = tt[r - ti*32][c - tj*32] stored as tt[col=(r)][row=(c)]
+      double wt = tt[tx][yy];
+      Z[off + (long long)c * n + r] -= W2[off + (long long)c * n + r] + hZ * wt;
+    }
+  }
+}
+
+// ------------------------------------------------------------ Pandya forward
+// DoPandyaTransformation_SingleChannel_XandY (src/Commutator.cc:1392-1485) plus the
+// flipped Ybar of comm222_phss (src/Commutator.cc:1766-1788).  Outputs, per CC
+// channel, three n_cc x 2nph column-major panels:
+//   Xb(ik, t)  = Xbar(ik, t) * normfactor * (n_a - n_b)
+//   Yt(ik, t)  = Ybar(t, ik) * normfactor
+//   Yf(ik, t') = Ybar(t, ik) * normfactor * phi_bra phi_ik hY, t' = t with halves swapped
+// One thread per (ik, t); blocks over a (channel, tile) list.
+__global__ void k_pandya_fwd(DevSpace S, DevWork W, const double* __restrict__ X, const double* __restrict__ Y,
+                             int hY, double* __restrict__ Xb, double* __restrict__ Yt, double* __restrict__ Yf,
+                             const int* __restrict__ tiles, int ntiles)
+{
+  int tix = blockIdx.x;
+  if (tix >= ntiles) return;
+  int cc = tiles[3 * tix], row0 = tiles[3 * tix + 1], t0 = tiles[3 * tix + 2];
+  int ncc = S.cc_n[cc];
+  int nph = W.cc_nph[cc];
+  int ik = row0 + (threadIdx.x & 63);
+  int t = t0 + (threadIdx.x >> 6);
+  if (ik >= ncc || t >= 2 * nph) return;
+  int Jcc = cc / 6;
+  int ibra = t < nph ? t : t - nph;
+  int ab_case = t < nph ? 0 : 1;
+  int kb = W.cc_ph[W.cc_ph_off[cc] + ibra];
+  int bp = S.cc_p[S.cc_kofs[cc] + kb], bq = S.cc_q[S.cc_kofs[cc] + kb];
+  int a = ab_case ? bq : bp, b = ab_case ? bp : bq;
+  int c = S.cc_p[S.cc_kofs[cc] + ik], d = S.cc_q[S.cc_kofs[cc] + ik];
+  double xbar = 0.0, ybar = 0.0;
+  double nf = 1.0;
+  if (S.tz2[a] + S.tz2[d] == S.tz2[b] + S.tz2[c]) {
+    if (a == d) nf *= kSqrt2;
+    if (c == b) nf *= kSqrt2;
+    int ja = S.j2[a], jb = S.j2[b], jc = S.j2[c], jd = S.j2[d];
+    int jmin = max(abs(ja - jd), abs(jc - jb)) / 2;
+    int jmax = min(ja + jd, jc + jb) / 2;
+    int dJ = 1;
+    if (a == d || c == b) {
+      dJ = 2;
+      jmin += jmin & 1;
+    }
+    // GetTBME_J_norm_twoOps(Y, J, J, c, b, a, d): same element of X and Y
+    int lc = S.l[c], lb = S.l[b], la = S.l[a], ld = S.l[d];
+    bool ok = (((lc + lb + la + ld) & 1) == 0) && (S.tz2[c] + S.tz2[b] == S.tz2[a] + S.tz2[d]);
+    if (ok) {
+      int k1 = ket_index(S.norb, min(c, b), max(c, b));
+      int k2 = ket_index(S.norb, min(a, d), max(a, d));
+      int par = (lc + lb) & 1, tz = (S.tz2[c] + S.tz2[b]) / 2;
+      for (int J = jmin; J <= jmax; J += dJ) {
+        double sj = dev_sixj(S, ja, jb, Jcc, jc, jd, J);
+        if (fabs(sj) < 1e-8) continue;
+        int bi = S.ketJ_loc[k1 * S.NJ + J], ki = S.ketJ_loc[k2 * S.NJ + J];
+        if (bi < 0 || ki < 0) continue;
+        int ch = chan_index(J, par, tz);
+        int n = S.ch_n[ch];
+        long long e = S.ch_off[ch] + (long long)ki * n + bi;
+        double ph = 1.0;
+        if (c > b) ph *= iphase((S.j2[c] + S.j2[b]) / 2 + 1 + J);
+        if (a > d) ph *= iphase((S.j2[a] + S.j2[d]) / 2 + 1 + J);
+        double coef = (2 * J + 1) * sj * ph;
+        xbar -= coef * X[e];
+        ybar -= coef * Y[e] * hY;
+      }
+    }
+  }
+  double na_nb = S.occ[a] - S.occ[b];
+  long long base = W.xb_off[cc];
+  Xb[base + (long long)t * ncc + ik] = xbar * nf * na_nb;
+  double yv = ybar * nf;
+  Yt[base + (long long)t * ncc + ik] = yv;
+  const int* phi = W.phase_tab + W.cc_phase_off[cc];
+  int tf = t < nph ? t + nph : t - nph;
+  Yf[base + (long long)tf * ncc + ik] = yv * phi[kb] * phi[ik] * hY;
+}
+
+// ------------------------------------------------------------ Pandya inverse
+// AddInversePandyaTransformation (src/Commutator.cc:1501-1616): for every
+// (ibra <= iket) element of every 2b channel block, the two J' sums over Zbar.
+__global__ void k_pandya_inv(DevSpace S, DevWork W, const double* __restrict__ Zb, double* __restrict__ Z, int hZ,
+                             const int* __restrict__ tiles, int ntiles)
+{
+  int tix = blockIdx.x;
+  if (tix >= ntiles) return;
+  int ch = tiles[3 * tix], ti = tiles[3 * tix + 1], tj = tiles[3 * tix + 2];
+  int n = S.ch_n[ch];
+  int ibra = ti * 16 + (threadIdx.x & 15);
+  int iket = tj * 16 + (threadIdx.x >> 4);
+  if (ibra >= n || iket >= n) return;
+  if (hZ == 1 ? (iket < ibra) : (iket <= ibra)) return;
+  int J = ch / 6;
+  int kofs = S.ch_kofs[ch];
+  int i = S.ket_p[kofs + ibra], j = S.ket_q[kofs + ibra];
+  int k = S.ket_p[kofs + iket], l = S.ket_q[kofs + iket];
+  int jji = S.j2[i], jjj = S.j2[j], jjk = S.j2[k], jjl = S.j2[l];
+  int N = S.norb;
+  double commij = 0.0, commji = 0.0;
+  {
+    int par = (S.l[i] + S.l[l]) & 1;
+    int tz = abs(S.tz2[i] - S.tz2[l]) / 2;
+    int Jpmin = max(abs(jji - jjl), abs(jjk - jjj)) / 2;
+    int Jpmax = min(jji + jjl, jjk + jjj) / 2;
+    int kil = ket_index(N, min(i, l), max(i, l)), kkj = ket_index(N, min(j, k), max(j, k));
+    for (int Jp = Jpmin; Jp <= Jpmax; ++Jp) {
+      double sj = dev_sixj(S, jji, jjj, J, jjk, jjl, Jp);
+      if (fabs(sj) < 1e-8) continue;
+      int cc = chan_index(Jp, par, tz);
+      int ncc = S.cc_n[cc];
+      int il = S.ccJ_loc[kil * S.NJ + Jp] + (i > l ? ncc : 0);
+      int kj = S.ccJ_loc[kkj * S.NJ + Jp] + (k > j ? ncc : 0);
+      commij -= (2 * Jp + 1) * sj * Zb[W.zb_off[cc] + (long long)kj * ncc + il];
+    }
+  }
+  if (k == l) {
+    commji = commij;
+  } else if (i == j) {
+    commji = iphase((jji + jjj + jjk + jjl) / 2) * commij;
+  } else {
+    int par = (S.l[i] + S.l[k]) & 1;
+    int tz = abs(S.tz2[i] - S.tz2[k]) / 2;
+    int Jpmin = max(abs(jjj - jjl), abs(jjk - jji)) / 2;
+    int Jpmax = min(jjj + jjl, jjk + jji) / 2;
+    int kik = ket_index(N, min(i, k), max(i, k)), klj = ket_index(N, min(l, j), max(l, j));
+    for (int Jp = Jpmin; Jp <= Jpmax; ++Jp) {
+      double sj = dev_sixj(S, jjj, jji, J, jjk, jjl, Jp);
+      if (fabs(sj) < 1e-8) continue;
+      int cc = chan_index(Jp, par, tz);
+      int ncc = S.cc_n[cc];
+      int ik = S.ccJ_loc[kik * S.NJ + Jp] + (i > k ? ncc : 0);
+      int lj = S.ccJ_loc[klj * S.NJ + Jp] + (l > j ? ncc : 0);
+      commji -= (2 * Jp + 1) * sj * Zb[W.zb_off[cc] + (long long)lj * ncc + ik];
+    }
+  }
+  int bd = (i == j), kd = (k == l);
+  double norm = bd == kd ? 1 + bd : kSqrt2;
+  double z = -(commij - iphase((jjk + jjl) / 2 - J) * commji) / norm;
+  long long off = S.ch_off[ch];
+  Z[off + (long long)iket * n + ibra] += z;
+  if (ibra != iket) Z[off + (long long)ibra * n + iket] += hZ * z;
+}
+
+// ------------------------------------------------------------ operator algebra
+__global__ void k_axpy(double* __restrict__ y, const double* __restrict__ x, double a, long long n)
+{
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) y[i] = fma(a, x[i], y[i]);
+}
+
+__global__ void k_scale(double* __restrict__ y, double a, long long n)
+{
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) y[i] *= a;
+}
+
+// Operator::Norm pieces: chunk c of the norm list sums weight * v^2 over its
+// range; partial[c] is written (no atomics, deterministic).
+__global__ void k_norm_chunks(const double* __restrict__ A, const long long* __restrict__ chunk_off,
+                              const int* __restrict__ chunk_len, const double* __restrict__ chunk_w,
+                              double* __restrict__ partial, int nchunks)
+{
+  __shared__ double red[32];
+  int c = blockIdx.x;
+  if (c >= nchunks) return;
+  const double* p = A + chunk_off[c];
+  int len = chunk_len[c];
+  double s = 0.0;
+  for (int t = threadIdx.x; t < len; t += blockDim.x) s = fma(p[t], p[t], s);
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) partial[c] = v * chunk_w[c];
+  }
+}
+
+// one-body norm: sum over p, q in one channel of (2 j_p + 1) O_pq^2
+__global__ void k_norm_onebody(DevSpace S, const double* __restrict__ A, double* __restrict__ out)
+{
+  __shared__ double red[32];
+  int N = S.norb;
+  double s = 0.0;
+  for (int t = threadIdx.x; t < N * N; t += blockDim.x) {
+    int p = t % N, q = t / N;
+    if (S.l[p] == S.l[q] && S.j2[p] == S.j2[q] && S.tz2[p] == S.tz2[q]) {
+      double v = A[32 + t];
+      s += v * v * (S.j2[p] + 1);
+    }
+  }
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) *out = v;
+  }
+}
+
+// ------------------------------------------------------------------ launchers
+cudaError_t launch_comm111_110(const Space& s, const double* X, const double* Y, double* Z, bool do111, bool do110,
+                               cudaStream_t st)
+{
+  int threads = s.norb <= 128 ? 128 : 256;
+  k_comm111_110<<<s.norb, threads, 0, st>>>(s.dev, X, Y, Z, do111, do110);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_comm220(const Space& s, const double* X, const double* Y, double* Z, int hX, cudaStream_t st)
+{
+  if (s.work.n220 == 0) return cudaSuccess;
+  int wpb = 8;
+  k_comm220<<<(s.work.n220 + wpb - 1) / wpb, 32 * wpb, 0, st>>>(s.dev, s.work, X, Y, Z, hX);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_comm121(const Space& s, const int* dev_holes, const double* X, const double* Y, double* Z,
+                           int hZ, cudaStream_t st)
+{
+  if (s.work.npairs1b == 0) return cudaSuccess;
+  int wpb = 4;
+  k_comm121<<<(s.work.npairs1b + wpb - 1) / wpb, 32 * wpb, 0, st>>>(s.dev, s.work, dev_holes, (int)s.holes.size(),
+                                                                    X, Y, Z, hZ);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, double* Z, int hX, int hZ,
+                              cudaStream_t st)
+{
+  if (s.work.n221 == 0) return cudaSuccess;
+  int wpb = 8;
+  k_comm221_1b<<<(s.work.n221 + wpb - 1) / wpb, 32 * wpb, 0, st>>>(s.dev, s.work, X, Y, Z, hX, hZ);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, double* Z, double* W2, int hZ,
+                           const int* sym_tiles, int nsym_tiles, cudaStream_t st)
+{
+  if (s.work.ncols122 == 0) return cudaSuccess;
+  k_comm122_w<<<s.work.ncols122, 128, 0, st>>>(s.dev, s.work, X, Y, W2);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_sym_subtract<<<nsym_tiles, 256, 0, st>>>(s.dev, W2, Z, hZ, sym_tiles, nsym_tiles);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pandya_fwd(const Space& s, const double* X, const double* Y, int hY, double* Xb, double* Yt,
+                              double* Yf, const int* tiles, int ntiles, cudaStream_t st)
+{
+  if (ntiles == 0) return cudaSuccess;
+  k_pandya_fwd<<<ntiles, 256, 0, st>>>(s.dev, s.work, X, Y, hY, Xb, Yt, Yf, tiles, ntiles);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pandya_inv(const Space& s, const double* Zb, double* Z, int hZ, const int* tiles, int ntiles,
+                              cudaStream_t st)
+{
+  if (ntiles == 0) return cudaSuccess;
+  k_pandya_inv<<<ntiles, 256, 0, st>>>(s.dev, s.work, Zb, Z, hZ, tiles, ntiles);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_axpy(double* y, const double* x, double a, long long n, cudaStream_t st)
+{
+  k_axpy<<<1216, 256, 0, st>>>(y, x, a, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scale(double* y, double a, long long n, cudaStream_t st)
+{
+  k_scale<<<1216, 256, 0, st>>>(y, a, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_norm(const Space& s, const double* A, const long long* chunk_off, const int* chunk_len,
+                        const double* chunk_w, int nchunks, double* partial, cudaStream_t st)
+{
+  k_norm_onebody<<<1, 256, 0, st>>>(s.dev, A, partial + nchunks);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || nchunks == 0) return e;
+  k_norm_chunks<<<nchunks, 256, 0, st>>>(A, chunk_off, chunk_len, chunk_w, partial, nchunks);
+  return cudaGetLastError();
+}
+
+}  // namespace imsrg

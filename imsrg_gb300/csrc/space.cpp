@@ -1,0 +1,394 @@
+// Model-space bookkeeping, restating the reference's rules:
+//   orbit order + reference occupations  ModelSpace::Init, GetOrbitsAZ
+//                                        (src/ModelSpace.cc:353-417, 610-645)
+//   kets p <= q, Index2, pp/hh/ph        ModelSpace::SetupKets (src/ModelSpace.cc:1108-1200)
+//   2b channel membership                TwoBodyChannel::CheckChannel_ket (src/TwoBodyChannel.cc:142-151)
+//   cross-coupled channel membership     TwoBodyChannel_CC::CheckChannel_ket (src/TwoBodyChannel.cc:180-188)
+//   channel index 6J + 2(Tz+1) + parity  ModelSpace::GetTwoBodyChannelIndex (src/ModelSpace.cc:1046-1053)
+// plus the arena layout and the per-kernel work lists.
+#include "space.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <map>
+#include <stdexcept>
+
+#include <cuda_runtime.h>
+
+namespace imsrg {
+
+static const double OCC_CUT = 1e-6;  // ModelSpace::OCC_CUT (src/ModelSpace.cc:14)
+
+static int64_t round32(int64_t x) { return (x + 31) / 32 * 32; }
+
+void reference_orbits(int emax, int A, int Z, std::vector<int>& n, std::vector<int>& l, std::vector<int>& j2,
+                      std::vector<int>& tz2, std::vector<double>& occ)
+{
+  // occupations: fill proton and neutron shells in the order of GetOrbitsAZ
+  std::map<std::vector<int>, double> filled;
+  double zz = 0, nn = 0;
+  bool done = false;
+  for (int N = 0; N <= emax && !done; ++N) {
+    for (int g = 2 * N + 1; g >= -2 * N; g -= 4) {
+      int jj = std::abs(g);
+      int ll = g < 0 ? (jj + 1) / 2 : (jj - 1) / 2;
+      int nr = (N - ll) / 2;
+      if (zz < Z) {
+        double dz = std::min(Z - zz, jj + 1.0);
+        filled[{nr, ll, jj, -1}] = dz / (jj + 1.0);
+        zz += dz;
+      }
+      if (nn < A - Z) {
+        double dn = std::min(A - Z - nn, jj + 1.0);
+        filled[{nr, ll, jj, 1}] = dn / (jj + 1.0);
+        nn += dn;
+      }
+      if (zz == Z && nn == A - Z) {
+        done = true;
+        break;
+      }
+    }
+  }
+  if (!done) throw std::runtime_error("model space too small for the reference nucleus");
+  n.clear(); l.clear(); j2.clear(); tz2.clear(); occ.clear();
+  for (int N = 0; N <= emax; ++N)
+    for (int ll = N; ll >= 0; ll -= 2) {
+      int nr = (N - ll) / 2;
+      for (int jj = 2 * ll + 1; jj >= 2 * ll - 1 && jj > 0; jj -= 2)
+        for (int tz : {-1, 1}) {
+          n.push_back(nr);
+          l.push_back(ll);
+          j2.push_back(jj);
+          tz2.push_back(tz);
+          auto it = filled.find({nr, ll, jj, tz});
+          occ.push_back(it == filled.end() ? 0.0 : it->second);
+        }
+    }
+}
+
+Space* build_space(int emax, const std::vector<int>& n, const std::vector<int>& l, const std::vector<int>& j2,
+                   const std::vector<int>& tz2, const std::vector<double>& occ)
+{
+  Space* sp = new Space();
+  Space& s = *sp;
+  s.emax = emax;
+  s.norb = (int)n.size();
+  s.n = n; s.l = l; s.j2 = j2; s.tz2 = tz2; s.occ = occ;
+  int j2max = 0;
+  for (int i = 0; i < s.norb; ++i) {
+    if (j2[i] < 1 || !(j2[i] & 1) || (tz2[i] != 1 && tz2[i] != -1) || l[i] < 0)
+      throw std::runtime_error("invalid orbit quantum numbers");
+    if (j2[i] > 2 * emax + 1) throw std::runtime_error("orbit j exceeds 2*emax+1");
+    j2max = std::max(j2max, j2[i]);
+    if (occ[i] >= OCC_CUT) s.holes.push_back(i);
+  }
+  s.NJ = j2max + 1;
+  s.nch = 6 * (j2max + 1);  // ModelSpace::AddOrbit, src/ModelSpace.cc:936-946
+  s.nkets = s.norb * (s.norb + 1) / 2;
+
+  // one-body channels (l, j2, tz2)
+  s.ob_start.resize(s.norb);
+  s.ob_count.resize(s.norb);
+  for (int i = 0; i < s.norb; ++i) {
+    s.ob_start[i] = (int)s.ob_list.size();
+    for (int a = 0; a < s.norb; ++a)
+      if (l[a] == l[i] && j2[a] == j2[i] && tz2[a] == tz2[i]) s.ob_list.push_back(a);
+    s.ob_count[i] = (int)s.ob_list.size() - s.ob_start[i];
+  }
+
+  // channels
+  s.ch.resize(s.nch);
+  s.cc.resize(s.nch);
+  s.ketJ_loc.assign((size_t)s.nkets * s.NJ, -1);
+  s.ccJ_loc.assign((size_t)s.nkets * s.NJ, -1);
+  for (int c = 0; c < s.nch; ++c) {
+    int J = c / 6, Tz = (c % 6) / 2 - 1, par = c % 2;
+    Chan& C = s.ch[c];
+    Chan& K = s.cc[c];
+    C.J = K.J = J;
+    C.parity = K.parity = par;
+    C.Tz = K.Tz = Tz;
+    for (int p = 0; p < s.norb; ++p)
+      for (int q = p; q < s.norb; ++q) {
+        if ((l[p] + l[q]) % 2 != par) continue;
+        if (j2[p] + j2[q] < 2 * J) continue;
+        if (std::abs(j2[p] - j2[q]) > 2 * J) continue;
+        int k = ket_index(s.norb, p, q);
+        bool hp = occ[p] > OCC_CUT, hq = occ[q] > OCC_CUT;
+        bool lp = occ[p] < OCC_CUT, lq = occ[q] < OCC_CUT;
+        if (!(p == q && J % 2 != 0) && tz2[p] + tz2[q] == 2 * Tz) {
+          int loc = C.n();
+          s.ketJ_loc[(size_t)k * s.NJ + J] = loc;
+          C.p.push_back(p);
+          C.q.push_back(q);
+          if (lp && lq) C.pp.push_back(loc);
+          if (hp != hq) C.ph.push_back(loc);
+          if (hp && hq) C.hh.push_back(loc);
+        }
+        if (std::abs(tz2[p] - tz2[q]) == 2 * Tz) {
+          int loc = K.n();
+          s.ccJ_loc[(size_t)k * s.NJ + J] = loc;
+          K.p.push_back(p);
+          K.q.push_back(q);
+          if (lp && lq) K.pp.push_back(loc);
+          if (hp != hq) K.ph.push_back(loc);
+          if (hp && hq) K.hh.push_back(loc);
+        }
+      }
+  }
+
+  // arena layout
+  int64_t cur = round32(32 + (int64_t)s.norb * s.norb);
+  for (int c = 0; c < s.nch; ++c) {
+    s.ch[c].off = cur;
+    cur = round32(cur + (int64_t)s.ch[c].n() * s.ch[c].n());
+  }
+  s.arena = cur;
+
+  build_sixj_table(s);
+
+  // ---- ladder work lists: w = (pp: 1) + (hh: nbar nbar - n n) + (ph: nbar nbar)
+  //      (ConstructScalarMpp_Mhh, src/Commutator.cc:1170-1183, Mpp - Mhh)
+  s.ladder_kidx_off.assign(s.nch, -1);
+  s.ladder_w_off.assign(s.nch, -1);
+  for (int c = 0; c < s.nch; ++c) {
+    const Chan& C = s.ch[c];
+    if (C.n() == 0) continue;
+    std::vector<std::pair<int, double>> kw;
+    for (int i = 0; i < C.n(); ++i) {
+      double op = occ[C.p[i]], oq = occ[C.q[i]];
+      double w = 0;
+      bool hp = op > OCC_CUT, hq = oq > OCC_CUT, lp = op < OCC_CUT, lq = oq < OCC_CUT;
+      if (lp && lq) w += 1.0;
+      if (hp && hq) w += (1 - op) * (1 - oq) - op * oq;
+      if (hp != hq) w += (1 - op) * (1 - oq);
+      if (w != 0.0) kw.push_back({i, w});
+    }
+    if (kw.empty()) continue;
+    s.ladder_kidx_off[c] = (int)s.kidx.size();
+    s.ladder_w_off[c] = (int)s.kweight.size();
+    for (auto& x : kw) {
+      s.kidx.push_back(x.first);
+      s.kweight.push_back(x.second);
+    }
+    SymGemmJob jb;
+    jb.a_off = C.off;
+    jb.b_off = C.off;
+    jb.out_off = C.off;
+    jb.m = C.n();
+    jb.K = (int)kw.size();
+    jb.lda = jb.ldb = jb.ldo = C.n();
+    jb.kidx_off = s.ladder_kidx_off[c];
+    jb.w_off = s.ladder_w_off[c];
+    s.ladder_jobs.push_back(jb);
+  }
+
+  // ---- Pandya work lists (DoPandyaTransformation_SingleChannel_XandY, src/Commutator.cc:1392-1485)
+  s.cc_nph.assign(s.nch, 0);
+  s.cc_ph_off.assign(s.nch, 0);
+  s.xb_off.assign(s.nch, 0);
+  s.zb_off.assign(s.nch, 0);
+  s.cc_phase_off.assign(s.nch, 0);
+  int64_t xb = 0, zb = 0;
+  for (int c = 0; c < s.nch; ++c) {
+    const Chan& K = s.cc[c];
+    s.cc_ph_off[c] = (int)s.cc_ph.size();
+    for (int x : K.hh) s.cc_ph.push_back(x);
+    for (int x : K.ph) s.cc_ph.push_back(x);
+    s.cc_nph[c] = (int)(K.hh.size() + K.ph.size());
+    s.cc_phase_off[c] = (int)s.phase_tab.size();
+    for (int i = 0; i < K.n(); ++i) s.phase_tab.push_back(iphase((j2[K.p[i]] + j2[K.q[i]]) / 2));
+    s.xb_off[c] = xb;
+    s.zb_off[c] = zb;
+    int ncc = K.n();
+    int K2 = 2 * s.cc_nph[c];
+    xb = round32(xb + (int64_t)ncc * K2);
+    zb = round32(zb + (int64_t)ncc * 2 * ncc);
+    if (ncc == 0 || K2 == 0) continue;
+    SymGemmJob head;
+    head.a_off = s.xb_off[c];
+    head.b_off = s.xb_off[c];
+    head.out_off = s.zb_off[c];
+    head.m = ncc;
+    head.K = K2;
+    head.lda = head.ldb = head.ldo = ncc;
+    SymGemmJob tail = head;
+    tail.out_off = s.zb_off[c] + (int64_t)ncc * ncc;
+    tail.phase_off = s.cc_phase_off[c];
+    s.zbar_jobs.push_back(head);
+    s.zbar_jobs.push_back(tail);
+  }
+  s.xb_total = xb;
+  s.zb_total = zb;
+
+  // ---- small-term work lists
+  s.hh_off.assign(s.nch + 1, 0);
+  for (int c = 0; c < s.nch; ++c) {
+    const Chan& C = s.ch[c];
+    int J = C.J;
+    (void)J;
+    s.hh_off[c] = (int)s.hh_list.size();
+    for (int x : C.hh) s.hh_list.push_back(x);
+    for (int i = 0; i < C.n(); ++i) {
+      double op = occ[C.p[i]], oq = occ[C.q[i]];
+      bool hp = op > OCC_CUT, hq = oq > OCC_CUT, lp = op < OCC_CUT, lq = oq < OCC_CUT;
+      double wpp = 0, wnn = 0;
+      if (lp && lq) wpp = 1.0;  // pp rows enter unweighted (src/Commutator.cc:1176, :619)
+      if (hp && hq) {
+        wpp = (1 - op) * (1 - oq);
+        wnn = op * oq;
+      }
+      if (hp != hq) wpp = (1 - op) * (1 - oq);
+      s.ket_wpp.push_back(wpp);
+      s.ket_nn.push_back(wnn);
+    }
+    for (int x : C.hh) {
+      s.items220.push_back(c);
+      s.items220.push_back(x);
+    }
+  }
+  s.hh_off[s.nch] = (int)s.hh_list.size();
+  for (int i = 0; i < s.norb; ++i)
+    for (int k = 0; k < s.ob_count[i]; ++k) {
+      int j = s.ob_list[s.ob_start[i] + k];
+      if (j < i) continue;
+      s.pairs1b.push_back(i);
+      s.pairs1b.push_back(j);
+      for (int c = 0; c < s.norb; ++c) {
+        s.items221.push_back(i);
+        s.items221.push_back(j);
+        s.items221.push_back(c);
+      }
+    }
+  // comm122ss gathers (src/Commutator.cc:862-903)
+  const double SQ2 = 1.4142135623730950488;
+  for (int c = 0; c < s.nch; ++c) {
+    const Chan& C = s.ch[c];
+    int J = C.J;
+    for (int ij = 0; ij < C.n(); ++ij) {
+      int i = C.p[ij], j = C.q[ij];
+      int flip = -iphase((j2[i] + j2[j]) / 2 - J);
+      int first = (int)s.it122_loc.size();
+      for (int k = 0; k < s.ob_count[i]; ++k) {
+        int a = s.ob_list[s.ob_start[i] + k];
+        int loc = s.ketJ_loc[(size_t)ket_index(s.norb, std::min(a, j), std::max(a, j)) * s.NJ + J];
+        if (loc < 0) continue;
+        double f = a > j ? flip : (a == j ? SQ2 : 1.0);
+        if (i == j) f = f / SQ2 * 2.0;
+        s.it122_loc.push_back(loc);
+        s.it122_a.push_back(a);
+        s.it122_src.push_back(i);
+        s.it122_f.push_back(f);
+      }
+      if (i != j)
+        for (int k = 0; k < s.ob_count[j]; ++k) {
+          int a = s.ob_list[s.ob_start[j] + k];
+          int loc = s.ketJ_loc[(size_t)ket_index(s.norb, std::min(a, i), std::max(a, i)) * s.NJ + J];
+          if (loc < 0) continue;
+          double f = i > a ? flip : (i == a ? SQ2 : 1.0);
+          s.it122_loc.push_back(loc);
+          s.it122_a.push_back(a);
+          s.it122_src.push_back(j);
+          s.it122_f.push_back(f);
+        }
+      s.cols122.push_back(c);
+      s.cols122.push_back(ij);
+      s.cols122.push_back(first);
+      s.cols122.push_back((int)s.it122_loc.size() - first);
+    }
+  }
+  return sp;
+}
+
+template <class T>
+static T* dev_copy(Space& s, const std::vector<T>& v)
+{
+  void* p = nullptr;
+  size_t bytes = std::max<size_t>(1, v.size()) * sizeof(T);
+  if (cudaMalloc(&p, bytes) != cudaSuccess) throw std::runtime_error("cudaMalloc failed for space tables");
+  s.dev_allocs.push_back(p);
+  if (!v.empty() && cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+    throw std::runtime_error("cudaMemcpy failed for space tables");
+  return (T*)p;
+}
+
+void upload_space(Space& s)
+{
+  DevSpace& d = s.dev;
+  d.norb = s.norb;
+  d.nch = s.nch;
+  d.nkets = s.nkets;
+  d.NJ = s.NJ;
+  d.d1 = s.d1;
+  d.l = dev_copy(s, s.l);
+  d.j2 = dev_copy(s, s.j2);
+  d.tz2 = dev_copy(s, s.tz2);
+  d.occ = dev_copy(s, s.occ);
+  d.ob_start = dev_copy(s, s.ob_start);
+  d.ob_count = dev_copy(s, s.ob_count);
+  d.ob_list = dev_copy(s, s.ob_list);
+  d.ketJ_loc = dev_copy(s, s.ketJ_loc);
+  d.ccJ_loc = dev_copy(s, s.ccJ_loc);
+  std::vector<int> ch_n(s.nch), ch_kofs(s.nch), kp, kq, cc_n(s.nch), cc_kofs(s.nch), cp, cq;
+  std::vector<long long> ch_off(s.nch);
+  for (int c = 0; c < s.nch; ++c) {
+    ch_n[c] = s.ch[c].n();
+    ch_off[c] = s.ch[c].off;
+    ch_kofs[c] = (int)kp.size();
+    kp.insert(kp.end(), s.ch[c].p.begin(), s.ch[c].p.end());
+    kq.insert(kq.end(), s.ch[c].q.begin(), s.ch[c].q.end());
+    cc_n[c] = s.cc[c].n();
+    cc_kofs[c] = (int)cp.size();
+    cp.insert(cp.end(), s.cc[c].p.begin(), s.cc[c].p.end());
+    cq.insert(cq.end(), s.cc[c].q.begin(), s.cc[c].q.end());
+  }
+  d.ch_n = dev_copy(s, ch_n);
+  d.ch_off = dev_copy(s, ch_off);
+  d.ch_kofs = dev_copy(s, ch_kofs);
+  d.ket_p = dev_copy(s, kp);
+  d.ket_q = dev_copy(s, kq);
+  d.cc_n = dev_copy(s, cc_n);
+  d.cc_kofs = dev_copy(s, cc_kofs);
+  d.cc_p = dev_copy(s, cp);
+  d.cc_q = dev_copy(s, cq);
+  d.sixj_base = dev_copy(s, s.sixj_base);
+  d.sixj_val = dev_copy(s, s.sixj_val);
+
+  DevWork& w = s.work;
+  w.ket_wpp = dev_copy(s, s.ket_wpp);
+  w.ket_nn = dev_copy(s, s.ket_nn);
+  w.hh_off = dev_copy(s, s.hh_off);
+  w.hh_list = dev_copy(s, s.hh_list);
+  w.items220 = dev_copy(s, s.items220);
+  w.n220 = (int)s.items220.size() / 2;
+  w.pairs1b = dev_copy(s, s.pairs1b);
+  w.npairs1b = (int)s.pairs1b.size() / 2;
+  w.items221 = dev_copy(s, s.items221);
+  w.n221 = (int)s.items221.size() / 3;
+  w.cols122 = dev_copy(s, s.cols122);
+  w.ncols122 = (int)s.cols122.size() / 4;
+  w.it122_loc = dev_copy(s, s.it122_loc);
+  w.it122_a = dev_copy(s, s.it122_a);
+  w.it122_src = dev_copy(s, s.it122_src);
+  w.it122_f = dev_copy(s, s.it122_f);
+  w.kidx = dev_copy(s, s.kidx);
+  w.kweight = dev_copy(s, s.kweight);
+  w.phase_tab = dev_copy(s, s.phase_tab);
+  w.cc_nph = dev_copy(s, s.cc_nph);
+  w.cc_ph_off = dev_copy(s, s.cc_ph_off);
+  w.cc_ph = dev_copy(s, s.cc_ph);
+  std::vector<long long> xo(s.xb_off.begin(), s.xb_off.end()), zo(s.zb_off.begin(), s.zb_off.end());
+  w.xb_off = dev_copy(s, xo);
+  w.zb_off = dev_copy(s, zo);
+  w.cc_phase_off = dev_copy(s, s.cc_phase_off);
+}
+
+Space::~Space()
+{
+  for (void* p : dev_allocs) cudaFree(p);
+  for (Scratch* sc : {&s_xb, &s_yb, &s_yf, &s_zb, &s_w2, &s_red, &s_split_a, &s_split_b, &s_split_e, &s_jobs})
+    if (sc->ptr) cudaFree(sc->ptr);
+}
+
+}  // namespace imsrg

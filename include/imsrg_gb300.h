@@ -1,0 +1,184 @@
+/*
+ * imsrg_gb300 -- C ABI of the GB300 (sm_103a) IMSRG(2) scalar commutator.
+ *
+ * Drop-in boundary for IMSRG++'s angular-momentum-coupled IMSRG(2)
+ * commutator [X,Y] and BCH transform.  Plain C types only: pointers, sizes,
+ * int status codes, and an opaque cudaStream_t passed as void* (NULL = the
+ * legacy default stream).  No entry point exits the process; every one
+ * returns IMSRG_OK or an error code, with a message in imsrg_last_error().
+ *
+ * Data model.  A model space (imsrg_space) holds the orbit list and the
+ * channel bookkeeping of the reference's ModelSpace, and the device tables
+ * the kernels read.  An operator (imsrg_op) is one device-resident FP64
+ * "arena" (the reference's Operator: ZeroBody, OneBody, TwoBody):
+ *     [0]                 ZeroBody
+ *     [32, 32+N*N)        OneBody, N x N column-major (N orbits)
+ *     offset(ch) ...      one n_ch x n_ch column-major block per two-body
+ *                         channel ch = 6J + 2(Tz+1) + parity, kets in the
+ *                         reference's local order; every block starts on a
+ *                         multiple of 32 doubles.
+ * Column-major n x n blocks are exactly arma::mat, so packing a reference
+ * Operator is one memcpy per block.
+ *
+ * Term entry points accumulate into Z, as the reference's
+ * Commutator::comm*ss(X, Y, Z) do; Z's hermiticity flag selects the
+ * symmetrisation.  X and Y must be hermitian or anti-hermitian.
+ *
+ * All calls that take the same imsrg_space share its scratch workspace and
+ * must be ordered on one stream (or otherwise serialised by the caller).
+ */
+#ifndef IMSRG_GB300_H
+#define IMSRG_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define IMSRG_OK 0
+#define IMSRG_ERR_ARG 1         /* bad argument (null, size, index) */
+#define IMSRG_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define IMSRG_ERR_UNSUPPORTED 3 /* operator symmetry the GPU path does not handle */
+#define IMSRG_ERR_NOMEM 4       /* device allocation failed */
+#define IMSRG_ERR_KERNEL 5      /* a kernel reported an error through its status word */
+
+/* precision of the dense contractions (ladder and Pandya channel GEMMs) */
+#define IMSRG_PREC_FP64 0  /* plain FP64 (CUDA-core DFMA) */
+#define IMSRG_PREC_SPLIT 1 /* Ozaki-style sliced BF16 tensor-core products (tcgen05), FP64 recombination */
+
+typedef struct imsrg_space imsrg_space;
+typedef struct imsrg_op imsrg_op;
+
+/* Last error message of the calling thread ("" if none). */
+const char* imsrg_last_error(void);
+
+/* ----------------------------------------------------------------- spaces */
+
+/* Model space from an explicit orbit list (orbit i = (n[i], l[i], j2[i], tz2[i])
+ * with occupation occ[i], in the reference's orbit order).  Builds kets p<=q,
+ * the two-body channels, the cross-coupled channels and the 6j table.
+ * Replaces ModelSpace::Init / SetupKets (src/ModelSpace.cc:353-417,1120-1200),
+ * TwoBodyChannel(_CC)::Initialize (src/TwoBodyChannel.cc:19-67) and the
+ * SixJCache_112112 fill (src/AngMomCache.cc:58-104).  emax bounds the 6j table
+ * (orbit j2 <= 2*emax+1). */
+int imsrg_space_create(int emax, int norb, const int* n, const int* l, const int* j2, const int* tz2,
+                       const double* occ, imsrg_space** out);
+
+/* Harmonic-oscillator space with every orbit 2n+l <= emax, both isospins,
+ * occupations of the reference nucleus (A, Z) filled as
+ * ModelSpace(emax, "<A,Z>", "<A,Z>") does (src/ModelSpace.cc:202-220,610-645). */
+int imsrg_space_create_reference(int emax, int A, int Z, imsrg_space** out);
+
+void imsrg_space_destroy(imsrg_space* s);
+
+/* Sizes: orbits, two-body channels, arena length in doubles. */
+int imsrg_space_sizes(const imsrg_space* s, int* norb, int* nch, long long* arena_len);
+
+/* Orbit i: ModelSpace::GetOrbit (src/ModelSpace.hh:41-57). */
+int imsrg_space_orbit(const imsrg_space* s, int i, int* n, int* l, int* j2, int* tz2, double* occ);
+
+/* Two-body channel ch: TwoBodyChannel (J, parity, Tz, GetNumberKets), plus its
+ * arena offset in doubles.  src/ModelSpace.cc:1046-1053, src/TwoBodyChannel.cc:19-67. */
+int imsrg_space_channel(const imsrg_space* s, int ch, int* J, int* parity, int* Tz, int* nkets, long long* offset);
+
+/* Kets of channel ch in local order: TwoBodyChannel::GetKet(i).p / .q
+ * (src/TwoBodyChannel.cc:79-80).  p and q hold nkets entries each. */
+int imsrg_space_channel_kets(const imsrg_space* s, int ch, int* p, int* q);
+
+/* Cross-coupled channel ch: TwoBodyChannel_CC (src/TwoBodyChannel.cc:160-188);
+ * p, q may be NULL, else hold nkets entries. */
+int imsrg_space_cc_channel(const imsrg_space* s, int ch, int* J, int* parity, int* Tz, int* nkets, int* p, int* q);
+
+/* 6j symbol {jj1/2 jj2/2 j3; jj4/2 jj5/2 j6} from the space's table
+ * (ModelSpace::GetCachedSixJ, src/ModelSpace.hh:502-505; arguments doubled for
+ * the half-integers, as there). */
+int imsrg_space_sixj(const imsrg_space* s, int jj1, int jj2, int j3, int jj4, int jj5, int j6, double* out);
+
+/* -------------------------------------------------------------- operators */
+
+/* Device-resident scalar operator (J=0, parity +, Tz=0, particle rank 2),
+ * zero-filled.  hermiticity: +1 hermitian, -1 anti-hermitian.
+ * Replaces Operator(ms, 0, 0, 0, 2) + SetHermitian/SetAntiHermitian
+ * (src/Operator.cc:57-80, src/Operator.hh:45-225). */
+int imsrg_op_create(imsrg_space* s, int hermiticity, imsrg_op** out);
+void imsrg_op_destroy(imsrg_op* op);
+int imsrg_op_hermiticity(const imsrg_op* op, int* h);
+int imsrg_op_set_hermiticity(imsrg_op* op, int h);
+
+/* Host <-> device copies of the whole arena (arena_len doubles). */
+int imsrg_op_upload(imsrg_op* op, const double* host, void* stream);
+int imsrg_op_download(const imsrg_op* op, double* host, void* stream);
+/* Device address of the arena (for callers that manage their own copies). */
+int imsrg_op_device_arena(const imsrg_op* op, double** dptr);
+
+/* Operator::Erase (src/Operator.cc), copy-assignment, operator*= and
+ * operator+=(a * x) (src/Operator.cc:132-210). */
+int imsrg_op_zero(imsrg_op* op, void* stream);
+int imsrg_op_copy(imsrg_op* dst, const imsrg_op* src, void* stream);
+int imsrg_op_scale(imsrg_op* op, double a, void* stream);
+int imsrg_op_axpy(imsrg_op* y, double a, const imsrg_op* x, void* stream);
+
+/* Operator::Norm of a scalar operator (src/Operator.cc:1610-1651,
+ * src/TwoBodyME.cc:703-723); synchronises the stream. */
+int imsrg_op_norm(const imsrg_op* op, double* out, void* stream);
+
+/* Seeded random operator: uniform[-1,1] on symmetry-allowed entries,
+ * (anti)symmetrised by the operator's hermiticity, unit Frobenius norm per
+ * two-body channel block and for the one-body matrix; ZeroBody uniform
+ * (hermitian) or 0.  Generated on the host, then uploaded.  The test fixture
+ * generator of the benchmark; UnitTest::RandomOp (src/UnitTest.cc:25-205) is
+ * the reference's counterpart. */
+int imsrg_op_fill_random(imsrg_op* op, unsigned long long seed, void* stream);
+
+/* ------------------------------------------------------------------ terms */
+/* Each accumulates its part of [X,Y] into Z, like the reference function
+ * named in its comment.  Z must be hermitian or anti-hermitian. */
+
+/* Commutator::comm110ss, src/Commutator.cc:564-581 */
+int imsrg_comm110ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
+/* Commutator::comm220ss, src/Commutator.cc:601-631 */
+int imsrg_comm220ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
+/* Commutator::comm111ss, src/Commutator.cc:644-649 */
+int imsrg_comm111ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
+/* Commutator::comm121ss, src/Commutator.cc:670-728 */
+int imsrg_comm121ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
+/* Commutator::comm122ss, src/Commutator.cc:837-932 */
+int imsrg_comm122ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
+/* Commutator::comm221ss, src/Commutator.cc:760-819 */
+int imsrg_comm221ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
+/* Commutator::comm222_pp_hhss, src/Commutator.cc:1062-1076 */
+int imsrg_comm222_pp_hhss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream);
+/* Commutator::comm222_pp_hh_221ss, src/Commutator.cc:1215-1301 */
+int imsrg_comm222_pp_hh_221ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream);
+/* Commutator::comm222_phss, src/Commutator.cc:1681-1823 */
+int imsrg_comm222_phss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream);
+
+/* Commutator::CommutatorScalarScalar, src/Commutator.cc:280-428 (IMSRG(2)
+ * terms): Z is overwritten with [X,Y] and its hermiticity set from X and Y;
+ * the terms switched on by imsrg_set_term run in the reference's order. */
+int imsrg_commutator_scalar_scalar(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream);
+
+/* Commutator::TurnOnTerm / TurnOffTerm (src/Commutator.cc:77-78) for the
+ * IMSRG(2) names "comm110ss", "comm220ss", "comm111ss", "comm121ss",
+ * "comm122ss", "comm221ss", "comm222_pp_hhss", "comm222_phss". Process-wide. */
+int imsrg_set_term(const char* name, int on);
+int imsrg_get_term(const char* name, int* on);
+
+/* Default precision used by the reference-signature shim (process-wide). */
+int imsrg_set_default_precision(int precision);
+int imsrg_get_default_precision(int* precision);
+
+/* BCH::Standard_BCH_Transform (src/BCH.cc:87-201): OpOut = e^Omega OpIn e^-Omega
+ * by nested commutators, stopping as the reference does (threshold:
+ * BCH::bch_transform_threshold, default 1e-9, src/BCH.cc:8-69; at most 40
+ * nested commutators).  n_nested (may be NULL) receives the number of nested
+ * commutators evaluated.  Synchronises the stream once per nested commutator
+ * for the convergence test. */
+int imsrg_bch_transform(const imsrg_op* OpIn, const imsrg_op* Omega, imsrg_op* OpOut, double threshold,
+                        int precision, int* n_nested, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IMSRG_GB300_H */

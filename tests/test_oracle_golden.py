@@ -1,0 +1,70 @@
+"""The C oracle (CPU restatement of the reference) against the reference's own
+outputs: golden fixtures made by tests/golden/make_golden.py from the
+reference compiled from its sources."""
+import numpy as np
+import pytest
+
+from helpers import CASES, TERMS, load_golden, rel_errors
+from oracle import Oracle
+
+
+@pytest.mark.parametrize("emax", [2, 3])
+@pytest.mark.parametrize("use_blas", [True, False])
+def test_oracle_terms_match_reference(emax, use_blas):
+    g = load_golden(emax)
+    o = Oracle(emax, use_blas=use_blas)
+    ops = {"X": g["X"], "Y": g["Y"], "W": g["W"]}
+    for cs, (a, b, ha, hb) in CASES.items():
+        if cs + "_full" not in g:
+            continue
+        for t in TERMS:
+            Z = o.zeros()
+            o.term(t, ops[a], ops[b], Z, ha, hb)
+            ref = g[cs + "_" + t]
+            assert np.abs(Z - ref).max() <= 1e-13 * max(1.0, np.abs(ref).max()), (cs, t)
+        Z = o.commutator(ops[a], ops[b], ha, hb)
+        assert max(rel_errors(o.ms, Z, g[cs + "_full"])) < 1e-13, cs
+
+
+@pytest.mark.parametrize("emax", [2, 3])
+def test_oracle_bch_matches_reference(emax):
+    g = load_golden(emax)
+    o = Oracle(emax)
+    X, Y = g["X"], g["Y"]
+    out, it = o.bch_transform(X, 1, Y * (0.25 / o.norm(Y)), -1)
+    assert 1 <= it <= 40
+    assert np.abs(out - g["bch"]).max() < 1e-13
+
+
+@pytest.mark.parametrize("emax", [2, 3])
+def test_oracle_norm_matches_reference(emax):
+    g = load_golden(emax)
+    o = Oracle(emax)
+    for k, name in enumerate("XYW"):
+        assert abs(o.norm(g[name]) - g["norms"][k]) < 1e-12 * g["norms"][k]
+
+
+def test_term_switches():
+    g = load_golden(2)
+    o = Oracle(2)
+    X, Y = g["X"], g["Y"]
+    o.set_term("comm222_phss", False)
+    Z = o.commutator(X, Y, 1, -1)
+    o.set_term("comm222_phss", True)
+    ref = g["xy_full"] - g["xy_comm222_phss"]
+    assert np.abs(Z - ref).max() < 1e-13
+
+
+def test_planted_mistake_is_caught():
+    """A wrong phase planted in the oracle's input must be visible at the
+    tolerance the parity tests use (the test is only as strong as this)."""
+    g = load_golden(2)
+    o = Oracle(2)
+    X = g["X"].copy()
+    ms = o.ms
+    ch = next(c for c in range(ms.nch) if len(ms.channels[c][3]) > 3)
+    blk = ms.block(X, ch)
+    blk[1, 2] *= -1
+    blk[2, 1] *= -1
+    Z = o.commutator(X, g["Y"], 1, -1)
+    assert max(rel_errors(ms, Z, g["xy_full"])) > 1e-6
