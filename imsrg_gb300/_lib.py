@@ -71,6 +71,11 @@ SIGNATURES = {
     "imsrg_set_default_precision": (I, [I]),
     "imsrg_get_default_precision": (I, [IP]),
     "imsrg_bch_transform": (I, [P, P, P, D, I, IP, P]),
+    "imsrg_profiler_enable": (I, [I]),
+    "imsrg_profiler_reset": (I, []),
+    "imsrg_profiler_get": (I, [ctypes.c_char_p, DP, LLP]),
+    "imsrg_profiler_names": (I, [ctypes.c_char_p, I]),
+    "imsrg_kernel_launches": (LL, []),
 }
 
 

@@ -15,6 +15,7 @@
 
 #include "../../include/imsrg_gb300.h"
 #include "kernels.cuh"
+#include "prof.hpp"
 #include "space.hpp"
 
 using namespace imsrg;
@@ -297,6 +298,7 @@ int do_111_110(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, bool do111, bo
   // comm110ss returns early when X and Y have the same hermiticity (src/Commutator.cc:567-570)
   if (do110 && X->herm == Y->herm) do110 = false;
   if (!do111 && !do110) return IMSRG_OK;
+  ProfScope ps(do111 ? (do110 ? "comm111ss+comm110ss" : "comm111ss") : "comm110ss", st);
   CUDA_TRY(launch_comm111_110(*X->sp->s, X->d, Y->d, Z->d, do111, do110, st));
   return IMSRG_OK;
 }
@@ -304,12 +306,14 @@ int do_111_110(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, bool do111, bo
 int do_220(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
 {
   if (X->herm == Y->herm) return IMSRG_OK;  // src/Commutator.cc:606-609
+  ProfScope ps("comm220ss", st);
   CUDA_TRY(launch_comm220(*X->sp->s, X->d, Y->d, Z->d, X->herm, st));
   return IMSRG_OK;
 }
 
 int do_121(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
 {
+  ProfScope ps("comm121ss", st);
   CUDA_TRY(launch_comm121(*X->sp->s, X->sp->d_holes, X->d, Y->d, Z->d, Z->herm, st));
   return IMSRG_OK;
 }
@@ -319,12 +323,14 @@ int do_122(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
   imsrg_space* sp = X->sp;
   int rc = ensure_scratch(sp, false, true);
   if (rc) return rc;
+  ProfScope ps("comm122ss", st);
   CUDA_TRY(launch_comm122(*sp->s, X->d, Y->d, Z->d, sp->d_w2, Z->herm, sp->d_sym122, sp->n_sym122, st));
   return IMSRG_OK;
 }
 
 int do_221_1b(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
 {
+  ProfScope ps("comm221ss", st);
   CUDA_TRY(launch_comm221_1b(*X->sp->s, X->d, Y->d, Z->d, X->herm, Z->herm, st));
   return IMSRG_OK;
 }
@@ -356,11 +362,12 @@ int do_ladder(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaS
 {
   imsrg_space* sp = X->sp;
   Space& s = *sp->s;
+  ProfScope ps("comm222_pp_hhss", st);
   if (prec == IMSRG_PREC_SPLIT) {
     int rc = ensure_split(sp);
     if (rc) return rc;
     CUDA_TRY(launch_symgemm_split(sp->split_ladder, X->d, Y->d, Y->d, Z->d, s.work.kidx, s.work.kweight,
-                                  s.work.phase_tab, sp->d_status, st));
+                                  s.work.phase_tab, sp->d_status, Z->herm, (double)Y->herm, st));
     return IMSRG_OK;
   }
   if (prec != IMSRG_PREC_FP64) return fail(IMSRG_ERR_ARG, "unknown precision");
@@ -375,19 +382,23 @@ int do_ph(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStrea
   Space& s = *sp->s;
   int rc = ensure_scratch(sp, true, false);
   if (rc) return rc;
+  ProfScope ps("comm222_phss", st);
+  int slot = prof_begin("Build Z_bar", st);
   CUDA_TRY(launch_pandya_fwd(s, X->d, Y->d, Y->herm, sp->d_xb, sp->d_yt, sp->d_yf, sp->d_pfwd, sp->n_pfwd, st));
   for (auto& zr : sp->zbar_zero) CUDA_TRY(cudaMemsetAsync(sp->d_zb + zr.first, 0, zr.second * sizeof(double), st));
   if (prec == IMSRG_PREC_SPLIT) {
     rc = ensure_split(sp);
     if (rc) return rc;
     CUDA_TRY(launch_symgemm_split(sp->split_zbar, sp->d_xb, sp->d_yt, sp->d_yf, sp->d_zb, s.work.kidx,
-                                  s.work.kweight, s.work.phase_tab, sp->d_status, st));
+                                  s.work.kweight, s.work.phase_tab, sp->d_status, Z->herm, 1.0, st));
   } else if (prec == IMSRG_PREC_FP64) {
     CUDA_TRY(launch_symgemm_fp64(sp->d_zbar_jobs, sp->d_zbar_pairs, sp->n_zbar_pairs, sp->d_xb, sp->d_yt, sp->d_yf,
                                  sp->d_zb, s.work.kidx, s.work.kweight, s.work.phase_tab, Z->herm, 1.0, st));
   } else {
     return fail(IMSRG_ERR_ARG, "unknown precision");
   }
+  prof_end(slot, st);
+  ProfScope pinv("InversePandyaTransformation", st);
   CUDA_TRY(launch_pandya_inv(s, sp->d_zb, Z->d, Z->herm, sp->d_pinv, sp->n_pinv, st));
   return IMSRG_OK;
 }
@@ -406,6 +417,7 @@ int commutator_impl(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec,
     std::lock_guard<std::mutex> g(g_mu);
     std::copy(g_term_on, g_term_on + NTERMS, on);
   }
+  ProfScope ps("CommutatorScalarScalar", st);
   CUDA_TRY(cudaMemsetAsync(Z->d, 0, X->sp->s->arena * sizeof(double), st));
   if ((rc = do_111_110(X, Y, Z, on[T111], on[T110], st))) return rc;
   if (on[T220] && (rc = do_220(X, Y, Z, st))) return rc;

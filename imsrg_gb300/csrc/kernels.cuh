@@ -48,7 +48,7 @@ struct SplitPlan;
 SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs, int family);
 void split_plan_destroy(SplitPlan* p);
 cudaError_t launch_symgemm_split(SplitPlan* p, const double* A, const double* B0, const double* B1, double* O,
-                                 const int* kidx, const double* kw, const int* phase, int* dev_status,
-                                 cudaStream_t st);
+                                 const int* kidx, const double* kw, const int* phase, int* dev_status, int gsign,
+                                 double gbscale, cudaStream_t st);
 
 }  // namespace imsrg

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include "kernels.cuh"
+#include "prof.hpp"
 
 namespace imsrg {
 
@@ -159,6 +160,7 @@ cudaError_t launch_symgemm_fp64(const GemmJobDev* jobs, const int* pairs, int np
     attr = true;
   }
   k_symgemm_fp64<<<npairs, 256, sm, st>>>(jobs, pairs, npairs, A, B0, B1, O, kidx, kw, phase, gsign, gbscale);
+  count_launch();
   return cudaGetLastError();
 }
 

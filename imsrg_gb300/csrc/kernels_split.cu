@@ -1,28 +1,853 @@
-// Split-precision symmetrised channel products (placeholder until the tcgen05
-// kernel lands): reports "not supported".
+// Split-precision symmetrised channel products on the Blackwell tensor cores.
+//
+// Computes, for every job (a channel block), the same quantity as
+// k_symgemm_fp64 (kernels_gemm.cu):
+//     Out (+)= P + s phi_i phi_j P^T,   P = A B^T,   A, B: m x K FP64
+// as an Ozaki-style sum of exact BF16 digit products:
+//
+//  * Digits.  Each row i gets one exponent a_i for its A row and b_i = a_i + c
+//    for its B row (c is one per job), chosen so both rows fit below the
+//    exponent.  Every element is rounded to an integer q = v * 2^(beta*S - e)
+//    (|q| <= 2^(beta*S)) and split into S balanced base-2^beta digits
+//    (|d_1| <= 2^beta, |d_s| <= 2^(beta-1)), all exact in BF16.  Only integer
+//    instructions are used (FP64 runs at 1/57 of the FP32 rate on this part).
+//  * Symmetrisation folded into K.  With the shared-exponent choice both
+//    A_i.B_j and B_i.A_j carry the scale 2^(a_i + a_j + c), so
+//        Out(i,j) = sum_t [A(i,t) | s phi_i B(i,t)] . [B(j,t) | phi_j A(j,t)]
+//    is one product with K doubled; only tiles of the upper triangle are
+//    computed and each is written together with its mirror (no transpose
+//    pass, no extra flops over P alone).
+//  * Products.  The digit products with s + t <= S + 1 are issued as
+//    tcgen05.mma kind::f16 (BF16 in, FP32 accumulate in tensor memory), one
+//    TMEM accumulator per weight group T = s + t.  beta is chosen from K so
+//    that the FP32 sums of the leading groups stay exact integers.
+//  * Recombination.  The epilogue reads the S group sums (tcgen05.ld), merges
+//    them exactly as int64, converts once to FP64 and applies the power-of-two
+//    scale by exponent arithmetic.
+//
+// Kernel layout (persistent, one CTA per SM, 192 threads):
+//   warp 0: TMA producer (cp.async.bulk.tensor, 64B swizzle, mbarrier pipeline)
+//   warp 1: TMEM allocator + single-thread MMA issuer
+//   warps 2-5: epilogue (TMEM lanes 0-127)
+// Every mbarrier wait is bounded; a timeout sets the status word and the CTA
+// drains and exits.
+#include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <vector>
+
 #include "kernels.cuh"
+#include "prof.hpp"
 
 namespace imsrg {
 
-struct SplitPlan {
-  int family = 0;
+namespace {
+
+constexpr int KB = 32;          // K elements (bf16) per pipeline stage: one 64-byte swizzle row
+constexpr int TILE_M = 128;     // rows per tile (UMMA M)
+constexpr int TILE_N = 64;      // columns per tile (UMMA N)
+constexpr int MAX_S = 7;
+constexpr int EPI_COLS = 8;     // TMEM columns read per tcgen05.ld
+constexpr int THREADS = 192;
+constexpr unsigned WAIT_LIMIT = 1u << 26;  // bounded spin (with nanosleep backoff: seconds)
+constexpr int EXP_NONE = -100000;          // exponent of an all-zero row
+
+struct SplitJob {
+  long long a_off, b_off, out_off;
+  int m, K, lda, ldb, ldo;
+  int kidx_off, w_off, phase_off;
+  int bsel, sign, accumulate;
+  double bscale;
+  // slice layout
+  long long row_base;  // first row of this job in the slice arrays (slice s at row_base + s * m_pad)
+  long long exp_base;  // first row of this job in the exponent arrays
+  int m_pad, K_pad, nkb;
 };
 
-SplitPlan* split_plan_create(const Space&, const std::vector<GemmJobDev>&, int family)
+struct SplitTile {
+  int job, I, J, diag;
+};
+
+}  // namespace
+
+struct SplitPlan {
+  int family = 0;
+  int S = 6, beta = 6;
+  int K_stride = 0;
+  long long total_rows = 0, total_exp_rows = 0;
+  int njobs = 0, ntiles = 0;
+  std::vector<SplitJob> jobs;
+  SplitJob* d_jobs = nullptr;
+  SplitTile* d_tiles = nullptr;
+  __nv_bfloat16* arr[4] = {nullptr, nullptr, nullptr, nullptr};  // alpha, beta, gamma, delta
+  int* d_rexpA = nullptr;   // raw row exponent of A rows
+  int* d_rexpB = nullptr;
+  int* d_jobmax = nullptr;  // [2 * njobs]: max exponent of A, of B
+  int* d_flags = nullptr;   // [2 * njobs]: gamma used, delta used (set per launch)
+  CUtensorMap maps[4];
+  int grid = 0;
+  size_t smem = 0;
+  int nstages = 0;
+};
+
+// ----------------------------------------------------------------- device
+namespace {
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned a, unsigned count)
 {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned a, unsigned bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned a)
+{
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(unsigned a, unsigned parity)
+{
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait: false on timeout
+__device__ __forceinline__ bool mbar_wait(unsigned a, unsigned parity)
+{
+  for (unsigned it = 0; it < WAIT_LIMIT; ++it) {
+    if (mbar_try(a, parity)) return true;
+    if (it > 64) __nanosleep(it > 4096 ? 256 : 32);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap* map, int x, int y, unsigned bar)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"((unsigned long long)map), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_mma(unsigned d_tmem, unsigned long long adesc, unsigned long long bdesc,
+                                       unsigned idesc, unsigned accumulate)
+{
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(unsigned bar)
+{
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// UMMA shared-memory descriptor: K-major operand, 64-byte swizzle
+// (8 rows x 64 bytes per swizzle atom, 512 bytes between 8-row groups).
+__device__ __forceinline__ unsigned long long sdesc_sw64(unsigned addr)
+{
+  unsigned long long d = 0;
+  d |= (unsigned long long)((addr >> 4) & 0x3FFF);
+  d |= (unsigned long long)1 << 16;             // leading byte offset (unused for swizzled K-major)
+  d |= (unsigned long long)(512 >> 4) << 32;    // stride byte offset
+  d |= (unsigned long long)1 << 46;             // descriptor version (sm_100 family)
+  d |= (unsigned long long)4 << 61;             // layout: 64-byte swizzle
+  return d;
+}
+
+// instruction descriptor, kind::f16: BF16 x BF16 -> F32, both K-major
+__host__ __device__ constexpr unsigned idesc_bf16(int M, int N)
+{
+  return (1u << 4)                   // D format F32
+         | (1u << 7)                 // A format BF16
+         | (1u << 10)                // B format BF16
+         | ((unsigned)(N >> 3) << 17)  // N / 8
+         | ((unsigned)(M >> 4) << 24); // M / 16
+}
+
+__device__ __forceinline__ void tmem_ld8(unsigned taddr, unsigned (&r)[8])
+{
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ void set_status(int* st, int code)
+{
+  if (st) atomicCAS(st, 0, code);
+}
+
+// biased exponent field of a double (0 for zero / subnormal)
+__device__ __forceinline__ int dexp(double v) { return (int)((__double_as_longlong(v) >> 52) & 0x7FF); }
+
+// operand value with the launch / job / column scale of B
+__device__ __forceinline__ double scaled(double v, double sc)
+{
+  if (sc == 1.0) return v;
+  if (sc == -1.0) return -v;
+  return v * sc;
+}
+
+// q = round(v * 2^(P - e)) for |v| < 2^e, P = beta*S <= 42; integer only
+__device__ __forceinline__ long long to_fixed(double v, int e, int P)
+{
+  long long bits = __double_as_longlong(v);
+  int E = (int)((bits >> 52) & 0x7FF);
+  if (E == 0) return 0;
+  long long M = (bits & 0xFFFFFFFFFFFFFll) | 0x10000000000000ll;
+  int r = 1075 - E - P + e;  // right shift, >= 11 since |v| < 2^e
+  if (r >= 64 || r <= 0) return 0;  // r >= 11 whenever |v| < 2^e
+  long long q = (M + (1ll << (r - 1))) >> r;
+  return bits < 0 ? -q : q;
+}
+
+// ------------------------------------------------------------ exponents
+// raw row exponents (max biased exponent over the row) of A and B, and the
+// per-job maxima.  One thread per (job, row).
+__global__ void k_split_rowexp(const SplitJob* __restrict__ jobs, int njobs, const double* __restrict__ Abase,
+                               const double* __restrict__ B0, const double* __restrict__ B1,
+                               const int* __restrict__ kidx, const double* __restrict__ kw, double gbscale,
+                               int* __restrict__ rexpA, int* __restrict__ rexpB, int* __restrict__ jobmax)
+{
+  int job = blockIdx.y;
+  if (job >= njobs) return;
+  const SplitJob jb = jobs[job];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= jb.m_pad) return;
+  int ea = 0, eb = 0;
+  if (i < jb.m) {
+    const double* A = Abase + jb.a_off;
+    const double* B = (jb.bsel ? B1 : B0) + jb.b_off;
+    const int* kx = jb.kidx_off >= 0 ? kidx + jb.kidx_off : nullptr;
+    const double* w = jb.w_off >= 0 ? kw + jb.w_off : nullptr;
+    double sc0 = jb.bscale * gbscale;
+    for (int t = 0; t < jb.K; ++t) {
+      int col = kx ? __ldg(kx + t) : t;
+      ea = max(ea, dexp(A[(long long)col * jb.lda + i]));
+      double sc = w ? sc0 * __ldg(w + t) : sc0;
+      eb = max(eb, dexp(scaled(B[(long long)col * jb.ldb + i], sc)));
+    }
+  }
+  rexpA[jb.exp_base + i] = ea;
+  rexpB[jb.exp_base + i] = eb;
+  // warp-level max then one atomic per warp
+  int wa = ea, wb = eb;
+  for (int o = 16; o > 0; o >>= 1) {
+    wa = max(wa, __shfl_xor_sync(0xffffffffu, wa, o));
+    wb = max(wb, __shfl_xor_sync(0xffffffffu, wb, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(jobmax + 2 * job, wa);
+    atomicMax(jobmax + 2 * job + 1, wb);
+  }
+}
+
+// exponent of row i (A side) from the raw exponents: a_i = max(eA, eB - c)
+__device__ __forceinline__ int row_exp(int eA, int eB, int c)
+{
+  int a = eA > 0 ? eA - 1022 : EXP_NONE;
+  int b = eB > 0 ? eB - 1022 - c : EXP_NONE;
+  return max(a, b);
+}
+
+__device__ __forceinline__ int job_c(const int* jobmax, int job)
+{
+  int ma = jobmax[2 * job], mb = jobmax[2 * job + 1];
+  if (ma == 0 || mb == 0) return 0;
+  return mb - ma;
+}
+
+// ---------------------------------------------------------------- digits
+// One block per (job, 32-row group, 64-column group): digits of A and B rows
+// into shared memory, then coalesced 16-byte stores of the four slice arrays
+//   alpha = A digits, beta = B digits, gamma = s phi_i B digits, delta = phi_i A digits
+// (gamma / delta written only when they differ from beta / alpha).
+template <int S>
+__global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict__ jobs, int njobs,
+                                                     const double* __restrict__ Abase,
+                                                     const double* __restrict__ B0, const double* __restrict__ B1,
+                                                     const int* __restrict__ kidx, const double* __restrict__ kw,
+                                                     const int* __restrict__ phase, double gbscale, int gsign,
+                                                     const int* __restrict__ rexpA, const int* __restrict__ rexpB,
+                                                     const int* __restrict__ jobmax, int beta, int K_stride,
+                                                     __nv_bfloat16* __restrict__ alpha, __nv_bfloat16* __restrict__ bet,
+                                                     __nv_bfloat16* __restrict__ gam, __nv_bfloat16* __restrict__ del)
+{
+  __shared__ unsigned short dA[S][32][KB + 8];
+  __shared__ unsigned short dB[S][32][KB + 8];
+  __shared__ int rowA[32], rowB[32], rowsg[32], rowph[32];
+  int job = blockIdx.z;
+  if (job >= njobs) return;
+  const SplitJob jb = jobs[job];
+  int r0 = blockIdx.y * 32;
+  int t0 = blockIdx.x * KB;
+  if (r0 >= jb.m_pad || t0 >= jb.K_pad) return;
+  int c = job_c(jobmax, job);
+  int sign = jb.sign != 0 ? jb.sign : gsign;
+  const int* ph = jb.phase_off >= 0 ? phase + jb.phase_off : nullptr;
+  if (threadIdx.x < 32) {
+    int i = r0 + threadIdx.x;
+    int a = row_exp(rexpA[jb.exp_base + i], rexpB[jb.exp_base + i], c);
+    rowA[threadIdx.x] = a;
+    rowB[threadIdx.x] = a + c;
+    int p = (ph && i < jb.m) ? ph[i] : 1;
+    rowph[threadIdx.x] = p;
+    rowsg[threadIdx.x] = sign * p;
+  }
+  __syncthreads();
+  const double* A = Abase + jb.a_off;
+  const double* B = (jb.bsel ? B1 : B0) + jb.b_off;
+  const int* kx = jb.kidx_off >= 0 ? kidx + jb.kidx_off : nullptr;
+  const double* w = jb.w_off >= 0 ? kw + jb.w_off : nullptr;
+  const int P = beta * S;
+  const long long half = 1ll << (beta - 1), mask = (1ll << beta) - 1;
+  double sc0 = jb.bscale * gbscale;
+  // element (r, tt): thread layout r fastest (coalesced column reads)
+  for (int e = threadIdx.x; e < 32 * KB; e += 256) {
+    int r = e & 31, tt = e >> 5;
+    int i = r0 + r, t = t0 + tt;
+    long long qa = 0, qb = 0;
+    if (i < jb.m && t < jb.K) {
+      int col = kx ? __ldg(kx + t) : t;
+      double sc = w ? sc0 * __ldg(w + t) : sc0;
+      qa = to_fixed(A[(long long)col * jb.lda + i], rowA[r], P);
+      qb = to_fixed(scaled(B[(long long)col * jb.ldb + i], sc), rowB[r], P);
+    }
+#pragma unroll
+    for (int s = S - 1; s >= 1; --s) {
+      long long da = ((qa + half) & mask) - half;
+      long long db = ((qb + half) & mask) - half;
+      qa = (qa - da) >> beta;
+      qb = (qb - db) >> beta;
+      // small integer -> bf16 bits (exact): 1.5*2^23 magic
+      dA[s][r][tt] = (unsigned short)(__float_as_uint(__int_as_float(0x4B400000 + (int)da) - 12582912.0f) >> 16);
+      dB[s][r][tt] = (unsigned short)(__float_as_uint(__int_as_float(0x4B400000 + (int)db) - 12582912.0f) >> 16);
+    }
+    dA[0][r][tt] = (unsigned short)(__float_as_uint(__int_as_float(0x4B400000 + (int)qa) - 12582912.0f) >> 16);
+    dB[0][r][tt] = (unsigned short)(__float_as_uint(__int_as_float(0x4B400000 + (int)qb) - 12582912.0f) >> 16);
+  }
+  __syncthreads();
+  bool need_g = false, need_d = false;
+  for (int r = 0; r < 32; ++r) {
+    need_g |= rowsg[r] != 1;
+    need_d |= rowph[r] != 1;
+  }
+  // stores: each thread one 16-byte vector (8 digits) of one row of one slice
+  for (int e = threadIdx.x; e < S * 32 * (KB / 8); e += 256) {
+    int v = e % (KB / 8), r = (e / (KB / 8)) & 31, s = e / (32 * (KB / 8));
+    long long row = jb.row_base + (long long)s * jb.m_pad + r0 + r;
+    long long o = row * K_stride + t0 + v * 8;
+    uint4 va, vb;
+    unsigned short* pa = (unsigned short*)&va;
+    unsigned short* pb = (unsigned short*)&vb;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      pa[k] = dA[s][r][v * 8 + k];
+      pb[k] = dB[s][r][v * 8 + k];
+    }
+    *(uint4*)(alpha + o) = va;
+    *(uint4*)(bet + o) = vb;
+    if (need_g) {
+      uint4 vg = vb;
+      if (rowsg[r] < 0) {
+        vg.x ^= 0x80008000u; vg.y ^= 0x80008000u; vg.z ^= 0x80008000u; vg.w ^= 0x80008000u;
+      }
+      *(uint4*)(gam + o) = vg;
+    }
+    if (need_d) {
+      uint4 vd = va;
+      if (rowph[r] < 0) {
+        vd.x ^= 0x80008000u; vd.y ^= 0x80008000u; vd.z ^= 0x80008000u; vd.w ^= 0x80008000u;
+      }
+      *(uint4*)(del + o) = vd;
+    }
+  }
+}
+
+// --------------------------------------------------------------- the GEMM
+struct GemmArgs {
+  const SplitJob* jobs;
+  const SplitTile* tiles;
+  int ntiles;
+  const int* rexpA;
+  const int* rexpB;
+  const int* jobmax;
+  const int* flags;   // [2*job]: gamma used, delta used
+  const int* phase;
+  double* out;
+  int* status;
+  int S, beta, nstages, gsign;
+};
+
+template <int S>
+__global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant__ CUtensorMap mAlpha,
+                                                          const __grid_constant__ CUtensorMap mBeta,
+                                                          const __grid_constant__ CUtensorMap mGamma,
+                                                          const __grid_constant__ CUtensorMap mDelta, GemmArgs g)
+{
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-byte aligned base
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int NST = g.nstages;
+  const unsigned A_SLICE = TILE_M * KB * 2;  // 8 KB
+  const unsigned B_SLICE = TILE_N * KB * 2;  // 4 KB
+  const unsigned STAGE = S * (A_SLICE + B_SLICE);
+  unsigned long long* bars = (unsigned long long*)(smem + NST * STAGE);
+  // bars: full[NST], empty[NST], acc_full, acc_empty ; then tmem slot
+  unsigned* tmem_slot = (unsigned*)(bars + 2 * NST + 2);
+  __shared__ int s_err_;
+  volatile int& s_err = s_err_;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned sbase = smem_u32(smem);
+  const unsigned bar0 = smem_u32(bars);
+  auto full_bar = [&](int s) { return bar0 + 8u * s; };
+  auto empty_bar = [&](int s) { return bar0 + 8u * (NST + s); };
+  const unsigned acc_full = bar0 + 8u * (2 * NST);
+  const unsigned acc_empty = bar0 + 8u * (2 * NST + 1);
+
+  if (threadIdx.x == 0) {
+    s_err = 0;
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(full_bar(s), 1);
+      mbar_init(empty_bar(s), 1);
+    }
+    mbar_init(acc_full, 1);
+    mbar_init(acc_empty, 128);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const unsigned tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------------------------ TMA producer
+    if (lane == 0) {
+      int it = 0;
+      for (int tix = blockIdx.x; tix < g.ntiles && !s_err; tix += gridDim.x) {
+        const SplitTile tl = g.tiles[tix];
+        const SplitJob& jb = g.jobs[tl.job];
+        const bool useG = g.flags[2 * tl.job] != 0, useD = g.flags[2 * tl.job + 1] != 0;
+        const CUtensorMap* mA2 = useG ? &mGamma : &mBeta;
+        const CUtensorMap* mB2 = useD ? &mDelta : &mAlpha;
+        for (int kb = 0; kb < 2 * jb.nkb; ++kb, ++it) {
+          int st = it % NST;
+          unsigned ph = (unsigned)((it / NST) & 1);
+          if (!mbar_wait(empty_bar(st), ph ^ 1u)) {
+            set_status(g.status, 101);
+            s_err = 1;
+            break;
+          }
+          mbar_expect_tx(full_bar(st), STAGE);
+          const bool second = kb >= jb.nkb;
+          const int k = (second ? kb - jb.nkb : kb) * KB;
+          const CUtensorMap* ma = second ? mA2 : &mAlpha;
+          const CUtensorMap* mb = second ? mB2 : &mBeta;
+          unsigned sA = sbase + st * STAGE;
+          unsigned sB = sA + S * A_SLICE;
+          for (int s = 0; s < S; ++s) {
+            int rowA = (int)(jb.row_base + (long long)s * jb.m_pad + tl.I * TILE_M);
+            int rowB = (int)(jb.row_base + (long long)s * jb.m_pad + tl.J * TILE_N);
+            tma_load_2d(sA + s * A_SLICE, ma, k, rowA, full_bar(st));
+            tma_load_2d(sA + s * A_SLICE + TILE_N * KB * 2, ma, k, rowA + TILE_N, full_bar(st));
+            tma_load_2d(sB + s * B_SLICE, mb, k, rowB, full_bar(st));
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      const unsigned idesc = idesc_bf16(TILE_M, TILE_N);
+      int it = 0, tc = 0;
+      for (int tix = blockIdx.x; tix < g.ntiles && !s_err; tix += gridDim.x, ++tc) {
+        const SplitJob& jb = g.jobs[g.tiles[tix].job];
+        if (!mbar_wait(acc_empty, (unsigned)((tc & 1) ^ 1))) {
+          set_status(g.status, 102);
+          s_err = 1;
+          break;
+        }
+        tc_fence_after();
+        unsigned started = 0;  // groups already written in this tile
+        bool ok = true;
+        for (int kb = 0; kb < 2 * jb.nkb; ++kb, ++it) {
+          int st = it % NST;
+          unsigned ph = (unsigned)((it / NST) & 1);
+          if (!mbar_wait(full_bar(st), ph)) {
+            set_status(g.status, 103);
+            s_err = 1;
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          unsigned sA = sbase + st * STAGE;
+          unsigned sB = sA + S * A_SLICE;
+#pragma unroll
+          for (int sub = 0; sub < KB / 16; ++sub) {
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+              unsigned long long ad = sdesc_sw64(sA + s * A_SLICE + sub * 32);
+#pragma unroll
+              for (int t = 0; t < S - s; ++t) {
+                int grp = s + t;  // weight group T = (s+1) + (t+1) - 2
+                unsigned long long bd = sdesc_sw64(sB + t * B_SLICE + sub * 32);
+                unsigned acc = (started >> grp) & 1u;
+                tc_mma(tmem + grp * TILE_N, ad, bd, idesc, acc);
+                started |= 1u << grp;
+              }
+            }
+          }
+          tc_commit(empty_bar(st));
+        }
+        if (!ok) break;
+        tc_commit(acc_full);
+      }
+    }
+  } else {
+    // ------------------------------------------------ epilogue (warps 2..5)
+    const int q = warp & 3;  // TMEM lane quarter of this warp
+    int tc = 0;
+    for (int tix = blockIdx.x; tix < g.ntiles; tix += gridDim.x, ++tc) {
+      const SplitTile tl = g.tiles[tix];
+      const SplitJob& jb = g.jobs[tl.job];
+      if (!mbar_wait(acc_full, (unsigned)(tc & 1))) {
+        set_status(g.status, 104);
+        s_err = 1;
+        break;
+      }
+      tc_fence_after();
+      const int c = job_c(g.jobmax, tl.job);
+      const int sign = jb.sign != 0 ? jb.sign : g.gsign;
+      const int* ph = jb.phase_off >= 0 ? g.phase + jb.phase_off : nullptr;
+      const int i = tl.I * TILE_M + q * 32 + lane;
+      const bool rowok = i < jb.m;
+      const int ai = rowok ? row_exp(g.rexpA[jb.exp_base + i], g.rexpB[jb.exp_base + i], c) : EXP_NONE;
+      const int phi_i = (ph && rowok) ? ph[i] : 1;
+      double* O = g.out + jb.out_off;
+      for (int c0 = 0; c0 < TILE_N; c0 += EPI_COLS) {
+        unsigned r[MAX_S][EPI_COLS];
+#pragma unroll
+        for (int gidx = 0; gidx < S; ++gidx)
+          tmem_ld8(tmem + ((unsigned)(q * 32) << 16) + (unsigned)(gidx * TILE_N + c0), r[gidx]);
+        tmem_wait_ld();
+#pragma unroll
+        for (int cc = 0; cc < EPI_COLS; ++cc) {
+          const int j = tl.J * TILE_N + c0 + cc;
+          if (!rowok || j >= jb.m) continue;
+          if (tl.diag && i > j) continue;
+          long long I64 = 0;
+#pragma unroll
+          for (int gidx = 0; gidx < S; ++gidx)
+            I64 += (long long)__float2ll_rn(__uint_as_float(r[gidx][cc])) * (1ll << (g.beta * (S - 1 - gidx)));
+          double v = 0.0;
+          if (I64 != 0) {
+            const int aj = row_exp(g.rexpA[jb.exp_base + j], g.rexpB[jb.exp_base + j], c);
+            const int X = ai + aj + c - g.beta * (S + 1);
+            double d = __ll2double_rn(I64);
+            long long bits = __double_as_longlong(d);
+            int e = (int)((bits >> 52) & 0x7FF) + X;
+            if (e > 0 && e < 2047) v = __longlong_as_double((bits & ~(0x7FFll << 52)) | ((long long)e << 52));
+          }
+          long long o = (long long)j * jb.ldo + i;
+          O[o] = jb.accumulate ? O[o] + v : v;
+          if (i != j) {
+            const int phi_j = ph ? ph[j] : 1;
+            double mv = (sign * phi_i * phi_j) < 0 ? -v : v;
+            long long o2 = (long long)i * jb.ldo + j;
+            O[o2] = jb.accumulate ? O[o2] + mv : mv;
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(acc_empty);
+    }
+  }
+  // drain: wait (bounded) for the last MMA commit of this CTA before freeing TMEM
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+  }
+}
+
+template <int S>
+size_t gemm_smem_bytes(int nstages)
+{
+  size_t stage = (size_t)S * (TILE_M + TILE_N) * KB * 2;
+  return 1024 + nstages * stage + (2 * nstages + 2) * 8 + 16;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static PFN_encodeTiled get_encode()
+{
+  static PFN_encodeTiled fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !p)
+      throw std::runtime_error("cuTensorMapEncodeTiled unavailable");
+    fn = (PFN_encodeTiled)p;
+  }
+  return fn;
+}
+
+static void encode_map(CUtensorMap* m, void* base, long long rows, int K_stride, int box_rows)
+{
+  cuuint64_t dims[2] = {(cuuint64_t)K_stride, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)K_stride * 2};
+  cuuint32_t box[2] = {(cuuint32_t)KB, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = get_encode()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed");
+}
+
+// Choose the digit width: largest beta whose leading weight groups (T <= 5)
+// sum exactly in FP32 for a reduction of length 2K, then S for >= 36 bits.
+static void choose_digits(int Kmax, int& beta, int& S)
+{
+  long long K2 = 2ll * std::max(1, Kmax);
+  for (beta = 7; beta >= 3; --beta) {
+    long long d1 = 1ll << beta, dl = 1ll << (beta - 1);
+    bool ok = true;
+    for (int T = 2; T <= 5; ++T) {
+      long long b = 0;
+      for (int s = 1; s < T; ++s) {
+        int t = T - s;
+        b += (s == 1 ? d1 : dl) * (t == 1 ? d1 : dl);
+      }
+      if (b * K2 > (1ll << 24)) ok = false;
+    }
+    if (ok) break;
+  }
+  S = (36 + beta - 1) / beta;
+  if (S > MAX_S) S = MAX_S;
+}
+
+SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs_in, int family)
+{
+  (void)s;
   SplitPlan* p = new SplitPlan();
   p->family = family;
+  int Kmax = 1;
+  for (const GemmJobDev& j : jobs_in) Kmax = std::max(Kmax, j.K);
+  choose_digits(Kmax, p->beta, p->S);
+  long long row = 0, erow = 0;
+  int kstride = KB;
+  std::vector<SplitTile> tiles;
+  std::vector<int> order(jobs_in.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return jobs_in[a].m > jobs_in[b].m; });
+  for (const GemmJobDev& j : jobs_in) {
+    SplitJob sj{};
+    sj.a_off = j.a_off;
+    sj.b_off = j.b_off;
+    sj.out_off = j.out_off;
+    sj.m = j.m;
+    sj.K = j.K;
+    sj.lda = j.lda;
+    sj.ldb = j.ldb;
+    sj.ldo = j.ldo;
+    sj.kidx_off = j.kidx_off;
+    sj.w_off = j.w_off;
+    sj.phase_off = j.phase_off;
+    sj.bsel = j.bsel;
+    sj.sign = j.sign;
+    sj.accumulate = j.accumulate;
+    sj.bscale = j.bscale;
+    sj.m_pad = (j.m + TILE_M - 1) / TILE_M * TILE_M;
+    sj.K_pad = std::max(KB, (j.K + KB - 1) / KB * KB);
+    sj.nkb = sj.K_pad / KB;
+    sj.row_base = row;
+    sj.exp_base = erow;
+    row += (long long)p->S * sj.m_pad;
+    erow += sj.m_pad;
+    kstride = std::max(kstride, sj.K_pad);
+    p->jobs.push_back(sj);
+  }
+  for (int jix : order) {
+    const SplitJob& sj = p->jobs[jix];
+    if (sj.m == 0 || sj.K == 0) continue;
+    int nI = sj.m_pad / TILE_M, nJ = (sj.m + TILE_N - 1) / TILE_N;
+    for (int I = 0; I < nI; ++I)
+      for (int J = 2 * I; J < nJ; ++J) tiles.push_back({jix, I, J, (J == 2 * I || J == 2 * I + 1) ? 1 : 0});
+  }
+  if (row > (1ll << 31) - TILE_M) throw std::runtime_error("split slice arrays exceed 2^31 rows");
+  p->K_stride = kstride;
+  p->total_rows = row;
+  p->total_exp_rows = erow;
+  p->njobs = (int)p->jobs.size();
+  p->ntiles = (int)tiles.size();
+  auto dm = [](size_t bytes) {
+    void* q = nullptr;
+    if (cudaMalloc(&q, std::max<size_t>(bytes, 16)) != cudaSuccess) throw std::runtime_error("cudaMalloc");
+    return q;
+  };
+  try {
+    p->d_jobs = (SplitJob*)dm(sizeof(SplitJob) * std::max(1, p->njobs));
+    p->d_tiles = (SplitTile*)dm(sizeof(SplitTile) * std::max(1, p->ntiles));
+    cudaMemcpy(p->d_jobs, p->jobs.data(), sizeof(SplitJob) * p->njobs, cudaMemcpyHostToDevice);
+    cudaMemcpy(p->d_tiles, tiles.data(), sizeof(SplitTile) * p->ntiles, cudaMemcpyHostToDevice);
+    size_t abytes = (size_t)std::max(row, (long long)TILE_M) * kstride * 2;
+    for (int a = 0; a < 4; ++a) {
+      p->arr[a] = (__nv_bfloat16*)dm(abytes);
+      cudaMemset(p->arr[a], 0, abytes);
+    }
+    p->d_rexpA = (int*)dm(sizeof(int) * std::max(1ll, erow));
+    p->d_rexpB = (int*)dm(sizeof(int) * std::max(1ll, erow));
+    p->d_jobmax = (int*)dm(sizeof(int) * 2 * std::max(1, p->njobs));
+    p->d_flags = (int*)dm(sizeof(int) * 2 * std::max(1, p->njobs));
+    long long rows_map = std::max(row, (long long)TILE_M);
+    // every operand tile is loaded in 64-row boxes (an A tile is two of them),
+    // so one map per array serves both operand roles
+    for (int a = 0; a < 4; ++a) encode_map(&p->maps[a], p->arr[a], rows_map, kstride, TILE_N);
+  } catch (...) {
+    split_plan_destroy(p);
+    throw;
+  }
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  p->grid = std::max(1, std::min(nsm, p->ntiles));
+  int maxsm = 0;
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  size_t stage = (size_t)p->S * (TILE_M + TILE_N) * KB * 2;
+  p->nstages = (int)std::min<size_t>(4, ((size_t)maxsm - 2048) / stage);
+  if (p->nstages < 2) throw std::runtime_error("not enough shared memory for the split GEMM pipeline");
+  p->smem = 1024 + p->nstages * stage + (2 * p->nstages + 2) * 8 + 16;
   return p;
 }
 
-void split_plan_destroy(SplitPlan* p) { delete p; }
-
-cudaError_t launch_symgemm_split(SplitPlan*, const double*, const double*, const double*, double*, const int*,
-                                 const double*, const int*, int*, cudaStream_t)
+void split_plan_destroy(SplitPlan* p)
 {
-  return cudaErrorNotSupported;
+  if (!p) return;
+  cudaFree(p->d_jobs);
+  cudaFree(p->d_tiles);
+  for (int a = 0; a < 4; ++a) cudaFree(p->arr[a]);
+  cudaFree(p->d_rexpA);
+  cudaFree(p->d_rexpB);
+  cudaFree(p->d_jobmax);
+  cudaFree(p->d_flags);
+  delete p;
+}
+
+template <int S>
+static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, const double* B1, double* O,
+                            const int* kidx, const double* kw, const int* phase, int* status, int gsign,
+                            double gbscale, cudaStream_t st)
+{
+  cudaError_t e;
+  {
+    ProfScope ps(p->family == 0 ? "split_slice_ladder" : "split_slice_zbar", st);
+    e = cudaMemsetAsync(p->d_jobmax, 0, sizeof(int) * 2 * p->njobs, st);
+    if (e != cudaSuccess) return e;
+    int mp = 0;
+    for (const SplitJob& j : p->jobs) mp = std::max(mp, j.m_pad);
+    dim3 g1((mp + 127) / 128, p->njobs);
+    k_split_rowexp<<<g1, 128, 0, st>>>(p->d_jobs, p->njobs, A, B0, B1, kidx, kw, gbscale, p->d_rexpA, p->d_rexpB,
+                                       p->d_jobmax);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // per-job gamma / delta use (sign and phases are known on the host)
+    std::vector<int> flags(2 * p->njobs, 0);
+    int kpmax = 0;
+    for (int j = 0; j < p->njobs; ++j) {
+      const SplitJob& sj = p->jobs[j];
+      int sign = sj.sign != 0 ? sj.sign : gsign;
+      flags[2 * j] = (sign != 1 || sj.phase_off >= 0) ? 1 : 0;
+      flags[2 * j + 1] = sj.phase_off >= 0 ? 1 : 0;
+      kpmax = std::max(kpmax, sj.K_pad);
+    }
+    e = cudaMemcpyAsync(p->d_flags, flags.data(), sizeof(int) * flags.size(), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(st);  // the flag vector lives on this host stack frame
+    if (e != cudaSuccess) return e;
+    dim3 g2((kpmax + KB - 1) / KB, (mp + 31) / 32, p->njobs);
+    k_split_digits<S><<<g2, 256, 0, st>>>(p->d_jobs, p->njobs, A, B0, B1, kidx, kw, phase, gbscale, gsign,
+                                          p->d_rexpA, p->d_rexpB, p->d_jobmax, p->beta, p->K_stride, p->arr[0],
+                                          p->arr[1], p->arr[2], p->arr[3]);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  {
+    ProfScope ps(p->family == 0 ? "split_gemm_ladder" : "split_gemm_zbar", st);
+    static bool attr_set[MAX_S + 1] = {};
+    if (!attr_set[S]) {
+      e = cudaFuncSetAttribute(k_split_gemm<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
+      if (e != cudaSuccess) return e;
+      attr_set[S] = true;
+    }
+    GemmArgs ga;
+    ga.jobs = p->d_jobs;
+    ga.tiles = p->d_tiles;
+    ga.ntiles = p->ntiles;
+    ga.rexpA = p->d_rexpA;
+    ga.rexpB = p->d_rexpB;
+    ga.jobmax = p->d_jobmax;
+    ga.flags = p->d_flags;
+    ga.phase = phase;
+    ga.out = O;
+    ga.status = status;
+    ga.S = S;
+    ga.beta = p->beta;
+    ga.nstages = p->nstages;
+    ga.gsign = gsign;
+    k_split_gemm<S><<<p->grid, THREADS, p->smem, st>>>(p->maps[0], p->maps[1], p->maps[2], p->maps[3], ga);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_symgemm_split(SplitPlan* p, const double* A, const double* B0, const double* B1, double* O,
+                                 const int* kidx, const double* kw, const int* phase, int* dev_status, int gsign,
+                                 double gbscale, cudaStream_t st)
+{
+  if (p->ntiles == 0) return cudaSuccess;
+  switch (p->S) {
+    case 5: return launch_s<5>(p, A, B0, B1, O, kidx, kw, phase, dev_status, gsign, gbscale, st);
+    case 6: return launch_s<6>(p, A, B0, B1, O, kidx, kw, phase, dev_status, gsign, gbscale, st);
+    case 7: return launch_s<7>(p, A, B0, B1, O, kidx, kw, phase, dev_status, gsign, gbscale, st);
+    default: return cudaErrorNotSupported;
+  }
 }
 
 }  // namespace imsrg

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "kernels.cuh"
+#include "prof.hpp"
 
 namespace imsrg {
 
@@ -464,6 +465,7 @@ cudaError_t launch_comm111_110(const Space& s, const double* X, const double* Y,
 {
   int threads = s.norb <= 128 ? 128 : 256;
   k_comm111_110<<<s.norb, threads, 0, st>>>(s.dev, X, Y, Z, do111, do110);
+  count_launch();
   return cudaGetLastError();
 }
 
@@ -472,6 +474,7 @@ cudaError_t launch_comm220(const Space& s, const double* X, const double* Y, dou
   if (s.work.n220 == 0) return cudaSuccess;
   int wpb = 8;
   k_comm220<<<(s.work.n220 + wpb - 1) / wpb, 32 * wpb, 0, st>>>(s.dev, s.work, X, Y, Z, hX);
+  count_launch();
   return cudaGetLastError();
 }
 
@@ -491,6 +494,7 @@ cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, 
   if (s.work.n221 == 0) return cudaSuccess;
   int wpb = 8;
   k_comm221_1b<<<(s.work.n221 + wpb - 1) / wpb, 32 * wpb, 0, st>>>(s.dev, s.work, X, Y, Z, hX, hZ);
+  count_launch();
   return cudaGetLastError();
 }
 
@@ -499,9 +503,11 @@ cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, dou
 {
   if (s.work.ncols122 == 0) return cudaSuccess;
   k_comm122_w<<<s.work.ncols122, 128, 0, st>>>(s.dev, s.work, X, Y, W2);
+  count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_sym_subtract<<<nsym_tiles, 256, 0, st>>>(s.dev, W2, Z, hZ, sym_tiles, nsym_tiles);
+  count_launch();
   return cudaGetLastError();
 }
 
@@ -510,6 +516,7 @@ cudaError_t launch_pandya_fwd(const Space& s, const double* X, const double* Y, 
 {
   if (ntiles == 0) return cudaSuccess;
   k_pandya_fwd<<<ntiles, 256, 0, st>>>(s.dev, s.work, X, Y, hY, Xb, Yt, Yf, tiles, ntiles);
+  count_launch();
   return cudaGetLastError();
 }
 
@@ -518,18 +525,21 @@ cudaError_t launch_pandya_inv(const Space& s, const double* Zb, double* Z, int h
 {
   if (ntiles == 0) return cudaSuccess;
   k_pandya_inv<<<ntiles, 256, 0, st>>>(s.dev, s.work, Zb, Z, hZ, tiles, ntiles);
+  count_launch();
   return cudaGetLastError();
 }
 
 cudaError_t launch_axpy(double* y, const double* x, double a, long long n, cudaStream_t st)
 {
   k_axpy<<<1216, 256, 0, st>>>(y, x, a, n);
+  count_launch();
   return cudaGetLastError();
 }
 
 cudaError_t launch_scale(double* y, double a, long long n, cudaStream_t st)
 {
   k_scale<<<1216, 256, 0, st>>>(y, a, n);
+  count_launch();
   return cudaGetLastError();
 }
 
@@ -537,9 +547,11 @@ cudaError_t launch_norm(const Space& s, const double* A, const long long* chunk_
                         const double* chunk_w, int nchunks, double* partial, cudaStream_t st)
 {
   k_norm_onebody<<<1, 256, 0, st>>>(s.dev, A, partial + nchunks);
+  count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || nchunks == 0) return e;
   k_norm_chunks<<<nchunks, 256, 0, st>>>(A, chunk_off, chunk_len, chunk_w, partial, nchunks);
+  count_launch();
   return cudaGetLastError();
 }
 

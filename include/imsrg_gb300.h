@@ -177,6 +177,19 @@ int imsrg_get_default_precision(int* precision);
 int imsrg_bch_transform(const imsrg_op* OpIn, const imsrg_op* Omega, imsrg_op* OpOut, double threshold,
                         int precision, int* n_nested, void* stream);
 
+/* ------------------------------------------------------------- profiling */
+/* Named phase timers measured with CUDA events on the stream each phase ran
+ * on, and a count of kernel launches: the counterpart of IMSRGProfiler's
+ * timer / counter maps (src/IMSRGProfiler.cc:14-137; the reference adds each
+ * term's wall time under its function name, e.g. src/Commutator.cc:580).
+ * Off by default; names are the reference's term names plus kernel phases. */
+int imsrg_profiler_enable(int on);
+int imsrg_profiler_reset(void);
+int imsrg_profiler_get(const char* name, double* total_ms, long long* count);
+/* newline-separated timer names; with buf == NULL returns the size needed */
+int imsrg_profiler_names(char* buf, int buflen);
+long long imsrg_kernel_launches(void);
+
 #ifdef __cplusplus
 }
 #endif

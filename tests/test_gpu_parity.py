@@ -149,4 +149,5 @@ def test_random_fill_symmetry():
             b = r.block(a, c)
             if b.size:
                 assert np.allclose(b, h * b.T, atol=0)
-                assert abs(np.linalg.norm(b) - 1) < 1e-12
+                if b.shape[0] > 1 or h == 1:  # a 1x1 anti-hermitian block is zero
+                    assert abs(np.linalg.norm(b) - 1) < 1e-12
