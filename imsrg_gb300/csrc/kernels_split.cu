@@ -54,7 +54,7 @@ constexpr int TILE_N = 64;      // columns per tile (UMMA N)
 constexpr int MAX_S = 7;
 constexpr int EPI_COLS = 8;     // TMEM columns read per tcgen05.ld
 constexpr int THREADS = 192;
-constexpr unsigned WAIT_LIMIT = 1u << 26;  // bounded spin (with nanosleep backoff: seconds)
+constexpr unsigned WAIT_LIMIT = 1u << 22;  // bounded spin (with nanosleep backoff: about a second)
 constexpr int EXP_NONE = -100000;          // exponent of an all-zero row
 
 struct SplitJob {
@@ -292,7 +292,8 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
                                                      const int* __restrict__ kidx, const double* __restrict__ kw,
                                                      const int* __restrict__ phase, double gbscale, int gsign,
                                                      const int* __restrict__ rexpA, const int* __restrict__ rexpB,
-                                                     const int* __restrict__ jobmax, int beta, int K_stride,
+                                                     const int* __restrict__ jobmax, const int* __restrict__ flags,
+                                                     int beta, int K_stride,
                                                      __nv_bfloat16* __restrict__ alpha, __nv_bfloat16* __restrict__ bet,
                                                      __nv_bfloat16* __restrict__ gam, __nv_bfloat16* __restrict__ del)
 {
@@ -350,11 +351,7 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
     dB[0][r][tt] = (unsigned short)(__float_as_uint(__int_as_float(0x4B400000 + (int)qb) - 12582912.0f) >> 16);
   }
   __syncthreads();
-  bool need_g = false, need_d = false;
-  for (int r = 0; r < 32; ++r) {
-    need_g |= rowsg[r] != 1;
-    need_d |= rowph[r] != 1;
-  }
+  const bool need_g = flags[2 * job] != 0, need_d = flags[2 * job + 1] != 0;
   // stores: each thread one 16-byte vector (8 digits) of one row of one slice
   for (int e = threadIdx.x; e < S * 32 * (KB / 8); e += 256) {
     int v = e % (KB / 8), r = (e / (KB / 8)) & 31, s = e / (32 * (KB / 8));
@@ -802,7 +799,8 @@ static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, con
     if (e != cudaSuccess) return e;
     dim3 g2((kpmax + KB - 1) / KB, (mp + 31) / 32, p->njobs);
     k_split_digits<S><<<g2, 256, 0, st>>>(p->d_jobs, p->njobs, A, B0, B1, kidx, kw, phase, gbscale, gsign,
-                                          p->d_rexpA, p->d_rexpB, p->d_jobmax, p->beta, p->K_stride, p->arr[0],
+                                          p->d_rexpA, p->d_rexpB, p->d_jobmax, p->d_flags, p->beta, p->K_stride,
+                                          p->arr[0],
                                           p->arr[1], p->arr[2], p->arr[3]);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
