@@ -1,0 +1,422 @@
+#!/usr/bin/env python3
+"""Benchmark: [X,Y] commutators/sec of the IMSRG(2) scalar commutator at emax=10.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One step is one full CommutatorScalarScalar [X,Y] (all IMSRG(2) terms) on the
+emax=10 O16 model space (132 orbits, largest two-body channel 1341 kets):
+X hermitian and Y anti-hermitian, seeded uniform[-1,1] entries on
+symmetry-allowed elements, each two-body channel block and the one-body matrix
+scaled to unit Frobenius norm (synthetic; the reference publishes no dataset).
+
+gb300 arm (default): value = whole-job commutators/s of the split-precision form
+with operands resident in HBM, timed with CUDA events over K steps between
+barriers + synchronisations (max over ranks).  Every step reads X2, Y2 (280 MiB
+each) and writes Zbar (761 MiB), so the working set exceeds the 129 MB L2
+between steps.  Also reported: the plain FP64 form ("plain_fp64"), e2e (host
+buffers in pinned memory, H2D of X and Y + commutator + D2H of Z per step,
+through the C ABI), the roofline of the dominant kernel (from the library's
+CUDA-event phase timers over the timed region), SM clocks sampled during the
+timed region, the number of kernel launches, and a CPU baseline (the C oracle,
+a restatement of the reference's OpenMP + BLAS path, on all host cores).
+
+reference arm: the reference's CPU implementation of the path, here the C
+oracle port (the reference's own build needs the reference sources, absent on
+the GPU host), on all host threads; rank 0 only.
+Multi-GPU: replicas only (each rank runs its own commutators; no collective
+on the data path).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "[X,Y] commutators/sec at emax=10: split-prec vs FP64 on 1 GB300, <=1e-10 rel err"
+UNIT = "commutators/s"
+WORKLOAD = ("IMSRG(2) CommutatorScalarScalar [X,Y], emax={emax} O16, X hermitian / Y anti-hermitian, "
+            "uniform[-1,1], unit Frobenius per channel")
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--emax", type=int, default=10)
+    p.add_argument("--precision", default="split", choices=["split", "fp64"])
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+# --------------------------------------------------------------- helpers
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.lines = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.idx)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+def algorithmic_work(ms):
+    """Per-commutator algorithmic work of the dense phases and the gathers
+    (FP64-equivalent flops; bytes of one read of each input and one write of
+    each output)."""
+    occ = [o[4] for o in ms.orbits]
+    ladder = 0
+    n2 = 0
+    for c in ms.channels:
+        n = c["nkets"]
+        if n == 0:
+            continue
+        n2 += n * n
+        K = 0
+        for (p, q) in c["kets"]:
+            hp, hq = occ[p] > 1e-6, occ[q] > 1e-6
+            if (not hp and not hq) or (hp and hq):
+                K += 1
+        ladder += 2 * n * n * K
+    zbar = 0
+    zbar_elems = 0
+    for ch in range(ms.nch):
+        cc = ms.cc_channel(ch)
+        ncc = cc["nkets"]
+        nph = sum(1 for (p, q) in cc["kets"] if occ[p] > 1e-6 or occ[q] > 1e-6)
+        zbar += 2 * ncc * (2 * nph) * (2 * ncc)
+        zbar_elems += 2 * ncc * ncc
+    return {"ladder_flops": ladder, "zbar_flops": zbar, "z2_elems": n2, "zbar_elems": zbar_elems}
+
+
+def kernel_work(name, w):
+    """(bound, algorithmic amount per launch, unit) of a profiled phase."""
+    if name == "split_gemm_ladder":
+        return "tensor", w["ladder_flops"], "flops"
+    if name == "split_gemm_zbar":
+        return "tensor", w["zbar_flops"], "flops"
+    if name == "InversePandyaTransformation":
+        return "hbm", 8 * (w["zbar_elems"] + 2 * w["z2_elems"]), "bytes"
+    if name == "comm122ss":
+        return "hbm", 8 * 4 * w["z2_elems"], "bytes"
+    if name in ("split_slice_ladder",):
+        return "hbm", 8 * 2 * w["z2_elems"], "bytes"
+    return None
+
+
+def cpu_oracle_rate(emax, seconds, threads):
+    """The C oracle on `threads` host threads: commutators/s over a bounded sample."""
+    code = r"""
+import sys, time, json
+sys.path.insert(0, %r)
+from oracle import Oracle
+o = Oracle(%d)
+X = o.ms.random_operator(1, True); Y = o.ms.random_operator(2, False)
+o.commutator(X, Y, 1, -1)
+n = 0; t0 = time.perf_counter()
+while True:
+    o.commutator(X, Y, 1, -1); n += 1
+    t = time.perf_counter() - t0
+    if t >= %f or n >= 50: break
+print(json.dumps({"n": n, "t": t, "threads": o.num_threads()}))
+""" % (os.path.join(ROOT, "oracle"), emax, seconds)
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads), OPENBLAS_NUM_THREADS="1", OMP_PROC_BIND="false")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=1800)
+    if r.returncode != 0:
+        raise RuntimeError("CPU oracle failed: " + r.stderr[-500:])
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    return d["n"] / d["t"], d["threads"], d["n"]
+
+
+# --------------------------------------------------------------- arms
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    orc.build()
+    threads = os.cpu_count() or 1
+    env_code = r"""
+import sys, time, json
+sys.path.insert(0, %r)
+from oracle import Oracle
+o = Oracle(%d)
+X = o.ms.random_operator(1, True); Y = o.ms.random_operator(2, False)
+for _ in range(%d): o.commutator(X, Y, 1, -1)
+t0 = time.perf_counter()
+for _ in range(%d): o.commutator(X, Y, 1, -1)
+t = time.perf_counter() - t0
+print(json.dumps({"t": t, "threads": o.num_threads()}))
+""" % (os.path.join(ROOT, "oracle"), args.emax, args.warmup, args.steps)
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads), OPENBLAS_NUM_THREADS="1")
+    r = subprocess.run([sys.executable, "-c", env_code], capture_output=True, text=True, env=env, timeout=3600)
+    if r.returncode != 0:
+        print(json.dumps({"impl": "reference", "unavailable": "C oracle failed: " + r.stderr[-200:]}))
+        return
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    value = args.steps / d["t"]
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * d["t"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD.format(emax=args.emax), "emax": args.emax,
+                   "precision": "fp64 (CPU, OpenMP + BLAS dgemm)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": d["threads"], "kind": "port",
+                         "sample": "%d commutators at emax=%d after %d warm-up" % (args.steps, args.emax,
+                                                                                   args.warmup)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_gb300(args):
+    import torch
+
+    import imsrg_gb300 as ig
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    L = ig.lib()
+    ms = ig.ModelSpace(args.emax, "O16", "O16")
+    dX = ig.DeviceOperator(ms, 1)
+    dY = ig.DeviceOperator(ms, -1)
+    dZ = ig.DeviceOperator(ms, 1)
+    dX.fill_random(1000 + rank)
+    dY.fill_random(2000 + rank)
+    prec = args.precision
+
+    def step(p=prec):
+        ig.Commutator.device_commutator(dX, dY, dZ, p)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    barrier()
+    # ---- timed region (device-resident operands)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    L.imsrg_profiler_reset()
+    L.imsrg_profiler_enable(1)
+    launches0 = L.imsrg_kernel_launches()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    barrier()
+    launches = L.imsrg_kernel_launches() - launches0
+    L.imsrg_profiler_enable(0)
+    clocks.stop()
+    elapsed_ms = max_over_ranks(e0.elapsed_time(e1))
+    value = world * args.steps / (elapsed_ms / 1000.0)
+    # per-phase CUDA-event timers over the timed region
+    n = L.imsrg_profiler_names(None, 0)
+    buf = ctypes.create_string_buffer(n)
+    L.imsrg_profiler_names(buf, n)
+    phases = {}
+    for name in [x for x in buf.value.decode().split("\n") if x]:
+        t = ctypes.c_double()
+        c = ctypes.c_longlong()
+        L.imsrg_profiler_get(name.encode(), ctypes.byref(t), ctypes.byref(c))
+        phases[name] = (t.value, c.value)
+    # ---- roofline of the dominant kernel
+    work = algorithmic_work(ms)
+    hbm_peak, bf16_peak, peak_src = measured_peaks()
+    roof = None
+    best = None
+    for name, (tot, cnt) in phases.items():
+        kw = kernel_work(name, work)
+        if kw and cnt and (best is None or tot > phases[best][0]):
+            best = name
+    if best:
+        bound, amount, unit = kernel_work(best, work)
+        avg_s = phases[best][0] / phases[best][1] / 1000.0
+        if bound == "tensor":
+            ach = amount / avg_s / 1e12
+            roof = {"kernel": best, "bound": "tensor", "achieved": ach, "peak": bf16_peak, "unit": "TFLOP/s",
+                    "frac": ach / bf16_peak, "traffic": None,
+                    "note": "achieved counts FP64-equivalent algorithmic flops (the digit products issue 21x "
+                            "as many BF16 flops); peak = bf16 dense, %s" % peak_src}
+        else:
+            ach = amount / avg_s / 1e9
+            roof = {"kernel": best, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": ach / hbm_peak, "traffic": None, "note": "peak = HBM copy, %s" % peak_src}
+        roof["share"] = phases[best][0] / max(1e-9, phases["CommutatorScalarScalar"][0]) \
+            if "CommutatorScalarScalar" in phases else None
+    # ---- plain FP64 form (the metric compares split vs FP64)
+    fp64 = None
+    if prec == "split":
+        step("fp64")
+        barrier()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        nf = 3
+        f0.record()
+        for _ in range(nf):
+            step("fp64")
+        f1.record()
+        torch.cuda.synchronize()
+        fms = max_over_ranks(f0.elapsed_time(f1)) / nf
+        fp64 = {"value": world * 1000.0 / fms, "unit": UNIT, "ms_per_step": fms, "steps": nf}
+    # ---- end to end: host buffers, H2D + commutator + D2H per step, through the C ABI
+    A = ms.arena_size
+    hX = torch.empty(A, dtype=torch.float64, pin_memory=True)
+    hY = torch.empty(A, dtype=torch.float64, pin_memory=True)
+    hZ = torch.empty(A, dtype=torch.float64, pin_memory=True)
+    dX.download_ptr(hX.data_ptr())
+    dY.download_ptr(hY.data_ptr())
+    ne = max(1, min(args.steps, 10))
+    barrier()
+    g0 = torch.cuda.Event(enable_timing=True)
+    g1 = torch.cuda.Event(enable_timing=True)
+    g0.record()
+    for _ in range(ne):
+        dX.upload_ptr(hX.data_ptr())
+        dY.upload_ptr(hY.data_ptr())
+        step()
+        dZ.download_ptr(hZ.data_ptr())
+    g1.record()
+    torch.cuda.synchronize()
+    ems = max_over_ranks(g0.elapsed_time(g1))
+    e2e = {"value": world * ne / (ems / 1000.0), "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * A,
+           "d2h_bytes_per_step": 8 * A}
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    # ---- CPU baseline (rank 0, N=1 only)
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        try:
+            threads = os.cpu_count() or 1
+            rate, used, nsamp = cpu_oracle_rate(args.emax, args.cpu_seconds, threads)
+            cpu = {"value": rate, "unit": UNIT, "cores": used, "kind": "port",
+                   "sample": "%d commutator(s) at emax=%d, C oracle (OpenMP over channels + SciPy BLAS dgemm)"
+                             % (nsamp, args.emax)}
+        except Exception as ex:  # reported, not fatal
+            cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": "failed: %s" % ex}
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD.format(emax=args.emax), "emax": args.emax, "orbits": ms.norb,
+                   "largest_2b_channel": max(c["nkets"] for c in ms.channels), "precision": prec,
+                   "gemm": "Ozaki BF16 digits on tcgen05, FP32 accumulate, int64/FP64 recombination"
+                   if prec == "split" else "FP64 CUDA cores",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "working set > L2 every step (X2, Y2 280 MiB each; Zbar 761 MiB)"},
+        "plain_fp64": fp64,
+        "e2e": e2e,
+        "roofline": roof,
+        "phases_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in sorted(phases.items())},
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+        "gpu_launches": int(launches),
+    }
+    print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -256,6 +256,14 @@ class DeviceOperator:
         if stream is not None:
             self._keep = a
 
+    def upload_ptr(self, host_ptr, stream=None):
+        """Copy the arena from a host address (e.g. pinned memory)."""
+        check(self._L.imsrg_op_upload(self._h, ctypes.cast(host_ptr, ctypes.POINTER(ctypes.c_double)), stream))
+
+    def download_ptr(self, host_ptr, stream=None):
+        """Copy the arena to a host address; synchronises the stream."""
+        check(self._L.imsrg_op_download(self._h, ctypes.cast(host_ptr, ctypes.POINTER(ctypes.c_double)), stream))
+
     def download(self, out=None, stream=None):
         if out is None:
             out = np.empty(self.modelspace.arena_size)
