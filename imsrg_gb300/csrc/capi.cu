@@ -195,9 +195,8 @@ void setup_device_lists(imsrg_space* sp)
         t122.push_back(a);
         t122.push_back(b);
       }
-    int n16 = (n + 15) / 16;
-    for (int a = 0; a < n16; ++a)
-      for (int b = a; b < n16; ++b) {
+    for (int a = 0; a < nt; ++a)
+      for (int b = a; b < nt; ++b) {
         tinv.push_back(c);
         tinv.push_back(a);
         tinv.push_back(b);

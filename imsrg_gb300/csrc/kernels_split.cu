@@ -226,43 +226,84 @@ __device__ __forceinline__ long long to_fixed(double v, int e, int P)
 
 // ------------------------------------------------------------ exponents
 // raw row exponents (max biased exponent over the row) of A and B, and the
-// per-job maxima.  One thread per (job, row).
-__global__ void k_split_rowexp(const SplitJob* __restrict__ jobs, int njobs, const double* __restrict__ Abase,
-                               const double* __restrict__ B0, const double* __restrict__ B1,
-                               const int* __restrict__ kidx, const double* __restrict__ kw, double gbscale,
-                               int* __restrict__ rexpA, int* __restrict__ rexpB, int* __restrict__ jobmax)
+// per-job maxima.  Block = 32 rows x 8 column lanes over a 256-column chunk;
+// partial maxima combine through atomicMax (the arrays are zeroed first).
+// The exponent of B includes the job / column scale (a power of two or a
+// weight) so the B digits are taken of the scaled values.
+__global__ void __launch_bounds__(256) k_split_rowexp(const SplitJob* __restrict__ jobs, int njobs,
+                                                      const double* __restrict__ Abase,
+                                                      const double* __restrict__ B0, const double* __restrict__ B1,
+                                                      const int* __restrict__ kidx, const double* __restrict__ kw,
+                                                      double gbscale, int* __restrict__ rexpA,
+                                                      int* __restrict__ rexpB, int* __restrict__ jobmax)
 {
-  int job = blockIdx.y;
+  __shared__ int sa[8][33], sb[8][33];
+  int job = blockIdx.z;
   if (job >= njobs) return;
   const SplitJob jb = jobs[job];
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= jb.m_pad) return;
+  const int r = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int i = blockIdx.y * 32 + r;
+  const int t0 = blockIdx.x * 256;
+  if (blockIdx.y * 32 >= jb.m_pad || t0 >= max(jb.K, 1)) return;
   int ea = 0, eb = 0;
   if (i < jb.m) {
     const double* A = Abase + jb.a_off;
     const double* B = (jb.bsel ? B1 : B0) + jb.b_off;
     const int* kx = jb.kidx_off >= 0 ? kidx + jb.kidx_off : nullptr;
     const double* w = jb.w_off >= 0 ? kw + jb.w_off : nullptr;
-    double sc0 = jb.bscale * gbscale;
-    for (int t = 0; t < jb.K; ++t) {
+    const double sc0 = jb.bscale * gbscale;
+    const int tend = min(jb.K, t0 + 256);
+    for (int t = t0 + ty; t < tend; t += 8) {
       int col = kx ? __ldg(kx + t) : t;
       ea = max(ea, dexp(A[(long long)col * jb.lda + i]));
       double sc = w ? sc0 * __ldg(w + t) : sc0;
       eb = max(eb, dexp(scaled(B[(long long)col * jb.ldb + i], sc)));
     }
   }
-  rexpA[jb.exp_base + i] = ea;
-  rexpB[jb.exp_base + i] = eb;
-  // warp-level max then one atomic per warp
-  int wa = ea, wb = eb;
-  for (int o = 16; o > 0; o >>= 1) {
-    wa = max(wa, __shfl_xor_sync(0xffffffffu, wa, o));
-    wb = max(wb, __shfl_xor_sync(0xffffffffu, wb, o));
+  sa[ty][r] = ea;
+  sb[ty][r] = eb;
+  __syncthreads();
+  if (ty == 0) {
+    for (int y = 1; y < 8; ++y) {
+      ea = max(ea, sa[y][r]);
+      eb = max(eb, sb[y][r]);
+    }
+    if (ea) atomicMax(rexpA + jb.exp_base + i, ea);
+    if (eb) atomicMax(rexpB + jb.exp_base + i, eb);
+    int wa = ea, wb = eb;
+    for (int o = 16; o > 0; o >>= 1) {
+      wa = max(wa, __shfl_xor_sync(0xffffffffu, wa, o));
+      wb = max(wb, __shfl_xor_sync(0xffffffffu, wb, o));
+    }
+    if (r == 0) {
+      if (wa) atomicMax(jobmax + 2 * job, wa);
+      if (wb) atomicMax(jobmax + 2 * job + 1, wb);
+    }
   }
-  if ((threadIdx.x & 31) == 0) {
-    atomicMax(jobmax + 2 * job, wa);
-    atomicMax(jobmax + 2 * job + 1, wb);
+}
+
+// signed 64-bit integer times 2^X as a double, integer instructions only
+// (round to nearest even); 0 on underflow of the exponent range.
+__device__ __forceinline__ double i64_ldexp(long long v, int X)
+{
+  if (v == 0) return 0.0;
+  unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
+  unsigned long long u = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+  int lz = __clzll((long long)u);
+  unsigned long long m = u << lz;            // leading one at bit 63
+  unsigned long long mant = m >> 11;         // 53 bits
+  unsigned long long rest = m & 0x7FFull;
+  if (rest > 0x400ull || (rest == 0x400ull && (mant & 1ull))) {
+    ++mant;
+    if (mant >> 53) {
+      mant >>= 1;
+      --lz;
+    }
   }
+  int e = (63 - lz) + 1023 + X;
+  if (e <= 0) return 0.0;
+  if (e >= 2047) return __longlong_as_double((long long)(sgn | (0x7FFull << 52)));
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)e << 52) | (mant & 0xFFFFFFFFFFFFFull)));
 }
 
 // exponent of row i (A side) from the raw exponents: a_i = max(eA, eB - c)
@@ -416,7 +457,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
   // bars: full[NST], empty[NST], acc_full, acc_empty ; then tmem slot
   unsigned* tmem_slot = (unsigned*)(bars + 2 * NST + 2);
   __shared__ int s_err_;
+  __shared__ int s_colexp[TILE_N];
+  __shared__ int s_colph[TILE_N];
+  __shared__ int s_epi_err_;
   volatile int& s_err = s_err_;
+  volatile int& s_epi_err = s_epi_err_;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned sbase = smem_u32(smem);
@@ -428,6 +473,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
 
   if (threadIdx.x == 0) {
     s_err = 0;
+    s_epi_err = 0;
     for (int s = 0; s < NST; ++s) {
       mbar_init(full_bar(s), 1);
       mbar_init(empty_bar(s), 1);
@@ -537,8 +583,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
     for (int tix = blockIdx.x; tix < g.ntiles; tix += gridDim.x, ++tc) {
       const SplitTile tl = g.tiles[tix];
       const SplitJob& jb = g.jobs[tl.job];
+      // the four epilogue warps decide together (named barrier 1), so a
+      // timeout never leaves one of them waiting at a barrier alone
       if (!mbar_wait(acc_full, (unsigned)(tc & 1))) {
         set_status(g.status, 104);
+        s_epi_err = 1;
+      }
+      asm volatile("bar.sync 1, 128;" ::: "memory");
+      if (s_epi_err) {
         s_err = 1;
         break;
       }
@@ -550,42 +602,61 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
       const bool rowok = i < jb.m;
       const int ai = rowok ? row_exp(g.rexpA[jb.exp_base + i], g.rexpB[jb.exp_base + i], c) : EXP_NONE;
       const int phi_i = (ph && rowok) ? ph[i] : 1;
+      // column exponents and phases of this tile, once per tile
+      {
+        const int et = threadIdx.x - 64;  // 0..127 over the epilogue warps
+        if (et < TILE_N) {
+          const int j = tl.J * TILE_N + et;
+          const bool ok = j < jb.m;
+          s_colexp[et] = ok ? row_exp(g.rexpA[jb.exp_base + j], g.rexpB[jb.exp_base + j], c) : EXP_NONE;
+          s_colph[et] = (ph && ok) ? ph[j] : 1;
+        }
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+      }
       double* O = g.out + jb.out_off;
+      const int Xi = ai + c - g.beta * (S + 1);
       for (int c0 = 0; c0 < TILE_N; c0 += EPI_COLS) {
         unsigned r[MAX_S][EPI_COLS];
 #pragma unroll
         for (int gidx = 0; gidx < S; ++gidx)
           tmem_ld8(tmem + ((unsigned)(q * 32) << 16) + (unsigned)(gidx * TILE_N + c0), r[gidx]);
         tmem_wait_ld();
+        // values of this chunk, then all old values (accumulate), then the
+        // stores: the loads of one chunk are in flight together
+        double v[EPI_COLS], mv[EPI_COLS], od[EPI_COLS], om[EPI_COLS];
+        bool wd[EPI_COLS], wm[EPI_COLS];
 #pragma unroll
         for (int cc = 0; cc < EPI_COLS; ++cc) {
           const int j = tl.J * TILE_N + c0 + cc;
-          if (!rowok || j >= jb.m) continue;
-          if (tl.diag && i > j) continue;
-          long long I64 = 0;
+          wd[cc] = rowok && j < jb.m && !(tl.diag && i > j);
+          wm[cc] = wd[cc] && i != j;
+          // exact merge of the weight groups: Horner in base 2^beta
+          long long I64 = __float2int_rn(__uint_as_float(r[0][cc]));
 #pragma unroll
-          for (int gidx = 0; gidx < S; ++gidx)
-            I64 += (long long)__float2ll_rn(__uint_as_float(r[gidx][cc])) * (1ll << (g.beta * (S - 1 - gidx)));
-          double v = 0.0;
-          if (I64 != 0) {
-            const int aj = row_exp(g.rexpA[jb.exp_base + j], g.rexpB[jb.exp_base + j], c);
-            const int X = ai + aj + c - g.beta * (S + 1);
-            double d = __ll2double_rn(I64);
-            long long bits = __double_as_longlong(d);
-            int e = (int)((bits >> 52) & 0x7FF) + X;
-            if (e > 0 && e < 2047) v = __longlong_as_double((bits & ~(0x7FFll << 52)) | ((long long)e << 52));
+          for (int gidx = 1; gidx < S; ++gidx)
+            I64 = I64 * (1ll << g.beta) + __float2int_rn(__uint_as_float(r[gidx][cc]));
+          v[cc] = i64_ldexp(I64, Xi + s_colexp[c0 + cc]);
+          mv[cc] = (sign * phi_i * s_colph[c0 + cc]) < 0 ? -v[cc] : v[cc];
+          od[cc] = 0.0;
+          om[cc] = 0.0;
+        }
+        if (jb.accumulate) {
+#pragma unroll
+          for (int cc = 0; cc < EPI_COLS; ++cc) {
+            const long long j = tl.J * TILE_N + c0 + cc;
+            if (wd[cc]) od[cc] = __ldcg(O + j * jb.ldo + i);
+            if (wm[cc]) om[cc] = __ldcg(O + (long long)i * jb.ldo + j);
           }
-          long long o = (long long)j * jb.ldo + i;
-          O[o] = jb.accumulate ? O[o] + v : v;
-          if (i != j) {
-            const int phi_j = ph ? ph[j] : 1;
-            double mv = (sign * phi_i * phi_j) < 0 ? -v : v;
-            long long o2 = (long long)i * jb.ldo + j;
-            O[o2] = jb.accumulate ? O[o2] + mv : mv;
-          }
+        }
+#pragma unroll
+        for (int cc = 0; cc < EPI_COLS; ++cc) {
+          const long long j = tl.J * TILE_N + c0 + cc;
+          if (wd[cc]) O[j * jb.ldo + i] = od[cc] + v[cc];
+          if (wm[cc]) O[(long long)i * jb.ldo + j] = om[cc] + mv[cc];
         }
       }
       tc_fence_before();
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // s_colexp reused by the next tile
       mbar_arrive(acc_empty);
     }
   }
@@ -731,7 +802,16 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
     p->d_rexpA = (int*)dm(sizeof(int) * std::max(1ll, erow));
     p->d_rexpB = (int*)dm(sizeof(int) * std::max(1ll, erow));
     p->d_jobmax = (int*)dm(sizeof(int) * 2 * std::max(1, p->njobs));
-    p->d_flags = (int*)dm(sizeof(int) * 2 * std::max(1, p->njobs));
+    p->d_flags = (int*)dm(sizeof(int) * 4 * std::max(1, p->njobs));
+    std::vector<int> flags(4 * p->njobs, 0);
+    for (int gs = 0; gs < 2; ++gs)
+      for (int j = 0; j < p->njobs; ++j) {
+        const SplitJob& sj = p->jobs[j];
+        int sign = sj.sign != 0 ? sj.sign : (gs == 0 ? 1 : -1);
+        flags[2 * p->njobs * gs + 2 * j] = (sign != 1 || sj.phase_off >= 0) ? 1 : 0;
+        flags[2 * p->njobs * gs + 2 * j + 1] = sj.phase_off >= 0 ? 1 : 0;
+      }
+    cudaMemcpy(p->d_flags, flags.data(), sizeof(int) * flags.size(), cudaMemcpyHostToDevice);
     long long rows_map = std::max(row, (long long)TILE_M);
     // every operand tile is loaded in 64-row boxes (an A tile is two of them),
     // so one map per array serves both operand roles
@@ -766,6 +846,10 @@ void split_plan_destroy(SplitPlan* p)
   delete p;
 }
 
+// per-job use of the gamma / delta arrays for a launch sign (precomputed for
+// both signs at plan creation): [0, 2 njobs) for sign +1, then for sign -1
+static const int* flags_for(const SplitPlan* p, int gsign) { return p->d_flags + (gsign == 1 ? 0 : 2 * p->njobs); }
+
 template <int S>
 static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, const double* B1, double* O,
                             const int* kidx, const double* kw, const int* phase, int* status, int gsign,
@@ -776,32 +860,26 @@ static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, con
     ProfScope ps(p->family == 0 ? "split_slice_ladder" : "split_slice_zbar", st);
     e = cudaMemsetAsync(p->d_jobmax, 0, sizeof(int) * 2 * p->njobs, st);
     if (e != cudaSuccess) return e;
-    int mp = 0;
-    for (const SplitJob& j : p->jobs) mp = std::max(mp, j.m_pad);
-    dim3 g1((mp + 127) / 128, p->njobs);
-    k_split_rowexp<<<g1, 128, 0, st>>>(p->d_jobs, p->njobs, A, B0, B1, kidx, kw, gbscale, p->d_rexpA, p->d_rexpB,
+    e = cudaMemsetAsync(p->d_rexpA, 0, sizeof(int) * std::max(1ll, p->total_exp_rows), st);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(p->d_rexpB, 0, sizeof(int) * std::max(1ll, p->total_exp_rows), st);
+    if (e != cudaSuccess) return e;
+    int mp = 0, kmax = 1;
+    for (const SplitJob& j : p->jobs) {
+      mp = std::max(mp, j.m_pad);
+      kmax = std::max(kmax, j.K);
+    }
+    dim3 g1((kmax + 255) / 256, (mp + 31) / 32, p->njobs);
+    k_split_rowexp<<<g1, 256, 0, st>>>(p->d_jobs, p->njobs, A, B0, B1, kidx, kw, gbscale, p->d_rexpA, p->d_rexpB,
                                        p->d_jobmax);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    // per-job gamma / delta use (sign and phases are known on the host)
-    std::vector<int> flags(2 * p->njobs, 0);
     int kpmax = 0;
-    for (int j = 0; j < p->njobs; ++j) {
-      const SplitJob& sj = p->jobs[j];
-      int sign = sj.sign != 0 ? sj.sign : gsign;
-      flags[2 * j] = (sign != 1 || sj.phase_off >= 0) ? 1 : 0;
-      flags[2 * j + 1] = sj.phase_off >= 0 ? 1 : 0;
-      kpmax = std::max(kpmax, sj.K_pad);
-    }
-    e = cudaMemcpyAsync(p->d_flags, flags.data(), sizeof(int) * flags.size(), cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return e;
-    e = cudaStreamSynchronize(st);  // the flag vector lives on this host stack frame
-    if (e != cudaSuccess) return e;
+    for (const SplitJob& sj : p->jobs) kpmax = std::max(kpmax, sj.K_pad);
     dim3 g2((kpmax + KB - 1) / KB, (mp + 31) / 32, p->njobs);
     k_split_digits<S><<<g2, 256, 0, st>>>(p->d_jobs, p->njobs, A, B0, B1, kidx, kw, phase, gbscale, gsign,
-                                          p->d_rexpA, p->d_rexpB, p->d_jobmax, p->d_flags, p->beta, p->K_stride,
-                                          p->arr[0],
-                                          p->arr[1], p->arr[2], p->arr[3]);
+                                          p->d_rexpA, p->d_rexpB, p->d_jobmax, flags_for(p, gsign), p->beta,
+                                          p->K_stride, p->arr[0], p->arr[1], p->arr[2], p->arr[3]);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
@@ -820,7 +898,7 @@ static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, con
     ga.rexpA = p->d_rexpA;
     ga.rexpB = p->d_rexpB;
     ga.jobmax = p->d_jobmax;
-    ga.flags = p->d_flags;
+    ga.flags = flags_for(p, gsign);
     ga.phase = phase;
     ga.out = O;
     ga.status = status;

@@ -336,66 +336,106 @@ __global__ void k_pandya_fwd(DevSpace S, DevWork W, const double* __restrict__ X
 // ------------------------------------------------------------ Pandya inverse
 // AddInversePandyaTransformation (src/Commutator.cc:1501-1616): for every
 // (ibra <= iket) element of every 2b channel block, the two J' sums over Zbar.
-__global__ void k_pandya_inv(DevSpace S, DevWork W, const double* __restrict__ Zb, double* __restrict__ Z, int hZ,
-                             const int* __restrict__ tiles, int ntiles)
+//
+// Access pattern: a block owns a 32 (bras) x 32 (kets) tile; lanes run over
+// kets, so for one bra (i,j) consecutive lanes share k and step through l.
+// The first sum reads Zbar(il, kj): one column kj, consecutive rows il.  The
+// second sum needs Zbar(ik, lj), which would be one row and scattered
+// columns; it is read through the symmetry of the symmetrised Zbar instead,
+//   head:  Zbar(r, c) = hZ Zbar(c, r),
+//   tail:  Zbar(r, n + c) = phi_r phi_c Zbar(c, n + r),
+// i.e. as Zbar(lj, ik): again one column, consecutive rows.  Results go
+// through shared memory so both the Z(ibra, iket) and the mirrored
+// Z(iket, ibra) updates are coalesced.
+__global__ void __launch_bounds__(256) k_pandya_inv(DevSpace S, DevWork W, const double* __restrict__ Zb,
+                                                    double* __restrict__ Z, int hZ, const int* __restrict__ tiles,
+                                                    int ntiles)
 {
+  __shared__ double T[32][33];
   int tix = blockIdx.x;
   if (tix >= ntiles) return;
-  int ch = tiles[3 * tix], ti = tiles[3 * tix + 1], tj = tiles[3 * tix + 2];
-  int n = S.ch_n[ch];
-  int ibra = ti * 16 + (threadIdx.x & 15);
-  int iket = tj * 16 + (threadIdx.x >> 4);
-  if (ibra >= n || iket >= n) return;
-  if (hZ == 1 ? (iket < ibra) : (iket <= ibra)) return;
-  int J = ch / 6;
-  int kofs = S.ch_kofs[ch];
-  int i = S.ket_p[kofs + ibra], j = S.ket_q[kofs + ibra];
-  int k = S.ket_p[kofs + iket], l = S.ket_q[kofs + iket];
-  int jji = S.j2[i], jjj = S.j2[j], jjk = S.j2[k], jjl = S.j2[l];
-  int N = S.norb;
-  double commij = 0.0, commji = 0.0;
-  {
-    int par = (S.l[i] + S.l[l]) & 1;
-    int tz = abs(S.tz2[i] - S.tz2[l]) / 2;
-    int Jpmin = max(abs(jji - jjl), abs(jjk - jjj)) / 2;
-    int Jpmax = min(jji + jjl, jjk + jjj) / 2;
-    int kil = ket_index(N, min(i, l), max(i, l)), kkj = ket_index(N, min(j, k), max(j, k));
-    for (int Jp = Jpmin; Jp <= Jpmax; ++Jp) {
-      double sj = dev_sixj(S, jji, jjj, J, jjk, jjl, Jp);
-      if (fabs(sj) < 1e-8) continue;
-      int cc = chan_index(Jp, par, tz);
-      int ncc = S.cc_n[cc];
-      int il = S.ccJ_loc[kil * S.NJ + Jp] + (i > l ? ncc : 0);
-      int kj = S.ccJ_loc[kkj * S.NJ + Jp] + (k > j ? ncc : 0);
-      commij -= (2 * Jp + 1) * sj * Zb[W.zb_off[cc] + (long long)kj * ncc + il];
-    }
+  const int ch = tiles[3 * tix], tb = tiles[3 * tix + 1], tk = tiles[3 * tix + 2];
+  const int n = S.ch_n[ch];
+  const int J = ch / 6;
+  const int kofs = S.ch_kofs[ch];
+  const int N = S.norb;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int iket = tk * 32 + lane;
+  int k = 0, l = 0, jjk = 0, jjl = 0;
+  if (iket < n) {
+    k = S.ket_p[kofs + iket];
+    l = S.ket_q[kofs + iket];
+    jjk = S.j2[k];
+    jjl = S.j2[l];
   }
-  if (k == l) {
-    commji = commij;
-  } else if (i == j) {
-    commji = iphase((jji + jjj + jjk + jjl) / 2) * commij;
-  } else {
-    int par = (S.l[i] + S.l[k]) & 1;
-    int tz = abs(S.tz2[i] - S.tz2[k]) / 2;
-    int Jpmin = max(abs(jjj - jjl), abs(jjk - jji)) / 2;
-    int Jpmax = min(jjj + jjl, jjk + jji) / 2;
-    int kik = ket_index(N, min(i, k), max(i, k)), klj = ket_index(N, min(l, j), max(l, j));
-    for (int Jp = Jpmin; Jp <= Jpmax; ++Jp) {
-      double sj = dev_sixj(S, jjj, jji, J, jjk, jjl, Jp);
-      if (fabs(sj) < 1e-8) continue;
-      int cc = chan_index(Jp, par, tz);
-      int ncc = S.cc_n[cc];
-      int ik = S.ccJ_loc[kik * S.NJ + Jp] + (i > k ? ncc : 0);
-      int lj = S.ccJ_loc[klj * S.NJ + Jp] + (l > j ? ncc : 0);
-      commji -= (2 * Jp + 1) * sj * Zb[W.zb_off[cc] + (long long)lj * ncc + ik];
+  for (int bb = warp; bb < 32; bb += 8) {
+    const int ibra = tb * 32 + bb;
+    double z = 0.0;
+    const bool valid = ibra < n && iket < n && (hZ == 1 ? iket >= ibra : iket > ibra);
+    if (valid) {
+      const int i = S.ket_p[kofs + ibra], j = S.ket_q[kofs + ibra];
+      const int jji = S.j2[i], jjj = S.j2[j];
+      double commij = 0.0, commji = 0.0;
+      {
+        int par = (S.l[i] + S.l[l]) & 1;
+        int tz = abs(S.tz2[i] - S.tz2[l]) / 2;
+        int Jpmin = max(abs(jji - jjl), abs(jjk - jjj)) / 2;
+        int Jpmax = min(jji + jjl, jjk + jjj) / 2;
+        int kil = ket_index(N, min(i, l), max(i, l)), kkj = ket_index(N, min(j, k), max(j, k));
+        for (int Jp = Jpmin; Jp <= Jpmax; ++Jp) {
+          double sj = dev_sixj(S, jji, jjj, J, jjk, jjl, Jp);
+          if (fabs(sj) < 1e-8) continue;
+          int cc = chan_index(Jp, par, tz);
+          int ncc = S.cc_n[cc];
+          int il = S.ccJ_loc[kil * S.NJ + Jp] + (i > l ? ncc : 0);
+          int kj = S.ccJ_loc[kkj * S.NJ + Jp] + (k > j ? ncc : 0);
+          commij -= (2 * Jp + 1) * sj * Zb[W.zb_off[cc] + (long long)kj * ncc + il];
+        }
+      }
+      if (k == l) {
+        commji = commij;
+      } else if (i == j) {
+        commji = iphase((jji + jjj + jjk + jjl) / 2) * commij;
+      } else {
+        int par = (S.l[i] + S.l[k]) & 1;
+        int tz = abs(S.tz2[i] - S.tz2[k]) / 2;
+        int Jpmin = max(abs(jjj - jjl), abs(jjk - jji)) / 2;
+        int Jpmax = min(jjj + jjl, jjk + jji) / 2;
+        int kik = ket_index(N, min(i, k), max(i, k)), klj = ket_index(N, min(l, j), max(l, j));
+        // i <= k always (ibra <= iket), so ik is a row of the head/tail blocks
+        double tsign = (l > j) ? (double)iphase((jji + jjk + jjl + jjj) / 2) : (double)hZ;
+        for (int Jp = Jpmin; Jp <= Jpmax; ++Jp) {
+          double sj = dev_sixj(S, jjj, jji, J, jjk, jjl, Jp);
+          if (fabs(sj) < 1e-8) continue;
+          int cc = chan_index(Jp, par, tz);
+          int ncc = S.cc_n[cc];
+          int ik = S.ccJ_loc[kik * S.NJ + Jp];
+          int lj = S.ccJ_loc[klj * S.NJ + Jp];
+          // Zbar(ik, lj[+n]) read as its symmetric partner Zbar(lj, ik[+n])
+          long long e = W.zb_off[cc] + (long long)(ik + (l > j ? ncc : 0)) * ncc + lj;
+          commji -= (2 * Jp + 1) * sj * tsign * Zb[e];
+        }
+      }
+      int bd = (i == j), kd = (k == l);
+      double norm = bd == kd ? 1 + bd : kSqrt2;
+      z = -(commij - iphase((jjk + jjl) / 2 - J) * commji) / norm;
     }
+    T[bb][lane] = z;
   }
-  int bd = (i == j), kd = (k == l);
-  double norm = bd == kd ? 1 + bd : kSqrt2;
-  double z = -(commij - iphase((jjk + jjl) / 2 - J) * commji) / norm;
-  long long off = S.ch_off[ch];
-  Z[off + (long long)iket * n + ibra] += z;
-  if (ibra != iket) Z[off + (long long)ibra * n + iket] += hZ * z;
+  __syncthreads();
+  const long long off = S.ch_off[ch];
+  // Z(ibra, iket) += z : threads run over bras (column-major rows)
+  for (int e = threadIdx.x; e < 1024; e += 256) {
+    int bb = e & 31, kk = e >> 5;
+    int ibra = tb * 32 + bb, ik2 = tk * 32 + kk;
+    if (ibra < n && ik2 < n && (hZ == 1 ? ik2 >= ibra : ik2 > ibra)) Z[off + (long long)ik2 * n + ibra] += T[bb][kk];
+  }
+  // Z(iket, ibra) += hZ z for ibra != iket : threads run over kets
+  for (int e = threadIdx.x; e < 1024; e += 256) {
+    int kk = e & 31, bb = e >> 5;
+    int ibra = tb * 32 + bb, ik2 = tk * 32 + kk;
+    if (ibra < n && ik2 < n && ik2 > ibra) Z[off + (long long)ibra * n + ik2] += hZ * T[bb][kk];
+  }
 }
 
 // ------------------------------------------------------------ operator algebra
