@@ -327,10 +327,12 @@ int do_122(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
   return IMSRG_OK;
 }
 
-int do_221_1b(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
+// Mz: the two-body blocks of Mpp - Mhh when already available (the ladder
+// product accumulated onto a zeroed Z), else nullptr (dot products)
+int do_221_1b(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st, const double* Mz = nullptr)
 {
   ProfScope ps("comm221ss", st);
-  CUDA_TRY(launch_comm221_1b(*X->sp->s, X->d, Y->d, Z->d, X->herm, Z->herm, st));
+  CUDA_TRY(launch_comm221_1b(*X->sp->s, X->d, Y->d, Z->d, X->herm, Z->herm, Mz, st));
   return IMSRG_OK;
 }
 
@@ -418,12 +420,18 @@ int commutator_impl(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec,
   }
   ProfScope ps("CommutatorScalarScalar", st);
   CUDA_TRY(cudaMemsetAsync(Z->d, 0, X->sp->s->arena * sizeof(double), st));
+  // The terms add into Z in an order of our own (the sum is the same up to
+  // rounding): the ladder product goes first, onto the zeroed two-body blocks,
+  // so the one-body part of comm221ss can read Mpp - Mhh straight from Z2
+  // instead of recomputing the pp dot products (ConstructScalarMpp_Mhh is
+  // shared the same way by the reference's comm222_pp_hh_221ss).
+  bool ladder_first = on[T222PPHH];
+  if (ladder_first && (rc = do_ladder(X, Y, Z, prec, st))) return rc;
+  if (on[T221] && (rc = do_221_1b(X, Y, Z, st, ladder_first ? Z->d : nullptr))) return rc;
   if ((rc = do_111_110(X, Y, Z, on[T111], on[T110], st))) return rc;
   if (on[T220] && (rc = do_220(X, Y, Z, st))) return rc;
   if (on[T121] && (rc = do_121(X, Y, Z, st))) return rc;
   if (on[T122] && (rc = do_122(X, Y, Z, st))) return rc;
-  if (on[T222PPHH] && (rc = do_ladder(X, Y, Z, prec, st))) return rc;
-  if (on[T221] && (rc = do_221_1b(X, Y, Z, st))) return rc;
   if (on[T222PH] && (rc = do_ph(X, Y, Z, prec, st))) return rc;
   return IMSRG_OK;
 }

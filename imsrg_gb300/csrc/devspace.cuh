@@ -20,8 +20,8 @@ struct DevSpace {
   const int* ob_start;  // one-body channel of each orbit: ob_list[ob_start[i] .. +ob_count[i])
   const int* ob_count;
   const int* ob_list;
-  const int* ketJ_loc;  // [ket * NJ + J] -> local index in the 2b channel (J, parity, Tz of the ket)
-  const int* ccJ_loc;   // [ket * NJ + J] -> local index in the CC channel (J, parity, |dTz|)
+  const int* ketJ_loc;  // [J * nkets + ket] -> local index in the 2b channel (J, parity, Tz of the ket)
+  const int* ccJ_loc;   // [J * nkets + ket] -> local index in the CC channel (J, parity, |dTz|)
   const int* ch_n;      // kets per 2b channel
   const long long* ch_off;  // arena offset per 2b channel
   const int* ch_kofs;   // start of the channel's kets in ket_p / ket_q
@@ -97,8 +97,9 @@ __device__ __forceinline__ double dev_tbme_J_norm(const DevSpace& S, const doubl
   if (((la + lb + lc + ld) & 1) || (ta + tb != tc + td)) return 0.0;
   int kb = ket_index(S.norb, a < b ? a : b, a < b ? b : a);
   int kk = ket_index(S.norb, c < d ? c : d, c < d ? d : c);
-  int bi = __ldg(S.ketJ_loc + kb * S.NJ + J);
-  int ki = __ldg(S.ketJ_loc + kk * S.NJ + J);
+  if (J >= S.NJ) return 0.0;
+  int bi = __ldg(S.ketJ_loc + J * S.nkets + kb);
+  int ki = __ldg(S.ketJ_loc + J * S.nkets + kk);
   if (bi < 0 || ki < 0) return 0.0;
   int ch = chan_index(J, (la + lb) & 1, (ta + tb) / 2);
   int n = __ldg(S.ch_n + ch);

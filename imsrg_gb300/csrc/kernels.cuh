@@ -25,7 +25,7 @@ cudaError_t launch_comm220(const Space& s, const double* X, const double* Y, dou
 cudaError_t launch_comm121(const Space& s, const int* dev_holes, const double* X, const double* Y, double* Z, int hZ,
                            cudaStream_t st);
 cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, double* Z, int hX, int hZ,
-                              cudaStream_t st);
+                              const double* Mz, cudaStream_t st);
 cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, double* Z, double* W2, int hZ,
                            const int* sym_tiles, int nsym_tiles, cudaStream_t st);
 cudaError_t launch_pandya_fwd(const Space& s, const double* X, const double* Y, int hY, double* Xb, double* Yt,

@@ -150,8 +150,11 @@ __device__ __forceinline__ double warp_dot_list(const double* a, const double* b
   return warp_sum(d);
 }
 
+// With Mz != nullptr, Mz holds the two-body blocks of Mpp - Mhh (symmetrised),
+// i.e. exactly what the ladder product added to a zeroed Z, and
+// Mpp = Mz + Mhh needs only the short hh dot products.
 __global__ void k_comm221_1b(DevSpace S, DevWork W, const double* __restrict__ X, const double* __restrict__ Y,
-                             double* __restrict__ Z, int hX, int hZ)
+                             double* __restrict__ Z, int hX, int hZ, const double* __restrict__ Mz)
 {
   int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   int lane = threadIdx.x & 31;
@@ -166,7 +169,7 @@ __global__ void k_comm221_1b(DevSpace S, DevWork W, const double* __restrict__ X
   int kci = ket_index(N, min(c, i), max(c, i)), kcj = ket_index(N, min(c, j), max(c, j));
   double z = 0.0;
   for (int J = Jmin; J <= Jmax; ++J) {
-    int r = S.ketJ_loc[kci * S.NJ + J], s = S.ketJ_loc[kcj * S.NJ + J];
+    int r = S.ketJ_loc[J * S.nkets + kci], s = S.ketJ_loc[J * S.nkets + kcj];
     if (r < 0 || s < 0) continue;
     int ch = chan_index(J, par, tz);
     int n = S.ch_n[ch];
@@ -182,20 +185,29 @@ __global__ void k_comm221_1b(DevSpace S, DevWork W, const double* __restrict__ X
     if (c == i) nrm *= kSqrt2;
     if (c == j) nrm *= kSqrt2;
     double fac = (2 * J + 1) * ph * nrm;
-    if (fabs(nc) > 1e-9) {
-      const double* w = W.ket_wpp + S.ch_kofs[ch];
-      double m_rs = hX * warp_dot_w(xr, ys, w, n, lane);
-      double m_sr = (r == s) ? m_rs : hX * warp_dot_w(xs, yr, w, n, lane);
-      z += fac * nc * (m_rs + hZ * m_sr);
-    }
-    if (fabs(nbarc) > 1e-9) {
+    const bool need_pp = fabs(nc) > 1e-9, need_hh = fabs(nbarc) > 1e-9;
+    double mhh = 0.0;
+    if (need_hh || (need_pp && Mz)) {
       const double* w = W.ket_nn + S.ch_kofs[ch];
       const int* hh = W.hh_list + W.hh_off[ch];
       int nhh = W.hh_off[ch + 1] - W.hh_off[ch];
       double m_rs = hX * warp_dot_list(xr, ys, w, hh, nhh, lane);
       double m_sr = (r == s) ? m_rs : hX * warp_dot_list(xs, yr, w, hh, nhh, lane);
-      z += fac * nbarc * (m_rs + hZ * m_sr);
+      mhh = m_rs + hZ * m_sr;
     }
+    if (need_pp) {
+      double mpp;
+      if (Mz) {
+        mpp = Mz[off + (long long)s * n + r] + mhh;
+      } else {
+        const double* w = W.ket_wpp + S.ch_kofs[ch];
+        double m_rs = hX * warp_dot_w(xr, ys, w, n, lane);
+        double m_sr = (r == s) ? m_rs : hX * warp_dot_w(xs, yr, w, n, lane);
+        mpp = m_rs + hZ * m_sr;
+      }
+      z += fac * nc * mpp;
+    }
+    if (need_hh) z += fac * nbarc * mhh;
   }
   if (lane == 0 && z != 0.0) {
     double v = z / (ji + 1.0);
@@ -309,7 +321,7 @@ __global__ void k_pandya_fwd(DevSpace S, DevWork W, const double* __restrict__ X
       for (int J = jmin; J <= jmax; J += dJ) {
         double sj = dev_sixj(S, ja, jb, Jcc, jc, jd, J);
         if (fabs(sj) < 1e-8) continue;
-        int bi = S.ketJ_loc[k1 * S.NJ + J], ki = S.ketJ_loc[k2 * S.NJ + J];
+        int bi = S.ketJ_loc[J * S.nkets + k1], ki = S.ketJ_loc[J * S.nkets + k2];
         if (bi < 0 || ki < 0) continue;
         int ch = chan_index(J, par, tz);
         int n = S.ch_n[ch];
@@ -387,8 +399,8 @@ __global__ void __launch_bounds__(256) k_pandya_inv(DevSpace S, DevWork W, const
           if (fabs(sj) < 1e-8) continue;
           int cc = chan_index(Jp, par, tz);
           int ncc = S.cc_n[cc];
-          int il = S.ccJ_loc[kil * S.NJ + Jp] + (i > l ? ncc : 0);
-          int kj = S.ccJ_loc[kkj * S.NJ + Jp] + (k > j ? ncc : 0);
+          int il = S.ccJ_loc[Jp * S.nkets + kil] + (i > l ? ncc : 0);
+          int kj = S.ccJ_loc[Jp * S.nkets + kkj] + (k > j ? ncc : 0);
           commij -= (2 * Jp + 1) * sj * Zb[W.zb_off[cc] + (long long)kj * ncc + il];
         }
       }
@@ -409,8 +421,8 @@ __global__ void __launch_bounds__(256) k_pandya_inv(DevSpace S, DevWork W, const
           if (fabs(sj) < 1e-8) continue;
           int cc = chan_index(Jp, par, tz);
           int ncc = S.cc_n[cc];
-          int ik = S.ccJ_loc[kik * S.NJ + Jp];
-          int lj = S.ccJ_loc[klj * S.NJ + Jp];
+          int ik = S.ccJ_loc[Jp * S.nkets + kik];
+          int lj = S.ccJ_loc[Jp * S.nkets + klj];
           // Zbar(ik, lj[+n]) read as its symmetric partner Zbar(lj, ik[+n])
           long long e = W.zb_off[cc] + (long long)(ik + (l > j ? ncc : 0)) * ncc + lj;
           commji -= (2 * Jp + 1) * sj * tsign * Zb[e];
@@ -529,11 +541,11 @@ cudaError_t launch_comm121(const Space& s, const int* dev_holes, const double* X
 }
 
 cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, double* Z, int hX, int hZ,
-                              cudaStream_t st)
+                              const double* Mz, cudaStream_t st)
 {
   if (s.work.n221 == 0) return cudaSuccess;
   int wpb = 8;
-  k_comm221_1b<<<(s.work.n221 + wpb - 1) / wpb, 32 * wpb, 0, st>>>(s.dev, s.work, X, Y, Z, hX, hZ);
+  k_comm221_1b<<<(s.work.n221 + wpb - 1) / wpb, 32 * wpb, 0, st>>>(s.dev, s.work, X, Y, Z, hX, hZ, Mz);
   count_launch();
   return cudaGetLastError();
 }

@@ -119,7 +119,7 @@ Space* build_space(int emax, const std::vector<int>& n, const std::vector<int>& 
         bool lp = occ[p] < OCC_CUT, lq = occ[q] < OCC_CUT;
         if (!(p == q && J % 2 != 0) && tz2[p] + tz2[q] == 2 * Tz) {
           int loc = C.n();
-          s.ketJ_loc[(size_t)k * s.NJ + J] = loc;
+          s.ketJ_loc[(size_t)J * s.nkets + k] = loc;
           C.p.push_back(p);
           C.q.push_back(q);
           if (lp && lq) C.pp.push_back(loc);
@@ -128,7 +128,7 @@ Space* build_space(int emax, const std::vector<int>& n, const std::vector<int>& 
         }
         if (std::abs(tz2[p] - tz2[q]) == 2 * Tz) {
           int loc = K.n();
-          s.ccJ_loc[(size_t)k * s.NJ + J] = loc;
+          s.ccJ_loc[(size_t)J * s.nkets + k] = loc;
           K.p.push_back(p);
           K.q.push_back(q);
           if (lp && lq) K.pp.push_back(loc);
@@ -272,7 +272,7 @@ Space* build_space(int emax, const std::vector<int>& n, const std::vector<int>& 
       int first = (int)s.it122_loc.size();
       for (int k = 0; k < s.ob_count[i]; ++k) {
         int a = s.ob_list[s.ob_start[i] + k];
-        int loc = s.ketJ_loc[(size_t)ket_index(s.norb, std::min(a, j), std::max(a, j)) * s.NJ + J];
+        int loc = s.ketJ_loc[(size_t)J * s.nkets + ket_index(s.norb, std::min(a, j), std::max(a, j))];
         if (loc < 0) continue;
         double f = a > j ? flip : (a == j ? SQ2 : 1.0);
         if (i == j) f = f / SQ2 * 2.0;
@@ -284,7 +284,7 @@ Space* build_space(int emax, const std::vector<int>& n, const std::vector<int>& 
       if (i != j)
         for (int k = 0; k < s.ob_count[j]; ++k) {
           int a = s.ob_list[s.ob_start[j] + k];
-          int loc = s.ketJ_loc[(size_t)ket_index(s.norb, std::min(a, i), std::max(a, i)) * s.NJ + J];
+          int loc = s.ketJ_loc[(size_t)J * s.nkets + ket_index(s.norb, std::min(a, i), std::max(a, i))];
           if (loc < 0) continue;
           double f = i > a ? flip : (i == a ? SQ2 : 1.0);
           s.it122_loc.push_back(loc);

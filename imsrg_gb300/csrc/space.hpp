@@ -41,8 +41,8 @@ struct Space {
   std::vector<int> ob_start, ob_count, ob_list;  // one-body channel members of each orbit
   // ---- channels
   std::vector<Chan> ch, cc;
-  std::vector<int> ketJ_loc;  // [ket * NJ + J] -> local index in 2b channel, -1
-  std::vector<int> ccJ_loc;   // [ket * NJ + J] -> local index in CC channel, -1
+  std::vector<int> ketJ_loc;  // [J * nkets + ket] -> local index in 2b channel, -1
+  std::vector<int> ccJ_loc;   // [J * nkets + ket] -> local index in CC channel, -1
   int64_t arena = 0;
   // ---- 6j table (compact, see sixj.cpp)
   int d1 = 0;
