@@ -94,6 +94,7 @@ struct imsrg_space {
   std::vector<double> h_norm_partial;
   // scratch
   double *d_xb = nullptr, *d_yt = nullptr, *d_yf = nullptr, *d_zb = nullptr, *d_w2 = nullptr;
+  float2 *d_xf = nullptr, *d_yff = nullptr;  // (hi, lo) copies of X and Y for the double-float comm122ss
   int* d_status = nullptr;
   // split-precision plans
   SplitPlan* split_ladder = nullptr;
@@ -317,12 +318,25 @@ int do_121(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
   return IMSRG_OK;
 }
 
-int do_122(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
+// FP64 form: FP64 gathers (the plain form keeps every term in FP64).
+// Split form: the same gathers in double-float on the FP32 pipe.
+int do_122(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st, int prec = IMSRG_PREC_FP64)
 {
   imsrg_space* sp = X->sp;
   int rc = ensure_scratch(sp, false, true);
   if (rc) return rc;
   ProfScope ps("comm122ss", st);
+  if (prec == IMSRG_PREC_SPLIT) {
+    try {
+      if (!sp->d_xf) sp->d_xf = sp->track(dmalloc<float2>(sp->s->arena));
+      if (!sp->d_yff) sp->d_yff = sp->track(dmalloc<float2>(sp->s->arena));
+    } catch (std::exception&) {
+      return fail(IMSRG_ERR_NOMEM, "comm122ss double-float scratch");
+    }
+    CUDA_TRY(launch_comm122_df(*sp->s, X->d, Y->d, Z->d, sp->d_xf, sp->d_yff, (float2*)sp->d_w2, Z->herm,
+                               sp->d_sym122, sp->n_sym122, st));
+    return IMSRG_OK;
+  }
   CUDA_TRY(launch_comm122(*sp->s, X->d, Y->d, Z->d, sp->d_w2, Z->herm, sp->d_sym122, sp->n_sym122, st));
   return IMSRG_OK;
 }
@@ -359,7 +373,9 @@ int ensure_split(imsrg_space* sp)
   return IMSRG_OK;
 }
 
-int do_ladder(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStream_t st)
+// overwrite: Z2 is known to be zero (fresh commutator), so the split product
+// writes its blocks instead of read-modify-write
+int do_ladder(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStream_t st, bool overwrite = false)
 {
   imsrg_space* sp = X->sp;
   Space& s = *sp->s;
@@ -367,6 +383,7 @@ int do_ladder(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaS
   if (prec == IMSRG_PREC_SPLIT) {
     int rc = ensure_split(sp);
     if (rc) return rc;
+    split_plan_set_accumulate(sp->split_ladder, overwrite ? 0 : -1);
     CUDA_TRY(launch_symgemm_split(sp->split_ladder, X->d, Y->d, Y->d, Z->d, s.work.kidx, s.work.kweight,
                                   s.work.phase_tab, sp->d_status, Z->herm, (double)Y->herm, st));
     return IMSRG_OK;
@@ -426,12 +443,12 @@ int commutator_impl(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec,
   // instead of recomputing the pp dot products (ConstructScalarMpp_Mhh is
   // shared the same way by the reference's comm222_pp_hh_221ss).
   bool ladder_first = on[T222PPHH];
-  if (ladder_first && (rc = do_ladder(X, Y, Z, prec, st))) return rc;
+  if (ladder_first && (rc = do_ladder(X, Y, Z, prec, st, true))) return rc;
   if (on[T221] && (rc = do_221_1b(X, Y, Z, st, ladder_first ? Z->d : nullptr))) return rc;
   if ((rc = do_111_110(X, Y, Z, on[T111], on[T110], st))) return rc;
   if (on[T220] && (rc = do_220(X, Y, Z, st))) return rc;
   if (on[T121] && (rc = do_121(X, Y, Z, st))) return rc;
-  if (on[T122] && (rc = do_122(X, Y, Z, st))) return rc;
+  if (on[T122] && (rc = do_122(X, Y, Z, st, prec))) return rc;
   if (on[T222PH] && (rc = do_ph(X, Y, Z, prec, st))) return rc;
   return IMSRG_OK;
 }

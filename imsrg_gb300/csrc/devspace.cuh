@@ -33,6 +33,10 @@ struct DevSpace {
   const int* cc_q;
   const int* sixj_base;  // [((a*d1+b)*d1+c)*d1+d] -> offset into sixj_val
   const double* sixj_val;
+  // (2 J6 + 1) {...}, exactly 0 where |{...}| < 1e-8: the weight of every
+  // Pandya recoupling sum (both cut and factor are the reference's,
+  // src/Commutator.cc:1456-1462, 1579-1583)
+  const double* sixj_wval;
 };
 
 // Device copies of the per-kernel work lists (built once per space).
@@ -85,6 +89,19 @@ __device__ __forceinline__ double dev_sixj(const DevSpace& S, int jj1, int jj2, 
 {
   int s = sixj_slot(S.d1, S.sixj_base, jj1, jj2, J3, jj4, jj5, J6);
   return s < 0 ? 0.0 : __ldg(S.sixj_val + s);
+}
+
+// (2 J6 + 1) {jj1/2 jj2/2 J3; jj4/2 jj5/2 J6}, 0 when the reference skips it
+__device__ __forceinline__ double dev_sixj_w(const DevSpace& S, int jj1, int jj2, int J3, int jj4, int jj5, int J6)
+{
+  int s = sixj_slot(S.d1, S.sixj_base, jj1, jj2, J3, jj4, jj5, J6);
+  return s < 0 ? 0.0 : __ldg(S.sixj_wval + s);
+}
+
+__device__ __forceinline__ bool dzero(double v) { return (__double_as_longlong(v) << 1) == 0; }
+__device__ __forceinline__ double dneg_if(double v, bool neg)
+{
+  return __longlong_as_double(__double_as_longlong(v) ^ (neg ? (long long)0x8000000000000000ull : 0ll));
 }
 
 // Normalised J-coupled matrix element of a scalar operator arena, with the

@@ -28,6 +28,8 @@ cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, 
                               const double* Mz, cudaStream_t st);
 cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, double* Z, double* W2, int hZ,
                            const int* sym_tiles, int nsym_tiles, cudaStream_t st);
+cudaError_t launch_comm122_df(const Space& s, const double* X, const double* Y, double* Z, float2* Xf, float2* Yf,
+                              float2* W2, int hZ, const int* sym_tiles, int nsym_tiles, cudaStream_t st);
 cudaError_t launch_pandya_fwd(const Space& s, const double* X, const double* Y, int hY, double* Xb, double* Yt,
                               double* Yf, const int* tiles, int ntiles, cudaStream_t st);
 cudaError_t launch_pandya_inv(const Space& s, const double* Zb, double* Z, int hZ, const int* tiles, int ntiles,
@@ -47,6 +49,8 @@ cudaError_t launch_symgemm_fp64(const GemmJobDev* jobs, const int* pairs, int np
 struct SplitPlan;
 SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs, int family);
 void split_plan_destroy(SplitPlan* p);
+// -1: each job's own accumulate flag; 0: overwrite the output; 1: accumulate
+void split_plan_set_accumulate(SplitPlan* p, int mode);
 cudaError_t launch_symgemm_split(SplitPlan* p, const double* A, const double* B0, const double* B1, double* O,
                                  const int* kidx, const double* kw, const int* phase, int* dev_status, int gsign,
                                  double gbscale, cudaStream_t st);

@@ -93,6 +93,7 @@ struct SplitPlan {
   int grid = 0;
   size_t smem = 0;
   int nstages = 0;
+  int accum_override = -1;
 };
 
 // ----------------------------------------------------------------- device
@@ -282,6 +283,19 @@ __global__ void __launch_bounds__(256) k_split_rowexp(const SplitJob* __restrict
   }
 }
 
+// integer value of an integer-valued float (|f| < 2^31), integer instructions
+// only (the float-to-int conversion instruction shares the slow FP64 pipe)
+__device__ __forceinline__ int f2i_exact(float f)
+{
+  unsigned b = __float_as_uint(f);
+  int e = (int)((b >> 23) & 0xFFu);
+  if (e < 127) return 0;  // |f| < 1: zero for an integer-valued float
+  int m = (int)((b & 0x7FFFFFu) | 0x800000u);
+  int sh = e - 150;
+  int v = sh >= 0 ? (m << sh) : (m >> (-sh));
+  return (b >> 31) ? -v : v;
+}
+
 // signed 64-bit integer times 2^X as a double, integer instructions only
 // (round to nearest even); 0 on underflow of the exponent range.
 __device__ __forceinline__ double i64_ldexp(long long v, int X)
@@ -438,6 +452,7 @@ struct GemmArgs {
   double* out;
   int* status;
   int S, beta, nstages, gsign;
+  int accum;  // -1: each job's flag; 0: overwrite; 1: accumulate
 };
 
 template <int S>
@@ -631,16 +646,16 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
           wd[cc] = rowok && j < jb.m && !(tl.diag && i > j);
           wm[cc] = wd[cc] && i != j;
           // exact merge of the weight groups: Horner in base 2^beta
-          long long I64 = __float2int_rn(__uint_as_float(r[0][cc]));
+          long long I64 = f2i_exact(__uint_as_float(r[0][cc]));
 #pragma unroll
           for (int gidx = 1; gidx < S; ++gidx)
-            I64 = I64 * (1ll << g.beta) + __float2int_rn(__uint_as_float(r[gidx][cc]));
+            I64 = I64 * (1ll << g.beta) + f2i_exact(__uint_as_float(r[gidx][cc]));
           v[cc] = i64_ldexp(I64, Xi + s_colexp[c0 + cc]);
           mv[cc] = (sign * phi_i * s_colph[c0 + cc]) < 0 ? -v[cc] : v[cc];
           od[cc] = 0.0;
           om[cc] = 0.0;
         }
-        if (jb.accumulate) {
+        if (g.accum > 0 || (g.accum < 0 && jb.accumulate)) {
 #pragma unroll
           for (int cc = 0; cc < EPI_COLS; ++cc) {
             const long long j = tl.J * TILE_N + c0 + cc;
@@ -906,12 +921,15 @@ static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, con
     ga.beta = p->beta;
     ga.nstages = p->nstages;
     ga.gsign = gsign;
+    ga.accum = p->accum_override;
     k_split_gemm<S><<<p->grid, THREADS, p->smem, st>>>(p->maps[0], p->maps[1], p->maps[2], p->maps[3], ga);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
+
+void split_plan_set_accumulate(SplitPlan* p, int mode) { p->accum_override = mode; }
 
 cudaError_t launch_symgemm_split(SplitPlan* p, const double* A, const double* B0, const double* B1, double* O,
                                  const int* kidx, const double* kw, const int* phase, int* dev_status, int gsign,

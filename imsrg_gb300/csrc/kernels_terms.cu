@@ -216,9 +216,206 @@ __global__ void k_comm221_1b(DevSpace S, DevWork W, const double* __restrict__ X
   }
 }
 
+// ------------------------------------------------ double-float arithmetic
+// FP64 runs at 1/57 of the FP32 rate on this part, so the gather-heavy
+// comm122ss product is evaluated in double-float arithmetic on the FP32 pipe
+// (Dekker / Knuth error-free transformations; about 2^-44 relative per term).
+// The conversions to and from the (hi, lo) pairs use integer instructions.
+
+// v -> (hi, lo): hi = v truncated to 24 bits, lo = the remaining 29 bits rounded
+// to 24; values below the float range give 0 (far below the tolerance).
+__device__ __forceinline__ float2 d2ff(double v)
+{
+  long long b = __double_as_longlong(v);
+  unsigned sgn = (unsigned)((unsigned long long)b >> 63) << 31;
+  int e = (int)((b >> 52) & 0x7FF);
+  int fe = e - 1023 + 127;
+  if (e == 0 || fe <= 0) return make_float2(0.f, 0.f);
+  if (fe >= 255) return make_float2(__uint_as_float(sgn | 0x7F800000u), 0.f);
+  unsigned long long m = (unsigned long long)b & 0xFFFFFFFFFFFFFull;
+  float hi = __uint_as_float(sgn | ((unsigned)fe << 23) | (unsigned)(m >> 29));
+  unsigned r = (unsigned)(m & 0x1FFFFFFFull);
+  float lo = 0.f;
+  if (r) {
+    int p = 31 - __clz(r);
+    int le = fe - 52 + p;
+    if (le > 0) {
+      unsigned mant = p >= 23 ? (r >> (p - 23)) : (r << (23 - p));
+      lo = __uint_as_float(sgn | ((unsigned)le << 23) | (mant & 0x7FFFFFu));
+    }
+  }
+  return make_float2(hi, lo);
+}
+
+// exact float -> double by exponent re-bias (zero / subnormal -> 0)
+__device__ __forceinline__ double f2d(float f)
+{
+  unsigned b = __float_as_uint(f);
+  unsigned e = (b >> 23) & 0xFFu;
+  if (e == 0) return 0.0;
+  unsigned long long db = ((unsigned long long)(b >> 31) << 63) | ((unsigned long long)(e - 127 + 1023) << 52) |
+                          ((unsigned long long)(b & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)db);
+}
+
+// (s, c) += a * b in double-float
+__device__ __forceinline__ void df_fma(float2 a, float2 b, float& s, float& c)
+{
+  float p = __fmul_rn(a.x, b.x);
+  float e = __fmaf_rn(a.x, b.x, -p);
+  e = __fmaf_rn(a.x, b.y, e);
+  e = __fmaf_rn(a.y, b.x, e);
+  float t = __fadd_rn(s, p);
+  float z = __fsub_rn(t, s);
+  float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+  s = t;
+  c = __fadd_rn(c, __fadd_rn(err, e));
+}
+
+// FP64 arena -> (hi, lo) pairs, integer instructions only
+__global__ void k_to_ff(const double* __restrict__ src, float2* __restrict__ dst, long long n)
+{
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) dst[i] = d2ff(src[i]);
+}
+
 // ---------------------------------------------------------------------- 122
 // comm122ss, src/Commutator.cc:837-932.  W2(:, ij) = sum_items f (Y2(:,loc) X1(a,src)
-// - X2(:,loc) Y1(a,src)); one block per column, threads over rows.
+// - X2(:,loc) Y1(a,src)); one block per column, threads over rows, in
+// double-float arithmetic from (hi, lo) copies of X2 and Y2; W2 is stored as
+// (hi, lo) pairs.
+__global__ void __launch_bounds__(128) k_comm122_w_df(DevSpace S, DevWork W, const double* __restrict__ X,
+                                                      const double* __restrict__ Y, const float2* __restrict__ Xf,
+                                                      const float2* __restrict__ Yf, float2* __restrict__ W2)
+{
+  __shared__ float2 cx[32], cy[32];
+  __shared__ int cl[32];
+  int col = blockIdx.x;
+  if (col >= W.ncols122) return;
+  int ch = W.cols122[4 * col], ij = W.cols122[4 * col + 1];
+  int first = W.cols122[4 * col + 2], cnt = min(W.cols122[4 * col + 3], 32);
+  int n = S.ch_n[ch];
+  long long off = S.ch_off[ch];
+  int N = S.norb;
+  if (threadIdx.x < cnt) {
+    int t = threadIdx.x;
+    int a = W.it122_a[first + t], src = W.it122_src[first + t];
+    double f = W.it122_f[first + t];
+    cx[t] = d2ff(X[32 + (size_t)src * N + a] * f);   //  X1(a,src) f multiplies Y2
+    cy[t] = d2ff(-Y[32 + (size_t)src * N + a] * f);  // -Y1(a,src) f multiplies X2
+    cl[t] = W.it122_loc[first + t];
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    float s = 0.f, c = 0.f;
+    for (int t = 0; t < cnt; ++t) {
+      long long e = off + (long long)cl[t] * n + r;
+      df_fma(cx[t], Yf[e], s, c);
+      df_fma(cy[t], Xf[e], s, c);
+    }
+    float hi = __fadd_rn(s, c);
+    float lo = __fsub_rn(c, __fsub_rn(hi, s));
+    W2[off + (long long)ij * n + r] = make_float2(hi, lo);
+  }
+}
+
+// Z2 -= W2 + hZ W2^T with W2 in (hi, lo) pairs, per channel in 32x32 tiles
+__global__ void k_sym_subtract_ff(DevSpace S, const float2* __restrict__ W2, double* __restrict__ Z, int hZ,
+                                  const int* __restrict__ tiles, int ntiles)
+{
+  __shared__ double tt[32][33];
+  int t = blockIdx.x;
+  if (t >= ntiles) return;
+  int ch = tiles[3 * t], ti = tiles[3 * t + 1], tj = tiles[3 * t + 2];
+  int n = S.ch_n[ch];
+  long long off = S.ch_off[ch];
+  int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int yy = ty; yy < 32; yy += 8) {
+    int r = tj * 32 + tx, c = ti * 32 + yy;
+    double v = 0.0;
+    if (r < n && c < n) {
+      float2 w = W2[off + (long long)c * n + r];
+      v = f2d(w.x) + f2d(w.y);
+    }
+    tt[yy][tx] = v;
+  }
+  __syncthreads();
+  for (int yy = ty; yy < 32; yy += 8) {
+    int r = ti * 32 + tx, c = tj * 32 + yy;
+    if (r < n && c < n) {
+      float2 w = W2[off + (long long)c * n + r];
+      double v = f2d(w.x) + f2d(w.y);
+      Z[off + (long long)c * n + r] -= v + hZ * tt[tx][yy];
+    }
+  }
+}
+
+// Same one-body part when Mpp - Mhh is already in Mz (the ladder product added
+// to a zeroed Z): one warp per (i <= j) pair, lanes over c; each lane forms the
+// short Mhh dot products (hh kets only) itself, so the warp reduces once.
+__global__ void k_comm221_1b_mz(DevSpace S, DevWork W, const double* __restrict__ X, const double* __restrict__ Y,
+                                double* __restrict__ Z, int hX, int hZ, const double* __restrict__ Mz)
+{
+  int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  if (item >= W.npairs1b) return;
+  const int i = W.pairs1b[2 * item], j = W.pairs1b[2 * item + 1];
+  const int N = S.norb;
+  const int ji = S.j2[i], jj = S.j2[j];
+  double z = 0.0;
+  for (int c = lane; c < N; c += 32) {
+    const double nc = S.occ[c], nbarc = 1.0 - nc;
+    const bool need_pp = fabs(nc) > 1e-9, need_hh = fabs(nbarc) > 1e-9;
+    const int jc = S.j2[c];
+    const int Jmin = max(abs(jc - ji), abs(jc - jj)) / 2;
+    const int Jmax = (jc + min(ji, jj)) / 2;
+    const int par = (S.l[c] + S.l[i]) & 1, tz = (S.tz2[c] + S.tz2[i]) / 2;
+    const int kci = ket_index(N, min(c, i), max(c, i)), kcj = ket_index(N, min(c, j), max(c, j));
+    for (int J = Jmin; J <= Jmax; ++J) {
+      int r = S.ketJ_loc[J * S.nkets + kci], s = S.ketJ_loc[J * S.nkets + kcj];
+      if (r < 0 || s < 0) continue;
+      int ch = chan_index(J, par, tz);
+      int n = S.ch_n[ch];
+      long long off = S.ch_off[ch];
+      const double* xr = X + off + (long long)r * n;
+      const double* xs = X + off + (long long)s * n;
+      const double* yr = Y + off + (long long)r * n;
+      const double* ys = Y + off + (long long)s * n;
+      const double* w = W.ket_nn + S.ch_kofs[ch];
+      const int* hh = W.hh_list + W.hh_off[ch];
+      const int nhh = W.hh_off[ch + 1] - W.hh_off[ch];
+      double m_rs = 0.0, m_sr = 0.0;
+      for (int t = 0; t < nhh; ++t) {
+        int k = hh[t];
+        double wk = w[k];
+        m_rs = fma(xr[k] * wk, ys[k], m_rs);
+        m_sr = fma(xs[k] * wk, yr[k], m_sr);
+      }
+      if (r == s) m_sr = m_rs;
+      double mhh = hX * (m_rs + hZ * m_sr);
+      double ph = 1.0;
+      if (c > i) ph *= iphase((jc + ji) / 2 + 1 + J);
+      if (c > j) ph *= iphase((jc + jj) / 2 + 1 + J);
+      double nrm = 1.0;
+      if (c == i) nrm *= kSqrt2;
+      if (c == j) nrm *= kSqrt2;
+      double fac = (2 * J + 1) * ph * nrm;
+      if (need_pp) z += fac * nc * (Mz[off + (long long)s * n + r] + mhh);
+      if (need_hh) z += fac * nbarc * mhh;
+    }
+  }
+  z = warp_sum(z);
+  if (lane == 0) {
+    double v = z / (ji + 1.0);
+    Z[32 + (size_t)j * N + i] += v;
+    if (i != j) Z[32 + (size_t)i * N + j] += hZ * v;
+  }
+}
+
+// ---------------------------------------------------------------------- 122
+// comm122ss, src/Commutator.cc:837-932.  W2(:, ij) = sum_items f (Y2(:,loc) X1(a,src)
+// - X2(:,loc) Y1(a,src)); one block per column, threads over rows (FP64).
 __global__ void k_comm122_w(DevSpace S, DevWork W, const double* __restrict__ X, const double* __restrict__ Y,
                             double* __restrict__ W2)
 {
@@ -318,27 +515,29 @@ __global__ void k_pandya_fwd(DevSpace S, DevWork W, const double* __restrict__ X
       int k1 = ket_index(S.norb, min(c, b), max(c, b));
       int k2 = ket_index(S.norb, min(a, d), max(a, d));
       int par = (lc + lb) & 1, tz = (S.tz2[c] + S.tz2[b]) / 2;
+      // (2J+1) 6j from the weighted table (0 where the reference skips |6j| < 1e-8);
+      // the swap phases are sign flips: one FP64 FMA per operand and J
+      const int pcb = (c > b) ? ((S.j2[c] + S.j2[b]) / 2 + 1) : 0;
+      const int pad = (a > d) ? ((S.j2[a] + S.j2[d]) / 2 + 1) : 0;
       for (int J = jmin; J <= jmax; J += dJ) {
-        double sj = dev_sixj(S, ja, jb, Jcc, jc, jd, J);
-        if (fabs(sj) < 1e-8) continue;
+        double w = dev_sixj_w(S, ja, jb, Jcc, jc, jd, J);
+        if (dzero(w)) continue;
         int bi = S.ketJ_loc[J * S.nkets + k1], ki = S.ketJ_loc[J * S.nkets + k2];
         if (bi < 0 || ki < 0) continue;
         int ch = chan_index(J, par, tz);
         int n = S.ch_n[ch];
         long long e = S.ch_off[ch] + (long long)ki * n + bi;
-        double ph = 1.0;
-        if (c > b) ph *= iphase((S.j2[c] + S.j2[b]) / 2 + 1 + J);
-        if (a > d) ph *= iphase((S.j2[a] + S.j2[d]) / 2 + 1 + J);
-        double coef = (2 * J + 1) * sj * ph;
-        xbar -= coef * X[e];
-        ybar -= coef * Y[e] * hY;
+        bool neg = ((c > b) && ((pcb + J) & 1)) != ((a > d) && ((pad + J) & 1));
+        double wx = dneg_if(w, !neg);  // accumulate -(2J+1) 6j ph
+        xbar = fma(wx, X[e], xbar);
+        ybar = fma(wx, Y[e], ybar);
       }
     }
   }
   double na_nb = S.occ[a] - S.occ[b];
   long long base = W.xb_off[cc];
-  Xb[base + (long long)t * ncc + ik] = xbar * nf * na_nb;
-  double yv = ybar * nf;
+  Xb[base + (long long)t * ncc + ik] = xbar * (nf * na_nb);
+  double yv = dneg_if(ybar * nf, hY < 0);
   Yt[base + (long long)t * ncc + ik] = yv;
   const int* phi = W.phase_tab + W.cc_phase_off[cc];
   int tf = t < nph ? t + nph : t - nph;
@@ -395,13 +594,13 @@ __global__ void __launch_bounds__(256) k_pandya_inv(DevSpace S, DevWork W, const
         int Jpmax = min(jji + jjl, jjk + jjj) / 2;
         int kil = ket_index(N, min(i, l), max(i, l)), kkj = ket_index(N, min(j, k), max(j, k));
         for (int Jp = Jpmin; Jp <= Jpmax; ++Jp) {
-          double sj = dev_sixj(S, jji, jjj, J, jjk, jjl, Jp);
-          if (fabs(sj) < 1e-8) continue;
+          double w = dev_sixj_w(S, jji, jjj, J, jjk, jjl, Jp);  // (2J'+1) 6j
+          if (dzero(w)) continue;
           int cc = chan_index(Jp, par, tz);
           int ncc = S.cc_n[cc];
           int il = S.ccJ_loc[Jp * S.nkets + kil] + (i > l ? ncc : 0);
           int kj = S.ccJ_loc[Jp * S.nkets + kkj] + (k > j ? ncc : 0);
-          commij -= (2 * Jp + 1) * sj * Zb[W.zb_off[cc] + (long long)kj * ncc + il];
+          commij = fma(-w, Zb[W.zb_off[cc] + (long long)kj * ncc + il], commij);
         }
       }
       if (k == l) {
@@ -415,22 +614,27 @@ __global__ void __launch_bounds__(256) k_pandya_inv(DevSpace S, DevWork W, const
         int Jpmax = min(jjj + jjl, jjk + jji) / 2;
         int kik = ket_index(N, min(i, k), max(i, k)), klj = ket_index(N, min(l, j), max(l, j));
         // i <= k always (ibra <= iket), so ik is a row of the head/tail blocks
-        double tsign = (l > j) ? (double)iphase((jji + jjk + jjl + jjj) / 2) : (double)hZ;
+        const int tsign = (l > j) ? iphase((jji + jjk + jjl + jjj) / 2) : hZ;
+        double acc = 0.0;
         for (int Jp = Jpmin; Jp <= Jpmax; ++Jp) {
-          double sj = dev_sixj(S, jjj, jji, J, jjk, jjl, Jp);
-          if (fabs(sj) < 1e-8) continue;
+          double w = dev_sixj_w(S, jjj, jji, J, jjk, jjl, Jp);
+          if (dzero(w)) continue;
           int cc = chan_index(Jp, par, tz);
           int ncc = S.cc_n[cc];
           int ik = S.ccJ_loc[Jp * S.nkets + kik];
           int lj = S.ccJ_loc[Jp * S.nkets + klj];
           // Zbar(ik, lj[+n]) read as its symmetric partner Zbar(lj, ik[+n])
           long long e = W.zb_off[cc] + (long long)(ik + (l > j ? ncc : 0)) * ncc + lj;
-          commji -= (2 * Jp + 1) * sj * tsign * Zb[e];
+          acc = fma(-w, Zb[e], acc);
         }
+        commji = dneg_if(acc, tsign < 0);
       }
+      // z = -(commij - (-1)^(jk+jl-J) commji) / norm
       int bd = (i == j), kd = (k == l);
-      double norm = bd == kd ? 1 + bd : kSqrt2;
-      z = -(commij - iphase((jjk + jjl) / 2 - J) * commji) / norm;
+      double inv_norm = bd == kd ? (bd ? 0.5 : 1.0) : 0.70710678118654752440;
+      double d = commij - dneg_if(commji, iphase((jjk + jjl) / 2 - J) < 0);
+      z = dneg_if(d, true);
+      if (bd || kd) z *= inv_norm;
     }
     T[bb][lane] = z;
   }
@@ -545,6 +749,12 @@ cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, 
 {
   if (s.work.n221 == 0) return cudaSuccess;
   int wpb = 8;
+  if (Mz) {
+    // no other kernel writes Z1 concurrently: plain stores per (i, j) pair
+    k_comm221_1b_mz<<<(s.work.npairs1b + 3) / 4, 128, 0, st>>>(s.dev, s.work, X, Y, Z, hX, hZ, Mz);
+    count_launch();
+    return cudaGetLastError();
+  }
   k_comm221_1b<<<(s.work.n221 + wpb - 1) / wpb, 32 * wpb, 0, st>>>(s.dev, s.work, X, Y, Z, hX, hZ, Mz);
   count_launch();
   return cudaGetLastError();
@@ -559,6 +769,23 @@ cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, dou
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_sym_subtract<<<nsym_tiles, 256, 0, st>>>(s.dev, W2, Z, hZ, sym_tiles, nsym_tiles);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_comm122_df(const Space& s, const double* X, const double* Y, double* Z, float2* Xf, float2* Yf,
+                              float2* W2, int hZ, const int* sym_tiles, int nsym_tiles, cudaStream_t st)
+{
+  if (s.work.ncols122 == 0) return cudaSuccess;
+  k_to_ff<<<2432, 256, 0, st>>>(X, Xf, s.arena);
+  count_launch();
+  k_to_ff<<<2432, 256, 0, st>>>(Y, Yf, s.arena);
+  count_launch();
+  k_comm122_w_df<<<s.work.ncols122, 128, 0, st>>>(s.dev, s.work, X, Y, Xf, Yf, W2);
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_sym_subtract_ff<<<nsym_tiles, 256, 0, st>>>(s.dev, W2, Z, hZ, sym_tiles, nsym_tiles);
   count_launch();
   return cudaGetLastError();
 }

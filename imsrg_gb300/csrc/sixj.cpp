@@ -170,6 +170,25 @@ void build_sixj_table(Space& s)
             for (int J6 = J6min; J6 <= J6max; ++J6)
               s.sixj_val[base + (J3 - J3min) * n6 + (J6 - J6min)] = sixj_dd(jj1, jj2, 2 * J3, jj4, jj5, 2 * J6);
         }
+  s.sixj_wval.assign(tot, 0.0);
+  for (int a = 0; a < d1; ++a)
+    for (int b = 0; b < d1; ++b)
+      for (int c = 0; c < d1; ++c)
+        for (int d = 0; d < d1; ++d) {
+          int jj1 = 2 * a + 1, jj2 = 2 * b + 1, jj4 = 2 * c + 1, jj5 = 2 * d + 1;
+          int J3min = std::abs(jj1 - jj2) / 2, J3max = (jj1 + jj2) / 2;
+          int J6min = std::max(std::abs(jj1 - jj5), std::abs(jj4 - jj2)) / 2;
+          int J6max = std::min(jj1 + jj5, jj4 + jj2) / 2;
+          int base = s.sixj_base[((a * d1 + b) * d1 + c) * d1 + d];
+          int n6 = J6max - J6min + 1;
+          if (n6 <= 0) continue;
+          for (int J3 = J3min; J3 <= J3max; ++J3)
+            for (int J6 = J6min; J6 <= J6max; ++J6) {
+              size_t k = base + (J3 - J3min) * n6 + (J6 - J6min);
+              double v = s.sixj_val[k];
+              s.sixj_wval[k] = std::fabs(v) < 1e-8 ? 0.0 : (2 * J6 + 1) * v;
+            }
+        }
 }
 
 double sixj_lookup(const Space& s, int jj1, int jj2, int J3, int jj4, int jj5, int J6)

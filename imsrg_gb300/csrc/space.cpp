@@ -354,6 +354,7 @@ void upload_space(Space& s)
   d.cc_q = dev_copy(s, cq);
   d.sixj_base = dev_copy(s, s.sixj_base);
   d.sixj_val = dev_copy(s, s.sixj_val);
+  d.sixj_wval = dev_copy(s, s.sixj_wval);
 
   DevWork& w = s.work;
   w.ket_wpp = dev_copy(s, s.ket_wpp);

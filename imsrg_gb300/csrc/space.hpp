@@ -48,6 +48,7 @@ struct Space {
   int d1 = 0;
   std::vector<int> sixj_base;
   std::vector<double> sixj_val;
+  std::vector<double> sixj_wval;  // (2 J6 + 1) * value, 0 where |value| < 1e-8
 
   // ---- work lists
   // ladder (comm222_pp_hh): per channel, kets with nonzero weight and weights
