@@ -283,19 +283,6 @@ __global__ void __launch_bounds__(256) k_split_rowexp(const SplitJob* __restrict
   }
 }
 
-// integer value of an integer-valued float (|f| < 2^31), integer instructions
-// only (the float-to-int conversion instruction shares the slow FP64 pipe)
-__device__ __forceinline__ int f2i_exact(float f)
-{
-  unsigned b = __float_as_uint(f);
-  int e = (int)((b >> 23) & 0xFFu);
-  if (e < 127) return 0;  // |f| < 1: zero for an integer-valued float
-  int m = (int)((b & 0x7FFFFFu) | 0x800000u);
-  int sh = e - 150;
-  int v = sh >= 0 ? (m << sh) : (m >> (-sh));
-  return (b >> 31) ? -v : v;
-}
-
 // signed 64-bit integer times 2^X as a double, integer instructions only
 // (round to nearest even); 0 on underflow of the exponent range.
 __device__ __forceinline__ double i64_ldexp(long long v, int X)
@@ -392,18 +379,44 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
       qa = to_fixed(A[(long long)col * jb.lda + i], rowA[r], P);
       qb = to_fixed(scaled(B[(long long)col * jb.ldb + i], sc), rowB[r], P);
     }
+    // digits of |q| by shifts (32-bit digit arithmetic), then the carry that
+    // makes them balanced, then the sign: |d| <= 2^(beta-1) below the top
+    // digit, |d_1| <= 2^beta + 1
+    const unsigned long long ua = (unsigned long long)(qa < 0 ? -qa : qa);
+    const unsigned long long ub = (unsigned long long)(qb < 0 ? -qb : qb);
+    int da[S], db[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const int sh = beta * (S - 1 - s);
+      da[s] = (int)(ua >> sh);
+      db[s] = (int)(ub >> sh);
+      if (s > 0) {
+        da[s] &= (int)mask;
+        db[s] &= (int)mask;
+      } else {
+        da[0] = (int)(ua >> sh);
+        db[0] = (int)(ub >> sh);
+      }
+    }
 #pragma unroll
     for (int s = S - 1; s >= 1; --s) {
-      long long da = ((qa + half) & mask) - half;
-      long long db = ((qb + half) & mask) - half;
-      qa = (qa - da) >> beta;
-      qb = (qb - db) >> beta;
-      // small integer -> bf16 bits (exact): 1.5*2^23 magic
-      dA[s][r][tt] = (unsigned short)(__float_as_uint(__int_as_float(0x4B400000 + (int)da) - 12582912.0f) >> 16);
-      dB[s][r][tt] = (unsigned short)(__float_as_uint(__int_as_float(0x4B400000 + (int)db) - 12582912.0f) >> 16);
+      if (da[s] >= (int)half) {
+        da[s] -= (int)(mask + 1);
+        da[s - 1] += 1;
+      }
+      if (db[s] >= (int)half) {
+        db[s] -= (int)(mask + 1);
+        db[s - 1] += 1;
+      }
     }
-    dA[0][r][tt] = (unsigned short)(__float_as_uint(__int_as_float(0x4B400000 + (int)qa) - 12582912.0f) >> 16);
-    dB[0][r][tt] = (unsigned short)(__float_as_uint(__int_as_float(0x4B400000 + (int)qb) - 12582912.0f) >> 16);
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const int xa = qa < 0 ? -da[s] : da[s];
+      const int xb = qb < 0 ? -db[s] : db[s];
+      // small integer -> bf16 bits (exact): 1.5*2^23 magic
+      dA[s][r][tt] = (unsigned short)(__float_as_uint(__int_as_float(0x4B400000 + xa) - 12582912.0f) >> 16);
+      dB[s][r][tt] = (unsigned short)(__float_as_uint(__int_as_float(0x4B400000 + xb) - 12582912.0f) >> 16);
+    }
   }
   __syncthreads();
   const bool need_g = flags[2 * job] != 0, need_d = flags[2 * job + 1] != 0;
@@ -646,12 +659,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
           wd[cc] = rowok && j < jb.m && !(tl.diag && i > j);
           wm[cc] = wd[cc] && i != j;
           // exact merge of the weight groups: Horner in base 2^beta
-          long long I64 = f2i_exact(__uint_as_float(r[0][cc]));
+          long long I64 = __float2int_rn(__uint_as_float(r[0][cc]));
 #pragma unroll
           for (int gidx = 1; gidx < S; ++gidx)
-            I64 = I64 * (1ll << g.beta) + f2i_exact(__uint_as_float(r[gidx][cc]));
+            I64 = I64 * (1ll << g.beta) + __float2int_rn(__uint_as_float(r[gidx][cc]));
           v[cc] = i64_ldexp(I64, Xi + s_colexp[c0 + cc]);
-          mv[cc] = (sign * phi_i * s_colph[c0 + cc]) < 0 ? -v[cc] : v[cc];
+          mv[cc] = __longlong_as_double(__double_as_longlong(v[cc]) ^
+                                        ((sign * phi_i * s_colph[c0 + cc]) < 0 ? (long long)0x8000000000000000ull
+                                                                                : 0ll));
           od[cc] = 0.0;
           om[cc] = 0.0;
         }
@@ -662,12 +677,20 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
             if (wd[cc]) od[cc] = __ldcg(O + j * jb.ldo + i);
             if (wm[cc]) om[cc] = __ldcg(O + (long long)i * jb.ldo + j);
           }
-        }
 #pragma unroll
-        for (int cc = 0; cc < EPI_COLS; ++cc) {
-          const long long j = tl.J * TILE_N + c0 + cc;
-          if (wd[cc]) O[j * jb.ldo + i] = od[cc] + v[cc];
-          if (wm[cc]) O[(long long)i * jb.ldo + j] = om[cc] + mv[cc];
+          for (int cc = 0; cc < EPI_COLS; ++cc) {
+            const long long j = tl.J * TILE_N + c0 + cc;
+            if (wd[cc]) O[j * jb.ldo + i] = od[cc] + v[cc];
+            if (wm[cc]) O[(long long)i * jb.ldo + j] = om[cc] + mv[cc];
+          }
+        } else {
+          // overwrite: no FP64 add (the FP64 pipe is the slow one on this part)
+#pragma unroll
+          for (int cc = 0; cc < EPI_COLS; ++cc) {
+            const long long j = tl.J * TILE_N + c0 + cc;
+            if (wd[cc]) O[j * jb.ldo + i] = v[cc];
+            if (wm[cc]) O[(long long)i * jb.ldo + j] = mv[cc];
+          }
         }
       }
       tc_fence_before();
@@ -729,7 +752,7 @@ static void choose_digits(int Kmax, int& beta, int& S)
 {
   long long K2 = 2ll * std::max(1, Kmax);
   for (beta = 7; beta >= 3; --beta) {
-    long long d1 = 1ll << beta, dl = 1ll << (beta - 1);
+    long long d1 = (1ll << beta) + 1, dl = 1ll << (beta - 1);
     bool ok = true;
     for (int T = 2; T <= 5; ++T) {
       long long b = 0;

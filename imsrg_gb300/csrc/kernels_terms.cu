@@ -11,6 +11,7 @@
 namespace imsrg {
 
 static constexpr double kSqrt2 = 1.4142135623730950488;
+static constexpr int kMaxChannels = 6 * 64;  // 2b / CC channels: 6 (j2max + 1), j2max <= 63
 
 __device__ __forceinline__ double warp_sum(double v)
 {
@@ -563,8 +564,15 @@ __global__ void __launch_bounds__(256) k_pandya_inv(DevSpace S, DevWork W, const
                                                     int ntiles)
 {
   __shared__ double T[32][33];
+  __shared__ int s_ccn[kMaxChannels];
+  __shared__ long long s_zboff[kMaxChannels];
   int tix = blockIdx.x;
   if (tix >= ntiles) return;
+  for (int c = threadIdx.x; c < S.nch; c += blockDim.x) {
+    s_ccn[c] = S.cc_n[c];
+    s_zboff[c] = W.zb_off[c];
+  }
+  __syncthreads();
   const int ch = tiles[3 * tix], tb = tiles[3 * tix + 1], tk = tiles[3 * tix + 2];
   const int n = S.ch_n[ch];
   const int J = ch / 6;
@@ -593,14 +601,17 @@ __global__ void __launch_bounds__(256) k_pandya_inv(DevSpace S, DevWork W, const
         int Jpmin = max(abs(jji - jjl), abs(jjk - jjj)) / 2;
         int Jpmax = min(jji + jjl, jjk + jjj) / 2;
         int kil = ket_index(N, min(i, l), max(i, l)), kkj = ket_index(N, min(j, k), max(j, k));
+        // (2J'+1) 6j for consecutive J' sit in consecutive table slots
+        const double* wrow = S.sixj_wval + sixj_slot(S.d1, S.sixj_base, jji, jjj, J, jjk, jjl, Jpmin) - Jpmin;
+#pragma unroll 2
         for (int Jp = Jpmin; Jp <= Jpmax; ++Jp) {
-          double w = dev_sixj_w(S, jji, jjj, J, jjk, jjl, Jp);  // (2J'+1) 6j
+          double w = __ldg(wrow + Jp);
           if (dzero(w)) continue;
           int cc = chan_index(Jp, par, tz);
-          int ncc = S.cc_n[cc];
-          int il = S.ccJ_loc[Jp * S.nkets + kil] + (i > l ? ncc : 0);
-          int kj = S.ccJ_loc[Jp * S.nkets + kkj] + (k > j ? ncc : 0);
-          commij = fma(-w, Zb[W.zb_off[cc] + (long long)kj * ncc + il], commij);
+          int ncc = s_ccn[cc];
+          int il = __ldg(S.ccJ_loc + Jp * S.nkets + kil) + (i > l ? ncc : 0);
+          int kj = __ldg(S.ccJ_loc + Jp * S.nkets + kkj) + (k > j ? ncc : 0);
+          commij = fma(-w, Zb[s_zboff[cc] + (long long)kj * ncc + il], commij);
         }
       }
       if (k == l) {
@@ -616,15 +627,17 @@ __global__ void __launch_bounds__(256) k_pandya_inv(DevSpace S, DevWork W, const
         // i <= k always (ibra <= iket), so ik is a row of the head/tail blocks
         const int tsign = (l > j) ? iphase((jji + jjk + jjl + jjj) / 2) : hZ;
         double acc = 0.0;
+        const double* wrow = S.sixj_wval + sixj_slot(S.d1, S.sixj_base, jjj, jji, J, jjk, jjl, Jpmin) - Jpmin;
+#pragma unroll 2
         for (int Jp = Jpmin; Jp <= Jpmax; ++Jp) {
-          double w = dev_sixj_w(S, jjj, jji, J, jjk, jjl, Jp);
+          double w = __ldg(wrow + Jp);
           if (dzero(w)) continue;
           int cc = chan_index(Jp, par, tz);
-          int ncc = S.cc_n[cc];
-          int ik = S.ccJ_loc[Jp * S.nkets + kik];
-          int lj = S.ccJ_loc[Jp * S.nkets + klj];
+          int ncc = s_ccn[cc];
+          int ik = __ldg(S.ccJ_loc + Jp * S.nkets + kik);
+          int lj = __ldg(S.ccJ_loc + Jp * S.nkets + klj);
           // Zbar(ik, lj[+n]) read as its symmetric partner Zbar(lj, ik[+n])
-          long long e = W.zb_off[cc] + (long long)(ik + (l > j ? ncc : 0)) * ncc + lj;
+          long long e = s_zboff[cc] + (long long)(ik + (l > j ? ncc : 0)) * ncc + lj;
           acc = fma(-w, Zb[e], acc);
         }
         commji = dneg_if(acc, tsign < 0);

@@ -83,6 +83,7 @@ Space* build_space(int emax, const std::vector<int>& n, const std::vector<int>& 
     j2max = std::max(j2max, j2[i]);
     if (occ[i] >= OCC_CUT) s.holes.push_back(i);
   }
+  if (j2max > 63) throw std::runtime_error("orbit j2 above 63 is not supported");
   s.NJ = j2max + 1;
   s.nch = 6 * (j2max + 1);  // ModelSpace::AddOrbit, src/ModelSpace.cc:936-946
   s.nkets = s.norb * (s.norb + 1) / 2;
