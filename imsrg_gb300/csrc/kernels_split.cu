@@ -50,10 +50,8 @@ namespace {
 
 constexpr int KB = 32;          // K elements (bf16) per pipeline stage: one 64-byte swizzle row
 constexpr int TILE_M = 128;     // rows per tile (UMMA M)
-constexpr int TILE_N = 64;      // columns per tile (UMMA N)
 constexpr int MAX_S = 7;
 constexpr int EPI_COLS = 8;     // TMEM columns read per tcgen05.ld
-constexpr int THREADS = 192;
 constexpr unsigned WAIT_LIMIT = 1u << 22;  // bounded spin (with nanosleep backoff: about a second)
 constexpr int EXP_NONE = -100000;          // exponent of an all-zero row
 
@@ -94,6 +92,7 @@ struct SplitPlan {
   size_t smem = 0;
   int nstages = 0;
   int accum_override = -1;
+  int tn = 64, nacc = 1, epiw = 4;  // tile columns, accumulator sets, epilogue warps
 };
 
 // ----------------------------------------------------------------- device
@@ -468,25 +467,33 @@ struct GemmArgs {
   int accum;  // -1: each job's flag; 0: overwrite; 1: accumulate
 };
 
-template <int S>
-__global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant__ CUtensorMap mAlpha,
-                                                          const __grid_constant__ CUtensorMap mBeta,
-                                                          const __grid_constant__ CUtensorMap mGamma,
-                                                          const __grid_constant__ CUtensorMap mDelta, GemmArgs g)
+// TN: tile columns (UMMA N); NACC: TMEM accumulator sets (2 lets the
+// epilogue of one tile overlap the MMAs of the next); EPIW: epilogue warps
+// (4 or 8; with 8, two warps share a TMEM lane quarter and split the columns).
+template <int S, int TN, int NACC, int EPIW>
+__global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_constant__ CUtensorMap mAlpha,
+                                                                 const __grid_constant__ CUtensorMap mBeta,
+                                                                 const __grid_constant__ CUtensorMap mGamma,
+                                                                 const __grid_constant__ CUtensorMap mDelta,
+                                                                 GemmArgs g)
 {
+  static_assert(NACC * S * TN <= 512, "TMEM accumulators exceed 512 columns");
+  static_assert(TILE_M % TN == 0 && TN % 16 == 0, "tile shape");
+  constexpr int EPI_T = 32 * EPIW;          // epilogue threads
+  constexpr int COLS_W = TN / (EPIW / 4);   // columns per epilogue warp
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-byte aligned base
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int NST = g.nstages;
   const unsigned A_SLICE = TILE_M * KB * 2;  // 8 KB
-  const unsigned B_SLICE = TILE_N * KB * 2;  // 4 KB
+  const unsigned B_SLICE = TN * KB * 2;
   const unsigned STAGE = S * (A_SLICE + B_SLICE);
   unsigned long long* bars = (unsigned long long*)(smem + NST * STAGE);
-  // bars: full[NST], empty[NST], acc_full, acc_empty ; then tmem slot
-  unsigned* tmem_slot = (unsigned*)(bars + 2 * NST + 2);
+  // bars: full[NST], empty[NST], acc_full[NACC], acc_empty[NACC]; then tmem slot
+  unsigned* tmem_slot = (unsigned*)(bars + 2 * NST + 2 * NACC);
   __shared__ int s_err_;
-  __shared__ int s_colexp[TILE_N];
-  __shared__ int s_colph[TILE_N];
+  __shared__ int s_colexp[2][TN];  // indexed by tile parity: warps run at most one tile apart
+  __shared__ int s_colph[2][TN];
   __shared__ int s_epi_err_;
   volatile int& s_err = s_err_;
   volatile int& s_epi_err = s_epi_err_;
@@ -496,8 +503,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
   const unsigned bar0 = smem_u32(bars);
   auto full_bar = [&](int s) { return bar0 + 8u * s; };
   auto empty_bar = [&](int s) { return bar0 + 8u * (NST + s); };
-  const unsigned acc_full = bar0 + 8u * (2 * NST);
-  const unsigned acc_empty = bar0 + 8u * (2 * NST + 1);
+  auto acc_full = [&](int b) { return bar0 + 8u * (2 * NST + b); };
+  auto acc_empty = [&](int b) { return bar0 + 8u * (2 * NST + NACC + b); };
 
   if (threadIdx.x == 0) {
     s_err = 0;
@@ -506,8 +513,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
       mbar_init(full_bar(s), 1);
       mbar_init(empty_bar(s), 1);
     }
-    mbar_init(acc_full, 1);
-    mbar_init(acc_empty, 128);
+    for (int b = 0; b < NACC; ++b) {
+      mbar_init(acc_full(b), 1);
+      mbar_init(acc_empty(b), EPI_T);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -548,9 +557,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
           unsigned sB = sA + S * A_SLICE;
           for (int s = 0; s < S; ++s) {
             int rowA = (int)(jb.row_base + (long long)s * jb.m_pad + tl.I * TILE_M);
-            int rowB = (int)(jb.row_base + (long long)s * jb.m_pad + tl.J * TILE_N);
-            tma_load_2d(sA + s * A_SLICE, ma, k, rowA, full_bar(st));
-            tma_load_2d(sA + s * A_SLICE + TILE_N * KB * 2, ma, k, rowA + TILE_N, full_bar(st));
+            int rowB = (int)(jb.row_base + (long long)s * jb.m_pad + tl.J * TN);
+            // the maps load TN-row boxes: an A tile is TILE_M / TN of them
+#pragma unroll
+            for (int h = 0; h < TILE_M / TN; ++h)
+              tma_load_2d(sA + s * A_SLICE + h * TN * KB * 2, ma, k, rowA + h * TN, full_bar(st));
             tma_load_2d(sB + s * B_SLICE, mb, k, rowB, full_bar(st));
           }
         }
@@ -559,16 +570,18 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
   } else if (warp == 1) {
     // ------------------------------------------------ MMA issuer
     if (lane == 0) {
-      const unsigned idesc = idesc_bf16(TILE_M, TILE_N);
+      const unsigned idesc = idesc_bf16(TILE_M, TN);
       int it = 0, tc = 0;
       for (int tix = blockIdx.x; tix < g.ntiles && !s_err; tix += gridDim.x, ++tc) {
         const SplitJob& jb = g.jobs[g.tiles[tix].job];
-        if (!mbar_wait(acc_empty, (unsigned)((tc & 1) ^ 1))) {
+        const int b = tc % NACC;
+        if (!mbar_wait(acc_empty(b), (unsigned)(((tc / NACC) & 1) ^ 1))) {
           set_status(g.status, 102);
           s_err = 1;
           break;
         }
         tc_fence_after();
+        const unsigned dbase = tmem + (unsigned)(b * S * TN);
         unsigned started = 0;  // groups already written in this tile
         bool ok = true;
         for (int kb = 0; kb < 2 * jb.nkb; ++kb, ++it) {
@@ -593,7 +606,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
                 int grp = s + t;  // weight group T = (s+1) + (t+1) - 2
                 unsigned long long bd = sdesc_sw64(sB + t * B_SLICE + sub * 32);
                 unsigned acc = (started >> grp) & 1u;
-                tc_mma(tmem + grp * TILE_N, ad, bd, idesc, acc);
+                tc_mma(dbase + grp * TN, ad, bd, idesc, acc);
                 started |= 1u << grp;
               }
             }
@@ -601,53 +614,53 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
           tc_commit(empty_bar(st));
         }
         if (!ok) break;
-        tc_commit(acc_full);
+        tc_commit(acc_full(b));
       }
     }
   } else {
-    // ------------------------------------------------ epilogue (warps 2..5)
-    const int q = warp & 3;  // TMEM lane quarter of this warp
+    // ------------------------------------------------ epilogue (warps 2 .. 1+EPIW)
+    const int q = warp & 3;                  // TMEM lane quarter of this warp
+    const int cbeg = ((warp - 2) >> 2) * COLS_W;  // first column of this warp
+    const int et = threadIdx.x - 64;         // 0 .. EPI_T-1
     int tc = 0;
     for (int tix = blockIdx.x; tix < g.ntiles; tix += gridDim.x, ++tc) {
       const SplitTile tl = g.tiles[tix];
       const SplitJob& jb = g.jobs[tl.job];
-      // the four epilogue warps decide together (named barrier 1), so a
-      // timeout never leaves one of them waiting at a barrier alone
-      if (!mbar_wait(acc_full, (unsigned)(tc & 1))) {
+      const int b = tc % NACC;
+      // the epilogue warps decide together (named barrier 1), so a timeout
+      // never leaves one of them waiting at a barrier alone
+      if (!mbar_wait(acc_full(b), (unsigned)((tc / NACC) & 1))) {
         set_status(g.status, 104);
         s_epi_err = 1;
       }
-      asm volatile("bar.sync 1, 128;" ::: "memory");
+      const int c = job_c(g.jobmax, tl.job);
+      const int* ph = jb.phase_off >= 0 ? g.phase + jb.phase_off : nullptr;
+      // column exponents and phases of this tile
+      if (et < TN) {
+        const int j = tl.J * TN + et;
+        const bool ok = j < jb.m;
+        s_colexp[tc & 1][et] = ok ? row_exp(g.rexpA[jb.exp_base + j], g.rexpB[jb.exp_base + j], c) : EXP_NONE;
+        s_colph[tc & 1][et] = (ph && ok) ? ph[j] : 1;
+      }
+      asm volatile("bar.sync 1, %0;" ::"r"(EPI_T) : "memory");
       if (s_epi_err) {
         s_err = 1;
         break;
       }
       tc_fence_after();
-      const int c = job_c(g.jobmax, tl.job);
       const int sign = jb.sign != 0 ? jb.sign : g.gsign;
-      const int* ph = jb.phase_off >= 0 ? g.phase + jb.phase_off : nullptr;
       const int i = tl.I * TILE_M + q * 32 + lane;
       const bool rowok = i < jb.m;
       const int ai = rowok ? row_exp(g.rexpA[jb.exp_base + i], g.rexpB[jb.exp_base + i], c) : EXP_NONE;
       const int phi_i = (ph && rowok) ? ph[i] : 1;
-      // column exponents and phases of this tile, once per tile
-      {
-        const int et = threadIdx.x - 64;  // 0..127 over the epilogue warps
-        if (et < TILE_N) {
-          const int j = tl.J * TILE_N + et;
-          const bool ok = j < jb.m;
-          s_colexp[et] = ok ? row_exp(g.rexpA[jb.exp_base + j], g.rexpB[jb.exp_base + j], c) : EXP_NONE;
-          s_colph[et] = (ph && ok) ? ph[j] : 1;
-        }
-        asm volatile("bar.sync 1, 128;" ::: "memory");
-      }
       double* O = g.out + jb.out_off;
       const int Xi = ai + c - g.beta * (S + 1);
-      for (int c0 = 0; c0 < TILE_N; c0 += EPI_COLS) {
+      const bool accumulate = g.accum > 0 || (g.accum < 0 && jb.accumulate);
+      const unsigned tbase = tmem + ((unsigned)(q * 32) << 16) + (unsigned)(b * S * TN);
+      for (int c0 = cbeg; c0 < cbeg + COLS_W; c0 += EPI_COLS) {
         unsigned r[MAX_S][EPI_COLS];
 #pragma unroll
-        for (int gidx = 0; gidx < S; ++gidx)
-          tmem_ld8(tmem + ((unsigned)(q * 32) << 16) + (unsigned)(gidx * TILE_N + c0), r[gidx]);
+        for (int gidx = 0; gidx < S; ++gidx) tmem_ld8(tbase + (unsigned)(gidx * TN + c0), r[gidx]);
         tmem_wait_ld();
         // values of this chunk, then all old values (accumulate), then the
         // stores: the loads of one chunk are in flight together
@@ -655,7 +668,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
         bool wd[EPI_COLS], wm[EPI_COLS];
 #pragma unroll
         for (int cc = 0; cc < EPI_COLS; ++cc) {
-          const int j = tl.J * TILE_N + c0 + cc;
+          const int j = tl.J * TN + c0 + cc;
           wd[cc] = rowok && j < jb.m && !(tl.diag && i > j);
           wm[cc] = wd[cc] && i != j;
           // exact merge of the weight groups: Horner in base 2^beta
@@ -663,23 +676,23 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
 #pragma unroll
           for (int gidx = 1; gidx < S; ++gidx)
             I64 = I64 * (1ll << g.beta) + __float2int_rn(__uint_as_float(r[gidx][cc]));
-          v[cc] = i64_ldexp(I64, Xi + s_colexp[c0 + cc]);
+          v[cc] = i64_ldexp(I64, Xi + s_colexp[tc & 1][c0 + cc]);
           mv[cc] = __longlong_as_double(__double_as_longlong(v[cc]) ^
-                                        ((sign * phi_i * s_colph[c0 + cc]) < 0 ? (long long)0x8000000000000000ull
-                                                                                : 0ll));
+                                        ((sign * phi_i * s_colph[tc & 1][c0 + cc]) < 0 ? (long long)0x8000000000000000ull
+                                                                                   : 0ll));
           od[cc] = 0.0;
           om[cc] = 0.0;
         }
-        if (g.accum > 0 || (g.accum < 0 && jb.accumulate)) {
+        if (accumulate) {
 #pragma unroll
           for (int cc = 0; cc < EPI_COLS; ++cc) {
-            const long long j = tl.J * TILE_N + c0 + cc;
+            const long long j = tl.J * TN + c0 + cc;
             if (wd[cc]) od[cc] = __ldcg(O + j * jb.ldo + i);
             if (wm[cc]) om[cc] = __ldcg(O + (long long)i * jb.ldo + j);
           }
 #pragma unroll
           for (int cc = 0; cc < EPI_COLS; ++cc) {
-            const long long j = tl.J * TILE_N + c0 + cc;
+            const long long j = tl.J * TN + c0 + cc;
             if (wd[cc]) O[j * jb.ldo + i] = od[cc] + v[cc];
             if (wm[cc]) O[(long long)i * jb.ldo + j] = om[cc] + mv[cc];
           }
@@ -687,30 +700,23 @@ __global__ void __launch_bounds__(THREADS, 1) k_split_gemm(const __grid_constant
           // overwrite: no FP64 add (the FP64 pipe is the slow one on this part)
 #pragma unroll
           for (int cc = 0; cc < EPI_COLS; ++cc) {
-            const long long j = tl.J * TILE_N + c0 + cc;
+            const long long j = tl.J * TN + c0 + cc;
             if (wd[cc]) O[j * jb.ldo + i] = v[cc];
             if (wm[cc]) O[(long long)i * jb.ldo + j] = mv[cc];
           }
         }
       }
       tc_fence_before();
-      asm volatile("bar.sync 1, 128;" ::: "memory");  // s_colexp reused by the next tile
-      mbar_arrive(acc_empty);
+      mbar_arrive(acc_empty(b));
     }
   }
-  // drain: wait (bounded) for the last MMA commit of this CTA before freeing TMEM
+  // every role has left its loop: all MMAs this CTA issued have been drained
+  // by the epilogue (or the CTA gave up after a bounded wait)
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
   }
-}
-
-template <int S>
-size_t gemm_smem_bytes(int nstages)
-{
-  size_t stage = (size_t)S * (TILE_M + TILE_N) * KB * 2;
-  return 1024 + nstages * stage + (2 * nstages + 2) * 8 + 16;
 }
 
 }  // namespace
@@ -773,6 +779,12 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
   (void)s;
   SplitPlan* p = new SplitPlan();
   p->family = family;
+  // the ladder products have long K (MMA-bound tiles): 64-column tiles, one
+  // accumulator set; the Pandya-space products have short K (epilogue-bound
+  // tiles): 32-column tiles, two accumulator sets and eight epilogue warps
+  p->tn = family == 0 ? 64 : 32;
+  p->nacc = family == 0 ? 1 : 2;
+  p->epiw = family == 0 ? 4 : 8;
   int Kmax = 1;
   for (const GemmJobDev& j : jobs_in) Kmax = std::max(Kmax, j.K);
   choose_digits(Kmax, p->beta, p->S);
@@ -812,9 +824,10 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
   for (int jix : order) {
     const SplitJob& sj = p->jobs[jix];
     if (sj.m == 0 || sj.K == 0) continue;
-    int nI = sj.m_pad / TILE_M, nJ = (sj.m + TILE_N - 1) / TILE_N;
+    const int per = TILE_M / p->tn;  // column tiles per 128-row block
+    int nI = sj.m_pad / TILE_M, nJ = (sj.m + p->tn - 1) / p->tn;
     for (int I = 0; I < nI; ++I)
-      for (int J = 2 * I; J < nJ; ++J) tiles.push_back({jix, I, J, (J == 2 * I || J == 2 * I + 1) ? 1 : 0});
+      for (int J = per * I; J < nJ; ++J) tiles.push_back({jix, I, J, J < per * (I + 1) ? 1 : 0});
   }
   if (row > (1ll << 31) - TILE_M) throw std::runtime_error("split slice arrays exceed 2^31 rows");
   p->K_stride = kstride;
@@ -853,7 +866,7 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
     long long rows_map = std::max(row, (long long)TILE_M);
     // every operand tile is loaded in 64-row boxes (an A tile is two of them),
     // so one map per array serves both operand roles
-    for (int a = 0; a < 4; ++a) encode_map(&p->maps[a], p->arr[a], rows_map, kstride, TILE_N);
+    for (int a = 0; a < 4; ++a) encode_map(&p->maps[a], p->arr[a], rows_map, kstride, p->tn);
   } catch (...) {
     split_plan_destroy(p);
     throw;
@@ -864,10 +877,10 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
   p->grid = std::max(1, std::min(nsm, p->ntiles));
   int maxsm = 0;
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  size_t stage = (size_t)p->S * (TILE_M + TILE_N) * KB * 2;
-  p->nstages = (int)std::min<size_t>(4, ((size_t)maxsm - 2048) / stage);
+  size_t stage = (size_t)p->S * (TILE_M + p->tn) * KB * 2;
+  p->nstages = (int)std::min<size_t>(6, ((size_t)maxsm - 3072) / stage);
   if (p->nstages < 2) throw std::runtime_error("not enough shared memory for the split GEMM pipeline");
-  p->smem = 1024 + p->nstages * stage + (2 * p->nstages + 2) * 8 + 16;
+  p->smem = 1024 + p->nstages * stage + (2 * p->nstages + 2 * p->nacc) * 8 + 16;
   return p;
 }
 
@@ -923,12 +936,6 @@ static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, con
   }
   {
     ProfScope ps(p->family == 0 ? "split_gemm_ladder" : "split_gemm_zbar", st);
-    static bool attr_set[MAX_S + 1] = {};
-    if (!attr_set[S]) {
-      e = cudaFuncSetAttribute(k_split_gemm<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
-      if (e != cudaSuccess) return e;
-      attr_set[S] = true;
-    }
     GemmArgs ga;
     ga.jobs = p->d_jobs;
     ga.tiles = p->d_tiles;
@@ -945,7 +952,17 @@ static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, con
     ga.nstages = p->nstages;
     ga.gsign = gsign;
     ga.accum = p->accum_override;
-    k_split_gemm<S><<<p->grid, THREADS, p->smem, st>>>(p->maps[0], p->maps[1], p->maps[2], p->maps[3], ga);
+    if (p->tn == 64) {
+      auto kern = k_split_gemm<S, 64, 1, 4>;
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
+      if (e != cudaSuccess) return e;
+      kern<<<p->grid, 64 + 32 * 4, p->smem, st>>>(p->maps[0], p->maps[1], p->maps[2], p->maps[3], ga);
+    } else {
+      auto kern = k_split_gemm<S, 32, 2, 8>;
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
+      if (e != cudaSuccess) return e;
+      kern<<<p->grid, 64 + 32 * 8, p->smem, st>>>(p->maps[0], p->maps[1], p->maps[2], p->maps[3], ga);
+    }
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
