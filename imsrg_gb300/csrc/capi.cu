@@ -203,6 +203,35 @@ void setup_device_lists(imsrg_space* sp)
         tinv.push_back(b);
       }
   }
+  // Inverse-Pandya tiles ordered so that blocks running at the same time
+  // cover the same orbit region for every J: a Zbar element is read by the
+  // elements of one orbit quadruple in all J channels, so this turns most of
+  // those rereads into L2 hits.  Key: (parity/Tz family, global index of the
+  // first bra, of the first ket, J).
+  {
+    struct Key {
+      int fam;
+      int gb, gk, J;
+      int t;
+    };
+    std::vector<Key> keys;
+    for (size_t t = 0; t < tinv.size() / 3; ++t) {
+      int c = tinv[3 * t], a = tinv[3 * t + 1], b = tinv[3 * t + 2];
+      const Chan& C = s.ch[c];
+      keys.push_back({c % 6, ket_index(s.norb, C.p[32 * a], C.q[32 * a]), ket_index(s.norb, C.p[32 * b], C.q[32 * b]),
+                      C.J, (int)t});
+    }
+    std::stable_sort(keys.begin(), keys.end(), [](const Key& x, const Key& y) {
+      if (x.fam != y.fam) return x.fam < y.fam;
+      if (x.gb != y.gb) return x.gb < y.gb;
+      if (x.gk != y.gk) return x.gk < y.gk;
+      return x.J < y.J;
+    });
+    std::vector<int> sorted;
+    for (const Key& k : keys)
+      for (int f = 0; f < 3; ++f) sorted.push_back(tinv[3 * k.t + f]);
+    tinv.swap(sorted);
+  }
   for (int c = 0; c < s.nch; ++c) {
     int ncc = s.cc[c].n();
     int K = 2 * s.cc_nph[c];

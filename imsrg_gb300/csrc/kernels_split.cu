@@ -238,6 +238,8 @@ __global__ void __launch_bounds__(256) k_split_rowexp(const SplitJob* __restrict
                                                       int* __restrict__ rexpB, int* __restrict__ jobmax)
 {
   __shared__ int sa[8][33], sb[8][33];
+  __shared__ int s_col[256];
+  __shared__ double s_sc[256];
   int job = blockIdx.z;
   if (job >= njobs) return;
   const SplitJob jb = jobs[job];
@@ -245,19 +247,27 @@ __global__ void __launch_bounds__(256) k_split_rowexp(const SplitJob* __restrict
   const int i = blockIdx.y * 32 + r;
   const int t0 = blockIdx.x * 256;
   if (blockIdx.y * 32 >= jb.m_pad || t0 >= max(jb.K, 1)) return;
+  const int tend = min(jb.K, t0 + 256);
+  {
+    // column indices and scales of this chunk, once per block
+    const int* kx = jb.kidx_off >= 0 ? kidx + jb.kidx_off : nullptr;
+    const double* w = jb.w_off >= 0 ? kw + jb.w_off : nullptr;
+    const double sc0 = jb.bscale * gbscale;
+    const int t = t0 + threadIdx.x;
+    if (t < tend) {
+      s_col[threadIdx.x] = kx ? kx[t] : t;
+      s_sc[threadIdx.x] = w ? sc0 * w[t] : sc0;
+    }
+  }
+  __syncthreads();
   int ea = 0, eb = 0;
   if (i < jb.m) {
     const double* A = Abase + jb.a_off;
     const double* B = (jb.bsel ? B1 : B0) + jb.b_off;
-    const int* kx = jb.kidx_off >= 0 ? kidx + jb.kidx_off : nullptr;
-    const double* w = jb.w_off >= 0 ? kw + jb.w_off : nullptr;
-    const double sc0 = jb.bscale * gbscale;
-    const int tend = min(jb.K, t0 + 256);
     for (int t = t0 + ty; t < tend; t += 8) {
-      int col = kx ? __ldg(kx + t) : t;
+      const int col = s_col[t - t0];
       ea = max(ea, dexp(A[(long long)col * jb.lda + i]));
-      double sc = w ? sc0 * __ldg(w + t) : sc0;
-      eb = max(eb, dexp(scaled(B[(long long)col * jb.ldb + i], sc)));
+      eb = max(eb, dexp(scaled(B[(long long)col * jb.ldb + i], s_sc[t - t0])));
     }
   }
   sa[ty][r] = ea;
