@@ -62,6 +62,7 @@ SIGNATURES = {
     "imsrg_comm121ss": (I, [P, P, P, P]),
     "imsrg_comm122ss": (I, [P, P, P, P]),
     "imsrg_comm221ss": (I, [P, P, P, P]),
+    "imsrg_comm122ss_noalloc": (I, [P, P, P, P, I, P]),
     "imsrg_comm222_pp_hhss": (I, [P, P, P, I, P]),
     "imsrg_comm222_pp_hh_221ss": (I, [P, P, P, I, P]),
     "imsrg_comm222_phss": (I, [P, P, P, I, P]),

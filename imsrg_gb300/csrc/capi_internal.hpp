@@ -1,0 +1,83 @@
+// Internal definitions of the opaque C-ABI handles (imsrg_space, imsrg_op),
+// shared by the translation units that implement include/imsrg_gb300.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <utility>
+#include <vector>
+
+#include "kernels.cuh"
+#include "space.hpp"
+
+using imsrg::GemmJobDev;
+using imsrg::Space;
+using imsrg::SplitPlan;
+
+namespace imsrg {
+// sets the calling thread's imsrg_last_error() message and returns code
+int set_error(int code, const char* msg);
+}  // namespace imsrg
+
+struct imsrg_space {
+  Space* s = nullptr;
+  bool dev_ready = false;
+  std::mutex mu;
+  std::vector<void*> allocs;
+  int* d_holes = nullptr;
+  // FP64 symmetrised products
+  GemmJobDev* d_ladder_jobs = nullptr;
+  int* d_ladder_pairs = nullptr;
+  int n_ladder_pairs = 0;
+  std::vector<GemmJobDev> ladder_jobs, zbar_jobs;
+  GemmJobDev* d_zbar_jobs = nullptr;
+  int* d_zbar_pairs = nullptr;
+  int n_zbar_pairs = 0;
+  // other tile lists
+  int* d_sym122 = nullptr;
+  int n_sym122 = 0;
+  int* d_pfwd = nullptr;
+  int n_pfwd = 0;
+  int* d_pinv = nullptr;
+  int n_pinv = 0;
+  std::vector<std::pair<int64_t, int64_t>> zbar_zero;  // Zbar regions with no ph kets
+  // norm chunks
+  long long* d_norm_off = nullptr;
+  int* d_norm_len = nullptr;
+  double* d_norm_w = nullptr;
+  int n_norm = 0;
+  double* d_norm_partial = nullptr;
+  std::vector<double> h_norm_partial;
+  // scratch
+  double *d_xb = nullptr, *d_yt = nullptr, *d_yf = nullptr, *d_zb = nullptr, *d_w2 = nullptr;
+  float2 *d_xf = nullptr, *d_yff = nullptr;  // (hi, lo) copies of X and Y for the double-float comm122ss
+  int* d_status = nullptr;
+  // split-precision plans
+  SplitPlan* split_ladder = nullptr;
+  SplitPlan* split_zbar = nullptr;
+  // BCH work operators
+  double *d_nested = nullptr, *d_next = nullptr;
+
+  template <class T>
+  T* track(T* p)
+  {
+    allocs.push_back((void*)p);
+    return p;
+  }
+  ~imsrg_space()
+  {
+    if (split_ladder) split_plan_destroy(split_ladder);
+    if (split_zbar) split_plan_destroy(split_zbar);
+    for (void* p : allocs) cudaFree(p);
+    delete s;
+  }
+};
+
+struct imsrg_op {
+  imsrg_space* sp = nullptr;
+  double* d = nullptr;
+  int herm = 1;
+};
+

@@ -144,6 +144,19 @@ int imsrg_comm111ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* str
 int imsrg_comm121ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
 /* Commutator::comm122ss, src/Commutator.cc:837-932 */
 int imsrg_comm122ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
+/* comm122ss (plain FP64 form) that allocates no device memory, for callers
+ * that cannot call cudaMalloc where they evaluate the term (fixed device
+ * budgets, allocators that own all device memory, regions where allocation
+ * is not allowed).  X, Y, Z are caller-owned device arenas of the space's
+ * layout (Z accumulates); hZ is Z's hermiticity.  The W2 intermediate lives
+ * in a static device array of 2^21 doubles (16 MiB) that every GPU loading
+ * the library holds until exit, so spaces with a longer arena are rejected
+ * (IMSRG_ERR_ARG); the space's device tables must already exist (they are
+ * built with its first operator).  The first call on a device looks up the
+ * array's device address; make it before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race.  No counterpart in the
+ * reference (its comm122ss, src/Commutator.cc:837-932, allocates W2 per call). */
+int imsrg_comm122ss_noalloc(const imsrg_space* s, const double* X, const double* Y, double* Z, int hZ, void* stream);
 /* Commutator::comm221ss, src/Commutator.cc:760-819 */
 int imsrg_comm221ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
 /* Commutator::comm222_pp_hhss, src/Commutator.cc:1062-1076 */
