@@ -66,6 +66,30 @@ def dist_env():
     return world, rank, local
 
 
+# Multi-GPU is replicas only: every rank runs its own commutators on its own
+# operators; the only communication is the barrier and the max of the timings.
+def replica_seeds(rank):
+    """Seeds of the X and Y operators of one replica."""
+    return 1000 + rank, 2000 + rank
+
+
+def whole_job_value(world, steps, elapsed_ms_max):
+    """Whole-job commutators/s: every rank ran `steps`, the slowest took elapsed_ms_max."""
+    return world * steps / (elapsed_ms_max / 1000.0)
+
+
+def max_over_ranks(x, device=None):
+    """Max of a float over the ranks of the default process group (identity
+    without one)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
 
@@ -257,8 +281,9 @@ def run_gb300(args):
     dX = ig.DeviceOperator(ms, 1)
     dY = ig.DeviceOperator(ms, -1)
     dZ = ig.DeviceOperator(ms, 1)
-    dX.fill_random(1000 + rank)
-    dY.fill_random(2000 + rank)
+    sx, sy = replica_seeds(rank)
+    dX.fill_random(sx)
+    dY.fill_random(sy)
     prec = args.precision
 
     def step(p=prec):
@@ -270,12 +295,8 @@ def run_gb300(args):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+    def max_ms(x):
+        return max_over_ranks(x, device="cuda")
 
     for _ in range(max(args.warmup, 3)):
         step()
@@ -299,8 +320,8 @@ def run_gb300(args):
     launches = L.imsrg_kernel_launches() - launches0
     L.imsrg_profiler_enable(0)
     clocks.stop()
-    elapsed_ms = max_over_ranks(e0.elapsed_time(e1))
-    value = world * args.steps / (elapsed_ms / 1000.0)
+    elapsed_ms = max_ms(e0.elapsed_time(e1))
+    value = whole_job_value(world, args.steps, elapsed_ms)
     # per-phase CUDA-event timers over the timed region
     n = L.imsrg_profiler_names(None, 0)
     buf = ctypes.create_string_buffer(n)
@@ -348,7 +369,7 @@ def run_gb300(args):
             step("fp64")
         f1.record()
         torch.cuda.synchronize()
-        fms = max_over_ranks(f0.elapsed_time(f1)) / nf
+        fms = max_ms(f0.elapsed_time(f1)) / nf
         fp64 = {"value": world * 1000.0 / fms, "unit": UNIT, "ms_per_step": fms, "steps": nf}
     # ---- end to end: host buffers, H2D + commutator + D2H per step, through the C ABI
     A = ms.arena_size
@@ -369,7 +390,7 @@ def run_gb300(args):
         dZ.download_ptr(hZ.data_ptr())
     g1.record()
     torch.cuda.synchronize()
-    ems = max_over_ranks(g0.elapsed_time(g1))
+    ems = max_ms(g0.elapsed_time(g1))
     e2e = {"value": world * ne / (ems / 1000.0), "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * A,
            "d2h_bytes_per_step": 8 * A}
     if rank != 0:
