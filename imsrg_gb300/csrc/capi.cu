@@ -199,6 +199,12 @@ void setup_device_lists(imsrg_space* sp)
   sp->d_sym122 = sp->track(dcopy(t122));
   sp->n_pinv = (int)tinv.size() / 3;
   sp->d_pinv = sp->track(dcopy(tinv));
+  build_invq_tasks(s, kInvqBudget);
+  sp->n_invq = (int)s.invq_tasks.size() / 4;
+  sp->d_invq = sp->track(dcopy(s.invq_tasks));
+  sp->d_cls_list = sp->track(dcopy(s.cls_list));
+  sp->d_cls_off = sp->track(dcopy(s.cls_off));
+  sp->d_cls_sort = sp->track(dcopy(s.cls_sort));
   sp->n_pfwd = (int)tfwd.size() / 3;
   sp->d_pfwd = sp->track(dcopy(tfwd));
   // norm chunks: every 2b block in pieces of <= 65536 elements, weight (2J+1)^2
@@ -394,7 +400,11 @@ int do_ph(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStrea
   }
   prof_end(slot, st);
   ProfScope pinv("InversePandyaTransformation", st);
-  CUDA_TRY(launch_pandya_inv(s, sp->d_zb, Z->d, Z->herm, sp->d_pinv, sp->n_pinv, st));
+  if (prec == IMSRG_PREC_SPLIT && sp->n_invq > 0)
+    CUDA_TRY(launch_pandya_inv_ff(s, sp->d_zb, Z->d, Z->herm, sp->d_invq, sp->n_invq, sp->d_cls_list, sp->d_cls_off,
+                                  sp->d_cls_sort, s.invq_smem, st));
+  else
+    CUDA_TRY(launch_pandya_inv(s, sp->d_zb, Z->d, Z->herm, sp->d_pinv, sp->n_pinv, st));
   return IMSRG_OK;
 }
 

@@ -42,6 +42,11 @@ struct imsrg_space {
   int n_pfwd = 0;
   int* d_pinv = nullptr;
   int n_pinv = 0;
+  int* d_invq = nullptr;  // quadruple blocks of the split-form inverse Pandya transform
+  int n_invq = 0;
+  int* d_cls_list = nullptr;
+  int* d_cls_off = nullptr;
+  unsigned char* d_cls_sort = nullptr;
   std::vector<std::pair<int64_t, int64_t>> zbar_zero;  // Zbar regions with no ph kets
   // norm chunks
   long long* d_norm_off = nullptr;

@@ -3,6 +3,8 @@
 
 #include <cstdint>
 
+#include <vector_types.h>
+
 #ifdef __CUDACC__
 #define IMSRG_HD __host__ __device__ __forceinline__
 #else
@@ -37,6 +39,8 @@ struct DevSpace {
   // Pandya recoupling sum (both cut and factor are the reference's,
   // src/Commutator.cc:1456-1462, 1579-1583)
   const double* sixj_wval;
+  // the same weights as (hi, lo) float pairs, hi + lo = weight to 2^-48
+  const float2* sixj_wf;
 };
 
 // Device copies of the per-kernel work lists (built once per space).
@@ -82,6 +86,45 @@ IMSRG_HD int sixj_slot(int d1, const int* base, int jj1, int jj2, int J3, int jj
   if (J3 < J3min || J3 > J3max || J6 < J6min || J6 > J6max) return -1;
   int a = (jj1 - 1) >> 1, b = (jj2 - 1) >> 1, c = (jj4 - 1) >> 1, d = (jj5 - 1) >> 1;
   return base[((a * d1 + b) * d1 + c) * d1 + d] + (J3 - J3min) * (J6max - J6min + 1) + (J6 - J6min);
+}
+
+// Inverse Pandya transform by orbit quadruple (i, j, k, l), bra (i, j), ket
+// (k, l), i <= j, k <= l, (i, j) <= (k, l): the quadruple's element lives in every
+// channel J of [Jlo, Jhi] (even J only when i == j or k == l), its first J'
+// sum has n1 terms (J' from lo1), its second n2 (from lo2; none when i == j or
+// k == l).  Returns false when the quadruple contributes nothing: an empty J
+// window, the lower triangle (i == k, j > l), or the diagonal of an
+// anti-hermitian Z (src/Commutator.cc:1541, 1559-1560, 1588-1589).
+constexpr int kInvqMaxOrb = 64;  // orbits of one (parity, Tz) class in a block
+constexpr int kInvqMaxJ = 32;    // J (or J') values one block spans: 2 j_max + 1 < 32
+
+IMSRG_HD bool invq_counts(int i, int j, int k, int l, int ji, int jj, int jk, int jl, int hZ, int& n1, int& n2,
+                          int& nJ, int& Jlo, int& lo1, int& lo2)
+{
+  n1 = n2 = nJ = 0;
+  Jlo = lo1 = lo2 = 0;
+  if (i == k && (j > l || (hZ < 0 && j == l))) return false;
+  int a = ji > jj ? ji - jj : jj - ji, b = jk > jl ? jk - jl : jl - jk;
+  int lo = (a > b ? a : b) >> 1;
+  int hi = ((ji + jj) < (jk + jl) ? ji + jj : jk + jl) >> 1;
+  const bool ev = (i == j) || (k == l);
+  if (ev) lo += lo & 1;
+  if (lo > hi) return false;
+  nJ = ev ? ((hi - lo) >> 1) + 1 : hi - lo + 1;
+  Jlo = lo;
+  a = ji > jl ? ji - jl : jl - ji;
+  b = jk > jj ? jk - jj : jj - jk;
+  lo1 = (a > b ? a : b) >> 1;
+  int h1 = ((ji + jl) < (jk + jj) ? ji + jl : jk + jj) >> 1;
+  n1 = h1 >= lo1 ? h1 - lo1 + 1 : 0;
+  if (!ev) {
+    a = jj > jl ? jj - jl : jl - jj;
+    b = jk > ji ? jk - ji : ji - jk;
+    lo2 = (a > b ? a : b) >> 1;
+    int h2 = ((jj + jl) < (jk + ji) ? jj + jl : jk + ji) >> 1;
+    n2 = h2 >= lo2 ? h2 - lo2 + 1 : 0;
+  }
+  return true;
 }
 
 #ifdef __CUDACC__

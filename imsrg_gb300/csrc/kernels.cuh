@@ -34,6 +34,12 @@ cudaError_t launch_pandya_fwd(const Space& s, const double* X, const double* Y, 
                               double* Yf, const int* tiles, int ntiles, cudaStream_t st);
 cudaError_t launch_pandya_inv(const Space& s, const double* Zb, double* Z, int hZ, const int* tiles, int ntiles,
                               cudaStream_t st);
+// split form: blocks of orbit quadruples (Space::invq_tasks), double-float sums
+cudaError_t launch_pandya_inv_ff(const Space& s, const double* Zb, double* Z, int hZ, const int* tasks, int ntasks,
+                                 const int* clist, const int* coff, const unsigned char* csort, int smem,
+                                 cudaStream_t st);
+// shared-memory budget of one quadruple block (dynamic part)
+constexpr int kInvqBudget = 36864;
 cudaError_t launch_axpy(double* y, const double* x, double a, long long n, cudaStream_t st);
 cudaError_t launch_scale(double* y, double a, long long n, cudaStream_t st);
 cudaError_t launch_norm(const Space& s, const double* A, const long long* chunk_off, const int* chunk_len,

@@ -545,6 +545,40 @@ __global__ void k_pandya_fwd(DevSpace S, DevWork W, const double* __restrict__ X
   Yf[base + (long long)tf * ncc + ik] = yv * phi[kb] * phi[ik] * hY;
 }
 
+// (hi, lo) -> double with integer instructions: hi exactly, then lo added as
+// a whole number of ulps of hi (|lo| <= ulp_f32(hi) / 2, so hi + lo stays in
+// hi's binade except just below a power of two, where the ulps halve)
+__device__ __forceinline__ double ff2d(float hi, float lo)
+{
+  unsigned hb = __float_as_uint(hi), lb = __float_as_uint(lo);
+  int eh = (hb >> 23) & 0xFF, el = (lb >> 23) & 0xFF;
+  if (eh == 0) return f2d(lo);
+  double h = f2d(hi);
+  if (el == 0) return h;
+  long long bits = __double_as_longlong(h);
+  int sh = el - eh + 29;  // lo = m 2^(el-150), ulp(h) = 2^(eh-179)
+  long long m = (long long)((lb & 0x7FFFFFu) | 0x800000u);
+  long long off = sh >= 0 ? (m << sh) : (sh > -25 ? (m >> -sh) : 0ll);
+  if ((hb ^ lb) >> 31) {
+    if ((bits & 0xFFFFFFFFFFFFFll) == 0) off <<= 1;
+    bits -= off;
+  } else {
+    bits += off;
+  }
+  return __longlong_as_double(bits);
+}
+
+// (hi, lo) = (s1 + c1) + (s2 + c2), renormalised
+__device__ __forceinline__ void df_add(float s1, float c1, float s2, float c2, float& hi, float& lo)
+{
+  float s = __fadd_rn(s1, s2);
+  float bb = __fsub_rn(s, s1);
+  float e = __fadd_rn(__fsub_rn(s1, __fsub_rn(s, bb)), __fsub_rn(s2, bb));
+  e = __fadd_rn(e, __fadd_rn(c1, c2));
+  hi = __fadd_rn(s, e);
+  lo = __fsub_rn(e, __fsub_rn(hi, s));
+}
+
 // ------------------------------------------------------------ Pandya inverse
 // AddInversePandyaTransformation (src/Commutator.cc:1501-1616): for every
 // (ibra <= iket) element of every 2b channel block, the two J' sums over Zbar.
@@ -664,6 +698,411 @@ __global__ void __launch_bounds__(256) k_pandya_inv(DevSpace S, DevWork W, const
     int kk = e & 31, bb = e >> 5;
     int ibra = tb * 32 + bb, ik2 = tk * 32 + kk;
     if (ibra < n && ik2 < n && ik2 > ibra) Z[off + (long long)ibra * n + ik2] += hZ * T[bb][kk];
+  }
+}
+
+// ------------------------------------------- Pandya inverse, by orbit quadruple
+// Split form of AddInversePandyaTransformation (src/Commutator.cc:1501-1616),
+// reorganised around orbit quadruples: the element Z_J(ij, kl) of every J is
+// a small recoupling of the same Zbar_J'(il, kj) and Zbar_J'(ik, lj) values,
+// so a block loads those values once for all J instead of once per J.
+//
+// A block owns one (i, k, class of j) group of quadruples (see
+// build_invq_tasks), laid out as a jn x ln rectangle of (j, l) pairs:
+//   1. per-pair counts and a block scan give each pair its slots in shared
+//      memory: n1 + n2 staged Zbar values, nJ results;
+//   2. staging, J' by J' (all lanes on one CC channel, consecutive l on
+//      consecutive rows il), Zbar values -> (hi, lo) float pairs;
+//   3. the J' sums in double-float on the FP32 pipe, with pairs taken in order
+//      of (j_j, j_l) so the lanes of a warp mostly share their loop lengths;
+//   4. per channel J the block's results form a rectangle of Z (rows i j,
+//      columns k l, consecutive kets), written row-coalesced for Z(ij, kl) and
+//      column-coalesced for the mirrored Z(kl, ij).
+// FP64 appears only in the final Z += z.  Values are carried with 48-bit
+// significands (double-float), far inside the split form's 1e-10 tolerance;
+// magnitudes below the FP32 normal range (1.2e-38) are flushed to zero.
+
+constexpr int kInvqThreads = 256;
+
+// the r-th set position of the first n predicate values (n <= 64) of a warp,
+// written to out[]: a ballot compaction; returns the count
+__device__ __forceinline__ int warp_compact64(bool v0, bool v1, unsigned char x0, unsigned char x1, unsigned char* out)
+{
+  const int lane = threadIdx.x & 31;
+  const unsigned m0 = __ballot_sync(0xffffffffu, v0), m1 = __ballot_sync(0xffffffffu, v1);
+  const unsigned below = (1u << lane) - 1;
+  if (v0) out[__popc(m0 & below)] = x0;
+  if (v1) out[__popc(m0) + __popc(m1 & below)] = x1;
+  return __popc(m0) + __popc(m1);
+}
+
+// floor(r / n) for 0 <= r <= 4096, 1 <= n <= 64, with rcp = 1.0f / n: the exact
+// quotient's fractional part stays >= 1/128 from an integer, far above the
+// product's rounding error (2^-11)
+__device__ __forceinline__ int small_div(int r, float rcp) { return __float2int_rz(__fmul_rn((float)r + 0.5f, rcp)); }
+
+__global__ void __launch_bounds__(kInvqThreads) k_pandya_inv_ff(DevSpace S, DevWork W, const double* __restrict__ Zb,
+                                                             double* __restrict__ Z, int hZ,
+                                                             const int4* __restrict__ tasks,
+                                                             const int* __restrict__ clist,
+                                                             const int* __restrict__ coff,
+                                                             const unsigned char* __restrict__ csort)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_j[kInvqMaxOrb], s_l[kInvqMaxOrb], s_jj[kInvqMaxOrb], s_jl[kInvqMaxOrb];
+  __shared__ int s_kkj[kInvqMaxOrb];       // global index of the ket (k, j) / (j, k)
+  __shared__ unsigned char s_jperm[kInvqMaxOrb], s_lperm[kInvqMaxOrb];
+  __shared__ unsigned char s_jv[kInvqMaxJ][kInvqMaxOrb], s_lv[kInvqMaxJ][kInvqMaxOrb];  // per J: valid j, l
+  __shared__ int s_wn[kInvqMaxJ][2];       // per J: valid rows, valid columns
+  __shared__ float s_wr[kInvqMaxJ][2];     // their reciprocals
+  __shared__ int s_wbk[kInvqMaxJ][3];      // per J: first bra, first ket, channel size
+  __shared__ long long s_woff[kInvqMaxJ];  // per J: arena offset of the channel
+  __shared__ int s_wpre[kInvqMaxJ + 1];    // per J: prefix of rows x columns
+  __shared__ int s_cn[2][kInvqMaxJ];       // per J': CC channel size, sums 1 and 2
+  __shared__ long long s_coff[2][kInvqMaxJ];
+  __shared__ int s_cik[kInvqMaxJ];         // per J': local index of the CC ket (i, k)
+  __shared__ unsigned long long s_wsum[kInvqThreads / 32];
+  __shared__ int s_red[6];                 // unions over the block: J' of sum 1, J' of sum 2, J
+
+  const int4 tk = tasks[blockIdx.x];
+  const int i = tk.x & 0xFFFF, k = tk.x >> 16;
+  const int cj = tk.y & 0xFF, cl = (tk.y >> 8) & 0xFF;
+  const int jf = tk.z & 0xFFFF, jn = tk.z >> 16, lf = tk.w & 0xFFFF, ln = tk.w >> 16;
+  const int P = jn * ln;
+  const float rln = 1.0f / ln;  // pair p = jx ln + lx: jx = small_div(p, rln)
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int N = S.norb, nk = S.nkets;
+  if (tid < jn) {
+    int o = clist[coff[cj] + jf + tid];
+    s_j[tid] = o;
+    s_jj[tid] = S.j2[o];
+    s_kkj[tid] = ket_index(N, min(k, o), max(k, o));
+  }
+  if (tid >= 64 && tid - 64 < ln) {
+    int o = clist[coff[cl] + lf + tid - 64];
+    s_l[tid - 64] = o;
+    s_jl[tid - 64] = S.j2[o];
+  }
+  if (tid < 6) s_red[tid] = (tid & 1) ? -1 : (1 << 20);
+  if (warp == 4 || warp == 5) {
+    // slot order: the block's j (warp 4) and l (warp 5) by (2j, orbit), from
+    // the class's sorted positions, so neighbouring slots have equal loop lengths
+    const int c = warp == 4 ? cj : cl, f = warp == 4 ? jf : lf, n = warp == 4 ? jn : ln;
+    const int nc = coff[c + 1] - coff[c];
+    const int x0 = lane < nc ? csort[coff[c] + lane] - f : -1;
+    const int x1 = lane + 32 < nc ? csort[coff[c] + lane + 32] - f : -1;
+    warp_compact64(x0 >= 0 && x0 < n, x1 >= 0 && x1 < n, (unsigned char)x0, (unsigned char)x1,
+                   warp == 4 ? s_jperm : s_lperm);
+  }
+  __syncthreads();
+  const int ji = S.j2[i], jk = S.j2[k];
+
+  // 1. per pair p = jx ln + lx: counts n1 | n2 << 5 | nJ << 10, slot offsets of
+  //    its staged values (off1, off2) and results (offO), assigned in slot order
+  unsigned short* cnt = (unsigned short*)smem;
+  unsigned short* off1 = cnt + P;
+  unsigned short* off2 = off1 + P;
+  unsigned short* offO = off2 + P;
+  float2* zs = (float2*)(smem + ((8 * P + 15) & ~15));
+  unsigned long long carry = 0;
+  for (int base = 0; base < P; base += kInvqThreads) {
+    const int sidx = base + tid;
+    unsigned long long v = 0;
+    int p = 0;
+    int r0 = 1 << 20, r1 = -1, r2 = 1 << 20, r3 = -1, r4 = 1 << 20, r5 = -1;
+    if (sidx < P) {
+      const int jsx = small_div(sidx, rln);
+      const int jx = s_jperm[jsx], lx = s_lperm[sidx - jsx * ln];
+      p = jx * ln + lx;
+      int n1, n2, nJ, Jlo, lo1, lo2;
+      if (invq_counts(i, s_j[jx], k, s_l[lx], ji, s_jj[jx], jk, s_jl[lx], hZ, n1, n2, nJ, Jlo, lo1, lo2)) {
+        v = (unsigned long long)n1 | ((unsigned long long)n2 << 21) | ((unsigned long long)nJ << 42);
+        if (n1) {
+          r0 = lo1;
+          r1 = lo1 + n1 - 1;
+        }
+        if (n2) {
+          r2 = lo2;
+          r3 = lo2 + n2 - 1;
+        }
+        const bool ev = (i == s_j[jx]) || (k == s_l[lx]);
+        r4 = Jlo;
+        r5 = Jlo + (ev ? 2 : 1) * (nJ - 1);
+      }
+      cnt[p] = (unsigned short)((v & 31) | (((v >> 21) & 31) << 5) | (((v >> 42) & 31) << 10));
+    }
+    r0 = __reduce_min_sync(0xffffffffu, r0);
+    r1 = __reduce_max_sync(0xffffffffu, r1);
+    r2 = __reduce_min_sync(0xffffffffu, r2);
+    r3 = __reduce_max_sync(0xffffffffu, r3);
+    r4 = __reduce_min_sync(0xffffffffu, r4);
+    r5 = __reduce_max_sync(0xffffffffu, r5);
+    if (lane == 0) {
+      atomicMin(&s_red[0], r0);
+      atomicMax(&s_red[1], r1);
+      atomicMin(&s_red[2], r2);
+      atomicMax(&s_red[3], r3);
+      atomicMin(&s_red[4], r4);
+      atomicMax(&s_red[5], r5);
+    }
+    unsigned long long x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long t = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += t;
+    }
+    if (lane == 31) s_wsum[warp] = x;
+    __syncthreads();
+    unsigned long long wpre = 0, tot = 0;
+#pragma unroll
+    for (int w = 0; w < kInvqThreads / 32; ++w) {
+      unsigned long long t = s_wsum[w];
+      if (w < warp) wpre += t;
+      tot += t;
+    }
+    if (sidx < P) {
+      unsigned long long e = carry + wpre + x - v;
+      off1[p] = (unsigned short)(e & 0x1FFFFF);
+      off2[p] = (unsigned short)((e >> 21) & 0x1FFFFF);
+      offO[p] = (unsigned short)(e >> 42);
+    }
+    carry += tot;
+    __syncthreads();
+  }
+  const int tot1 = (int)(carry & 0x1FFFFF), tot2 = (int)((carry >> 21) & 0x1FFFFF), totO = (int)(carry >> 42);
+  const int tot12 = tot1 + tot2, nslot = tot12 + totO;
+  // regions: sum-1 values [0, tot1), sum-2 values [tot1, tot12), results [tot12, nslot);
+  // owner[slot] = its pair
+  double* outs = (double*)(zs + tot12);
+  unsigned short* owner = (unsigned short*)(zs + nslot);
+  for (int p = tid; p < P; p += kInvqThreads) {
+    const int c = cnt[p];
+    off2[p] = (unsigned short)(off2[p] + tot1);
+    const int n1 = c & 31, n2 = (c >> 5) & 31, nJ = c >> 10;
+    for (int x = 0; x < n1; ++x) owner[off1[p] + x] = (unsigned short)p;
+    for (int x = 0; x < n2; ++x) owner[off2[p] + x] = (unsigned short)p;
+    for (int x = 0; x < nJ; ++x) owner[tot12 + offO[p] + x] = (unsigned short)p;
+  }
+
+  // per-J' CC channels of both sums (a thread each) and per-J output
+  // rectangles (a warp each); empty unions (no sum-2 pairs, or no pair at all
+  // when Z is anti-hermitian and the block's only pair is diagonal) count 0
+  const int u1 = s_red[0], u2 = s_red[2], uJ = s_red[4];
+  const int n1u = max(0, s_red[1] - u1 + 1), n2u = max(0, s_red[3] - u2 + 1), nJu = max(0, s_red[5] - uJ + 1);
+  const int pl = cl & 1, tzl = (cl & 2) ? 1 : -1;
+  const int pj = cj & 1, tzj = (cj & 2) ? 1 : -1;
+  if (tid < n1u) {
+    const int cc = chan_index(u1 + tid, (S.l[i] + pl) & 1, abs(S.tz2[i] - tzl) / 2);
+    s_cn[0][tid] = S.cc_n[cc];
+    s_coff[0][tid] = W.zb_off[cc];
+  } else if (tid >= 32 && tid - 32 < n2u) {
+    const int t = tid - 32, Jp = u2 + t;
+    const int cc = chan_index(Jp, (S.l[i] + S.l[k]) & 1, abs(S.tz2[i] - S.tz2[k]) / 2);
+    s_cn[1][t] = S.cc_n[cc];
+    s_coff[1][t] = W.zb_off[cc];
+    s_cik[t] = S.ccJ_loc[(size_t)Jp * nk + ket_index(N, i, k)];
+  }
+  for (int t = warp; t < nJu; t += kInvqThreads / 32) {
+    // rows (i, j) and columns (k, l) of channel J: consecutive kets
+    const int J = uJ + t;
+    bool v0 = false, v1 = false;
+    if (lane < jn) {
+      const int jj = s_jj[lane];
+      v0 = abs(ji - jj) <= 2 * J && ji + jj >= 2 * J && !(s_j[lane] == i && (J & 1));
+    }
+    if (lane + 32 < jn) {
+      const int jj = s_jj[lane + 32];
+      v1 = abs(ji - jj) <= 2 * J && ji + jj >= 2 * J && !(s_j[lane + 32] == i && (J & 1));
+    }
+    const int nr = warp_compact64(v0, v1, (unsigned char)lane, (unsigned char)(lane + 32), s_jv[t]);
+    v0 = v1 = false;
+    if (lane < ln) {
+      const int jl = s_jl[lane];
+      v0 = abs(jk - jl) <= 2 * J && jk + jl >= 2 * J && !(s_l[lane] == k && (J & 1));
+    }
+    if (lane + 32 < ln) {
+      const int jl = s_jl[lane + 32];
+      v1 = abs(jk - jl) <= 2 * J && jk + jl >= 2 * J && !(s_l[lane + 32] == k && (J & 1));
+    }
+    const int nc = warp_compact64(v0, v1, (unsigned char)lane, (unsigned char)(lane + 32), s_lv[t]);
+    __syncwarp();
+    if (lane == 0) {
+      s_wn[t][0] = nr;
+      s_wn[t][1] = nc;
+      s_wr[t][0] = nr ? 1.0f / nr : 0.f;
+      s_wr[t][1] = nc ? 1.0f / nc : 0.f;
+      if (nr && nc) {
+        const int ch = chan_index(J, (S.l[i] + pj) & 1, (S.tz2[i] + tzj) / 2);
+        s_wbk[t][0] = S.ketJ_loc[(size_t)J * nk + ket_index(N, i, s_j[s_jv[t][0]])];
+        s_wbk[t][1] = S.ketJ_loc[(size_t)J * nk + ket_index(N, k, s_l[s_lv[t][0]])];
+        s_wbk[t][2] = S.ch_n[ch];
+        s_woff[t] = S.ch_off[ch];
+      }
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {
+    // prefix of the rectangle areas over J (nJu <= 32)
+    const int a = lane < nJu ? s_wn[lane][0] * s_wn[lane][1] : 0;
+    int x = a;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += t;
+    }
+    s_wpre[lane] = x - a;
+    if (lane == 31) s_wpre[32] = x;
+  }
+
+  // 2. staging, a thread per slot: Zbar values as (hi, lo) pairs, batches of
+  //    four slots with their loads in flight together
+  //    sum 1: Zbar_J'(il, kj); sum 2: Zbar_J'(ik, lj), read as its symmetric
+  //    partner Zbar_J'(lj, ik[+n]) (head: hZ, tail: phi phi; the sign is
+  //    applied with the sum)
+  {
+    const int kk = ket_index(N, i, 0);  // ket (i, l) = kk + l
+    for (int e0 = tid; e0 < tot12; e0 += 4 * kInvqThreads) {
+      double v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int e = e0 + u * kInvqThreads;
+        v[u] = 0.0;
+        if (e >= tot12) continue;
+        const int p = owner[e];
+        const int jx = small_div(p, rln), lx = p - jx * ln;
+        const int j = s_j[jx], l = s_l[lx], jj = s_jj[jx], jl = s_jl[lx];
+        if (e < tot1) {
+          const int Jp = (max(abs(ji - jl), abs(jk - jj)) >> 1) + e - off1[p], t = Jp - u1;
+          const int ncc = s_cn[0][t];
+          const int* cmap = S.ccJ_loc + (size_t)Jp * nk;
+          const int il = __ldg(cmap + kk + l);
+          const int kj = __ldg(cmap + s_kkj[jx]) + (k > j ? ncc : 0);
+          v[u] = __ldg(Zb + s_coff[0][t] + (long long)kj * ncc + il);
+        } else {
+          const int Jp = (max(abs(jj - jl), abs(jk - ji)) >> 1) + e - off2[p], t = Jp - u2;
+          const int ncc = s_cn[1][t];
+          const int lj = __ldg(S.ccJ_loc + (size_t)Jp * nk + ket_index(N, min(l, j), max(l, j)));
+          v[u] = __ldg(Zb + s_coff[1][t] + (long long)(s_cik[t] + (l > j ? ncc : 0)) * ncc + lj);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int e = e0 + u * kInvqThreads;
+        if (e < tot12) zs[e] = d2ff(v[u]);
+      }
+    }
+  }
+  __syncthreads();
+
+  // 3. the J' sums, a thread per result slot (pair, J)
+  {
+    const int d1 = S.d1;
+    const int a6 = (ji - 1) >> 1, c6 = (jk - 1) >> 1;
+    for (int e = tid; e < totO; e += kInvqThreads) {
+      const int p = owner[tot12 + e];
+      const int t = e - offO[p];
+      const int jx = small_div(p, rln), lx = p - jx * ln;
+      const int j = s_j[jx], l = s_l[lx], jj = s_jj[jx], jl = s_jl[lx];
+      const int c = cnt[p];
+      const int n1 = c & 31, n2 = (c >> 5) & 31;
+      const bool ev = (i == j) || (k == l);
+      int Jlo = max(abs(ji - jj), abs(jk - jl)) >> 1;
+      if (ev) Jlo += Jlo & 1;
+      const int J = Jlo + (ev ? 2 * t : t);
+      const int J3min = abs(ji - jj) >> 1;
+      const int b6 = (jj - 1) >> 1, e6 = (jl - 1) >> 1;
+      const float2* wr = S.sixj_wf + __ldg(S.sixj_base + ((a6 * d1 + b6) * d1 + c6) * d1 + e6) + (J - J3min) * n1;
+      const float2* z1 = zs + off1[p];
+      // two accumulators halve the dependency chain
+      float s1 = 0.f, c1 = 0.f, s1b = 0.f, c1b = 0.f;
+      int x = 0;
+      for (; x + 1 < n1; x += 2) {
+        df_fma(__ldg(wr + x), z1[x], s1, c1);
+        df_fma(__ldg(wr + x + 1), z1[x + 1], s1b, c1b);
+      }
+      if (x < n1) df_fma(__ldg(wr + x), z1[x], s1, c1);
+      float hi, lo;
+      df_add(s1, c1, s1b, c1b, s1, c1);
+      const int phJ = iphase((jk + jl) / 2 - J);
+      if (ev) {
+        // z = (1 - phJ [ph4]) A1: 0 or 2 A1
+        const int f = (k == l) ? phJ : phJ * iphase((ji + jj + jk + jl) / 2);
+        hi = f > 0 ? 0.f : __fmul_rn(s1, 2.f);
+        lo = f > 0 ? 0.f : __fmul_rn(c1, 2.f);
+      } else {
+        const float2* wq = S.sixj_wf + __ldg(S.sixj_base + ((b6 * d1 + a6) * d1 + c6) * d1 + e6) + (J - J3min) * n2;
+        const float2* z2 = zs + off2[p];
+        float s2 = 0.f, c2 = 0.f, s2b = 0.f, c2b = 0.f;
+        x = 0;
+        for (; x + 1 < n2; x += 2) {
+          df_fma(__ldg(wq + x), z2[x], s2, c2);
+          df_fma(__ldg(wq + x + 1), z2[x + 1], s2b, c2b);
+        }
+        if (x < n2) df_fma(__ldg(wq + x), z2[x], s2, c2);
+        df_add(s2, c2, s2b, c2b, s2, c2);
+        // z = A1 - phJ tsign A2
+        const int tsign = (l > j) ? iphase((ji + jj + jk + jl) / 2) : hZ;
+        if (phJ * tsign > 0) {
+          s2 = -s2;
+          c2 = -c2;
+        }
+        df_add(s1, c1, s2, c2, hi, lo);
+      }
+      double z = ff2d(hi, lo);
+      if (i == j && k == l) z *= 0.5;
+      else if (ev) z *= 0.70710678118654752440;
+      outs[e] = z;
+    }
+  }
+  __syncthreads();
+
+  // 4. Z += z over the block's rectangles, all J at once: pass 0 writes
+  //    Z(ij, kl) with consecutive lanes on consecutive bras, pass 1 the
+  //    mirrored Z(kl, ij) = hZ z with consecutive lanes on consecutive kets.
+  //    Items of a thread increase, so the rectangle index only moves forward;
+  //    batches of four items keep four loads of Z in flight.
+  const int T = s_wpre[nJu];
+  for (int mir = 0; mir < 2; ++mir) {
+    int t = 0;
+    for (int e0 = tid; e0 < T; e0 += 4 * kInvqThreads) {
+      long long addr[4];
+      double zv[4], old[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        addr[u] = -1;
+        const int e = e0 + u * kInvqThreads;
+        if (e >= T) continue;
+        while (s_wpre[t + 1] <= e) ++t;
+        const int r = e - s_wpre[t];
+        int jr, lr;
+        if (mir) {
+          jr = small_div(r, s_wr[t][1]);
+          lr = r - jr * s_wn[t][1];
+        } else {
+          lr = small_div(r, s_wr[t][0]);
+          jr = r - lr * s_wn[t][0];
+        }
+        const int jx = s_jv[t][jr], lx = s_lv[t][lr];
+        const int p = jx * ln + lx;
+        if (!(cnt[p] >> 10)) continue;
+        const int ib = s_wbk[t][0] + jr, ik = s_wbk[t][1] + lr;
+        if (mir && ib == ik) continue;
+        const int J = uJ + t;
+        const bool ev = (i == s_j[jx]) || (k == s_l[lx]);
+        int Jlo = max(abs(ji - s_jj[jx]), abs(jk - s_jl[lx])) >> 1;
+        if (ev) Jlo += Jlo & 1;
+        const double z = outs[offO[p] + (ev ? (J - Jlo) >> 1 : J - Jlo)];
+        const int n = s_wbk[t][2];
+        addr[u] = s_woff[t] + (mir ? (long long)ib * n + ik : (long long)ik * n + ib);
+        zv[u] = mir ? dneg_if(z, hZ < 0) : z;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (addr[u] >= 0) old[u] = Z[addr[u]];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (addr[u] >= 0) Z[addr[u]] = old[u] + zv[u];
+    }
   }
 }
 
@@ -817,6 +1256,19 @@ cudaError_t launch_pandya_inv(const Space& s, const double* Zb, double* Z, int h
 {
   if (ntiles == 0) return cudaSuccess;
   k_pandya_inv<<<ntiles, 256, 0, st>>>(s.dev, s.work, Zb, Z, hZ, tiles, ntiles);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pandya_inv_ff(const Space& s, const double* Zb, double* Z, int hZ, const int* tasks, int ntasks,
+                                 const int* clist, const int* coff, const unsigned char* csort, int smem,
+                                 cudaStream_t st)
+{
+  if (ntasks == 0) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(k_pandya_inv_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  k_pandya_inv_ff<<<ntasks, kInvqThreads, smem, st>>>(s.dev, s.work, Zb, Z, hZ, (const int4*)tasks, clist, coff,
+                                                        csort);
   count_launch();
   return cudaGetLastError();
 }

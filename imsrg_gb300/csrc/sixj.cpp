@@ -189,6 +189,12 @@ void build_sixj_table(Space& s)
               s.sixj_wval[k] = std::fabs(v) < 1e-8 ? 0.0 : (2 * J6 + 1) * v;
             }
         }
+  // (hi, lo) float pairs of the weights for the double-float kernels
+  s.sixj_wf.resize(tot);
+  for (size_t k = 0; k < tot; ++k) {
+    float hi = (float)s.sixj_wval[k];
+    s.sixj_wf[k] = float2{hi, (float)(s.sixj_wval[k] - (double)hi)};
+  }
 }
 
 double sixj_lookup(const Space& s, int jj1, int jj2, int J3, int jj4, int jj5, int J6)

@@ -356,6 +356,7 @@ void upload_space(Space& s)
   d.sixj_base = dev_copy(s, s.sixj_base);
   d.sixj_val = dev_copy(s, s.sixj_val);
   d.sixj_wval = dev_copy(s, s.sixj_wval);
+  d.sixj_wf = dev_copy(s, s.sixj_wf);
 
   DevWork& w = s.work;
   w.ket_wpp = dev_copy(s, s.ket_wpp);
@@ -384,6 +385,92 @@ void upload_space(Space& s)
   w.xb_off = dev_copy(s, xo);
   w.zb_off = dev_copy(s, zo);
   w.cc_phase_off = dev_copy(s, s.cc_phase_off);
+}
+
+// Blocks of the quadruple-ordered inverse Pandya transform (split form).
+// Orbits fall into four classes by (parity, Tz).  For a bra orbit i, a ket
+// orbit k >= i and the class of j, the class of l is fixed by parity and Tz
+// conservation, and every quadruple (i, j, k, l) of that (i, k, class) has its
+// Z elements in one rectangle per channel J: rows (i, j), columns (k, l),
+// consecutive kets in the channel's order.  A block takes such an (i, k, class)
+// group, or a run of its j rows when the group's Zbar values and results would
+// not fit in `budget` bytes of shared memory.
+void build_invq_tasks(Space& s, int budget)
+{
+  const int N = s.norb;
+  s.cls_list.clear();
+  s.cls_off.assign(5, 0);
+  s.invq_tasks.clear();
+  s.invq_smem = 0;
+  bool fits = s.NJ < kInvqMaxJ;  // J' and J counts < 32: 5-bit fields
+  for (int c = 0; c < 4; ++c) {
+    s.cls_off[c] = (int)s.cls_list.size();
+    for (int o = 0; o < N; ++o)
+      if (((s.l[o] & 1) | (s.tz2[o] > 0 ? 2 : 0)) == c) s.cls_list.push_back(o);
+    if ((int)s.cls_list.size() - s.cls_off[c] > kInvqMaxOrb) fits = false;
+  }
+  s.cls_off[4] = (int)s.cls_list.size();
+  s.cls_sort.assign(s.cls_list.size(), 0);
+  for (int c = 0; c < 4; ++c) {
+    std::vector<int> pos;
+    for (int x = 0; x < s.cls_off[c + 1] - s.cls_off[c]; ++x) pos.push_back(x);
+    const int* o = s.cls_list.data() + s.cls_off[c];
+    std::stable_sort(pos.begin(), pos.end(), [&](int a, int b) { return s.j2[o[a]] < s.j2[o[b]]; });
+    for (size_t x = 0; x < pos.size(); ++x) s.cls_sort[s.cls_off[c] + x] = (unsigned char)pos[x];
+  }
+  // beyond the block's table sizes (emax > 14 for a full space) the split form
+  // keeps the channel-tiled kernel: no blocks
+  if (!fits) return;
+  auto emit = [&](int i, int k, int cj, int cl, int jf, int jn, int lf, int ln, int slots) {
+    s.invq_tasks.push_back(i | (k << 16));
+    s.invq_tasks.push_back(cj | (cl << 8));
+    s.invq_tasks.push_back(jf | (jn << 16));
+    s.invq_tasks.push_back(lf | (ln << 16));
+    s.invq_smem = std::max(s.invq_smem, invq_block_bytes(jn, ln, slots));
+  };
+  for (int i = 0; i < N; ++i)
+    for (int k = i; k < N; ++k)
+      for (int cj = 0; cj < 4; ++cj) {
+        int pj = cj & 1, tzj = (cj & 2) ? 1 : -1;
+        int tzl = s.tz2[i] + tzj - s.tz2[k];
+        if (tzl != 1 && tzl != -1) continue;
+        int cl = ((s.l[i] + pj + s.l[k]) & 1) | (tzl > 0 ? 2 : 0);
+        const int* Jc = s.cls_list.data() + s.cls_off[cj];
+        const int* Lc = s.cls_list.data() + s.cls_off[cl];
+        int nJc = s.cls_off[cj + 1] - s.cls_off[cj], nLc = s.cls_off[cl + 1] - s.cls_off[cl];
+        int jf = (int)(std::lower_bound(Jc, Jc + nJc, i) - Jc);
+        int lf = (int)(std::lower_bound(Lc, Lc + nLc, k) - Lc);
+        int jtot = nJc - jf, ln = nLc - lf;
+        if (jtot <= 0 || ln <= 0) continue;
+        int r0 = 0, slots = 0;
+        bool any = false;
+        for (int r = 0; r < jtot; ++r) {
+          int j = Jc[jf + r];
+          int rs = 0;
+          bool ra = false;
+          for (int x = 0; x < ln; ++x) {
+            int l = Lc[lf + x];
+            int n1, n2, nJ, Jlo, lo1, lo2;
+            if (invq_counts(i, j, k, l, s.j2[i], s.j2[j], s.j2[k], s.j2[l], 1, n1, n2, nJ, Jlo, lo1, lo2)) {
+              rs += n1 + n2 + nJ;
+              ra = true;
+            }
+          }
+          if (r > r0 && invq_block_bytes(r - r0 + 1, ln, slots + rs) > budget) {
+            if (any) emit(i, k, cj, cl, jf + r0, r - r0, lf, ln, slots);
+            r0 = r;
+            slots = 0;
+            any = false;
+          }
+          slots += rs;
+          any = any || ra;
+        }
+        if (any) emit(i, k, cj, cl, jf + r0, jtot - r0, lf, ln, slots);
+      }
+  if (s.invq_smem > 160 * 1024) {
+    s.invq_tasks.clear();
+    s.invq_smem = 0;
+  }
 }
 
 Space::~Space()

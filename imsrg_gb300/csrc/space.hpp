@@ -49,6 +49,7 @@ struct Space {
   std::vector<int> sixj_base;
   std::vector<double> sixj_val;
   std::vector<double> sixj_wval;  // (2 J6 + 1) * value, 0 where |value| < 1e-8
+  std::vector<float2> sixj_wf;    // sixj_wval as (hi, lo) float pairs
 
   // ---- work lists
   // ladder (comm222_pp_hh): per channel, kets with nonzero weight and weights
@@ -76,6 +77,11 @@ struct Space {
   std::vector<int> cols122;             // (ch, column, first item, item count), flattened
   std::vector<int> it122_loc, it122_a, it122_src;
   std::vector<double> it122_f;
+  // inverse Pandya by orbit quadruple (split form, see build_invq_tasks)
+  std::vector<int> cls_list, cls_off;  // orbits of each (parity, Tz) class, ascending; offsets (5)
+  std::vector<unsigned char> cls_sort; // per class: positions in cls_list ordered by (2j, position)
+  std::vector<int> invq_tasks;         // 4 ints per block: i | k << 16, cj | cl << 8, jf | jn << 16, lf | ln << 16
+  int invq_smem = 0;                   // dynamic shared memory of the largest block (bytes)
 
   DevSpace dev{};     // device copies of the tables (pointers owned below)
   DevWork work{};
@@ -99,6 +105,12 @@ void reference_orbits(int emax, int A, int Z, std::vector<int>& n, std::vector<i
                       std::vector<int>& tz2, std::vector<double>& occ);
 // copies the tables to the device (cudaMalloc); throws on failure
 void upload_space(Space& s);
+// blocks of the quadruple-ordered inverse Pandya transform, each within
+// budget bytes of shared memory (fills cls_list, cls_off, invq_tasks, invq_smem)
+void build_invq_tasks(Space& s, int budget);
+// shared memory of one block of jn x ln quadruples holding `slots` values:
+// four 16-bit counts/offsets per pair, per slot an 8-byte value and its 16-bit owner
+inline int invq_block_bytes(int jn, int ln, int slots) { return ((8 * jn * ln + 15) & ~15) + 10 * slots; }
 
 // 6j table construction (sixj.cpp)
 double sixj_dd(int jj1, int jj2, int jj3, int jj4, int jj5, int jj6);  // doubled arguments
