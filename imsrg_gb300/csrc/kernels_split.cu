@@ -87,6 +87,9 @@ struct SplitPlan {
   int* d_rexpB = nullptr;
   int* d_jobmax = nullptr;  // [2 * njobs]: max exponent of A, of B
   int* d_flags = nullptr;   // [2 * njobs]: gamma used, delta used (set per launch)
+  int4* d_rblk = nullptr;   // exponent blocks (job, 32-row group, 256-column chunk)
+  int4* d_dblk = nullptr;   // digit blocks (job, 32-row group, KB-column chunk), jobs in reverse order
+  int n_rblk = 0, n_dblk = 0;
   CUtensorMap maps[4];
   int grid = 0;
   size_t smem = 0;
@@ -203,14 +206,6 @@ __device__ __forceinline__ void set_status(int* st, int code)
 // biased exponent field of a double (0 for zero / subnormal)
 __device__ __forceinline__ int dexp(double v) { return (int)((__double_as_longlong(v) >> 52) & 0x7FF); }
 
-// operand value with the launch / job / column scale of B
-__device__ __forceinline__ double scaled(double v, double sc)
-{
-  if (sc == 1.0) return v;
-  if (sc == -1.0) return -v;
-  return v * sc;
-}
-
 // q = round(v * 2^(P - e)) for |v| < 2^e, P = beta*S <= 42; integer only
 __device__ __forceinline__ long long to_fixed(double v, int e, int P)
 {
@@ -224,13 +219,39 @@ __device__ __forceinline__ long long to_fixed(double v, int e, int P)
   return bits < 0 ? -q : q;
 }
 
+// ------------------------------------------------------------ column scales
+// The B operand is taken with a per-column scale (job scale x launch scale x
+// ladder weight).  A scale that is a signed power of two, as every weight of
+// a closed-shell reference is, is applied by exponent arithmetic and a sign
+// (integer instructions); any other scale by an FP64 multiply.
+constexpr int SC_GENERAL = 0x40000000;
+
+// code of a scale: (k << 1) | sign for +-2^k, SC_GENERAL otherwise
+__device__ __forceinline__ int scale_code(double sc)
+{
+  const long long b = __double_as_longlong(sc);
+  const int E = (int)((b >> 52) & 0x7FF);
+  if ((b & 0xFFFFFFFFFFFFFll) != 0 || E == 0 || E == 0x7FF) return SC_GENERAL;
+  return ((E - 1023) << 1) | (int)((unsigned long long)b >> 63);
+}
+
+// biased exponent of v * scale (0 for zero / subnormal)
+__device__ __forceinline__ int dexp_scaled(double v, int code, double sc)
+{
+  if (code == SC_GENERAL) return dexp(v * sc);
+  const int e = dexp(v);
+  if (e == 0) return 0;
+  const int es = e + (code >> 1);
+  return es < 1 ? 0 : es;
+}
+
 // ------------------------------------------------------------ exponents
 // raw row exponents (max biased exponent over the row) of A and B, and the
-// per-job maxima.  Block = 32 rows x 8 column lanes over a 256-column chunk;
-// partial maxima combine through atomicMax (the arrays are zeroed first).
-// The exponent of B includes the job / column scale (a power of two or a
-// weight) so the B digits are taken of the scaled values.
-__global__ void __launch_bounds__(256) k_split_rowexp(const SplitJob* __restrict__ jobs, int njobs,
+// per-job maxima.  One block per listed (job, 32-row group, 256-column chunk):
+// 32 rows x 8 column lanes; partial maxima combine through atomicMax (the
+// arrays are zeroed first).  The exponent of B includes the column scale so
+// the B digits are taken of the scaled values.
+__global__ void __launch_bounds__(256) k_split_rowexp(const SplitJob* __restrict__ jobs, const int4* __restrict__ blocks,
                                                       const double* __restrict__ Abase,
                                                       const double* __restrict__ B0, const double* __restrict__ B1,
                                                       const int* __restrict__ kidx, const double* __restrict__ kw,
@@ -238,15 +259,14 @@ __global__ void __launch_bounds__(256) k_split_rowexp(const SplitJob* __restrict
                                                       int* __restrict__ rexpB, int* __restrict__ jobmax)
 {
   __shared__ int sa[8][33], sb[8][33];
-  __shared__ int s_col[256];
+  __shared__ int s_col[256], s_code[256];
   __shared__ double s_sc[256];
-  int job = blockIdx.z;
-  if (job >= njobs) return;
+  const int4 bk = blocks[blockIdx.x];
+  const int job = bk.x;
   const SplitJob jb = jobs[job];
   const int r = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int i = blockIdx.y * 32 + r;
-  const int t0 = blockIdx.x * 256;
-  if (blockIdx.y * 32 >= jb.m_pad || t0 >= max(jb.K, 1)) return;
+  const int i = bk.y * 32 + r;
+  const int t0 = bk.z * 256;
   const int tend = min(jb.K, t0 + 256);
   {
     // column indices and scales of this chunk, once per block
@@ -255,8 +275,10 @@ __global__ void __launch_bounds__(256) k_split_rowexp(const SplitJob* __restrict
     const double sc0 = jb.bscale * gbscale;
     const int t = t0 + threadIdx.x;
     if (t < tend) {
+      const double sc = w ? sc0 * w[t] : sc0;
       s_col[threadIdx.x] = kx ? kx[t] : t;
-      s_sc[threadIdx.x] = w ? sc0 * w[t] : sc0;
+      s_sc[threadIdx.x] = sc;
+      s_code[threadIdx.x] = scale_code(sc);
     }
   }
   __syncthreads();
@@ -267,7 +289,7 @@ __global__ void __launch_bounds__(256) k_split_rowexp(const SplitJob* __restrict
     for (int t = t0 + ty; t < tend; t += 8) {
       const int col = s_col[t - t0];
       ea = max(ea, dexp(A[(long long)col * jb.lda + i]));
-      eb = max(eb, dexp(scaled(B[(long long)col * jb.ldb + i], s_sc[t - t0])));
+      eb = max(eb, dexp_scaled(B[(long long)col * jb.ldb + i], s_code[t - t0], s_sc[t - t0]));
     }
   }
   sa[ty][r] = ea;
@@ -332,12 +354,13 @@ __device__ __forceinline__ int job_c(const int* jobmax, int job)
 }
 
 // ---------------------------------------------------------------- digits
-// One block per (job, 32-row group, 64-column group): digits of A and B rows
-// into shared memory, then coalesced 16-byte stores of the four slice arrays
+// One block per listed (job, 32-row group, KB-column group): digits of A and
+// B rows into shared memory, then coalesced 16-byte stores of the four slice
+// arrays
 //   alpha = A digits, beta = B digits, gamma = s phi_i B digits, delta = phi_i A digits
 // (gamma / delta written only when they differ from beta / alpha).
 template <int S>
-__global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict__ jobs, int njobs,
+__global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict__ jobs, const int4* __restrict__ blocks,
                                                      const double* __restrict__ Abase,
                                                      const double* __restrict__ B0, const double* __restrict__ B1,
                                                      const int* __restrict__ kidx, const double* __restrict__ kw,
@@ -348,45 +371,56 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
                                                      __nv_bfloat16* __restrict__ alpha, __nv_bfloat16* __restrict__ bet,
                                                      __nv_bfloat16* __restrict__ gam, __nv_bfloat16* __restrict__ del)
 {
-  __shared__ unsigned short dA[S][32][KB + 8];
-  __shared__ unsigned short dB[S][32][KB + 8];
+  __shared__ __align__(16) unsigned short dA[S][32][KB + 8];
+  __shared__ __align__(16) unsigned short dB[S][32][KB + 8];
   __shared__ int rowA[32], rowB[32], rowsg[32], rowph[32];
-  int job = blockIdx.z;
-  if (job >= njobs) return;
+  __shared__ int s_col[KB], s_code[KB];
+  __shared__ double s_sc[KB];
+  const int4 bk = blocks[blockIdx.x];
+  const int job = bk.x;
   const SplitJob jb = jobs[job];
-  int r0 = blockIdx.y * 32;
-  int t0 = blockIdx.x * KB;
-  if (r0 >= jb.m_pad || t0 >= jb.K_pad) return;
-  int c = job_c(jobmax, job);
-  int sign = jb.sign != 0 ? jb.sign : gsign;
+  const int r0 = bk.y * 32;
+  const int t0 = bk.z * KB;
+  const int c = job_c(jobmax, job);
+  const int sign = jb.sign != 0 ? jb.sign : gsign;
   const int* ph = jb.phase_off >= 0 ? phase + jb.phase_off : nullptr;
   if (threadIdx.x < 32) {
-    int i = r0 + threadIdx.x;
-    int a = row_exp(rexpA[jb.exp_base + i], rexpB[jb.exp_base + i], c);
+    const int i = r0 + threadIdx.x;
+    const int a = row_exp(rexpA[jb.exp_base + i], rexpB[jb.exp_base + i], c);
     rowA[threadIdx.x] = a;
     rowB[threadIdx.x] = a + c;
-    int p = (ph && i < jb.m) ? ph[i] : 1;
+    const int p = (ph && i < jb.m) ? ph[i] : 1;
     rowph[threadIdx.x] = p;
     rowsg[threadIdx.x] = sign * p;
+  } else if (threadIdx.x < 32 + KB) {
+    const int tt = threadIdx.x - 32, t = t0 + tt;
+    if (t < jb.K) {
+      const double sc = jb.w_off >= 0 ? jb.bscale * gbscale * kw[jb.w_off + t] : jb.bscale * gbscale;
+      s_col[tt] = jb.kidx_off >= 0 ? kidx[jb.kidx_off + t] : t;
+      s_sc[tt] = sc;
+      s_code[tt] = scale_code(sc);
+    }
   }
   __syncthreads();
   const double* A = Abase + jb.a_off;
   const double* B = (jb.bsel ? B1 : B0) + jb.b_off;
-  const int* kx = jb.kidx_off >= 0 ? kidx + jb.kidx_off : nullptr;
-  const double* w = jb.w_off >= 0 ? kw + jb.w_off : nullptr;
   const int P = beta * S;
   const long long half = 1ll << (beta - 1), mask = (1ll << beta) - 1;
-  double sc0 = jb.bscale * gbscale;
   // element (r, tt): thread layout r fastest (coalesced column reads)
   for (int e = threadIdx.x; e < 32 * KB; e += 256) {
     int r = e & 31, tt = e >> 5;
     int i = r0 + r, t = t0 + tt;
     long long qa = 0, qb = 0;
     if (i < jb.m && t < jb.K) {
-      int col = kx ? __ldg(kx + t) : t;
-      double sc = w ? sc0 * __ldg(w + t) : sc0;
+      const int col = s_col[tt], code = s_code[tt];
       qa = to_fixed(A[(long long)col * jb.lda + i], rowA[r], P);
-      qb = to_fixed(scaled(B[(long long)col * jb.ldb + i], sc), rowB[r], P);
+      const double vb = B[(long long)col * jb.ldb + i];
+      if (code == SC_GENERAL) {
+        qb = to_fixed(vb * s_sc[tt], rowB[r], P);
+      } else {
+        qb = to_fixed(vb, rowB[r] - (code >> 1), P);
+        if (code & 1) qb = -qb;
+      }
     }
     // digits of |q| by shifts (32-bit digit arithmetic), then the carry that
     // makes them balanced, then the sign: |d| <= 2^(beta-1) below the top
@@ -402,9 +436,6 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
       if (s > 0) {
         da[s] &= (int)mask;
         db[s] &= (int)mask;
-      } else {
-        da[0] = (int)(ua >> sh);
-        db[0] = (int)(ub >> sh);
       }
     }
 #pragma unroll
@@ -431,17 +462,11 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
   const bool need_g = flags[2 * job] != 0, need_d = flags[2 * job + 1] != 0;
   // stores: each thread one 16-byte vector (8 digits) of one row of one slice
   for (int e = threadIdx.x; e < S * 32 * (KB / 8); e += 256) {
-    int v = e % (KB / 8), r = (e / (KB / 8)) & 31, s = e / (32 * (KB / 8));
-    long long row = jb.row_base + (long long)s * jb.m_pad + r0 + r;
-    long long o = row * K_stride + t0 + v * 8;
-    uint4 va, vb;
-    unsigned short* pa = (unsigned short*)&va;
-    unsigned short* pb = (unsigned short*)&vb;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      pa[k] = dA[s][r][v * 8 + k];
-      pb[k] = dB[s][r][v * 8 + k];
-    }
+    const int v = e % (KB / 8), r = (e / (KB / 8)) & 31, s = e / (32 * (KB / 8));
+    const long long row = jb.row_base + (long long)s * jb.m_pad + r0 + r;
+    const long long o = row * K_stride + t0 + v * 8;
+    const uint4 va = *(const uint4*)&dA[s][r][v * 8];
+    const uint4 vb = *(const uint4*)&dB[s][r][v * 8];
     *(uint4*)(alpha + o) = va;
     *(uint4*)(bet + o) = vb;
     if (need_g) {
@@ -873,6 +898,28 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
         flags[2 * p->njobs * gs + 2 * j + 1] = sj.phase_off >= 0 ? 1 : 0;
       }
     cudaMemcpy(p->d_flags, flags.data(), sizeof(int) * flags.size(), cudaMemcpyHostToDevice);
+    // slicing blocks: only the (row group, column chunk) blocks each job has;
+    // the digit pass visits jobs in the reverse order of the exponent pass, so
+    // it starts on the operands the exponent pass read last (still in L2)
+    std::vector<int4> rb, db;
+    for (int j = 0; j < p->njobs; ++j) {
+      const SplitJob& sj = p->jobs[j];
+      if (sj.m == 0) continue;
+      for (int y = 0; y < sj.m_pad / 32; ++y)
+        for (int x = 0; x < (std::max(sj.K, 1) + 255) / 256; ++x) rb.push_back(make_int4(j, y, x, 0));
+    }
+    for (int j = p->njobs - 1; j >= 0; --j) {
+      const SplitJob& sj = p->jobs[j];
+      if (sj.m == 0) continue;
+      for (int y = 0; y < sj.m_pad / 32; ++y)
+        for (int x = 0; x < sj.K_pad / KB; ++x) db.push_back(make_int4(j, y, x, 0));
+    }
+    p->n_rblk = (int)rb.size();
+    p->n_dblk = (int)db.size();
+    p->d_rblk = (int4*)dm(sizeof(int4) * std::max<size_t>(1, rb.size()));
+    p->d_dblk = (int4*)dm(sizeof(int4) * std::max<size_t>(1, db.size()));
+    cudaMemcpy(p->d_rblk, rb.data(), sizeof(int4) * rb.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(p->d_dblk, db.data(), sizeof(int4) * db.size(), cudaMemcpyHostToDevice);
     long long rows_map = std::max(row, (long long)TILE_M);
     // every operand tile is loaded in 64-row boxes (an A tile is two of them),
     // so one map per array serves both operand roles
@@ -904,6 +951,8 @@ void split_plan_destroy(SplitPlan* p)
   cudaFree(p->d_rexpB);
   cudaFree(p->d_jobmax);
   cudaFree(p->d_flags);
+  cudaFree(p->d_rblk);
+  cudaFree(p->d_dblk);
   delete p;
 }
 
@@ -925,24 +974,20 @@ static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, con
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(p->d_rexpB, 0, sizeof(int) * std::max(1ll, p->total_exp_rows), st);
     if (e != cudaSuccess) return e;
-    int mp = 0, kmax = 1;
-    for (const SplitJob& j : p->jobs) {
-      mp = std::max(mp, j.m_pad);
-      kmax = std::max(kmax, j.K);
+    if (p->n_rblk > 0) {
+      k_split_rowexp<<<p->n_rblk, 256, 0, st>>>(p->d_jobs, p->d_rblk, A, B0, B1, kidx, kw, gbscale, p->d_rexpA,
+                                                p->d_rexpB, p->d_jobmax);
+      count_launch();
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    dim3 g1((kmax + 255) / 256, (mp + 31) / 32, p->njobs);
-    k_split_rowexp<<<g1, 256, 0, st>>>(p->d_jobs, p->njobs, A, B0, B1, kidx, kw, gbscale, p->d_rexpA, p->d_rexpB,
-                                       p->d_jobmax);
-    count_launch();
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    int kpmax = 0;
-    for (const SplitJob& sj : p->jobs) kpmax = std::max(kpmax, sj.K_pad);
-    dim3 g2((kpmax + KB - 1) / KB, (mp + 31) / 32, p->njobs);
-    k_split_digits<S><<<g2, 256, 0, st>>>(p->d_jobs, p->njobs, A, B0, B1, kidx, kw, phase, gbscale, gsign,
-                                          p->d_rexpA, p->d_rexpB, p->d_jobmax, flags_for(p, gsign), p->beta,
-                                          p->K_stride, p->arr[0], p->arr[1], p->arr[2], p->arr[3]);
-    count_launch();
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (p->n_dblk > 0) {
+      k_split_digits<S><<<p->n_dblk, 256, 0, st>>>(p->d_jobs, p->d_dblk, A, B0, B1, kidx, kw, phase, gbscale, gsign,
+                                                    p->d_rexpA, p->d_rexpB, p->d_jobmax, flags_for(p, gsign),
+                                                    p->beta, p->K_stride, p->arr[0], p->arr[1], p->arr[2],
+                                                    p->arr[3]);
+      count_launch();
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
   }
   {
     ProfScope ps(p->family == 0 ? "split_gemm_ladder" : "split_gemm_zbar", st);
