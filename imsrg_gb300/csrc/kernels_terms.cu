@@ -273,6 +273,40 @@ __device__ __forceinline__ void df_fma(float2 a, float2 b, float& s, float& c)
   c = __fadd_rn(c, __fadd_rn(err, e));
 }
 
+// (hi, lo) -> double with integer instructions: hi exactly, then lo added as
+// a whole number of ulps of hi (|lo| <= ulp_f32(hi) / 2, so hi + lo stays in
+// hi's binade except just below a power of two, where the ulps halve)
+__device__ __forceinline__ double ff2d(float hi, float lo)
+{
+  unsigned hb = __float_as_uint(hi), lb = __float_as_uint(lo);
+  int eh = (hb >> 23) & 0xFF, el = (lb >> 23) & 0xFF;
+  if (eh == 0) return f2d(lo);
+  double h = f2d(hi);
+  if (el == 0) return h;
+  long long bits = __double_as_longlong(h);
+  int sh = el - eh + 29;  // lo = m 2^(el-150), ulp(h) = 2^(eh-179)
+  long long m = (long long)((lb & 0x7FFFFFu) | 0x800000u);
+  long long off = sh >= 0 ? (m << sh) : (sh > -25 ? (m >> -sh) : 0ll);
+  if ((hb ^ lb) >> 31) {
+    if ((bits & 0xFFFFFFFFFFFFFll) == 0) off <<= 1;
+    bits -= off;
+  } else {
+    bits += off;
+  }
+  return __longlong_as_double(bits);
+}
+
+// (hi, lo) = (s1 + c1) + (s2 + c2), renormalised
+__device__ __forceinline__ void df_add(float s1, float c1, float s2, float c2, float& hi, float& lo)
+{
+  float s = __fadd_rn(s1, s2);
+  float bb = __fsub_rn(s, s1);
+  float e = __fadd_rn(__fsub_rn(s1, __fsub_rn(s, bb)), __fsub_rn(s2, bb));
+  e = __fadd_rn(e, __fadd_rn(c1, c2));
+  hi = __fadd_rn(s, e);
+  lo = __fsub_rn(e, __fsub_rn(hi, s));
+}
+
 // FP64 arena -> (hi, lo) pairs, integer instructions only
 __global__ void k_to_ff(const double* __restrict__ src, float2* __restrict__ dst, long long n)
 {
@@ -321,11 +355,13 @@ __global__ void __launch_bounds__(128) k_comm122_w_df(DevSpace S, DevWork W, con
   }
 }
 
-// Z2 -= W2 + hZ W2^T with W2 in (hi, lo) pairs, per channel in 32x32 tiles
+// Z2 -= W2 + hZ W2^T with W2 in (hi, lo) pairs, per channel in 32x32 tiles:
+// the pair sum in double-float, converted with integer instructions, so the
+// only FP64 instruction per element is the subtraction from Z2
 __global__ void k_sym_subtract_ff(DevSpace S, const float2* __restrict__ W2, double* __restrict__ Z, int hZ,
                                   const int* __restrict__ tiles, int ntiles)
 {
-  __shared__ double tt[32][33];
+  __shared__ float2 tt[32][33];
   int t = blockIdx.x;
   if (t >= ntiles) return;
   int ch = tiles[3 * t], ti = tiles[3 * t + 1], tj = tiles[3 * t + 2];
@@ -334,20 +370,23 @@ __global__ void k_sym_subtract_ff(DevSpace S, const float2* __restrict__ W2, dou
   int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   for (int yy = ty; yy < 32; yy += 8) {
     int r = tj * 32 + tx, c = ti * 32 + yy;
-    double v = 0.0;
-    if (r < n && c < n) {
-      float2 w = W2[off + (long long)c * n + r];
-      v = f2d(w.x) + f2d(w.y);
-    }
+    float2 v = make_float2(0.f, 0.f);
+    if (r < n && c < n) v = W2[off + (long long)c * n + r];
     tt[yy][tx] = v;
   }
   __syncthreads();
   for (int yy = ty; yy < 32; yy += 8) {
     int r = ti * 32 + tx, c = tj * 32 + yy;
     if (r < n && c < n) {
-      float2 w = W2[off + (long long)c * n + r];
-      double v = f2d(w.x) + f2d(w.y);
-      Z[off + (long long)c * n + r] -= v + hZ * tt[tx][yy];
+      const float2 w = W2[off + (long long)c * n + r];
+      float2 u = tt[tx][yy];
+      if (hZ < 0) {
+        u.x = -u.x;
+        u.y = -u.y;
+      }
+      float hi, lo;
+      df_add(w.x, w.y, u.x, u.y, hi, lo);
+      Z[off + (long long)c * n + r] -= ff2d(hi, lo);
     }
   }
 }
@@ -543,40 +582,6 @@ __global__ void k_pandya_fwd(DevSpace S, DevWork W, const double* __restrict__ X
   const int* phi = W.phase_tab + W.cc_phase_off[cc];
   int tf = t < nph ? t + nph : t - nph;
   Yf[base + (long long)tf * ncc + ik] = yv * phi[kb] * phi[ik] * hY;
-}
-
-// (hi, lo) -> double with integer instructions: hi exactly, then lo added as
-// a whole number of ulps of hi (|lo| <= ulp_f32(hi) / 2, so hi + lo stays in
-// hi's binade except just below a power of two, where the ulps halve)
-__device__ __forceinline__ double ff2d(float hi, float lo)
-{
-  unsigned hb = __float_as_uint(hi), lb = __float_as_uint(lo);
-  int eh = (hb >> 23) & 0xFF, el = (lb >> 23) & 0xFF;
-  if (eh == 0) return f2d(lo);
-  double h = f2d(hi);
-  if (el == 0) return h;
-  long long bits = __double_as_longlong(h);
-  int sh = el - eh + 29;  // lo = m 2^(el-150), ulp(h) = 2^(eh-179)
-  long long m = (long long)((lb & 0x7FFFFFu) | 0x800000u);
-  long long off = sh >= 0 ? (m << sh) : (sh > -25 ? (m >> -sh) : 0ll);
-  if ((hb ^ lb) >> 31) {
-    if ((bits & 0xFFFFFFFFFFFFFll) == 0) off <<= 1;
-    bits -= off;
-  } else {
-    bits += off;
-  }
-  return __longlong_as_double(bits);
-}
-
-// (hi, lo) = (s1 + c1) + (s2 + c2), renormalised
-__device__ __forceinline__ void df_add(float s1, float c1, float s2, float c2, float& hi, float& lo)
-{
-  float s = __fadd_rn(s1, s2);
-  float bb = __fsub_rn(s, s1);
-  float e = __fadd_rn(__fsub_rn(s1, __fsub_rn(s, bb)), __fsub_rn(s2, bb));
-  e = __fadd_rn(e, __fadd_rn(c1, c2));
-  hi = __fadd_rn(s, e);
-  lo = __fsub_rn(e, __fsub_rn(hi, s));
 }
 
 // ------------------------------------------------------------ Pandya inverse
