@@ -25,10 +25,10 @@
 //    them exactly as int64, converts once to FP64 and applies the power-of-two
 //    scale by exponent arithmetic.
 //
-// Kernel layout (persistent, one CTA per SM, 192 threads):
+// Kernel layout (persistent, one CTA per SM, 320 threads):
 //   warp 0: TMA producer (cp.async.bulk.tensor, 64B swizzle, mbarrier pipeline)
 //   warp 1: TMEM allocator + single-thread MMA issuer
-//   warps 2-5: epilogue (TMEM lanes 0-127)
+//   warps 2-9: epilogue (two warps per TMEM lane quarter, each on half the columns)
 // Every mbarrier wait is bounded; a timeout sets the status word and the CTA
 // drains and exits.
 #include <cuda.h>
@@ -816,10 +816,10 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
   p->family = family;
   // the ladder products have long K (MMA-bound tiles): 64-column tiles, one
   // accumulator set; the Pandya-space products have short K (epilogue-bound
-  // tiles): 32-column tiles, two accumulator sets and eight epilogue warps
+  // tiles): 32-column tiles and two accumulator sets; eight epilogue warps
   p->tn = family == 0 ? 64 : 32;
   p->nacc = family == 0 ? 1 : 2;
-  p->epiw = family == 0 ? 4 : 8;
+  p->epiw = 8;
   int Kmax = 1;
   for (const GemmJobDev& j : jobs_in) Kmax = std::max(Kmax, j.K);
   choose_digits(Kmax, p->beta, p->S);
@@ -1008,10 +1008,10 @@ static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, con
     ga.gsign = gsign;
     ga.accum = p->accum_override;
     if (p->tn == 64) {
-      auto kern = k_split_gemm<S, 64, 1, 4>;
+      auto kern = k_split_gemm<S, 64, 1, 8>;
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
       if (e != cudaSuccess) return e;
-      kern<<<p->grid, 64 + 32 * 4, p->smem, st>>>(p->maps[0], p->maps[1], p->maps[2], p->maps[3], ga);
+      kern<<<p->grid, 64 + 32 * 8, p->smem, st>>>(p->maps[0], p->maps[1], p->maps[2], p->maps[3], ga);
     } else {
       auto kern = k_split_gemm<S, 32, 2, 8>;
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
