@@ -617,7 +617,6 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
         }
         tc_fence_after();
         const unsigned dbase = tmem + (unsigned)(b * S * TN);
-        unsigned started = 0;  // groups already written in this tile
         bool ok = true;
         for (int kb = 0; kb < 2 * jb.nkb; ++kb, ++it) {
           int st = it % NST;
@@ -629,20 +628,24 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
             break;
           }
           tc_fence_after();
-          unsigned sA = sbase + st * STAGE;
-          unsigned sB = sA + S * A_SLICE;
+          // descriptors of this stage: a base each, every operand tile a
+          // compile-time offset from it (the start-address field is addr >> 4,
+          // and the stage never crosses its 14 bits); each group is written
+          // (not accumulated) by the first K16 step of the tile, whose s = 0
+          // products are the first ones issued into every group
+          const unsigned sA = sbase + st * STAGE;
+          const unsigned long long a0 = sdesc_sw64(sA), b0 = sdesc_sw64(sA + S * A_SLICE);
+          const unsigned first = kb == 0 ? 0u : 1u;
 #pragma unroll
           for (int sub = 0; sub < KB / 16; ++sub) {
 #pragma unroll
             for (int s = 0; s < S; ++s) {
-              unsigned long long ad = sdesc_sw64(sA + s * A_SLICE + sub * 32);
+              const unsigned long long ad = a0 + (unsigned long long)((s * A_SLICE + sub * 32) >> 4);
 #pragma unroll
               for (int t = 0; t < S - s; ++t) {
-                int grp = s + t;  // weight group T = (s+1) + (t+1) - 2
-                unsigned long long bd = sdesc_sw64(sB + t * B_SLICE + sub * 32);
-                unsigned acc = (started >> grp) & 1u;
-                tc_mma(dbase + grp * TN, ad, bd, idesc, acc);
-                started |= 1u << grp;
+                const int grp = s + t;  // weight group T = (s+1) + (t+1) - 2
+                const unsigned long long bd = b0 + (unsigned long long)((t * B_SLICE + sub * 32) >> 4);
+                tc_mma(dbase + grp * TN, ad, bd, idesc, (sub == 0 && s == 0) ? first : 1u);
               }
             }
           }
