@@ -15,7 +15,8 @@ barriers + synchronisations (max over ranks).  Every step reads X2, Y2 (280 MiB
 each) and writes Zbar (761 MiB), so the working set exceeds the 129 MB L2
 between steps.  Also reported: the plain FP64 form ("plain_fp64"), e2e (host
 buffers in pinned memory, H2D of X and Y + commutator + D2H of Z per step,
-through the C ABI), the roofline of the dominant kernel (from the library's
+through the C ABI; independent steps streamed over two operator sets, with the
+serial figure beside it), the roofline of the dominant kernel (from the library's
 CUDA-event phase timers over the timed region), SM clocks sampled during the
 timed region, the number of kernel launches, and a CPU baseline (the C oracle,
 a restatement of the reference's OpenMP + BLAS path, on all host cores).
@@ -154,6 +155,19 @@ def measured_peaks():
         return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
     except Exception:
         return 6800.0, 1900.0, "fallback"
+
+
+def profiled_traffic(phase, emax):
+    """DRAM bytes per launch of a phase's kernel from a committed ncu summary
+    (lines `traffic: <phase> emax=<e> <bytes>` under profiles/), or None."""
+    import glob
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        with open(path) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) == 4 and parts[0] == "traffic:" and parts[1] == phase and parts[2] == "emax=%d" % emax:
+                    return int(parts[3]), os.path.relpath(path, ROOT)
+    return None
 
 
 def algorithmic_work(ms):
@@ -403,6 +417,7 @@ def run_gb300(args):
             ach = amount / avg_s / 1e12
             roof = {"kernel": best, "bound": "tensor", "achieved": ach, "peak": bf16_peak, "unit": "TFLOP/s",
                     "frac": ach / bf16_peak, "traffic": None,
+                    "issued_bf16_tflops": 21 * ach, "issued_frac": 21 * ach / bf16_peak,
                     "note": "achieved counts FP64-equivalent algorithmic flops (the digit products issue 21x "
                             "as many BF16 flops); peak = bf16 dense, %s" % peak_src}
         else:
@@ -411,6 +426,10 @@ def run_gb300(args):
                     "frac": ach / hbm_peak, "traffic": None, "note": "peak = HBM copy, %s" % peak_src}
         roof["share"] = phases[best][0] / max(1e-9, phases["CommutatorScalarScalar"][0]) \
             if "CommutatorScalarScalar" in phases else None
+        tr = profiled_traffic(best, args.emax)
+        if tr:
+            roof["traffic"] = tr[0]
+            roof["traffic_source"] = "dram__bytes_read.sum + dram__bytes_write.sum per launch, ncu, " + tr[1]
     # ---- plain FP64 form (the metric compares split vs FP64)
     fp64 = None
     if prec == "split":

@@ -73,6 +73,21 @@ def test_split_full_vs_oracle(emax):
     assert max(errs) < TOL_SPLIT, errs
 
 
+@pytest.mark.parametrize("emax", [7, 8])
+def test_split_full_antihermitian_z_vs_oracle(emax):
+    # two hermitian operators: Z anti-hermitian, so the inverse Pandya blocks
+    # skip diagonal elements; at these sizes some blocks are split into runs
+    # of j rows to fit shared memory
+    o = Oracle(emax)
+    ms = ig.ModelSpace(emax, "O16", "O16")
+    X = o.ms.random_operator(51 + emax, True)
+    W = o.ms.random_operator(61 + emax, True)
+    R = o.commutator(X, W, 1, 1)
+    Z = full(ms, X, W, 1, 1, "split")
+    errs = rel_errors(o.ms, Z, R)
+    assert max(errs) < TOL_SPLIT, errs
+
+
 def test_split_bch_vs_reference():
     g = load_golden(3)
     ms = ig.ModelSpace(3, "O16", "O16")
