@@ -605,7 +605,7 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
   } else if (warp == 1) {
     // ------------------------------------------------ MMA issuer
     if (lane == 0) {
-      const unsigned idesc = idesc_bf16(TILE_M, TN);
+      constexpr int MAXT = 256 / TN;  // B digit tiles per MMA (UMMA N <= 256)
       int it = 0, tc = 0;
       for (int tix = blockIdx.x; tix < g.ntiles && !s_err; tix += gridDim.x, ++tc) {
         const SplitJob& jb = g.jobs[g.tiles[tix].job];
@@ -636,16 +636,21 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
           const unsigned sA = sbase + st * STAGE;
           const unsigned long long a0 = sdesc_sw64(sA), b0 = sdesc_sw64(sA + S * A_SLICE);
           const unsigned first = kb == 0 ? 0u : 1u;
+          // The products (s, t) of one A digit s go to the weight groups s + t,
+          // which are consecutive TN-column blocks of tensor memory, and the B
+          // digit tiles t are consecutive TN-row blocks of shared memory with
+          // the same 512-byte swizzle-atom stride: so the products of one s
+          // over a run of t are one MMA with N = (run length) x TN, up to 256
 #pragma unroll
           for (int sub = 0; sub < KB / 16; ++sub) {
 #pragma unroll
             for (int s = 0; s < S; ++s) {
               const unsigned long long ad = a0 + (unsigned long long)((s * A_SLICE + sub * 32) >> 4);
 #pragma unroll
-              for (int t = 0; t < S - s; ++t) {
-                const int grp = s + t;  // weight group T = (s+1) + (t+1) - 2
-                const unsigned long long bd = b0 + (unsigned long long)((t * B_SLICE + sub * 32) >> 4);
-                tc_mma(dbase + grp * TN, ad, bd, idesc, (sub == 0 && s == 0) ? first : 1u);
+              for (int t0 = 0; t0 < S - s; t0 += MAXT) {
+                const int nt = (S - s - t0) < MAXT ? (S - s - t0) : MAXT;
+                const unsigned long long bd = b0 + (unsigned long long)((t0 * B_SLICE + sub * 32) >> 4);
+                tc_mma(dbase + (s + t0) * TN, ad, bd, idesc_bf16(TILE_M, nt * TN), (sub == 0 && s == 0) ? first : 1u);
               }
             }
           }
