@@ -301,25 +301,41 @@ int do_121(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
   return IMSRG_OK;
 }
 
-// FP64 form: FP64 gathers (the plain form keeps every term in FP64).
-// Split form: the same gathers in double-float on the FP32 pipe.
-int do_122(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st, int prec = IMSRG_PREC_FP64)
+// Split form, first half: the (hi, lo) float-pair copies of X and Y
+int prep_122_df(const imsrg_op* X, const imsrg_op* Y, cudaStream_t st)
 {
   imsrg_space* sp = X->sp;
   int rc = ensure_scratch(sp, false, true);
   if (rc) return rc;
-  ProfScope ps("comm122ss", st);
+  try {
+    if (!sp->d_xf) sp->d_xf = sp->track(dmalloc<float2>(sp->s->arena));
+    if (!sp->d_yff) sp->d_yff = sp->track(dmalloc<float2>(sp->s->arena));
+  } catch (std::exception&) {
+    return fail(IMSRG_ERR_NOMEM, "comm122ss double-float scratch");
+  }
+  ProfScope ps("comm122ss prep", st);
+  CUDA_TRY(launch_to_ff(*sp->s, X->d, sp->d_xf, st));
+  CUDA_TRY(launch_to_ff(*sp->s, Y->d, sp->d_yff, st));
+  return IMSRG_OK;
+}
+
+// FP64 form: FP64 gathers (the plain form keeps every term in FP64).
+// Split form: the same gathers in double-float on the FP32 pipe (prepared:
+// the float-pair copies are already made, on a stream ordered before st).
+int do_122(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st, int prec = IMSRG_PREC_FP64,
+           bool prepared = false)
+{
+  imsrg_space* sp = X->sp;
+  int rc = ensure_scratch(sp, false, true);
+  if (rc) return rc;
   if (prec == IMSRG_PREC_SPLIT) {
-    try {
-      if (!sp->d_xf) sp->d_xf = sp->track(dmalloc<float2>(sp->s->arena));
-      if (!sp->d_yff) sp->d_yff = sp->track(dmalloc<float2>(sp->s->arena));
-    } catch (std::exception&) {
-      return fail(IMSRG_ERR_NOMEM, "comm122ss double-float scratch");
-    }
+    if (!prepared && (rc = prep_122_df(X, Y, st))) return rc;
+    ProfScope ps("comm122ss", st);
     CUDA_TRY(launch_comm122_df(*sp->s, X->d, Y->d, Z->d, sp->d_xf, sp->d_yff, (float2*)sp->d_w2, Z->herm,
                                sp->d_sym122, sp->n_sym122, st));
     return IMSRG_OK;
   }
+  ProfScope ps("comm122ss", st);
   CUDA_TRY(launch_comm122(*sp->s, X->d, Y->d, Z->d, sp->d_w2, Z->herm, sp->d_sym122, sp->n_sym122, st));
   return IMSRG_OK;
 }
@@ -377,16 +393,30 @@ int do_ladder(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaS
   return IMSRG_OK;
 }
 
-int do_ph(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStream_t st)
+// comm222_phss, first half: the Pandya-transformed operands (X bar, Y bar,
+// Y bar flipped) and the zero blocks of Z bar
+int prep_ph(const imsrg_op* X, const imsrg_op* Y, cudaStream_t st)
 {
   imsrg_space* sp = X->sp;
   Space& s = *sp->s;
   int rc = ensure_scratch(sp, true, false);
   if (rc) return rc;
-  ProfScope ps("comm222_phss", st);
-  int slot = prof_begin("Build Z_bar", st);
+  ProfScope ps("Pandya transform of X, Y", st);
   CUDA_TRY(launch_pandya_fwd(s, X->d, Y->d, Y->herm, sp->d_xb, sp->d_yt, sp->d_yf, sp->d_pfwd, sp->n_pfwd, st));
   for (auto& zr : sp->zbar_zero) CUDA_TRY(cudaMemsetAsync(sp->d_zb + zr.first, 0, zr.second * sizeof(double), st));
+  return IMSRG_OK;
+}
+
+// prepared: prep_ph already ran, on a stream ordered before st
+int do_ph(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStream_t st, bool prepared = false)
+{
+  imsrg_space* sp = X->sp;
+  Space& s = *sp->s;
+  int rc = ensure_scratch(sp, true, false);
+  if (rc) return rc;
+  if (!prepared && (rc = prep_ph(X, Y, st))) return rc;
+  ProfScope ps("comm222_phss", st);
+  int slot = prof_begin("Build Z_bar", st);
   if (prec == IMSRG_PREC_SPLIT) {
     rc = ensure_split(sp);
     if (rc) return rc;
@@ -422,21 +452,41 @@ int commutator_impl(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec,
     std::lock_guard<std::mutex> g(g_mu);
     std::copy(g_term_on, g_term_on + NTERMS, on);
   }
+  imsrg_space* sp = X->sp;
+  if (!sp->side) {
+    CUDA_TRY(cudaStreamCreateWithFlags(&sp->side, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&sp->ev_fork, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&sp->ev_join, cudaEventDisableTiming));
+  }
+  cudaStream_t sd = sp->side;
   ProfScope ps("CommutatorScalarScalar", st);
-  CUDA_TRY(cudaMemsetAsync(Z->d, 0, X->sp->s->arena * sizeof(double), st));
+  CUDA_TRY(cudaMemsetAsync(Z->d, 0, sp->s->arena * sizeof(double), st));
   // The terms add into Z in an order of our own (the sum is the same up to
   // rounding): the ladder product goes first, onto the zeroed two-body blocks,
   // so the one-body part of comm221ss can read Mpp - Mhh straight from Z2
   // instead of recomputing the pp dot products (ConstructScalarMpp_Mhh is
   // shared the same way by the reference's comm222_pp_hh_221ss).
+  //
+  // While the ladder product runs on st, a second stream does what does not
+  // depend on it: the operand preparation of comm122ss and comm222_phss and
+  // the zero- and one-body terms 111/110, 220, 121 (they write only Z0 and Z1,
+  // the ladder only Z2).  The streams join before comm221ss, which reads Z2
+  // and writes Z1.
+  CUDA_TRY(cudaEventRecord(sp->ev_fork, st));
+  CUDA_TRY(cudaStreamWaitEvent(sd, sp->ev_fork, 0));
+  const bool split = prec == IMSRG_PREC_SPLIT;
+  if (on[T122] && split && (rc = prep_122_df(X, Y, sd))) return rc;
+  if (on[T222PH] && (rc = prep_ph(X, Y, sd))) return rc;
+  if ((rc = do_111_110(X, Y, Z, on[T111], on[T110], sd))) return rc;
+  if (on[T220] && (rc = do_220(X, Y, Z, sd))) return rc;
+  if (on[T121] && (rc = do_121(X, Y, Z, sd))) return rc;
+  CUDA_TRY(cudaEventRecord(sp->ev_join, sd));
   bool ladder_first = on[T222PPHH];
   if (ladder_first && (rc = do_ladder(X, Y, Z, prec, st, true))) return rc;
+  CUDA_TRY(cudaStreamWaitEvent(st, sp->ev_join, 0));
   if (on[T221] && (rc = do_221_1b(X, Y, Z, st, ladder_first ? Z->d : nullptr))) return rc;
-  if ((rc = do_111_110(X, Y, Z, on[T111], on[T110], st))) return rc;
-  if (on[T220] && (rc = do_220(X, Y, Z, st))) return rc;
-  if (on[T121] && (rc = do_121(X, Y, Z, st))) return rc;
-  if (on[T122] && (rc = do_122(X, Y, Z, st, prec))) return rc;
-  if (on[T222PH] && (rc = do_ph(X, Y, Z, prec, st))) return rc;
+  if (on[T122] && (rc = do_122(X, Y, Z, st, prec, split))) return rc;
+  if (on[T222PH] && (rc = do_ph(X, Y, Z, prec, st, true))) return rc;
   return IMSRG_OK;
 }
 

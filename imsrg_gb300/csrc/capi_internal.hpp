@@ -64,6 +64,10 @@ struct imsrg_space {
   SplitPlan* split_zbar = nullptr;
   // BCH work operators
   double *d_nested = nullptr, *d_next = nullptr;
+  // second stream of CommutatorScalarScalar (work independent of the ladder
+  // product) and the events that fork it from and join it to the caller's
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
   template <class T>
   T* track(T* p)
@@ -75,6 +79,9 @@ struct imsrg_space {
   {
     if (split_ladder) split_plan_destroy(split_ladder);
     if (split_zbar) split_plan_destroy(split_zbar);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side) cudaStreamDestroy(side);
     for (void* p : allocs) cudaFree(p);
     delete s;
   }

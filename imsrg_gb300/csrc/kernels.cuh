@@ -28,8 +28,12 @@ cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, 
                               const double* Mz, cudaStream_t st);
 cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, double* Z, double* W2, int hZ,
                            const int* sym_tiles, int nsym_tiles, cudaStream_t st);
-cudaError_t launch_comm122_df(const Space& s, const double* X, const double* Y, double* Z, float2* Xf, float2* Yf,
-                              float2* W2, int hZ, const int* sym_tiles, int nsym_tiles, cudaStream_t st);
+// (hi, lo) float-pair copy of an arena (integer instructions)
+cudaError_t launch_to_ff(const Space& s, const double* A, float2* Af, cudaStream_t st);
+// split-form comm122ss from the (hi, lo) copies Xf, Yf of X and Y
+cudaError_t launch_comm122_df(const Space& s, const double* X, const double* Y, double* Z, const float2* Xf,
+                              const float2* Yf, float2* W2, int hZ, const int* sym_tiles, int nsym_tiles,
+                              cudaStream_t st);
 cudaError_t launch_pandya_fwd(const Space& s, const double* X, const double* Y, int hY, double* Xb, double* Yt,
                               double* Yf, const int* tiles, int ntiles, cudaStream_t st);
 cudaError_t launch_pandya_inv(const Space& s, const double* Zb, double* Z, int hZ, const int* tiles, int ntiles,

@@ -1230,14 +1230,18 @@ cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, dou
   return cudaGetLastError();
 }
 
-cudaError_t launch_comm122_df(const Space& s, const double* X, const double* Y, double* Z, float2* Xf, float2* Yf,
-                              float2* W2, int hZ, const int* sym_tiles, int nsym_tiles, cudaStream_t st)
+cudaError_t launch_to_ff(const Space& s, const double* A, float2* Af, cudaStream_t st)
+{
+  k_to_ff<<<2432, 256, 0, st>>>(A, Af, s.arena);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_comm122_df(const Space& s, const double* X, const double* Y, double* Z, const float2* Xf,
+                              const float2* Yf, float2* W2, int hZ, const int* sym_tiles, int nsym_tiles,
+                              cudaStream_t st)
 {
   if (s.work.ncols122 == 0) return cudaSuccess;
-  k_to_ff<<<2432, 256, 0, st>>>(X, Xf, s.arena);
-  count_launch();
-  k_to_ff<<<2432, 256, 0, st>>>(Y, Yf, s.arena);
-  count_launch();
   k_comm122_w_df<<<s.work.ncols122, 128, 0, st>>>(s.dev, s.work, X, Y, Xf, Yf, W2);
   count_launch();
   cudaError_t e = cudaGetLastError();
