@@ -715,14 +715,14 @@ __global__ void __launch_bounds__(256) k_pandya_inv(DevSpace S, DevWork W, const
 // A block owns one (i, k, class of j) group of quadruples (see
 // build_invq_tasks), laid out as a jn x ln rectangle of (j, l) pairs:
 //   1. per-pair counts and a block scan give each pair its slots in shared
-//      memory: n1 + n2 staged Zbar values, nJ results;
-//   2. staging, J' by J' (all lanes on one CC channel, consecutive l on
-//      consecutive rows il), Zbar values -> (hi, lo) float pairs;
-//   3. the J' sums in double-float on the FP32 pipe, with pairs taken in order
-//      of (j_j, j_l) so the lanes of a warp mostly share their loop lengths;
-//   4. per channel J the block's results form a rectangle of Z (rows i j,
-//      columns k l, consecutive kets), written row-coalesced for Z(ij, kl) and
-//      column-coalesced for the mirrored Z(kl, ij).
+//      memory: n1 + n2 staged Zbar values and nJ result slots, in order of
+//      (2j_j, 2j_l) so neighbouring slots share loop lengths;
+//   2. staging, a thread per value slot (four loads in flight): Zbar values
+//      -> (hi, lo) float pairs;
+//   3. a thread per result slot (pair, J): the two J' sums in double-float on
+//      the FP32 pipe, then Z(ij, kl) += z and Z(kl, ij) += hZ z.  The rows
+//      (i, j) and columns (k, l) of the block in channel J are runs of
+//      consecutive kets, so a ket's index is its run's first plus its rank.
 // FP64 appears only in the final Z += z.  Values are carried with 48-bit
 // significands (double-float), far inside the split form's 1e-10 tolerance;
 // magnitudes below the FP32 normal range (1.2e-38) are flushed to zero.
@@ -731,13 +731,22 @@ constexpr int kInvqThreads = 256;
 
 // the r-th set position of the first n predicate values (n <= 64) of a warp,
 // written to out[]: a ballot compaction; returns the count
-__device__ __forceinline__ int warp_compact64(bool v0, bool v1, unsigned char x0, unsigned char x1, unsigned char* out)
+// (and, with rank, each value's position: rank[x] = r)
+__device__ __forceinline__ int warp_compact64(bool v0, bool v1, unsigned char x0, unsigned char x1, unsigned char* out,
+                                              unsigned char* rank = nullptr)
 {
   const int lane = threadIdx.x & 31;
   const unsigned m0 = __ballot_sync(0xffffffffu, v0), m1 = __ballot_sync(0xffffffffu, v1);
   const unsigned below = (1u << lane) - 1;
-  if (v0) out[__popc(m0 & below)] = x0;
-  if (v1) out[__popc(m0) + __popc(m1 & below)] = x1;
+  const int r0 = __popc(m0 & below), r1 = __popc(m0) + __popc(m1 & below);
+  if (v0) {
+    out[r0] = x0;
+    if (rank) rank[x0] = (unsigned char)r0;
+  }
+  if (v1) {
+    out[r1] = x1;
+    if (rank) rank[x1] = (unsigned char)r1;
+  }
   return __popc(m0) + __popc(m1);
 }
 
@@ -758,11 +767,9 @@ __global__ void __launch_bounds__(kInvqThreads) k_pandya_inv_ff(DevSpace S, DevW
   __shared__ int s_kkj[kInvqMaxOrb];       // global index of the ket (k, j) / (j, k)
   __shared__ unsigned char s_jperm[kInvqMaxOrb], s_lperm[kInvqMaxOrb];
   __shared__ unsigned char s_jv[kInvqMaxJ][kInvqMaxOrb], s_lv[kInvqMaxJ][kInvqMaxOrb];  // per J: valid j, l
-  __shared__ int s_wn[kInvqMaxJ][2];       // per J: valid rows, valid columns
-  __shared__ float s_wr[kInvqMaxJ][2];     // their reciprocals
+  __shared__ unsigned char s_jrk[kInvqMaxJ][kInvqMaxOrb], s_lrk[kInvqMaxJ][kInvqMaxOrb];  // per J: their ranks
   __shared__ int s_wbk[kInvqMaxJ][3];      // per J: first bra, first ket, channel size
   __shared__ long long s_woff[kInvqMaxJ];  // per J: arena offset of the channel
-  __shared__ int s_wpre[kInvqMaxJ + 1];    // per J: prefix of rows x columns
   __shared__ int s_cn[2][kInvqMaxJ];       // per J': CC channel size, sums 1 and 2
   __shared__ long long s_coff[2][kInvqMaxJ];
   __shared__ int s_cik[kInvqMaxJ];         // per J': local index of the CC ket (i, k)
@@ -875,11 +882,11 @@ __global__ void __launch_bounds__(kInvqThreads) k_pandya_inv_ff(DevSpace S, DevW
     __syncthreads();
   }
   const int tot1 = (int)(carry & 0x1FFFFF), tot2 = (int)((carry >> 21) & 0x1FFFFF), totO = (int)(carry >> 42);
-  const int tot12 = tot1 + tot2, nslot = tot12 + totO;
-  // regions: sum-1 values [0, tot1), sum-2 values [tot1, tot12), results [tot12, nslot);
+  const int tot12 = tot1 + tot2;
+  // regions: sum-1 values [0, tot1), sum-2 values [tot1, tot12), then the
+  // owner of each value slot and of each result slot (tot12 + e);
   // owner[slot] = its pair
-  double* outs = (double*)(zs + tot12);
-  unsigned short* owner = (unsigned short*)(zs + nslot);
+  unsigned short* owner = (unsigned short*)(zs + tot12);
   for (int p = tid; p < P; p += kInvqThreads) {
     const int c = cnt[p];
     off2[p] = (unsigned short)(off2[p] + tot1);
@@ -919,7 +926,7 @@ __global__ void __launch_bounds__(kInvqThreads) k_pandya_inv_ff(DevSpace S, DevW
       const int jj = s_jj[lane + 32];
       v1 = abs(ji - jj) <= 2 * J && ji + jj >= 2 * J && !(s_j[lane + 32] == i && (J & 1));
     }
-    const int nr = warp_compact64(v0, v1, (unsigned char)lane, (unsigned char)(lane + 32), s_jv[t]);
+    const int nr = warp_compact64(v0, v1, (unsigned char)lane, (unsigned char)(lane + 32), s_jv[t], s_jrk[t]);
     v0 = v1 = false;
     if (lane < ln) {
       const int jl = s_jl[lane];
@@ -929,13 +936,9 @@ __global__ void __launch_bounds__(kInvqThreads) k_pandya_inv_ff(DevSpace S, DevW
       const int jl = s_jl[lane + 32];
       v1 = abs(jk - jl) <= 2 * J && jk + jl >= 2 * J && !(s_l[lane + 32] == k && (J & 1));
     }
-    const int nc = warp_compact64(v0, v1, (unsigned char)lane, (unsigned char)(lane + 32), s_lv[t]);
+    const int nc = warp_compact64(v0, v1, (unsigned char)lane, (unsigned char)(lane + 32), s_lv[t], s_lrk[t]);
     __syncwarp();
     if (lane == 0) {
-      s_wn[t][0] = nr;
-      s_wn[t][1] = nc;
-      s_wr[t][0] = nr ? 1.0f / nr : 0.f;
-      s_wr[t][1] = nc ? 1.0f / nc : 0.f;
       if (nr && nc) {
         const int ch = chan_index(J, (S.l[i] + pj) & 1, (S.tz2[i] + tzj) / 2);
         s_wbk[t][0] = S.ketJ_loc[(size_t)J * nk + ket_index(N, i, s_j[s_jv[t][0]])];
@@ -946,18 +949,6 @@ __global__ void __launch_bounds__(kInvqThreads) k_pandya_inv_ff(DevSpace S, DevW
     }
   }
   __syncthreads();
-  if (warp == 0) {
-    // prefix of the rectangle areas over J (nJu <= 32)
-    const int a = lane < nJu ? s_wn[lane][0] * s_wn[lane][1] : 0;
-    int x = a;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int t = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += t;
-    }
-    s_wpre[lane] = x - a;
-    if (lane == 31) s_wpre[32] = x;
-  }
 
   // 2. staging, a thread per slot: Zbar values as (hi, lo) pairs, batches of
   //    four slots with their loads in flight together
@@ -1056,57 +1047,14 @@ __global__ void __launch_bounds__(kInvqThreads) k_pandya_inv_ff(DevSpace S, DevW
       double z = ff2d(hi, lo);
       if (i == j && k == l) z *= 0.5;
       else if (ev) z *= 0.70710678118654752440;
-      outs[e] = z;
-    }
-  }
-  __syncthreads();
-
-  // 4. Z += z over the block's rectangles, all J at once: pass 0 writes
-  //    Z(ij, kl) with consecutive lanes on consecutive bras, pass 1 the
-  //    mirrored Z(kl, ij) = hZ z with consecutive lanes on consecutive kets.
-  //    Items of a thread increase, so the rectangle index only moves forward;
-  //    batches of four items keep four loads of Z in flight.
-  const int T = s_wpre[nJu];
-  for (int mir = 0; mir < 2; ++mir) {
-    int t = 0;
-    for (int e0 = tid; e0 < T; e0 += 4 * kInvqThreads) {
-      long long addr[4];
-      double zv[4], old[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        addr[u] = -1;
-        const int e = e0 + u * kInvqThreads;
-        if (e >= T) continue;
-        while (s_wpre[t + 1] <= e) ++t;
-        const int r = e - s_wpre[t];
-        int jr, lr;
-        if (mir) {
-          jr = small_div(r, s_wr[t][1]);
-          lr = r - jr * s_wn[t][1];
-        } else {
-          lr = small_div(r, s_wr[t][0]);
-          jr = r - lr * s_wn[t][0];
-        }
-        const int jx = s_jv[t][jr], lx = s_lv[t][lr];
-        const int p = jx * ln + lx;
-        if (!(cnt[p] >> 10)) continue;
-        const int ib = s_wbk[t][0] + jr, ik = s_wbk[t][1] + lr;
-        if (mir && ib == ik) continue;
-        const int J = uJ + t;
-        const bool ev = (i == s_j[jx]) || (k == s_l[lx]);
-        int Jlo = max(abs(ji - s_jj[jx]), abs(jk - s_jl[lx])) >> 1;
-        if (ev) Jlo += Jlo & 1;
-        const double z = outs[offO[p] + (ev ? (J - Jlo) >> 1 : J - Jlo)];
-        const int n = s_wbk[t][2];
-        addr[u] = s_woff[t] + (mir ? (long long)ib * n + ik : (long long)ik * n + ib);
-        zv[u] = mir ? dneg_if(z, hZ < 0) : z;
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        if (addr[u] >= 0) old[u] = Z[addr[u]];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        if (addr[u] >= 0) Z[addr[u]] = old[u] + zv[u];
+      // Z(ij, kl) += z and Z(kl, ij) += hZ z: bra (i, j) and ket (k, l) are
+      // consecutive kets of channel J, found by their ranks among the block's
+      // rows and columns of that channel
+      const int tJ = J - uJ;
+      const int ib = s_wbk[tJ][0] + s_jrk[tJ][jx], ik = s_wbk[tJ][1] + s_lrk[tJ][lx], n = s_wbk[tJ][2];
+      double* Zc = Z + s_woff[tJ];
+      Zc[(long long)ik * n + ib] += z;
+      if (ib != ik) Zc[(long long)ib * n + ik] += dneg_if(z, hZ < 0);
     }
   }
 }

@@ -452,7 +452,7 @@ void build_invq_tasks(Space& s, int budget)
             int l = Lc[lf + x];
             int n1, n2, nJ, Jlo, lo1, lo2;
             if (invq_counts(i, j, k, l, s.j2[i], s.j2[j], s.j2[k], s.j2[l], 1, n1, n2, nJ, Jlo, lo1, lo2)) {
-              rs += n1 + n2 + nJ;
+              rs += invq_slot_bytes(n1, n2, nJ);
               ra = true;
             }
           }

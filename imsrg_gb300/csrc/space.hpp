@@ -108,9 +108,11 @@ void upload_space(Space& s);
 // blocks of the quadruple-ordered inverse Pandya transform, each within
 // budget bytes of shared memory (fills cls_list, cls_off, invq_tasks, invq_smem)
 void build_invq_tasks(Space& s, int budget);
-// shared memory of one block of jn x ln quadruples holding `slots` values:
-// four 16-bit counts/offsets per pair, per slot an 8-byte value and its 16-bit owner
-inline int invq_block_bytes(int jn, int ln, int slots) { return ((8 * jn * ln + 15) & ~15) + 10 * slots; }
+// shared memory of one block of jn x ln quadruples: four 16-bit counts /
+// offsets per pair, then `slot_bytes` (per staged Zbar value 8 bytes and its
+// 16-bit owner, per result slot its 16-bit owner)
+inline int invq_slot_bytes(int n1, int n2, int nJ) { return 10 * (n1 + n2) + 2 * nJ; }
+inline int invq_block_bytes(int jn, int ln, int slot_bytes) { return ((8 * jn * ln + 15) & ~15) + slot_bytes; }
 
 // 6j table construction (sixj.cpp)
 double sixj_dd(int jj1, int jj2, int jj3, int jj4, int jj5, int jj6);  // doubled arguments
