@@ -371,8 +371,11 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
                                                      __nv_bfloat16* __restrict__ alpha, __nv_bfloat16* __restrict__ bet,
                                                      __nv_bfloat16* __restrict__ gam, __nv_bfloat16* __restrict__ del)
 {
-  __shared__ __align__(16) unsigned short dA[S][32][KB + 8];
-  __shared__ __align__(16) unsigned short dB[S][32][KB + 8];
+  // rows of KB + 2 digits = 17 words: the 32 rows a warp writes at once fall
+  // in 32 different banks
+  constexpr int RW = (KB + 2) / 2;
+  __shared__ unsigned dA[S][32][RW];
+  __shared__ unsigned dB[S][32][RW];
   __shared__ int rowA[32], rowB[32], rowsg[32], rowph[32];
   __shared__ int s_col[KB], s_code[KB];
   __shared__ double s_sc[KB];
@@ -406,56 +409,69 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
   const double* B = (jb.bsel ? B1 : B0) + jb.b_off;
   const int P = beta * S;
   const long long half = 1ll << (beta - 1), mask = (1ll << beta) - 1;
-  // element (r, tt): thread layout r fastest (coalesced column reads)
-  for (int e = threadIdx.x; e < 32 * KB; e += 256) {
-    int r = e & 31, tt = e >> 5;
-    int i = r0 + r, t = t0 + tt;
-    long long qa = 0, qb = 0;
-    if (i < jb.m && t < jb.K) {
-      const int col = s_col[tt], code = s_code[tt];
-      qa = to_fixed(A[(long long)col * jb.lda + i], rowA[r], P);
-      const double vb = B[(long long)col * jb.ldb + i];
-      if (code == SC_GENERAL) {
-        qb = to_fixed(vb * s_sc[tt], rowB[r], P);
-      } else {
-        qb = to_fixed(vb, rowB[r] - (code >> 1), P);
-        if (code & 1) qb = -qb;
+  // column pair (tt, tt + 1) of row r: thread layout r fastest (coalesced
+  // column reads), the two digits of a pair packed in one 32-bit word
+  for (int e = threadIdx.x; e < 32 * (KB / 2); e += 256) {
+    const int r = e & 31, tp = e >> 5;
+    const int i = r0 + r;
+    unsigned wa[S], wb[S];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int tt = 2 * tp + h, t = t0 + tt;
+      long long qa = 0, qb = 0;
+      if (i < jb.m && t < jb.K) {
+        const int col = s_col[tt], code = s_code[tt];
+        qa = to_fixed(A[(long long)col * jb.lda + i], rowA[r], P);
+        const double vb = B[(long long)col * jb.ldb + i];
+        if (code == SC_GENERAL) {
+          qb = to_fixed(vb * s_sc[tt], rowB[r], P);
+        } else {
+          qb = to_fixed(vb, rowB[r] - (code >> 1), P);
+          if (code & 1) qb = -qb;
+        }
+      }
+      // digits of |q| by shifts (32-bit digit arithmetic), then the carry that
+      // makes them balanced, then the sign: |d| <= 2^(beta-1) below the top
+      // digit, |d_1| <= 2^beta + 1
+      const unsigned long long ua = (unsigned long long)(qa < 0 ? -qa : qa);
+      const unsigned long long ub = (unsigned long long)(qb < 0 ? -qb : qb);
+      int da[S], db[S];
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int sh = beta * (S - 1 - s);
+        da[s] = (int)(ua >> sh);
+        db[s] = (int)(ub >> sh);
+        if (s > 0) {
+          da[s] &= (int)mask;
+          db[s] &= (int)mask;
+        }
+      }
+#pragma unroll
+      for (int s = S - 1; s >= 1; --s) {
+        if (da[s] >= (int)half) {
+          da[s] -= (int)(mask + 1);
+          da[s - 1] += 1;
+        }
+        if (db[s] >= (int)half) {
+          db[s] -= (int)(mask + 1);
+          db[s - 1] += 1;
+        }
+      }
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int xa = qa < 0 ? -da[s] : da[s];
+        const int xb = qb < 0 ? -db[s] : db[s];
+        // small integer -> bf16 bits (exact): 1.5*2^23 magic
+        const unsigned ba = __float_as_uint(__int_as_float(0x4B400000 + xa) - 12582912.0f) >> 16;
+        const unsigned bb = __float_as_uint(__int_as_float(0x4B400000 + xb) - 12582912.0f) >> 16;
+        wa[s] = h ? (wa[s] | (ba << 16)) : ba;
+        wb[s] = h ? (wb[s] | (bb << 16)) : bb;
       }
     }
-    // digits of |q| by shifts (32-bit digit arithmetic), then the carry that
-    // makes them balanced, then the sign: |d| <= 2^(beta-1) below the top
-    // digit, |d_1| <= 2^beta + 1
-    const unsigned long long ua = (unsigned long long)(qa < 0 ? -qa : qa);
-    const unsigned long long ub = (unsigned long long)(qb < 0 ? -qb : qb);
-    int da[S], db[S];
 #pragma unroll
     for (int s = 0; s < S; ++s) {
-      const int sh = beta * (S - 1 - s);
-      da[s] = (int)(ua >> sh);
-      db[s] = (int)(ub >> sh);
-      if (s > 0) {
-        da[s] &= (int)mask;
-        db[s] &= (int)mask;
-      }
-    }
-#pragma unroll
-    for (int s = S - 1; s >= 1; --s) {
-      if (da[s] >= (int)half) {
-        da[s] -= (int)(mask + 1);
-        da[s - 1] += 1;
-      }
-      if (db[s] >= (int)half) {
-        db[s] -= (int)(mask + 1);
-        db[s - 1] += 1;
-      }
-    }
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-      const int xa = qa < 0 ? -da[s] : da[s];
-      const int xb = qb < 0 ? -db[s] : db[s];
-      // small integer -> bf16 bits (exact): 1.5*2^23 magic
-      dA[s][r][tt] = (unsigned short)(__float_as_uint(__int_as_float(0x4B400000 + xa) - 12582912.0f) >> 16);
-      dB[s][r][tt] = (unsigned short)(__float_as_uint(__int_as_float(0x4B400000 + xb) - 12582912.0f) >> 16);
+      dA[s][r][tp] = wa[s];
+      dB[s][r][tp] = wb[s];
     }
   }
   __syncthreads();
@@ -465,8 +481,10 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
     const int v = e % (KB / 8), r = (e / (KB / 8)) & 31, s = e / (32 * (KB / 8));
     const long long row = jb.row_base + (long long)s * jb.m_pad + r0 + r;
     const long long o = row * K_stride + t0 + v * 8;
-    const uint4 va = *(const uint4*)&dA[s][r][v * 8];
-    const uint4 vb = *(const uint4*)&dB[s][r][v * 8];
+    const unsigned* qa = &dA[s][r][v * 4];
+    const unsigned* qb = &dB[s][r][v * 4];
+    const uint4 va = make_uint4(qa[0], qa[1], qa[2], qa[3]);
+    const uint4 vb = make_uint4(qb[0], qb[1], qb[2], qb[3]);
     *(uint4*)(alpha + o) = va;
     *(uint4*)(bet + o) = vb;
     if (need_g) {
