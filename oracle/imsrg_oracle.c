@@ -787,6 +787,225 @@ int oracle_bch_transform(const ospace* s, const double* OpIn, int hIn, const dou
   return iters;
 }
 
+/* BCH::BCH_Product, src/BCH.cc:267-350: Z with e^Z = e^X e^Y,
+ *   Z = X + Y + 1/2 [X,Y] + 1/12 ([X,[X,Y]] + [Y,[Y,X]]) - 1/720 [Y,[Y,[Y,[Y,X]]]] + ...
+ * with the Bernoulli coefficients of src/BCH.cc:273-274, the [X,[X,Y]] term
+ * only when |[Y,X]| |X| exceeds the threshold (:289-292), and the loop stops of
+ * :304-335 (the factorized correction, off by default, is not restated).
+ * Z must not alias X or Y and is overwritten.  Returns the number of
+ * commutators evaluated. */
+int oracle_bch_product(const ospace* s, const double* X, int hX, const double* Y, int hY, double* Z,
+                       double threshold)
+{
+  static const double bern[9] = {1.0, -0.5, 1. / 6, 0.0, -1. / 30, 0.0, 1. / 42, 0, -1. / 30};
+  static const double fact[9] = {1.0, 1.0, 2.0, 6.0, 24., 120., 720., 5040., 40320.};
+  int64_t A = s->arena;
+  double nx = oracle_norm(s, X), ny = oracle_norm(s, Y);
+  for (int64_t t = 0; t < A; ++t) Z[t] = X[t] + Y[t];
+  double* nested = dalloc(A);
+  double* next = dalloc(A);
+  oracle_commutator(s, Y, X, nested, hY, hX);
+  int hN = z_herm(hY, hX);
+  int ncomm = 1;
+  double nxy = oracle_norm(s, nested);
+  if (nxy * nx > threshold) {
+    oracle_commutator(s, nested, X, next, hN, hX);
+    ++ncomm;
+    for (int64_t t = 0; t < A; ++t) Z[t] += (1. / 12) * next[t];
+  }
+  size_t k = 1;
+  while (nxy > threshold) {
+    if (k < 2 || k % 2 == 0) {
+      double c = bern[k] / fact[k];
+      for (int64_t t = 0; t < A; ++t) Z[t] += c * nested[t];
+    }
+    ++k;
+    if (k >= 9) break;
+    if (2 * ny * nxy < threshold) break;
+    memset(next, 0, A * sizeof(double));
+    oracle_commutator(s, Y, nested, next, hY, hN);
+    hN = z_herm(hY, hN);
+    double* tmp = nested;
+    nested = next;
+    next = tmp;
+    ++ncomm;
+    nxy = oracle_norm(s, nested);
+  }
+  free(nested);
+  free(next);
+  return ncomm;
+}
+
+/* ------------------------------------------------------------- generator */
+/* Generator types (src/Generator.cc:12-15) and denominator partitionings
+ * (src/Generator.cc:23-28) restated here. */
+enum { GEN_WHITE = 0, GEN_ATAN = 1, GEN_WEGNER = 2, GEN_IMAGTIME = 3 };
+enum { PART_EPSTEIN_NESBET = 0, PART_MOLLER_PLESSET = 1 };
+#define DELTA_ALL (-12345)
+
+static double eta_func(int type, double hod, double den)
+{
+  switch (type) {
+    case GEN_ATAN: return 0.5 * atan(2 * hod / den);
+    case GEN_WEGNER: return hod * den;
+    case GEN_IMAGTIME: return hod * ((den > 0) - (den < 0));
+    default: return hod / den;
+  }
+}
+
+/* Generator::Get1bDenominator, src/Generator.cc:110-139 */
+static double denom_1b(const ospace* s, const double* H, int part, double cutoff, double delta, int delta_index,
+                       int i, int j)
+{
+  int N = s->norb;
+  double d = ONE(H, i, i) - ONE(H, j, j);
+  if (part == PART_EPSTEIN_NESBET) d += (s->occ[i] - s->occ[j]) * tbme_monopole(s, H, i, j, i, j);
+  if (delta_index == DELTA_ALL || i == delta_index || j == delta_index) d += delta;
+  if (fabs(d) < cutoff) d = cutoff;
+  return d;
+}
+
+/* Generator::Get2bDenominator, src/Generator.cc:142-188, bra (i,j), ket (k,l) */
+static double denom_2b(const ospace* s, const double* H, int part, double cutoff, double delta, int delta_index,
+                       int i, int j, int k, int l)
+{
+  int N = s->norb;
+  double d = ONE(H, i, i) + ONE(H, j, j) - ONE(H, k, k) - ONE(H, l, l);
+  if (delta_index == DELTA_ALL) d += delta;
+  double ni = s->occ[i], nj = s->occ[j], nk = s->occ[k], nl = s->occ[l];
+  if (part == PART_EPSTEIN_NESBET) {
+    d += (1 - ni - nj) * tbme_monopole(s, H, i, j, i, j);
+    d -= (1 - nk - nl) * tbme_monopole(s, H, k, l, k, l);
+    d += (ni - nk) * tbme_monopole(s, H, i, k, i, k);
+    d += (ni - nl) * tbme_monopole(s, H, i, l, i, l);
+    d += (nj - nk) * tbme_monopole(s, H, j, k, j, k);
+    d += (nj - nl) * tbme_monopole(s, H, j, l, j, l);
+  }
+  if (fabs(d) < cutoff) d = cutoff;
+  return d;
+}
+
+/* Generator::Update -> ConstructGenerator_SingleRef, src/Generator.cc:32-76,
+ * 236-297, for a single-reference space: the core is the set of occupied
+ * orbits (src/ModelSpace.cc:278-280: the reference's own filling), every other
+ * orbit is in the q space.  Eta is overwritten: zero except the 1b ph block
+ * (core a, non-core i) and the 2b blocks <pp'|Eta|hh'> with both bra orbits
+ * outside and both ket orbits inside the core, antisymmetrised. */
+void oracle_generator(const ospace* s, const double* H, double* Eta, int type, int part, double cutoff, double delta,
+                      int delta_index)
+{
+  int N = s->norb;
+  memset(Eta, 0, s->arena * sizeof(double));
+  for (int ia = 0; ia < s->nholes; ++ia) {
+    int a = s->holes[ia];
+    for (int i = 0; i < N; ++i) {
+      if (s->occ[i] >= OCC_CUT) continue;
+      double d = denom_1b(s, H, part, cutoff, delta, delta_index, i, a);
+      double e = eta_func(type, ONE(H, i, a), d);
+      ONE(Eta, i, a) = e;
+      ONE(Eta, a, i) = -e;
+    }
+  }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int c = 0; c < s->nch; ++c) {
+    const ochan* C = &s->ch[c];
+    int n = C->n;
+    const double* H2 = H + s->off2[c];
+    double* E2 = Eta + s->off2[c];
+    for (int ik = 0; ik < n; ++ik) {
+      int k = C->p[ik], l = C->q[ik];
+      if (s->occ[k] < OCC_CUT || s->occ[l] < OCC_CUT) continue;
+      for (int ib = 0; ib < n; ++ib) {
+        int i = C->p[ib], j = C->q[ib];
+        if (s->occ[i] >= OCC_CUT || s->occ[j] >= OCC_CUT) continue;
+        double d = denom_2b(s, H, part, cutoff, delta, delta_index, i, j, k, l);
+        double e = eta_func(type, H2[(size_t)ik * n + ib], d);
+        E2[(size_t)ik * n + ib] = e;
+        E2[(size_t)ib * n + ik] = -e;
+      }
+    }
+  }
+}
+
+/* ---------------------------------------------------------------- solver */
+/* IMSRGSolver settings (src/IMSRGSolver.cc:31-37, src/IMSRGSolver.hh:117-148,
+ * src/BCH.cc:16-17, src/Generator.cc:18-20). */
+typedef struct {
+  double ds, ds_max, smax, norm_domega, omega_norm_max, eta_criterion;
+  int magnus_adaptive;
+  int generator, partitioning;
+  double denominator_cutoff, denominator_delta;
+  int denominator_delta_index;
+  double bch_transform_threshold, bch_product_threshold;
+} oflow_params;
+
+/* IMSRGSolver::Solve_magnus_euler, src/IMSRGSolver.cc:236-321, with
+ * IMSRGSolver::NewOmega (src/IMSRGSolver.cc:44-83) for Omega splitting
+ * (no scratch files: the earlier Omegas are not kept).  Starts from s = *s_io
+ * and the flowing state Hs (H(s)), Omega (the last Omega), Hsaved (the
+ * starting point of that Omega; equal to H0 while only one Omega exists) and
+ * *n_omega (Omegas so far, >= 1).  Per step, the flow parameter and
+ * H(s).ZeroBody are appended to s_hist / e0_hist (up to maxhist entries).
+ * Returns the number of steps taken, or -1 if the flow blew up (the
+ * reference's "things are clearly broken" exit, :263-270). */
+int oracle_magnus_euler(const ospace* s, const double* H0, double* Hs, double* Hsaved, double* Omega, double* Eta,
+                        const oflow_params* p, double* s_io, int* n_omega, double* s_hist, double* e0_hist,
+                        int maxhist)
+{
+  int64_t A = s->arena;
+  double sflow = *s_io;
+  double ds = p->ds;
+  double norm_domega = p->norm_domega;
+  oracle_generator(s, Hs, Eta, p->generator, p->partitioning, p->denominator_cutoff, p->denominator_delta,
+                   p->denominator_delta_index);
+  if (fabs(p->omega_norm_max - norm_domega) < 1e-6) norm_domega += 1e-4;
+  double Elast = H0[0];
+  double* om = dalloc(A);
+  int steps = 0;
+  for (int istep = 1; sflow < p->smax; ++istep) {
+    double norm_eta = oracle_norm(s, Eta);
+    if (norm_eta < p->eta_criterion) break;
+    if (norm_eta > 1e12 || fabs(Elast) > 1e9) {
+      free(om);
+      *s_io = sflow;
+      return -1;
+    }
+    double norm_omega = oracle_norm(s, Omega);
+    if (norm_omega > p->omega_norm_max) {
+      memcpy(Hsaved, Hs, A * sizeof(double));
+      memset(Omega, 0, A * sizeof(double));
+      ++*n_omega;
+      norm_omega = 0;
+    }
+    if (p->magnus_adaptive) {
+      double a = norm_domega / norm_eta;
+      double b = norm_domega / norm_eta / (norm_omega + 1.0e-9);
+      double c = (p->omega_norm_max + 1e-5) / norm_eta;
+      ds = a;
+      if (b < ds) ds = b;
+      if (c < ds) ds = c;
+      if (p->ds_max < ds) ds = p->ds_max;
+    }
+    if (p->smax - sflow < ds) ds = p->smax - sflow;
+    sflow += ds;
+    for (int64_t t = 0; t < A; ++t) Eta[t] *= ds;
+    oracle_bch_product(s, Eta, -1, Omega, -1, om, p->bch_product_threshold);
+    memcpy(Omega, om, A * sizeof(double));
+    oracle_bch_transform(s, *n_omega < 2 ? H0 : Hsaved, 1, Omega, -1, Hs, p->bch_transform_threshold);
+    oracle_generator(s, Hs, Eta, p->generator, p->partitioning, p->denominator_cutoff, p->denominator_delta,
+                     p->denominator_delta_index);
+    Elast = Hs[0];
+    if (steps < maxhist) {
+      s_hist[steps] = sflow;
+      e0_hist[steps] = Hs[0];
+    }
+    ++steps;
+  }
+  free(om);
+  *s_io = sflow;
+  return steps;
+}
+
 int oracle_num_threads(void)
 {
 #ifdef _OPENMP

@@ -168,6 +168,27 @@ class RefModelSpace:
             self.block(a, ch)[:, :] = S
         return a
 
+    def flow_hamiltonian(self, seed, v2=1.0):
+        """Seeded Hamiltonian for a synthetic Magnus flow: one-body diagonal
+        2n+l+3/2 (oscillator energies in units of hbar*omega), symmetric
+        off-diagonal part uniform[-0.1,0.1] within each (l, j2, tz2) block,
+        two-body part a random hermitian operator (as random_operator) with
+        every channel block scaled to Frobenius norm v2, ZeroBody 0."""
+        a = self.random_operator(seed, hermitian=True)
+        rng = np.random.Generator(np.random.PCG64(seed + 7919))
+        a[0] = 0.0
+        one = self.onebody(a)
+        one[:, :] = 0.0
+        for grp in self.onebody_channels():
+            m = len(grp)
+            R = rng.uniform(-0.1, 0.1, size=(m, m))
+            S = np.triu(R, 1)
+            S = S + S.T
+            S[np.diag_indices(m)] = [2 * self.n[i] + self.l[i] + 1.5 for i in grp]
+            one[np.ix_(grp, grp)] = S
+        a[self.off2[0]:] *= v2
+        return a
+
     def norm(self, arena):
         """Operator::Norm for a scalar operator (src/Operator.cc:1610-1651,
         src/TwoBodyME.cc:703-723)."""

@@ -1,7 +1,8 @@
 """Test infrastructure: NOT part of the product.
 
 ctypes wrapper around the C oracle (oracle/imsrg_oracle.c), the CPU
-restatement of the reference's IMSRG(2) commutator used as the checker in
+restatement of the reference's IMSRG(2) commutator, BCH transform and
+product, White-type generators and Magnus-Euler solver, used as the checker in
 tests/ and as the CPU baseline in bench.py.  Compiled on first use with gcc
 into oracle/_build/ (a plain C + OpenMP shared library).  Matrix products go
 through SciPy's BLAS dgemm (the reference multiplies through BLAS too); pass
@@ -72,9 +73,39 @@ def _load():
             L.oracle_norm.argtypes = [P, D]
             L.oracle_bch_transform.restype = ctypes.c_int
             L.oracle_bch_transform.argtypes = [P, D, ctypes.c_int, D, ctypes.c_int, D, ctypes.c_double]
+            L.oracle_bch_product.restype = ctypes.c_int
+            L.oracle_bch_product.argtypes = [P, D, ctypes.c_int, D, ctypes.c_int, D, ctypes.c_double]
+            L.oracle_generator.argtypes = [P, D, D, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_int]
+            L.oracle_magnus_euler.restype = ctypes.c_int
+            L.oracle_magnus_euler.argtypes = [P, D, D, D, D, D, ctypes.POINTER(FlowParams), D,
+                                              ctypes.POINTER(ctypes.c_int), D, D, ctypes.c_int]
             L.oracle_num_threads.restype = ctypes.c_int
             _lib = L
     return _lib
+
+
+GENERATORS = {"white": 0, "atan": 1, "wegner": 2, "imaginary-time": 3}
+PARTITIONINGS = {"Epstein_Nesbet": 0, "Moller_Plesset": 1}
+
+
+class FlowParams(ctypes.Structure):
+    """oflow_params of imsrg_oracle.c; defaults of IMSRGSolver(H)
+    (src/IMSRGSolver.cc:31-37), Generator() (src/Generator.cc:18-20) and BCH
+    (src/BCH.cc:16-17)."""
+    _fields_ = [("ds", ctypes.c_double), ("ds_max", ctypes.c_double), ("smax", ctypes.c_double),
+                ("norm_domega", ctypes.c_double), ("omega_norm_max", ctypes.c_double),
+                ("eta_criterion", ctypes.c_double), ("magnus_adaptive", ctypes.c_int), ("generator", ctypes.c_int),
+                ("partitioning", ctypes.c_int), ("denominator_cutoff", ctypes.c_double),
+                ("denominator_delta", ctypes.c_double), ("denominator_delta_index", ctypes.c_int),
+                ("bch_transform_threshold", ctypes.c_double), ("bch_product_threshold", ctypes.c_double)]
+
+    def __init__(self, **kw):
+        d = dict(ds=0.1, ds_max=0.5, smax=2.0, norm_domega=0.1, omega_norm_max=2.0, eta_criterion=1e-6,
+                 magnus_adaptive=1, generator=0, partitioning=0, denominator_cutoff=1e-6, denominator_delta=0.0,
+                 denominator_delta_index=-1, bch_transform_threshold=1e-9, bch_product_threshold=1e-4)
+        d.update(kw)
+        super().__init__(**d)
 
 
 def scipy_dgemm_pointer():
@@ -191,6 +222,38 @@ class Oracle:
         out = self.zeros()
         it = self.lib.oracle_bch_transform(self.s, _dptr(H), hH, _dptr(Omega), hOm, _dptr(out), threshold)
         return out, it
+
+    def bch_product(self, X, hX, Y, hY, threshold=1e-4):
+        """BCH::BCH_Product(X, Y); returns (Z, commutators evaluated)."""
+        Z = self.zeros()
+        n = self.lib.oracle_bch_product(self.s, _dptr(X), hX, _dptr(Y), hY, _dptr(Z), threshold)
+        return Z, n
+
+    def generator(self, H, kind="white", partitioning="Epstein_Nesbet", cutoff=1e-6, delta=0.0, delta_index=-1):
+        """Generator::Update(H, Eta) for a single-reference space."""
+        Eta = self.zeros()
+        self.lib.oracle_generator(self.s, _dptr(H), _dptr(Eta), GENERATORS[kind], PARTITIONINGS[partitioning],
+                                  cutoff, delta, delta_index)
+        return Eta
+
+    def magnus_euler(self, H0, params, state=None, maxhist=10000):
+        """IMSRGSolver::Solve_magnus_euler from `state` (a dict with s, Hs,
+        Hsaved, Omega, n_omega; a fresh IMSRGSolver(H0) if None).  Returns
+        the new state plus "steps", "s_hist" and "e0_hist"."""
+        if state is None:
+            state = dict(s=0.0, Hs=H0.copy(), Hsaved=H0.copy(), Omega=self.zeros(), n_omega=1)
+        st = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in state.items()}
+        Eta = self.zeros()
+        s_io = np.array([st["s"]])
+        n_om = ctypes.c_int(st["n_omega"])
+        sh = np.zeros(maxhist)
+        eh = np.zeros(maxhist)
+        steps = self.lib.oracle_magnus_euler(self.s, _dptr(H0), _dptr(st["Hs"]), _dptr(st["Hsaved"]),
+                                             _dptr(st["Omega"]), _dptr(Eta), ctypes.byref(params), _dptr(s_io),
+                                             ctypes.byref(n_om), _dptr(sh), _dptr(eh), maxhist)
+        st.update(s=float(s_io[0]), n_omega=n_om.value, Eta=Eta, steps=steps, s_hist=sh[:max(steps, 0)],
+                  e0_hist=eh[:max(steps, 0)])
+        return st
 
     def num_threads(self):
         return self.lib.oracle_num_threads()

@@ -2,7 +2,8 @@
 #
 # Compiles the reference implementation (IMSRG++) from its own, unmodified
 # sources where they lie, plus the stand-ins in oracle/ref_stubs/ for the
-# libraries this image lacks (GSL coupling coefficients, Boost iostreams), and
+# libraries this image lacks (GSL coupling coefficients, Boost iostreams, the
+# Boost odeint solvers of IMSRGSolver), and
 # links oracle/ref_harness.cc against them.  Armadillo is the copy vendored in
 # the reference (extern/armadillo); BLAS/LAPACK are not installed, so Armadillo
 # runs on its built-in matrix product (ARMA_DONT_USE_BLAS / _LAPACK / _WRAPPER).
@@ -23,13 +24,13 @@ DEFS := -DARMA_DONT_USE_WRAPPER -DARMA_DONT_USE_BLAS -DARMA_DONT_USE_LAPACK -DAR
 INCS := -I$(ORACLE)ref_stubs -I$(SRC) -I$(REF)/extern/armadillo -I$(REF)/extern/half/include
 CXXFLAGS := -std=c++17 -O2 -fopenmp -w $(DEFS) $(INCS)
 
-# the closure of the IMSRG(2) commutator + BCH path (the three-body, tensor and
+# the closure of the IMSRG(2) commutator + BCH path and the Magnus solver (the three-body, tensor and
 # dagger objects only satisfy references from Commutator.cc / Operator.cc)
 REF_UNITS := AngMom AngMomCache ModelSpace TwoBodyChannel TwoBodyME Operator \
   Commutator BCH IMSRGProfiler ThreeBodyME ThreeBodyChannel ThreeBodyStorage \
   ThreeBodyStorage_pn ThreeBodyStorage_iso ThreeBodyStorage_no2b ThreeBodyStorage_mono \
   ThreeLegME IMSRG3Commutators Commutator232 TensorCommutators DaggerCommutators \
-  FactorizedDoubleCommutator ReferenceImplementations version
+  FactorizedDoubleCommutator ReferenceImplementations Generator IMSRGSolver version
 
 REF_OBJS := $(addprefix $(OBJ)/,$(addsuffix .o,$(REF_UNITS)))
 
@@ -44,10 +45,13 @@ $(OBJ)/%.o: $(SRC)/%.cc | $(OBJ)
 $(OBJ)/coupling_stub.o: $(ORACLE)ref_stubs/coupling_stub.c | $(OBJ)
 	$(CC) -O2 -fPIC -c $< -o $@
 
+$(OBJ)/ode_stub.o: $(ORACLE)ref_stubs/ode_stub.cc | $(OBJ)
+	$(CXX) $(CXXFLAGS) -c $< -o $@
+
 $(OBJ)/ref_harness.o: $(ORACLE)ref_harness.cc | $(OBJ)
 	$(CXX) $(CXXFLAGS) -c $< -o $@
 
-$(OUT)/ref_harness: $(REF_OBJS) $(OBJ)/coupling_stub.o $(OBJ)/ref_harness.o
+$(OUT)/ref_harness: $(REF_OBJS) $(OBJ)/coupling_stub.o $(OBJ)/ode_stub.o $(OBJ)/ref_harness.o
 	$(CXX) -fopenmp -o $@ $^ -lm
 
 clean:

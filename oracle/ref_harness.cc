@@ -22,11 +22,28 @@
 //   xw = [X,W] (Z anti-hermitian), and
 //     bch.bin                         BCH::BCH_Transform(X, 0.25*Y/|Y|)
 //     norms.txt                       Operator::Norm of the inputs
+//
+// usage: ref_harness flow <emax> <H.bin> <A.bin> <B.bin> <nsteps> <outdir>
+//   H hermitian (a flow Hamiltonian), A and B anti-hermitian.  Writes
+//     bchp.bin                        BCH::BCH_Product(A, B)
+//     bchp_big.bin                    BCH::BCH_Product(6A, 2B)
+//     eta_white.bin, eta_atan.bin     Generator::Update(H, Eta), types white / atan
+//     eta_white_mp.bin                white with Moller-Plesset denominators
+//     flow_steps.txt                  "s E0" after each of <nsteps> Magnus-Euler
+//                                     steps: IMSRGSolver(H), white generator,
+//                                     ds = ds_max = 0.5, fixed step, no Omega split
+//     flow_Hs.bin, flow_Omega.bin     H(s) and Omega after the last step
+//     flow2_Hs.bin, flow2_Omega.bin,  the same flow with adaptive steps
+//     flow2.txt                       (defaults: norm_domega 0.1, ds_max 0.5),
+//                                     Omega split at |Omega| > 0.3, to s = 2:
+//                                     "s nOmega E0"
 
 #include "ModelSpace.hh"
 #include "Operator.hh"
 #include "Commutator.hh"
 #include "BCH.hh"
+#include "Generator.hh"
+#include "IMSRGSolver.hh"
 
 #include <cstdio>
 #include <cstdlib>
@@ -146,7 +163,82 @@ static void dump_tables(ModelSpace& ms, const std::string& path) {
 
 typedef void (*term_fn)(const Operator&, const Operator&, Operator&);
 
+static int flow_main(int argc, char** argv) {
+  if (argc != 8) {
+    std::cerr << "usage: ref_harness flow <emax> <H.bin> <A.bin> <B.bin> <nsteps> <outdir>\n";
+    return 1;
+  }
+  int emax = std::atoi(argv[2]);
+  int nsteps = std::atoi(argv[6]);
+  std::string outdir = argv[7];
+  ModelSpace ms(emax, "O16", "O16");
+  ArenaLayout L = make_layout(ms);
+  Operator H(ms, 0, 0, 0, 2), A(ms, 0, 0, 0, 2), B(ms, 0, 0, 0, 2);
+  H.SetHermitian();
+  A.SetAntiHermitian();
+  B.SetAntiHermitian();
+  load(H, read_file(argv[3], L.total), L);
+  load(A, read_file(argv[4], L.total), L);
+  load(B, read_file(argv[5], L.total), L);
+
+  write_file(outdir + "/bchp.bin", store(BCH::BCH_Product(A, B), L));
+  {
+    Operator A6 = A * 6.0;
+    Operator B2 = B * 2.0;
+    write_file(outdir + "/bchp_big.bin", store(BCH::BCH_Product(A6, B2), L));
+  }
+
+  struct GenCase { const char* file; const char* type; const char* part; };
+  const GenCase gens[] = {{"eta_white", "white", "Epstein_Nesbet"},
+                          {"eta_atan", "atan", "Epstein_Nesbet"},
+                          {"eta_white_mp", "white", "Moller_Plesset"}};
+  for (const GenCase& g : gens) {
+    Generator gen;
+    gen.SetType(g.type);
+    gen.SetDenominatorPartitioning(g.part);
+    Operator Eta(H);
+    Eta.Erase();
+    Eta.SetAntiHermitian();
+    gen.Update(H, Eta);
+    write_file(outdir + "/" + g.file + ".bin", store(Eta, L));
+  }
+
+  {
+    IMSRGSolver solver(H);
+    solver.SetGenerator("white");
+    solver.SetDs(0.5);
+    solver.SetDsmax(0.5);
+    solver.SetMagnusAdaptive(false);
+    solver.SetOmegaNormMax(1e9);
+    solver.SetEtaCriterion(1e-20);
+    std::ofstream f(outdir + "/flow_steps.txt");
+    f << std::setprecision(17);
+    for (int k = 1; k <= nsteps; ++k) {
+      solver.SetSmax(0.5 * k);
+      solver.Solve();
+      f << solver.GetS() << " " << solver.GetH_s().ZeroBody << "\n";
+    }
+    write_file(outdir + "/flow_Hs.bin", store(solver.GetH_s(), L));
+    write_file(outdir + "/flow_Omega.bin", store(solver.GetOmega(solver.GetOmegaSize() - 1), L));
+  }
+  {
+    IMSRGSolver solver(H);
+    solver.SetGenerator("white");
+    solver.SetOmegaNormMax(0.3);
+    solver.SetEtaCriterion(1e-20);
+    solver.SetSmax(2.0);
+    solver.Solve();
+    std::ofstream f(outdir + "/flow2.txt");
+    f << std::setprecision(17) << solver.GetS() << " " << solver.GetOmegaSize() << " " << solver.GetH_s().ZeroBody
+      << "\n";
+    write_file(outdir + "/flow2_Hs.bin", store(solver.GetH_s(), L));
+    write_file(outdir + "/flow2_Omega.bin", store(solver.GetOmega(solver.GetOmegaSize() - 1), L));
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc > 1 && std::string(argv[1]) == "flow") return flow_main(argc, argv);
   if (argc != 6) {
     std::cerr << "usage: ref_harness <emax> <X.bin> <Y.bin> <W.bin> <outdir>\n";
     return 1;

@@ -15,6 +15,16 @@ Fixtures (arena layout: see oracle/modelspace_ref.py):
                      BCH_Transform of X with Omega = 0.25 Y/|Y|; the reference's
                      channel tables; Operator::Norm of the inputs.
   golden_emax3.npz   the same for the case xy only, plus bch.
+  golden_flow_emax2.npz, golden_flow_emax3.npz
+                     H (flow Hamiltonian, RefModelSpace.flow_hamiltonian with
+                     two-body scale 0.5), A = 0.05 V/|V| and B = 0.5 U/|U|
+                     (anti-hermitian); BCH::BCH_Product(A, B) and of (6A, 2B); the White and
+                     atan generators of H (Epstein-Nesbet) and White with
+                     Moller-Plesset denominators; ten fixed Magnus-Euler steps
+                     (ds 0.5, White generator) with s and E0 after each step and
+                     the final H(s), Omega; an adaptive flow to s = 2 with Omega
+                     split at |Omega| > 0.3 (final s, number of Omegas, E0,
+                     H(s), last Omega).
   sixj_exact.npz     6j symbols {j1 j2 J3; j4 j5 J6} for half-integer
                      j <= 9/2 and integer J <= 9, evaluated in exact rational
                      arithmetic (Racah formula with Python integers), the pin for
@@ -61,6 +71,38 @@ def run_reference(emax, cases):
             out["tables"] = np.array(f.read())
         with open(os.path.join(td, "norms.txt")) as f:
             out["norms"] = np.array([float(x) for x in f.read().split()])
+    return out
+
+
+FLOW_STEPS = 10
+FLOW_V2 = 0.5
+
+
+def flow_inputs(emax):
+    ms = RefModelSpace(emax)
+    H = ms.flow_hamiltonian(5000 + emax, FLOW_V2)
+    A = ms.random_operator(6000 + emax, hermitian=False)
+    A *= 0.05 / ms.norm(A)
+    B = ms.random_operator(7000 + emax, hermitian=False)
+    B *= 0.5 / ms.norm(B)
+    return H, A, B
+
+
+def run_reference_flow(emax):
+    H, A, B = flow_inputs(emax)
+    harness = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+    with tempfile.TemporaryDirectory() as td:
+        for name, a in (("H", H), ("A", A), ("B", B)):
+            a.tofile(os.path.join(td, name + ".bin"))
+        subprocess.run([harness, "flow", str(emax), os.path.join(td, "H.bin"), os.path.join(td, "A.bin"),
+                        os.path.join(td, "B.bin"), str(FLOW_STEPS), td], check=True, stdout=subprocess.DEVNULL,
+                       env=dict(os.environ, OMP_NUM_THREADS="1"))
+        out = {"H": H, "A": A, "B": B, "emax": np.array(emax), "v2": np.array(FLOW_V2)}
+        for k in ("bchp", "bchp_big", "eta_white", "eta_atan", "eta_white_mp", "flow_Hs", "flow_Omega", "flow2_Hs",
+                  "flow2_Omega"):
+            out[k] = np.fromfile(os.path.join(td, k + ".bin"))
+        out["flow_steps"] = np.loadtxt(os.path.join(td, "flow_steps.txt"))
+        out["flow2"] = np.loadtxt(os.path.join(td, "flow2.txt"))
     return out
 
 
@@ -115,11 +157,18 @@ def main():
     np.savez_compressed(os.path.join(HERE, "golden_emax2.npz"), **g2)
     g3 = run_reference(3, ["xy"])
     np.savez_compressed(os.path.join(HERE, "golden_emax3.npz"), **g3)
+    for e in (2, 3):
+        np.savez_compressed(os.path.join(HERE, "golden_flow_emax%d.npz" % e), **run_reference_flow(e))
     keys, vals = make_sixj_table()
     np.savez_compressed(os.path.join(HERE, "sixj_exact.npz"), keys=keys, values=vals)
-    for f in ("golden_emax2.npz", "golden_emax3.npz", "sixj_exact.npz"):
+    for f in ("golden_emax2.npz", "golden_emax3.npz", "golden_flow_emax2.npz", "golden_flow_emax3.npz",
+              "sixj_exact.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["--flow"]:
+        for e in (2, 3):
+            np.savez_compressed(os.path.join(HERE, "golden_flow_emax%d.npz" % e), **run_reference_flow(e))
+    else:
+        main()

@@ -39,3 +39,7 @@ def rel_errors(ms, Z, R, floor=None):
 
 def ref_space(emax):
     return RefModelSpace(emax)
+
+
+def load_flow_golden(emax):
+    return dict(np.load(os.path.join(GOLDEN, "golden_flow_emax%d.npz" % emax)))
