@@ -17,6 +17,7 @@ ERR_CUDA = 2
 ERR_UNSUPPORTED = 3
 ERR_NOMEM = 4
 ERR_KERNEL = 5
+ERR_DIVERGED = 6
 PREC_FP64 = 0
 PREC_SPLIT = 1
 
@@ -72,6 +73,21 @@ SIGNATURES = {
     "imsrg_set_default_precision": (I, [I]),
     "imsrg_get_default_precision": (I, [IP]),
     "imsrg_bch_transform": (I, [P, P, P, D, I, IP, P]),
+    "imsrg_bch_product": (I, [P, P, P, D, I, IP, P]),
+    "imsrg_generator_update": (I, [P, P, I, I, D, D, I, P]),
+    "imsrg_solver_create": (I, [P, ctypes.POINTER(P)]),
+    "imsrg_solver_destroy": (None, [P]),
+    "imsrg_solver_set": (I, [P, ctypes.c_char_p, D]),
+    "imsrg_solver_get": (I, [P, ctypes.c_char_p, DP]),
+    "imsrg_solver_set_generator": (I, [P, ctypes.c_char_p, P]),
+    "imsrg_solver_set_denominator_partitioning": (I, [P, ctypes.c_char_p]),
+    "imsrg_solver_solve": (I, [P, I, P]),
+    "imsrg_solver_hs": (I, [P, ctypes.POINTER(P)]),
+    "imsrg_solver_eta": (I, [P, ctypes.POINTER(P)]),
+    "imsrg_solver_omega": (I, [P, I, ctypes.POINTER(P)]),
+    "imsrg_solver_history": (I, [P, I, IP, DP, DP, DP, DP, IP]),
+    "imsrg_solver_transform": (I, [P, P, P, I, P]),
+    "imsrg_solver_inverse_transform": (I, [P, P, P, I, P]),
     "imsrg_profiler_enable": (I, [I]),
     "imsrg_profiler_reset": (I, []),
     "imsrg_profiler_get": (I, [ctypes.c_char_p, DP, LLP]),

@@ -11,6 +11,7 @@ against pyIMSRG reads the same:
     Z = Commutator.Commutator(X, Y)            # CommutatorScalarScalar
     Commutator.comm222_phss(X, Y, Z)           # accumulate one term into Z
     Hs = BCH.BCH_Transform(H, Omega)
+    solver = IMSRGSolver(H); solver.Solve(); Hs = solver.GetH_s()
 
 Operator keeps its data on the host in the arena layout (numpy); every call
 uploads the operands, runs the CUDA kernels and downloads the result.
@@ -213,8 +214,20 @@ class DeviceOperator:
     def __init__(self, ms, hermiticity=1):
         self.modelspace = ms
         self._L = _lib.lib()
+        self._owned = True
         self._h = ctypes.c_void_p()
         check(self._L.imsrg_op_create(ms._h, int(hermiticity), ctypes.byref(self._h)))
+
+    @classmethod
+    def _view(cls, ms, handle, owner):
+        """An operator owned by another object (a solver's H(s), Eta, Omega)."""
+        d = cls.__new__(cls)
+        d.modelspace = ms
+        d._L = _lib.lib()
+        d._owned = False
+        d._owner = owner
+        d._h = handle
+        return d
 
     @classmethod
     def from_host(cls, op, stream=None):
@@ -223,9 +236,9 @@ class DeviceOperator:
         return d
 
     def close(self):
-        if self._h:
+        if self._h and self._owned:
             self._L.imsrg_op_destroy(self._h)
-            self._h = None
+        self._h = None
 
     def __enter__(self):
         return self
@@ -385,9 +398,31 @@ class _BCHNamespace:
 
     def __init__(self):
         self.bch_transform_threshold = 1e-9
+        self.bch_product_threshold = 1e-4
 
     def Set_BCH_Transform_Threshold(self, x):
         self.bch_transform_threshold = float(x)
+
+    def Set_BCH_Product_Threshold(self, x):
+        self.bch_product_threshold = float(x)
+
+    def BCH_Product(self, X, Y, precision=None):
+        """Z with e^Z = e^X e^Y (src/BCH.cc:267-350)."""
+        ms = X.modelspace
+        out = Operator(ms)
+        with DeviceOperator.from_host(X) as dx, DeviceOperator.from_host(Y) as dy, DeviceOperator(ms) as dz:
+            self.last_n_commutators = self.device_product(dx, dy, dz, precision)
+            dz.download(out.arena)
+            out.hermitian = dz.hermiticity
+        return out
+
+    def device_product(self, dX, dY, dZ, precision=None, stream=None):
+        """BCH_Product on device operators; dZ may be dX or dY.  Returns the
+        number of commutators evaluated."""
+        n = ctypes.c_int()
+        check(_lib.lib().imsrg_bch_product(dX._h, dY._h, dZ._h, self.bch_product_threshold, _precision(precision),
+                                           ctypes.byref(n), stream))
+        return n.value
 
     def BCH_Transform(self, OpIn, Omega, precision=None):
         ms = OpIn.modelspace
@@ -407,3 +442,202 @@ class _BCHNamespace:
 
 
 BCH = _BCHNamespace()
+
+
+_GENERATOR_TYPES = {"white": 0, "atan": 1, "wegner": 2, "imaginary-time": 3}
+DELTA_ALL = -12345
+
+
+class Generator:
+    """Generator (src/Generator.hh:21-90) for the single-reference types
+    white, atan, wegner and imaginary-time; Epstein-Nesbet (default) or
+    Moller-Plesset denominators."""
+
+    def __init__(self):
+        self.generator_type = "white"
+        self.denominator_partitioning = "Epstein_Nesbet"
+        self.denominator_cutoff = 1e-6
+        self.denominator_delta = 0.0
+        self.denominator_delta_index = -1
+
+    def SetType(self, g):
+        if g not in _GENERATOR_TYPES:
+            raise NotImplementedError("generator type %r is not on the GPU path" % g)
+        self.generator_type = g
+
+    def GetType(self):
+        return self.generator_type
+
+    def SetDenominatorPartitioning(self, dp):
+        if dp == "MP_isospin":
+            raise NotImplementedError("MP_isospin partitioning is not on the GPU path")
+        self.denominator_partitioning = "Moller_Plesset" if dp == "Moller_Plesset" else "Epstein_Nesbet"
+
+    def SetDenominatorCutoff(self, c):
+        self.denominator_cutoff = float(c)
+
+    def SetDenominatorDelta(self, d):
+        self.denominator_delta = float(d)
+
+    def SetDenominatorDeltaIndex(self, i):
+        self.denominator_delta_index = int(i)
+
+    def device_update(self, dH, dEta, stream=None):
+        part = 1 if self.denominator_partitioning == "Moller_Plesset" else 0
+        check(_lib.lib().imsrg_generator_update(dH._h, dEta._h, _GENERATOR_TYPES[self.generator_type], part,
+                                                self.denominator_cutoff, self.denominator_delta,
+                                                self.denominator_delta_index, stream))
+
+    def Update(self, H, Eta):
+        """Generator::Update(H_s, Eta_s): Eta overwritten (anti-hermitian)."""
+        with DeviceOperator.from_host(H) as dh, DeviceOperator(H.modelspace, -1) as de:
+            self.device_update(dh, de)
+            de.download(Eta.arena)
+        Eta.hermitian = -1
+
+
+class IMSRGSolver:
+    """IMSRGSolver (src/IMSRGSolver.hh:35-210) with the Magnus-Euler method,
+    every operator resident on the device.  H may be a host Operator (copied to
+    the device) or a DeviceOperator (used in place; it must not change while
+    the solver lives)."""
+
+    def __init__(self, H, precision=None):
+        ms = H.modelspace
+        self.modelspace = ms
+        self._L = _lib.lib()
+        self._H0 = H if isinstance(H, DeviceOperator) else DeviceOperator.from_host(H)
+        self._h = ctypes.c_void_p()
+        check(self._L.imsrg_solver_create(self._H0._h, ctypes.byref(self._h)))
+        self.precision = precision
+        self.method = "magnus_euler"
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.imsrg_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _set(self, name, v):
+        check(self._L.imsrg_solver_set(self._h, name.encode(), float(v)))
+
+    def _get(self, name):
+        v = ctypes.c_double()
+        check(self._L.imsrg_solver_get(self._h, name.encode(), ctypes.byref(v)))
+        return v.value
+
+    # settings (pyIMSRG names, src/pyIMSRG.cc:539-595)
+    def SetDs(self, d):
+        self._set("ds", d)
+
+    def SetDsmax(self, d):
+        self._set("ds_max", d)
+
+    def SetSmax(self, d):
+        self._set("smax", d)
+
+    def SetdOmega(self, d):
+        self._set("domega", d)
+
+    def SetOmegaNormMax(self, x):
+        self._set("omega_norm_max", x)
+
+    def SetEtaCriterion(self, x):
+        self._set("eta_criterion", x)
+
+    def SetMagnusAdaptive(self, b=True):
+        self._set("magnus_adaptive", 1 if b else 0)
+
+    def SetHunterGatherer(self, b=True):
+        self._set("hunter_gatherer", 1 if b else 0)
+
+    def SetDenominatorCutoff(self, c):
+        self._set("denominator_cutoff", c)
+
+    def SetDenominatorDelta(self, d):
+        self._set("denominator_delta", d)
+
+    def SetDenominatorDeltaIndex(self, i):
+        self._set("denominator_delta_index", i)
+
+    def SetGenerator(self, g, stream=None):
+        check(self._L.imsrg_solver_set_generator(self._h, g.encode(), stream))
+
+    def SetDenominatorPartitioning(self, dp):
+        check(self._L.imsrg_solver_set_denominator_partitioning(self._h, dp.encode()))
+
+    def SetMethod(self, m):
+        if m not in ("magnus_euler", "magnus"):
+            raise NotImplementedError("solver method %r is not on the GPU path" % m)
+        self.method = m
+
+    def SetBCHTransformThreshold(self, x):
+        self._set("bch_transform_threshold", x)
+
+    def SetBCHProductThreshold(self, x):
+        self._set("bch_product_threshold", x)
+
+    # flow
+    def Solve(self, stream=None):
+        check(self._L.imsrg_solver_solve(self._h, _precision(self.precision), stream))
+
+    def GetS(self):
+        return self._get("s")
+
+    def GetOmegaSize(self):
+        return int(self._get("n_omega"))
+
+    def device_hs(self):
+        h = ctypes.c_void_p()
+        check(self._L.imsrg_solver_hs(self._h, ctypes.byref(h)))
+        return DeviceOperator._view(self.modelspace, h, self)
+
+    def device_eta(self):
+        h = ctypes.c_void_p()
+        check(self._L.imsrg_solver_eta(self._h, ctypes.byref(h)))
+        return DeviceOperator._view(self.modelspace, h, self)
+
+    def device_omega(self, i):
+        h = ctypes.c_void_p()
+        check(self._L.imsrg_solver_omega(self._h, int(i), ctypes.byref(h)))
+        return DeviceOperator._view(self.modelspace, h, self)
+
+    def GetH_s(self):
+        return self.device_hs().to_host()
+
+    def GetEta(self):
+        return self.device_eta().to_host()
+
+    def GetOmega(self, i):
+        return self.device_omega(i).to_host()
+
+    def history(self):
+        """Per step: (istep, s, E0, |eta|, |Omega|) arrays."""
+        n = ctypes.c_int()
+        check(self._L.imsrg_solver_history(self._h, 0, None, None, None, None, None, ctypes.byref(n)))
+        m = n.value
+        it = np.zeros(max(m, 1), dtype=np.int32)
+        cols = [np.zeros(max(m, 1)) for _ in range(4)]
+        check(self._L.imsrg_solver_history(self._h, m, _ip(it), *[_dp(c) for c in cols], ctypes.byref(n)))
+        return it[:m], cols[0][:m], cols[1][:m], cols[2][:m], cols[3][:m]
+
+    def Transform(self, op):
+        out = Operator(op.modelspace)
+        with DeviceOperator.from_host(op) as di, DeviceOperator(op.modelspace, op.hermitian) as do:
+            check(self._L.imsrg_solver_transform(self._h, di._h, do._h, _precision(self.precision), None))
+            do.download(out.arena)
+            out.hermitian = do.hermiticity
+        return out
+
+    def InverseTransform(self, op):
+        out = Operator(op.modelspace)
+        with DeviceOperator.from_host(op) as di, DeviceOperator(op.modelspace, op.hermitian) as do:
+            check(self._L.imsrg_solver_inverse_transform(self._h, di._h, do._h, _precision(self.precision), None))
+            do.download(out.arena)
+            out.hermitian = do.hermiticity
+        return out

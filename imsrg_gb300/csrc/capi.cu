@@ -927,3 +927,13 @@ int imsrg_bch_transform(const imsrg_op* OpIn, const imsrg_op* Omega, imsrg_op* O
 }
 
 }  // extern "C"
+
+// entry points of this file the flow layer (capi_flow.cu) builds on
+namespace imsrg {
+int commutator_dev(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStream_t st)
+{
+  return commutator_impl(X, Y, Z, prec, st);
+}
+int norm_dev(const imsrg_op* op, double* out, cudaStream_t st) { return norm_impl(op, out, st); }
+int status_dev(imsrg_space* sp, cudaStream_t st) { return check_status(sp, st); }
+}  // namespace imsrg

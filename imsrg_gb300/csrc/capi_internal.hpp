@@ -16,9 +16,17 @@ using imsrg::GemmJobDev;
 using imsrg::Space;
 using imsrg::SplitPlan;
 
+struct imsrg_op;
+struct imsrg_space;
+
 namespace imsrg {
 // sets the calling thread's imsrg_last_error() message and returns code
 int set_error(int code, const char* msg);
+// CommutatorScalarScalar into Z (overwritten), Operator::Norm (synchronises
+// st), and the kernels' error word (synchronises st; IMSRG_ERR_KERNEL if set)
+int commutator_dev(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStream_t st);
+int norm_dev(const imsrg_op* op, double* out, cudaStream_t st);
+int status_dev(imsrg_space* sp, cudaStream_t st);
 }  // namespace imsrg
 
 struct imsrg_space {
@@ -62,8 +70,10 @@ struct imsrg_space {
   // split-precision plans
   SplitPlan* split_ladder = nullptr;
   SplitPlan* split_zbar = nullptr;
-  // BCH work operators
-  double *d_nested = nullptr, *d_next = nullptr;
+  // BCH work operators (d_prod: BCH_Product result when Z aliases X or Y)
+  double *d_nested = nullptr, *d_next = nullptr, *d_prod = nullptr;
+  // generator scratch: monopoles V(ab, ab) of H, norb^2
+  double* d_mono = nullptr;
   // second stream of CommutatorScalarScalar (work independent of the ladder
   // product) and the events that fork it from and join it to the caller's
   cudaStream_t side = nullptr;

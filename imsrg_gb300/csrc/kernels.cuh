@@ -44,6 +44,18 @@ cudaError_t launch_pandya_inv_ff(const Space& s, const double* Zb, double* Z, in
                                  cudaStream_t st);
 // shared-memory budget of one quadruple block (dynamic part)
 constexpr int kInvqBudget = 36864;
+// Generator::Update for a single-reference space (white / atan / wegner /
+// imaginary-time functions, Epstein-Nesbet or Moller-Plesset denominators):
+// Eta is overwritten; mono is norb^2 doubles of scratch
+enum { GEN_WHITE = 0, GEN_ATAN = 1, GEN_WEGNER = 2, GEN_IMAGINARY_TIME = 3 };
+enum { DENOM_EPSTEIN_NESBET = 0, DENOM_MOLLER_PLESSET = 1 };
+constexpr int kDeltaAll = -12345;  // denominator_delta_index that adds the delta everywhere
+struct GenParams {
+  int type = GEN_WHITE, partitioning = DENOM_EPSTEIN_NESBET, delta_index = -1;
+  double cutoff = 1e-6, delta = 0.0;
+};
+cudaError_t launch_generator(const Space& s, const double* H, double* Eta, double* mono, const GenParams& p,
+                             cudaStream_t st);
 cudaError_t launch_axpy(double* y, const double* x, double a, long long n, cudaStream_t st);
 cudaError_t launch_scale(double* y, double a, long long n, cudaStream_t st);
 cudaError_t launch_norm(const Space& s, const double* A, const long long* chunk_off, const int* chunk_len,

@@ -1059,6 +1059,98 @@ __global__ void __launch_bounds__(kInvqThreads) k_pandya_inv_ff(DevSpace S, DevW
   }
 }
 
+// ------------------------------------------------------------------ generator
+// Generator::Update -> ConstructGenerator_SingleRef (src/Generator.cc:32-76,
+// 236-297) for a single-reference space, whose core is the set of occupied
+// orbits: Eta is zero except <i|Eta|a> (i outside, a inside the core) and
+// <ij|Eta|kl> (i, j outside, k, l inside), each the generator function of the
+// matching element of H and its energy denominator, antisymmetrised.
+constexpr double kGenOccCut = 1e-6;  // ModelSpace::OCC_CUT (src/ModelSpace.cc:14)
+
+// the generator functions of src/Generator.cc:12-15
+__device__ __forceinline__ double eta_value(int type, double hod, double den)
+{
+  switch (type) {
+    case GEN_ATAN: return 0.5 * atan(2 * hod / den);
+    case GEN_WEGNER: return hod * den;
+    case GEN_IMAGINARY_TIME: return hod * (double)((den > 0) - (den < 0));
+    default: return hod / den;
+  }
+}
+
+// M[a * N + b] = GetTBMEmonopole(a, b, a, b): the monopoles the Epstein-Nesbet
+// denominators add (src/Generator.cc:116-119, 172-180)
+__global__ void k_gen_monopoles(DevSpace S, const double* __restrict__ H, double* __restrict__ M)
+{
+  int N = S.norb;
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= N * N) return;
+  int a = idx / N, b = idx - a * N;
+  M[idx] = dev_monopole(S, H, a, b, a, b);
+}
+
+// one-body part; Generator::Get1bDenominator, src/Generator.cc:110-139
+__global__ void k_gen_onebody(DevSpace S, const double* __restrict__ H, const double* __restrict__ M,
+                              double* __restrict__ Eta, GenParams p)
+{
+  int N = S.norb;
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= N * N) return;
+  int a = idx / N, i = idx - a * N;  // column a (core), row i (outside the core)
+  double na = S.occ[a], ni = S.occ[i];
+  if (na < kGenOccCut || ni >= kGenOccCut) return;
+  const double* H1 = H + 32;
+  double d = H1[(long long)i * N + i] - H1[(long long)a * N + a];
+  if (p.partitioning == DENOM_EPSTEIN_NESBET) d += (ni - na) * M[(long long)i * N + a];
+  if (p.delta_index == kDeltaAll || i == p.delta_index || a == p.delta_index) d += p.delta;
+  if (fabs(d) < p.cutoff) d = p.cutoff;
+  double e = eta_value(p.type, H1[(long long)a * N + i], d);
+  Eta[32 + (long long)a * N + i] = e;
+  Eta[32 + (long long)i * N + a] = -e;
+}
+
+// two-body part, one block per channel: columns are the channel's hh kets,
+// threads run over the bra kets; Generator::Get2bDenominator,
+// src/Generator.cc:142-188
+__global__ void k_gen_twobody(DevSpace S, DevWork W, const double* __restrict__ H, const double* __restrict__ M,
+                              double* __restrict__ Eta, GenParams p)
+{
+  int ch = blockIdx.x;
+  int n = S.ch_n[ch];
+  int h0 = W.hh_off[ch], h1 = W.hh_off[ch + 1];
+  if (n == 0 || h0 == h1) return;
+  int N = S.norb;
+  long long off = S.ch_off[ch];
+  int kofs = S.ch_kofs[ch];
+  const double* H1 = H + 32;
+  const bool en = p.partitioning == DENOM_EPSTEIN_NESBET;
+  for (int h = h0; h < h1; ++h) {
+    int ik = W.hh_list[h];
+    int k = S.ket_p[kofs + ik], l = S.ket_q[kofs + ik];
+    double nk = S.occ[k], nl = S.occ[l];
+    double fk = H1[(long long)k * N + k], fl = H1[(long long)l * N + l];
+    for (int ib = threadIdx.x; ib < n; ib += blockDim.x) {
+      int i = S.ket_p[kofs + ib], j = S.ket_q[kofs + ib];
+      double ni = S.occ[i], nj = S.occ[j];
+      if (ni >= kGenOccCut || nj >= kGenOccCut) continue;
+      double d = H1[(long long)i * N + i] + H1[(long long)j * N + j] - fk - fl;
+      if (p.delta_index == kDeltaAll) d += p.delta;
+      if (en) {
+        d += (1 - ni - nj) * M[(long long)i * N + j];
+        d -= (1 - nk - nl) * M[(long long)k * N + l];
+        d += (ni - nk) * M[(long long)i * N + k];
+        d += (ni - nl) * M[(long long)i * N + l];
+        d += (nj - nk) * M[(long long)j * N + k];
+        d += (nj - nl) * M[(long long)j * N + l];
+      }
+      if (fabs(d) < p.cutoff) d = p.cutoff;
+      double e = eta_value(p.type, H[off + (long long)ik * n + ib], d);
+      Eta[off + (long long)ik * n + ib] = e;
+      Eta[off + (long long)ib * n + ik] = -e;
+    }
+  }
+}
+
 // ------------------------------------------------------------ operator algebra
 __global__ void k_axpy(double* __restrict__ y, const double* __restrict__ x, double a, long long n)
 {
@@ -1226,6 +1318,24 @@ cudaError_t launch_pandya_inv_ff(const Space& s, const double* Zb, double* Z, in
   if (e != cudaSuccess) return e;
   k_pandya_inv_ff<<<ntasks, kInvqThreads, smem, st>>>(s.dev, s.work, Zb, Z, hZ, (const int4*)tasks, clist, coff,
                                                         csort);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_generator(const Space& s, const double* H, double* Eta, double* mono, const GenParams& p,
+                             cudaStream_t st)
+{
+  cudaError_t e = cudaMemsetAsync(Eta, 0, s.arena * sizeof(double), st);
+  if (e != cudaSuccess) return e;
+  int nn = s.norb * s.norb;
+  int blocks = (nn + 255) / 256;
+  if (p.partitioning == DENOM_EPSTEIN_NESBET) {
+    k_gen_monopoles<<<blocks, 256, 0, st>>>(s.dev, H, mono);
+    count_launch();
+  }
+  k_gen_onebody<<<blocks, 256, 0, st>>>(s.dev, H, mono, Eta, p);
+  count_launch();
+  k_gen_twobody<<<s.nch, 256, 0, st>>>(s.dev, s.work, H, mono, Eta, p);
   count_launch();
   return cudaGetLastError();
 }

@@ -41,13 +41,26 @@ extern "C" {
 #define IMSRG_ERR_UNSUPPORTED 3 /* operator symmetry the GPU path does not handle */
 #define IMSRG_ERR_NOMEM 4       /* device allocation failed */
 #define IMSRG_ERR_KERNEL 5      /* a kernel reported an error through its status word */
+#define IMSRG_ERR_DIVERGED 6    /* the IMSRG flow blew up (|eta| > 1e12 or |E0| > 1e9) */
 
 /* precision of the dense contractions (ladder and Pandya channel GEMMs) */
 #define IMSRG_PREC_FP64 0  /* plain FP64 (CUDA-core DFMA) */
 #define IMSRG_PREC_SPLIT 1 /* Ozaki-style sliced BF16 tensor-core products (tcgen05), FP64 recombination */
 
+/* generator functions (src/Generator.cc:12-15) and energy-denominator
+ * partitionings (src/Generator.cc:23-28) */
+#define IMSRG_GEN_WHITE 0          /* Hod / denominator (the default) */
+#define IMSRG_GEN_ATAN 1           /* atan(2 Hod / denominator) / 2 */
+#define IMSRG_GEN_WEGNER 2         /* Hod * denominator */
+#define IMSRG_GEN_IMAGINARY_TIME 3 /* Hod * sign(denominator) */
+#define IMSRG_DENOM_EPSTEIN_NESBET 0
+#define IMSRG_DENOM_MOLLER_PLESSET 1
+/* denominator_delta_index that adds denominator_delta to every denominator */
+#define IMSRG_DELTA_ALL (-12345)
+
 typedef struct imsrg_space imsrg_space;
 typedef struct imsrg_op imsrg_op;
+typedef struct imsrg_solver imsrg_solver;
 
 /* Last error message of the calling thread ("" if none). */
 const char* imsrg_last_error(void);
@@ -189,6 +202,81 @@ int imsrg_get_default_precision(int* precision);
  * for the convergence test. */
 int imsrg_bch_transform(const imsrg_op* OpIn, const imsrg_op* Omega, imsrg_op* OpOut, double threshold,
                         int precision, int* n_nested, void* stream);
+
+/* BCH::BCH_Product (src/BCH.cc:267-350): Z with e^Z = e^X e^Y,
+ * Z = X + Y + 1/2 [X,Y] + 1/12 ([X,[X,Y]] + [Y,[Y,X]]) + ..., nested [Y, .]
+ * commutators with Bernoulli coefficients while their norm exceeds threshold
+ * (BCH::bch_product_threshold, default 1e-4; at most 8 nested terms); the
+ * [X,[X,Y]] term only when |[Y,X]| |X| > threshold.  Z may alias X or Y and
+ * takes X's hermiticity (Operator Z = X + Y).  n_commutators (may be NULL)
+ * receives the number of commutators evaluated.  Synchronises the stream once
+ * per commutator.  The factorized three-body correction (off by default in the
+ * reference) is not on the GPU path. */
+int imsrg_bch_product(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, double threshold, int precision,
+                      int* n_commutators, void* stream);
+
+/* -------------------------------------------------------------- generator */
+/* Generator::Update(H, Eta) (src/Generator.cc:32-76) for the single-reference
+ * generators (ConstructGenerator_SingleRef, :236-297): Eta is overwritten with
+ * an anti-hermitian operator that is zero except <i|Eta|a> for core orbit a
+ * and non-core i, and <ij|Eta|kl> for non-core i, j and core k, l; each is
+ * type's function of H's element and its energy denominator
+ * (Get1bDenominator / Get2bDenominator, :110-188: Epstein-Nesbet adds the
+ * monopoles of H; |denominator| < cutoff is replaced by cutoff; delta is added
+ * to the denominators selected by delta_index: IMSRG_DELTA_ALL for all, an
+ * orbit index for the one-body ones touching that orbit, -1 for none).  The
+ * core is the set of occupied orbits (the reference's core for a
+ * single-reference space, src/ModelSpace.cc:278-280).  Reference defaults:
+ * cutoff 1e-6, delta 0, delta_index -1.  MP_isospin partitioning and the
+ * shell-model / Hartree-Fock / three-body generators are not on the GPU path. */
+int imsrg_generator_update(const imsrg_op* H, imsrg_op* Eta, int type, int partitioning, double cutoff,
+                           double delta, int delta_index, void* stream);
+
+/* ----------------------------------------------------------------- solver */
+/* IMSRGSolver (src/IMSRGSolver.hh:35-210) with the Magnus-Euler method
+ * (Solve_magnus_euler, src/IMSRGSolver.cc:236-321), every operator in device
+ * memory.  The solver refers to H0, which must outlive it unchanged; it owns
+ * H(s), Eta and the Omegas (no scratch files: IMSRGSolver::NewOmega keeps
+ * earlier Omegas in device memory).  Defaults are IMSRGSolver(H)'s:
+ * ds 0.1, ds_max 0.5, smax 2, domega 0.1, omega_norm_max 2, eta_criterion
+ * 1e-6, adaptive steps, White generator, Epstein-Nesbet denominators. */
+int imsrg_solver_create(const imsrg_op* H0, imsrg_solver** out);
+void imsrg_solver_destroy(imsrg_solver* solver);
+/* Settings by name, the IMSRGSolver / Generator / BCH setters:
+ * "ds" (SetDs), "ds_max" (SetDsmax), "smax" (SetSmax), "domega" (SetdOmega),
+ * "omega_norm_max", "eta_criterion" (stored as float, as SetEtaCriterion
+ * does), "magnus_adaptive", "hunter_gatherer" (0/1), "denominator_cutoff",
+ * "denominator_delta", "denominator_delta_index", "bch_transform_threshold",
+ * "bch_product_threshold".  imsrg_solver_get also reads "s" (flow parameter),
+ * "n_omega" (Omegas kept) and "istep" (steps of the last solve, + 1). */
+int imsrg_solver_set(imsrg_solver* solver, const char* name, double value);
+int imsrg_solver_get(const imsrg_solver* solver, const char* name, double* value);
+/* IMSRGSolver::SetGenerator ("white", "atan", "wegner", "imaginary-time"):
+ * starts a new Omega when the current one is not empty (src/IMSRGSolver.cc:157-183). */
+int imsrg_solver_set_generator(imsrg_solver* solver, const char* type, void* stream);
+/* IMSRGSolver::SetDenominatorPartitioning ("Epstein_Nesbet", "Moller_Plesset") */
+int imsrg_solver_set_denominator_partitioning(imsrg_solver* solver, const char* partitioning);
+/* IMSRGSolver::Solve() with method magnus_euler: flows from the current s to
+ * smax (or until |eta| < eta_criterion).  IMSRG_ERR_DIVERGED when the
+ * reference's give-up test fires (H(s) is then multiplied by 1/0, as there). */
+int imsrg_solver_solve(imsrg_solver* solver, int precision, void* stream);
+/* GetH_s, GetEta and GetOmega(i) (0 <= i < n_omega): the solver's operators */
+int imsrg_solver_hs(imsrg_solver* solver, imsrg_op** out);
+int imsrg_solver_eta(imsrg_solver* solver, imsrg_op** out);
+int imsrg_solver_omega(imsrg_solver* solver, int i, imsrg_op** out);
+/* Flow record, one entry per step of every solve (WriteFlowStatus columns,
+ * src/IMSRGSolver.cc:1206-1231): step, s, H(s).ZeroBody, |eta| and |Omega|
+ * before the step.  Arrays may be NULL; *n receives the number of entries,
+ * at most cap are written. */
+int imsrg_solver_history(const imsrg_solver* solver, int cap, int* istep, double* s, double* e0, double* norm_eta,
+                         double* norm_omega, int* n);
+/* IMSRGSolver::Transform (src/IMSRGSolver.cc:928-1002): OpOut = e^Omega OpIn
+ * e^-Omega through every Omega in order; InverseTransform (:939-952) undoes it.
+ * OpOut may alias OpIn. */
+int imsrg_solver_transform(const imsrg_solver* solver, const imsrg_op* OpIn, imsrg_op* OpOut, int precision,
+                           void* stream);
+int imsrg_solver_inverse_transform(const imsrg_solver* solver, const imsrg_op* OpIn, imsrg_op* OpOut, int precision,
+                                   void* stream);
 
 /* ------------------------------------------------------------- profiling */
 /* Named phase timers measured with CUDA events on the stream each phase ran
