@@ -26,6 +26,14 @@ oracle port (the reference's own build needs the reference sources, absent on
 the GPU host), on all host threads; rank 0 only.
 Multi-GPU: replicas only (each rank runs its own commutators; no collective
 on the data path).
+
+--workload flow: the synthetic Magnus flow instead (IMSRGSolver,
+magnus_euler, White generator, fixed ds = 0.5, no Omega split) at emax=12 by
+default: H has one-body diagonal 2n+l+3/2, off-diagonal uniform[-0.1,0.1]
+within (l, j2, tz2) blocks and a random hermitian two-body part scaled to
+Frobenius norm 0.5 per channel.  value = ms per flow step of the split form
+(after W warm-up steps of a separate flow), with the plain FP64 form's ms per
+step and both forms' zero-body energies beside it.
 """
 import argparse
 import ctypes
@@ -52,7 +60,9 @@ def parse_args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--emax", type=int, default=10)
+    p.add_argument("--emax", type=int, default=None, help="default 10 (commutator), 12 (flow)")
+    p.add_argument("--workload", default="commutator", choices=["commutator", "flow"])
+    p.add_argument("--fp64-steps", type=int, default=None, help="flow steps timed in the FP64 form")
     p.add_argument("--precision", default="split", choices=["split", "fp64"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -515,8 +525,160 @@ def run_gb300(args):
         torch.distributed.destroy_process_group()
 
 
+FLOW_METRIC = "ms per Magnus-Euler flow step (White generator, ds=0.5) at emax={emax}: split vs FP64 on 1 GB300"
+
+
+def flow_hamiltonian(ig, ms, seed, v2=0.5):
+    """The flow workload's H through the product API: a seeded random
+    hermitian operator (imsrg_op_fill_random), one-body part replaced by the
+    oscillator diagonal 2n+l+3/2 plus symmetric uniform[-0.1,0.1] couplings
+    within each (l, j2, tz2) block, two-body part scaled by v2, ZeroBody 0."""
+    import numpy as np
+    with ig.DeviceOperator(ms, 1) as d:
+        d.fill_random(seed)
+        a = d.download()
+    rng = np.random.Generator(np.random.PCG64(seed + 7919))
+    N = ms.norb
+    one = a[32:32 + N * N].reshape(N, N, order="F")
+    one[:, :] = 0.0
+    groups = {}
+    for i, (n, l, j2, tz2, _) in enumerate(ms.orbits):
+        groups.setdefault((l, j2, tz2), []).append(i)
+    for grp in groups.values():
+        m = len(grp)
+        R = np.triu(rng.uniform(-0.1, 0.1, size=(m, m)), 1)
+        S = R + R.T
+        S[np.diag_indices(m)] = [2 * ms.orbits[i][0] + ms.orbits[i][1] + 1.5 for i in grp]
+        one[np.ix_(grp, grp)] = S
+    a[0] = 0.0
+    a[ms.channels[0]["offset"]:] *= v2
+    return a
+
+
+def run_flow(args):
+    import torch
+
+    import imsrg_gb300 as ig
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    L = ig.lib()
+    emax = args.emax
+    ms = ig.ModelSpace(emax, "O16", "O16")
+    H = ig.DeviceOperator(ms, 1)
+    H.upload(flow_hamiltonian(ig, ms, 5000 + emax + rank))
+
+    def solver(prec, nsteps):
+        sv = ig.IMSRGSolver(H, precision=prec)
+        sv.SetGenerator("white")
+        sv.SetDs(0.5)
+        sv.SetDsmax(0.5)
+        sv.SetMagnusAdaptive(False)
+        sv.SetOmegaNormMax(1e9)
+        sv.SetEtaCriterion(1e-20)
+        sv.SetSmax(0.5 * nsteps)
+        return sv
+
+    def timed_flow(prec, nsteps):
+        sv = solver(prec, max(3, args.warmup))
+        sv.Solve()  # warm-up flow: scratch, plans, tables
+        del sv
+        sv = solver(prec, nsteps)
+        torch.cuda.synchronize()
+        L.imsrg_profiler_reset()
+        L.imsrg_profiler_enable(1)
+        l0 = L.imsrg_kernel_launches()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        sv.Solve()
+        e1.record()
+        torch.cuda.synchronize()
+        launches = L.imsrg_kernel_launches() - l0
+        L.imsrg_profiler_enable(0)
+        ncomm = ctypes.c_longlong()
+        t = ctypes.c_double()
+        L.imsrg_profiler_get(b"CommutatorScalarScalar", ctypes.byref(t), ctypes.byref(ncomm))
+        it, s, e0s, ne, no = sv.history()
+        ms_step = e0.elapsed_time(e1) / nsteps
+        return {"ms_per_step": ms_step, "steps": int(len(it)), "e0": float(e0s[-1]), "s": float(s[-1]),
+                "commutators_per_step": ncomm.value / nsteps, "commutator_ms_per_step": t.value / nsteps,
+                "norm_eta_last": float(ne[-1]), "launches": int(launches)}, e0s
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    split, e_split = timed_flow("split", args.steps)
+    clocks.stop()
+    nf = args.fp64_steps if args.fp64_steps is not None else min(args.steps, 5)
+    fp64, e_fp64 = timed_flow("fp64", nf)
+    m = min(len(e_split), len(e_fp64))
+    dev = float(max(abs(a - b) / abs(b) for a, b in zip(e_split[:m], e_fp64[:m]))) if m else None
+    if rank != 0:
+        return
+    # CPU baseline: the C oracle's Magnus-Euler flow on the same H for the
+    # first step(s), all host cores (bounded sample)
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        import tempfile
+        ha = H.download()
+        with tempfile.TemporaryDirectory() as td:
+            fn = os.path.join(td, "H.npy")
+            import numpy as np
+            np.save(fn, ha)
+            code = r"""
+import sys, time, json
+import numpy as np
+sys.path.insert(0, %r)
+from oracle import Oracle, FlowParams
+o = Oracle(%d)
+H = np.load(%r)
+p = FlowParams(ds=0.5, ds_max=0.5, smax=0.5, magnus_adaptive=0, omega_norm_max=1e9, eta_criterion=1e-20)
+t0 = time.perf_counter()
+st = o.magnus_euler(H, p)
+t = time.perf_counter() - t0
+print(json.dumps({"t": t, "steps": st["steps"], "e0": list(st["e0_hist"]), "threads": o.num_threads()}))
+""" % (os.path.join(ROOT, "oracle"), emax, fn)
+            threads = os.cpu_count() or 1
+            env = dict(os.environ, OMP_NUM_THREADS=str(threads), OPENBLAS_NUM_THREADS="1")
+            try:
+                r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env,
+                                   timeout=1800)
+                d = json.loads(r.stdout.strip().splitlines()[-1])
+                e_cpu = d["e0"][0]
+                cpu = {"value": 1000.0 * d["t"] / d["steps"], "unit": "ms/step", "cores": d["threads"],
+                       "kind": "port", "sample": "first flow step at emax=%d, C oracle (OpenMP + SciPy BLAS); "
+                                                 "includes its 6j table fill" % emax,
+                       "e0_step1": e_cpu,
+                       "e0_step1_rel_split": abs(e_split[0] - e_cpu) / abs(e_cpu),
+                       "e0_step1_rel_fp64": abs(e_fp64[0] - e_cpu) / abs(e_cpu)}
+            except Exception as ex:  # reported, not fatal
+                cpu = {"value": None, "unit": "ms/step", "kind": "port", "sample": "failed: %s" % ex}
+    out = {
+        "metric": FLOW_METRIC.format(emax=emax), "value": split["ms_per_step"], "unit": "ms/step",
+        "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": split["ms_per_step"],
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "Magnus-Euler flow, White generator, Epstein-Nesbet, ds=0.5 fixed, emax=%d O16, "
+                               "H: oscillator 1b diagonal + uniform[-0.1,0.1] couplings, random hermitian 2b at "
+                               "Frobenius 0.5 per channel" % emax,
+                   "emax": emax, "orbits": ms.norb, "precision": "split",
+                   "l2": "working set > L2 every step"},
+        "split": split, "plain_fp64": fp64,
+        "e0_max_rel_split_vs_fp64": dev, "e0_steps_compared": m, "cpu_baseline": cpu,
+        "clocks": clocks.summary(), "gpu_launches": split["launches"],
+    }
+    print(json.dumps(out))
+
+
 def main():
     args = parse_args()
+    if args.emax is None:
+        args.emax = 12 if args.workload == "flow" else 10
+    if args.workload == "flow":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the CPU flow at emax=12 takes hours; the flow "
+                              "parity tests compare against the reference's own flow at emax 2-3"}))
+            return
+        run_flow(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
