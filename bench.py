@@ -646,7 +646,7 @@ print(json.dumps({"t": t, "steps": st["steps"], "e0": list(st["e0_hist"]), "thre
                 e_cpu = d["e0"][0]
                 cpu = {"value": 1000.0 * d["t"] / d["steps"], "unit": "ms/step", "cores": d["threads"],
                        "kind": "port", "sample": "first flow step at emax=%d, C oracle (OpenMP + SciPy BLAS); "
-                                                 "includes its 6j table fill" % emax,
+                                                 "table setup excluded" % emax,
                        "e0_step1": e_cpu,
                        "e0_step1_rel_split": abs(e_split[0] - e_cpu) / abs(e_cpu),
                        "e0_step1_rel_fp64": abs(e_fp64[0] - e_cpu) / abs(e_cpu)}
