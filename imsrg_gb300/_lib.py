@@ -44,6 +44,8 @@ SIGNATURES = {
     "imsrg_space_channel_kets": (I, [P, I, IP, IP]),
     "imsrg_space_cc_channel": (I, [P, I, IP, IP, IP, IP, IP, IP]),
     "imsrg_space_sixj": (I, [P, I, I, I, I, I, I, DP]),
+    "imsrg_space_pandya_layout": (I, [P, I, IP, IP, LLP, LLP]),
+    "imsrg_pandya_transform": (I, [P, I, P, P]),
     "imsrg_op_create": (I, [P, I, ctypes.POINTER(P)]),
     "imsrg_op_destroy": (None, [P]),
     "imsrg_op_hermiticity": (I, [P, IP]),

@@ -367,6 +367,43 @@ class _CommutatorNamespace:
 
     Commutator = CommutatorScalarScalar
 
+    def pandya_layout(self, ms):
+        """[(rows, cols, offset)] per cross-coupled channel and the buffer length."""
+        L = _lib.lib()
+        total = ctypes.c_longlong()
+        check(L.imsrg_space_pandya_layout(ms._h, -1, None, None, None, ctypes.byref(total)))
+        out = []
+        for ch in range(ms.nch):
+            r, c, o = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+            check(L.imsrg_space_pandya_layout(ms._h, ch, ctypes.byref(r), ctypes.byref(c), ctypes.byref(o), None))
+            out.append((r.value, c.value, o.value))
+        return out, total.value
+
+    def device_pandya(self, dZ, out_ptr, orientation="normal", stream=None):
+        """Pandya transform of a device operator into a device buffer (layout:
+        pandya_layout)."""
+        if orientation not in ("normal", "transpose"):
+            raise ValueError("unknown orientation %r" % orientation)
+        check(_lib.lib().imsrg_pandya_transform(dZ._h, 1 if orientation == "transpose" else 0,
+                                                ctypes.c_void_p(out_ptr), stream))
+
+    def DoPandyaTransformation(self, Z, orientation="normal"):
+        """Commutator::DoPandyaTransformation(Z, TwoBody_CC_ph, orientation):
+        one matrix per cross-coupled channel, 2nph x ncc ("normal") or
+        ncc x 2nph times herm (n_a - n_b) ("transpose")."""
+        import torch
+        ms = Z.modelspace
+        layout, total = self.pandya_layout(ms)
+        buf = torch.empty(total, dtype=torch.float64, device="cuda")
+        with DeviceOperator.from_host(Z) as dz:
+            self.device_pandya(dz, buf.data_ptr(), orientation)
+            host = buf.cpu().numpy()
+        mats = []
+        for rows, cols, off in layout:
+            shape = (rows, cols) if orientation == "normal" else (cols, rows)
+            mats.append(host[off:off + rows * cols].reshape(shape, order="F").copy())
+        return mats
+
     def device_commutator(self, dX, dY, dZ, precision=None, stream=None):
         """[X,Y] on device-resident operators (Z overwritten)."""
         check(_lib.lib().imsrg_commutator_scalar_scalar(dX._h, dY._h, dZ._h, _precision(precision), stream))

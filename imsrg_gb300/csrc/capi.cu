@@ -619,6 +619,29 @@ int imsrg_space_sixj(const imsrg_space* sp, int jj1, int jj2, int j3, int jj4, i
   return IMSRG_OK;
 }
 
+int imsrg_space_pandya_layout(const imsrg_space* sp, int ch_cc, int* rows, int* cols, long long* offset,
+                              long long* total)
+{
+  if (!sp) return fail(IMSRG_ERR_ARG, "bad arguments");
+  const Space& s = *sp->s;
+  if (total) *total = std::max<int64_t>(1, s.xb_total);
+  if (ch_cc < 0) return IMSRG_OK;
+  if (ch_cc >= s.nch) return fail(IMSRG_ERR_ARG, "channel index out of range");
+  if (rows) *rows = 2 * s.cc_nph[ch_cc];
+  if (cols) *cols = s.cc[ch_cc].n();
+  if (offset) *offset = s.xb_off[ch_cc];
+  return IMSRG_OK;
+}
+
+int imsrg_pandya_transform(const imsrg_op* Z, int transpose, double* out, void* stream)
+{
+  if (!Z || !out) return fail(IMSRG_ERR_ARG, "bad arguments");
+  if (Z->herm != 1 && Z->herm != -1) return fail(IMSRG_ERR_UNSUPPORTED, "Z must be hermitian or anti-hermitian");
+  ProfScope ps("DoPandyaTransformation", S_(stream));
+  CUDA_TRY(launch_pandya_single(*Z->sp->s, Z->d, Z->herm, transpose ? 1 : 0, out, S_(stream)));
+  return IMSRG_OK;
+}
+
 int imsrg_op_create(imsrg_space* sp, int hermiticity, imsrg_op** out)
 {
   if (!sp || !out) return fail(IMSRG_ERR_ARG, "bad arguments");

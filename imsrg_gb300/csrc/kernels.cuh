@@ -44,6 +44,9 @@ cudaError_t launch_pandya_inv_ff(const Space& s, const double* Zb, double* Z, in
                                  cudaStream_t st);
 // shared-memory budget of one quadruple block (dynamic part)
 constexpr int kInvqBudget = 36864;
+// single-operator Pandya transform into the Xbar panel layout (xb_off)
+cudaError_t launch_pandya_single(const Space& s, const double* Z, int herm, int transpose, double* out,
+                                 cudaStream_t st);
 // Generator::Update for a single-reference space (white / atan / wegner /
 // imaginary-time functions, Epstein-Nesbet or Moller-Plesset denominators):
 // Eta is overwritten; mono is norb^2 doubles of scratch

@@ -5,6 +5,8 @@
 // Each kernel states the reference lines it reproduces.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "kernels.cuh"
 #include "prof.hpp"
 
@@ -1059,6 +1061,56 @@ __global__ void __launch_bounds__(kInvqThreads) k_pandya_inv_ff(DevSpace S, DevW
   }
 }
 
+// -------------------------------------------------- single-operator Pandya
+// Commutator::DoPandyaTransformation (src/Commutator.cc:1319-1390, 1487-1497):
+// for cross-coupled channel ch (blockIdx.y), bras are its hh then ph kets (a,b)
+// in both orders (rows ib and ib + nph), kets (c,d) all its kets, and
+//   Xbar = - sum_J (2J+1) {ja jb Jcc; jc jd J} Z^J_{ad,cb}   (|6j| < 1e-8 skipped)
+// normal: 2nph x ncc column-major, Xbar; transpose: ncc x 2nph, herm (na-nb) Xbar.
+// One thread per element, in output order, so the writes coalesce.
+__global__ void k_pandya_single(DevSpace S, DevWork W, const double* __restrict__ Z, int herm, int transpose,
+                                double* __restrict__ out)
+{
+  int ch = blockIdx.y;
+  int ncc = S.cc_n[ch], nph = W.cc_nph[ch];
+  long long tot = 2LL * nph * ncc;
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= tot) return;
+  int row, ik;
+  if (transpose) {
+    row = (int)(e / ncc);
+    ik = (int)(e - (long long)row * ncc);
+  } else {
+    ik = (int)(e / (2 * nph));
+    row = (int)(e - (long long)ik * 2 * nph);
+  }
+  const int second = row >= nph;
+  const int kb = W.cc_ph[W.cc_ph_off[ch] + row - second * nph];
+  const int kofs = S.cc_kofs[ch];
+  const int p = S.cc_p[kofs + kb], q = S.cc_q[kofs + kb];
+  const int a = second ? q : p, b = second ? p : q;
+  const int c = S.cc_p[kofs + ik], d = S.cc_q[kofs + ik];
+  const int ja = S.j2[a], jb = S.j2[b], jc = S.j2[c], jd = S.j2[d];
+  const int Jcc = ch / 6;
+  int t1 = abs(ja - jd), t2 = abs(jc - jb);
+  const int jmin = (t1 > t2 ? t1 : t2) >> 1;
+  const int jmax = ((ja + jd) < (jc + jb) ? ja + jd : jc + jb) >> 1;
+  double nrm = 1.0;
+  if (a == d) nrm *= kSqrt2;
+  if (c == b) nrm *= kSqrt2;
+  double xbar = 0.0;
+  for (int J = jmin; J <= jmax; ++J) {
+    double w = dev_sixj_w(S, ja, jb, Jcc, jc, jd, J);
+    if (w == 0.0) continue;
+    xbar -= w * (nrm * dev_tbme_J_norm(S, Z, J, a, d, c, b));
+  }
+  double* o = out + W.xb_off[ch];
+  if (transpose)
+    o[e] = herm * xbar * (S.occ[a] - S.occ[b]);
+  else
+    o[e] = xbar;
+}
+
 // ------------------------------------------------------------------ generator
 // Generator::Update -> ConstructGenerator_SingleRef (src/Generator.cc:32-76,
 // 236-297) for a single-reference space, whose core is the set of occupied
@@ -1318,6 +1370,20 @@ cudaError_t launch_pandya_inv_ff(const Space& s, const double* Zb, double* Z, in
   if (e != cudaSuccess) return e;
   k_pandya_inv_ff<<<ntasks, kInvqThreads, smem, st>>>(s.dev, s.work, Zb, Z, hZ, (const int4*)tasks, clist, coff,
                                                         csort);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pandya_single(const Space& s, const double* Z, int herm, int transpose, double* out,
+                                 cudaStream_t st)
+{
+  cudaError_t e = cudaMemsetAsync(out, 0, std::max<int64_t>(1, s.xb_total) * sizeof(double), st);
+  if (e != cudaSuccess) return e;
+  long long most = 0;
+  for (int c = 0; c < s.nch; ++c) most = std::max(most, 2LL * s.cc_nph[c] * s.cc[c].n());
+  if (most == 0) return cudaSuccess;
+  dim3 grid((unsigned)((most + 255) / 256), (unsigned)s.nch);
+  k_pandya_single<<<grid, 256, 0, st>>>(s.dev, s.work, Z, herm, transpose, out);
   count_launch();
   return cudaGetLastError();
 }

@@ -107,6 +107,13 @@ int imsrg_space_cc_channel(const imsrg_space* s, int ch, int* J, int* parity, in
  * the half-integers, as there). */
 int imsrg_space_sixj(const imsrg_space* s, int jj1, int jj2, int j3, int jj4, int jj5, int j6, double* out);
 
+/* Layout of a Pandya-transform buffer (imsrg_pandya_transform): total
+ * length in doubles, and for cross-coupled channel ch_cc (ch_cc < 0: total
+ * only) its matrix's rows = 2 nph (hh then ph kets of the channel, in both
+ * orders) and cols = the channel's kets, starting at offset. */
+int imsrg_space_pandya_layout(const imsrg_space* s, int ch_cc, int* rows, int* cols, long long* offset,
+                              long long* total);
+
 /* -------------------------------------------------------------- operators */
 
 /* Device-resident scalar operator (J=0, parity +, Tz=0, particle rank 2),
@@ -178,6 +185,17 @@ int imsrg_comm222_pp_hhss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int
 int imsrg_comm222_pp_hh_221ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream);
 /* Commutator::comm222_phss, src/Commutator.cc:1681-1823 */
 int imsrg_comm222_phss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream);
+
+/* Commutator::DoPandyaTransformation(Z, TwoBody_CC_ph, orientation),
+ * src/Commutator.cc:1319-1390,1487-1497: the Pandya (particle-hole) transform
+ * of one operator in every cross-coupled channel,
+ *   Zbar(ab, cd) = - sum_J (2J+1) {ja jb Jcc; jc jd J} Z^J_{ad,cb}
+ * (|6j| < 1e-8 skipped).  transpose = 0: the "normal" orientation, rows x
+ * cols column-major (imsrg_space_pandya_layout); transpose = 1: "transpose",
+ * cols x rows column-major, times herm (n_a - n_b).  out is a device buffer of
+ * the layout's total length (zeroed first).  Not on the commutator's own path
+ * (comm222_phss transforms X and Y together, in its own layout). */
+int imsrg_pandya_transform(const imsrg_op* Z, int transpose, double* out, void* stream);
 
 /* Commutator::CommutatorScalarScalar, src/Commutator.cc:280-428 (IMSRG(2)
  * terms): Z is overwritten with [X,Y] and its hermiticity set from X and Y;

@@ -787,6 +787,47 @@ int oracle_bch_transform(const ospace* s, const double* OpIn, int hIn, const dou
   return iters;
 }
 
+/* Commutator::DoPandyaTransformation_SingleChannel, src/Commutator.cc:1319-1390:
+ * the Pandya transform of one operator in cross-coupled channel chcc.
+ * Bras are the channel's hh then ph kets (a,b) in both orders (rows ibra and
+ * ibra + nph), kets (c,d) all of the channel's kets;
+ *   Xbar = - sum_J (2J+1) {ja jb Jcc; jc jd J} Z^J_{ad,cb}     (|6j| < 1e-8 skipped)
+ * normal orientation: out is 2nph x ncc column-major, out(bra, ket) = Xbar;
+ * transpose: out is ncc x 2nph, out(ket, bra) = herm (na - nb) Xbar.
+ * Returns nph. */
+int oracle_pandya_channel(const ospace* s, const double* Z, int herm, int chcc, int transpose, double* out)
+{
+  const ochan* K = &s->cc[chcc];
+  int ncc = K->n, nph = K->nhh + K->nph;
+  int Jcc = chcc / 6;
+  for (int ib = 0; ib < nph; ++ib) {
+    int kb = ib < K->nhh ? K->hh[ib] : K->ph[ib - K->nhh];
+    int pq[2] = {K->p[kb], K->q[kb]};
+    for (int ab_case = 0; ab_case <= 1; ++ab_case) {
+      int a = pq[ab_case], b = pq[1 - ab_case];
+      int row = ib + ab_case * nph;
+      double nanb = s->occ[a] - s->occ[b];
+      for (int ik = 0; ik < ncc; ++ik) {
+        int c = K->p[ik], d = K->q[ik];
+        int ja2 = s->j2[a], jb2 = s->j2[b], jc2 = s->j2[c], jd2 = s->j2[d];
+        int jmin = abs(ja2 - jd2) > abs(jc2 - jb2) ? abs(ja2 - jd2) / 2 : abs(jc2 - jb2) / 2;
+        int jmax = (ja2 + jd2) < (jc2 + jb2) ? (ja2 + jd2) / 2 : (jc2 + jb2) / 2;
+        double xbar = 0;
+        for (int J = jmin; J <= jmax; ++J) {
+          double sixj = sixj_cached(s, ja2, jb2, Jcc, jc2, jd2, J);
+          if (fabs(sixj) < 1e-8) continue;
+          xbar -= (2 * J + 1) * sixj * tbme_J(s, Z, J, a, d, c, b);
+        }
+        if (transpose)
+          out[(size_t)row * ncc + ik] = herm * xbar * nanb;
+        else
+          out[(size_t)ik * 2 * nph + row] = xbar;
+      }
+    }
+  }
+  return nph;
+}
+
 /* BCH::BCH_Product, src/BCH.cc:267-350: Z with e^Z = e^X e^Y,
  *   Z = X + Y + 1/2 [X,Y] + 1/12 ([X,[X,Y]] + [Y,[Y,X]]) - 1/720 [Y,[Y,[Y,[Y,X]]]] + ...
  * with the Bernoulli coefficients of src/BCH.cc:273-274, the [X,[X,Y]] term

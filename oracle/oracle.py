@@ -73,6 +73,8 @@ def _load():
             L.oracle_norm.argtypes = [P, D]
             L.oracle_bch_transform.restype = ctypes.c_int
             L.oracle_bch_transform.argtypes = [P, D, ctypes.c_int, D, ctypes.c_int, D, ctypes.c_double]
+            L.oracle_pandya_channel.restype = ctypes.c_int
+            L.oracle_pandya_channel.argtypes = [P, D, ctypes.c_int, ctypes.c_int, ctypes.c_int, D]
             L.oracle_bch_product.restype = ctypes.c_int
             L.oracle_bch_product.argtypes = [P, D, ctypes.c_int, D, ctypes.c_int, D, ctypes.c_double]
             L.oracle_generator.argtypes = [P, D, D, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
@@ -222,6 +224,19 @@ class Oracle:
         out = self.zeros()
         it = self.lib.oracle_bch_transform(self.s, _dptr(H), hH, _dptr(Omega), hOm, _dptr(out), threshold)
         return out, it
+
+    def pandya(self, Z, herm, transpose=False):
+        """Commutator::DoPandyaTransformation(Z, mats, "normal" / "transpose"):
+        one matrix per cross-coupled channel (2nph x ncc, or ncc x 2nph)."""
+        out = []
+        for ch, cc in enumerate(self.ms.cc_channels):
+            ncc = len(cc[3])
+            nph = sum(1 for (p, q) in cc[3] if self.ms.ket_class(p, q) in ("hh", "ph"))
+            buf = np.zeros(max(1, 2 * nph * ncc))
+            self.lib.oracle_pandya_channel(self.s, _dptr(Z), herm, ch, 1 if transpose else 0, _dptr(buf))
+            shape = (ncc, 2 * nph) if transpose else (2 * nph, ncc)
+            out.append(buf[:2 * nph * ncc].reshape(shape, order="F"))
+        return out
 
     def bch_product(self, X, hX, Y, hY, threshold=1e-4):
         """BCH::BCH_Product(X, Y); returns (Z, commutators evaluated)."""

@@ -22,6 +22,11 @@
 //   xw = [X,W] (Z anti-hermitian), and
 //     bch.bin                         BCH::BCH_Transform(X, 0.25*Y/|Y|)
 //     norms.txt                       Operator::Norm of the inputs
+//     pandya_{X,Y}_{normal,transpose}.bin
+//                                     Commutator::DoPandyaTransformation of X
+//                                     and Y: each cross-coupled channel's
+//                                     matrix, column-major, in channel order
+//     pandya_dims.txt                 "ch rows cols" of the normal orientation
 //
 // usage: ref_harness flow <emax> <H.bin> <A.bin> <B.bin> <nsteps> <outdir>
 //   H hermitian (a flow Hamiltonian), A and B anti-hermitian.  Writes
@@ -46,6 +51,7 @@
 #include "IMSRGSolver.hh"
 
 #include <cstdio>
+#include <deque>
 #include <cstdlib>
 #include <fstream>
 #include <iomanip>
@@ -291,5 +297,25 @@ int main(int argc, char** argv) {
   Operator Omega = Y * (0.25 / Y.Norm());
   Operator Hs = BCH::BCH_Transform(X, Omega);
   write_file(outdir + "/bch.bin", store(Hs, L));
+
+  // single-operator Pandya transform of X and Y, both orientations: every
+  // cross-coupled channel's matrix, column-major, concatenated in channel order
+  {
+    std::ofstream dims(outdir + "/pandya_dims.txt");
+    struct PCase { const char* name; const Operator* op; const char* orient; };
+    const PCase pcs[] = {{"X_normal", &X, "normal"}, {"X_transpose", &X, "transpose"},
+                         {"Y_normal", &Y, "normal"}, {"Y_transpose", &Y, "transpose"}};
+    for (const PCase& pc : pcs) {
+      std::deque<arma::mat> mats(ms.GetNumberTwoBodyChannels());
+      Commutator::DoPandyaTransformation(*pc.op, mats, pc.orient);
+      std::vector<double> flat;
+      for (size_t ch = 0; ch < mats.size(); ++ch) {
+        const arma::mat& M = mats[ch];
+        if (pc.op == &X && std::string(pc.orient) == "normal") dims << ch << " " << M.n_rows << " " << M.n_cols << "\n";
+        flat.insert(flat.end(), M.memptr(), M.memptr() + M.n_elem);
+      }
+      write_file(outdir + "/pandya_" + pc.name + ".bin", flat);
+    }
+  }
   return 0;
 }

@@ -13,7 +13,10 @@ Fixtures (arena layout: see oracle/modelspace_ref.py):
                      cases xy=[X,Y], yx=[Y,X], xw=[X,W]: every IMSRG(2) term on a
                      zeroed Z and the full CommutatorScalarScalar; the
                      BCH_Transform of X with Omega = 0.25 Y/|Y|; the reference's
-                     channel tables; Operator::Norm of the inputs.
+                     channel tables; Operator::Norm of the inputs; the
+                     single-operator Pandya transform of X and Y in both
+                     orientations (every cross-coupled channel, concatenated,
+                     with the normal orientation's dimensions).
   golden_emax3.npz   the same for the case xy only, plus bch.
   golden_flow_emax2.npz, golden_flow_emax3.npz
                      H (flow Hamiltonian, RefModelSpace.flow_hamiltonian with
@@ -67,6 +70,9 @@ def run_reference(emax, cases):
             for t in TERMS:
                 out["%s_%s" % (cs, t)] = np.fromfile(os.path.join(td, "%s_%s.bin" % (cs, t)))
         out["bch"] = np.fromfile(os.path.join(td, "bch.bin"))
+        for k in ("X_normal", "X_transpose", "Y_normal", "Y_transpose"):
+            out["pandya_" + k] = np.fromfile(os.path.join(td, "pandya_%s.bin" % k))
+        out["pandya_dims"] = np.loadtxt(os.path.join(td, "pandya_dims.txt"), dtype=np.int64).reshape(-1, 3)
         with open(os.path.join(td, "tables.txt")) as f:
             out["tables"] = np.array(f.read())
         with open(os.path.join(td, "norms.txt")) as f:
@@ -167,7 +173,10 @@ def main():
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] == ["--flow"]:
+    if sys.argv[1:] == ["--commutator"]:
+        np.savez_compressed(os.path.join(HERE, "golden_emax2.npz"), **run_reference(2, ["xy", "yx", "xw"]))
+        np.savez_compressed(os.path.join(HERE, "golden_emax3.npz"), **run_reference(3, ["xy"]))
+    elif sys.argv[1:] == ["--flow"]:
         for e in (2, 3):
             np.savez_compressed(os.path.join(HERE, "golden_flow_emax%d.npz" % e), **run_reference_flow(e))
     else:

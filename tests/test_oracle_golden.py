@@ -68,3 +68,24 @@ def test_planted_mistake_is_caught():
     blk[2, 1] *= -1
     Z = o.commutator(X, g["Y"], 1, -1)
     assert max(rel_errors(ms, Z, g["xy_full"])) > 1e-6
+
+
+@pytest.mark.parametrize("emax", [2, 3])
+def test_oracle_pandya_matches_reference(emax):
+    # Commutator::DoPandyaTransformation, both orientations, X hermitian and Y
+    # anti-hermitian; the fixture holds every channel's matrix in channel order
+    g = load_golden(emax)
+    o = Oracle(emax)
+    dims = g["pandya_dims"]
+    for name, h in (("X", 1), ("Y", -1)):
+        for orient in ("normal", "transpose"):
+            mats = o.pandya(g[name], h, transpose=orient == "transpose")
+            ref = g["pandya_%s_%s" % (name, orient)]
+            pos = 0
+            for ch, rows, cols in dims:
+                shape = (rows, cols) if orient == "normal" else (cols, rows)
+                R = ref[pos:pos + rows * cols].reshape(shape, order="F")
+                pos += rows * cols
+                assert mats[ch].shape == R.shape, (name, orient, ch)
+                assert np.abs(mats[ch] - R).max(initial=0.0) <= 1e-14, (name, orient, ch)
+            assert pos == ref.size
