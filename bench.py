@@ -27,6 +27,11 @@ the GPU host), on all host threads; rank 0 only.
 Multi-GPU: replicas only (each rank runs its own commutators; no collective
 on the data path).
 
+--workload batch: 64 independent (X, Y) pairs, emax drawn uniformly from
+{2,...,6} by seed, each pair in its own model space; value = commutators/s of
+the pairs replayed as one CUDA graph (imsrg_batch_*, split form), beside the
+same pairs as 64 sequential single-pair calls, and both in FP64.
+
 --workload flow: the synthetic Magnus flow instead (IMSRGSolver,
 magnus_euler, White generator, fixed ds = 0.5, no Omega split) at emax=12 by
 default: H has one-body diagonal 2n+l+3/2, off-diagonal uniform[-0.1,0.1]
@@ -61,7 +66,8 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--emax", type=int, default=None, help="default 10 (commutator), 12 (flow)")
-    p.add_argument("--workload", default="commutator", choices=["commutator", "flow"])
+    p.add_argument("--workload", default="commutator", choices=["commutator", "flow", "batch"])
+    p.add_argument("--pairs", type=int, default=64, help="batch workload: independent (X, Y) pairs")
     p.add_argument("--fp64-steps", type=int, default=None, help="flow steps timed in the FP64 form")
     p.add_argument("--precision", default="split", choices=["split", "fp64"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
@@ -668,10 +674,87 @@ print(json.dumps({"t": t, "steps": st["steps"], "e0": list(st["e0_hist"]), "thre
     print(json.dumps(out))
 
 
+BATCH_METRIC = "[X,Y] commutators/sec, {n} independent pairs with emax drawn from {{2..6}}, one CUDA graph"
+
+
+def run_batch(args):
+    import numpy as np
+    import torch
+
+    import imsrg_gb300 as ig
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    L = ig.lib()
+    rng = np.random.Generator(np.random.PCG64(4 + rank))
+    es = [int(e) for e in rng.choice([2, 3, 4, 5, 6], size=args.pairs)]
+    pairs = []
+    arena_bytes = 0
+    for i, e in enumerate(es):
+        ms = ig.ModelSpace(e, "O16", "O16")
+        dX, dY, dZ = ig.DeviceOperator(ms, 1), ig.DeviceOperator(ms, -1), ig.DeviceOperator(ms, 1)
+        dX.fill_random(1000 + 2 * i)
+        dY.fill_random(1001 + 2 * i)
+        pairs.append((dX, dY, dZ))
+        arena_bytes += 3 * 8 * ms.arena_size
+    K, W = args.steps, max(3, args.warmup)
+
+    def timed(fn):
+        for _ in range(W):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(K):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / K
+
+    res = {}
+    for prec in ("split", "fp64"):
+        def sequential(p=prec):
+            for dX, dY, dZ in pairs:
+                ig.Commutator.device_commutator(dX, dY, dZ, p)
+        seq_ms = timed(sequential)
+        b = ig.CommutatorBatch(pairs, prec)
+        n, groups, nodes = b.info()
+        l0 = L.imsrg_kernel_launches()
+        bat_ms = timed(b.launch)
+        b.sync()
+        launches = (L.imsrg_kernel_launches() - l0) // (K + W)
+        res[prec] = {"batched_ms": bat_ms, "sequential_ms": seq_ms,
+                     "batched": args.pairs * 1000.0 / bat_ms, "sequential": args.pairs * 1000.0 / seq_ms,
+                     "speedup": seq_ms / bat_ms, "graph_branches": groups, "kernel_nodes": nodes,
+                     "launches_per_step": int(launches)}
+        b.close()
+    if rank != 0:
+        return
+    sp = res["split"]
+    out = {
+        "metric": BATCH_METRIC.format(n=args.pairs), "value": sp["batched"], "unit": "commutators/s",
+        "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": sp["batched_ms"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "%d pairs, X hermitian / Y anti-hermitian, emax per pair %s (seeded), one model "
+                               "space per pair" % (args.pairs, "".join(str(e) for e in es)),
+                   "emax_counts": {str(e): es.count(e) for e in sorted(set(es))},
+                   "operator_bytes": arena_bytes, "precision": "split"},
+        "split": sp, "plain_fp64": res["fp64"], "gpu_launches": sp["launches_per_step"] * K,
+    }
+    print(json.dumps(out))
+
+
 def main():
     args = parse_args()
     if args.emax is None:
         args.emax = 12 if args.workload == "flow" else 10
+    if args.workload == "batch":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the batch workload compares the GPU's batched "
+                              "and one-by-one launches; the CPU reference arm is the emax=10 commutator"}))
+            return
+        run_batch(args)
+        return
     if args.workload == "flow":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the CPU flow at emax=12 takes hours; the flow "

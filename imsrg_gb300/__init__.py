@@ -7,8 +7,8 @@ interface (ModelSpace, Operator, Commutator, BCH, Generator, IMSRGSolver).
 """
 
 from ._lib import IMSRGError, PREC_FP64, PREC_SPLIT, lib, library_path  # noqa: F401
-from .api import (BCH, Commutator, DeviceOperator, Generator, IMSRGSolver, ModelSpace, Operator,  # noqa: F401
-                  parse_reference)
+from .api import (BCH, Commutator, CommutatorBatch, DeviceOperator, Generator, IMSRGSolver,  # noqa: F401
+                  ModelSpace, Operator, parse_reference)
 
-__all__ = ["BCH", "Commutator", "DeviceOperator", "Generator", "IMSRGSolver", "ModelSpace", "Operator",
+__all__ = ["BCH", "Commutator", "CommutatorBatch", "DeviceOperator", "Generator", "IMSRGSolver", "ModelSpace", "Operator",
            "IMSRGError", "PREC_FP64", "PREC_SPLIT", "lib", "library_path", "parse_reference"]

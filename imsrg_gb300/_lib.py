@@ -72,6 +72,11 @@ SIGNATURES = {
     "imsrg_commutator_scalar_scalar": (I, [P, P, P, I, P]),
     "imsrg_set_term": (I, [ctypes.c_char_p, I]),
     "imsrg_get_term": (I, [ctypes.c_char_p, IP]),
+    "imsrg_batch_create": (I, [I, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P), I, ctypes.POINTER(P)]),
+    "imsrg_batch_destroy": (None, [P]),
+    "imsrg_batch_launch": (I, [P, P]),
+    "imsrg_batch_sync": (I, [P, P]),
+    "imsrg_batch_info": (I, [P, IP, IP, LLP]),
     "imsrg_set_default_precision": (I, [I]),
     "imsrg_get_default_precision": (I, [IP]),
     "imsrg_bch_transform": (I, [P, P, P, D, I, IP, P]),

@@ -416,6 +416,44 @@ class _CommutatorNamespace:
             check(fn(dX._h, dY._h, dZ._h, stream))
 
 
+class CommutatorBatch:
+    """Many independent commutators Z_i = [X_i, Y_i] (device operators of any
+    mix of model spaces) captured once into a CUDA graph and replayed by
+    launch(); pairs of different spaces run concurrently.  The operators must
+    stay alive and in place while the batch exists (the batch keeps references)."""
+
+    def __init__(self, pairs, precision=None):
+        self._L = _lib.lib()
+        self.pairs = list(pairs)
+        n = len(self.pairs)
+        arr = [(ctypes.c_void_p * n)(*[p[k]._h.value for p in self.pairs]) for k in range(3)]
+        self._h = ctypes.c_void_p()
+        check(self._L.imsrg_batch_create(n, arr[0], arr[1], arr[2], _precision(precision), ctypes.byref(self._h)))
+
+    def launch(self, stream=None):
+        check(self._L.imsrg_batch_launch(self._h, stream))
+
+    def sync(self, stream=None):
+        check(self._L.imsrg_batch_sync(self._h, stream))
+
+    def info(self):
+        """(pairs, graph branches, kernel nodes per replay)"""
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+        check(self._L.imsrg_batch_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.imsrg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _make_term(name):
     def f(self, X, Y, Z, precision=None):
         self._run_term(name, X, Y, Z, precision)

@@ -1322,9 +1322,19 @@ cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, dou
   return cudaGetLastError();
 }
 
+// grid of a grid-stride elementwise kernel over n elements: at most cap blocks
+// (a few waves at emax >= 8), fewer for small arenas, so that small operators
+// do not fill the GPU with idle blocks (commutators of different spaces run
+// side by side in a batch)
+static unsigned stride_grid(long long n, unsigned cap)
+{
+  long long b = (n + 255) / 256;
+  return (unsigned)std::max(1LL, std::min<long long>(b, cap));
+}
+
 cudaError_t launch_to_ff(const Space& s, const double* A, float2* Af, cudaStream_t st)
 {
-  k_to_ff<<<2432, 256, 0, st>>>(A, Af, s.arena);
+  k_to_ff<<<stride_grid(s.arena, 2432), 256, 0, st>>>(A, Af, s.arena);
   count_launch();
   return cudaGetLastError();
 }
@@ -1408,14 +1418,14 @@ cudaError_t launch_generator(const Space& s, const double* H, double* Eta, doubl
 
 cudaError_t launch_axpy(double* y, const double* x, double a, long long n, cudaStream_t st)
 {
-  k_axpy<<<1216, 256, 0, st>>>(y, x, a, n);
+  k_axpy<<<stride_grid(n, 1216), 256, 0, st>>>(y, x, a, n);
   count_launch();
   return cudaGetLastError();
 }
 
 cudaError_t launch_scale(double* y, double a, long long n, cudaStream_t st)
 {
-  k_scale<<<1216, 256, 0, st>>>(y, a, n);
+  k_scale<<<stride_grid(n, 1216), 256, 0, st>>>(y, a, n);
   count_launch();
   return cudaGetLastError();
 }

@@ -61,6 +61,7 @@ extern "C" {
 typedef struct imsrg_space imsrg_space;
 typedef struct imsrg_op imsrg_op;
 typedef struct imsrg_solver imsrg_solver;
+typedef struct imsrg_batch imsrg_batch;
 
 /* Last error message of the calling thread ("" if none). */
 const char* imsrg_last_error(void);
@@ -207,6 +208,26 @@ int imsrg_commutator_scalar_scalar(const imsrg_op* X, const imsrg_op* Y, imsrg_o
  * "comm122ss", "comm221ss", "comm222_pp_hhss", "comm222_phss". Process-wide. */
 int imsrg_set_term(const char* name, int on);
 int imsrg_get_term(const char* name, int* on);
+
+/* Batched commutators: n independent Z[i] = [X[i], Y[i]] (each as
+ * imsrg_commutator_scalar_scalar), of any mix of model spaces and sizes,
+ * recorded once into a CUDA graph and replayed by imsrg_batch_launch.  Pairs
+ * that share a model space run one after the other (they share its scratch);
+ * pairs of different spaces run concurrently, one graph branch per space.
+ * Creating a batch evaluates every pair once (allocating all scratch) and
+ * captures the graph; the operators, their spaces and the term switches are
+ * fixed from then on, and every operator must outlive the batch.  No Z may
+ * appear twice.  No reference counterpart (the reference evaluates
+ * commutators one at a time). */
+int imsrg_batch_create(int n, const imsrg_op* const* X, const imsrg_op* const* Y, imsrg_op* const* Z, int precision,
+                       imsrg_batch** out);
+void imsrg_batch_destroy(imsrg_batch* batch);
+/* Enqueue one replay of the whole batch on stream (asynchronous). */
+int imsrg_batch_launch(imsrg_batch* batch, void* stream);
+/* Synchronise stream and, in split precision, check the kernels' status words. */
+int imsrg_batch_sync(imsrg_batch* batch, void* stream);
+/* Pairs, graph branches (distinct model spaces) and kernel nodes per replay. */
+int imsrg_batch_info(const imsrg_batch* batch, int* n_pairs, int* n_groups, long long* kernel_nodes);
 
 /* Default precision used by the reference-signature shim (process-wide). */
 int imsrg_set_default_precision(int precision);
