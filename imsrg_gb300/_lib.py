@@ -18,6 +18,7 @@ ERR_UNSUPPORTED = 3
 ERR_NOMEM = 4
 ERR_KERNEL = 5
 ERR_DIVERGED = 6
+ERR_IO = 7
 PREC_FP64 = 0
 PREC_SPLIT = 1
 
@@ -58,6 +59,8 @@ SIGNATURES = {
     "imsrg_op_scale": (I, [P, D, P]),
     "imsrg_op_axpy": (I, [P, D, P, P]),
     "imsrg_op_norm": (I, [P, DP, P]),
+    "imsrg_op_write_binary": (I, [P, ctypes.c_char_p, P]),
+    "imsrg_op_read_binary": (I, [P, ctypes.c_char_p, P]),
     "imsrg_op_fill_random": (I, [P, ctypes.c_ulonglong, P]),
     "imsrg_comm110ss": (I, [P, P, P, P]),
     "imsrg_comm220ss": (I, [P, P, P, P]),
@@ -87,6 +90,7 @@ SIGNATURES = {
     "imsrg_solver_set": (I, [P, ctypes.c_char_p, D]),
     "imsrg_solver_get": (I, [P, ctypes.c_char_p, DP]),
     "imsrg_solver_set_generator": (I, [P, ctypes.c_char_p, P]),
+    "imsrg_solver_set_scratch_dir": (I, [P, ctypes.c_char_p]),
     "imsrg_solver_set_denominator_partitioning": (I, [P, ctypes.c_char_p]),
     "imsrg_solver_solve": (I, [P, I, P]),
     "imsrg_solver_hs": (I, [P, ctypes.POINTER(P)]),

@@ -20,6 +20,7 @@ DeviceOperator keeps an operator resident in HBM for chained device work
 """
 
 import ctypes
+import os
 import re
 
 import numpy as np
@@ -188,6 +189,18 @@ class Operator:
         with DeviceOperator.from_host(self) as d:
             return d.norm()
 
+    def WriteBinary(self, path):
+        """Operator::WriteBinary to a file path."""
+        with DeviceOperator.from_host(self) as d:
+            d.write_binary(path)
+
+    def ReadBinary(self, path):
+        """Operator::ReadBinary from a file path (hermiticity from the file)."""
+        with DeviceOperator(self.modelspace, self.hermitian) as d:
+            d.read_binary(path)
+            d.download(self.arena)
+            self.hermitian = d.hermiticity
+
     def __iadd__(self, other):
         self.arena += other.arena
         return self
@@ -310,6 +323,14 @@ class DeviceOperator:
 
     def fill_random(self, seed, stream=None):
         check(self._L.imsrg_op_fill_random(self._h, int(seed), stream))
+
+    def write_binary(self, path, stream=None):
+        """Operator::WriteBinary layout (files interchange with IMSRG++)."""
+        check(self._L.imsrg_op_write_binary(self._h, os.fsencode(path), stream))
+
+    def read_binary(self, path, stream=None):
+        """Operator::ReadBinary; hermiticity taken from the file."""
+        check(self._L.imsrg_op_read_binary(self._h, os.fsencode(path), stream))
 
 
 def _precision(p):
@@ -639,6 +660,12 @@ class IMSRGSolver:
 
     def SetDenominatorDeltaIndex(self, i):
         self._set("denominator_delta_index", i)
+
+    def SetScratchDir(self, d):
+        check(self._L.imsrg_solver_set_scratch_dir(self._h, os.fsencode(d)))
+
+    def GetNOmegaWritten(self):
+        return int(self._get("n_omega_written"))
 
     def SetGenerator(self, g, stream=None):
         check(self._L.imsrg_solver_set_generator(self._h, g.encode(), stream))

@@ -7,8 +7,11 @@
 // truncation, step size, Omega splitting) depends on an operator norm.
 #include <cuda_runtime.h>
 
+#include <unistd.h>
+
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <limits>
 #include <string>
@@ -165,6 +168,11 @@ struct imsrg_solver {
     double s, e0, norm_eta, norm_omega;
   };
   std::vector<Record> history;
+  // IMSRGSolver::SetScratchDir: split Omegas go to files instead of device
+  // memory (src/IMSRGSolver.cc:44-83); max_omega_written as there
+  std::string scratch;
+  int n_written = 0, max_omega_written = 500;
+  std::vector<std::string> files;
 
   ~imsrg_solver()
   {
@@ -172,6 +180,7 @@ struct imsrg_solver {
     imsrg_op_destroy(Eta);
     imsrg_op_destroy(Hsaved);
     for (imsrg_op* o : omega) imsrg_op_destroy(o);
+    for (const std::string& f : files) std::remove(f.c_str());  // CleanupScratch
   }
 };
 
@@ -186,12 +195,27 @@ int new_zero_omega(imsrg_solver* sv, cudaStream_t st)
   return IMSRG_OK;
 }
 
-// IMSRGSolver::NewOmega, src/IMSRGSolver.cc:44-83 (no scratch files)
+// IMSRGSolver::NewOmega, src/IMSRGSolver.cc:44-83: with a scratch directory
+// the finished Omega goes to a file (the reference's OMEGA_<pid><n> naming
+// and binary layout) and its device operator is reused; without one a new
+// device operator is kept
 int new_omega(imsrg_solver* sv, cudaStream_t st)
 {
   if (!sv->Hsaved) FLOW_TRY(imsrg_op_create(sv->sp, 1, &sv->Hsaved));
   FLOW_TRY(imsrg_op_copy(sv->Hsaved, sv->Hs, st));
-  return new_zero_omega(sv, st);
+  if (sv->scratch.empty()) return new_zero_omega(sv, st);
+  if (sv->scratch.find("/dev/null") == std::string::npos) {
+    char name[64];
+    std::snprintf(name, sizeof(name), "/OMEGA_%06d%03d", (int)getpid(), sv->n_written);
+    std::string path = sv->scratch + name;
+    FLOW_TRY(imsrg_op_write_binary(sv->omega.back(), path.c_str(), st));
+    sv->files.push_back(path);
+    if (sv->n_written > sv->max_omega_written)
+      return err(IMSRG_ERR_ARG, "more Omegas written than max_omega_written");
+  }
+  ++sv->n_written;
+  FLOW_CUDA(cudaMemsetAsync(sv->omega.back()->d, 0, sv->sp->s->arena * sizeof(double), st));
+  return IMSRG_OK;
 }
 
 // IMSRGSolver::GatherOmega, src/IMSRGSolver.cc:99-120
@@ -251,7 +275,7 @@ int solve_magnus_euler(imsrg_solver* sv, int prec, cudaStream_t st)
     FLOW_TRY(imsrg_op_scale(sv->Eta, sv->ds, st));
     FLOW_TRY(bch_product_impl(sv->Eta, sv->omega.back(), sv->omega.back(), sv->bch_product_threshold, prec, nullptr,
                               st));
-    const imsrg_op* Hin = sv->omega.size() < 2 ? sv->H0 : sv->Hsaved;
+    const imsrg_op* Hin = sv->omega.size() + sv->n_written < 2 ? sv->H0 : sv->Hsaved;
     FLOW_TRY(imsrg_bch_transform(Hin, sv->omega.back(), sv->Hs, sv->bch_transform_threshold, prec, nullptr, st));
     FLOW_TRY(generator_impl(sv->Hs, sv->Eta, sv->gen, st));
     Elast = zero_body(sv->Hs, st, &rc);
@@ -332,7 +356,15 @@ int imsrg_solver_set(imsrg_solver* sv, const char* name, double v)
   else if (n == "denominator_delta_index") sv->gen.delta_index = (int)v;
   else if (n == "bch_transform_threshold") sv->bch_transform_threshold = v;
   else if (n == "bch_product_threshold") sv->bch_product_threshold = v;
+  else if (n == "max_omega_written") sv->max_omega_written = (int)v;
   else return err(IMSRG_ERR_ARG, "unknown solver setting " + n);
+  return IMSRG_OK;
+}
+
+int imsrg_solver_set_scratch_dir(imsrg_solver* sv, const char* dir)
+{
+  if (!sv || !dir) return err(IMSRG_ERR_ARG, "bad arguments");
+  sv->scratch = dir;
   return IMSRG_OK;
 }
 
@@ -356,6 +388,8 @@ int imsrg_solver_get(const imsrg_solver* sv, const char* name, double* v)
   else if (n == "bch_product_threshold") *v = sv->bch_product_threshold;
   else if (n == "n_omega") *v = (double)sv->omega.size();
   else if (n == "istep") *v = sv->istep;
+  else if (n == "n_omega_written") *v = sv->n_written;
+  else if (n == "max_omega_written") *v = sv->max_omega_written;
   else return err(IMSRG_ERR_ARG, "unknown solver setting " + n);
   return IMSRG_OK;
 }
@@ -443,8 +477,21 @@ int imsrg_solver_transform(const imsrg_solver* sv, const imsrg_op* OpIn, imsrg_o
   if (!sv || !OpIn || !OpOut) return err(IMSRG_ERR_ARG, "bad arguments");
   if (OpIn->sp != sv->sp || OpOut->sp != sv->sp) return err(IMSRG_ERR_ARG, "operator from another model space");
   cudaStream_t st = S_(stream);
-  // IMSRGSolver::Transform_Partial(OpIn, 0), src/IMSRGSolver.cc:957-1002
+  // IMSRGSolver::Transform_Partial(OpIn, 0), src/IMSRGSolver.cc:957-1002:
+  // the Omegas written to scratch files first, then those in device memory
   FLOW_TRY(imsrg_op_copy(OpOut, OpIn, st));
+  if (!sv->files.empty()) {
+    imsrg_op* om = nullptr;
+    FLOW_TRY(imsrg_op_create(sv->sp, -1, &om));
+    int rc = IMSRG_OK;
+    for (size_t i = 0; rc == IMSRG_OK && i < sv->files.size(); ++i) {
+      rc = imsrg_op_read_binary(om, sv->files[i].c_str(), st);
+      if (!rc) rc = imsrg_bch_transform(OpOut, om, OpOut, sv->bch_transform_threshold, precision, nullptr, st);
+    }
+    cudaStreamSynchronize(st);
+    imsrg_op_destroy(om);
+    if (rc) return rc;
+  }
   for (imsrg_op* om : sv->omega)
     FLOW_TRY(imsrg_bch_transform(OpOut, om, OpOut, sv->bch_transform_threshold, precision, nullptr, st));
   return IMSRG_OK;

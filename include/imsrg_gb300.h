@@ -42,6 +42,7 @@ extern "C" {
 #define IMSRG_ERR_NOMEM 4       /* device allocation failed */
 #define IMSRG_ERR_KERNEL 5      /* a kernel reported an error through its status word */
 #define IMSRG_ERR_DIVERGED 6    /* the IMSRG flow blew up (|eta| > 1e12 or |E0| > 1e9) */
+#define IMSRG_ERR_IO 7          /* a file could not be opened, read or written */
 
 /* precision of the dense contractions (ladder and Pandya channel GEMMs) */
 #define IMSRG_PREC_FP64 0  /* plain FP64 (CUDA-core DFMA) */
@@ -138,6 +139,18 @@ int imsrg_op_zero(imsrg_op* op, void* stream);
 int imsrg_op_copy(imsrg_op* dst, const imsrg_op* src, void* stream);
 int imsrg_op_scale(imsrg_op* op, double a, void* stream);
 int imsrg_op_axpy(imsrg_op* y, double a, const imsrg_op* x, void* stream);
+
+/* Operator::WriteBinary / ReadBinary (src/Operator.cc:341-388,
+ * src/TwoBodyME.cc:812-836): the operator in the reference's binary layout
+ * (Operator header, ZeroBody, OneBody, TwoBodyME header, every channel block
+ * column-major in channel order), so files interchange with IMSRG++.  The
+ * E2max field is written as 2 emax (the reference writes an uninitialised
+ * value there) and ignored on reading.  Reading checks the header against the
+ * space (scalar, two-body, channel count, exact length) and sets the
+ * operator's hermiticity from the file.  Both stream the arena through pinned
+ * staging buffers on stream and return when the file is complete. */
+int imsrg_op_write_binary(const imsrg_op* op, const char* path, void* stream);
+int imsrg_op_read_binary(imsrg_op* op, const char* path, void* stream);
 
 /* Operator::Norm of a scalar operator (src/Operator.cc:1610-1651,
  * src/TwoBodyME.cc:703-723); synchronises the stream. */
@@ -290,6 +303,14 @@ void imsrg_solver_destroy(imsrg_solver* solver);
  * "n_omega" (Omegas kept) and "istep" (steps of the last solve, + 1). */
 int imsrg_solver_set(imsrg_solver* solver, const char* name, double value);
 int imsrg_solver_get(const imsrg_solver* solver, const char* name, double* value);
+/* IMSRGSolver::SetScratchDir (src/IMSRGSolver.hh:90): when not empty, each
+ * Omega finished by an Omega split is written to <dir>/OMEGA_<pid><n> in the
+ * reference's binary layout (imsrg_op_write_binary) and its device memory is
+ * reused; Transform reads the files back.  A directory containing "/dev/null"
+ * counts the Omegas without writing them, as the reference does.  The files
+ * are removed when the solver is destroyed.  "" (the default) keeps every
+ * Omega in device memory.  imsrg_solver_get reads "n_omega_written". */
+int imsrg_solver_set_scratch_dir(imsrg_solver* solver, const char* dir);
 /* IMSRGSolver::SetGenerator ("white", "atan", "wegner", "imaginary-time"):
  * starts a new Omega when the current one is not empty (src/IMSRGSolver.cc:157-183). */
 int imsrg_solver_set_generator(imsrg_solver* solver, const char* type, void* stream);
@@ -310,8 +331,9 @@ int imsrg_solver_omega(imsrg_solver* solver, int i, imsrg_op** out);
 int imsrg_solver_history(const imsrg_solver* solver, int cap, int* istep, double* s, double* e0, double* norm_eta,
                          double* norm_omega, int* n);
 /* IMSRGSolver::Transform (src/IMSRGSolver.cc:928-1002): OpOut = e^Omega OpIn
- * e^-Omega through every Omega in order; InverseTransform (:939-952) undoes it.
- * OpOut may alias OpIn. */
+ * e^-Omega through every Omega in order (scratch files first); InverseTransform
+ * (:939-952) undoes the Omegas held in device memory (as the reference, it
+ * does not read scratch files).  OpOut may alias OpIn. */
 int imsrg_solver_transform(const imsrg_solver* solver, const imsrg_op* OpIn, imsrg_op* OpOut, int precision,
                            void* stream);
 int imsrg_solver_inverse_transform(const imsrg_solver* solver, const imsrg_op* OpIn, imsrg_op* OpOut, int precision,

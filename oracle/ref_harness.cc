@@ -22,6 +22,7 @@
 //   xw = [X,W] (Z anti-hermitian), and
 //     bch.bin                         BCH::BCH_Transform(X, 0.25*Y/|Y|)
 //     norms.txt                       Operator::Norm of the inputs
+//     X_op.bin, Y_op.bin              Operator::WriteBinary of X and Y
 //     pandya_{X,Y}_{normal,transpose}.bin
 //                                     Commutator::DoPandyaTransformation of X
 //                                     and Y: each cross-coupled channel's
@@ -266,6 +267,14 @@ int main(int argc, char** argv) {
   {
     std::ofstream nf(outdir + "/norms.txt");
     nf << std::setprecision(17) << X.Norm() << " " << Y.Norm() << " " << W.Norm() << "\n";
+  }
+  {
+    // Operator::WriteBinary of X and Y (the E2max field is written from an
+    // uninitialised member there, src/Operator.cc:65-75; readers skip it)
+    std::ofstream ox(outdir + "/X_op.bin", std::ios::binary);
+    X.WriteBinary(ox);
+    std::ofstream oy(outdir + "/Y_op.bin", std::ios::binary);
+    Y.WriteBinary(oy);
   }
 
   struct Term { const char* name; term_fn fn; };

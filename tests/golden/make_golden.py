@@ -16,7 +16,8 @@ Fixtures (arena layout: see oracle/modelspace_ref.py):
                      channel tables; Operator::Norm of the inputs; the
                      single-operator Pandya transform of X and Y in both
                      orientations (every cross-coupled channel, concatenated,
-                     with the normal orientation's dimensions).
+                     with the normal orientation's dimensions); the bytes
+                     Operator::WriteBinary writes for X and Y.
   golden_emax3.npz   the same for the case xy only, plus bch.
   golden_flow_emax2.npz, golden_flow_emax3.npz
                      H (flow Hamiltonian, RefModelSpace.flow_hamiltonian with
@@ -70,6 +71,8 @@ def run_reference(emax, cases):
             for t in TERMS:
                 out["%s_%s" % (cs, t)] = np.fromfile(os.path.join(td, "%s_%s.bin" % (cs, t)))
         out["bch"] = np.fromfile(os.path.join(td, "bch.bin"))
+        for k in ("X", "Y"):
+            out[k + "_binary"] = np.fromfile(os.path.join(td, k + "_op.bin"), dtype=np.uint8)
         for k in ("X_normal", "X_transpose", "Y_normal", "Y_transpose"):
             out["pandya_" + k] = np.fromfile(os.path.join(td, "pandya_%s.bin" % k))
         out["pandya_dims"] = np.loadtxt(os.path.join(td, "pandya_dims.txt"), dtype=np.int64).reshape(-1, 3)

@@ -4,7 +4,7 @@ reference compiled from its sources."""
 import numpy as np
 import pytest
 
-from helpers import CASES, TERMS, load_golden, rel_errors
+from helpers import CASES, TERMS, load_golden, ref_space, rel_errors
 from oracle import Oracle
 
 
@@ -89,3 +89,42 @@ def test_oracle_pandya_matches_reference(emax):
                 assert mats[ch].shape == R.shape, (name, orient, ch)
                 assert np.abs(mats[ch] - R).max(initial=0.0) <= 1e-14, (name, orient, ch)
             assert pos == ref.size
+
+
+def parse_reference_binary(ms, raw):
+    """Operator::WriteBinary layout (src/Operator.cc:341-363,
+    src/TwoBodyME.cc:812-823) of a scalar two-body operator -> (arena,
+    hermitian flags, header fields)."""
+    import struct
+    b = bytes(raw)
+    rank_J, rank_T, parity, prank, legs, e2max, e3max = struct.unpack_from("<7i", b, 0)
+    herm, anti = struct.unpack_from("<??", b, 28)
+    nch, = struct.unpack_from("<i", b, 30)
+    pos = 34
+    a = np.zeros(ms.arena_size)
+    a[0], = struct.unpack_from("<d", b, pos)
+    pos += 8
+    N = ms.norb
+    a[32:32 + N * N] = np.frombuffer(b, dtype="<f8", count=N * N, offset=pos)
+    pos += 8 * N * N
+    nch2, h2, a2, rj, rt, par = struct.unpack_from("<Q??3i", b, pos)
+    pos += 22
+    for ch in range(ms.nch):
+        n = len(ms.channels[ch][3])
+        a[ms.off2[ch]:ms.off2[ch] + n * n] = np.frombuffer(b, dtype="<f8", count=n * n, offset=pos)
+        pos += 8 * n * n
+    assert pos == len(b)
+    return a, (herm, anti, h2, a2), (rank_J, rank_T, parity, prank, legs, e3max, nch, nch2, rj, rt, par)
+
+
+@pytest.mark.parametrize("emax", [2, 3])
+def test_reference_binary_layout(emax):
+    # the byte layout the GPU reader and writer follow, pinned on the
+    # reference's own files
+    g = load_golden(emax)
+    ms = ref_space(emax)
+    for name, h in (("X", 1), ("Y", -1)):
+        a, flags, hdr = parse_reference_binary(ms, g[name + "_binary"])
+        assert np.array_equal(a, g[name])
+        assert flags == ((h == 1), (h == -1), (h == 1), (h == -1))
+        assert hdr == (0, 0, 0, 2, 4, min(14, 3 * emax), ms.nch, ms.nch, 0, 0, 0)
