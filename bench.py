@@ -718,14 +718,15 @@ def run_batch(args):
                 ig.Commutator.device_commutator(dX, dY, dZ, p)
         seq_ms = timed(sequential)
         b = ig.CommutatorBatch(pairs, prec)
-        n, groups, nodes = b.info()
+        n, groups, grouped, nodes = b.info()
         l0 = L.imsrg_kernel_launches()
         bat_ms = timed(b.launch)
         b.sync()
         launches = (L.imsrg_kernel_launches() - l0) // (K + W)
         res[prec] = {"batched_ms": bat_ms, "sequential_ms": seq_ms,
                      "batched": args.pairs * 1000.0 / bat_ms, "sequential": args.pairs * 1000.0 / seq_ms,
-                     "speedup": seq_ms / bat_ms, "graph_branches": groups, "kernel_nodes": nodes,
+                     "speedup": seq_ms / bat_ms, "graph_branches": groups, "grouped_product_launches": grouped,
+                     "kernel_nodes": nodes,
                      "launches_per_step": int(launches)}
         b.close()
     if rank != 0:

@@ -79,7 +79,7 @@ SIGNATURES = {
     "imsrg_batch_destroy": (None, [P]),
     "imsrg_batch_launch": (I, [P, P]),
     "imsrg_batch_sync": (I, [P, P]),
-    "imsrg_batch_info": (I, [P, IP, IP, LLP]),
+    "imsrg_batch_info": (I, [P, IP, IP, IP, LLP]),
     "imsrg_set_default_precision": (I, [I]),
     "imsrg_get_default_precision": (I, [IP]),
     "imsrg_bch_transform": (I, [P, P, P, D, I, IP, P]),

@@ -458,10 +458,11 @@ class CommutatorBatch:
         check(self._L.imsrg_batch_sync(self._h, stream))
 
     def info(self):
-        """(pairs, graph branches, kernel nodes per replay)"""
-        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
-        check(self._L.imsrg_batch_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
-        return a.value, b.value, c.value
+        """(pairs, graph branches, grouped product launches per product
+        family (0: products per pair), kernel nodes per replay)"""
+        a, b, g, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+        check(self._L.imsrg_batch_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(g), ctypes.byref(c)))
+        return a.value, b.value, g.value, c.value
 
     def close(self):
         if getattr(self, "_h", None):

@@ -960,3 +960,148 @@ int commutator_dev(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, 
 int norm_dev(const imsrg_op* op, double* out, cudaStream_t st) { return norm_impl(op, out, st); }
 int status_dev(imsrg_space* sp, cudaStream_t st) { return check_status(sp, st); }
 }  // namespace imsrg
+
+// ------------------------------------------------------------- batch phases
+// CommutatorScalarScalar in the split form cut at its two dense products, so
+// a batch can run the products of many pairs as one launch each (see
+// capi_batch.cu): pre (Z zeroed, operand preparation, the zero- and one-body
+// terms), the ladder product, mid (comm221ss, comm122ss), the Zbar product,
+// post (inverse Pandya transform).  Every term must be on.
+namespace imsrg {
+
+bool batch_phases_usable()
+{
+  std::lock_guard<std::mutex> g(g_mu);
+  for (int t = 0; t < NTERMS; ++t)
+    if (!g_term_on[t]) return false;
+  return true;
+}
+
+int batch_pre(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
+{
+  Z->herm = z_herm(X->herm, Y->herm);
+  int rc = check_ops(X, Y, Z);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemsetAsync(Z->d, 0, X->sp->s->arena * sizeof(double), st));
+  if ((rc = prep_122_df(X, Y, st)) || (rc = prep_ph(X, Y, st)) || (rc = do_111_110(X, Y, Z, true, true, st)) ||
+      (rc = do_220(X, Y, Z, st)) || (rc = do_121(X, Y, Z, st)))
+    return rc;
+  return IMSRG_OK;
+}
+
+int batch_mid(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
+{
+  int rc = do_221_1b(X, Y, Z, st, Z->d);
+  if (!rc) rc = do_122(X, Y, Z, st, IMSRG_PREC_SPLIT, true);
+  return rc;
+}
+
+int batch_post(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
+{
+  (void)Y;
+  imsrg_space* sp = X->sp;
+  Space& s = *sp->s;
+  if (sp->n_invq > 0)
+    CUDA_TRY(launch_pandya_inv_ff(s, sp->d_zb, Z->d, Z->herm, sp->d_invq, sp->n_invq, sp->d_cls_list, sp->d_cls_off,
+                                  sp->d_cls_sort, s.invq_smem, st));
+  else
+    CUDA_TRY(launch_pandya_inv(s, sp->d_zb, Z->d, Z->herm, sp->d_pinv, sp->n_pinv, st));
+  return IMSRG_OK;
+}
+
+// Products of several pairs whose spaces have the same structure (equal
+// orbit lists, hence equal channel tables and product job lists) and whose
+// operators have the same hermiticities, as one split-form launch per
+// product family.  The jobs of pair p address its own operands: every job
+// offset is moved by the distance, in doubles, from pair 0's operand to pair
+// p's (all operands are 8-byte aligned device allocations), so the kernels
+// run unchanged on pair 0's base pointers, and the digit splitting (chosen
+// from K) is the one each pair's own plan makes.
+struct GroupedProducts {
+  std::vector<const imsrg_op*> X, Y;
+  std::vector<imsrg_op*> Z;
+  SplitPlan* ladder = nullptr;
+  SplitPlan* zbar = nullptr;
+  ~GroupedProducts()
+  {
+    if (ladder) split_plan_destroy(ladder);
+    if (zbar) split_plan_destroy(zbar);
+  }
+};
+
+static long long dist(const void* a, const void* b)
+{
+  return ((long long)(intptr_t)a - (long long)(intptr_t)b) / (long long)sizeof(double);
+}
+
+GroupedProducts* grouped_products_create(const std::vector<const imsrg_op*>& X, const std::vector<const imsrg_op*>& Y,
+                                         const std::vector<imsrg_op*>& Z, std::string* why)
+{
+  if (X.empty()) return nullptr;
+  imsrg_space* s0 = X[0]->sp;
+  for (size_t p = 0; p < X.size(); ++p) {
+    imsrg_space* sp = X[p]->sp;
+    if (sp->s->norb != s0->s->norb || sp->s->arena != s0->s->arena || sp->s->emax != s0->s->emax ||
+        sp->ladder_jobs.size() != s0->ladder_jobs.size() || sp->zbar_jobs.size() != s0->zbar_jobs.size() ||
+        X[p]->herm != X[0]->herm || Y[p]->herm != Y[0]->herm || !sp->d_zb || !sp->d_xb) {
+      if (why) *why = "pairs differ in structure or hermiticity";
+      return nullptr;
+    }
+  }
+  std::vector<GemmJobDev> lj, zj;
+  for (size_t p = 0; p < X.size(); ++p) {
+    imsrg_space* sp = X[p]->sp;
+    const long long dX = dist(X[p]->d, X[0]->d), dY = dist(Y[p]->d, Y[0]->d), dZ = dist(Z[p]->d, Z[0]->d);
+    for (GemmJobDev j : sp->ladder_jobs) {
+      j.a_off += dX;
+      j.b_off += dY;  // B0 = B1 = Y
+      j.out_off += dZ;
+      lj.push_back(j);
+    }
+    const long long dA = dist(sp->d_xb, s0->d_xb), dB0 = dist(sp->d_yt, s0->d_yt), dB1 = dist(sp->d_yf, s0->d_yf),
+                    dO = dist(sp->d_zb, s0->d_zb);
+    for (GemmJobDev j : sp->zbar_jobs) {
+      j.a_off += dA;
+      j.b_off += j.bsel ? dB1 : dB0;
+      j.out_off += dO;
+      zj.push_back(j);
+    }
+  }
+  GroupedProducts* g = new GroupedProducts();
+  g->X = X;
+  g->Y = Y;
+  g->Z = Z;
+  try {
+    g->ladder = split_plan_create(*s0->s, lj, 0);
+    g->zbar = split_plan_create(*s0->s, zj, 1);
+  } catch (std::exception& e) {
+    if (why) *why = std::string("grouped product plans: ") + e.what();
+    delete g;
+    return nullptr;
+  }
+  return g;
+}
+
+void grouped_products_destroy(GroupedProducts* g) { delete g; }
+
+int grouped_ladder(GroupedProducts* g, cudaStream_t st)
+{
+  imsrg_space* s0 = g->X[0]->sp;
+  const Space& s = *s0->s;
+  split_plan_set_accumulate(g->ladder, 0);  // Z was zeroed in the pre phase
+  CUDA_TRY(launch_symgemm_split(g->ladder, g->X[0]->d, g->Y[0]->d, g->Y[0]->d, g->Z[0]->d, s.work.kidx,
+                                s.work.kweight, s.work.phase_tab, s0->d_status, g->Z[0]->herm,
+                                (double)g->Y[0]->herm, st));
+  return IMSRG_OK;
+}
+
+int grouped_zbar(GroupedProducts* g, cudaStream_t st)
+{
+  imsrg_space* s0 = g->X[0]->sp;
+  const Space& s = *s0->s;
+  CUDA_TRY(launch_symgemm_split(g->zbar, s0->d_xb, s0->d_yt, s0->d_yf, s0->d_zb, s.work.kidx, s.work.kweight,
+                                s.work.phase_tab, s0->d_status, g->Z[0]->herm, 1.0, st));
+  return IMSRG_OK;
+}
+
+}  // namespace imsrg

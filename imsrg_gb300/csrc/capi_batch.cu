@@ -1,10 +1,19 @@
 // extern "C" boundary, batched commutators (include/imsrg_gb300.h): many
 // independent CommutatorScalarScalar calls of uneven size replayed as one
-// CUDA graph.  Pairs are grouped by model space (a space's scratch buffers
-// serialise the pairs that share it); each group runs on its own stream, so the
-// graph holds one branch per space and the GPU runs the branches concurrently.
-// Capturing removes the per-kernel launch latency that dominates commutators at
-// small emax (a few microseconds of work per kernel).
+// CUDA graph.  Capturing removes the per-kernel launch latency that dominates
+// commutators at small emax (a few microseconds of work per kernel).
+//
+// Two graph shapes:
+//  - grouped (split form, every term on, one model space per pair): the
+//    commutator runs in five stages; the per-pair stages (operand preparation
+//    and small terms; comm221ss and comm122ss; the inverse Pandya transform)
+//    run as one branch per pair, and each of the two dense products runs as
+//    one persistent launch per group of same-structure pairs, so the tiles of
+//    every pair share one grid instead of each pair's product taking every SM
+//    in turn;
+//  - branches (otherwise): pairs grouped by model space (a space's scratch
+//    serialises the pairs that share it), one branch per space running whole
+//    commutators.
 #include <cuda_runtime.h>
 
 #include <map>
@@ -30,9 +39,17 @@ struct imsrg_batch {
   cudaGraphExec_t exec = nullptr;
   int prec = IMSRG_PREC_FP64;
   size_t kernel_nodes = 0;
+  // grouped shape: products per structure group, their streams and joins
+  bool grouped = false;
+  std::vector<GroupedProducts*> products;
+  std::vector<cudaStream_t> gstreams;
+  std::vector<cudaEvent_t> gjoins;
 
   ~imsrg_batch()
   {
+    for (GroupedProducts* g : products) grouped_products_destroy(g);
+    for (cudaEvent_t e : gjoins) cudaEventDestroy(e);
+    for (cudaStream_t s : gstreams) cudaStreamDestroy(s);
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     for (cudaEvent_t e : joins) cudaEventDestroy(e);
@@ -52,10 +69,84 @@ int berr(int code, const std::string& msg) { return set_error(code, msg.c_str())
     if (_e != cudaSuccess) return berr(IMSRG_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
   } while (0)
 
+// grouped shape: per-pair stages fork one branch per pair (group g of the
+// branch shape holds exactly pair g), product stages one branch per structure
+// group; every stage joins back into the capture stream
+template <class F>
+int pair_stage(imsrg_batch* b, F fn)
+{
+  BATCH_CUDA(cudaEventRecord(b->fork, b->cap));
+  for (size_t g = 0; g < b->groups.size(); ++g) {
+    cudaStream_t s = b->streams[g];
+    BATCH_CUDA(cudaStreamWaitEvent(s, b->fork, 0));
+    const int i = b->groups[g][0];
+    int rc = fn(b->X[i], b->Y[i], b->Z[i], s);
+    if (rc) return rc;
+    BATCH_CUDA(cudaEventRecord(b->joins[g], s));
+    BATCH_CUDA(cudaStreamWaitEvent(b->cap, b->joins[g], 0));
+  }
+  return IMSRG_OK;
+}
+
+template <class F>
+int product_stage(imsrg_batch* b, F fn)
+{
+  BATCH_CUDA(cudaEventRecord(b->fork, b->cap));
+  for (size_t g = 0; g < b->products.size(); ++g) {
+    cudaStream_t s = b->gstreams[g];
+    BATCH_CUDA(cudaStreamWaitEvent(s, b->fork, 0));
+    int rc = fn(b->products[g], s);
+    if (rc) return rc;
+    BATCH_CUDA(cudaEventRecord(b->gjoins[g], s));
+    BATCH_CUDA(cudaStreamWaitEvent(b->cap, b->gjoins[g], 0));
+  }
+  return IMSRG_OK;
+}
+
+int record_grouped(imsrg_batch* b)
+{
+  int rc;
+  if ((rc = pair_stage(b, batch_pre)) || (rc = product_stage(b, grouped_ladder)) || (rc = pair_stage(b, batch_mid)) ||
+      (rc = product_stage(b, grouped_zbar)) || (rc = pair_stage(b, batch_post)))
+    return rc;
+  return IMSRG_OK;
+}
+
+// the grouped shape's product groups: pairs of equal structure and hermiticity
+int setup_grouped(imsrg_batch* b)
+{
+  std::map<std::vector<long long>, std::vector<int>> keyed;
+  for (size_t i = 0; i < b->X.size(); ++i) {
+    const Space& s = *b->X[i]->sp->s;
+    keyed[{s.emax, s.norb, s.nch, s.arena, b->X[i]->herm, b->Y[i]->herm}].push_back((int)i);
+  }
+  for (auto& kv : keyed) {
+    std::vector<const imsrg_op*> X, Y;
+    std::vector<imsrg_op*> Z;
+    for (int i : kv.second) {
+      X.push_back(b->X[i]);
+      Y.push_back(b->Y[i]);
+      Z.push_back(b->Z[i]);
+    }
+    std::string why;
+    GroupedProducts* g = grouped_products_create(X, Y, Z, &why);
+    if (!g) return berr(IMSRG_ERR_UNSUPPORTED, why);
+    b->products.push_back(g);
+    cudaStream_t s = nullptr;
+    cudaEvent_t e = nullptr;
+    BATCH_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    b->gstreams.push_back(s);
+    BATCH_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    b->gjoins.push_back(e);
+  }
+  return IMSRG_OK;
+}
+
 // the graph's branches: fork from the capture stream, every group's pairs in
 // order on the group's stream, join back
 int record(imsrg_batch* b)
 {
+  if (b->grouped) return record_grouped(b);
   BATCH_CUDA(cudaEventRecord(b->fork, b->cap));
   for (size_t g = 0; g < b->groups.size(); ++g) {
     cudaStream_t s = b->streams[g];
@@ -137,6 +228,15 @@ int imsrg_batch_create(int n, const imsrg_op* const* X, const imsrg_op* const* Y
         return rc;
       }
     }
+  // the grouped shape when it applies; the branch shape otherwise
+  if (precision == IMSRG_PREC_SPLIT && batch_phases_usable() && (int)b->groups.size() == n) {
+    b->grouped = true;
+    if (setup_grouped(b) != IMSRG_OK) {
+      for (GroupedProducts* g : b->products) grouped_products_destroy(g);
+      b->products.clear();
+      b->grouped = false;
+    }
+  }
   // the phase timers record events and read them back: not inside a graph
   const bool prof_was_on = prof_enabled();
   imsrg_profiler_enable(0);
@@ -197,11 +297,13 @@ int imsrg_batch_sync(imsrg_batch* b, void* stream)
   return IMSRG_OK;
 }
 
-int imsrg_batch_info(const imsrg_batch* b, int* n_pairs, int* n_groups, long long* kernel_nodes)
+int imsrg_batch_info(const imsrg_batch* b, int* n_pairs, int* n_branches, int* n_product_groups,
+                     long long* kernel_nodes)
 {
   if (!b) return berr(IMSRG_ERR_ARG, "null batch");
   if (n_pairs) *n_pairs = (int)b->X.size();
-  if (n_groups) *n_groups = (int)b->groups.size();
+  if (n_branches) *n_branches = (int)b->groups.size();
+  if (n_product_groups) *n_product_groups = b->grouped ? (int)b->products.size() : 0;
   if (kernel_nodes) *kernel_nodes = (long long)b->kernel_nodes;
   return IMSRG_OK;
 }

@@ -226,7 +226,10 @@ int imsrg_get_term(const char* name, int* on);
  * imsrg_commutator_scalar_scalar), of any mix of model spaces and sizes,
  * recorded once into a CUDA graph and replayed by imsrg_batch_launch.  Pairs
  * that share a model space run one after the other (they share its scratch);
- * pairs of different spaces run concurrently, one graph branch per space.
+ * pairs of different spaces run concurrently, one graph branch per space.  In
+ * the split form with every term on and one model space per pair, the two
+ * dense products of all pairs whose spaces have the same orbits (and whose
+ * operators the same hermiticities) run as one grouped launch each.
  * Creating a batch evaluates every pair once (allocating all scratch) and
  * captures the graph; the operators, their spaces and the term switches are
  * fixed from then on, and every operator must outlive the batch.  No Z may
@@ -239,8 +242,11 @@ void imsrg_batch_destroy(imsrg_batch* batch);
 int imsrg_batch_launch(imsrg_batch* batch, void* stream);
 /* Synchronise stream and, in split precision, check the kernels' status words. */
 int imsrg_batch_sync(imsrg_batch* batch, void* stream);
-/* Pairs, graph branches (distinct model spaces) and kernel nodes per replay. */
-int imsrg_batch_info(const imsrg_batch* batch, int* n_pairs, int* n_groups, long long* kernel_nodes);
+/* Pairs, graph branches (distinct model spaces), groups of pairs whose
+ * products run as one launch (0 when products run per pair) and kernel nodes
+ * per replay. */
+int imsrg_batch_info(const imsrg_batch* batch, int* n_pairs, int* n_branches, int* n_product_groups,
+                     long long* kernel_nodes);
 
 /* Default precision used by the reference-signature shim (process-wide). */
 int imsrg_set_default_precision(int precision);

@@ -1,8 +1,9 @@
 """Batched commutators (imsrg_batch_*: 64 pairs of uneven size in one CUDA
 graph, the 64-pair configuration with emax drawn from {2..6}) against the same
-commutators evaluated one by one and against the C oracle.  The only
-difference allowed against the one-by-one results is the order of the
-zero-body atomic sums: 1e-14 relative per body rank."""
+commutators evaluated one by one and against the C oracle.  The grouped
+products split every pair's operands into the same digits as the pair's own
+plan, so the only difference allowed against the one-by-one results is the
+order of the zero-body atomic sums: 1e-14 relative."""
 import numpy as np
 import pytest
 
@@ -39,8 +40,10 @@ def test_batch_matches_single_launches(prec):
     for _, _, dZ in pairs:
         dZ.zero()
     b = ig.CommutatorBatch(pairs, prec)
-    n, groups, nodes = b.info()
-    assert (n, groups) == (64, 64) and nodes > 64
+    n, branches, grouped, nodes = b.info()
+    assert (n, branches) == (64, 64) and nodes > 64
+    # split form: the products of the pairs of each emax run as one launch
+    assert grouped == (5 if prec == "split" else 0)
     for _, _, dZ in pairs:
         dZ.zero()
     for _ in range(2):
@@ -72,7 +75,7 @@ def test_batch_vs_oracle_shared_spaces():
         pairs.append((dX, dY, dZ))
         inputs.append((e, X, Y))
     b = ig.CommutatorBatch(pairs, "fp64")
-    assert b.info()[:2] == (5, 3)
+    assert b.info()[:3] == (5, 3, 0)
     for _, _, dZ in pairs:
         dZ.zero()
     b.launch()
