@@ -48,6 +48,16 @@ SIGNATURES = {
     "imsrg_space_pandya_layout": (I, [P, I, IP, IP, LLP, LLP]),
     "imsrg_pandya_transform": (I, [P, I, P, P]),
     "imsrg_op_create": (I, [P, I, ctypes.POINTER(P)]),
+    "imsrg_op_create_tensor": (I, [P, I, I, I, I, ctypes.POINTER(P)]),
+    "imsrg_op_rank": (I, [P, IP, IP, IP, LLP]),
+    "imsrg_space_tensor_layout": (I, [P, I, I, I, I, IP, IP, LLP, IP, LLP]),
+    "imsrg_space_ninej": (I, [P, I, I, I, I, I, I, I, I, I, DP]),
+    "imsrg_commutator_scalar_tensor": (I, [P, P, P, P]),
+    "imsrg_comm111st": (I, [P, P, P, P]),
+    "imsrg_comm121st": (I, [P, P, P, P]),
+    "imsrg_comm122st": (I, [P, P, P, P]),
+    "imsrg_comm222_pp_hh_221st": (I, [P, P, P, P]),
+    "imsrg_comm222_phst": (I, [P, P, P, P]),
     "imsrg_op_destroy": (None, [P]),
     "imsrg_op_hermiticity": (I, [P, IP]),
     "imsrg_op_set_hermiticity": (I, [P, I]),

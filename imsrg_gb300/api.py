@@ -117,6 +117,37 @@ class ModelSpace:
         return dict(J=J.value, parity=par.value, Tz=Tz.value, nkets=nk.value,
                     kets=list(zip(p[:nk.value].tolist(), q[:nk.value].tolist())))
 
+    def tensor_layout(self, jrank, trank, parity):
+        """{(ch_bra, ch_ket): arena offset} of the two-body blocks of a tensor
+        operator of that rank (TwoBodyME::Allocate order)."""
+        key = (int(jrank), int(trank), int(parity))
+        cache = self.__dict__.setdefault("_tensor_layouts", {})
+        if key not in cache:
+            nb, tot = ctypes.c_int(), ctypes.c_longlong()
+            check(self._L.imsrg_space_tensor_layout(self._h, *key, -1, None, None, None, ctypes.byref(nb),
+                                                    ctypes.byref(tot)))
+            blocks = {}
+            for b in range(nb.value):
+                cb, ck, off = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+                check(self._L.imsrg_space_tensor_layout(self._h, *key, b, ctypes.byref(cb), ctypes.byref(ck),
+                                                        ctypes.byref(off), None, None))
+                blocks[(cb.value, ck.value)] = off.value
+            cache[key] = (blocks, tot.value)
+        return cache[key][0]
+
+    def tensor_size(self, jrank, trank, parity):
+        self.tensor_layout(jrank, trank, parity)
+        return self._tensor_layouts[(int(jrank), int(trank), int(parity))][1]
+
+    def GetNineJ(self, ja, jd, J1, jb, jc, J2, Jbra, Jket, lam):
+        """{ja jd J1; jb jc J2; Jbra Jket lam} with ja..jd half-integers, the
+        other six integers (ModelSpace::GetNineJ argument order)."""
+        out = ctypes.c_double()
+        check(self._L.imsrg_space_ninej(self._h, int(lam), int(round(2 * ja)), int(round(2 * jd)), int(J1),
+                                        int(round(2 * jb)), int(round(2 * jc)), int(J2), int(Jbra), int(Jket),
+                                        ctypes.byref(out)))
+        return out.value
+
     def GetSixJ(self, j1, j2, j3, j4, j5, j6):
         """{j1 j2 j3; j4 j5 j6} with j1, j2, j4, j5 half-integer and j3, j6
         integer (ModelSpace::GetCachedSixJ argument convention doubled)."""
@@ -131,27 +162,47 @@ class _TwoBody:
         self._op = op
 
     def GetMatrix(self, ch_bra, ch_ket=None):
+        ms = self._op.modelspace
+        if self._op.rank != (0, 0, 0):
+            ch_ket = ch_bra if ch_ket is None else ch_ket
+            blocks = ms.tensor_layout(*self._op.rank)
+            if (ch_bra, ch_ket) not in blocks:
+                raise KeyError("no block (%d, %d) for this tensor rank" % (ch_bra, ch_ket))
+            o = blocks[(ch_bra, ch_ket)]
+            nb, nk = ms.channels[ch_bra]["nkets"], ms.channels[ch_ket]["nkets"]
+            return self._op.arena[o:o + nb * nk].reshape(nb, nk, order="F")
         if ch_ket is not None and ch_ket != ch_bra:
             raise KeyError("scalar operators only store diagonal channel blocks")
-        ms = self._op.modelspace
         c = ms.channels[ch_bra]
         n, o = c["nkets"], c["offset"]
         return self._op.arena[o:o + n * n].reshape(n, n, order="F")
 
 
 class Operator:
-    """Scalar operator (J=0, parity +, Tz=0, particle rank 2) in the arena
-    layout, host resident.  Operator(ms, 0, 0, 0, 2) as in the reference."""
+    """Two-body operator in the arena layout, host resident:
+    Operator(ms, 0, 0, 0, 2) a scalar (J=0, parity +, Tz=0), Operator(ms,
+    jrank, trank, parity, 2) a reduced tensor (tensor arena of that rank)."""
 
     def __init__(self, ms, jrank=0, trank=0, parity=0, particle_rank=2, arena=None, hermitian=True):
-        if (jrank, trank, parity) != (0, 0, 0) or particle_rank != 2:
-            raise NotImplementedError("only scalar particle-rank-2 operators are on the GPU path")
+        if particle_rank != 2:
+            raise NotImplementedError("only particle-rank-2 operators are on the GPU path")
         self.modelspace = ms
-        self.arena = np.zeros(ms.arena_size) if arena is None else np.ascontiguousarray(arena, dtype=np.float64)
-        if self.arena.shape != (ms.arena_size,):
+        self.rank = (int(jrank), int(trank), int(parity))
+        size = ms.arena_size if self.rank == (0, 0, 0) else ms.tensor_size(*self.rank)
+        self.arena = np.zeros(size) if arena is None else np.ascontiguousarray(arena, dtype=np.float64)
+        if self.arena.shape != (size,):
             raise ValueError("arena has the wrong length")
         self.hermitian = 1 if hermitian else -1
         self.TwoBody = _TwoBody(self)
+
+    def GetJRank(self):
+        return self.rank[0]
+
+    def GetTRank(self):
+        return self.rank[1]
+
+    def GetParity(self):
+        return self.rank[2]
 
     # hermiticity
     def SetHermitian(self):
@@ -180,7 +231,7 @@ class Operator:
         return self.arena[32:32 + N * N].reshape(N, N, order="F")
 
     def copy(self):
-        return Operator(self.modelspace, arena=self.arena.copy(), hermitian=self.hermitian == 1)
+        return Operator(self.modelspace, *self.rank, arena=self.arena.copy(), hermitian=self.hermitian == 1)
 
     def Erase(self):
         self.arena[:] = 0
@@ -224,12 +275,18 @@ class Operator:
 class DeviceOperator:
     """Operator resident in device memory (imsrg_op)."""
 
-    def __init__(self, ms, hermiticity=1):
+    def __init__(self, ms, hermiticity=1, rank=(0, 0, 0)):
         self.modelspace = ms
         self._L = _lib.lib()
         self._owned = True
         self._h = ctypes.c_void_p()
-        check(self._L.imsrg_op_create(ms._h, int(hermiticity), ctypes.byref(self._h)))
+        self.rank = tuple(int(x) for x in rank)
+        if self.rank == (0, 0, 0):
+            check(self._L.imsrg_op_create(ms._h, int(hermiticity), ctypes.byref(self._h)))
+            self.size = ms.arena_size
+        else:
+            check(self._L.imsrg_op_create_tensor(ms._h, *self.rank, int(hermiticity), ctypes.byref(self._h)))
+            self.size = ms.tensor_size(*self.rank)
 
     @classmethod
     def _view(cls, ms, handle, owner):
@@ -240,11 +297,13 @@ class DeviceOperator:
         d._owned = False
         d._owner = owner
         d._h = handle
+        d.rank = (0, 0, 0)
+        d.size = ms.arena_size
         return d
 
     @classmethod
     def from_host(cls, op, stream=None):
-        d = cls(op.modelspace, op.hermitian)
+        d = cls(op.modelspace, op.hermitian, getattr(op, "rank", (0, 0, 0)))
         d.upload(op.arena, stream)
         return d
 
@@ -277,7 +336,7 @@ class DeviceOperator:
 
     def upload(self, arena, stream=None):
         a = np.ascontiguousarray(arena, dtype=np.float64)
-        assert a.shape == (self.modelspace.arena_size,)
+        assert a.shape == (self.size,)
         check(self._L.imsrg_op_upload(self._h, _dp(a), stream))
         if stream is not None:
             self._keep = a
@@ -292,12 +351,12 @@ class DeviceOperator:
 
     def download(self, out=None, stream=None):
         if out is None:
-            out = np.empty(self.modelspace.arena_size)
+            out = np.empty(self.size)
         check(self._L.imsrg_op_download(self._h, _dp(out), stream))
         return out
 
     def to_host(self):
-        return Operator(self.modelspace, arena=self.download(), hermitian=self.hermiticity == 1)
+        return Operator(self.modelspace, *self.rank, arena=self.download(), hermitian=self.hermiticity == 1)
 
     def device_ptr(self):
         p = ctypes.c_void_p()
@@ -348,6 +407,7 @@ class _CommutatorNamespace:
 
     _TERMS_3 = ("comm110ss", "comm220ss", "comm111ss", "comm121ss", "comm122ss", "comm221ss")
     _TERMS_P = ("comm222_pp_hhss", "comm222_pp_hh_221ss", "comm222_phss")
+    _TERMS_ST = ("comm111st", "comm121st", "comm122st", "comm222_pp_hh_221st", "comm222_phst")
 
     def TurnOnTerm(self, name):
         check(_lib.lib().imsrg_set_term(name.encode(), 1))
@@ -386,7 +446,40 @@ class _CommutatorNamespace:
             Z.hermitian = dz.hermiticity
         return Z
 
-    Commutator = CommutatorScalarScalar
+    def CommutatorScalarTensor(self, X, Y):
+        """Commutator::CommutatorScalarTensor(X, Y): X scalar, Y a reduced tensor."""
+        ms = X.modelspace
+        Z = Operator(ms, *Y.rank)
+        with DeviceOperator.from_host(X) as dx, DeviceOperator.from_host(Y) as dy, \
+                DeviceOperator(ms, 1, Y.rank) as dz:
+            self.device_scalar_tensor(dx, dy, dz)
+            dz.download(Z.arena)
+            Z.hermitian = dz.hermiticity
+        return Z
+
+    def device_scalar_tensor(self, dX, dY, dZ, stream=None):
+        check(_lib.lib().imsrg_commutator_scalar_tensor(dX._h, dY._h, dZ._h, stream))
+
+    def device_tensor_term(self, name, dX, dY, dZ, stream=None):
+        """One scalar-tensor term (comm111st, comm121st, comm122st,
+        comm222_pp_hh_221st, comm222_phst) accumulated into dZ."""
+        if name not in self._TERMS_ST:
+            raise KeyError(name)
+        check(getattr(_lib.lib(), "imsrg_" + name)(dX._h, dY._h, dZ._h, stream))
+
+    def Commutator(self, X, Y, precision=None):
+        """Commutator::Commutator: dispatch on the tensor ranks
+        (src/Commutator.cc:182-276)."""
+        rx, ry = getattr(X, "rank", (0, 0, 0)), getattr(Y, "rank", (0, 0, 0))
+        if rx == (0, 0, 0) and ry == (0, 0, 0):
+            return self.CommutatorScalarScalar(X, Y, precision)
+        if rx == (0, 0, 0):
+            return self.CommutatorScalarTensor(X, Y)
+        if ry == (0, 0, 0):
+            Z = self.CommutatorScalarTensor(Y, X)  # [T, S] = -[S, T]
+            Z.arena *= -1
+            return Z
+        raise NotImplementedError("tensor-tensor commutators are not implemented in the reference either")
 
     def pandya_layout(self, ms):
         """[(rows, cols, offset)] per cross-coupled channel and the buffer length."""

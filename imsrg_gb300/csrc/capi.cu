@@ -266,6 +266,8 @@ int ensure_scratch(imsrg_space* sp, bool pandya, bool w2)
 int check_ops(const imsrg_op* X, const imsrg_op* Y, const imsrg_op* Z)
 {
   if (!X || !Y || !Z) return fail(IMSRG_ERR_ARG, "null operator");
+  if (X->tl || Y->tl || Z->tl)
+    return fail(IMSRG_ERR_UNSUPPORTED, "tensor operator passed to a scalar-scalar term (use imsrg_commutator_scalar_tensor)");
   if (X->sp != Y->sp || X->sp != Z->sp) return fail(IMSRG_ERR_ARG, "operators belong to different model spaces");
   if ((X->herm != 1 && X->herm != -1) || (Y->herm != 1 && Y->herm != -1))
     return fail(IMSRG_ERR_UNSUPPORTED, "X and Y must be hermitian or anti-hermitian");
@@ -652,6 +654,7 @@ int imsrg_op_create(imsrg_space* sp, int hermiticity, imsrg_op** out)
   imsrg_op* op = new imsrg_op();
   op->sp = sp;
   op->herm = hermiticity;
+  op->len = sp->s->arena;
   if (cudaMalloc(&op->d, sp->s->arena * sizeof(double)) != cudaSuccess) {
     delete op;
     cudaGetLastError();
@@ -663,6 +666,88 @@ int imsrg_op_create(imsrg_space* sp, int hermiticity, imsrg_op** out)
     return fail(IMSRG_ERR_CUDA, "operator arena memset failed");
   }
   *out = op;
+  return IMSRG_OK;
+}
+
+int imsrg_op_create_tensor(imsrg_space* sp, int lam, int trank, int parity, int hermiticity, imsrg_op** out)
+{
+  if (!sp || !out) return fail(IMSRG_ERR_ARG, "bad arguments");
+  if (lam < 0 || trank < 0 || trank > 1 || (parity != 0 && parity != 1) || lam >= sp->s->NJ)
+    return fail(IMSRG_ERR_ARG, "bad tensor rank");
+  if (hermiticity != 1 && hermiticity != -1) return fail(IMSRG_ERR_UNSUPPORTED, "hermiticity must be +1 or -1");
+  *out = nullptr;
+  int rc = ensure_device(sp);
+  if (rc) return rc;
+  TensorLayout* tl = nullptr;
+  try {
+    std::lock_guard<std::mutex> g(sp->mu);
+    tl = tensor_layout(*sp->s, lam, trank, parity);
+    tensor_upload(*tl);
+  } catch (std::exception& e) {
+    return fail(IMSRG_ERR_NOMEM, std::string("tensor tables: ") + e.what());
+  }
+  imsrg_op* op = new imsrg_op();
+  op->sp = sp;
+  op->herm = hermiticity;
+  op->tl = tl;
+  op->len = tl->total;
+  if (cudaMalloc(&op->d, op->len * sizeof(double)) != cudaSuccess) {
+    delete op;
+    cudaGetLastError();
+    return fail(IMSRG_ERR_NOMEM, "operator arena allocation failed");
+  }
+  if (cudaMemset(op->d, 0, op->len * sizeof(double)) != cudaSuccess) {
+    cudaFree(op->d);
+    delete op;
+    return fail(IMSRG_ERR_CUDA, "operator arena memset failed");
+  }
+  *out = op;
+  return IMSRG_OK;
+}
+
+int imsrg_op_rank(const imsrg_op* op, int* lam, int* trank, int* parity, long long* len)
+{
+  if (!op) return fail(IMSRG_ERR_ARG, "null operator");
+  if (lam) *lam = op->tl ? op->tl->lam : 0;
+  if (trank) *trank = op->tl ? op->tl->trank : 0;
+  if (parity) *parity = op->tl ? op->tl->parity : 0;
+  if (len) *len = op->len;
+  return IMSRG_OK;
+}
+
+int imsrg_space_tensor_layout(imsrg_space* sp, int lam, int trank, int parity, int block, int* ch_bra, int* ch_ket,
+                              long long* offset, int* nblocks, long long* total)
+{
+  if (!sp) return fail(IMSRG_ERR_ARG, "bad arguments");
+  if (lam < 0 || trank < 0 || trank > 1 || (parity != 0 && parity != 1) || lam >= sp->s->NJ)
+    return fail(IMSRG_ERR_ARG, "bad tensor rank");
+  TensorLayout* tl = nullptr;
+  {
+    std::lock_guard<std::mutex> g(sp->mu);
+    tl = tensor_layout(*sp->s, lam, trank, parity);
+  }
+  if (nblocks) *nblocks = (int)tl->bra.size();
+  if (total) *total = tl->total;
+  if (block < 0) return IMSRG_OK;
+  if (block >= (int)tl->bra.size()) return fail(IMSRG_ERR_ARG, "block index out of range");
+  if (ch_bra) *ch_bra = tl->bra[block];
+  if (ch_ket) *ch_ket = tl->ket[block];
+  if (offset) *offset = tl->off[block];
+  return IMSRG_OK;
+}
+
+int imsrg_space_ninej(imsrg_space* sp, int lam, int ja, int jd, int J1, int jb, int jc, int J2, int Jbra, int Jket,
+                      double* out)
+{
+  if (!sp || !out) return fail(IMSRG_ERR_ARG, "bad arguments");
+  if (lam < 0 || lam >= sp->s->NJ) return fail(IMSRG_ERR_ARG, "bad rank");
+  TensorLayout* tl = nullptr;
+  {
+    std::lock_guard<std::mutex> g(sp->mu);
+    tl = tensor_layout(*sp->s, lam, 0, 0);
+  }
+  DevTensor h = tensor_host_view(*tl);
+  *out = ninej_tensor(h, lam, ja, jb, jc, jd, J1, J2, Jbra, Jket);
   return IMSRG_OK;
 }
 
@@ -691,14 +776,14 @@ int imsrg_op_set_hermiticity(imsrg_op* op, int h)
 int imsrg_op_upload(imsrg_op* op, const double* host, void* stream)
 {
   if (!op || !host) return fail(IMSRG_ERR_ARG, "bad arguments");
-  CUDA_TRY(cudaMemcpyAsync(op->d, host, op->sp->s->arena * sizeof(double), cudaMemcpyHostToDevice, S_(stream)));
+  CUDA_TRY(cudaMemcpyAsync(op->d, host, op->len * sizeof(double), cudaMemcpyHostToDevice, S_(stream)));
   return IMSRG_OK;
 }
 
 int imsrg_op_download(const imsrg_op* op, double* host, void* stream)
 {
   if (!op || !host) return fail(IMSRG_ERR_ARG, "bad arguments");
-  CUDA_TRY(cudaMemcpyAsync(host, op->d, op->sp->s->arena * sizeof(double), cudaMemcpyDeviceToHost, S_(stream)));
+  CUDA_TRY(cudaMemcpyAsync(host, op->d, op->len * sizeof(double), cudaMemcpyDeviceToHost, S_(stream)));
   CUDA_TRY(cudaStreamSynchronize(S_(stream)));
   return IMSRG_OK;
 }
@@ -713,16 +798,16 @@ int imsrg_op_device_arena(const imsrg_op* op, double** dptr)
 int imsrg_op_zero(imsrg_op* op, void* stream)
 {
   if (!op) return fail(IMSRG_ERR_ARG, "null operator");
-  CUDA_TRY(cudaMemsetAsync(op->d, 0, op->sp->s->arena * sizeof(double), S_(stream)));
+  CUDA_TRY(cudaMemsetAsync(op->d, 0, op->len * sizeof(double), S_(stream)));
   return IMSRG_OK;
 }
 
 int imsrg_op_copy(imsrg_op* dst, const imsrg_op* src, void* stream)
 {
   if (!dst || !src || dst->sp != src->sp) return fail(IMSRG_ERR_ARG, "bad arguments");
+  if (dst->tl != src->tl) return fail(IMSRG_ERR_ARG, "operators of different tensor rank");
   if (dst == src) return IMSRG_OK;
-  CUDA_TRY(cudaMemcpyAsync(dst->d, src->d, src->sp->s->arena * sizeof(double), cudaMemcpyDeviceToDevice,
-                           S_(stream)));
+  CUDA_TRY(cudaMemcpyAsync(dst->d, src->d, src->len * sizeof(double), cudaMemcpyDeviceToDevice, S_(stream)));
   dst->herm = src->herm;
   return IMSRG_OK;
 }
@@ -730,26 +815,29 @@ int imsrg_op_copy(imsrg_op* dst, const imsrg_op* src, void* stream)
 int imsrg_op_scale(imsrg_op* op, double a, void* stream)
 {
   if (!op) return fail(IMSRG_ERR_ARG, "null operator");
-  CUDA_TRY(launch_scale(op->d, a, op->sp->s->arena, S_(stream)));
+  CUDA_TRY(launch_scale(op->d, a, op->len, S_(stream)));
   return IMSRG_OK;
 }
 
 int imsrg_op_axpy(imsrg_op* y, double a, const imsrg_op* x, void* stream)
 {
   if (!y || !x || y->sp != x->sp) return fail(IMSRG_ERR_ARG, "bad arguments");
-  CUDA_TRY(launch_axpy(y->d, x->d, a, y->sp->s->arena, S_(stream)));
+  if (y->tl != x->tl) return fail(IMSRG_ERR_ARG, "operators of different tensor rank");
+  CUDA_TRY(launch_axpy(y->d, x->d, a, y->len, S_(stream)));
   return IMSRG_OK;
 }
 
 int imsrg_op_norm(const imsrg_op* op, double* out, void* stream)
 {
   if (!op || !out) return fail(IMSRG_ERR_ARG, "bad arguments");
+  if (op->tl) return fail(IMSRG_ERR_UNSUPPORTED, "norm of a tensor operator is not on the GPU path");
   return norm_impl(op, out, S_(stream));
 }
 
 int imsrg_op_fill_random(imsrg_op* op, unsigned long long seed, void* stream)
 {
   if (!op) return fail(IMSRG_ERR_ARG, "null operator");
+  if (op->tl) return fail(IMSRG_ERR_UNSUPPORTED, "random fill of a tensor operator is not on the GPU path");
   const Space& s = *op->sp->s;
   std::vector<double> a((size_t)s.arena, 0.0);
   Rng rng{seed * 0x2545F4914F6CDD1Dull + 0x1234567ull};
@@ -909,6 +997,7 @@ int imsrg_bch_transform(const imsrg_op* OpIn, const imsrg_op* Omega, imsrg_op* O
 {
   if (!OpIn || !Omega || !OpOut) return fail(IMSRG_ERR_ARG, "null operator");
   if (OpIn->sp != Omega->sp || OpIn->sp != OpOut->sp) return fail(IMSRG_ERR_ARG, "different model spaces");
+  if (OpIn->tl || Omega->tl || OpOut->tl) return fail(IMSRG_ERR_UNSUPPORTED, "BCH_Transform of tensor operators is not on the GPU path");
   if (OpOut == Omega) return fail(IMSRG_ERR_ARG, "OpOut must not alias Omega");
   cudaStream_t st = S_(stream);
   imsrg_space* sp = OpIn->sp;

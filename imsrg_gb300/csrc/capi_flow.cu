@@ -293,6 +293,7 @@ int imsrg_generator_update(const imsrg_op* H, imsrg_op* Eta, int type, int parti
                            double delta, int delta_index, void* stream)
 {
   if (!H || !Eta || H == Eta) return err(IMSRG_ERR_ARG, "bad operators");
+  if (H->tl || Eta->tl) return err(IMSRG_ERR_UNSUPPORTED, "the generator takes scalar operators");
   if (H->sp != Eta->sp) return err(IMSRG_ERR_ARG, "operators belong to different model spaces");
   if (type < IMSRG_GEN_WHITE || type > IMSRG_GEN_IMAGINARY_TIME) return err(IMSRG_ERR_ARG, "bad generator type");
   if (partitioning != IMSRG_DENOM_EPSTEIN_NESBET && partitioning != IMSRG_DENOM_MOLLER_PLESSET)
@@ -311,6 +312,7 @@ int imsrg_bch_product(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, double 
 {
   if (!X || !Y || !Z) return err(IMSRG_ERR_ARG, "null operator");
   if (X->sp != Y->sp || X->sp != Z->sp) return err(IMSRG_ERR_ARG, "operators belong to different model spaces");
+  if (X->tl || Y->tl || Z->tl) return err(IMSRG_ERR_UNSUPPORTED, "BCH_Product of tensor operators is not on the GPU path");
   if ((X->herm != 1 && X->herm != -1) || (Y->herm != 1 && Y->herm != -1))
     return err(IMSRG_ERR_UNSUPPORTED, "X and Y must be hermitian or anti-hermitian");
   return bch_product_impl(X, Y, Z, threshold, precision, n_commutators, S_(stream));
@@ -319,6 +321,7 @@ int imsrg_bch_product(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, double 
 int imsrg_solver_create(const imsrg_op* H0, imsrg_solver** out)
 {
   if (!H0 || !out) return err(IMSRG_ERR_ARG, "bad arguments");
+  if (H0->tl) return err(IMSRG_ERR_UNSUPPORTED, "the flow takes a scalar Hamiltonian");
   *out = nullptr;
   imsrg_solver* sv = new imsrg_solver();
   sv->sp = H0->sp;
@@ -476,6 +479,7 @@ int imsrg_solver_transform(const imsrg_solver* sv, const imsrg_op* OpIn, imsrg_o
 {
   if (!sv || !OpIn || !OpOut) return err(IMSRG_ERR_ARG, "bad arguments");
   if (OpIn->sp != sv->sp || OpOut->sp != sv->sp) return err(IMSRG_ERR_ARG, "operator from another model space");
+  if (OpIn->tl || OpOut->tl) return err(IMSRG_ERR_UNSUPPORTED, "transforms of tensor operators are not on the GPU path");
   cudaStream_t st = S_(stream);
   // IMSRGSolver::Transform_Partial(OpIn, 0), src/IMSRGSolver.cc:957-1002:
   // the Omegas written to scratch files first, then those in device memory
@@ -502,6 +506,7 @@ int imsrg_solver_inverse_transform(const imsrg_solver* sv, const imsrg_op* OpIn,
 {
   if (!sv || !OpIn || !OpOut) return err(IMSRG_ERR_ARG, "bad arguments");
   if (OpIn->sp != sv->sp || OpOut->sp != sv->sp) return err(IMSRG_ERR_ARG, "operator from another model space");
+  if (OpIn->tl || OpOut->tl) return err(IMSRG_ERR_UNSUPPORTED, "transforms of tensor operators are not on the GPU path");
   cudaStream_t st = S_(stream);
   // IMSRGSolver::InverseTransform, src/IMSRGSolver.cc:939-952: Omegas in
   // reverse order, each negated

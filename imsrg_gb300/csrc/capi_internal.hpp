@@ -12,6 +12,7 @@
 
 #include "kernels.cuh"
 #include "space.hpp"
+#include "tensor.hpp"
 
 using imsrg::GemmJobDev;
 using imsrg::Space;
@@ -115,5 +116,9 @@ struct imsrg_op {
   imsrg_space* sp = nullptr;
   double* d = nullptr;
   int herm = 1;
+  long long len = 0;  // arena length in doubles
+  // reduced tensor operators (imsrg_op_create_tensor): their layout; nullptr
+  // for the scalar operators of the IMSRG(2) scalar commutator
+  imsrg::TensorLayout* tl = nullptr;
 };
 

@@ -100,6 +100,7 @@ extern "C" {
 int imsrg_op_write_binary(const imsrg_op* op, const char* path, void* stream)
 {
   if (!op || !path) return ioerr(IMSRG_ERR_ARG, "bad arguments");
+  if (op->tl) return ioerr(IMSRG_ERR_UNSUPPORTED, "tensor operator files are not on the GPU path");
   if (op->herm != 1 && op->herm != -1) return ioerr(IMSRG_ERR_UNSUPPORTED, "hermiticity must be +1 or -1");
   const Space& s = *op->sp->s;
   cudaStream_t st = (cudaStream_t)stream;
@@ -160,6 +161,7 @@ int imsrg_op_write_binary(const imsrg_op* op, const char* path, void* stream)
 int imsrg_op_read_binary(imsrg_op* op, const char* path, void* stream)
 {
   if (!op || !path) return ioerr(IMSRG_ERR_ARG, "bad arguments");
+  if (op->tl) return ioerr(IMSRG_ERR_UNSUPPORTED, "tensor operator files are not on the GPU path");
   const Space& s = *op->sp->s;
   cudaStream_t st = (cudaStream_t)stream;
   File fh;

@@ -64,6 +64,22 @@ cudaError_t launch_scale(double* y, double a, long long n, cudaStream_t st);
 cudaError_t launch_norm(const Space& s, const double* A, const long long* chunk_off, const int* chunk_len,
                         const double* chunk_w, int nchunks, double* partial, cudaStream_t st);
 
+// kernels_tensor.cu: the scalar-tensor commutator [X, Y] (X scalar, Y a
+// reduced tensor of layout t); each adds its term into Z (layout t)
+struct TensorLayout;
+cudaError_t launch_tensor_111(const Space& s, const double* X, const double* Y, double* Z, cudaStream_t st);
+cudaError_t launch_tensor_121(const Space& s, const TensorLayout& t, const int* dev_holes, const double* X,
+                              const double* Y, int hY, double* Z, int hZ, cudaStream_t st);
+cudaError_t launch_tensor_122(const Space& s, const TensorLayout& t, const double* X, const double* Y, int hY,
+                              double* Z, cudaStream_t st);
+// Mpp, Mhh: scratch arenas of layout t
+cudaError_t launch_tensor_222_221(const Space& s, const TensorLayout& t, const double* X, const double* Y,
+                                  double* Mpp, double* Mhh, double* Z, int hZ, cudaStream_t st);
+// Xbar: the transposed single-operator Pandya transform of X (xb layout);
+// Ybar, Zbar: scratch of t's yb_total and zb_total doubles
+cudaError_t launch_tensor_ph(const Space& s, const TensorLayout& t, const double* Xbar, const double* Y, int hX,
+                             int hY, double* Ybar, double* Zbar, double* Z, int hZ, cudaStream_t st);
+
 // kernels_gemm.cu
 int symgemm_fp64_tile();
 cudaError_t launch_symgemm_fp64(const GemmJobDev* jobs, const int* pairs, int npairs, const double* A,

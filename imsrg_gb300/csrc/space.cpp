@@ -7,6 +7,7 @@
 //   channel index 6J + 2(Tz+1) + parity  ModelSpace::GetTwoBodyChannelIndex (src/ModelSpace.cc:1046-1053)
 // plus the arena layout and the per-kernel work lists.
 #include "space.hpp"
+#include "tensor.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -475,6 +476,7 @@ void build_invq_tasks(Space& s, int budget)
 
 Space::~Space()
 {
+  for (auto& kv : tensors) delete kv.second;
   for (void* p : dev_allocs) cudaFree(p);
   for (Scratch* sc : {&s_xb, &s_yb, &s_yf, &s_zb, &s_w2, &s_red, &s_split_a, &s_split_b, &s_split_e, &s_jobs})
     if (sc->ptr) cudaFree(sc->ptr);

@@ -5,12 +5,15 @@
 #pragma once
 
 #include <cstdint>
+#include <map>
 #include <string>
 #include <vector>
 
 #include "devspace.cuh"
 
 namespace imsrg {
+
+struct TensorLayout;
 
 struct Chan {
   int J = 0, parity = 0, Tz = 0;
@@ -93,6 +96,9 @@ struct Space {
     size_t bytes = 0;
   };
   Scratch s_xb, s_yb, s_yf, s_zb, s_w2, s_red, s_split_a, s_split_b, s_split_e, s_jobs;
+
+  // tensor-operator layouts by rank, built on first use (tensor.cpp)
+  std::map<int, TensorLayout*> tensors;
 
   ~Space();
 };

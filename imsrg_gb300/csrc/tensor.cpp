@@ -1,0 +1,227 @@
+// Tensor-operator layouts and angular-momentum tables (see tensor.hpp).
+#include "tensor.hpp"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdlib>
+#include <stdexcept>
+
+#include "space.hpp"
+
+namespace imsrg {
+namespace {
+
+int64_t round32(int64_t x) { return (x + 31) / 32 * 32; }
+
+bool triad2(int a, int b, int c)  // doubled arguments
+{
+  if ((a + b + c) & 1) return false;
+  return c <= a + b && c >= std::abs(a - b);
+}
+
+// compact {h1 h2 I3; h4 h5 I6} table of extent d1 (the layout sixj_slot reads)
+void build_compact(int d1, std::vector<int>& base, std::vector<double>& val)
+{
+  base.assign((size_t)d1 * d1 * d1 * d1, 0);
+  size_t tot = 0;
+  for (int a = 0; a < d1; ++a)
+    for (int b = 0; b < d1; ++b)
+      for (int c = 0; c < d1; ++c)
+        for (int d = 0; d < d1; ++d) {
+          int jj1 = 2 * a + 1, jj2 = 2 * b + 1, jj4 = 2 * c + 1, jj5 = 2 * d + 1;
+          int n3 = (jj1 + jj2 - std::abs(jj1 - jj2)) / 2 + 1;
+          int J6min = std::max(std::abs(jj1 - jj5), std::abs(jj4 - jj2)) / 2;
+          int J6max = std::min(jj1 + jj5, jj4 + jj2) / 2;
+          base[((a * d1 + b) * d1 + c) * d1 + d] = (int)tot;
+          tot += (size_t)n3 * std::max(0, J6max - J6min + 1);
+        }
+  val.assign(tot, 0.0);
+#pragma omp parallel for schedule(dynamic, 1) collapse(2)
+  for (int a = 0; a < d1; ++a)
+    for (int b = 0; b < d1; ++b)
+      for (int c = 0; c < d1; ++c)
+        for (int d = 0; d < d1; ++d) {
+          int jj1 = 2 * a + 1, jj2 = 2 * b + 1, jj4 = 2 * c + 1, jj5 = 2 * d + 1;
+          int J3min = std::abs(jj1 - jj2) / 2, J3max = (jj1 + jj2) / 2;
+          int J6min = std::max(std::abs(jj1 - jj5), std::abs(jj4 - jj2)) / 2;
+          int J6max = std::min(jj1 + jj5, jj4 + jj2) / 2;
+          int n6 = J6max - J6min + 1;
+          if (n6 <= 0) continue;
+          size_t b0 = base[((a * d1 + b) * d1 + c) * d1 + d];
+          for (int J3 = J3min; J3 <= J3max; ++J3)
+            for (int J6 = J6min; J6 <= J6max; ++J6)
+              val[b0 + (J3 - J3min) * n6 + (J6 - J6min)] = sixj_dd(jj1, jj2, 2 * J3, jj4, jj5, 2 * J6);
+        }
+}
+
+template <class T>
+T* dev_copy(TensorLayout& t, const std::vector<T>& v)
+{
+  void* p = nullptr;
+  size_t bytes = std::max<size_t>(1, v.size()) * sizeof(T);
+  if (cudaMalloc(&p, bytes) != cudaSuccess) throw std::runtime_error("cudaMalloc (tensor tables)");
+  t.dev_allocs.push_back(p);
+  if (!v.empty() && cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+    throw std::runtime_error("cudaMemcpy (tensor tables)");
+  return (T*)p;
+}
+
+}  // namespace
+
+TensorLayout::~TensorLayout()
+{
+  for (void* p : dev_allocs) cudaFree(p);
+}
+
+TensorLayout* tensor_layout(Space& s, int lam, int trank, int parity)
+{
+  const int key = (lam * 4 + trank) * 2 + parity;
+  auto it = s.tensors.find(key);
+  if (it != s.tensors.end()) return it->second;
+  TensorLayout* t = new TensorLayout();
+  t->lam = lam;
+  t->trank = trank;
+  t->parity = parity;
+  // blocks in TwoBodyME::Allocate order
+  t->lookup.assign((size_t)s.nch * s.nch, -1);
+  int64_t cur = round32(32 + (int64_t)s.norb * s.norb);
+  for (int cb = 0; cb < s.nch; ++cb)
+    for (int ck = cb; ck < s.nch; ++ck) {
+      const Chan &B = s.ch[cb], &K = s.ch[ck];
+      if (std::abs(B.J - K.J) > lam || B.J + K.J < lam) continue;
+      if (std::abs(B.Tz - K.Tz) != trank) continue;
+      if ((B.parity + K.parity + parity) & 1) continue;
+      t->lookup[(size_t)cb * s.nch + ck] = (int)t->bra.size();
+      t->bra.push_back(cb);
+      t->ket.push_back(ck);
+      t->off.push_back(cur);
+      cur = round32(cur + (int64_t)B.n() * K.n());
+    }
+  t->total = cur;
+  for (size_t b = 0; b < t->bra.size(); ++b)
+    t->max_blk_elems = std::max<int64_t>(t->max_blk_elems, (int64_t)s.ch[t->bra[b]].n() * s.ch[t->ket[b]].n());
+  // comm222_phst (src/TensorCommutators.cc:1059-1386): Zbar blocks for the
+  // cross-coupled channel pairs lo <= hi allowed by the rank, and the ordered
+  // pairs of the tensor Pandya transform of Y they read, (lo, hi) and (hi, lo)
+  t->zb_lookup.assign((size_t)s.nch * s.nch, -1);
+  t->yb_lookup.assign((size_t)s.nch * s.nch, -1);
+  int64_t zc = 0, yc = 0;
+  auto need_y = [&](int b, int k) {
+    int64_t& slot = t->yb_lookup[(size_t)b * s.nch + k];
+    if (slot >= 0) return;
+    slot = yc;
+    t->yb_bra.push_back(b);
+    t->yb_ket.push_back(k);
+    t->yb_off.push_back(yc);
+    int64_t e = (int64_t)2 * s.cc_nph[b] * s.cc[k].n();
+    t->yb_maxelems = (int)std::max<int64_t>(t->yb_maxelems, e);
+    yc = round32(yc + e);
+  };
+  for (int b = 0; b < s.nch; ++b) {
+    const Chan& B = s.cc[b];
+    if (B.n() < 1) continue;
+    for (int k = b; k < s.nch; ++k) {
+      const Chan& K = s.cc[k];
+      if (K.n() < 1) continue;
+      if ((B.parity + K.parity + parity) & 1) continue;
+      if (B.J + K.J < lam || std::abs(B.J - K.J) > lam) continue;
+      if (!(B.Tz + K.Tz == trank || std::abs(B.Tz - K.Tz) == trank)) continue;
+      t->zb_lookup[(size_t)b * s.nch + k] = zc;
+      t->zb_bra.push_back(b);
+      t->zb_ket.push_back(k);
+      t->zb_off.push_back(zc);
+      int64_t e = (int64_t)B.n() * 2 * K.n();
+      t->zb_maxelems = (int)std::max<int64_t>(t->zb_maxelems, e);
+      zc = round32(zc + e);
+      need_y(b, k);
+      need_y(k, b);
+    }
+  }
+  t->zb_total = zc;
+  t->yb_total = yc;
+  // one-body elements: Operator::SetUpOneBodyChannels (src/Operator.cc:248-291)
+  const int N = s.norb;
+  t->ob_ok.assign((size_t)N * N, 0);
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j)
+      t->ob_ok[(size_t)i * N + j] = ((s.l[i] + s.l[j] + parity) % 2 == 0) && triad2(s.j2[i], s.j2[j], 2 * lam) &&
+                                    std::abs(s.tz2[i] - s.tz2[j]) == 2 * trank;
+  // angular tables, half-integers widened by lam (the 9j sums reach j + lam)
+  t->NJ = s.NJ;
+  t->d1x = s.d1 + lam;
+  const int NJ = t->NJ, d1x = t->d1x;
+  t->sixjA.assign((size_t)NJ * NJ * d1x * d1x * d1x, 0.0);
+#pragma omp parallel for schedule(dynamic, 1) collapse(2)
+  for (int I1 = 0; I1 < NJ; ++I1)
+    for (int I2 = 0; I2 < NJ; ++I2) {
+      if (!triad2(2 * I1, 2 * I2, 2 * lam)) continue;
+      for (int a = 0; a < d1x; ++a)
+        for (int b = 0; b < d1x; ++b)
+          for (int c = 0; c < d1x; ++c) {
+            int ja = 2 * a + 1, jb = 2 * b + 1, jc = 2 * c + 1;
+            // {I1 I2 lam; ja jb jc}: triads (I1 jb jc), (ja I2 jc), (ja jb lam)
+            if (!triad2(2 * I1, jb, jc) || !triad2(ja, 2 * I2, jc) || !triad2(ja, jb, 2 * lam)) continue;
+            t->sixjA[((((size_t)I1 * NJ + I2) * d1x + a) * d1x + b) * d1x + c] =
+                sixj_dd(2 * I1, 2 * I2, 2 * lam, ja, jb, jc);
+          }
+    }
+  build_compact(d1x, t->sixjx_base, t->sixjx_val);
+  s.tensors[key] = t;
+  return t;
+}
+
+DevTensor tensor_host_view(const TensorLayout& t)
+{
+  DevTensor d;
+  d.lam = t.lam;
+  d.trank = t.trank;
+  d.parity = t.parity;
+  d.nblk = (int)t.bra.size();
+  d.total = t.total;
+  d.sixjA = t.sixjA.data();
+  d.sixjx_base = t.sixjx_base.data();
+  d.sixjx_val = t.sixjx_val.data();
+  d.NJ = t.NJ;
+  d.d1x = t.d1x;
+  return d;
+}
+
+void tensor_upload(TensorLayout& t)
+{
+  if (t.dev_ready) return;
+  DevTensor& d = t.dev;
+  d.lam = t.lam;
+  d.trank = t.trank;
+  d.parity = t.parity;
+  d.nblk = (int)t.bra.size();
+  d.total = t.total;
+  d.bra = dev_copy(t, t.bra);
+  d.ket = dev_copy(t, t.ket);
+  std::vector<long long> off(t.off.begin(), t.off.end());
+  d.off = dev_copy(t, off);
+  d.lookup = dev_copy(t, t.lookup);
+  d.ob_ok = dev_copy(t, t.ob_ok);
+  d.sixjA = dev_copy(t, t.sixjA);
+  d.sixjx_base = dev_copy(t, t.sixjx_base);
+  d.sixjx_val = dev_copy(t, t.sixjx_val);
+  d.NJ = t.NJ;
+  d.d1x = t.d1x;
+  d.nzb = (int)t.zb_bra.size();
+  d.nyb = (int)t.yb_bra.size();
+  d.zb_bra = dev_copy(t, t.zb_bra);
+  d.zb_ket = dev_copy(t, t.zb_ket);
+  std::vector<long long> zo(t.zb_off.begin(), t.zb_off.end()), yo(t.yb_off.begin(), t.yb_off.end());
+  std::vector<long long> zl(t.zb_lookup.begin(), t.zb_lookup.end()), yl(t.yb_lookup.begin(), t.yb_lookup.end());
+  d.zb_off = dev_copy(t, zo);
+  d.zb_lookup = dev_copy(t, zl);
+  d.yb_bra = dev_copy(t, t.yb_bra);
+  d.yb_ket = dev_copy(t, t.yb_ket);
+  d.yb_off = dev_copy(t, yo);
+  d.yb_lookup = dev_copy(t, yl);
+  d.zb_total = t.zb_total;
+  d.yb_total = t.yb_total;
+  t.dev_ready = true;
+}
+
+}  // namespace imsrg

@@ -1,0 +1,136 @@
+// Reduced tensor operators of rank (lambda, |delta Tz|, parity): the arena
+// layout of their two-body blocks, the angular-momentum tables the
+// scalar-tensor commutator needs (6j symbols with three integer and three
+// half-integer arguments, 6j symbols with the half-integer range widened by
+// lambda, and 9j symbols built from them), and the device view of all of it.
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <vector>
+
+#include "devspace.cuh"
+
+namespace imsrg {
+
+struct Space;
+
+// Device view of one tensor layout.  Arena of a tensor operator: ZeroBody at
+// [0], OneBody N x N column-major at [32], then block b = (ch_bra[b] <=
+// ch_ket[b]) as n_bra x n_ket column-major at off[b] (a multiple of 32), in
+// TwoBodyME::Allocate order (src/TwoBodyME.cc:77-95).
+struct DevTensor {
+  int lam = 0, trank = 0, parity = 0, nblk = 0;
+  long long total = 0;
+  const int* bra = nullptr;
+  const int* ket = nullptr;
+  const long long* off = nullptr;
+  const int* lookup = nullptr;  // [ch_bra * nch + ch_ket] -> block, -1 (ch_bra <= ch_ket)
+  const unsigned char* ob_ok = nullptr;  // [i * N + j]: <i||T||j> allowed
+  // 6j {I1 I2 lam; h1 h2 h3} for I1, I2 < NJ and doubled half-integers
+  // 2h + 1 <= 2 d1x - 1: [(((I1 * NJ + I2) * d1x + a) * d1x + b) * d1x + c]
+  const double* sixjA = nullptr;
+  // 6j {h1 h2 I3; h4 h5 I6} with the compact layout of the space's table,
+  // half-integers up to 2 d1x - 1 (the 9j sums reach j + lambda)
+  const int* sixjx_base = nullptr;
+  const double* sixjx_val = nullptr;
+  int NJ = 0, d1x = 0;
+  // comm222_phst: cross-coupled channel pairs (lo <= hi) of Zbar, n_lo x
+  // 2 n_hi column-major at zb_off; and the ordered pairs (bra, ket) of the
+  // tensor Pandya transform of Y, 2 nph_bra x n_ket column-major at yb_off
+  int nzb = 0, nyb = 0;
+  const int* zb_bra = nullptr;
+  const int* zb_ket = nullptr;
+  const long long* zb_off = nullptr;
+  const long long* zb_lookup = nullptr;  // [lo * nch + hi] -> offset, -1
+  const int* yb_bra = nullptr;
+  const int* yb_ket = nullptr;
+  const long long* yb_off = nullptr;
+  const long long* yb_lookup = nullptr;  // [bra * nch + ket] -> offset, -1
+  long long zb_total = 0, yb_total = 0;
+};
+
+struct TensorLayout {
+  int lam = 0, trank = 0, parity = 0;
+  std::vector<int> bra, ket, lookup;
+  std::vector<int64_t> off;
+  int64_t total = 0;
+  std::vector<unsigned char> ob_ok;
+  std::vector<double> sixjA;
+  std::vector<int> sixjx_base;
+  std::vector<double> sixjx_val;
+  int NJ = 0, d1x = 0;
+  std::vector<int> zb_bra, zb_ket, yb_bra, yb_ket;
+  std::vector<int64_t> zb_off, yb_off, zb_lookup, yb_lookup;
+  int64_t zb_total = 0, yb_total = 0;
+  int zb_maxelems = 0, yb_maxelems = 0;  // largest block of each list (grid sizing)
+  int max_blk_elems = 0;                 // largest two-body block of the layout
+  // scratch of the scalar-tensor commutator (device, lazily allocated):
+  // Mpp, Mhh (layout total), X bar (the space's xb_total), Y bar, Z bar
+  double *d_mpp = nullptr, *d_mhh = nullptr, *d_xbar = nullptr, *d_ybar = nullptr, *d_zbar = nullptr;
+  DevTensor dev;
+  bool dev_ready = false;
+  std::vector<void*> dev_allocs;
+  ~TensorLayout();
+};
+
+// the space's layout of rank (lam, trank, parity), built on first use
+// (host tables only; tensor_upload copies them to the device)
+TensorLayout* tensor_layout(Space& s, int lam, int trank, int parity);
+void tensor_upload(TensorLayout& t);
+// the same view with host pointers (host-side 9j and 6j evaluation)
+DevTensor tensor_host_view(const TensorLayout& t);
+
+IMSRG_HD int sixjA_index(int NJ, int d1x, int I1, int I2, int jj1, int jj2, int jj3)
+{
+  if (I1 < 0 || I2 < 0 || I1 >= NJ || I2 >= NJ) return -1;
+  if (jj1 < 1 || jj2 < 1 || jj3 < 1) return -1;
+  int a = (jj1 - 1) >> 1, b = (jj2 - 1) >> 1, c = (jj3 - 1) >> 1;
+  if (a >= d1x || b >= d1x || c >= d1x) return -1;
+  return (((I1 * NJ + I2) * d1x + a) * d1x + b) * d1x + c;
+}
+
+// {I1 I2 lam; jj1/2 jj2/2 jj3/2}
+IMSRG_HD double sixjA_get(const double* tab, int NJ, int d1x, int I1, int I2, int jj1, int jj2, int jj3)
+{
+  int k = sixjA_index(NJ, d1x, I1, I2, jj1, jj2, jj3);
+  return k < 0 ? 0.0 : tab[k];
+}
+
+// {jj1/2 jj2/2 J3; jj4/2 jj5/2 J6} from a compact table of extent d1
+IMSRG_HD double sixj_compact_get(const int* base, const double* val, int d1, int jj1, int jj2, int J3, int jj4,
+                                 int jj5, int J6)
+{
+  if (jj1 < 1 || jj2 < 1 || jj4 < 1 || jj5 < 1) return 0.0;
+  if (((jj1 - 1) >> 1) >= d1 || ((jj2 - 1) >> 1) >= d1 || ((jj4 - 1) >> 1) >= d1 || ((jj5 - 1) >> 1) >= d1)
+    return 0.0;
+  int s = sixj_slot(d1, base, jj1, jj2, J3, jj4, jj5, J6);
+  return s < 0 ? 0.0 : val[s];
+}
+
+// 9j {ja/2 jd/2 J1; jb/2 jc/2 J2; Jbra Jket lam} for half-integer ja..jd and
+// integer J1, J2, Jbra, Jket, as the sum over x of three 6j symbols
+// (Edmonds, "Angular Momentum in Quantum Mechanics", eq. 6.4.3):
+//   {j1 j2 j3; j4 j5 j6; j7 j8 j9} = sum_x (-1)^(2x) (2x+1)
+//       {j1 j4 j7; j8 j9 x} {j2 j5 j8; j4 x j6} {j3 j6 j9; x j1 j2}
+// with {ja jb Jbra; Jket lam x} = {Jket Jbra lam; ja x jb} and
+// {J1 J2 lam; x ja jd} read from the integer-row table, and
+// {jd jc Jket; jb x J2} from the widened compact table.
+IMSRG_HD double ninej_tensor(const DevTensor& T, int lam, int ja, int jb, int jc, int jd, int J1, int J2, int Jbra,
+                             int Jket)
+{
+  int xlo = ja > 2 * lam ? ja - 2 * lam : 2 * lam - ja;  // doubled x: |ja - lam| .. ja + lam
+  int xhi = ja + 2 * lam;
+  double s = 0.0;
+  for (int x = xlo; x <= xhi; x += 2) {
+    double a = sixjA_get(T.sixjA, T.NJ, T.d1x, Jket, Jbra, ja, x, jb);
+    if (a == 0.0) continue;
+    double b = sixj_compact_get(T.sixjx_base, T.sixjx_val, T.d1x, jd, jc, Jket, jb, x, J2);
+    if (b == 0.0) continue;
+    double c = sixjA_get(T.sixjA, T.NJ, T.d1x, J1, J2, x, ja, jd);
+    s -= (x + 1) * a * b * c;  // (-1)^(2x) = -1 for half-integer x
+  }
+  return s;
+}
+
+}  // namespace imsrg

@@ -127,6 +127,32 @@ void imsrg_op_destroy(imsrg_op* op);
 int imsrg_op_hermiticity(const imsrg_op* op, int* h);
 int imsrg_op_set_hermiticity(imsrg_op* op, int h);
 
+/* Reduced tensor operator of rank lam (J), trank (|delta Tz|, 0 or 1) and
+ * parity (0, 1), zero-filled: Operator(ms, lam, trank, parity, 2)
+ * (src/Operator.cc:65-84) with reduced matrix elements.  Its arena: ZeroBody
+ * at [0], OneBody N x N column-major at [32] (<i||T||j>, nonzero where
+ * Operator::SetUpOneBodyChannels allows), then every TwoBodyME block
+ * (ch_bra <= ch_ket allowed by the rank, in TwoBodyME::Allocate order,
+ * src/TwoBodyME.cc:77-95) n_bra x n_ket column-major, each on a multiple of 32
+ * doubles (imsrg_space_tensor_layout).  Blocks with ch_bra > ch_ket are the
+ * conjugates: <a|T|b> = h (-1)^(J_bra - J_ket) <b|T|a>.  Upload, download,
+ * zero, copy, scale and axpy take tensor operators like scalar ones (copy and
+ * axpy between equal ranks); norm, random fill, files, BCH and the flow take
+ * scalar operators only. */
+int imsrg_op_create_tensor(imsrg_space* s, int lam, int trank, int parity, int hermiticity, imsrg_op** out);
+/* rank of an operator (0, 0, 0 for scalars) and its arena length in doubles */
+int imsrg_op_rank(const imsrg_op* op, int* lam, int* trank, int* parity, long long* arena_len);
+/* Tensor arena layout of rank (lam, trank, parity): number of two-body blocks
+ * and total length; for block >= 0 also its channels and offset. */
+int imsrg_space_tensor_layout(imsrg_space* s, int lam, int trank, int parity, int block, int* ch_bra, int* ch_ket,
+                              long long* offset, int* nblocks, long long* total);
+/* 9j symbol {ja/2 jd/2 J1; jb/2 jc/2 J2; Jbra Jket lam} (half-integers
+ * doubled) as the scalar-tensor kernels evaluate it: a sum over three 6j
+ * symbols from the space's tables (AngMom::NineJ's counterpart,
+ * src/AngMom.cc:96-104). */
+int imsrg_space_ninej(imsrg_space* s, int lam, int ja, int jd, int J1, int jb, int jc, int J2, int Jbra, int Jket,
+                      double* out);
+
 /* Host <-> device copies of the whole arena (arena_len doubles). */
 int imsrg_op_upload(imsrg_op* op, const double* host, void* stream);
 int imsrg_op_download(const imsrg_op* op, double* host, void* stream);
@@ -199,6 +225,24 @@ int imsrg_comm222_pp_hhss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int
 int imsrg_comm222_pp_hh_221ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream);
 /* Commutator::comm222_phss, src/Commutator.cc:1681-1823 */
 int imsrg_comm222_phss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream);
+
+/* ------------------------------------------------------- scalar-tensor */
+/* Commutator::CommutatorScalarTensor (src/Commutator.cc:432-500) in IMSRG(2):
+ * Z = [X, Y] for X scalar and Y a reduced tensor; Z, a tensor operator of Y's
+ * rank, is overwritten and its hermiticity set from X and Y.  FP64 throughout. */
+int imsrg_commutator_scalar_tensor(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
+/* its terms, each accumulating into Z (src/TensorCommutators.cc) */
+/* comm111st, src/TensorCommutators.cc:25-30 */
+int imsrg_comm111st(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
+/* comm121st, src/TensorCommutators.cc:46-150 */
+int imsrg_comm121st(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
+/* comm122st, src/TensorCommutators.cc:158-312 */
+int imsrg_comm122st(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
+/* comm222_pp_hh_221st, src/TensorCommutators.cc:314-495 */
+int imsrg_comm222_pp_hh_221st(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
+/* comm222_phst, src/TensorCommutators.cc:1059-1386, with the tensor Pandya
+ * transforms of :637-752 and :754-920 */
+int imsrg_comm222_phst(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
 
 /* Commutator::DoPandyaTransformation(Z, TwoBody_CC_ph, orientation),
  * src/Commutator.cc:1319-1390,1487-1497: the Pandya (particle-hole) transform

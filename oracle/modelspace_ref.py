@@ -189,6 +189,84 @@ class RefModelSpace:
         a[self.off2[0]:] *= v2
         return a
 
+    # ---- tensor operators (rank_J = lam, rank_T = trank, parity) -------------
+    def tensor_blocks(self, lam, trank, parity):
+        """Two-body blocks of a tensor operator in TwoBodyME::Allocate order
+        (src/TwoBodyME.cc:77-95): (ch_bra, ch_ket), ch_bra <= ch_ket, with
+        |J_bra - J_ket| <= lam <= J_bra + J_ket, |Tz_bra - Tz_ket| = trank and
+        parity_bra + parity_ket + parity even."""
+        out = []
+        for cb in range(self.nch):
+            Jb, pb, Tb, _ = self.channels[cb]
+            for ck in range(cb, self.nch):
+                Jk, pk, Tk, _ = self.channels[ck]
+                if abs(Jb - Jk) > lam or Jb + Jk < lam:
+                    continue
+                if abs(Tb - Tk) != trank:
+                    continue
+                if (pb + pk + parity) % 2:
+                    continue
+                out.append((cb, ck))
+        return out
+
+    def tensor_layout(self, lam, trank, parity):
+        """Arena of a tensor operator: ZeroBody at [0], OneBody N x N at [32],
+        then every block of tensor_blocks (n_bra x n_ket, column-major), each
+        starting on a multiple of 32 doubles.  Returns (blocks, offsets, size)."""
+        blocks = self.tensor_blocks(lam, trank, parity)
+        cur = _round32(32 + self.norb * self.norb)
+        offs = []
+        for cb, ck in blocks:
+            offs.append(cur)
+            cur = _round32(cur + len(self.channels[cb][3]) * len(self.channels[ck][3]))
+        return blocks, offs, cur
+
+    def tensor_onebody_allowed(self, i, j, lam, trank, parity):
+        """<i||T||j> allowed by Operator::SetUpOneBodyChannels (src/Operator.cc:248-291)."""
+        if (self.l[i] + self.l[j] + parity) % 2:
+            return False
+        if abs(self.j2[i] - self.j2[j]) > 2 * lam or self.j2[i] + self.j2[j] < 2 * lam:
+            return False
+        return abs(self.tz2[i] - self.tz2[j]) == 2 * trank
+
+    def random_tensor(self, seed, lam, trank, parity, hermitian=True):
+        """Seeded random reduced tensor operator in the tensor_layout arena:
+        uniform[-1,1] on allowed elements; one-body <j||T||i> = h (-1)^(ji-jj)
+        <i||T||j> (the reduced-element conjugation of Operator's one-body part);
+        diagonal two-body blocks (ch, ch) symmetric (h = 1) or antisymmetric;
+        every block and the one-body matrix scaled to unit Frobenius norm."""
+        rng = np.random.Generator(np.random.PCG64(seed))
+        blocks, offs, size = self.tensor_layout(lam, trank, parity)
+        a = np.zeros(size)
+        h = 1.0 if hermitian else -1.0
+        N = self.norb
+        one = a[32:32 + N * N].reshape(N, N, order="F")
+        for i in range(N):
+            for j in range(i, N):
+                if not self.tensor_onebody_allowed(i, j, lam, trank, parity):
+                    continue
+                ph = -1.0 if ((self.j2[i] - self.j2[j]) // 2) % 2 else 1.0
+                if i == j and h * ph < 0:
+                    continue
+                v = rng.uniform(-1, 1)
+                one[i, j] = v
+                one[j, i] = h * ph * v
+        nrm = np.linalg.norm(one)
+        if nrm > 0:
+            one /= nrm
+        for (cb, ck), o in zip(blocks, offs):
+            nb, nk = len(self.channels[cb][3]), len(self.channels[ck][3])
+            if nb == 0 or nk == 0:
+                continue
+            R = rng.uniform(-1, 1, size=(nb, nk))
+            if cb == ck:
+                R = 0.5 * (R + h * R.T)
+            f = np.linalg.norm(R)
+            if f > 0:
+                R /= f
+            a[o:o + nb * nk] = R.ravel(order="F")
+        return a
+
     def norm(self, arena):
         """Operator::Norm for a scalar operator (src/Operator.cc:1610-1651,
         src/TwoBodyME.cc:703-723)."""

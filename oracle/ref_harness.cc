@@ -170,6 +170,79 @@ static void dump_tables(ModelSpace& ms, const std::string& path) {
 
 typedef void (*term_fn)(const Operator&, const Operator&, Operator&);
 
+static size_t tensor_total(const Operator& op, size_t n_orb) {
+  size_t cur = round32(32 + n_orb * n_orb);
+  for (auto& it : op.TwoBody.MatEl) cur = round32(cur + it.second.n_elem);
+  return cur;
+}
+
+static void load_tensor(Operator& op, const std::vector<double>& a, size_t n_orb) {
+  op.ZeroBody = a[0];
+  for (size_t c = 0; c < n_orb; ++c)
+    for (size_t r = 0; r < n_orb; ++r) op.OneBody(r, c) = a[32 + c * n_orb + r];
+  size_t cur = round32(32 + n_orb * n_orb);
+  for (auto& it : op.TwoBody.MatEl) {
+    arma::mat& M = it.second;
+    for (size_t e = 0; e < M.n_elem; ++e) M.memptr()[e] = a[cur + e];
+    cur = round32(cur + M.n_elem);
+  }
+}
+
+static std::vector<double> store_tensor(const Operator& op, size_t n_orb) {
+  std::vector<double> a(tensor_total(op, n_orb), 0.0);
+  a[0] = op.ZeroBody;
+  for (size_t c = 0; c < n_orb; ++c)
+    for (size_t r = 0; r < n_orb; ++r) a[32 + c * n_orb + r] = op.OneBody(r, c);
+  size_t cur = round32(32 + n_orb * n_orb);
+  for (auto& it : op.TwoBody.MatEl) {
+    const arma::mat& M = it.second;
+    for (size_t e = 0; e < M.n_elem; ++e) a[cur + e] = M.memptr()[e];
+    cur = round32(cur + M.n_elem);
+  }
+  return a;
+}
+
+static int tensor_main(int argc, char** argv) {
+  if (argc != 10) {
+    std::cerr << "usage: ref_harness tensor <emax> <lam> <trank> <parity> <herm> <X.bin> <T.bin> <outdir>\n";
+    return 1;
+  }
+  int emax = std::atoi(argv[2]), lam = std::atoi(argv[3]), trank = std::atoi(argv[4]), parity = std::atoi(argv[5]);
+  int herm = std::atoi(argv[6]);
+  std::string outdir = argv[9];
+  ModelSpace ms(emax, "O16", "O16");
+  ArenaLayout L = make_layout(ms);
+  size_t N = L.n_orb;
+  Operator X(ms, 0, 0, 0, 2);
+  X.SetHermitian();
+  load(X, read_file(argv[7], L.total), L);
+  Operator T(ms, lam, trank, parity, 2);
+  if (herm > 0) T.SetHermitian(); else T.SetAntiHermitian();
+  load_tensor(T, read_file(argv[8], tensor_total(T, N)), N);
+  {
+    std::ofstream bf(outdir + "/tensor_blocks.txt");
+    for (auto& it : T.TwoBody.MatEl)
+      bf << it.first[0] << " " << it.first[1] << " " << it.second.n_rows << " " << it.second.n_cols << "\n";
+  }
+  struct Term { const char* name; term_fn fn; };
+  const Term terms[] = {
+      {"comm111st", Commutator::comm111st},
+      {"comm121st", Commutator::comm121st},
+      {"comm122st", Commutator::comm122st},
+      {"comm222_pp_hh_221st", Commutator::comm222_pp_hh_221st},
+      {"comm222_phst", Commutator::comm222_phst},
+  };
+  for (const Term& t : terms) {
+    Operator Z(ms, lam, trank, parity, 2);
+    if (herm > 0) Z.SetAntiHermitian(); else Z.SetHermitian();
+    t.fn(X, T, Z);
+    write_file(outdir + "/st_" + t.name + ".bin", store_tensor(Z, N));
+  }
+  Operator Zf = Commutator::CommutatorScalarTensor(X, T);
+  write_file(outdir + "/st_full.bin", store_tensor(Zf, N));
+  return 0;
+}
+
 static int flow_main(int argc, char** argv) {
   if (argc != 8) {
     std::cerr << "usage: ref_harness flow <emax> <H.bin> <A.bin> <B.bin> <nsteps> <outdir>\n";
@@ -246,6 +319,7 @@ static int flow_main(int argc, char** argv) {
 
 int main(int argc, char** argv) {
   if (argc > 1 && std::string(argv[1]) == "flow") return flow_main(argc, argv);
+  if (argc > 1 && std::string(argv[1]) == "tensor") return tensor_main(argc, argv);
   if (argc != 6) {
     std::cerr << "usage: ref_harness <emax> <X.bin> <Y.bin> <W.bin> <outdir>\n";
     return 1;

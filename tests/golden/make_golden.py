@@ -29,6 +29,14 @@ Fixtures (arena layout: see oracle/modelspace_ref.py):
                      the final H(s), Omega; an adaptive flow to s = 2 with Omega
                      split at |Omega| > 0.3 (final s, number of Omegas, E0,
                      H(s), last Omega).
+  golden_tensor_emax2.npz, golden_tensor_emax3.npz
+                     Commutator::CommutatorScalarTensor [X, T] and its five
+                     IMSRG(2) terms (comm111st, comm121st, comm122st,
+                     comm222_pp_hh_221st, comm222_phst) for X a random hermitian
+                     scalar and T random reduced tensors (RefModelSpace.
+                     random_tensor) of rank (J, T, parity) = (2, 0, 0)
+                     hermitian, (1, 0, 1) hermitian and (1, 1, 0)
+                     anti-hermitian at emax 2; the first case only at emax 3.
   sixj_exact.npz     6j symbols {j1 j2 J3; j4 j5 J6} for half-integer
                      j <= 9/2 and integer J <= 9, evaluated in exact rational
                      arithmetic (Racah formula with Python integers), the pin for
@@ -115,6 +123,32 @@ def run_reference_flow(emax):
     return out
 
 
+TENSOR_CASES = {"e2": (2, 0, 0, 1), "e1": (1, 0, 1, 1), "gt": (1, 1, 0, -1)}
+TENSOR_TERMS = ["comm111st", "comm121st", "comm122st", "comm222_pp_hh_221st", "comm222_phst", "full"]
+
+
+def run_reference_tensor(emax, cases):
+    ms = RefModelSpace(emax)
+    X = ms.random_operator(1000 + emax, hermitian=True)
+    harness = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+    out = {"X": X, "emax": np.array(emax)}
+    with tempfile.TemporaryDirectory() as td:
+        X.tofile(os.path.join(td, "X.bin"))
+        for i, name in enumerate(cases):
+            lam, trank, par, herm = TENSOR_CASES[name]
+            T = ms.random_tensor(8000 + 10 * emax + i, lam, trank, par, hermitian=herm > 0)
+            T.tofile(os.path.join(td, "T.bin"))
+            subprocess.run([harness, "tensor", str(emax), str(lam), str(trank), str(par), str(herm),
+                            os.path.join(td, "X.bin"), os.path.join(td, "T.bin"), td], check=True,
+                           stdout=subprocess.DEVNULL, env=dict(os.environ, OMP_NUM_THREADS="1"))
+            out[name + "_T"] = T
+            out[name + "_rank"] = np.array([lam, trank, par, herm])
+            for t in TENSOR_TERMS:
+                out["%s_%s" % (name, t)] = np.fromfile(os.path.join(td, "st_%s.bin" % t))
+            out[name + "_blocks"] = np.loadtxt(os.path.join(td, "tensor_blocks.txt"), dtype=np.int64).reshape(-1, 4)
+    return out
+
+
 def _delta2(a, b, c):
     # a, b, c doubled
     return Fraction(factorial((a + b - c) // 2) * factorial((a - b + c) // 2) * factorial((-a + b + c) // 2),
@@ -168,10 +202,12 @@ def main():
     np.savez_compressed(os.path.join(HERE, "golden_emax3.npz"), **g3)
     for e in (2, 3):
         np.savez_compressed(os.path.join(HERE, "golden_flow_emax%d.npz" % e), **run_reference_flow(e))
+    np.savez_compressed(os.path.join(HERE, "golden_tensor_emax2.npz"), **run_reference_tensor(2, ["e2", "e1", "gt"]))
+    np.savez_compressed(os.path.join(HERE, "golden_tensor_emax3.npz"), **run_reference_tensor(3, ["e2"]))
     keys, vals = make_sixj_table()
     np.savez_compressed(os.path.join(HERE, "sixj_exact.npz"), keys=keys, values=vals)
     for f in ("golden_emax2.npz", "golden_emax3.npz", "golden_flow_emax2.npz", "golden_flow_emax3.npz",
-              "sixj_exact.npz"):
+              "golden_tensor_emax2.npz", "golden_tensor_emax3.npz", "sixj_exact.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 
@@ -179,6 +215,10 @@ if __name__ == "__main__":
     if sys.argv[1:] == ["--commutator"]:
         np.savez_compressed(os.path.join(HERE, "golden_emax2.npz"), **run_reference(2, ["xy", "yx", "xw"]))
         np.savez_compressed(os.path.join(HERE, "golden_emax3.npz"), **run_reference(3, ["xy"]))
+    elif sys.argv[1:] == ["--tensor"]:
+        np.savez_compressed(os.path.join(HERE, "golden_tensor_emax2.npz"),
+                            **run_reference_tensor(2, ["e2", "e1", "gt"]))
+        np.savez_compressed(os.path.join(HERE, "golden_tensor_emax3.npz"), **run_reference_tensor(3, ["e2"]))
     elif sys.argv[1:] == ["--flow"]:
         for e in (2, 3):
             np.savez_compressed(os.path.join(HERE, "golden_flow_emax%d.npz" % e), **run_reference_flow(e))

@@ -43,3 +43,26 @@ def ref_space(emax):
 
 def load_flow_golden(emax):
     return dict(np.load(os.path.join(GOLDEN, "golden_flow_emax%d.npz" % emax)))
+
+
+def load_tensor_golden(emax):
+    return dict(np.load(os.path.join(GOLDEN, "golden_tensor_emax%d.npz" % emax)))
+
+
+def tensor_rel_errors(ms, rank, Z, R):
+    """rel_errors for tensor arenas of rank (J, T, parity): one-body matrix and
+    the concatenated two-body blocks."""
+    blocks, offs, _ = ms.tensor_layout(*rank)
+
+    def parts(a):
+        N = ms.norb
+        two = [a[o:o + len(ms.channels[cb][3]) * len(ms.channels[ck][3])] for (cb, ck), o in zip(blocks, offs)]
+        return a[32:32 + N * N], np.concatenate(two) if two else np.zeros(0)
+
+    tot = max(np.linalg.norm(R), 1e-300)
+    out = []
+    for x, y in zip(parts(Z), parts(R)):
+        d = np.linalg.norm(x - y)
+        ny = np.linalg.norm(y)
+        out.append(d / ny if ny > 1e-12 * tot else d / tot)
+    return out

@@ -4,6 +4,9 @@ import ctypes
 import os
 import re
 
+import numpy as np
+import pytest
+
 import imsrg_gb300 as ig
 from imsrg_gb300 import _lib
 
@@ -45,3 +48,44 @@ def test_term_switch_roundtrip():
     assert not ig.Commutator.IsTermOn("comm122ss")
     ig.Commutator.TurnOnTerm("comm122ss")
     assert ig.Commutator.IsTermOn("comm122ss")
+
+
+def test_tensor_layout_matches_reference_rules():
+    # the C ABI's tensor arena layout equals the one the reference harness
+    # reads (TwoBodyME::Allocate order, 32-double alignment)
+    from modelspace_ref import RefModelSpace
+    for emax in (2, 3):
+        ms = ig.ModelSpace(emax, "O16", "O16")
+        r = RefModelSpace(emax)
+        for rank in ((2, 0, 0), (1, 0, 1), (1, 1, 0), (0, 0, 0), (3, 1, 1)):
+            blocks, offs, total = r.tensor_layout(*rank)
+            mine = ms.tensor_layout(*rank)
+            assert list(mine) == blocks and list(mine.values()) == offs
+            assert ms.tensor_size(*rank) == total
+
+
+def test_ninej_vs_exact():
+    # the 9j of the scalar-tensor kernels (a sum of three tabulated 6j) against
+    # SymPy's exact Racah-formula 9j, on argument sets that satisfy the triads
+    sympy = pytest.importorskip("sympy")
+    from sympy.physics.wigner import wigner_9j
+    R = sympy.Rational
+    ms = ig.ModelSpace(4, "O16", "O16")
+
+    def tri(a, b, c):  # doubled
+        return (a + b + c) % 2 == 0 and abs(a - b) <= c <= a + b
+
+    rng = np.random.default_rng(7)
+    n = 0
+    while n < 300:
+        ja, jb, jc, jd = (int(x) for x in rng.choice([1, 3, 5, 7, 9], 4))
+        lam = int(rng.integers(0, 4))
+        J1 = int(rng.integers(0, 10)); J2 = int(rng.integers(0, 10))
+        Jb = int(rng.integers(0, 10)); Jk = int(rng.integers(0, 10))
+        if not (tri(ja, jd, 2 * J1) and tri(jb, jc, 2 * J2) and tri(2 * Jb, 2 * Jk, 2 * lam) and tri(ja, jb, 2 * Jb)
+                and tri(jd, jc, 2 * Jk) and tri(2 * J1, 2 * J2, 2 * lam)):
+            continue
+        n += 1
+        v = ms.GetNineJ(ja / 2, jd / 2, J1, jb / 2, jc / 2, J2, Jb, Jk, lam)
+        ref = float(wigner_9j(R(ja, 2), R(jd, 2), J1, R(jb, 2), R(jc, 2), J2, Jb, Jk, lam, prec=None))
+        assert abs(v - ref) < 1e-14, (ja, jd, J1, jb, jc, J2, Jb, Jk, lam, v, ref)

@@ -1,0 +1,76 @@
+"""Scalar-tensor commutator [X, T] (X scalar, T a reduced tensor) on the GPU
+through the C ABI, against the reference's own outputs
+(golden_tensor_emax*.npz, from Commutator::CommutatorScalarTensor and its
+terms, src/TensorCommutators.cc).  Tensor ranks (J, |dTz|, parity): (2, 0, 0)
+hermitian, (1, 0, 1) hermitian, (1, 1, 0) anti-hermitian.  FP64 throughout;
+tolerance 1e-12 relative Frobenius per body rank."""
+import numpy as np
+import pytest
+
+import imsrg_gb300 as ig
+from helpers import load_tensor_golden, ref_space, tensor_rel_errors
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+TERMS = ["comm111st", "comm121st", "comm122st", "comm222_pp_hh_221st", "comm222_phst"]
+CASES = [(2, "e2"), (2, "e1"), (2, "gt"), (3, "e2")]
+
+
+def setup(emax, case):
+    g = load_tensor_golden(emax)
+    lam, trank, par, herm = (int(x) for x in g[case + "_rank"])
+    ms = ig.ModelSpace(emax, "O16", "O16")
+    dX = ig.DeviceOperator(ms, 1)
+    dX.upload(g["X"])
+    dT = ig.DeviceOperator(ms, herm, (lam, trank, par))
+    dT.upload(g[case + "_T"])
+    return g, ms, dX, dT, (lam, trank, par), herm
+
+
+@pytest.mark.parametrize("emax,case", CASES)
+@pytest.mark.parametrize("term", TERMS)
+def test_tensor_term_vs_reference(emax, case, term):
+    g, ms, dX, dT, rank, herm = setup(emax, case)
+    hz = -1 if herm == 1 else 1
+    with ig.DeviceOperator(ms, hz, rank) as dZ:
+        ig.Commutator.device_tensor_term(term, dX, dT, dZ)
+        Z = dZ.download()
+    R = g["%s_%s" % (case, term)]
+    errs = tensor_rel_errors(ref_space(emax), rank, Z, R)
+    assert max(errs) < TOL, (term, errs)
+
+
+@pytest.mark.parametrize("emax,case", CASES)
+def test_commutator_scalar_tensor_vs_reference(emax, case):
+    g, ms, dX, dT, rank, herm = setup(emax, case)
+    with ig.DeviceOperator(ms, 1, rank) as dZ:
+        dZ.upload(np.full(dZ.size, 3.0))  # overwritten
+        ig.Commutator.device_scalar_tensor(dX, dT, dZ)
+        assert dZ.hermiticity == (-1 if herm == 1 else 1)
+        Z = dZ.download()
+    errs = tensor_rel_errors(ref_space(emax), rank, Z, g[case + "_full"])
+    assert max(errs) < TOL, errs
+
+
+def test_host_api_dispatch():
+    # Commutator.Commutator dispatches on rank; [T, S] = -[S, T]
+    g = load_tensor_golden(2)
+    ms = ig.ModelSpace(2, "O16", "O16")
+    X = ig.Operator(ms, arena=g["X"], hermitian=True)
+    T = ig.Operator(ms, 2, 0, 0, 2, arena=g["e2_T"], hermitian=True)
+    Z = ig.Commutator.Commutator(X, T)
+    assert Z.rank == (2, 0, 0) and Z.IsAntiHermitian()
+    assert max(tensor_rel_errors(ref_space(2), (2, 0, 0), Z.arena, g["e2_full"])) < TOL
+    W = ig.Commutator.Commutator(T, X)
+    assert np.allclose(W.arena, -Z.arena, rtol=0, atol=1e-15)
+
+
+def test_tensor_rejected_by_scalar_paths():
+    ms = ig.ModelSpace(2, "O16", "O16")
+    with ig.DeviceOperator(ms, 1) as dX, ig.DeviceOperator(ms, 1, (2, 0, 0)) as dT, \
+            ig.DeviceOperator(ms, -1) as dZ:
+        with pytest.raises(ig.IMSRGError):
+            ig.Commutator.device_commutator(dX, dT, dZ)
+        with pytest.raises(ig.IMSRGError):
+            dT.norm()
