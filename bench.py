@@ -32,6 +32,10 @@ on the data path).
 the pairs replayed as one CUDA graph (imsrg_batch_*, split form), beside the
 same pairs as 64 sequential single-pair calls, and both in FP64.
 
+--workload tensor: the scalar-tensor commutator [X, T] (X hermitian scalar, T a
+random hermitian reduced tensor of rank J=2, |dTz|=0, parity + (an E2-like
+operator)) at emax=8 by default, FP64; value = ms per commutator.
+
 --workload flow: the synthetic Magnus flow instead (IMSRGSolver,
 magnus_euler, White generator, fixed ds = 0.5, no Omega split) at emax=12 by
 default: H has one-body diagonal 2n+l+3/2, off-diagonal uniform[-0.1,0.1]
@@ -66,7 +70,7 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--emax", type=int, default=None, help="default 10 (commutator), 12 (flow)")
-    p.add_argument("--workload", default="commutator", choices=["commutator", "flow", "batch"])
+    p.add_argument("--workload", default="commutator", choices=["commutator", "flow", "batch", "tensor"])
     p.add_argument("--pairs", type=int, default=64, help="batch workload: independent (X, Y) pairs")
     p.add_argument("--fp64-steps", type=int, default=None, help="flow steps timed in the FP64 form")
     p.add_argument("--precision", default="split", choices=["split", "fp64"])
@@ -745,10 +749,112 @@ def run_batch(args):
     print(json.dumps(out))
 
 
+TENSOR_METRIC = "ms per scalar-tensor commutator [X,T], rank (J,dTz,parity)=(2,0,+), emax={emax}, FP64, 1 GB300"
+
+
+def random_tensor(ms, seed, rank, hermitian=True):
+    """Seeded random reduced tensor in the C ABI's tensor arena (uniform[-1,1]
+    on allowed elements, unit Frobenius norm per block and for the one-body
+    matrix, <j||T||i> = h (-1)^(ji-jj) <i||T||j>, diagonal blocks (anti)symmetric)."""
+    import numpy as np
+    lam, trank, par = rank
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = np.zeros(ms.tensor_size(*rank))
+    h = 1.0 if hermitian else -1.0
+    N = ms.norb
+    orb = ms.orbits
+    one = a[32:32 + N * N].reshape(N, N, order="F")
+    for i in range(N):
+        for j in range(i, N):
+            li, ji, ti = orb[i][1], orb[i][2], orb[i][3]
+            lj, jj, tj = orb[j][1], orb[j][2], orb[j][3]
+            if (li + lj + par) % 2 or abs(ji - jj) > 2 * lam or ji + jj < 2 * lam or abs(ti - tj) != 2 * trank:
+                continue
+            ph = -1.0 if ((ji - jj) // 2) % 2 else 1.0
+            if i == j and h * ph < 0:
+                continue
+            v = rng.uniform(-1, 1)
+            one[i, j] = v
+            one[j, i] = h * ph * v
+    one /= max(np.linalg.norm(one), 1e-300)
+    for (cb, ck), o in ms.tensor_layout(*rank).items():
+        nb, nk = ms.channels[cb]["nkets"], ms.channels[ck]["nkets"]
+        if nb == 0 or nk == 0:
+            continue
+        R = rng.uniform(-1, 1, size=(nb, nk))
+        if cb == ck:
+            R = 0.5 * (R + h * R.T)
+        a[o:o + nb * nk] = (R / max(np.linalg.norm(R), 1e-300)).ravel(order="F")
+    return a
+
+
+def run_tensor(args):
+    import torch
+
+    import imsrg_gb300 as ig
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    L = ig.lib()
+    emax = args.emax
+    ms = ig.ModelSpace(emax, "O16", "O16")
+    rk = (2, 0, 0)
+    dX = ig.DeviceOperator(ms, 1)
+    dX.fill_random(31 + rank)
+    dT = ig.DeviceOperator(ms, 1, rk)
+    dT.upload(random_tensor(ms, 41 + rank, rk))
+    dZ = ig.DeviceOperator(ms, 1, rk)
+    for _ in range(max(3, args.warmup)):
+        ig.Commutator.device_scalar_tensor(dX, dT, dZ)
+    torch.cuda.synchronize()
+    L.imsrg_profiler_reset()
+    L.imsrg_profiler_enable(1)
+    l0 = L.imsrg_kernel_launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        ig.Commutator.device_scalar_tensor(dX, dT, dZ)
+    e1.record()
+    torch.cuda.synchronize()
+    launches = L.imsrg_kernel_launches() - l0
+    L.imsrg_profiler_enable(0)
+    n = L.imsrg_profiler_names(None, 0)
+    buf = ctypes.create_string_buffer(n)
+    L.imsrg_profiler_names(buf, n)
+    phases = {}
+    for name in [x for x in buf.value.decode().split("\n") if x]:
+        t = ctypes.c_double()
+        c = ctypes.c_longlong()
+        L.imsrg_profiler_get(name.encode(), ctypes.byref(t), ctypes.byref(c))
+        phases[name] = t.value / args.steps
+    ms_step = e0.elapsed_time(e1) / args.steps
+    if rank != 0:
+        return
+    out = {
+        "metric": TENSOR_METRIC.format(emax=emax), "value": ms_step, "unit": "ms/commutator", "n_gpus": world,
+        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_step, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "CommutatorScalarTensor [X, T], X random hermitian scalar, T random hermitian "
+                               "reduced tensor of rank (2, 0, 0), emax=%d O16" % emax, "emax": emax,
+                   "tensor_arena_doubles": dT.size},
+        "phases_ms_per_step": phases, "gpu_launches": int(launches),
+        "cpu_baseline": {"value": None, "unit": "ms/commutator", "kind": "port",
+                         "sample": "not measured: the C oracle restates the scalar-scalar path only"},
+    }
+    print(json.dumps(out))
+
+
 def main():
     args = parse_args()
     if args.emax is None:
-        args.emax = 12 if args.workload == "flow" else 10
+        args.emax = {"flow": 12, "tensor": 8}.get(args.workload, 10)
+    if args.workload == "tensor":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference's scalar-tensor commutator is not "
+                              "built for the GPU host; the headline reference arm is the emax=10 commutator"}))
+            return
+        run_tensor(args)
+        return
     if args.workload == "batch":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the batch workload compares the GPU's batched "
