@@ -1051,11 +1051,11 @@ int status_dev(imsrg_space* sp, cudaStream_t st) { return check_status(sp, st); 
 }  // namespace imsrg
 
 // ------------------------------------------------------------- batch phases
-// CommutatorScalarScalar in the split form cut at its two dense products, so
-// a batch can run the products of many pairs as one launch each (see
-// capi_batch.cu): pre (Z zeroed, operand preparation, the zero- and one-body
-// terms), the ladder product, mid (comm221ss, comm122ss), the Zbar product,
-// post (inverse Pandya transform).  Every term must be on.
+// CommutatorScalarScalar in the split form for a group of pairs of the same
+// structure, every kernel launched once for all of them (see capi_batch.cu):
+// pre (Z zeroed, operand preparation, the zero- and one-body terms), the
+// ladder product, mid (comm221ss, comm122ss), the Zbar product, post (inverse
+// Pandya transform).  Every term must be on.
 namespace imsrg {
 
 bool batch_phases_usable()
@@ -1064,38 +1064,6 @@ bool batch_phases_usable()
   for (int t = 0; t < NTERMS; ++t)
     if (!g_term_on[t]) return false;
   return true;
-}
-
-int batch_pre(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
-{
-  Z->herm = z_herm(X->herm, Y->herm);
-  int rc = check_ops(X, Y, Z);
-  if (rc) return rc;
-  CUDA_TRY(cudaMemsetAsync(Z->d, 0, X->sp->s->arena * sizeof(double), st));
-  if ((rc = prep_122_df(X, Y, st)) || (rc = prep_ph(X, Y, st)) || (rc = do_111_110(X, Y, Z, true, true, st)) ||
-      (rc = do_220(X, Y, Z, st)) || (rc = do_121(X, Y, Z, st)))
-    return rc;
-  return IMSRG_OK;
-}
-
-int batch_mid(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
-{
-  int rc = do_221_1b(X, Y, Z, st, Z->d);
-  if (!rc) rc = do_122(X, Y, Z, st, IMSRG_PREC_SPLIT, true);
-  return rc;
-}
-
-int batch_post(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
-{
-  (void)Y;
-  imsrg_space* sp = X->sp;
-  Space& s = *sp->s;
-  if (sp->n_invq > 0)
-    CUDA_TRY(launch_pandya_inv_ff(s, sp->d_zb, Z->d, Z->herm, sp->d_invq, sp->n_invq, sp->d_cls_list, sp->d_cls_off,
-                                  sp->d_cls_sort, s.invq_smem, st));
-  else
-    CUDA_TRY(launch_pandya_inv(s, sp->d_zb, Z->d, Z->herm, sp->d_pinv, sp->n_pinv, st));
-  return IMSRG_OK;
 }
 
 // Products of several pairs whose spaces have the same structure (equal
@@ -1111,12 +1079,18 @@ struct GroupedProducts {
   std::vector<imsrg_op*> Z;
   SplitPlan* ladder = nullptr;
   SplitPlan* zbar = nullptr;
+  // byte offsets of every pair's operands and scratch from pair 0's, for
+  // the grouped launches of the other kernels (kZRoles per pair)
+  long long* d_zoff = nullptr;
   ~GroupedProducts()
   {
     if (ladder) split_plan_destroy(ladder);
     if (zbar) split_plan_destroy(zbar);
+    if (d_zoff) cudaFree(d_zoff);
   }
 };
+
+static long long bdist(const void* a, const void* b) { return (long long)(intptr_t)a - (long long)(intptr_t)b; }
 
 static long long dist(const void* a, const void* b)
 {
@@ -1160,15 +1134,88 @@ GroupedProducts* grouped_products_create(const std::vector<const imsrg_op*>& X, 
   g->X = X;
   g->Y = Y;
   g->Z = Z;
+  std::vector<long long> zo;
+  for (size_t p = 0; p < X.size(); ++p) {
+    imsrg_space* sp = X[p]->sp;
+    long long r[kZRoles];
+    r[ZR_X] = bdist(X[p]->d, X[0]->d);
+    r[ZR_Y] = bdist(Y[p]->d, Y[0]->d);
+    r[ZR_Z] = bdist(Z[p]->d, Z[0]->d);
+    r[ZR_XF] = bdist(sp->d_xf, s0->d_xf);
+    r[ZR_YF] = bdist(sp->d_yff, s0->d_yff);
+    r[ZR_W2] = bdist(sp->d_w2, s0->d_w2);
+    r[ZR_XB] = bdist(sp->d_xb, s0->d_xb);
+    r[ZR_YT] = bdist(sp->d_yt, s0->d_yt);
+    r[ZR_YFL] = bdist(sp->d_yf, s0->d_yf);
+    r[ZR_ZB] = bdist(sp->d_zb, s0->d_zb);
+    zo.insert(zo.end(), r, r + kZRoles);
+  }
   try {
     g->ladder = split_plan_create(*s0->s, lj, 0);
     g->zbar = split_plan_create(*s0->s, zj, 1);
+    g->d_zoff = dcopy(zo);
   } catch (std::exception& e) {
     if (why) *why = std::string("grouped product plans: ") + e.what();
     delete g;
     return nullptr;
   }
   return g;
+}
+
+// the per-pair phases of a group as one launch per kernel (the grid's z is the pair)
+int group_pre(GroupedProducts* g, cudaStream_t st)
+{
+  const int nz = (int)g->X.size();
+  for (int p = 0; p < nz; ++p) {
+    imsrg_space* sp = g->X[p]->sp;
+    g->Z[p]->herm = z_herm(g->X[p]->herm, g->Y[p]->herm);
+    CUDA_TRY(cudaMemsetAsync(g->Z[p]->d, 0, sp->s->arena * sizeof(double), st));
+    for (auto& zr : sp->zbar_zero) CUDA_TRY(cudaMemsetAsync(sp->d_zb + zr.first, 0, zr.second * sizeof(double), st));
+  }
+  const imsrg_op *X = g->X[0], *Y = g->Y[0];
+  imsrg_op* Z = g->Z[0];
+  imsrg_space* sp = X->sp;
+  const Space& s = *sp->s;
+  const long long* zo = g->d_zoff;
+  CUDA_TRY(launch_to_ff(s, X->d, sp->d_xf, st, zo, nz, ZR_X, ZR_XF));
+  CUDA_TRY(launch_to_ff(s, Y->d, sp->d_yff, st, zo, nz, ZR_Y, ZR_YF));
+  CUDA_TRY(launch_pandya_fwd(s, X->d, Y->d, Y->herm, sp->d_xb, sp->d_yt, sp->d_yf, sp->d_pfwd, sp->n_pfwd, st, zo, nz));
+  CUDA_TRY(launch_comm111_110(s, X->d, Y->d, Z->d, true, X->herm != Y->herm, st, zo, nz));
+  if (X->herm != Y->herm) CUDA_TRY(launch_comm220(s, X->d, Y->d, Z->d, X->herm, st, zo, nz));
+  CUDA_TRY(launch_comm121(s, sp->d_holes, X->d, Y->d, Z->d, Z->herm, st, zo, nz));
+  return IMSRG_OK;
+}
+
+int group_mid(GroupedProducts* g, cudaStream_t st)
+{
+  const int nz = (int)g->X.size();
+  const imsrg_op *X = g->X[0], *Y = g->Y[0];
+  imsrg_op* Z = g->Z[0];
+  imsrg_space* sp = X->sp;
+  const Space& s = *sp->s;
+  const long long* zo = g->d_zoff;
+  CUDA_TRY(launch_comm221_1b(s, X->d, Y->d, Z->d, X->herm, Z->herm, Z->d, st, zo, nz));
+  CUDA_TRY(launch_comm122_df(s, X->d, Y->d, Z->d, sp->d_xf, sp->d_yff, (float2*)sp->d_w2, Z->herm, sp->d_sym122,
+                             sp->n_sym122, st, zo, nz));
+  return IMSRG_OK;
+}
+
+int group_post(GroupedProducts* g, cudaStream_t st)
+{
+  const int nz = (int)g->X.size();
+  imsrg_op* Z = g->Z[0];
+  imsrg_space* sp = g->X[0]->sp;
+  const Space& s = *sp->s;
+  if (sp->n_invq > 0) {
+    CUDA_TRY(launch_pandya_inv_ff(s, sp->d_zb, Z->d, Z->herm, sp->d_invq, sp->n_invq, sp->d_cls_list, sp->d_cls_off,
+                                  sp->d_cls_sort, s.invq_smem, st, g->d_zoff, nz));
+  } else {
+    for (int p = 0; p < nz; ++p) {
+      imsrg_space* q = g->X[p]->sp;
+      CUDA_TRY(launch_pandya_inv(*q->s, q->d_zb, g->Z[p]->d, g->Z[p]->herm, q->d_pinv, q->n_pinv, st));
+    }
+  }
+  return IMSRG_OK;
 }
 
 void grouped_products_destroy(GroupedProducts* g) { delete g; }

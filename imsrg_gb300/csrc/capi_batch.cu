@@ -4,13 +4,12 @@
 // commutators at small emax (a few microseconds of work per kernel).
 //
 // Two graph shapes:
-//  - grouped (split form, every term on, one model space per pair): the
-//    commutator runs in five stages; the per-pair stages (operand preparation
-//    and small terms; comm221ss and comm122ss; the inverse Pandya transform)
-//    run as one branch per pair, and each of the two dense products runs as
-//    one persistent launch per group of same-structure pairs, so the tiles of
-//    every pair share one grid instead of each pair's product taking every SM
-//    in turn;
+//  - grouped (split form, every term on, one model space per pair): pairs of
+//    the same structure form a group, and each group is one chain of
+//    launches in which every kernel of the commutator runs once for all the
+//    group's pairs (the grid's z runs over pairs; the two dense products are
+//    one persistent grid over the tiles of every pair), so the pairs share
+//    the GPU inside each launch instead of taking it in turn;
 //  - branches (otherwise): pairs grouped by model space (a space's scratch
 //    serialises the pairs that share it), one branch per space running whole
 //    commutators.
@@ -69,46 +68,22 @@ int berr(int code, const std::string& msg) { return set_error(code, msg.c_str())
     if (_e != cudaSuccess) return berr(IMSRG_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
   } while (0)
 
-// grouped shape: per-pair stages fork one branch per pair (group g of the
-// branch shape holds exactly pair g), product stages one branch per structure
-// group; every stage joins back into the capture stream
-template <class F>
-int pair_stage(imsrg_batch* b, F fn)
-{
-  BATCH_CUDA(cudaEventRecord(b->fork, b->cap));
-  for (size_t g = 0; g < b->groups.size(); ++g) {
-    cudaStream_t s = b->streams[g];
-    BATCH_CUDA(cudaStreamWaitEvent(s, b->fork, 0));
-    const int i = b->groups[g][0];
-    int rc = fn(b->X[i], b->Y[i], b->Z[i], s);
-    if (rc) return rc;
-    BATCH_CUDA(cudaEventRecord(b->joins[g], s));
-    BATCH_CUDA(cudaStreamWaitEvent(b->cap, b->joins[g], 0));
-  }
-  return IMSRG_OK;
-}
-
-template <class F>
-int product_stage(imsrg_batch* b, F fn)
+// grouped shape: every structure group is one chain on its own stream --
+// the group's per-pair phases and products each as one launch over its pairs
+int record_grouped(imsrg_batch* b)
 {
   BATCH_CUDA(cudaEventRecord(b->fork, b->cap));
   for (size_t g = 0; g < b->products.size(); ++g) {
     cudaStream_t s = b->gstreams[g];
+    GroupedProducts* gp = b->products[g];
     BATCH_CUDA(cudaStreamWaitEvent(s, b->fork, 0));
-    int rc = fn(b->products[g], s);
-    if (rc) return rc;
+    int rc;
+    if ((rc = group_pre(gp, s)) || (rc = grouped_ladder(gp, s)) || (rc = group_mid(gp, s)) ||
+        (rc = grouped_zbar(gp, s)) || (rc = group_post(gp, s)))
+      return rc;
     BATCH_CUDA(cudaEventRecord(b->gjoins[g], s));
     BATCH_CUDA(cudaStreamWaitEvent(b->cap, b->gjoins[g], 0));
   }
-  return IMSRG_OK;
-}
-
-int record_grouped(imsrg_batch* b)
-{
-  int rc;
-  if ((rc = pair_stage(b, batch_pre)) || (rc = product_stage(b, grouped_ladder)) || (rc = pair_stage(b, batch_mid)) ||
-      (rc = product_stage(b, grouped_zbar)) || (rc = pair_stage(b, batch_post)))
-    return rc;
   return IMSRG_OK;
 }
 

@@ -29,12 +29,9 @@ int set_error(int code, const char* msg);
 int commutator_dev(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStream_t st);
 int norm_dev(const imsrg_op* op, double* out, cudaStream_t st);
 int status_dev(imsrg_space* sp, cudaStream_t st);
-// the split-form commutator cut at its two dense products, for batches:
-// usable only with every term switched on
+// the split-form commutator of a group of same-structure pairs, one launch
+// per kernel for the whole group: usable only with every term switched on
 bool batch_phases_usable();
-int batch_pre(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st);
-int batch_mid(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st);
-int batch_post(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st);
 // the ladder and Zbar products of same-structure pairs as one launch each
 struct GroupedProducts;
 GroupedProducts* grouped_products_create(const std::vector<const imsrg_op*>& X, const std::vector<const imsrg_op*>& Y,
@@ -42,6 +39,10 @@ GroupedProducts* grouped_products_create(const std::vector<const imsrg_op*>& X, 
 void grouped_products_destroy(GroupedProducts* g);
 int grouped_ladder(GroupedProducts* g, cudaStream_t st);
 int grouped_zbar(GroupedProducts* g, cudaStream_t st);
+// the per-pair phases of the same pairs as one launch per kernel
+int group_pre(GroupedProducts* g, cudaStream_t st);
+int group_mid(GroupedProducts* g, cudaStream_t st);
+int group_post(GroupedProducts* g, cudaStream_t st);
 }  // namespace imsrg
 
 struct imsrg_space {

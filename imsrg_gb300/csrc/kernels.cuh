@@ -19,29 +19,45 @@ struct GemmJobDev {
 };
 
 // kernels_terms.cu
+//
+// Launchers marked (grouped) also run nz pairs of the same structure at once
+// (batches): pair z's operands sit at byte offsets zo[z * kZRoles + role] from
+// the pointers passed (pair 0's); zo = nullptr, nz = 1 is one pair.
+enum ZRole { ZR_X, ZR_Y, ZR_Z, ZR_XF, ZR_YF, ZR_W2, ZR_XB, ZR_YT, ZR_YFL, ZR_ZB, kZRoles };
+// (grouped)
 cudaError_t launch_comm111_110(const Space& s, const double* X, const double* Y, double* Z, bool do111, bool do110,
-                               cudaStream_t st);
-cudaError_t launch_comm220(const Space& s, const double* X, const double* Y, double* Z, int hX, cudaStream_t st);
+                               cudaStream_t st, const long long* zo = nullptr, int nz = 1);
+// (grouped)
+cudaError_t launch_comm220(const Space& s, const double* X, const double* Y, double* Z, int hX, cudaStream_t st,
+                           const long long* zo = nullptr, int nz = 1);
+// (grouped)
 cudaError_t launch_comm121(const Space& s, const int* dev_holes, const double* X, const double* Y, double* Z, int hZ,
-                           cudaStream_t st);
+                           cudaStream_t st, const long long* zo = nullptr, int nz = 1);
+// (grouped with Mz)
 cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, double* Z, int hX, int hZ,
-                              const double* Mz, cudaStream_t st);
+                              const double* Mz, cudaStream_t st, const long long* zo = nullptr, int nz = 1);
 cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, double* Z, double* W2, int hZ,
                            const int* sym_tiles, int nsym_tiles, cudaStream_t st);
-// (hi, lo) float-pair copy of an arena (integer instructions)
-cudaError_t launch_to_ff(const Space& s, const double* A, float2* Af, cudaStream_t st);
+// (hi, lo) float-pair copy of an arena (integer instructions); (grouped, with
+// the roles of A and Af)
+cudaError_t launch_to_ff(const Space& s, const double* A, float2* Af, cudaStream_t st, const long long* zo = nullptr,
+                         int nz = 1, int rsrc = ZR_X, int rdst = ZR_XF);
 // split-form comm122ss from the (hi, lo) copies Xf, Yf of X and Y
+// (grouped)
 cudaError_t launch_comm122_df(const Space& s, const double* X, const double* Y, double* Z, const float2* Xf,
                               const float2* Yf, float2* W2, int hZ, const int* sym_tiles, int nsym_tiles,
-                              cudaStream_t st);
+                              cudaStream_t st, const long long* zo = nullptr, int nz = 1);
+// (grouped)
 cudaError_t launch_pandya_fwd(const Space& s, const double* X, const double* Y, int hY, double* Xb, double* Yt,
-                              double* Yf, const int* tiles, int ntiles, cudaStream_t st);
+                              double* Yf, const int* tiles, int ntiles, cudaStream_t st, const long long* zo = nullptr,
+                              int nz = 1);
 cudaError_t launch_pandya_inv(const Space& s, const double* Zb, double* Z, int hZ, const int* tiles, int ntiles,
                               cudaStream_t st);
 // split form: blocks of orbit quadruples (Space::invq_tasks), double-float sums
+// (grouped)
 cudaError_t launch_pandya_inv_ff(const Space& s, const double* Zb, double* Z, int hZ, const int* tasks, int ntasks,
                                  const int* clist, const int* coff, const unsigned char* csort, int smem,
-                                 cudaStream_t st);
+                                 cudaStream_t st, const long long* zo = nullptr, int nz = 1);
 // shared-memory budget of one quadruple block (dynamic part)
 constexpr int kInvqBudget = 36864;
 // single-operator Pandya transform into the Xbar panel layout (xb_off)

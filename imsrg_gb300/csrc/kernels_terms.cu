@@ -13,6 +13,15 @@
 namespace imsrg {
 
 static constexpr double kSqrt2 = 1.4142135623730950488;
+
+// grouped launches over several pairs of the same structure (batches): the
+// pair is blockIdx.z and its operands sit at byte offsets zo[z * kZRoles +
+// role] from the pointers the launch passes (zo null: one pair, no shift)
+template <class T>
+__device__ __forceinline__ T* zsh(T* p, const long long* zo, int role)
+{
+  return zo ? (T*)((char*)p + zo[blockIdx.z * kZRoles + role]) : p;
+}
 static constexpr int kMaxChannels = 6 * 64;  // 2b / CC channels: 6 (j2max + 1), j2max <= 63
 
 __device__ __forceinline__ double warp_sum(double v)
@@ -25,8 +34,11 @@ __device__ __forceinline__ double warp_sum(double v)
 // Z1 += X1 Y1 - Y1 X1  (comm111ss, src/Commutator.cc:644-649) and
 // Z0 += sum_a (2j_a+1) n_a (X1 Y1 - Y1 X1)_aa over holes (comm110ss, :564-581)
 __global__ void k_comm111_110(DevSpace S, const double* __restrict__ X, const double* __restrict__ Y,
-                              double* __restrict__ Z, int do111, int do110)
+                              double* __restrict__ Z, int do111, int do110, const long long* __restrict__ zo)
 {
+  X = zsh(X, zo, ZR_X);
+  Y = zsh(Y, zo, ZR_Y);
+  Z = zsh(Z, zo, ZR_Z);
   int N = S.norb;
   int i = blockIdx.x;
   const double* X1 = X + 32;
@@ -50,8 +62,11 @@ __global__ void k_comm111_110(DevSpace S, const double* __restrict__ X, const do
 // Z0 += 2 sum_ch (2J+1) sum_{h in hh} n_h n_h' (X_{h,nbar} (nbar nbar) Y_{nbar,h})
 // (comm220ss, src/Commutator.cc:601-631); one warp per hh ket.
 __global__ void k_comm220(DevSpace S, DevWork W, const double* __restrict__ X, const double* __restrict__ Y,
-                          double* __restrict__ Z, int hX)
+                          double* __restrict__ Z, int hX, const long long* __restrict__ zo)
 {
+  X = zsh(X, zo, ZR_X);
+  Y = zsh(Y, zo, ZR_Y);
+  Z = zsh(Z, zo, ZR_Z);
   int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   int lane = threadIdx.x & 31;
   if (item >= W.n220) return;
@@ -91,8 +106,12 @@ __device__ double dev_monopole(const DevSpace& S, const double* op, int a, int b
 // comm121ss, src/Commutator.cc:670-728: one warp per (i <= j) pair, lanes over
 // (hole a, b in the one-body channel of a).
 __global__ void k_comm121(DevSpace S, DevWork W, const int* __restrict__ holes, int nholes,
-                          const double* __restrict__ X, const double* __restrict__ Y, double* __restrict__ Z, int hZ)
+                          const double* __restrict__ X, const double* __restrict__ Y, double* __restrict__ Z, int hZ,
+                          const long long* __restrict__ zo)
 {
+  X = zsh(X, zo, ZR_X);
+  Y = zsh(Y, zo, ZR_Y);
+  Z = zsh(Z, zo, ZR_Z);
   int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   int lane = threadIdx.x & 31;
   if (item >= W.npairs1b) return;
@@ -310,8 +329,11 @@ __device__ __forceinline__ void df_add(float s1, float c1, float s2, float c2, f
 }
 
 // FP64 arena -> (hi, lo) pairs, integer instructions only
-__global__ void k_to_ff(const double* __restrict__ src, float2* __restrict__ dst, long long n)
+__global__ void k_to_ff(const double* __restrict__ src, float2* __restrict__ dst, long long n,
+                        const long long* __restrict__ zo, int rsrc, int rdst)
 {
+  src = zsh(src, zo, rsrc);
+  dst = zsh(dst, zo, rdst);
   long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   long long stride = (long long)gridDim.x * blockDim.x;
   for (; i < n; i += stride) dst[i] = d2ff(src[i]);
@@ -324,8 +346,14 @@ __global__ void k_to_ff(const double* __restrict__ src, float2* __restrict__ dst
 // (hi, lo) pairs.
 __global__ void __launch_bounds__(128) k_comm122_w_df(DevSpace S, DevWork W, const double* __restrict__ X,
                                                       const double* __restrict__ Y, const float2* __restrict__ Xf,
-                                                      const float2* __restrict__ Yf, float2* __restrict__ W2)
+                                                      const float2* __restrict__ Yf, float2* __restrict__ W2,
+                                                      const long long* __restrict__ zo)
 {
+  X = zsh(X, zo, ZR_X);
+  Y = zsh(Y, zo, ZR_Y);
+  Xf = zsh(Xf, zo, ZR_XF);
+  Yf = zsh(Yf, zo, ZR_YF);
+  W2 = zsh(W2, zo, ZR_W2);
   __shared__ float2 cx[32], cy[32];
   __shared__ int cl[32];
   int col = blockIdx.x;
@@ -361,8 +389,10 @@ __global__ void __launch_bounds__(128) k_comm122_w_df(DevSpace S, DevWork W, con
 // the pair sum in double-float, converted with integer instructions, so the
 // only FP64 instruction per element is the subtraction from Z2
 __global__ void k_sym_subtract_ff(DevSpace S, const float2* __restrict__ W2, double* __restrict__ Z, int hZ,
-                                  const int* __restrict__ tiles, int ntiles)
+                                  const int* __restrict__ tiles, int ntiles, const long long* __restrict__ zo)
 {
+  W2 = zsh(W2, zo, ZR_W2);
+  Z = zsh(Z, zo, ZR_Z);
   __shared__ float2 tt[32][33];
   int t = blockIdx.x;
   if (t >= ntiles) return;
@@ -397,8 +427,13 @@ __global__ void k_sym_subtract_ff(DevSpace S, const float2* __restrict__ W2, dou
 // to a zeroed Z): one warp per (i <= j) pair, lanes over c; each lane forms the
 // short Mhh dot products (hh kets only) itself, so the warp reduces once.
 __global__ void k_comm221_1b_mz(DevSpace S, DevWork W, const double* __restrict__ X, const double* __restrict__ Y,
-                                double* __restrict__ Z, int hX, int hZ, const double* __restrict__ Mz)
+                                double* __restrict__ Z, int hX, int hZ, const double* __restrict__ Mz,
+                                const long long* __restrict__ zo)
 {
+  X = zsh(X, zo, ZR_X);
+  Y = zsh(Y, zo, ZR_Y);
+  Z = zsh(Z, zo, ZR_Z);
+  Mz = zsh(Mz, zo, ZR_Z);
   int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   int lane = threadIdx.x & 31;
   if (item >= W.npairs1b) return;
@@ -520,8 +555,13 @@ __global__ void k_sym_subtract(DevSpace S, const double* __restrict__ W2, double
 // One thread per (ik, t); blocks over a (channel, tile) list.
 __global__ void k_pandya_fwd(DevSpace S, DevWork W, const double* __restrict__ X, const double* __restrict__ Y,
                              int hY, double* __restrict__ Xb, double* __restrict__ Yt, double* __restrict__ Yf,
-                             const int* __restrict__ tiles, int ntiles)
+                             const int* __restrict__ tiles, int ntiles, const long long* __restrict__ zo)
 {
+  X = zsh(X, zo, ZR_X);
+  Y = zsh(Y, zo, ZR_Y);
+  Xb = zsh(Xb, zo, ZR_XB);
+  Yt = zsh(Yt, zo, ZR_YT);
+  Yf = zsh(Yf, zo, ZR_YFL);
   int tix = blockIdx.x;
   if (tix >= ntiles) return;
   int cc = tiles[3 * tix], row0 = tiles[3 * tix + 1], t0 = tiles[3 * tix + 2];
@@ -762,8 +802,11 @@ __global__ void __launch_bounds__(kInvqThreads) k_pandya_inv_ff(DevSpace S, DevW
                                                              const int4* __restrict__ tasks,
                                                              const int* __restrict__ clist,
                                                              const int* __restrict__ coff,
-                                                             const unsigned char* __restrict__ csort)
+                                                             const unsigned char* __restrict__ csort,
+                                                             const long long* __restrict__ zo)
 {
+  Zb = zsh(Zb, zo, ZR_ZB);
+  Z = zsh(Z, zo, ZR_Z);
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_j[kInvqMaxOrb], s_l[kInvqMaxOrb], s_jj[kInvqMaxOrb], s_jl[kInvqMaxOrb];
   __shared__ int s_kkj[kInvqMaxOrb];       // global index of the ket (k, j) / (j, k)
@@ -1266,41 +1309,43 @@ __global__ void k_norm_onebody(DevSpace S, const double* __restrict__ A, double*
 
 // ------------------------------------------------------------------ launchers
 cudaError_t launch_comm111_110(const Space& s, const double* X, const double* Y, double* Z, bool do111, bool do110,
-                               cudaStream_t st)
+                               cudaStream_t st, const long long* zo, int nz)
 {
   int threads = s.norb <= 128 ? 128 : 256;
-  k_comm111_110<<<s.norb, threads, 0, st>>>(s.dev, X, Y, Z, do111, do110);
+  k_comm111_110<<<dim3(s.norb, 1, nz), threads, 0, st>>>(s.dev, X, Y, Z, do111, do110, zo);
   count_launch();
   return cudaGetLastError();
 }
 
-cudaError_t launch_comm220(const Space& s, const double* X, const double* Y, double* Z, int hX, cudaStream_t st)
+cudaError_t launch_comm220(const Space& s, const double* X, const double* Y, double* Z, int hX, cudaStream_t st,
+                           const long long* zo, int nz)
 {
   if (s.work.n220 == 0) return cudaSuccess;
   int wpb = 8;
-  k_comm220<<<(s.work.n220 + wpb - 1) / wpb, 32 * wpb, 0, st>>>(s.dev, s.work, X, Y, Z, hX);
+  k_comm220<<<dim3((s.work.n220 + wpb - 1) / wpb, 1, nz), 32 * wpb, 0, st>>>(s.dev, s.work, X, Y, Z, hX, zo);
   count_launch();
   return cudaGetLastError();
 }
 
 cudaError_t launch_comm121(const Space& s, const int* dev_holes, const double* X, const double* Y, double* Z,
-                           int hZ, cudaStream_t st)
+                           int hZ, cudaStream_t st, const long long* zo, int nz)
 {
   if (s.work.npairs1b == 0) return cudaSuccess;
   int wpb = 4;
-  k_comm121<<<(s.work.npairs1b + wpb - 1) / wpb, 32 * wpb, 0, st>>>(s.dev, s.work, dev_holes, (int)s.holes.size(),
-                                                                    X, Y, Z, hZ);
+  k_comm121<<<dim3((s.work.npairs1b + wpb - 1) / wpb, 1, nz), 32 * wpb, 0, st>>>(
+      s.dev, s.work, dev_holes, (int)s.holes.size(), X, Y, Z, hZ, zo);
+  count_launch();
   return cudaGetLastError();
 }
 
 cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, double* Z, int hX, int hZ,
-                              const double* Mz, cudaStream_t st)
+                              const double* Mz, cudaStream_t st, const long long* zo, int nz)
 {
   if (s.work.n221 == 0) return cudaSuccess;
   int wpb = 8;
   if (Mz) {
     // no other kernel writes Z1 concurrently: plain stores per (i, j) pair
-    k_comm221_1b_mz<<<(s.work.npairs1b + 3) / 4, 128, 0, st>>>(s.dev, s.work, X, Y, Z, hX, hZ, Mz);
+    k_comm221_1b_mz<<<dim3((s.work.npairs1b + 3) / 4, 1, nz), 128, 0, st>>>(s.dev, s.work, X, Y, Z, hX, hZ, Mz, zo);
     count_launch();
     return cudaGetLastError();
   }
@@ -1332,32 +1377,33 @@ static unsigned stride_grid(long long n, unsigned cap)
   return (unsigned)std::max(1LL, std::min<long long>(b, cap));
 }
 
-cudaError_t launch_to_ff(const Space& s, const double* A, float2* Af, cudaStream_t st)
+cudaError_t launch_to_ff(const Space& s, const double* A, float2* Af, cudaStream_t st, const long long* zo, int nz,
+                         int rsrc, int rdst)
 {
-  k_to_ff<<<stride_grid(s.arena, 2432), 256, 0, st>>>(A, Af, s.arena);
+  k_to_ff<<<dim3(stride_grid(s.arena, 2432), 1, nz), 256, 0, st>>>(A, Af, s.arena, zo, rsrc, rdst);
   count_launch();
   return cudaGetLastError();
 }
 
 cudaError_t launch_comm122_df(const Space& s, const double* X, const double* Y, double* Z, const float2* Xf,
                               const float2* Yf, float2* W2, int hZ, const int* sym_tiles, int nsym_tiles,
-                              cudaStream_t st)
+                              cudaStream_t st, const long long* zo, int nz)
 {
   if (s.work.ncols122 == 0) return cudaSuccess;
-  k_comm122_w_df<<<s.work.ncols122, 128, 0, st>>>(s.dev, s.work, X, Y, Xf, Yf, W2);
+  k_comm122_w_df<<<dim3(s.work.ncols122, 1, nz), 128, 0, st>>>(s.dev, s.work, X, Y, Xf, Yf, W2, zo);
   count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_sym_subtract_ff<<<nsym_tiles, 256, 0, st>>>(s.dev, W2, Z, hZ, sym_tiles, nsym_tiles);
+  k_sym_subtract_ff<<<dim3(nsym_tiles, 1, nz), 256, 0, st>>>(s.dev, W2, Z, hZ, sym_tiles, nsym_tiles, zo);
   count_launch();
   return cudaGetLastError();
 }
 
 cudaError_t launch_pandya_fwd(const Space& s, const double* X, const double* Y, int hY, double* Xb, double* Yt,
-                              double* Yf, const int* tiles, int ntiles, cudaStream_t st)
+                              double* Yf, const int* tiles, int ntiles, cudaStream_t st, const long long* zo, int nz)
 {
   if (ntiles == 0) return cudaSuccess;
-  k_pandya_fwd<<<ntiles, 256, 0, st>>>(s.dev, s.work, X, Y, hY, Xb, Yt, Yf, tiles, ntiles);
+  k_pandya_fwd<<<dim3(ntiles, 1, nz), 256, 0, st>>>(s.dev, s.work, X, Y, hY, Xb, Yt, Yf, tiles, ntiles, zo);
   count_launch();
   return cudaGetLastError();
 }
@@ -1373,13 +1419,13 @@ cudaError_t launch_pandya_inv(const Space& s, const double* Zb, double* Z, int h
 
 cudaError_t launch_pandya_inv_ff(const Space& s, const double* Zb, double* Z, int hZ, const int* tasks, int ntasks,
                                  const int* clist, const int* coff, const unsigned char* csort, int smem,
-                                 cudaStream_t st)
+                                 cudaStream_t st, const long long* zo, int nz)
 {
   if (ntasks == 0) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(k_pandya_inv_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  k_pandya_inv_ff<<<ntasks, kInvqThreads, smem, st>>>(s.dev, s.work, Zb, Z, hZ, (const int4*)tasks, clist, coff,
-                                                        csort);
+  k_pandya_inv_ff<<<dim3(ntasks, 1, nz), kInvqThreads, smem, st>>>(s.dev, s.work, Zb, Z, hZ, (const int4*)tasks,
+                                                                     clist, coff, csort, zo);
   count_launch();
   return cudaGetLastError();
 }
