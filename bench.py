@@ -72,6 +72,7 @@ def parse_args():
     p.add_argument("--emax", type=int, default=None, help="default 10 (commutator), 12 (flow)")
     p.add_argument("--workload", default="commutator", choices=["commutator", "flow", "batch", "tensor"])
     p.add_argument("--pairs", type=int, default=64, help="batch workload: independent (X, Y) pairs")
+    p.add_argument("--batch-emax", type=int, default=None, help="batch workload: every pair at this emax")
     p.add_argument("--fp64-steps", type=int, default=None, help="flow steps timed in the FP64 form")
     p.add_argument("--precision", default="split", choices=["split", "fp64"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
@@ -691,6 +692,8 @@ def run_batch(args):
     L = ig.lib()
     rng = np.random.Generator(np.random.PCG64(4 + rank))
     es = [int(e) for e in rng.choice([2, 3, 4, 5, 6], size=args.pairs)]
+    if args.batch_emax is not None:
+        es = [args.batch_emax] * args.pairs
     pairs = []
     arena_bytes = 0
     for i, e in enumerate(es):
