@@ -746,8 +746,9 @@ int imsrg_space_ninej(imsrg_space* sp, int lam, int ja, int jd, int J1, int jb, 
     std::lock_guard<std::mutex> g(sp->mu);
     tl = tensor_layout(*sp->s, lam, 0, 0);
   }
+  // the tabulated value the kernels read (ninej_tensor fills the table)
   DevTensor h = tensor_host_view(*tl);
-  *out = ninej_tensor(h, lam, ja, jb, jc, jd, J1, J2, Jbra, Jket);
+  *out = ninej_get(h, ja, jb, jc, jd, J1, J2, Jbra, Jket);
   return IMSRG_OK;
 }
 

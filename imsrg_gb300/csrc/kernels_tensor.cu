@@ -19,6 +19,13 @@ namespace {
 constexpr double kSqrt2t = 1.4142135623730950488;
 constexpr double kOccCut = 1e-6;  // ModelSpace::OCC_CUT (src/ModelSpace.cc:14)
 
+__device__ __forceinline__ double wsum(double v)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 __device__ __forceinline__ int ch_J(int ch) { return ch / 6; }
 __device__ __forceinline__ int ch_Tz(int ch) { return (ch % 6) / 2 - 1; }
 __device__ __forceinline__ int ch_par(int ch) { return ch & 1; }
@@ -117,27 +124,28 @@ __global__ void k_t111(DevSpace S, const double* __restrict__ X, const double* _
 }
 
 // -------------------------------------------------------------- comm121st
-// src/TensorCommutators.cc:46-150: a thread per (i, j >= i) with <i||Z||j>
-// allowed; the mirror element takes hZ (-1)^(ji - jj)
+// src/TensorCommutators.cc:46-150: a warp per (i, j >= i) with <i||Z||j>
+// allowed, lanes over (hole a, orbit b); the mirror element takes
+// hZ (-1)^(ji - jj)
 __global__ void k_t121(DevSpace S, DevTensor T, const int* __restrict__ holes, int nholes, const double* __restrict__ X,
                        const double* __restrict__ Y, int hY, double* __restrict__ Z, int hZ)
 {
   const int N = S.norb;
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (e >= N * N) return;
-  int i = e / N, j = e - i * N;
+  const int i = e / N, j = e - i * N;
   if (j < i || !T.ob_ok[i * N + j]) return;
   const int Lam = T.lam;
   const int ji = S.j2[i], jj = S.j2[j];
   const double *X1 = X + 32, *Y1 = Y + 32;
   double zij = 0.0;
-  for (int ih = 0; ih < nholes; ++ih) {
-    const int a = holes[ih], ja = S.j2[a];
-    const double na = S.occ[a];
-    // X one-body, Y two-body
-    for (int q = 0; q < S.ob_count[a]; ++q) {
-      const int b = S.ob_list[S.ob_start[a] + q];
-      const double nanb = na * (1 - S.occ[b]);
+  for (int w = lane; w < nholes * N; w += 32) {
+    const int a = holes[w / N], b = w - (w / N) * N;
+    const int ja = S.j2[a], jb = S.j2[b];
+    const double na = S.occ[a], nb = S.occ[b];
+    // X one-body (b in a's one-body channel), Y two-body
+    if (S.l[b] == S.l[a] && jb == ja && S.tz2[b] == S.tz2[a]) {
+      const double nanb = na * (1 - nb);
       const int J1min = abs(ji - ja) >> 1, J1max = (ji + ja) >> 1;
       for (int J1 = J1min; J1 <= J1max; ++J1) {
         const int phasefactor = iphase(((jj + ja) >> 1) + J1 + Lam);
@@ -150,11 +158,7 @@ __global__ void k_t121(DevSpace S, DevTensor T, const int* __restrict__ holes, i
       }
     }
     // X two-body, Y one-body
-    for (int b = 0; b < N; ++b) {
-      if (!T.ob_ok[a * N + b]) continue;
-      const double nb = S.occ[b];
-      if (fabs(nb - 1) < kOccCut) continue;
-      const int jb = S.j2[b];
+    if (T.ob_ok[a * N + b] && !(fabs(nb - 1) < kOccCut)) {
       const double nanb = na * (1 - nb);
       double xab = 0.0;
       int J1min = max(abs(ji - jb), abs(jj - ja)) >> 1, J1max = min(ji + jb, jj + ja) >> 1;
@@ -169,6 +173,8 @@ __global__ void k_t121(DevSpace S, DevTensor T, const int* __restrict__ holes, i
       zij += nanb * Y1[(long long)a * N + b] * xba;
     }
   }
+  zij = wsum(zij);
+  if (lane) return;
   Z[32 + (long long)j * N + i] += zij;
   if (i != j) Z[32 + (long long)i * N + j] += hZ * iphase((ji - jj) >> 1) * zij;
 }
@@ -294,19 +300,19 @@ __global__ void k_t222(DevSpace S, DevWork W, DevTensor T, const double* __restr
   Z[o] += pp - hh;
 }
 
-// one-body part, src/TensorCommutators.cc:421-495: a thread per (i, j >= i)
-// with <i||Z||j> allowed; Mpp and Mhh carry Z's hermiticity
+// one-body part, src/TensorCommutators.cc:421-495: a warp per (i, j >= i)
+// with <i||Z||j> allowed, lanes over c; Mpp and Mhh carry Z's hermiticity
 __global__ void k_t221(DevSpace S, DevTensor T, const double* __restrict__ Mpp, const double* __restrict__ Mhh,
                        int hZ, double* __restrict__ Z)
 {
   const int N = S.norb;
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (e >= N * N) return;
-  int i = e / N, j = e - i * N;
+  const int i = e / N, j = e - i * N;
   if (j < i || !T.ob_ok[i * N + j]) return;
   const int Lam = T.lam, ji = S.j2[i], jj = S.j2[j];
   double cij = 0.0;
-  for (int c = 0; c < N; ++c) {
+  for (int c = lane; c < N; c += 32) {
     const int jc = S.j2[c];
     const double nc = S.occ[c];
     const bool hole = nc >= kOccCut;
@@ -324,6 +330,8 @@ __global__ void k_t221(DevSpace S, DevTensor T, const double* __restrict__ Mpp, 
       }
     }
   }
+  cij = wsum(cij);
+  if (lane) return;
   Z[32 + (long long)j * N + i] += cij;
   if (i != j) Z[32 + (long long)i * N + j] += hZ * iphase((ji - jj) >> 1) * cij;
 }
@@ -360,7 +368,7 @@ __global__ void k_tpandya(DevSpace S, DevWork W, DevTensor T, const double* __re
   for (int J1 = J1min; J1 <= J1max; ++J1) {
     const int J2min = max(abs(jc - jb) >> 1, abs(J1 - Lam)), J2max = min((jc + jb) >> 1, J1 + Lam);
     for (int J2 = J2min; J2 <= J2max; ++J2) {
-      double nj = ninej_tensor(T, Lam, ja, jb, jc, jd, J1, J2, Jbra, Jket);
+      double nj = ninej_get(T, ja, jb, jc, jd, J1, J2, Jbra, Jket);
       if (fabs(nj) < 1e-8) continue;
       double hat = sqrt((double)((2 * J1 + 1) * (2 * J2 + 1) * (2 * Jbra + 1) * (2 * Jket + 1)));
       double tbme = y_tbme_J(S, T, Y, hY, J1, J2, a, d, c, b);
@@ -476,7 +484,7 @@ __global__ void k_tinv(DevSpace S, DevTensor T, const double* __restrict__ Zb, i
       const int J4min = max(abs(jk - jj) >> 1, abs(J3 - Lam)), J4max = min((jk + jj) >> 1, J3 + Lam);
       for (int J4 = J4min; J4 <= J4max; ++J4) {
         const int cket = chan_index(J4, pkc, tkc);
-        double nj = ninej_tensor(T, Lam, ji, jj, jk, jl, J3, J4, J1, J2);
+        double nj = ninej_get(T, ji, jj, jk, jl, J3, J4, J1, J2);
         if (fabs(nj) < 1e-8) continue;
         bool found;
         double tbme = zbar_get(S, T, Zb, hZ, cbra, cket, i, l, k, j, ji, jj, jk, jl, J3, J4, &found);
@@ -497,7 +505,7 @@ __global__ void k_tinv(DevSpace S, DevTensor T, const double* __restrict__ Zb, i
       const int J4min = max(abs(jk - ji) >> 1, abs(J3 - Lam)), J4max = min((jk + ji) >> 1, J3 + Lam);
       for (int J4 = J4min; J4 <= J4max; ++J4) {
         const int cket = chan_index(J4, pkc, tkc);
-        double nj = ninej_tensor(T, Lam, jj, ji, jk, jl, J3, J4, J1, J2);
+        double nj = ninej_get(T, jj, ji, jk, jl, J3, J4, J1, J2);
         if (fabs(nj) < 1e-8) continue;
         bool found;
         double tbme = zbar_get(S, T, Zb, hZ, cbra, cket, j, l, k, i, jj, ji, jk, jl, J3, J4, &found);
@@ -530,7 +538,7 @@ cudaError_t launch_tensor_121(const Space& s, const TensorLayout& t, const int* 
                               const double* Y, int hY, double* Z, int hZ, cudaStream_t st)
 {
   int nn = s.norb * s.norb;
-  k_t121<<<grid_for(nn), 256, 0, st>>>(s.dev, t.dev, dev_holes, (int)s.holes.size(), X, Y, hY, Z, hZ);
+  k_t121<<<(nn + 7) / 8, 256, 0, st>>>(s.dev, t.dev, dev_holes, (int)s.holes.size(), X, Y, hY, Z, hZ);
   count_launch();
   return cudaGetLastError();
 }
@@ -558,7 +566,7 @@ cudaError_t launch_tensor_222_221(const Space& s, const TensorLayout& t, const d
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   int nn = s.norb * s.norb;
-  k_t221<<<grid_for(nn), 256, 0, st>>>(s.dev, t.dev, Mpp, Mhh, hZ, Z);
+  k_t221<<<(nn + 7) / 8, 256, 0, st>>>(s.dev, t.dev, Mpp, Mhh, hZ, Z);
   count_launch();
   return cudaGetLastError();
 }

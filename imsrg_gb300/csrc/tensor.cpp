@@ -167,6 +167,43 @@ TensorLayout* tensor_layout(Space& s, int lam, int trank, int parity)
           }
     }
   build_compact(d1x, t->sixjx_base, t->sixjx_val);
+  // the 9j table (ninej_get), filled from the 6j tables above
+  {
+    const int d1 = s.d1, w = 2 * lam + 1;
+    t->nj_d1 = d1;
+    t->nj_base.assign((size_t)d1 * d1 * d1 * d1, 0);
+    long long tot = 0;
+    for (int a = 0; a < d1; ++a)
+      for (int b = 0; b < d1; ++b)
+        for (int c = 0; c < d1; ++c)
+          for (int d = 0; d < d1; ++d) {
+            const int ja = 2 * a + 1, jb = 2 * b + 1, jd = 2 * d + 1;
+            const int nJ1 = (ja + jd - std::abs(ja - jd)) / 2 + 1, nJb = (ja + jb - std::abs(ja - jb)) / 2 + 1;
+            t->nj_base[((size_t)(a * d1 + b) * d1 + c) * d1 + d] = tot;
+            tot += (long long)nJ1 * w * nJb * w;
+          }
+    t->nj_val.assign((size_t)tot, 0.0);
+    DevTensor h = tensor_host_view(*t);
+#pragma omp parallel for schedule(dynamic, 1) collapse(2)
+    for (int a = 0; a < d1; ++a)
+      for (int b = 0; b < d1; ++b)
+        for (int c = 0; c < d1; ++c)
+          for (int d = 0; d < d1; ++d) {
+            const int ja = 2 * a + 1, jb = 2 * b + 1, jc = 2 * c + 1, jd = 2 * d + 1;
+            const int J1min = std::abs(ja - jd) / 2, J1max = (ja + jd) / 2;
+            const int Jbmin = std::abs(ja - jb) / 2, Jbmax = (ja + jb) / 2, nJb = Jbmax - Jbmin + 1;
+            long long k = t->nj_base[((size_t)(a * d1 + b) * d1 + c) * d1 + d];
+            for (int J1 = J1min; J1 <= J1max; ++J1)
+              for (int o2 = 0; o2 < w; ++o2)
+                for (int Jb = Jbmin; Jb <= Jbmax; ++Jb)
+                  for (int o4 = 0; o4 < w; ++o4, ++k) {
+                    const int J2 = J1 - lam + o2, Jk = Jb - lam + o4;
+                    if (J2 < 0 || Jk < 0 || !triad2(jb, jc, 2 * J2) || !triad2(jd, jc, 2 * Jk)) continue;
+                    t->nj_val[k] = ninej_tensor(h, lam, ja, jb, jc, jd, J1, J2, Jb, Jk);
+                  }
+            (void)nJb;
+          }
+  }
   s.tensors[key] = t;
   return t;
 }
@@ -184,6 +221,9 @@ DevTensor tensor_host_view(const TensorLayout& t)
   d.sixjx_val = t.sixjx_val.data();
   d.NJ = t.NJ;
   d.d1x = t.d1x;
+  d.nj_base = t.nj_base.empty() ? nullptr : t.nj_base.data();
+  d.nj_val = t.nj_val.empty() ? nullptr : t.nj_val.data();
+  d.d1 = t.nj_d1;
   return d;
 }
 
@@ -221,6 +261,9 @@ void tensor_upload(TensorLayout& t)
   d.yb_lookup = dev_copy(t, yl);
   d.zb_total = t.zb_total;
   d.yb_total = t.yb_total;
+  d.nj_base = dev_copy(t, t.nj_base);
+  d.nj_val = dev_copy(t, t.nj_val);
+  d.d1 = t.nj_d1;
   t.dev_ready = true;
 }
 

@@ -48,6 +48,13 @@ struct DevTensor {
   const long long* yb_off = nullptr;
   const long long* yb_lookup = nullptr;  // [bra * nch + ket] -> offset, -1
   long long zb_total = 0, yb_total = 0;
+  // tabulated 9j {ja jd J1; jb jc J2; Jbra Jket lam} for orbit j's (extent
+  // d1): nj_base[((a d1 + b) d1 + c) d1 + d] starts an (nJ1, 2 lam + 1, nJbra,
+  // 2 lam + 1) block over J1 in [|ja-jd|, ja+jd], J2 = J1 - lam + o2, Jbra in
+  // [|ja-jb|, ja+jb], Jket = Jbra - lam + o4 (see ninej_get)
+  const long long* nj_base = nullptr;
+  const double* nj_val = nullptr;
+  int d1 = 0;
 };
 
 struct TensorLayout {
@@ -62,6 +69,9 @@ struct TensorLayout {
   int NJ = 0, d1x = 0;
   std::vector<int> zb_bra, zb_ket, yb_bra, yb_ket;
   std::vector<int64_t> zb_off, yb_off, zb_lookup, yb_lookup;
+  std::vector<long long> nj_base;
+  std::vector<double> nj_val;
+  int nj_d1 = 0;  // orbit j extent of the 9j table
   int64_t zb_total = 0, yb_total = 0;
   int zb_maxelems = 0, yb_maxelems = 0;  // largest block of each list (grid sizing)
   int max_blk_elems = 0;                 // largest two-body block of the layout
@@ -131,6 +141,22 @@ IMSRG_HD double ninej_tensor(const DevTensor& T, int lam, int ja, int jb, int jc
     s -= (x + 1) * a * b * c;  // (-1)^(2x) = -1 for half-integer x
   }
   return s;
+}
+
+// the tabulated 9j (the same value as ninej_tensor), 0 outside its windows
+IMSRG_HD double ninej_get(const DevTensor& T, int ja, int jb, int jc, int jd, int J1, int J2, int Jbra, int Jket)
+{
+  const int d1 = T.d1, L = T.lam, w = 2 * L + 1;
+  const int a = (ja - 1) >> 1, b = (jb - 1) >> 1, c = (jc - 1) >> 1, d = (jd - 1) >> 1;
+  if (a < 0 || b < 0 || c < 0 || d < 0 || a >= d1 || b >= d1 || c >= d1 || d >= d1) return 0.0;
+  const int J1min = (ja > jd ? ja - jd : jd - ja) >> 1, J1max = (ja + jd) >> 1;
+  const int Jbmin = (ja > jb ? ja - jb : jb - ja) >> 1, Jbmax = (ja + jb) >> 1;
+  const int o2 = J2 - J1 + L, o4 = Jket - Jbra + L;
+  if (J1 < J1min || J1 > J1max || Jbra < Jbmin || Jbra > Jbmax || o2 < 0 || o2 >= w || o4 < 0 || o4 >= w) return 0.0;
+  const int nJb = Jbmax - Jbmin + 1;
+  const long long k = T.nj_base[((a * d1 + b) * d1 + c) * d1 + d] +
+                      (((long long)(J1 - J1min) * w + o2) * nJb + (Jbra - Jbmin)) * w + o4;
+  return T.nj_val[k];
 }
 
 }  // namespace imsrg

@@ -147,9 +147,9 @@ int imsrg_op_rank(const imsrg_op* op, int* lam, int* trank, int* parity, long lo
 int imsrg_space_tensor_layout(imsrg_space* s, int lam, int trank, int parity, int block, int* ch_bra, int* ch_ket,
                               long long* offset, int* nblocks, long long* total);
 /* 9j symbol {ja/2 jd/2 J1; jb/2 jc/2 J2; Jbra Jket lam} (half-integers
- * doubled) as the scalar-tensor kernels evaluate it: a sum over three 6j
- * symbols from the space's tables (AngMom::NineJ's counterpart,
- * src/AngMom.cc:96-104). */
+ * doubled) as the scalar-tensor kernels read it: the layout's 9j table, filled
+ * by a sum over three 6j symbols from the space's tables (AngMom::NineJ's
+ * counterpart, src/AngMom.cc:96-104); 0 outside the orbits' j range. */
 int imsrg_space_ninej(imsrg_space* s, int lam, int ja, int jd, int J1, int jb, int jc, int J2, int Jbra, int Jket,
                       double* out);
 
