@@ -57,7 +57,8 @@ int scratch(imsrg_space* sp, TensorLayout* tl)
   int rc;
   if ((rc = alloc(tl, tl->d_mpp, tl->total)) || (rc = alloc(tl, tl->d_mhh, tl->total)) ||
       (rc = alloc(tl, tl->d_xbar, sp->s->xb_total)) || (rc = alloc(tl, tl->d_ybar, tl->yb_total)) ||
-      (rc = alloc(tl, tl->d_zbar, tl->zb_total)))
+      (rc = alloc(tl, tl->d_zbar, tl->zb_total)) || (rc = alloc(tl, tl->d_xw, sp->s->arena)) ||
+      (rc = alloc(tl, tl->d_wx, sp->s->arena)))
     return rc;
   return IMSRG_OK;
 }
@@ -89,7 +90,8 @@ int t222(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
   int rc = scratch(X->sp, tl);
   if (rc) return rc;
   ProfScope ps("comm222_pp_hh_221st", st);
-  T_CUDA(launch_tensor_222_221(*X->sp->s, *tl, X->d, Y->d, tl->d_mpp, tl->d_mhh, Z->d, Z->herm, st));
+  T_CUDA(launch_tensor_222_221(*X->sp->s, *tl, X->d, Y->d, tl->d_xw, tl->d_wx, tl->d_mpp, tl->d_mhh, Z->d, Z->herm,
+                               st));
   return IMSRG_OK;
 }
 

@@ -88,9 +88,10 @@ cudaError_t launch_tensor_121(const Space& s, const TensorLayout& t, const int* 
                               const double* Y, int hY, double* Z, int hZ, cudaStream_t st);
 cudaError_t launch_tensor_122(const Space& s, const TensorLayout& t, const double* X, const double* Y, int hY,
                               double* Z, cudaStream_t st);
-// Mpp, Mhh: scratch arenas of layout t
+// XW, WX: scratch of the space's arena length; D (= Mpp - Mhh), Mhh: scratch
+// arenas of layout t
 cudaError_t launch_tensor_222_221(const Space& s, const TensorLayout& t, const double* X, const double* Y,
-                                  double* Mpp, double* Mhh, double* Z, int hZ, cudaStream_t st);
+                                  double* XW, double* WX, double* D, double* Mhh, double* Z, int hZ, cudaStream_t st);
 // Xbar: the transposed single-operator Pandya transform of X (xb layout);
 // Ybar, Zbar: scratch of t's yb_total and zb_total doubles
 cudaError_t launch_tensor_ph(const Space& s, const TensorLayout& t, const double* Xbar, const double* Y, int hX,

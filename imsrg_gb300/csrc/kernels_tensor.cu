@@ -26,6 +26,27 @@ __device__ __forceinline__ double wsum(double v)
   return v;
 }
 
+// v with its sign flipped when odd is odd: an integer XOR on the sign bit in
+// place of a multiplication by (-1)^odd (FP64 instructions are the scarce
+// resource of these kernels on this part)
+__device__ __forceinline__ double flip(double v, int odd)
+{
+  return __longlong_as_double(__double_as_longlong(v) ^ ((long long)(odd & 1) << 63));
+}
+
+// v == 0 (either sign), tested on the bits
+__device__ __forceinline__ bool is_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
+
+constexpr double kInvSqrt2 = 0.70710678118654752440;
+
+// z / norm for the normalisation of a (bra, ket) element:
+// norm = 1 + delta (both or neither a == b pair), sqrt(2) otherwise
+__device__ __forceinline__ double unnorm(double z, int bd, int kd)
+{
+  if (bd == kd) return bd ? z * 0.5 : z;
+  return z * kInvSqrt2;
+}
+
 __device__ __forceinline__ int ch_J(int ch) { return ch / 6; }
 __device__ __forceinline__ int ch_Tz(int ch) { return (ch % 6) / 2 - 1; }
 __device__ __forceinline__ int ch_par(int ch) { return ch & 1; }
@@ -47,9 +68,10 @@ __device__ double x_tbme(const DevSpace& S, const double* X, int ch, int a, int 
   int bi = ket_in(S, ch, a, b), ki = ket_in(S, ch, c, d);
   if (bi < 0 || ki < 0) return 0.0;
   int J = ch_J(ch), n = S.ch_n[ch];
-  double v = X[S.ch_off[ch] + (long long)ki * n + bi];
-  if (a > b) v *= iphase(((S.j2[a] + S.j2[b]) >> 1) + 1 + J);
-  if (c > d) v *= iphase(((S.j2[c] + S.j2[d]) >> 1) + 1 + J);
+  int odd = 0;
+  if (a > b) odd += ((S.j2[a] + S.j2[b]) >> 1) + 1 + J;
+  if (c > d) odd += ((S.j2[c] + S.j2[d]) >> 1) + 1 + J;
+  double v = flip(X[S.ch_off[ch] + (long long)ki * n + bi], odd);
   if (a == b) v *= kSqrt2t;
   if (c == d) v *= kSqrt2t;
   return v;
@@ -64,44 +86,68 @@ __device__ double x_tbme_J(const DevSpace& S, const double* X, int J, int a, int
   return x_tbme(S, X, chan_index(J, pb, tb), a, b, c, d);
 }
 
-// <ab|Y|cd> of a reduced tensor between channels chb and chk: TwoBodyME::
-// GetTBME(chb, chk, a, b, c, d) with the conjugation of the block stored as
-// (chk, chb) when chb > chk (src/TwoBodyME.cc:131-150)
-__device__ double y_tbme(const DevSpace& S, const DevTensor& T, const double* Y, int herm, int chb, int chk, int a,
-                         int b, int c, int d)
+// where <ab|Y|cd> of a reduced tensor between channels chb and chk sits:
+// TwoBodyME::GetTBME(chb, chk, a, b, c, d) with the conjugation of the block
+// stored as (chk, chb) when chb > chk (src/TwoBodyME.cc:131-150).  The value is
+// flip(Y[idx], odd), times sqrt(2) for each of a == b, c == d; idx < 0: zero.
+struct YLoc {
+  long long idx;
+  int odd, sab, scd;
+};
+
+__device__ YLoc y_loc(const DevSpace& S, const DevTensor& T, int herm, int chb, int chk, int a, int b, int c, int d)
 {
+  YLoc L{-1, 0, a == b, c == d};
   int bi = ket_in(S, chb, a, b), ki = ket_in(S, chk, c, d);
-  if (bi < 0 || ki < 0) return 0.0;
+  if (bi < 0 || ki < 0) return L;
   int Jb = ch_J(chb), Jk = ch_J(chk);
-  double v;
   if (chb <= chk) {
     int blk = T.lookup[chb * S.nch + chk];
-    if (blk < 0) return 0.0;
-    v = Y[T.off[blk] + (long long)ki * S.ch_n[chb] + bi];
+    if (blk < 0) return L;
+    L.idx = T.off[blk] + (long long)ki * S.ch_n[chb] + bi;
   } else {
     int blk = T.lookup[chk * S.nch + chb];
-    if (blk < 0) return 0.0;
-    v = Y[T.off[blk] + (long long)bi * S.ch_n[chk] + ki];
-    if ((herm < 0) != ((Jb - Jk) & 1)) v = -v;
+    if (blk < 0) return L;
+    L.idx = T.off[blk] + (long long)bi * S.ch_n[chk] + ki;
+    L.odd = (herm < 0) != ((Jb - Jk) & 1);
   }
-  if (a > b) v *= iphase(((S.j2[a] + S.j2[b]) >> 1) + 1 + Jb);
-  if (c > d) v *= iphase(((S.j2[c] + S.j2[d]) >> 1) + 1 + Jk);
-  if (a == b) v *= kSqrt2t;
-  if (c == d) v *= kSqrt2t;
+  if (a > b) L.odd += ((S.j2[a] + S.j2[b]) >> 1) + 1 + Jb;
+  if (c > d) L.odd += ((S.j2[c] + S.j2[d]) >> 1) + 1 + Jk;
+  return L;
+}
+
+__device__ __forceinline__ double y_at(const YLoc& L, const double* Y)
+{
+  if (L.idx < 0) return 0.0;
+  double v = flip(Y[L.idx], L.odd);
+  if (L.sab) v *= kSqrt2t;
+  if (L.scd) v *= kSqrt2t;
   return v;
 }
 
-// tensor <ab|Y|cd>_(Jb, Jk): TwoBodyME::GetTBME_J(Jb, Jk, a, b, c, d) (src/TwoBodyME.cc:300-318)
-__device__ double y_tbme_J(const DevSpace& S, const DevTensor& T, const double* Y, int herm, int Jb, int Jk, int a,
-                           int b, int c, int d)
+// <ab|Y|cd> of a reduced tensor between channels chb and chk
+__device__ double y_tbme(const DevSpace& S, const DevTensor& T, const double* Y, int herm, int chb, int chk, int a,
+                         int b, int c, int d)
+{
+  return y_at(y_loc(S, T, herm, chb, chk, a, b, c, d), Y);
+}
+
+// where tensor <ab|Y|cd>_(Jb, Jk) sits: TwoBodyME::GetTBME_J(Jb, Jk, a, b, c, d)
+// (src/TwoBodyME.cc:300-318)
+__device__ YLoc y_loc_J(const DevSpace& S, const DevTensor& T, int herm, int Jb, int Jk, int a, int b, int c, int d)
 {
   int pb = (S.l[a] + S.l[b]) & 1, pk = (S.l[c] + S.l[d]) & 1;
   int tb = (S.tz2[a] + S.tz2[b]) / 2, tk = (S.tz2[c] + S.tz2[d]) / 2;
-  if ((T.parity + pb + pk) & 1) return 0.0;
-  if (abs(tb - tk) != T.trank) return 0.0;
-  if (abs(Jb - Jk) > T.lam || Jb + Jk < T.lam) return 0.0;
-  if (Jb >= S.NJ || Jk >= S.NJ) return 0.0;
-  return y_tbme(S, T, Y, herm, chan_index(Jb, pb, tb), chan_index(Jk, pk, tk), a, b, c, d);
+  if (((T.parity + pb + pk) & 1) || abs(tb - tk) != T.trank || abs(Jb - Jk) > T.lam || Jb + Jk < T.lam ||
+      Jb >= S.NJ || Jk >= S.NJ)
+    return YLoc{-1, 0, 0, 0};
+  return y_loc(S, T, herm, chan_index(Jb, pb, tb), chan_index(Jk, pk, tk), a, b, c, d);
+}
+
+__device__ double y_tbme_J(const DevSpace& S, const DevTensor& T, const double* Y, int herm, int Jb, int Jk, int a,
+                           int b, int c, int d)
+{
+  return y_at(y_loc_J(S, T, herm, Jb, Jk, a, b, c, d), Y);
 }
 
 __device__ __forceinline__ double sixjA(const DevTensor& T, int I1, int I2, int jj1, int jj2, int jj3)
@@ -151,7 +197,7 @@ __global__ void k_t121(DevSpace S, DevTensor T, const int* __restrict__ holes, i
         const int phasefactor = iphase(((jj + ja) >> 1) + J1 + Lam);
         const int J2min = max(abs(Lam - J1), abs(ja - jj) >> 1), J2max = min(Lam + J1, (ja + jj) >> 1);
         for (int J2 = J2min; J2 <= J2max; ++J2) {
-          double pre = nanb * phasefactor * sqrt((double)((2 * J1 + 1) * (2 * J2 + 1))) * sixjA(T, J1, J2, jj, ji, ja);
+          double pre = flip(nanb, phasefactor < 0) * T.hat2[J1 * T.NJ + J2] * sixjA(T, J1, J2, jj, ji, ja);
           zij += pre * (X1[(long long)b * N + a] * y_tbme_J(S, T, Y, hY, J1, J2, b, i, a, j) -
                         X1[(long long)a * N + b] * y_tbme_J(S, T, Y, hY, J1, J2, a, i, b, j));
         }
@@ -176,7 +222,7 @@ __global__ void k_t121(DevSpace S, DevTensor T, const int* __restrict__ holes, i
   zij = wsum(zij);
   if (lane) return;
   Z[32 + (long long)j * N + i] += zij;
-  if (i != j) Z[32 + (long long)i * N + j] += hZ * iphase((ji - jj) >> 1) * zij;
+  if (i != j) Z[32 + (long long)i * N + j] += flip(zij, (hZ < 0) + ((ji - jj) >> 1));
 }
 
 // -------------------------------------------------------------- comm122st
@@ -225,9 +271,9 @@ __global__ void k_t122(DevSpace S, DevTensor T, const double* __restrict__ X, co
   }
   double cijkl = c1 + c2 - c3 - c4;
   c1 = c2 = c3 = c4 = 0;
-  const int phase1 = iphase(((ji + jj) >> 1) + J2 + Lam);
-  const int phase2 = iphase(J1 - J2 + Lam), phase3 = phase2;
-  const int phase4 = iphase(((jk + jl) >> 1) - J1 + Lam);
+  const int odd1 = ((ji + jj) >> 1) + J2 + Lam;
+  const int odd2 = J1 - J2 + Lam, odd3 = odd2;
+  const int odd4 = ((jk + jl) >> 1) - J1 + Lam;
   for (int a = 0; a < N; ++a) {
     if (!T.ob_ok[i * N + a]) continue;
     c1 -= sixjA(T, J2, J1, ji, S.j2[a], jj) * Y1[(long long)a * N + i] * x_tbme(S, X, chk, a, j, k, l);
@@ -252,57 +298,116 @@ __global__ void k_t122(DevSpace S, DevTensor T, const double* __restrict__ X, co
       c4 += sixjA(T, J1, J2, jl, S.j2[a], jk) * Y1[(long long)l * N + a] * x_tbme(S, X, chb, i, j, k, a);
     }
   }
-  const double hat = sqrt((double)((2 * J1 + 1) * (2 * J2 + 1)));
-  cijkl += hat * (phase1 * c1 + phase2 * c2 + phase3 * c3 + phase4 * c4);
-  const int bd = i == j, kd = k == l;
-  const double norm = bd == kd ? 1.0 + bd : kSqrt2t;
-  Z[T.off[blk] + (long long)ik * nb + ib] += cijkl / norm;
+  const double hat = T.hat2[J1 * T.NJ + J2];
+  cijkl += hat * (flip(c1, odd1) + flip(c2, odd2) + flip(c3, odd3) + flip(c4, odd4));
+  Z[T.off[blk] + (long long)ik * nb + ib] += unnorm(cijkl, i == j, k == l);
 }
 
 // --------------------------------------------------- comm222_pp_hh_221st
-// two-body part, src/TensorCommutators.cc:314-420: for every stored block
-// (chb, chk), with Xb = X(chb, chb), Xk = X(chk, chk), Yc = Y(chb, chk) and
-// per-ket weights wpp (pp 1, hh and ph (1-na)(1-nb)) and nn (hh na nb):
-//   Mpp = Xb wpp_b Yc - Yc wpp_k Xk,  Mhh = Xb nn_b Yc - Yc nn_k Xk,
-//   Z2 += Mpp - Mhh.  A thread per element; Mpp and Mhh are kept for the
-// one-body part.
+// src/TensorCommutators.cc:314-495.  With per-ket weights wpp (pp 1; hh and
+// ph (1-na)(1-nb)) and nn (hh na nb), for every stored block (chb, chk),
+// Xb = X(chb, chb), Xk = X(chk, chk), Yc = Y(chb, chk):
+//   Mpp = Xb wpp Yc - Yc wpp Xk,  Mhh = Xb nn Yc - Yc nn Xk,  Z2 += Mpp - Mhh,
+// and the one-body part reads Mpp and Mhh.  Here D = Mpp - Mhh is one product
+// with the combined weight w = wpp - nn over the kets where w != 0 (the scalar
+// ladder's gather lists), Mhh runs over the hh kets only, and the one-body
+// part reads Mpp as D + Mhh.
+
+// weighted copies of X over the gather list K_t, w_t of each channel, at the
+// channel's arena offset: XW[t n + r] = X(r, K_t) w_t, WX[t n + c] = w_t X(K_t, c)
+__global__ void k_t222_weights(DevSpace S, DevWork W, DevTensor T, const double* __restrict__ X,
+                               double* __restrict__ XW, double* __restrict__ WX)
+{
+  const int ch = blockIdx.y;
+  const int n = S.ch_n[ch], K = T.lad_n[ch];
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)n * K) return;
+  const int t = (int)(e / n), r = (int)(e - (long long)t * n);
+  const int kt = W.kidx[T.lad_koff[ch] + t];
+  const double w = W.kweight[T.lad_woff[ch] + t];
+  const double* Xc = X + S.ch_off[ch];
+  XW[S.ch_off[ch] + e] = Xc[(long long)kt * n + r] * w;
+  WX[S.ch_off[ch] + e] = Xc[(long long)r * n + kt] * w;
+}
+
+// D and Mhh for the element pair (r, c0), (r, c1 = c0 + 1) of every stored
+// block (blockIdx.y); Z2 += D
 __global__ void k_t222(DevSpace S, DevWork W, DevTensor T, const double* __restrict__ X,
-                       const double* __restrict__ Y, double* __restrict__ Mpp, double* __restrict__ Mhh,
-                       double* __restrict__ Z)
+                       const double* __restrict__ Y, const double* __restrict__ XW, const double* __restrict__ WX,
+                       double* __restrict__ D, double* __restrict__ Mhh, double* __restrict__ Z)
 {
   const int blk = blockIdx.y;
   const int chb = T.bra[blk], chk = T.ket[blk];
   const int nb = S.ch_n[chb], nk = S.ch_n[chk];
   long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (e >= (long long)nb * nk) return;
-  const int c = (int)(e / nb), r = (int)(e - (long long)c * nb);
-  const double* Xb = X + S.ch_off[chb];
-  const double* Xk = X + S.ch_off[chk];
+  if (e >= (long long)nb * ((nk + 1) >> 1)) return;
+  const int q = (int)(e / nb), r = (int)(e - (long long)q * nb);
+  const int c0 = 2 * q, c1 = min(c0 + 1, nk - 1);
   const double* Yc = Y + T.off[blk];
-  const double* wb = W.ket_wpp + S.ch_kofs[chb];
-  const double* nnb = W.ket_nn + S.ch_kofs[chb];
-  const double* wk = W.ket_wpp + S.ch_kofs[chk];
-  const double* nnk = W.ket_nn + S.ch_kofs[chk];
-  double pp = 0.0, hh = 0.0;
-  for (int K = 0; K < nb; ++K) {
-    double xy = Xb[(long long)K * nb + r] * Yc[(long long)c * nb + K];
-    pp += wb[K] * xy;
-    hh += nnb[K] * xy;
+  const double* Y0 = Yc + (long long)c0 * nb;
+  const double* Y1 = Yc + (long long)c1 * nb;
+  double d0 = 0.0, d1 = 0.0, h0 = 0.0, h1 = 0.0;
+  {
+    const int Kb = T.lad_n[chb];
+    const int* kx = W.kidx + T.lad_koff[chb];
+    const double* xw = XW + S.ch_off[chb] + r;
+    for (int t = 0; t < Kb; ++t) {
+      const double a = xw[(long long)t * nb];
+      const int K = kx[t];
+      d0 = fma(a, Y0[K], d0);
+      d1 = fma(a, Y1[K], d1);
+    }
   }
-  for (int K = 0; K < nk; ++K) {
-    double yx = Yc[(long long)K * nb + r] * Xk[(long long)c * nk + K];
-    pp -= wk[K] * yx;
-    hh -= nnk[K] * yx;
+  {
+    const int Kk = T.lad_n[chk];
+    const int* kx = W.kidx + T.lad_koff[chk];
+    const double* wx = WX + S.ch_off[chk];
+    for (int t = 0; t < Kk; ++t) {
+      const double y = Yc[(long long)kx[t] * nb + r];
+      const double* wt = wx + (long long)t * nk;
+      d0 = fma(-y, wt[c0], d0);
+      d1 = fma(-y, wt[c1], d1);
+    }
   }
-  const long long o = T.off[blk] + (long long)c * nb + r;
-  Mpp[o] = pp;
-  Mhh[o] = hh;
-  Z[o] += pp - hh;
+  {
+    const int* hh = W.hh_list + W.hh_off[chb];
+    const int nh = W.hh_off[chb + 1] - W.hh_off[chb];
+    const double* nn = W.ket_nn + S.ch_kofs[chb];
+    const double* Xb = X + S.ch_off[chb] + r;
+    for (int t = 0; t < nh; ++t) {
+      const int K = hh[t];
+      const double a = Xb[(long long)K * nb] * nn[K];
+      h0 = fma(a, Y0[K], h0);
+      h1 = fma(a, Y1[K], h1);
+    }
+  }
+  {
+    const int* hh = W.hh_list + W.hh_off[chk];
+    const int nh = W.hh_off[chk + 1] - W.hh_off[chk];
+    const double* nn = W.ket_nn + S.ch_kofs[chk];
+    const double* Xk = X + S.ch_off[chk];
+    for (int t = 0; t < nh; ++t) {
+      const int K = hh[t];
+      const double y = Yc[(long long)K * nb + r] * nn[K];
+      h0 = fma(-y, Xk[(long long)c0 * nk + K], h0);
+      h1 = fma(-y, Xk[(long long)c1 * nk + K], h1);
+    }
+  }
+  const long long o0 = T.off[blk] + (long long)c0 * nb + r;
+  D[o0] = d0;
+  Mhh[o0] = h0;
+  Z[o0] += d0;
+  if (c1 != c0) {
+    const long long o1 = o0 + nb;
+    D[o1] = d1;
+    Mhh[o1] = h1;
+    Z[o1] += d1;
+  }
 }
 
 // one-body part, src/TensorCommutators.cc:421-495: a warp per (i, j >= i)
-// with <i||Z||j> allowed, lanes over c; Mpp and Mhh carry Z's hermiticity
-__global__ void k_t221(DevSpace S, DevTensor T, const double* __restrict__ Mpp, const double* __restrict__ Mhh,
+// with <i||Z||j> allowed, lanes over c; D and Mhh carry Z's hermiticity
+__global__ void k_t221(DevSpace S, DevTensor T, const double* __restrict__ D, const double* __restrict__ Mhh,
                        int hZ, double* __restrict__ Z)
 {
   const int N = S.norb;
@@ -320,11 +425,11 @@ __global__ void k_t221(DevSpace S, DevTensor T, const double* __restrict__ Mpp, 
     for (int J1 = J1min; J1 <= J1max; ++J1) {
       const int J2min = max(abs(jc - jj) >> 1, abs(Lam - J1)), J2max = min((jc + jj) >> 1, J1 + Lam);
       for (int J2 = J2min; J2 <= J2max; ++J2) {
-        double w = sqrt((double)((2 * J1 + 1) * (2 * J2 + 1))) * sixjA(T, J1, J2, jj, ji, jc) *
-                   iphase(((jj + jc) >> 1) + J1 + Lam);
-        double mhh = y_tbme_J(S, T, Mhh, hZ, J1, J2, c, i, c, j);
+        const double w = flip(T.hat2[J1 * T.NJ + J2] * sixjA(T, J1, J2, jj, ji, jc), ((jj + jc) >> 1) + J1 + Lam);
+        const YLoc L = y_loc_J(S, T, hZ, J1, J2, c, i, c, j);
+        const double mhh = y_at(L, Mhh);
         if (hole)
-          cij += w * (nc * y_tbme_J(S, T, Mpp, hZ, J1, J2, c, i, c, j) + (1 - nc) * mhh);
+          cij += w * (nc * (y_at(L, D) + mhh) + (1 - nc) * mhh);
         else
           cij += w * mhh;
       }
@@ -333,7 +438,7 @@ __global__ void k_t221(DevSpace S, DevTensor T, const double* __restrict__ Mpp, 
   cij = wsum(cij);
   if (lane) return;
   Z[32 + (long long)j * N + i] += cij;
-  if (i != j) Z[32 + (long long)i * N + j] += hZ * iphase((ji - jj) >> 1) * cij;
+  if (i != j) Z[32 + (long long)i * N + j] += flip(cij, (hZ < 0) + ((ji - jj) >> 1));
 }
 
 // ------------------------------------------------------------ comm222_phst
@@ -368,11 +473,11 @@ __global__ void k_tpandya(DevSpace S, DevWork W, DevTensor T, const double* __re
   for (int J1 = J1min; J1 <= J1max; ++J1) {
     const int J2min = max(abs(jc - jb) >> 1, abs(J1 - Lam)), J2max = min((jc + jb) >> 1, J1 + Lam);
     for (int J2 = J2min; J2 <= J2max; ++J2) {
-      double nj = ninej_get(T, ja, jb, jc, jd, J1, J2, Jbra, Jket);
-      if (fabs(nj) < 1e-8) continue;
-      double hat = sqrt((double)((2 * J1 + 1) * (2 * J2 + 1) * (2 * Jbra + 1) * (2 * Jket + 1)));
-      double tbme = y_tbme_J(S, T, Y, hY, J1, J2, a, d, c, b);
-      sm -= hat * iphase(((jb + jd) >> 1) + Jket + J2) * nj * tbme;
+      // sm -= hat (-1)^(jb+jd+Jket+J2) 9j tbme; the table holds hat 9j, 0 where |9j| < 1e-8
+      const double nh = ninej_hat(T, ja, jb, jc, jd, J1, J2, Jbra, Jket);
+      if (is_zero(nh)) continue;
+      const double tbme = y_tbme_J(S, T, Y, hY, J1, J2, a, d, c, b);
+      sm = fma(flip(nh, 1 + ((jb + jd) >> 1) + Jket + J2), tbme, sm);
     }
   }
   out[e] = sm;
@@ -400,35 +505,35 @@ __global__ void k_tzbar(DevSpace S, DevWork W, DevTensor T, const double* __rest
   const double* X2 = Xb + W.xb_off[hi];  // nhi x 2 nph2
   const double* Y12 = Yb + T.yb_lookup[lo * S.nch + hi];  // 2 nph1 x nhi
   const double* Y21 = Yb + T.yb_lookup[hi * S.nch + lo];  // 2 nph2 x nlo
-  const int f = ((hY < 0) != ((ch_J(lo) - ch_J(hi)) & 1)) ? -1 : 1;
-  const int* ph_lo = phase_tab + W.cc_phase_off[lo];  // (-1)^(ja+jb) per CC ket
+  const int fneg = (hY < 0) != ((ch_J(lo) - ch_J(hi)) & 1);  // f = -1
+  const int* ph_lo = phase_tab + W.cc_phase_off[lo];     // (-1)^(ja+jb) per CC ket
   const int* ph_hi = phase_tab + W.cc_phase_off[hi];
-  const int* phl_lo = W.cc_ph + W.cc_ph_off[lo];      // local index of each ph ket
+  const int* phl_lo = W.cc_ph + W.cc_ph_off[lo];         // local index of each ph ket
   const int* phl_hi = W.cc_ph + W.cc_ph_off[hi];
   const bool tail = col >= nhi;
   const int c = tail ? col - nhi : col;
+  const double* y12 = Y12 + (long long)c * 2 * nph1;
+  const double* y21 = Y21 + (long long)r * 2 * nph2;
+  const double* x1 = X1 + r;
+  // the second product enters as -f hX Y21^T [...]
+  const int sneg = 1 + fneg + (hX < 0);
   double s = 0.0;
-  for (int K = 0; K < 2 * nph1; ++K) {
-    double top;
-    if (!tail) {
-      top = Y12[(long long)c * 2 * nph1 + K];
-    } else {
-      const int Kh = K < nph1 ? K : K - nph1;
-      const int src = K < nph1 ? K + nph1 : K - nph1;
-      top = Y12[(long long)c * 2 * nph1 + src] * (f * ph_lo[phl_lo[Kh]] * ph_hi[c]);
+  if (!tail) {
+    for (int K = 0; K < 2 * nph1; ++K) s = fma(x1[(long long)K * nlo], y12[K], s);
+    for (int K = 0; K < 2 * nph2; ++K) s = fma(flip(y21[K], sneg), X2[(long long)K * nhi + c], s);
+  } else {
+    // the halves of the ph index swap, with the phases of the kets involved
+    const int cneg = ph_hi[c] < 0;
+    for (int Kh = 0; Kh < nph1; ++Kh) {
+      const int odd = fneg + cneg + (ph_lo[phl_lo[Kh]] < 0);
+      s = fma(x1[(long long)Kh * nlo], flip(y12[Kh + nph1], odd), s);
+      s = fma(x1[(long long)(Kh + nph1) * nlo], flip(y12[Kh], odd), s);
     }
-    s += X1[(long long)K * nlo + r] * top;
-  }
-  for (int K = 0; K < 2 * nph2; ++K) {
-    double bot;
-    if (!tail) {
-      bot = X2[(long long)K * nhi + c];
-    } else {
-      const int Kh = K < nph2 ? K : K - nph2;
-      const int src = K < nph2 ? K + nph2 : K - nph2;
-      bot = X2[(long long)src * nhi + c] * (ph_hi[c] * ph_hi[phl_hi[Kh]]);
+    for (int Kh = 0; Kh < nph2; ++Kh) {
+      const int odd = sneg + cneg + (ph_hi[phl_hi[Kh]] < 0);
+      s = fma(flip(y21[Kh], odd), X2[(long long)(Kh + nph2) * nhi + c], s);
+      s = fma(flip(y21[Kh + nph2], odd), X2[(long long)Kh * nhi + c], s);
     }
-    s -= f * Y21[(long long)r * 2 * nph2 + K] * (hX * bot);
   }
   Zb[T.zb_off[p] + (long long)col * nlo + r] = s;
 }
@@ -448,12 +553,13 @@ __device__ double zbar_get(const DevSpace& S, const DevTensor& T, const double* 
   const double* M = Zb + off;
   const int nrow = S.cc_n[lo];
   const int sum4 = (ji + jj + jk + jl) >> 1;
+  const int hneg = hZ < 0;
   if (cbra <= cket) {
     if (i <= l) return M[(long long)(ixkj + (k > j ? nkets : 0)) * nrow + ixil];
-    return M[(long long)(ixkj + (k > j ? 0 : nkets)) * nrow + ixil] * (hZ * iphase(J3 - J4 + sum4));
+    return flip(M[(long long)(ixkj + (k > j ? 0 : nkets)) * nrow + ixil], hneg + J3 - J4 + sum4);
   }
-  if (k <= j) return M[(long long)(ixil + (i > l ? nbras : 0)) * nrow + ixkj] * (hZ * iphase(J3 - J4));
-  return M[(long long)(ixil + (i > l ? 0 : nbras)) * nrow + ixkj] * iphase(sum4);
+  if (k <= j) return flip(M[(long long)(ixil + (i > l ? nbras : 0)) * nrow + ixkj], hneg + J3 - J4);
+  return flip(M[(long long)(ixil + (i > l ? 0 : nbras)) * nrow + ixkj], sum4);
 }
 
 // inverse tensor Pandya transform, AddInverseTensorPandyaTransformation
@@ -473,7 +579,6 @@ __global__ void k_tinv(DevSpace S, DevTensor T, const double* __restrict__ Zb, i
   const int k = S.ket_p[S.ch_kofs[chk] + ik], l = S.ket_q[S.ch_kofs[chk] + ik];
   const int J1 = ch_J(chb), J2 = ch_J(chk), Lam = T.lam;
   const int ji = S.j2[i], jj = S.j2[j], jk = S.j2[k], jl = S.j2[l];
-  const double h12 = (double)((2 * J1 + 1) * (2 * J2 + 1));
   double commij = 0.0, commji = 0.0;
   {
     const int pbc = (S.l[i] + S.l[l]) & 1, pkc = (S.l[k] + S.l[j]) & 1;
@@ -484,13 +589,13 @@ __global__ void k_tinv(DevSpace S, DevTensor T, const double* __restrict__ Zb, i
       const int J4min = max(abs(jk - jj) >> 1, abs(J3 - Lam)), J4max = min((jk + jj) >> 1, J3 + Lam);
       for (int J4 = J4min; J4 <= J4max; ++J4) {
         const int cket = chan_index(J4, pkc, tkc);
-        double nj = ninej_get(T, ji, jj, jk, jl, J3, J4, J1, J2);
-        if (fabs(nj) < 1e-8) continue;
+        // commij += hat (-1)^(jj+jl+J2+J4) 9j tbme (the table holds hat 9j)
+        const double nh = ninej_hat(T, ji, jj, jk, jl, J3, J4, J1, J2);
+        if (is_zero(nh)) continue;
         bool found;
-        double tbme = zbar_get(S, T, Zb, hZ, cbra, cket, i, l, k, j, ji, jj, jk, jl, J3, J4, &found);
+        const double tbme = zbar_get(S, T, Zb, hZ, cbra, cket, i, l, k, j, ji, jj, jk, jl, J3, J4, &found);
         if (!found) continue;
-        double hat = sqrt(h12 * (double)((2 * J3 + 1) * (2 * J4 + 1)));
-        commij += hat * iphase(((jj + jl) >> 1) + J2 + J4) * nj * tbme;
+        commij = fma(flip(nh, ((jj + jl) >> 1) + J2 + J4), tbme, commij);
       }
     }
   }
@@ -505,21 +610,18 @@ __global__ void k_tinv(DevSpace S, DevTensor T, const double* __restrict__ Zb, i
       const int J4min = max(abs(jk - ji) >> 1, abs(J3 - Lam)), J4max = min((jk + ji) >> 1, J3 + Lam);
       for (int J4 = J4min; J4 <= J4max; ++J4) {
         const int cket = chan_index(J4, pkc, tkc);
-        double nj = ninej_get(T, jj, ji, jk, jl, J3, J4, J1, J2);
-        if (fabs(nj) < 1e-8) continue;
+        const double nh = ninej_hat(T, jj, ji, jk, jl, J3, J4, J1, J2);
+        if (is_zero(nh)) continue;
         bool found;
-        double tbme = zbar_get(S, T, Zb, hZ, cbra, cket, j, l, k, i, jj, ji, jk, jl, J3, J4, &found);
+        const double tbme = zbar_get(S, T, Zb, hZ, cbra, cket, j, l, k, i, jj, ji, jk, jl, J3, J4, &found);
         if (!found) continue;
-        double hat = sqrt(h12 * (double)((2 * J3 + 1) * (2 * J4 + 1)));
-        commji += hat * iphase(((ji + jl) >> 1) + J2 + J4) * nj * tbme;
+        commji = fma(flip(nh, ((ji + jl) >> 1) + J2 + J4), tbme, commji);
       }
     }
   }
-  const int bd = i == j, kd = k == l;
-  const double norm = bd == kd ? 1.0 + bd : kSqrt2t;
-  const double z = (commij - iphase(((ji + jj) >> 1) - J1) * commji) / norm;
+  const double z = unnorm(commij + flip(commji, 1 + ((ji + jj) >> 1) - J1), i == j, k == l);
   Z[T.off[blk] + (long long)ik * nb + ib] += z;
-  if (chb == chk && ik != ib) Z[T.off[blk] + (long long)ib * nb + ik] += hZ * z;
+  if (chb == chk && ik != ib) Z[T.off[blk] + (long long)ib * nb + ik] += flip(z, hZ < 0);
 }
 
 unsigned grid_for(long long n) { return (unsigned)std::max(1LL, (n + 255) / 256); }
@@ -554,19 +656,26 @@ cudaError_t launch_tensor_122(const Space& s, const TensorLayout& t, const doubl
 }
 
 cudaError_t launch_tensor_222_221(const Space& s, const TensorLayout& t, const double* X, const double* Y,
-                                  double* Mpp, double* Mhh, double* Z, int hZ, cudaStream_t st)
+                                  double* XW, double* WX, double* D, double* Mhh, double* Z, int hZ, cudaStream_t st)
 {
-  cudaError_t e = cudaMemsetAsync(Mpp, 0, t.total * sizeof(double), st);
+  cudaError_t e = cudaMemsetAsync(D, 0, t.total * sizeof(double), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(Mhh, 0, t.total * sizeof(double), st);
   if (e != cudaSuccess) return e;
   if (!t.bra.empty() && t.max_blk_elems > 0) {
-    dim3 grid(grid_for(t.max_blk_elems), (unsigned)t.bra.size());
-    k_t222<<<grid, 256, 0, st>>>(s.dev, s.work, t.dev, X, Y, Mpp, Mhh, Z);
+    if (t.lad_maxelems > 0) {
+      dim3 gw(grid_for(t.lad_maxelems), (unsigned)s.nch);
+      k_t222_weights<<<gw, 256, 0, st>>>(s.dev, s.work, t.dev, X, XW, WX);
+      count_launch();
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    // element pairs: a block's columns come two at a time
+    dim3 grid(grid_for(t.max_pair_elems), (unsigned)t.bra.size());
+    k_t222<<<grid, 256, 0, st>>>(s.dev, s.work, t.dev, X, Y, XW, WX, D, Mhh, Z);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   int nn = s.norb * s.norb;
-  k_t221<<<(nn + 7) / 8, 256, 0, st>>>(s.dev, t.dev, Mpp, Mhh, hZ, Z);
+  k_t221<<<(nn + 7) / 8, 256, 0, st>>>(s.dev, t.dev, D, Mhh, hZ, Z);
   count_launch();
   return cudaGetLastError();
 }

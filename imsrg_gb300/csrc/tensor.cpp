@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <stdexcept>
 
@@ -99,8 +100,11 @@ TensorLayout* tensor_layout(Space& s, int lam, int trank, int parity)
       cur = round32(cur + (int64_t)B.n() * K.n());
     }
   t->total = cur;
-  for (size_t b = 0; b < t->bra.size(); ++b)
-    t->max_blk_elems = std::max<int64_t>(t->max_blk_elems, (int64_t)s.ch[t->bra[b]].n() * s.ch[t->ket[b]].n());
+  for (size_t b = 0; b < t->bra.size(); ++b) {
+    const int64_t nb = s.ch[t->bra[b]].n(), nk = s.ch[t->ket[b]].n();
+    t->max_blk_elems = std::max<int64_t>(t->max_blk_elems, nb * nk);
+    t->max_pair_elems = std::max<int64_t>(t->max_pair_elems, nb * ((nk + 1) / 2));
+  }
   // comm222_phst (src/TensorCommutators.cc:1059-1386): Zbar blocks for the
   // cross-coupled channel pairs lo <= hi allowed by the rank, and the ordered
   // pairs of the tensor Pandya transform of Y they read, (lo, hi) and (hi, lo)
@@ -183,6 +187,7 @@ TensorLayout* tensor_layout(Space& s, int lam, int trank, int parity)
             tot += (long long)nJ1 * w * nJb * w;
           }
     t->nj_val.assign((size_t)tot, 0.0);
+    t->nj_hat.assign((size_t)tot, 0.0);
     DevTensor h = tensor_host_view(*t);
 #pragma omp parallel for schedule(dynamic, 1) collapse(2)
     for (int a = 0; a < d1; ++a)
@@ -199,11 +204,31 @@ TensorLayout* tensor_layout(Space& s, int lam, int trank, int parity)
                   for (int o4 = 0; o4 < w; ++o4, ++k) {
                     const int J2 = J1 - lam + o2, Jk = Jb - lam + o4;
                     if (J2 < 0 || Jk < 0 || !triad2(jb, jc, 2 * J2) || !triad2(jd, jc, 2 * Jk)) continue;
-                    t->nj_val[k] = ninej_tensor(h, lam, ja, jb, jc, jd, J1, J2, Jb, Jk);
+                    const double v = ninej_tensor(h, lam, ja, jb, jc, jd, J1, J2, Jb, Jk);
+                    t->nj_val[k] = v;
+                    if (std::fabs(v) >= 1e-8)
+                      t->nj_hat[k] = std::sqrt((double)((2 * J1 + 1) * (2 * J2 + 1) * (2 * Jb + 1) * (2 * Jk + 1))) * v;
                   }
             (void)nJb;
           }
   }
+  // the scalar ladder's gather lists per channel (weights wpp - nn)
+  t->lad_koff.assign(s.nch, 0);
+  t->lad_woff.assign(s.nch, 0);
+  t->lad_n.assign(s.nch, 0);
+  for (const SymGemmJob& jb : s.ladder_jobs) {
+    int c = -1;
+    for (int x = 0; x < s.nch; ++x)
+      if (s.ch[x].n() && s.ch[x].off == jb.a_off) c = x;
+    if (c < 0) continue;
+    t->lad_koff[c] = jb.kidx_off;
+    t->lad_woff[c] = jb.w_off;
+    t->lad_n[c] = jb.K;
+    t->lad_maxelems = std::max(t->lad_maxelems, (long long)jb.m * jb.K);
+  }
+  t->hat2.assign((size_t)t->NJ * t->NJ, 0.0);
+  for (int J1 = 0; J1 < t->NJ; ++J1)
+    for (int J2 = 0; J2 < t->NJ; ++J2) t->hat2[(size_t)J1 * t->NJ + J2] = std::sqrt((double)((2 * J1 + 1) * (2 * J2 + 1)));
   s.tensors[key] = t;
   return t;
 }
@@ -223,7 +248,12 @@ DevTensor tensor_host_view(const TensorLayout& t)
   d.d1x = t.d1x;
   d.nj_base = t.nj_base.empty() ? nullptr : t.nj_base.data();
   d.nj_val = t.nj_val.empty() ? nullptr : t.nj_val.data();
+  d.nj_hat = t.nj_hat.empty() ? nullptr : t.nj_hat.data();
   d.d1 = t.nj_d1;
+  d.hat2 = t.hat2.data();
+  d.lad_koff = t.lad_koff.data();
+  d.lad_woff = t.lad_woff.data();
+  d.lad_n = t.lad_n.data();
   return d;
 }
 
@@ -262,8 +292,13 @@ void tensor_upload(TensorLayout& t)
   d.zb_total = t.zb_total;
   d.yb_total = t.yb_total;
   d.nj_base = dev_copy(t, t.nj_base);
-  d.nj_val = dev_copy(t, t.nj_val);
+  d.nj_val = nullptr;  // the kernels read the hat-weighted table only
+  d.nj_hat = dev_copy(t, t.nj_hat);
   d.d1 = t.nj_d1;
+  d.hat2 = dev_copy(t, t.hat2);
+  d.lad_koff = dev_copy(t, t.lad_koff);
+  d.lad_woff = dev_copy(t, t.lad_woff);
+  d.lad_n = dev_copy(t, t.lad_n);
   t.dev_ready = true;
 }
 

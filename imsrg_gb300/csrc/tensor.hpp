@@ -51,10 +51,19 @@ struct DevTensor {
   // tabulated 9j {ja jd J1; jb jc J2; Jbra Jket lam} for orbit j's (extent
   // d1): nj_base[((a d1 + b) d1 + c) d1 + d] starts an (nJ1, 2 lam + 1, nJbra,
   // 2 lam + 1) block over J1 in [|ja-jd|, ja+jd], J2 = J1 - lam + o2, Jbra in
-  // [|ja-jb|, ja+jb], Jket = Jbra - lam + o4 (see ninej_get)
+  // [|ja-jb|, ja+jb], Jket = Jbra - lam + o4 (see ninej_slot).  nj_val holds
+  // the 9j (host view only); nj_hat the 9j times sqrt((2J1+1)(2J2+1)(2Jbra+1)
+  // (2Jket+1)), exactly 0 where |9j| < 1e-8 (the kernels' skip rule)
   const long long* nj_base = nullptr;
   const double* nj_val = nullptr;
+  const double* nj_hat = nullptr;
   int d1 = 0;
+  const double* hat2 = nullptr;  // [J1 * NJ + J2] = sqrt((2J1+1)(2J2+1))
+  // per two-body channel: the ladder gather list (its start in the space's
+  // kidx / kweight tables and its length, 0 when empty)
+  const int* lad_koff = nullptr;
+  const int* lad_woff = nullptr;
+  const int* lad_n = nullptr;
 };
 
 struct TensorLayout {
@@ -70,14 +79,20 @@ struct TensorLayout {
   std::vector<int> zb_bra, zb_ket, yb_bra, yb_ket;
   std::vector<int64_t> zb_off, yb_off, zb_lookup, yb_lookup;
   std::vector<long long> nj_base;
-  std::vector<double> nj_val;
+  std::vector<double> nj_val, nj_hat;
   int nj_d1 = 0;  // orbit j extent of the 9j table
+  std::vector<double> hat2;
+  std::vector<int> lad_koff, lad_woff, lad_n;
+  long long lad_maxelems = 0;  // largest n_channel x gather length (grid sizing)
   int64_t zb_total = 0, yb_total = 0;
   int zb_maxelems = 0, yb_maxelems = 0;  // largest block of each list (grid sizing)
   int max_blk_elems = 0;                 // largest two-body block of the layout
+  long long max_pair_elems = 0;          // largest n_bra x ceil(n_ket / 2) (column pairs)
   // scratch of the scalar-tensor commutator (device, lazily allocated):
-  // Mpp, Mhh (layout total), X bar (the space's xb_total), Y bar, Z bar
+  // Mpp - Mhh, Mhh (layout total), X bar (the space's xb_total), Y bar, Z bar,
+  // and the two weighted copies of X the ladder reads (the space's arena each)
   double *d_mpp = nullptr, *d_mhh = nullptr, *d_xbar = nullptr, *d_ybar = nullptr, *d_zbar = nullptr;
+  double *d_xw = nullptr, *d_wx = nullptr;
   DevTensor dev;
   bool dev_ready = false;
   std::vector<void*> dev_allocs;
@@ -143,20 +158,35 @@ IMSRG_HD double ninej_tensor(const DevTensor& T, int lam, int ja, int jb, int jc
   return s;
 }
 
-// the tabulated 9j (the same value as ninej_tensor), 0 outside its windows
-IMSRG_HD double ninej_get(const DevTensor& T, int ja, int jb, int jc, int jd, int J1, int J2, int Jbra, int Jket)
+// slot of {ja jd J1; jb jc J2; Jbra Jket lam} in the 9j tables, -1 outside
+// their windows
+IMSRG_HD long long ninej_slot(const DevTensor& T, int ja, int jb, int jc, int jd, int J1, int J2, int Jbra, int Jket)
 {
   const int d1 = T.d1, L = T.lam, w = 2 * L + 1;
   const int a = (ja - 1) >> 1, b = (jb - 1) >> 1, c = (jc - 1) >> 1, d = (jd - 1) >> 1;
-  if (a < 0 || b < 0 || c < 0 || d < 0 || a >= d1 || b >= d1 || c >= d1 || d >= d1) return 0.0;
+  if (a < 0 || b < 0 || c < 0 || d < 0 || a >= d1 || b >= d1 || c >= d1 || d >= d1) return -1;
   const int J1min = (ja > jd ? ja - jd : jd - ja) >> 1, J1max = (ja + jd) >> 1;
   const int Jbmin = (ja > jb ? ja - jb : jb - ja) >> 1, Jbmax = (ja + jb) >> 1;
   const int o2 = J2 - J1 + L, o4 = Jket - Jbra + L;
-  if (J1 < J1min || J1 > J1max || Jbra < Jbmin || Jbra > Jbmax || o2 < 0 || o2 >= w || o4 < 0 || o4 >= w) return 0.0;
+  if (J1 < J1min || J1 > J1max || Jbra < Jbmin || Jbra > Jbmax || o2 < 0 || o2 >= w || o4 < 0 || o4 >= w) return -1;
   const int nJb = Jbmax - Jbmin + 1;
-  const long long k = T.nj_base[((a * d1 + b) * d1 + c) * d1 + d] +
-                      (((long long)(J1 - J1min) * w + o2) * nJb + (Jbra - Jbmin)) * w + o4;
-  return T.nj_val[k];
+  return T.nj_base[((a * d1 + b) * d1 + c) * d1 + d] +
+         (((long long)(J1 - J1min) * w + o2) * nJb + (Jbra - Jbmin)) * w + o4;
+}
+
+// the tabulated 9j (the same value as ninej_tensor), 0 outside its windows
+IMSRG_HD double ninej_get(const DevTensor& T, int ja, int jb, int jc, int jd, int J1, int J2, int Jbra, int Jket)
+{
+  const long long k = ninej_slot(T, ja, jb, jc, jd, J1, J2, Jbra, Jket);
+  return k < 0 ? 0.0 : T.nj_val[k];
+}
+
+// hat-weighted 9j: sqrt((2J1+1)(2J2+1)(2Jbra+1)(2Jket+1)) {ja jd J1; jb jc J2;
+// Jbra Jket lam}, 0 where |9j| < 1e-8 or outside the windows
+IMSRG_HD double ninej_hat(const DevTensor& T, int ja, int jb, int jc, int jd, int J1, int J2, int Jbra, int Jket)
+{
+  const long long k = ninej_slot(T, ja, jb, jc, jd, J1, J2, Jbra, Jket);
+  return k < 0 ? 0.0 : T.nj_hat[k];
 }
 
 }  // namespace imsrg
