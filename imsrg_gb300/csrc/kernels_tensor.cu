@@ -232,10 +232,11 @@ __global__ void k_t122(DevSpace S, DevTensor T, const double* __restrict__ X, co
                        double* __restrict__ Z)
 {
   const int blk = blockIdx.y;
-  const int chb = T.bra[blk], chk = T.ket[blk];
+  const int chb = T.bra[blk], chk = T.ket[blk];  // chb <= chk: the element's own block is stored
   const int nb = S.ch_n[chb], nk = S.ch_n[chk];
   long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (e >= (long long)nb * nk) return;
+  (void)hY;
   const int ik = (int)(e / nb), ib = (int)(e - (long long)ik * nb);
   const int N = S.norb, Lam = T.lam;
   const int i = S.ket_p[S.ch_kofs[chb] + ib], j = S.ket_q[S.ch_kofs[chb] + ib];
@@ -244,62 +245,99 @@ __global__ void k_t122(DevSpace S, DevTensor T, const double* __restrict__ X, co
   const int ji = S.j2[i], jj = S.j2[j], jk = S.j2[k], jl = S.j2[l];
   const double* X1 = X + 32;
   const double* Y1 = Y + 32;
+  // <ab|Y|kl> for a bra (a, b) of chb: column ik of the element's block;
+  // <ij|Y|cd> for a ket (c, d) of chk: row ib of it (TwoBodyME::GetTBME with
+  // the swap phase and sqrt(2) of the bra or ket that varies; the fixed side's
+  // sqrt(2) is applied to the sums)
+  const double* Yblk = Y + T.off[blk];
+  const double* Ycol = Yblk + (long long)ik * nb;
+  auto y_bra = [&](int a, int b) -> double {
+    const int bi = ket_in(S, chb, a, b);
+    if (bi < 0) return 0.0;
+    double v = flip(Ycol[bi], a > b ? ((S.j2[a] + S.j2[b]) >> 1) + 1 + J1 : 0);
+    return a == b ? v * kSqrt2t : v;
+  };
+  auto y_ket = [&](int c, int d) -> double {
+    const int ki = ket_in(S, chk, c, d);
+    if (ki < 0) return 0.0;
+    double v = flip(Yblk[(long long)ki * nb + ib], c > d ? ((S.j2[c] + S.j2[d]) >> 1) + 1 + J2 : 0);
+    return c == d ? v * kSqrt2t : v;
+  };
+  // scalar <ab|X|kl>_(J2) (column ik of X's chk block) and <ij|X|cd>_(J1)
+  // (row ib of X's chb block)
+  const double* Xk = X + S.ch_off[chk] + (long long)ik * nk;
+  const double* Xb = X + S.ch_off[chb] + ib;
+  auto x_bra = [&](int a, int b) -> double {
+    const int bi = ket_in(S, chk, a, b);
+    if (bi < 0) return 0.0;
+    double v = flip(Xk[bi], a > b ? ((S.j2[a] + S.j2[b]) >> 1) + 1 + J2 : 0);
+    return a == b ? v * kSqrt2t : v;
+  };
+  auto x_ket = [&](int c, int d) -> double {
+    const int ki = ket_in(S, chb, c, d);
+    if (ki < 0) return 0.0;
+    double v = flip(Xb[(long long)ki * nb], c > d ? ((S.j2[c] + S.j2[d]) >> 1) + 1 + J1 : 0);
+    return c == d ? v * kSqrt2t : v;
+  };
+  const double sk = k == l ? kSqrt2t : 1.0, sb = i == j ? kSqrt2t : 1.0;
+  // X one-body, Y two-body
   double c1 = 0, c2 = 0, c3 = 0, c4 = 0;
   for (int q = 0; q < S.ob_count[i]; ++q) {
-    int a = S.ob_list[S.ob_start[i] + q];
-    c1 += X1[(long long)a * N + i] * y_tbme(S, T, Y, hY, chb, chk, a, j, k, l);
+    const int a = S.ob_list[S.ob_start[i] + q];
+    c1 = fma(X1[(long long)a * N + i], y_bra(a, j), c1);
   }
   if (i == j) {
     c2 = c1;
   } else {
     for (int q = 0; q < S.ob_count[j]; ++q) {
-      int a = S.ob_list[S.ob_start[j] + q];
-      c2 += X1[(long long)a * N + j] * y_tbme(S, T, Y, hY, chb, chk, i, a, k, l);
+      const int a = S.ob_list[S.ob_start[j] + q];
+      c2 = fma(X1[(long long)a * N + j], y_bra(i, a), c2);
     }
   }
   for (int q = 0; q < S.ob_count[k]; ++q) {
-    int a = S.ob_list[S.ob_start[k] + q];
-    c3 += X1[(long long)k * N + a] * y_tbme(S, T, Y, hY, chb, chk, i, j, a, l);
+    const int a = S.ob_list[S.ob_start[k] + q];
+    c3 = fma(X1[(long long)k * N + a], y_ket(a, l), c3);
   }
   if (k == l) {
     c4 = c3;
   } else {
     for (int q = 0; q < S.ob_count[l]; ++q) {
-      int a = S.ob_list[S.ob_start[l] + q];
-      c4 += X1[(long long)l * N + a] * y_tbme(S, T, Y, hY, chb, chk, i, j, k, a);
+      const int a = S.ob_list[S.ob_start[l] + q];
+      c4 = fma(X1[(long long)l * N + a], y_ket(k, a), c4);
     }
   }
-  double cijkl = c1 + c2 - c3 - c4;
+  double cijkl = (c1 + c2) * sk - (c3 + c4) * sb;
+  // Y one-body, X two-body
   c1 = c2 = c3 = c4 = 0;
-  const int odd1 = ((ji + jj) >> 1) + J2 + Lam;
-  const int odd2 = J1 - J2 + Lam, odd3 = odd2;
-  const int odd4 = ((jk + jl) >> 1) - J1 + Lam;
-  for (int a = 0; a < N; ++a) {
-    if (!T.ob_ok[i * N + a]) continue;
-    c1 -= sixjA(T, J2, J1, ji, S.j2[a], jj) * Y1[(long long)a * N + i] * x_tbme(S, X, chk, a, j, k, l);
+  for (int q = T.tob_off[i]; q < T.tob_off[i + 1]; ++q) {
+    const int a = T.tob_list[q];
+    c1 -= sixjA(T, J2, J1, ji, S.j2[a], jj) * Y1[(long long)a * N + i] * x_bra(a, j);
   }
   if (i == j) {
     c2 = -c1;
   } else {
-    for (int a = 0; a < N; ++a) {
-      if (!T.ob_ok[j * N + a]) continue;
-      c2 += sixjA(T, J2, J1, jj, S.j2[a], ji) * Y1[(long long)a * N + j] * x_tbme(S, X, chk, a, i, k, l);
+    for (int q = T.tob_off[j]; q < T.tob_off[j + 1]; ++q) {
+      const int a = T.tob_list[q];
+      c2 += sixjA(T, J2, J1, jj, S.j2[a], ji) * Y1[(long long)a * N + j] * x_bra(a, i);
     }
   }
-  for (int a = 0; a < N; ++a) {
-    if (!T.ob_ok[a * N + k]) continue;
-    c3 -= sixjA(T, J1, J2, jk, S.j2[a], jl) * Y1[(long long)k * N + a] * x_tbme(S, X, chb, i, j, l, a);
+  for (int q = T.tob_off[k]; q < T.tob_off[k + 1]; ++q) {
+    const int a = T.tob_list[q];
+    c3 -= sixjA(T, J1, J2, jk, S.j2[a], jl) * Y1[(long long)k * N + a] * x_ket(l, a);
   }
   if (k == l) {
     c4 = -c3;
   } else {
-    for (int a = 0; a < N; ++a) {
-      if (!T.ob_ok[a * N + l]) continue;
-      c4 += sixjA(T, J1, J2, jl, S.j2[a], jk) * Y1[(long long)l * N + a] * x_tbme(S, X, chb, i, j, k, a);
+    for (int q = T.tob_off[l]; q < T.tob_off[l + 1]; ++q) {
+      const int a = T.tob_list[q];
+      c4 += sixjA(T, J1, J2, jl, S.j2[a], jk) * Y1[(long long)l * N + a] * x_ket(k, a);
     }
   }
+  const int odd1 = ((ji + jj) >> 1) + J2 + Lam;
+  const int odd2 = J1 - J2 + Lam, odd3 = odd2;
+  const int odd4 = ((jk + jl) >> 1) - J1 + Lam;
   const double hat = T.hat2[J1 * T.NJ + J2];
-  cijkl += hat * (flip(c1, odd1) + flip(c2, odd2) + flip(c3, odd3) + flip(c4, odd4));
+  cijkl += hat * ((flip(c1, odd1) + flip(c2, odd2)) * sk + (flip(c3, odd3) + flip(c4, odd4)) * sb);
   Z[T.off[blk] + (long long)ik * nb + ib] += unnorm(cijkl, i == j, k == l);
 }
 
@@ -470,11 +508,12 @@ __global__ void k_tpandya(DevSpace S, DevWork W, DevTensor T, const double* __re
   const int ja = S.j2[a], jb = S.j2[b], jc = S.j2[c], jd = S.j2[d];
   double sm = 0.0;
   const int J1min = abs(ja - jd) >> 1, J1max = (ja + jd) >> 1;
+  const NineJRow nj = ninej_row(T, ja, jb, jc, jd, Jbra, Jket);
   for (int J1 = J1min; J1 <= J1max; ++J1) {
     const int J2min = max(abs(jc - jb) >> 1, abs(J1 - Lam)), J2max = min((jc + jb) >> 1, J1 + Lam);
     for (int J2 = J2min; J2 <= J2max; ++J2) {
       // sm -= hat (-1)^(jb+jd+Jket+J2) 9j tbme; the table holds hat 9j, 0 where |9j| < 1e-8
-      const double nh = ninej_hat(T, ja, jb, jc, jd, J1, J2, Jbra, Jket);
+      const double nh = nj.get(J1, J2);
       if (is_zero(nh)) continue;
       const double tbme = y_tbme_J(S, T, Y, hY, J1, J2, a, d, c, b);
       sm = fma(flip(nh, 1 + ((jb + jd) >> 1) + Jket + J2), tbme, sm);
@@ -538,28 +577,55 @@ __global__ void k_tzbar(DevSpace S, DevWork W, DevTensor T, const double* __rest
   Zb[T.zb_off[p] + (long long)col * nlo + r] = s;
 }
 
-// Zbar element (il | kj) of cross-coupled channels (cbra, cket) as the
-// inverse transform reads it (src/TensorCommutators.cc:830-852)
-__device__ double zbar_get(const DevSpace& S, const DevTensor& T, const double* Zb, int hZ, int cbra, int cket,
-                           int i, int l, int k, int j, int ji, int jj, int jk, int jl, int J3, int J4, bool* found)
+// sum over the cross-coupled channels (J3 for (i, l), J4 for (k, j)) of
+// hat 9j (-1)^(j_j' + jl + J2 + J4) Zbar(il | kj): one of the two sums of the
+// inverse tensor Pandya transform (src/TensorCommutators.cc:790-900), with the
+// orbits (i, j) of the bra taken as given (the caller swaps them for the
+// other sum).  Zbar of (cbra, cket) is stored in the block of (lo, hi) =
+// (min, max) as n_lo x 2 n_hi; the element's place and phase follow the
+// reference's four cases (src/TensorCommutators.cc:830-852).
+__device__ double tinv_sum(const DevSpace& S, const DevTensor& T, const double* Zb, int hZ, int i, int j, int k,
+                           int l, int J1, int J2)
 {
-  const int lo = min(cbra, cket), hi = max(cbra, cket);
-  const long long off = T.zb_lookup[lo * S.nch + hi];
-  *found = off >= 0;
-  if (off < 0) return 0.0;
-  const int nbras = S.cc_n[cbra], nkets = S.cc_n[cket];
-  const int ixil = S.ccJ_loc[J3 * S.nkets + ket_index(S.norb, min(i, l), max(i, l))];
-  const int ixkj = S.ccJ_loc[J4 * S.nkets + ket_index(S.norb, min(j, k), max(j, k))];
-  const double* M = Zb + off;
-  const int nrow = S.cc_n[lo];
-  const int sum4 = (ji + jj + jk + jl) >> 1;
-  const int hneg = hZ < 0;
-  if (cbra <= cket) {
-    if (i <= l) return M[(long long)(ixkj + (k > j ? nkets : 0)) * nrow + ixil];
-    return flip(M[(long long)(ixkj + (k > j ? 0 : nkets)) * nrow + ixil], hneg + J3 - J4 + sum4);
+  const int ji = S.j2[i], jj = S.j2[j], jk = S.j2[k], jl = S.j2[l], Lam = T.lam;
+  const int pbc = (S.l[i] + S.l[l]) & 1, pkc = (S.l[k] + S.l[j]) & 1;
+  const int tbc = abs(S.tz2[i] - S.tz2[l]) / 2, tkc = abs(S.tz2[k] - S.tz2[j]) / 2;
+  const int kil = ket_index(S.norb, min(i, l), max(i, l)), kkj = ket_index(S.norb, min(j, k), max(j, k));
+  const int sum4 = (ji + jj + jk + jl) >> 1, hneg = hZ < 0;
+  const NineJRow nj = ninej_row(T, ji, jj, jk, jl, J1, J2);
+  const int J3min = abs(ji - jl) >> 1, J3max = (ji + jl) >> 1;
+  double acc = 0.0;
+  for (int J3 = J3min; J3 <= J3max; ++J3) {
+    const int cbra = chan_index(J3, pbc, tbc);
+    const int ixil = S.ccJ_loc[J3 * S.nkets + kil];
+    const int nbras = S.cc_n[cbra];
+    const int J4min = max(abs(jk - jj) >> 1, abs(J3 - Lam)), J4max = min((jk + jj) >> 1, J3 + Lam);
+    for (int J4 = J4min; J4 <= J4max; ++J4) {
+      const double nh = nj.get(J3, J4);
+      if (is_zero(nh)) continue;
+      const int cket = chan_index(J4, pkc, tkc);
+      const int lo = min(cbra, cket), hi = max(cbra, cket);
+      const long long off = T.zb_lookup[lo * S.nch + hi];
+      if (off < 0) continue;
+      const int ixkj = S.ccJ_loc[J4 * S.nkets + kkj];
+      const double* M = Zb + off;
+      const int nrow = S.cc_n[lo];
+      double z;
+      if (cbra <= cket) {
+        if (i <= l)
+          z = M[(long long)(ixkj + (k > j ? S.cc_n[cket] : 0)) * nrow + ixil];
+        else
+          z = flip(M[(long long)(ixkj + (k > j ? 0 : S.cc_n[cket])) * nrow + ixil], hneg + J3 - J4 + sum4);
+      } else {
+        if (k <= j)
+          z = flip(M[(long long)(ixil + (i > l ? nbras : 0)) * nrow + ixkj], hneg + J3 - J4);
+        else
+          z = flip(M[(long long)(ixil + (i > l ? 0 : nbras)) * nrow + ixkj], sum4);
+      }
+      acc = fma(flip(nh, ((jj + jl) >> 1) + J2 + J4), z, acc);
+    }
   }
-  if (k <= j) return flip(M[(long long)(ixil + (i > l ? nbras : 0)) * nrow + ixkj], hneg + J3 - J4);
-  return flip(M[(long long)(ixil + (i > l ? 0 : nbras)) * nrow + ixkj], sum4);
+  return acc;
 }
 
 // inverse tensor Pandya transform, AddInverseTensorPandyaTransformation
@@ -577,48 +643,10 @@ __global__ void k_tinv(DevSpace S, DevTensor T, const double* __restrict__ Zb, i
   if (chb == chk && ik < ib) return;
   const int i = S.ket_p[S.ch_kofs[chb] + ib], j = S.ket_q[S.ch_kofs[chb] + ib];
   const int k = S.ket_p[S.ch_kofs[chk] + ik], l = S.ket_q[S.ch_kofs[chk] + ik];
-  const int J1 = ch_J(chb), J2 = ch_J(chk), Lam = T.lam;
-  const int ji = S.j2[i], jj = S.j2[j], jk = S.j2[k], jl = S.j2[l];
-  double commij = 0.0, commji = 0.0;
-  {
-    const int pbc = (S.l[i] + S.l[l]) & 1, pkc = (S.l[k] + S.l[j]) & 1;
-    const int tbc = abs(S.tz2[i] - S.tz2[l]) / 2, tkc = abs(S.tz2[k] - S.tz2[j]) / 2;
-    const int J3min = abs(ji - jl) >> 1, J3max = (ji + jl) >> 1;
-    for (int J3 = J3min; J3 <= J3max; ++J3) {
-      const int cbra = chan_index(J3, pbc, tbc);
-      const int J4min = max(abs(jk - jj) >> 1, abs(J3 - Lam)), J4max = min((jk + jj) >> 1, J3 + Lam);
-      for (int J4 = J4min; J4 <= J4max; ++J4) {
-        const int cket = chan_index(J4, pkc, tkc);
-        // commij += hat (-1)^(jj+jl+J2+J4) 9j tbme (the table holds hat 9j)
-        const double nh = ninej_hat(T, ji, jj, jk, jl, J3, J4, J1, J2);
-        if (is_zero(nh)) continue;
-        bool found;
-        const double tbme = zbar_get(S, T, Zb, hZ, cbra, cket, i, l, k, j, ji, jj, jk, jl, J3, J4, &found);
-        if (!found) continue;
-        commij = fma(flip(nh, ((jj + jl) >> 1) + J2 + J4), tbme, commij);
-      }
-    }
-  }
-  if (i == j) {
-    commji = commij;
-  } else {
-    const int pbc = (S.l[j] + S.l[l]) & 1, pkc = (S.l[k] + S.l[i]) & 1;
-    const int tbc = abs(S.tz2[j] - S.tz2[l]) / 2, tkc = abs(S.tz2[k] - S.tz2[i]) / 2;
-    const int J3min = abs(jj - jl) >> 1, J3max = (jj + jl) >> 1;
-    for (int J3 = J3min; J3 <= J3max; ++J3) {
-      const int cbra = chan_index(J3, pbc, tbc);
-      const int J4min = max(abs(jk - ji) >> 1, abs(J3 - Lam)), J4max = min((jk + ji) >> 1, J3 + Lam);
-      for (int J4 = J4min; J4 <= J4max; ++J4) {
-        const int cket = chan_index(J4, pkc, tkc);
-        const double nh = ninej_hat(T, jj, ji, jk, jl, J3, J4, J1, J2);
-        if (is_zero(nh)) continue;
-        bool found;
-        const double tbme = zbar_get(S, T, Zb, hZ, cbra, cket, j, l, k, i, jj, ji, jk, jl, J3, J4, &found);
-        if (!found) continue;
-        commji = fma(flip(nh, ((ji + jl) >> 1) + J2 + J4), tbme, commji);
-      }
-    }
-  }
+  const int J1 = ch_J(chb), J2 = ch_J(chk);
+  const int ji = S.j2[i], jj = S.j2[j];
+  const double commij = tinv_sum(S, T, Zb, hZ, i, j, k, l, J1, J2);
+  const double commji = i == j ? commij : tinv_sum(S, T, Zb, hZ, j, i, k, l, J1, J2);
   const double z = unnorm(commij + flip(commji, 1 + ((ji + jj) >> 1) - J1), i == j, k == l);
   Z[T.off[blk] + (long long)ik * nb + ib] += z;
   if (chb == chk && ik != ib) Z[T.off[blk] + (long long)ib * nb + ik] += flip(z, hZ < 0);

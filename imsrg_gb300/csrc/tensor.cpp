@@ -151,6 +151,15 @@ TensorLayout* tensor_layout(Space& s, int lam, int trank, int parity)
     for (int j = 0; j < N; ++j)
       t->ob_ok[(size_t)i * N + j] = ((s.l[i] + s.l[j] + parity) % 2 == 0) && triad2(s.j2[i], s.j2[j], 2 * lam) &&
                                     std::abs(s.tz2[i] - s.tz2[j]) == 2 * trank;
+  // the same as lists: tob_list[tob_off[i] .. tob_off[i + 1]) = the j with ob_ok(i, j)
+  t->tob_off.assign(N + 1, 0);
+  t->tob_list.clear();
+  for (int i = 0; i < N; ++i) {
+    t->tob_off[i] = (int)t->tob_list.size();
+    for (int j = 0; j < N; ++j)
+      if (t->ob_ok[(size_t)i * N + j]) t->tob_list.push_back(j);
+  }
+  t->tob_off[N] = (int)t->tob_list.size();
   // angular tables, half-integers widened by lam (the 9j sums reach j + lam)
   t->NJ = s.NJ;
   t->d1x = s.d1 + lam;
@@ -251,6 +260,8 @@ DevTensor tensor_host_view(const TensorLayout& t)
   d.nj_hat = t.nj_hat.empty() ? nullptr : t.nj_hat.data();
   d.d1 = t.nj_d1;
   d.hat2 = t.hat2.data();
+  d.tob_off = t.tob_off.data();
+  d.tob_list = t.tob_list.data();
   d.lad_koff = t.lad_koff.data();
   d.lad_woff = t.lad_woff.data();
   d.lad_n = t.lad_n.data();
@@ -296,6 +307,8 @@ void tensor_upload(TensorLayout& t)
   d.nj_hat = dev_copy(t, t.nj_hat);
   d.d1 = t.nj_d1;
   d.hat2 = dev_copy(t, t.hat2);
+  d.tob_off = dev_copy(t, t.tob_off);
+  d.tob_list = dev_copy(t, t.tob_list);
   d.lad_koff = dev_copy(t, t.lad_koff);
   d.lad_woff = dev_copy(t, t.lad_woff);
   d.lad_n = dev_copy(t, t.lad_n);

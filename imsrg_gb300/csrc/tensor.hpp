@@ -59,6 +59,10 @@ struct DevTensor {
   const double* nj_hat = nullptr;
   int d1 = 0;
   const double* hat2 = nullptr;  // [J1 * NJ + J2] = sqrt((2J1+1)(2J2+1))
+  // per orbit i: the orbits j with <i||T||j> allowed (tob_list[tob_off[i] ..
+  // tob_off[i + 1]))
+  const int* tob_off = nullptr;
+  const int* tob_list = nullptr;
   // per two-body channel: the ladder gather list (its start in the space's
   // kidx / kweight tables and its length, 0 when empty)
   const int* lad_koff = nullptr;
@@ -83,6 +87,7 @@ struct TensorLayout {
   int nj_d1 = 0;  // orbit j extent of the 9j table
   std::vector<double> hat2;
   std::vector<int> lad_koff, lad_woff, lad_n;
+  std::vector<int> tob_off, tob_list;
   long long lad_maxelems = 0;  // largest n_channel x gather length (grid sizing)
   int64_t zb_total = 0, yb_total = 0;
   int zb_maxelems = 0, yb_maxelems = 0;  // largest block of each list (grid sizing)
@@ -179,6 +184,39 @@ IMSRG_HD double ninej_get(const DevTensor& T, int ja, int jb, int jc, int jd, in
 {
   const long long k = ninej_slot(T, ja, jb, jc, jd, J1, J2, Jbra, Jket);
   return k < 0 ? 0.0 : T.nj_val[k];
+}
+
+// the hat-weighted 9j of fixed (ja, jb, jc, jd, Jbra, Jket) as a function of
+// (J1, J2): one row of the table, read with one load per (J1, J2)
+struct NineJRow {
+  const double* p = nullptr;  // slot of (J1min, o2 = 0)
+  long long stride = 0;       // between consecutive (J1, o2) slots
+  int J1min = 0, J1max = -1, w = 0, L = 0;
+  IMSRG_HD double get(int J1, int J2) const
+  {
+    const int o2 = J2 - J1 + L;
+    if (!p || J1 < J1min || J1 > J1max || o2 < 0 || o2 >= w) return 0.0;
+    return p[((long long)(J1 - J1min) * w + o2) * stride];
+  }
+};
+
+IMSRG_HD NineJRow ninej_row(const DevTensor& T, int ja, int jb, int jc, int jd, int Jbra, int Jket)
+{
+  NineJRow r;
+  const int d1 = T.d1, L = T.lam, w = 2 * L + 1;
+  const int a = (ja - 1) >> 1, b = (jb - 1) >> 1, c = (jc - 1) >> 1, d = (jd - 1) >> 1;
+  if (a < 0 || b < 0 || c < 0 || d < 0 || a >= d1 || b >= d1 || c >= d1 || d >= d1) return r;
+  const int Jbmin = (ja > jb ? ja - jb : jb - ja) >> 1, Jbmax = (ja + jb) >> 1;
+  const int o4 = Jket - Jbra + L;
+  if (Jbra < Jbmin || Jbra > Jbmax || o4 < 0 || o4 >= w) return r;
+  const int nJb = Jbmax - Jbmin + 1;
+  r.p = T.nj_hat + T.nj_base[((a * d1 + b) * d1 + c) * d1 + d] + (long long)(Jbra - Jbmin) * w + o4;
+  r.stride = (long long)nJb * w;
+  r.J1min = (ja > jd ? ja - jd : jd - ja) >> 1;
+  r.J1max = (ja + jd) >> 1;
+  r.w = w;
+  r.L = L;
+  return r;
 }
 
 // hat-weighted 9j: sqrt((2J1+1)(2J2+1)(2Jbra+1)(2Jket+1)) {ja jd J1; jb jc J2;
