@@ -752,7 +752,8 @@ def run_batch(args):
     print(json.dumps(out))
 
 
-TENSOR_METRIC = "ms per scalar-tensor commutator [X,T], rank (J,dTz,parity)=(2,0,+), emax={emax}, FP64, 1 GB300"
+TENSOR_METRIC = ("ms per scalar-tensor commutator [X,T], rank (J,dTz,parity)=(2,0,+), emax={emax}: {form} form "
+                 "(split-prec vs FP64 products), 1 GB300")
 
 
 def random_tensor(ms, seed, rank, hermitian=True):
@@ -792,6 +793,11 @@ def random_tensor(ms, seed, rank, hermitian=True):
 
 
 def run_tensor(args):
+    """Scalar-tensor commutator [X, T] at emax (default 8), both forms of its
+    ladder and Z bar products: split (tensor cores) and FP64.  `value` is the
+    form --precision names; the other is reported beside it, with the
+    relative difference of the two results per body rank."""
+    import numpy as np
     import torch
 
     import imsrg_gb300 as ig
@@ -806,41 +812,55 @@ def run_tensor(args):
     dT = ig.DeviceOperator(ms, 1, rk)
     dT.upload(random_tensor(ms, 41 + rank, rk))
     dZ = ig.DeviceOperator(ms, 1, rk)
-    for _ in range(max(3, args.warmup)):
-        ig.Commutator.device_scalar_tensor(dX, dT, dZ)
-    torch.cuda.synchronize()
-    L.imsrg_profiler_reset()
-    L.imsrg_profiler_enable(1)
-    l0 = L.imsrg_kernel_launches()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        ig.Commutator.device_scalar_tensor(dX, dT, dZ)
-    e1.record()
-    torch.cuda.synchronize()
-    launches = L.imsrg_kernel_launches() - l0
-    L.imsrg_profiler_enable(0)
-    n = L.imsrg_profiler_names(None, 0)
-    buf = ctypes.create_string_buffer(n)
-    L.imsrg_profiler_names(buf, n)
-    phases = {}
-    for name in [x for x in buf.value.decode().split("\n") if x]:
-        t = ctypes.c_double()
-        c = ctypes.c_longlong()
-        L.imsrg_profiler_get(name.encode(), ctypes.byref(t), ctypes.byref(c))
-        phases[name] = t.value / args.steps
-    ms_step = e0.elapsed_time(e1) / args.steps
+
+    def timed(prec):
+        for _ in range(max(3, args.warmup)):
+            ig.Commutator.device_scalar_tensor(dX, dT, dZ, prec)
+        torch.cuda.synchronize()
+        L.imsrg_profiler_reset()
+        L.imsrg_profiler_enable(1)
+        l0 = L.imsrg_kernel_launches()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            ig.Commutator.device_scalar_tensor(dX, dT, dZ, prec)
+        e1.record()
+        torch.cuda.synchronize()
+        launches = L.imsrg_kernel_launches() - l0
+        L.imsrg_profiler_enable(0)
+        n = L.imsrg_profiler_names(None, 0)
+        buf = ctypes.create_string_buffer(n)
+        L.imsrg_profiler_names(buf, n)
+        phases = {}
+        for name in [x for x in buf.value.decode().split("\n") if x]:
+            t = ctypes.c_double()
+            c = ctypes.c_longlong()
+            L.imsrg_profiler_get(name.encode(), ctypes.byref(t), ctypes.byref(c))
+            phases[name] = t.value / args.steps
+        return e0.elapsed_time(e1) / args.steps, phases, int(launches), dZ.download()
+
+    forms = [args.precision] + [p for p in ("split", "fp64") if p != args.precision]
+    res = {p: timed(p) for p in forms}
+    ms_step, phases, launches, Zv = res[args.precision]
+    Zo = res[forms[1]][3]
+    N = ms.norb
+    diff = []
+    for a, b in ((Zv[32:32 + N * N], Zo[32:32 + N * N]), (Zv[32 + N * N:], Zo[32 + N * N:])):
+        nb = np.linalg.norm(b)
+        diff.append(float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a - b)))
     if rank != 0:
         return
     out = {
-        "metric": TENSOR_METRIC.format(emax=emax), "value": ms_step, "unit": "ms/commutator", "n_gpus": world,
-        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_step, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "metric": TENSOR_METRIC.format(emax=emax, form=args.precision), "value": ms_step, "unit": "ms/commutator",
+        "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_step,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "CommutatorScalarTensor [X, T], X random hermitian scalar, T random hermitian "
                                "reduced tensor of rank (2, 0, 0), emax=%d O16" % emax, "emax": emax,
-                   "tensor_arena_doubles": dT.size},
-        "phases_ms_per_step": phases, "gpu_launches": int(launches),
+                   "tensor_arena_doubles": dT.size, "precision": args.precision},
+        "phases_ms_per_step": phases, "gpu_launches": launches,
+        forms[1]: {"ms_per_step": res[forms[1]][0], "phases_ms_per_step": res[forms[1]][1]},
+        "rel_diff_%s_vs_%s" % (forms[0], forms[1]): {"one_body": diff[0], "two_body": diff[1]},
         "cpu_baseline": {"value": None, "unit": "ms/commutator", "kind": "port",
                          "sample": "not measured: the C oracle restates the scalar-scalar path only"},
     }

@@ -52,12 +52,12 @@ SIGNATURES = {
     "imsrg_op_rank": (I, [P, IP, IP, IP, LLP]),
     "imsrg_space_tensor_layout": (I, [P, I, I, I, I, IP, IP, LLP, IP, LLP]),
     "imsrg_space_ninej": (I, [P, I, I, I, I, I, I, I, I, I, DP]),
-    "imsrg_commutator_scalar_tensor": (I, [P, P, P, P]),
+    "imsrg_commutator_scalar_tensor": (I, [P, P, P, I, P]),
     "imsrg_comm111st": (I, [P, P, P, P]),
     "imsrg_comm121st": (I, [P, P, P, P]),
     "imsrg_comm122st": (I, [P, P, P, P]),
-    "imsrg_comm222_pp_hh_221st": (I, [P, P, P, P]),
-    "imsrg_comm222_phst": (I, [P, P, P, P]),
+    "imsrg_comm222_pp_hh_221st": (I, [P, P, P, I, P]),
+    "imsrg_comm222_phst": (I, [P, P, P, I, P]),
     "imsrg_op_destroy": (None, [P]),
     "imsrg_op_hermiticity": (I, [P, IP]),
     "imsrg_op_set_hermiticity": (I, [P, I]),

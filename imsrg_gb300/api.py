@@ -446,26 +446,33 @@ class _CommutatorNamespace:
             Z.hermitian = dz.hermiticity
         return Z
 
-    def CommutatorScalarTensor(self, X, Y):
+    def CommutatorScalarTensor(self, X, Y, precision=None):
         """Commutator::CommutatorScalarTensor(X, Y): X scalar, Y a reduced tensor."""
         ms = X.modelspace
         Z = Operator(ms, *Y.rank)
         with DeviceOperator.from_host(X) as dx, DeviceOperator.from_host(Y) as dy, \
                 DeviceOperator(ms, 1, Y.rank) as dz:
-            self.device_scalar_tensor(dx, dy, dz)
+            self.device_scalar_tensor(dx, dy, dz, precision)
             dz.download(Z.arena)
             Z.hermitian = dz.hermiticity
         return Z
 
-    def device_scalar_tensor(self, dX, dY, dZ, stream=None):
-        check(_lib.lib().imsrg_commutator_scalar_tensor(dX._h, dY._h, dZ._h, stream))
+    def device_scalar_tensor(self, dX, dY, dZ, precision=None, stream=None):
+        check(_lib.lib().imsrg_commutator_scalar_tensor(dX._h, dY._h, dZ._h, _precision(precision), stream))
 
-    def device_tensor_term(self, name, dX, dY, dZ, stream=None):
+    _TERMS_STP = ("comm222_pp_hh_221st", "comm222_phst")
+
+    def device_tensor_term(self, name, dX, dY, dZ, precision=None, stream=None):
         """One scalar-tensor term (comm111st, comm121st, comm122st,
-        comm222_pp_hh_221st, comm222_phst) accumulated into dZ."""
+        comm222_pp_hh_221st, comm222_phst) accumulated into dZ; precision
+        applies to the two with products."""
         if name not in self._TERMS_ST:
             raise KeyError(name)
-        check(getattr(_lib.lib(), "imsrg_" + name)(dX._h, dY._h, dZ._h, stream))
+        fn = getattr(_lib.lib(), "imsrg_" + name)
+        if name in self._TERMS_STP:
+            check(fn(dX._h, dY._h, dZ._h, _precision(precision), stream))
+        else:
+            check(fn(dX._h, dY._h, dZ._h, stream))
 
     def Commutator(self, X, Y, precision=None):
         """Commutator::Commutator: dispatch on the tensor ranks
@@ -474,9 +481,9 @@ class _CommutatorNamespace:
         if rx == (0, 0, 0) and ry == (0, 0, 0):
             return self.CommutatorScalarScalar(X, Y, precision)
         if rx == (0, 0, 0):
-            return self.CommutatorScalarTensor(X, Y)
+            return self.CommutatorScalarTensor(X, Y, precision)
         if ry == (0, 0, 0):
-            Z = self.CommutatorScalarTensor(Y, X)  # [T, S] = -[S, T]
+            Z = self.CommutatorScalarTensor(Y, X, precision)  # [T, S] = -[S, T]
             Z.arena *= -1
             return Z
         raise NotImplementedError("tensor-tensor commutators are not implemented in the reference either")

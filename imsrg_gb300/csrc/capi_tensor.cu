@@ -1,12 +1,16 @@
 // extern "C" boundary, scalar-tensor commutator (include/imsrg_gb300.h):
 // Commutator::CommutatorScalarTensor (src/Commutator.cc:432-500) and its
 // IMSRG(2) terms on device operators.  X is a scalar operator, Y and Z are
-// reduced tensors of the same rank (imsrg_op_create_tensor).
+// reduced tensors of the same rank (imsrg_op_create_tensor).  The ladder and
+// Z bar products run in FP64 on the CUDA cores, or in the split form on the
+// tensor cores (plain rectangular split products, kernels_split.cu).
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <exception>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/imsrg_gb300.h"
 #include "capi_internal.hpp"
@@ -60,6 +64,163 @@ int scratch(imsrg_space* sp, TensorLayout* tl)
       (rc = alloc(tl, tl->d_zbar, tl->zb_total)) || (rc = alloc(tl, tl->d_xw, sp->s->arena)) ||
       (rc = alloc(tl, tl->d_wx, sp->s->arena)))
     return rc;
+  return IMSRG_OK;
+}
+
+// ---------------------------------------------------------- split form
+// plain split products of the ladder: term 1, D = Xb w Yc (A = X of the bra
+// channel gathered by its ladder list, B = Y's block transposed), overwrite;
+// term 2, D -= Yc w Xk (A = Y's block gathered by the ket channel's list,
+// B = Xk, taken as hX Xk^T: the launch scale is hX), accumulate
+std::vector<GemmJobDev> ladder_jobs(const Space& s, const TensorLayout& t, int term)
+{
+  std::vector<GemmJobDev> v;
+  for (size_t b = 0; b < t.bra.size(); ++b) {
+    const int chb = t.bra[b], chk = t.ket[b];
+    const int nb = s.ch[chb].n(), nk = s.ch[chk].n();
+    const int ch = term == 1 ? chb : chk;
+    if (!nb || !nk || !t.lad_n[ch]) continue;
+    GemmJobDev j{};
+    j.nosym = 1;
+    j.m = nb;
+    j.n = nk;
+    j.K = t.lad_n[ch];
+    j.kidx_off = t.lad_koff[ch];
+    j.w_off = t.lad_woff[ch];
+    j.phase_off = -1;
+    j.out_off = t.off[b];
+    j.ldo = nb;
+    j.lda = nb;
+    j.ldb = nk;
+    if (term == 1) {
+      j.a_off = s.ch[chb].off;
+      j.b_off = t.off[b];
+      j.bscale = 1.0;
+      j.accumulate = 0;
+    } else {
+      j.a_off = t.off[b];
+      j.b_off = s.ch[chk].off;
+      j.bscale = -1.0;
+      j.accumulate = 1;
+    }
+    v.push_back(j);
+  }
+  return v;
+}
+
+// plain split products of Z bar (lo, hi) = M_left M_right, columns [0, n_hi)
+// (head) and [n_hi, 2 n_hi) (tail), src/TensorCommutators.cc:1130-1190:
+// part 1, K over the 2 nph_lo rows of X bar (lo): A = X bar (lo), B = the
+// transposed panel Ybar(lo, hi) (head) or its half-swapped copy (tail, which
+// carries hY and the ket phases; the job adds (-1)^(Jlo - Jhi)), overwrite;
+// part 2, K over the 2 nph_hi rows of X bar (hi): A = the transposed panel
+// Ybar(hi, lo), B = X bar (hi) (head) or its half-swapped copy (tail), scale
+// -(-1)^(Jlo - Jhi) hY hX (the launch scale carries hY hX), accumulate
+std::vector<GemmJobDev> zbar_jobs(const Space& s, const TensorLayout& t, int part)
+{
+  std::vector<GemmJobDev> v;
+  for (size_t p = 0; p < t.zb_bra.size(); ++p) {
+    const int lo = t.zb_bra[p], hi = t.zb_ket[p];
+    const int nlo = s.cc[lo].n(), nhi = s.cc[hi].n();
+    const int nph = part == 1 ? s.cc_nph[lo] : s.cc_nph[hi];
+    if (!nlo || !nhi || !nph) continue;
+    const long long y = part == 1 ? t.yb_lookup[(size_t)lo * s.nch + hi] : t.yb_lookup[(size_t)hi * s.nch + lo];
+    if (y < 0) continue;
+    const double f0 = ((lo / 6 - hi / 6) & 1) ? -1.0 : 1.0;
+    for (int tail = 0; tail < 2; ++tail) {
+      GemmJobDev j{};
+      j.nosym = 1;
+      j.m = nlo;
+      j.n = nhi;
+      j.K = 2 * nph;
+      j.kidx_off = -1;
+      j.w_off = -1;
+      j.phase_off = -1;
+      j.bsel = tail;
+      j.out_off = t.zb_off[p] + (long long)tail * nhi * nlo;
+      j.ldo = nlo;
+      j.lda = nlo;
+      j.ldb = nhi;
+      if (part == 1) {
+        j.a_off = s.xb_off[lo];
+        j.b_off = y;
+        j.bscale = tail ? f0 : 1.0;
+        j.accumulate = 0;
+      } else {
+        j.a_off = y;
+        j.b_off = s.xb_off[hi];
+        j.bscale = -f0;
+        j.accumulate = 1;
+      }
+      v.push_back(j);
+    }
+  }
+  return v;
+}
+
+int split_ready(imsrg_space* sp, TensorLayout* tl)
+{
+  int rc = scratch(sp, tl);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> g(sp->mu);
+  const Space& s = *sp->s;
+  if ((rc = alloc(tl, tl->d_yt, tl->total)) || (rc = alloc(tl, tl->d_ybt, tl->yb_total)) ||
+      (rc = alloc(tl, tl->d_ybtf, tl->yb_total)) || (rc = alloc(tl, tl->d_xbf, s.xb_total)))
+    return rc;
+  try {
+    if (!tl->sp_lad1) tl->sp_lad1 = split_plan_create(s, ladder_jobs(s, *tl, 1), 0);
+    if (!tl->sp_lad2) tl->sp_lad2 = split_plan_create(s, ladder_jobs(s, *tl, 2), 0);
+    if (!tl->sp_zb1) tl->sp_zb1 = split_plan_create(s, zbar_jobs(s, *tl, 1), 1);
+    if (!tl->sp_zb2) tl->sp_zb2 = split_plan_create(s, zbar_jobs(s, *tl, 2), 1);
+  } catch (std::exception& e) {
+    return terr(IMSRG_ERR_NOMEM, std::string("split-precision plan: ") + e.what());
+  }
+  return IMSRG_OK;
+}
+
+// X bar and the split products' operands (Y transposed, Pandya panels)
+int split_operands(const imsrg_op* X, const imsrg_op* Y, cudaStream_t st)
+{
+  TensorLayout* tl = Y->tl;
+  const Space& s = *X->sp->s;
+  T_CUDA(launch_pandya_single(s, X->d, X->herm, 1, tl->d_xbar, st));
+  T_CUDA(launch_tensor_split_operands(s, *tl, Y->d, Y->herm, tl->d_xbar, tl->d_yt, tl->d_ybt, tl->d_ybtf, tl->d_xbf,
+                                      st));
+  return IMSRG_OK;
+}
+
+int t222_split(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
+{
+  TensorLayout* tl = Y->tl;
+  const Space& s = *X->sp->s;
+  ProfScope ps("comm222_pp_hh_221st", st);
+  T_CUDA(cudaMemsetAsync(tl->d_mpp, 0, std::max<long long>(1, tl->total) * sizeof(double), st));
+  T_CUDA(launch_symgemm_split(tl->sp_lad1, X->d, tl->d_yt, tl->d_yt, tl->d_mpp, s.work.kidx, s.work.kweight,
+                              s.work.phase_tab, X->sp->d_status, 1, 1.0, st));
+  T_CUDA(launch_symgemm_split(tl->sp_lad2, Y->d, X->d, X->d, tl->d_mpp, s.work.kidx, s.work.kweight,
+                              s.work.phase_tab, X->sp->d_status, 1, (double)X->herm, st));
+  T_CUDA(launch_tensor_222_221_split(s, *tl, X->d, Y->d, tl->d_mpp, tl->d_mhh, Z->d, Z->herm, st));
+  return IMSRG_OK;
+}
+
+int tph_split(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
+{
+  TensorLayout* tl = Y->tl;
+  const Space& s = *X->sp->s;
+  ProfScope ps("comm222_phst", st);
+  T_CUDA(cudaMemsetAsync(tl->d_zbar, 0, std::max<long long>(1, tl->zb_total) * sizeof(double), st));
+  T_CUDA(launch_symgemm_split(tl->sp_zb1, tl->d_xbar, tl->d_ybt, tl->d_ybtf, tl->d_zbar, s.work.kidx,
+                              s.work.kweight, s.work.phase_tab, X->sp->d_status, 1, 1.0, st));
+  T_CUDA(launch_symgemm_split(tl->sp_zb2, tl->d_ybt, tl->d_xbar, tl->d_xbf, tl->d_zbar, s.work.kidx,
+                              s.work.kweight, s.work.phase_tab, X->sp->d_status, 1, (double)(X->herm * Y->herm),
+                              st));
+  T_CUDA(launch_tensor_inverse_pandya(s, *tl, tl->d_zbar, Z->d, Z->herm, st));
+  return IMSRG_OK;
+}
+
+int check_prec(int precision)
+{
+  if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_SPLIT) return terr(IMSRG_ERR_ARG, "bad precision");
   return IMSRG_OK;
 }
 
@@ -133,31 +294,47 @@ int imsrg_comm122st(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* str
   return rc ? rc : t122(X, Y, Z, (cudaStream_t)stream);
 }
 
-int imsrg_comm222_pp_hh_221st(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream)
+int imsrg_comm222_pp_hh_221st(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream)
 {
   int rc = check_st(X, Y, Z);
-  return rc ? rc : t222(X, Y, Z, (cudaStream_t)stream);
+  if (rc || (rc = check_prec(precision))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (precision == IMSRG_PREC_FP64) return t222(X, Y, Z, st);
+  if ((rc = split_ready(X->sp, Y->tl)) || (rc = split_operands(X, Y, st)) || (rc = t222_split(X, Y, Z, st)))
+    return rc;
+  return status_dev(X->sp, st);
 }
 
-int imsrg_comm222_phst(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream)
+int imsrg_comm222_phst(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream)
 {
   int rc = check_st(X, Y, Z);
-  return rc ? rc : tph(X, Y, Z, (cudaStream_t)stream);
+  if (rc || (rc = check_prec(precision))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (precision == IMSRG_PREC_FP64) return tph(X, Y, Z, st);
+  if ((rc = split_ready(X->sp, Y->tl)) || (rc = split_operands(X, Y, st)) || (rc = tph_split(X, Y, Z, st)))
+    return rc;
+  return status_dev(X->sp, st);
 }
 
-int imsrg_commutator_scalar_tensor(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream)
+int imsrg_commutator_scalar_tensor(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream)
 {
   if (!X || !Y || !Z) return terr(IMSRG_ERR_ARG, "null operator");
   if (Z == X || Z == Y) return terr(IMSRG_ERR_ARG, "Z must not alias X or Y");
-  Z->herm = z_herm_st(X->herm, Y->herm);
-  int rc = check_st(X, Y, Z);
+  int rc = check_prec(precision);
   if (rc) return rc;
+  Z->herm = z_herm_st(X->herm, Y->herm);
+  if ((rc = check_st(X, Y, Z))) return rc;
   cudaStream_t st = (cudaStream_t)stream;
+  if (precision == IMSRG_PREC_SPLIT && (rc = split_ready(X->sp, Y->tl))) return rc;
   ProfScope ps("CommutatorScalarTensor", st);
   T_CUDA(cudaMemsetAsync(Z->d, 0, Z->len * sizeof(double), st));
-  if ((rc = t111(X, Y, Z, st)) || (rc = t121(X, Y, Z, st)) || (rc = t122(X, Y, Z, st)) || (rc = t222(X, Y, Z, st)) ||
-      (rc = tph(X, Y, Z, st)))
-    return rc;
+  if ((rc = t111(X, Y, Z, st)) || (rc = t121(X, Y, Z, st)) || (rc = t122(X, Y, Z, st))) return rc;
+  if (precision == IMSRG_PREC_FP64) {
+    if ((rc = t222(X, Y, Z, st)) || (rc = tph(X, Y, Z, st))) return rc;
+  } else {
+    if ((rc = split_operands(X, Y, st)) || (rc = t222_split(X, Y, Z, st)) || (rc = tph_split(X, Y, Z, st))) return rc;
+    return status_dev(X->sp, st);
+  }
   return IMSRG_OK;
 }
 

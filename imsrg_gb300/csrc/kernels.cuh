@@ -16,6 +16,10 @@ struct GemmJobDev {
   int sign;        // +-1, or 0: the launch's sign
   int accumulate;  // 1: Out += ..., 0: Out = ...
   double bscale;   // times the launch's scale
+  // plain product (split form only): Out (+)= A B^T with A m x K and B n x K,
+  // no symmetrisation, no phases, every tile; 0: the symmetrised m x m form
+  int nosym;
+  int n;
 };
 
 // kernels_terms.cu
@@ -96,6 +100,17 @@ cudaError_t launch_tensor_222_221(const Space& s, const TensorLayout& t, const d
 // Ybar, Zbar: scratch of t's yb_total and zb_total doubles
 cudaError_t launch_tensor_ph(const Space& s, const TensorLayout& t, const double* Xbar, const double* Y, int hX,
                              int hY, double* Ybar, double* Zbar, double* Z, int hZ, cudaStream_t st);
+// split form: the operands the split products read (Y with its blocks
+// transposed, the tensor Pandya panels transposed and half-swapped, X bar
+// half-swapped); the ladder's remainder (Mhh, Z2 += D, the one-body part) once
+// D = Mpp - Mhh is in place; the inverse tensor Pandya transform of Zbar
+cudaError_t launch_tensor_split_operands(const Space& s, const TensorLayout& t, const double* Y, int hY,
+                                         const double* Xbar, double* YT, double* YbT, double* YbTF, double* XbF,
+                                         cudaStream_t st);
+cudaError_t launch_tensor_222_221_split(const Space& s, const TensorLayout& t, const double* X, const double* Y,
+                                        double* D, double* Mhh, double* Z, int hZ, cudaStream_t st);
+cudaError_t launch_tensor_inverse_pandya(const Space& s, const TensorLayout& t, const double* Zbar, double* Z, int hZ,
+                                         cudaStream_t st);
 
 // kernels_gemm.cu
 int symgemm_fp64_tile();

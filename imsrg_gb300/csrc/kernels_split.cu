@@ -24,6 +24,9 @@
 //  * Recombination.  The epilogue reads the S group sums (tcgen05.ld), merges
 //    them exactly as int64, converts once to FP64 and applies the power-of-two
 //    scale by exponent arithmetic.
+//  * Plain jobs (nosym): Out (+)= A B^T with A m x K, B n x K, each row of A
+//    and of B with its own exponent, K not doubled, every tile of the m x n
+//    output (the rectangular products of the scalar-tensor commutator).
 //
 // Kernel layout (persistent, one CTA per SM, 320 threads):
 //   warp 0: TMA producer (cp.async.bulk.tensor, 64B swizzle, mbarrier pipeline)
@@ -65,6 +68,8 @@ struct SplitJob {
   long long row_base;  // first row of this job in the slice arrays (slice s at row_base + s * m_pad)
   long long exp_base;  // first row of this job in the exponent arrays
   int m_pad, K_pad, nkb;
+  int nosym, n;        // plain product: B rows (n = m for the symmetrised form)
+  int nkt;             // K blocks per tile: nkb (plain) or 2 nkb (K doubled)
 };
 
 struct SplitTile {
@@ -96,6 +101,7 @@ struct SplitPlan {
   int nstages = 0;
   int accum_override = -1;
   int tn = 64, nacc = 1, epiw = 4;  // tile columns, accumulator sets, epilogue warps
+  bool shared_gd = false;           // gamma / delta alias beta / alpha (plain jobs only)
 };
 
 // ----------------------------------------------------------------- device
@@ -283,13 +289,14 @@ __global__ void __launch_bounds__(256) k_split_rowexp(const SplitJob* __restrict
   }
   __syncthreads();
   int ea = 0, eb = 0;
-  if (i < jb.m) {
+  const bool arow = i < jb.m, brow = i < jb.n;
+  if (arow || brow) {
     const double* A = Abase + jb.a_off;
     const double* B = (jb.bsel ? B1 : B0) + jb.b_off;
     for (int t = t0 + ty; t < tend; t += 8) {
       const int col = s_col[t - t0];
-      ea = max(ea, dexp(A[(long long)col * jb.lda + i]));
-      eb = max(eb, dexp_scaled(B[(long long)col * jb.ldb + i], s_code[t - t0], s_sc[t - t0]));
+      if (arow) ea = max(ea, dexp(A[(long long)col * jb.lda + i]));
+      if (brow) eb = max(eb, dexp_scaled(B[(long long)col * jb.ldb + i], s_code[t - t0], s_sc[t - t0]));
     }
   }
   sa[ty][r] = ea;
@@ -346,6 +353,9 @@ __device__ __forceinline__ int row_exp(int eA, int eB, int c)
   return max(a, b);
 }
 
+// exponent of a row of a plain job's A or B from its raw exponent
+__device__ __forceinline__ int own_exp(int e) { return e > 0 ? e - 1022 : EXP_NONE; }
+
 __device__ __forceinline__ int job_c(const int* jobmax, int job)
 {
   int ma = jobmax[2 * job], mb = jobmax[2 * job + 1];
@@ -384,14 +394,19 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
   const SplitJob jb = jobs[job];
   const int r0 = bk.y * 32;
   const int t0 = bk.z * KB;
-  const int c = job_c(jobmax, job);
+  const int c = jb.nosym ? 0 : job_c(jobmax, job);
   const int sign = jb.sign != 0 ? jb.sign : gsign;
   const int* ph = jb.phase_off >= 0 ? phase + jb.phase_off : nullptr;
   if (threadIdx.x < 32) {
     const int i = r0 + threadIdx.x;
-    const int a = row_exp(rexpA[jb.exp_base + i], rexpB[jb.exp_base + i], c);
-    rowA[threadIdx.x] = a;
-    rowB[threadIdx.x] = a + c;
+    if (jb.nosym) {
+      rowA[threadIdx.x] = own_exp(rexpA[jb.exp_base + i]);
+      rowB[threadIdx.x] = own_exp(rexpB[jb.exp_base + i]);
+    } else {
+      const int a = row_exp(rexpA[jb.exp_base + i], rexpB[jb.exp_base + i], c);
+      rowA[threadIdx.x] = a;
+      rowB[threadIdx.x] = a + c;
+    }
     const int p = (ph && i < jb.m) ? ph[i] : 1;
     rowph[threadIdx.x] = p;
     rowsg[threadIdx.x] = sign * p;
@@ -419,15 +434,17 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
     for (int h = 0; h < 2; ++h) {
       const int tt = 2 * tp + h, t = t0 + tt;
       long long qa = 0, qb = 0;
-      if (i < jb.m && t < jb.K) {
+      if (t < jb.K) {
         const int col = s_col[tt], code = s_code[tt];
-        qa = to_fixed(A[(long long)col * jb.lda + i], rowA[r], P);
-        const double vb = B[(long long)col * jb.ldb + i];
-        if (code == SC_GENERAL) {
-          qb = to_fixed(vb * s_sc[tt], rowB[r], P);
-        } else {
-          qb = to_fixed(vb, rowB[r] - (code >> 1), P);
-          if (code & 1) qb = -qb;
+        if (i < jb.m) qa = to_fixed(A[(long long)col * jb.lda + i], rowA[r], P);
+        if (i < jb.n) {
+          const double vb = B[(long long)col * jb.ldb + i];
+          if (code == SC_GENERAL) {
+            qb = to_fixed(vb * s_sc[tt], rowB[r], P);
+          } else {
+            qb = to_fixed(vb, rowB[r] - (code >> 1), P);
+            if (code & 1) qb = -qb;
+          }
         }
       }
       // digits of |q| by shifts (32-bit digit arithmetic), then the carry that
@@ -593,7 +610,7 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
         const bool useG = g.flags[2 * tl.job] != 0, useD = g.flags[2 * tl.job + 1] != 0;
         const CUtensorMap* mA2 = useG ? &mGamma : &mBeta;
         const CUtensorMap* mB2 = useD ? &mDelta : &mAlpha;
-        for (int kb = 0; kb < 2 * jb.nkb; ++kb, ++it) {
+        for (int kb = 0; kb < jb.nkt; ++kb, ++it) {
           int st = it % NST;
           unsigned ph = (unsigned)((it / NST) & 1);
           if (!mbar_wait(empty_bar(st), ph ^ 1u)) {
@@ -636,7 +653,7 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
         tc_fence_after();
         const unsigned dbase = tmem + (unsigned)(b * S * TN);
         bool ok = true;
-        for (int kb = 0; kb < 2 * jb.nkb; ++kb, ++it) {
+        for (int kb = 0; kb < jb.nkt; ++kb, ++it) {
           int st = it % NST;
           unsigned ph = (unsigned)((it / NST) & 1);
           if (!mbar_wait(full_bar(st), ph)) {
@@ -694,13 +711,16 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
         set_status(g.status, 104);
         s_epi_err = 1;
       }
-      const int c = job_c(g.jobmax, tl.job);
+      const int c = jb.nosym ? 0 : job_c(g.jobmax, tl.job);
       const int* ph = jb.phase_off >= 0 ? g.phase + jb.phase_off : nullptr;
-      // column exponents and phases of this tile
+      // column exponents and phases of this tile (a plain job's columns are
+      // B rows with their own exponents)
       if (et < TN) {
         const int j = tl.J * TN + et;
-        const bool ok = j < jb.m;
-        s_colexp[tc & 1][et] = ok ? row_exp(g.rexpA[jb.exp_base + j], g.rexpB[jb.exp_base + j], c) : EXP_NONE;
+        const bool ok = j < jb.n;
+        s_colexp[tc & 1][et] = !ok ? EXP_NONE
+                               : jb.nosym ? own_exp(g.rexpB[jb.exp_base + j])
+                                          : row_exp(g.rexpA[jb.exp_base + j], g.rexpB[jb.exp_base + j], c);
         s_colph[tc & 1][et] = (ph && ok) ? ph[j] : 1;
       }
       asm volatile("bar.sync 1, %0;" ::"r"(EPI_T) : "memory");
@@ -712,7 +732,9 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
       const int sign = jb.sign != 0 ? jb.sign : g.gsign;
       const int i = tl.I * TILE_M + q * 32 + lane;
       const bool rowok = i < jb.m;
-      const int ai = rowok ? row_exp(g.rexpA[jb.exp_base + i], g.rexpB[jb.exp_base + i], c) : EXP_NONE;
+      const int ai = !rowok   ? EXP_NONE
+                     : jb.nosym ? own_exp(g.rexpA[jb.exp_base + i])
+                                : row_exp(g.rexpA[jb.exp_base + i], g.rexpB[jb.exp_base + i], c);
       const int phi_i = (ph && rowok) ? ph[i] : 1;
       double* O = g.out + jb.out_off;
       const int Xi = ai + c - g.beta * (S + 1);
@@ -730,8 +752,8 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
 #pragma unroll
         for (int cc = 0; cc < EPI_COLS; ++cc) {
           const int j = tl.J * TN + c0 + cc;
-          wd[cc] = rowok && j < jb.m && !(tl.diag && i > j);
-          wm[cc] = wd[cc] && i != j;
+          wd[cc] = rowok && j < jb.n && !(tl.diag && i > j);
+          wm[cc] = wd[cc] && i != j && !jb.nosym;
           // exact merge of the weight groups: Horner in base 2^beta
           long long I64 = __float2int_rn(__uint_as_float(r[0][cc]));
 #pragma unroll
@@ -872,9 +894,14 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
     sj.sign = j.sign;
     sj.accumulate = j.accumulate;
     sj.bscale = j.bscale;
-    sj.m_pad = (j.m + TILE_M - 1) / TILE_M * TILE_M;
+    sj.nosym = j.nosym ? 1 : 0;
+    sj.n = j.nosym ? j.n : j.m;
+    sj.m_pad = (std::max(sj.m, sj.n) + TILE_M - 1) / TILE_M * TILE_M;
     sj.K_pad = std::max(KB, (j.K + KB - 1) / KB * KB);
     sj.nkb = sj.K_pad / KB;
+    sj.nkt = sj.nosym ? sj.nkb : 2 * sj.nkb;
+    if (sj.nosym && (sj.sign != 0 || sj.phase_off >= 0))
+      throw std::invalid_argument("a plain split job takes no sign or phases (fold a sign into bscale)");
     sj.row_base = row;
     sj.exp_base = erow;
     row += (long long)p->S * sj.m_pad;
@@ -884,11 +911,18 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
   }
   for (int jix : order) {
     const SplitJob& sj = p->jobs[jix];
-    if (sj.m == 0 || sj.K == 0) continue;
+    if (sj.m == 0 || sj.n == 0 || sj.K == 0) continue;
     const int per = TILE_M / p->tn;  // column tiles per 128-row block
-    int nI = sj.m_pad / TILE_M, nJ = (sj.m + p->tn - 1) / p->tn;
-    for (int I = 0; I < nI; ++I)
-      for (int J = per * I; J < nJ; ++J) tiles.push_back({jix, I, J, J < per * (I + 1) ? 1 : 0});
+    const int nJ = (sj.n + p->tn - 1) / p->tn;
+    if (sj.nosym) {
+      const int nI = (sj.m + TILE_M - 1) / TILE_M;
+      for (int I = 0; I < nI; ++I)
+        for (int J = 0; J < nJ; ++J) tiles.push_back({jix, I, J, 0});
+    } else {
+      const int nI = sj.m_pad / TILE_M;
+      for (int I = 0; I < nI; ++I)
+        for (int J = per * I; J < nJ; ++J) tiles.push_back({jix, I, J, J < per * (I + 1) ? 1 : 0});
+    }
   }
   if (row > (1ll << 31) - TILE_M) throw std::runtime_error("split slice arrays exceed 2^31 rows");
   p->K_stride = kstride;
@@ -907,9 +941,17 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
     cudaMemcpy(p->d_jobs, p->jobs.data(), sizeof(SplitJob) * p->njobs, cudaMemcpyHostToDevice);
     cudaMemcpy(p->d_tiles, tiles.data(), sizeof(SplitTile) * p->ntiles, cudaMemcpyHostToDevice);
     size_t abytes = (size_t)std::max(row, (long long)TILE_M) * kstride * 2;
-    for (int a = 0; a < 4; ++a) {
+    // gamma / delta (the second half of a doubled K) only for symmetrised jobs
+    bool any_sym = false;
+    for (const SplitJob& sj : p->jobs) any_sym = any_sym || !sj.nosym;
+    for (int a = 0; a < (any_sym ? 4 : 2); ++a) {
       p->arr[a] = (__nv_bfloat16*)dm(abytes);
       cudaMemset(p->arr[a], 0, abytes);
+    }
+    if (!any_sym) {
+      p->arr[2] = p->arr[1];
+      p->arr[3] = p->arr[0];
+      p->shared_gd = true;
     }
     p->d_rexpA = (int*)dm(sizeof(int) * std::max(1ll, erow));
     p->d_rexpB = (int*)dm(sizeof(int) * std::max(1ll, erow));
@@ -920,8 +962,9 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
       for (int j = 0; j < p->njobs; ++j) {
         const SplitJob& sj = p->jobs[j];
         int sign = sj.sign != 0 ? sj.sign : (gs == 0 ? 1 : -1);
-        flags[2 * p->njobs * gs + 2 * j] = (sign != 1 || sj.phase_off >= 0) ? 1 : 0;
-        flags[2 * p->njobs * gs + 2 * j + 1] = sj.phase_off >= 0 ? 1 : 0;
+        // plain jobs have no second K half: gamma / delta stay unwritten
+        flags[2 * p->njobs * gs + 2 * j] = !sj.nosym && (sign != 1 || sj.phase_off >= 0) ? 1 : 0;
+        flags[2 * p->njobs * gs + 2 * j + 1] = !sj.nosym && sj.phase_off >= 0 ? 1 : 0;
       }
     cudaMemcpy(p->d_flags, flags.data(), sizeof(int) * flags.size(), cudaMemcpyHostToDevice);
     // slicing blocks: only the (row group, column chunk) blocks each job has;
@@ -972,7 +1015,7 @@ void split_plan_destroy(SplitPlan* p)
   if (!p) return;
   cudaFree(p->d_jobs);
   cudaFree(p->d_tiles);
-  for (int a = 0; a < 4; ++a) cudaFree(p->arr[a]);
+  for (int a = 0; a < (p->shared_gd ? 2 : 4); ++a) cudaFree(p->arr[a]);
   cudaFree(p->d_rexpA);
   cudaFree(p->d_rexpB);
   cudaFree(p->d_jobmax);

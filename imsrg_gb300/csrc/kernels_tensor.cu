@@ -370,6 +370,9 @@ __global__ void k_t222_weights(DevSpace S, DevWork W, DevTensor T, const double*
 
 // D and Mhh for the element pair (r, c0), (r, c1 = c0 + 1) of every stored
 // block (blockIdx.y); Z2 += D
+// (SPLIT: D is already there, from the split-form products; only Mhh and
+// Z2 += D remain)
+template <bool SPLIT>
 __global__ void k_t222(DevSpace S, DevWork W, DevTensor T, const double* __restrict__ X,
                        const double* __restrict__ Y, const double* __restrict__ XW, const double* __restrict__ WX,
                        double* __restrict__ D, double* __restrict__ Mhh, double* __restrict__ Z)
@@ -385,7 +388,7 @@ __global__ void k_t222(DevSpace S, DevWork W, DevTensor T, const double* __restr
   const double* Y0 = Yc + (long long)c0 * nb;
   const double* Y1 = Yc + (long long)c1 * nb;
   double d0 = 0.0, d1 = 0.0, h0 = 0.0, h1 = 0.0;
-  {
+  if (!SPLIT) {
     const int Kb = T.lad_n[chb];
     const int* kx = W.kidx + T.lad_koff[chb];
     const double* xw = XW + S.ch_off[chb] + r;
@@ -396,7 +399,7 @@ __global__ void k_t222(DevSpace S, DevWork W, DevTensor T, const double* __restr
       d1 = fma(a, Y1[K], d1);
     }
   }
-  {
+  if (!SPLIT) {
     const int Kk = T.lad_n[chk];
     const int* kx = W.kidx + T.lad_koff[chk];
     const double* wx = WX + S.ch_off[chk];
@@ -432,15 +435,61 @@ __global__ void k_t222(DevSpace S, DevWork W, DevTensor T, const double* __restr
     }
   }
   const long long o0 = T.off[blk] + (long long)c0 * nb + r;
-  D[o0] = d0;
+  if (SPLIT) {
+    d0 = D[o0];
+    if (c1 != c0) d1 = D[o0 + nb];
+  } else {
+    D[o0] = d0;
+    if (c1 != c0) D[o0 + nb] = d1;
+  }
   Mhh[o0] = h0;
   Z[o0] += d0;
   if (c1 != c0) {
-    const long long o1 = o0 + nb;
-    D[o1] = d1;
-    Mhh[o1] = h1;
-    Z[o1] += d1;
+    Mhh[o0 + nb] = h1;
+    Z[o0 + nb] += d1;
   }
+}
+
+// ------------------------------------------------------- split-form operands
+// Y with every stored block transposed: YT[off + r n_ket + c] = Y[off + c n_bra + r]
+// (32 x 32 tiles through shared memory; blockIdx.y = block)
+__global__ void k_ttranspose(DevSpace S, DevTensor T, const double* __restrict__ Y, double* __restrict__ YT)
+{
+  __shared__ double tile[32][33];
+  const int blk = blockIdx.y;
+  const int nb = S.ch_n[T.bra[blk]], nk = S.ch_n[T.ket[blk]];
+  const int tr = (nb + 31) >> 5, tcn = (nk + 31) >> 5;
+  if ((int)blockIdx.x >= tr * tcn) return;
+  const int r0 = (blockIdx.x % tr) * 32, c0 = (blockIdx.x / tr) * 32;
+  const double* src = Y + T.off[blk];
+  double* dst = YT + T.off[blk];
+  for (int y = threadIdx.y; y < 32; y += 8) {
+    const int r = r0 + threadIdx.x, c = c0 + y;
+    if (r < nb && c < nk) tile[y][threadIdx.x] = src[(long long)c * nb + r];
+  }
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += 8) {
+    const int c = c0 + threadIdx.x, r = r0 + y;
+    if (r < nb && c < nk) dst[(long long)r * nk + c] = tile[threadIdx.x][y];
+  }
+}
+
+// X bar's half-swapped copy for the Z bar tails: per CC channel (blockIdx.y),
+// XbF[K n + c] = (-1)^(ket c) (-1)^(ph ket Kh) Xb[swap(K) n + c], with swap
+// exchanging the two halves of the 2 nph rows (src/TensorCommutators.cc:
+// 1160-1185)
+__global__ void k_xbar_flip(DevSpace S, DevWork W, const double* __restrict__ Xb, double* __restrict__ XbF)
+{
+  const int cc = blockIdx.y;
+  const int n = S.cc_n[cc], nph = W.cc_nph[cc];
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= 2LL * nph * n) return;
+  const int K = (int)(e / n), c = (int)(e - (long long)K * n);
+  const int Kh = K < nph ? K : K - nph, src = K < nph ? K + nph : K - nph;
+  const int* ph = W.phase_tab + W.cc_phase_off[cc];
+  const int* phl = W.cc_ph + W.cc_ph_off[cc];
+  const long long o = W.xb_off[cc];
+  XbF[o + e] = flip(Xb[o + (long long)src * n + c], (ph[c] < 0) + (ph[phl[Kh]] < 0));
 }
 
 // one-body part, src/TensorCommutators.cc:421-495: a warp per (i, j >= i)
@@ -484,8 +533,11 @@ __global__ void k_t221(DevSpace S, DevTensor T, const double* __restrict__ D, co
 // (bra, ket) = blockIdx.y (DoTensorPandyaTransformation_SingleChannel,
 // src/TensorCommutators.cc:637-752): 2 nph_bra x n_ket, rows the bra's hh
 // then ph kets (a, b) in both orders
+// Split form (YbF != nullptr): the panel is written transposed, Yb[off +
+// row n_ket + ik], and its half-swapped copy for the Z bar tails, YbF[off +
+// swap(row) n_ket + ik] = hY (-1)^(bra ph ket) (-1)^(ket ik) value.
 __global__ void k_tpandya(DevSpace S, DevWork W, DevTensor T, const double* __restrict__ Y, int hY,
-                          double* __restrict__ Yb)
+                          double* __restrict__ Yb, double* __restrict__ YbF)
 {
   const int p = blockIdx.y;
   const int cb = T.yb_bra[p], ck = T.yb_ket[p];
@@ -496,12 +548,18 @@ __global__ void k_tpandya(DevSpace S, DevWork W, DevTensor T, const double* __re
   double* out = Yb + T.yb_off[p];
   const int Jbra = ch_J(cb), Jket = ch_J(ck);
   const int Lam = T.lam;
-  if (Jbra + Jket < Lam || abs(Jbra - Jket) > Lam || ((ch_par(cb) + ch_par(ck) + T.parity) & 1)) {
-    out[e] = 0.0;
-    return;
-  }
   const int second = row >= nph;
   const int kb = W.cc_ph[W.cc_ph_off[cb] + row - second * nph];
+  const long long et = (long long)row * nk + ik, ets = (long long)(second ? row - nph : row + nph) * nk + ik;
+  if (Jbra + Jket < Lam || abs(Jbra - Jket) > Lam || ((ch_par(cb) + ch_par(ck) + T.parity) & 1)) {
+    if (YbF) {
+      out[et] = 0.0;
+      YbF[T.yb_off[p] + ets] = 0.0;
+    } else {
+      out[e] = 0.0;
+    }
+    return;
+  }
   const int p0 = S.cc_p[S.cc_kofs[cb] + kb], q0 = S.cc_q[S.cc_kofs[cb] + kb];
   const int a = second ? q0 : p0, b = second ? p0 : q0;
   const int c = S.cc_p[S.cc_kofs[ck] + ik], d = S.cc_q[S.cc_kofs[ck] + ik];
@@ -519,7 +577,14 @@ __global__ void k_tpandya(DevSpace S, DevWork W, DevTensor T, const double* __re
       sm = fma(flip(nh, 1 + ((jb + jd) >> 1) + Jket + J2), tbme, sm);
     }
   }
-  out[e] = sm;
+  if (YbF) {
+    out[et] = sm;
+    const int* ph_b = W.phase_tab + W.cc_phase_off[cb];
+    const int* ph_k = W.phase_tab + W.cc_phase_off[ck];
+    YbF[T.yb_off[p] + ets] = flip(sm, (hY < 0) + (ph_b[kb] < 0) + (ph_k[ik] < 0));
+  } else {
+    out[e] = sm;
+  }
 }
 
 // Zbar(lo, hi) = Mleft Mright for the pair blockIdx.y (src/TensorCommutators.cc:
@@ -698,7 +763,7 @@ cudaError_t launch_tensor_222_221(const Space& s, const TensorLayout& t, const d
     }
     // element pairs: a block's columns come two at a time
     dim3 grid(grid_for(t.max_pair_elems), (unsigned)t.bra.size());
-    k_t222<<<grid, 256, 0, st>>>(s.dev, s.work, t.dev, X, Y, XW, WX, D, Mhh, Z);
+    k_t222<false><<<grid, 256, 0, st>>>(s.dev, s.work, t.dev, X, Y, XW, WX, D, Mhh, Z);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
@@ -713,7 +778,7 @@ cudaError_t launch_tensor_ph(const Space& s, const TensorLayout& t, const double
 {
   if (t.yb_bra.empty()) return cudaSuccess;
   dim3 gy(grid_for(std::max(1, t.yb_maxelems)), (unsigned)t.yb_bra.size());
-  k_tpandya<<<gy, 256, 0, st>>>(s.dev, s.work, t.dev, Y, hY, Ybar);
+  k_tpandya<<<gy, 256, 0, st>>>(s.dev, s.work, t.dev, Y, hY, Ybar, nullptr);
   count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -721,6 +786,59 @@ cudaError_t launch_tensor_ph(const Space& s, const TensorLayout& t, const double
   k_tzbar<<<gz, 256, 0, st>>>(s.dev, s.work, t.dev, Xbar, Ybar, hX, hY, Zbar, s.work.phase_tab);
   count_launch();
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (t.bra.empty() || t.max_blk_elems == 0) return cudaSuccess;
+  dim3 gi(grid_for(t.max_blk_elems), (unsigned)t.bra.size());
+  k_tinv<<<gi, 256, 0, st>>>(s.dev, t.dev, Zbar, hZ, Z);
+  count_launch();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------- split form
+cudaError_t launch_tensor_split_operands(const Space& s, const TensorLayout& t, const double* Y, int hY,
+                                         const double* Xbar, double* YT, double* YbT, double* YbTF, double* XbF,
+                                         cudaStream_t st)
+{
+  cudaError_t e;
+  if (!t.bra.empty() && t.max_tiles32 > 0) {
+    k_ttranspose<<<dim3((unsigned)t.max_tiles32, (unsigned)t.bra.size()), dim3(32, 8), 0, st>>>(s.dev, t.dev, Y,
+                                                                                              YT);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  if (!t.yb_bra.empty()) {
+    dim3 gy(grid_for(std::max(1, t.yb_maxelems)), (unsigned)t.yb_bra.size());
+    k_tpandya<<<gy, 256, 0, st>>>(s.dev, s.work, t.dev, Y, hY, YbT, YbTF);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  if (t.max_xbf > 0) {
+    k_xbar_flip<<<dim3(grid_for(t.max_xbf), (unsigned)s.nch), 256, 0, st>>>(s.dev, s.work, Xbar, XbF);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_tensor_222_221_split(const Space& s, const TensorLayout& t, const double* X, const double* Y,
+                                        double* D, double* Mhh, double* Z, int hZ, cudaStream_t st)
+{
+  cudaError_t e = cudaMemsetAsync(Mhh, 0, t.total * sizeof(double), st);
+  if (e != cudaSuccess) return e;
+  if (!t.bra.empty() && t.max_blk_elems > 0) {
+    dim3 grid(grid_for(t.max_pair_elems), (unsigned)t.bra.size());
+    k_t222<true><<<grid, 256, 0, st>>>(s.dev, s.work, t.dev, X, Y, nullptr, nullptr, D, Mhh, Z);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  int nn = s.norb * s.norb;
+  k_t221<<<(nn + 7) / 8, 256, 0, st>>>(s.dev, t.dev, D, Mhh, hZ, Z);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tensor_inverse_pandya(const Space& s, const TensorLayout& t, const double* Zbar, double* Z, int hZ,
+                                         cudaStream_t st)
+{
   if (t.bra.empty() || t.max_blk_elems == 0) return cudaSuccess;
   dim3 gi(grid_for(t.max_blk_elems), (unsigned)t.bra.size());
   k_tinv<<<gi, 256, 0, st>>>(s.dev, t.dev, Zbar, hZ, Z);

@@ -8,6 +8,7 @@
 #include <cstdlib>
 #include <stdexcept>
 
+#include "kernels.cuh"
 #include "space.hpp"
 
 namespace imsrg {
@@ -72,6 +73,8 @@ T* dev_copy(TensorLayout& t, const std::vector<T>& v)
 
 TensorLayout::~TensorLayout()
 {
+  for (SplitPlan* p : {sp_lad1, sp_lad2, sp_zb1, sp_zb2})
+    if (p) split_plan_destroy(p);
   for (void* p : dev_allocs) cudaFree(p);
 }
 
@@ -104,7 +107,10 @@ TensorLayout* tensor_layout(Space& s, int lam, int trank, int parity)
     const int64_t nb = s.ch[t->bra[b]].n(), nk = s.ch[t->ket[b]].n();
     t->max_blk_elems = std::max<int64_t>(t->max_blk_elems, nb * nk);
     t->max_pair_elems = std::max<int64_t>(t->max_pair_elems, nb * ((nk + 1) / 2));
+    t->max_tiles32 = std::max<int>(t->max_tiles32, (int)(((nb + 31) / 32) * ((nk + 31) / 32)));
   }
+  for (int c = 0; c < s.nch; ++c)
+    t->max_xbf = std::max<long long>(t->max_xbf, 2LL * s.cc_nph[c] * s.cc[c].n());
   // comm222_phst (src/TensorCommutators.cc:1059-1386): Zbar blocks for the
   // cross-coupled channel pairs lo <= hi allowed by the rank, and the ordered
   // pairs of the tensor Pandya transform of Y they read, (lo, hi) and (hi, lo)

@@ -70,6 +70,8 @@ struct DevTensor {
   const int* lad_n = nullptr;
 };
 
+struct SplitPlan;
+
 struct TensorLayout {
   int lam = 0, trank = 0, parity = 0;
   std::vector<int> bra, ket, lookup;
@@ -98,6 +100,15 @@ struct TensorLayout {
   // and the two weighted copies of X the ladder reads (the space's arena each)
   double *d_mpp = nullptr, *d_mhh = nullptr, *d_xbar = nullptr, *d_ybar = nullptr, *d_zbar = nullptr;
   double *d_xw = nullptr, *d_wx = nullptr;
+  // split form (lazily built): Y with every block transposed (layout total),
+  // the tensor Pandya panels transposed and their half-swapped copies (yb_total
+  // each), X bar's half-swapped copy (the space's xb_total), and the product
+  // plans: ladder D = Xb w Yc (overwrite) and D -= Yc w Xk (accumulate), Z bar
+  // first K half (overwrite) and second K half (accumulate)
+  double *d_yt = nullptr, *d_ybt = nullptr, *d_ybtf = nullptr, *d_xbf = nullptr;
+  SplitPlan *sp_lad1 = nullptr, *sp_lad2 = nullptr, *sp_zb1 = nullptr, *sp_zb2 = nullptr;
+  int max_tiles32 = 0;        // largest block in 32 x 32 tiles (transpose grid)
+  long long max_xbf = 0;      // largest X bar panel (2 nph x n_cc)
   DevTensor dev;
   bool dev_ready = false;
   std::vector<void*> dev_allocs;

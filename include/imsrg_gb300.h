@@ -229,8 +229,12 @@ int imsrg_comm222_phss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int pr
 /* ------------------------------------------------------- scalar-tensor */
 /* Commutator::CommutatorScalarTensor (src/Commutator.cc:432-500) in IMSRG(2):
  * Z = [X, Y] for X scalar and Y a reduced tensor; Z, a tensor operator of Y's
- * rank, is overwritten and its hermiticity set from X and Y.  FP64 throughout. */
-int imsrg_commutator_scalar_tensor(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
+ * rank, is overwritten and its hermiticity set from X and Y.  precision
+ * selects the form of the ladder and Pandya-space (Z bar) products, as for the
+ * scalar commutator: IMSRG_PREC_FP64, or IMSRG_PREC_SPLIT (tensor cores; the call
+ * then synchronises the stream and checks the kernels' status word, as the
+ * scalar entry points do); every other sum is FP64. */
+int imsrg_commutator_scalar_tensor(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream);
 /* its terms, each accumulating into Z (src/TensorCommutators.cc) */
 /* comm111st, src/TensorCommutators.cc:25-30 */
 int imsrg_comm111st(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
@@ -239,10 +243,10 @@ int imsrg_comm121st(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* str
 /* comm122st, src/TensorCommutators.cc:158-312 */
 int imsrg_comm122st(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
 /* comm222_pp_hh_221st, src/TensorCommutators.cc:314-495 */
-int imsrg_comm222_pp_hh_221st(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
+int imsrg_comm222_pp_hh_221st(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream);
 /* comm222_phst, src/TensorCommutators.cc:1059-1386, with the tensor Pandya
  * transforms of :637-752 and :754-920 */
-int imsrg_comm222_phst(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
+int imsrg_comm222_phst(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream);
 
 /* Commutator::DoPandyaTransformation(Z, TwoBody_CC_ph, orientation),
  * src/Commutator.cc:1319-1390,1487-1497: the Pandya (particle-hole) transform

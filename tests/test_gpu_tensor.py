@@ -74,3 +74,49 @@ def test_tensor_rejected_by_scalar_paths():
             ig.Commutator.device_commutator(dX, dT, dZ)
         with pytest.raises(ig.IMSRGError):
             dT.norm()
+
+
+# ------------------------------------------------------------- split form
+# The ladder and Z bar products on the tensor cores (plain split products);
+# every other sum stays FP64.  Tolerance 1e-10 relative Frobenius per body
+# rank, as for the scalar commutator's split form.
+SPLIT_TOL = 1e-10
+
+
+@pytest.mark.parametrize("emax,case", CASES)
+def test_commutator_scalar_tensor_split_vs_reference(emax, case):
+    g, ms, dX, dT, rank, herm = setup(emax, case)
+    with ig.DeviceOperator(ms, 1, rank) as dZ:
+        dZ.upload(np.full(dZ.size, 3.0))  # overwritten
+        ig.Commutator.device_scalar_tensor(dX, dT, dZ, precision="split")
+        Z = dZ.download()
+    errs = tensor_rel_errors(ref_space(emax), rank, Z, g[case + "_full"])
+    assert max(errs) < SPLIT_TOL, errs
+
+
+@pytest.mark.parametrize("emax,case", [(2, "e2"), (2, "gt"), (3, "e2")])
+@pytest.mark.parametrize("term", ["comm222_pp_hh_221st", "comm222_phst"])
+def test_tensor_term_split_vs_reference(emax, case, term):
+    g, ms, dX, dT, rank, herm = setup(emax, case)
+    hz = -1 if herm == 1 else 1
+    with ig.DeviceOperator(ms, hz, rank) as dZ:
+        ig.Commutator.device_tensor_term(term, dX, dT, dZ, precision="split")
+        Z = dZ.download()
+    errs = tensor_rel_errors(ref_space(emax), rank, Z, g["%s_%s" % (case, term)])
+    assert max(errs) < SPLIT_TOL, (term, errs)
+
+
+@pytest.mark.parametrize("rank,herm", [((2, 0, 0), 1), ((1, 1, 0), -1), ((3, 0, 1), 1)])
+def test_tensor_split_vs_fp64_emax5(rank, herm):
+    # larger channels than the golden spaces (several 128-row tiles, ragged
+    # edges, K past one pipeline stage): the split form against the FP64 one
+    ms = ig.ModelSpace(5, "O16", "O16")
+    with ig.DeviceOperator(ms, 1) as dX, ig.DeviceOperator(ms, herm, rank) as dT, \
+            ig.DeviceOperator(ms, 1, rank) as dF, ig.DeviceOperator(ms, 1, rank) as dS:
+        dX.fill_random(5)
+        dT.upload(ref_space(5).random_tensor(9, *rank, hermitian=herm == 1))
+        ig.Commutator.device_scalar_tensor(dX, dT, dF, precision="fp64")
+        ig.Commutator.device_scalar_tensor(dX, dT, dS, precision="split")
+        F, S = dF.download(), dS.download()
+    errs = tensor_rel_errors(ref_space(5), rank, S, F)
+    assert max(errs) < SPLIT_TOL, errs
