@@ -52,6 +52,8 @@ SIGNATURES = {
     "imsrg_op_rank": (I, [P, IP, IP, IP, LLP]),
     "imsrg_space_tensor_layout": (I, [P, I, I, I, I, IP, IP, LLP, IP, LLP]),
     "imsrg_space_ninej": (I, [P, I, I, I, I, I, I, I, I, I, DP]),
+    "imsrg_space_wait_selftest": (I, [P, ctypes.c_uint, ctypes.POINTER(ctypes.c_longlong),
+                                      ctypes.POINTER(ctypes.c_uint), P]),
     "imsrg_commutator_scalar_tensor": (I, [P, P, P, I, P]),
     "imsrg_comm111st": (I, [P, P, P, P]),
     "imsrg_comm121st": (I, [P, P, P, P]),

@@ -736,6 +736,26 @@ int imsrg_space_tensor_layout(imsrg_space* sp, int lam, int trank, int parity, i
   return IMSRG_OK;
 }
 
+int imsrg_space_wait_selftest(imsrg_space* sp, unsigned limit, long long* cycles, unsigned* production_limit,
+                              void* stream)
+{
+  if (!sp) return fail(IMSRG_ERR_ARG, "null space");
+  if (production_limit) *production_limit = wait_limit();
+  if (limit == 0 || limit > wait_limit()) return fail(IMSRG_ERR_ARG, "limit must be in [1, the production bound]");
+  cudaStream_t st = (cudaStream_t)stream;
+  long long* d_cyc = nullptr;
+  CUDA_TRY(cudaMalloc((void**)&d_cyc, sizeof(long long)));
+  long long h = 0;
+  cudaError_t e = cudaMemsetAsync(d_cyc, 0, sizeof(long long), st);
+  if (e == cudaSuccess) e = launch_wait_selftest(sp->d_status, limit, d_cyc, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d_cyc, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  int rc = e == cudaSuccess ? check_status(sp, st) : fail(IMSRG_ERR_CUDA, cudaGetErrorString(e));
+  cudaStreamSynchronize(st);
+  cudaFree(d_cyc);
+  if (cycles) *cycles = h;
+  return rc;
+}
+
 int imsrg_space_ninej(imsrg_space* sp, int lam, int ja, int jd, int J1, int jb, int jc, int J2, int Jbra, int Jket,
                       double* out)
 {

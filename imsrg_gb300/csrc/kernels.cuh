@@ -124,6 +124,11 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
 void split_plan_destroy(SplitPlan* p);
 // -1: each job's own accumulate flag; 0: overwrite the output; 1: accumulate
 void split_plan_set_accumulate(SplitPlan* p, int mode);
+// one bounded mbarrier wait of `limit` iterations that runs out (no arrival):
+// status = 105, *cycles = the SM clock cycles it waited (device pointer)
+cudaError_t launch_wait_selftest(int* status, unsigned limit, long long* cycles, cudaStream_t st);
+// the iteration bound of every wait in the split products
+unsigned wait_limit();
 cudaError_t launch_symgemm_split(SplitPlan* p, const double* A, const double* B0, const double* B1, double* O,
                                  const int* kidx, const double* kw, const int* phase, int* dev_status, int gsign,
                                  double gbscale, cudaStream_t st);

@@ -55,7 +55,12 @@ constexpr int KB = 32;          // K elements (bf16) per pipeline stage: one 64-
 constexpr int TILE_M = 128;     // rows per tile (UMMA M)
 constexpr int MAX_S = 7;
 constexpr int EPI_COLS = 8;     // TMEM columns read per tcgen05.ld
-constexpr unsigned WAIT_LIMIT = 1u << 22;  // bounded spin (with nanosleep backoff: about a second)
+// bounded spin: every mbarrier wait gives up after WAIT_LIMIT try_wait rounds.
+// One round (try_wait's own suspend plus the nanosleep backoff) measured
+// about 8000 SM cycles on GB300 (imsrg_space_wait_selftest), so the bound is
+// about 2 s at 2 GHz; the longest wait of a healthy launch (one tile's MMAs)
+// is microseconds
+constexpr unsigned WAIT_LIMIT = 1u << 19;
 constexpr int EXP_NONE = -100000;          // exponent of an all-zero row
 
 struct SplitJob {
@@ -102,6 +107,7 @@ struct SplitPlan {
   int accum_override = -1;
   int tn = 64, nacc = 1, epiw = 4;  // tile columns, accumulator sets, epilogue warps
   bool shared_gd = false;           // gamma / delta alias beta / alpha (plain jobs only)
+  bool plain = false;               // every job is a plain product (a plan holds one kind)
 };
 
 // ----------------------------------------------------------------- device
@@ -136,9 +142,9 @@ __device__ __forceinline__ bool mbar_try(unsigned a, unsigned parity)
 }
 
 // bounded wait: false on timeout
-__device__ __forceinline__ bool mbar_wait(unsigned a, unsigned parity)
+__device__ __forceinline__ bool mbar_wait(unsigned a, unsigned parity, unsigned limit = WAIT_LIMIT)
 {
-  for (unsigned it = 0; it < WAIT_LIMIT; ++it) {
+  for (unsigned it = 0; it < limit; ++it) {
     if (mbar_try(a, parity)) return true;
     if (it > 64) __nanosleep(it > 4096 ? 256 : 32);
   }
@@ -257,6 +263,9 @@ __device__ __forceinline__ int dexp_scaled(double v, int code, double sc)
 // 32 rows x 8 column lanes; partial maxima combine through atomicMax (the
 // arrays are zeroed first).  The exponent of B includes the column scale so
 // the B digits are taken of the scaled values.
+// (PLAIN: a plan of plain jobs, whose A rows (i < m) and B rows (i < n) are
+// counted separately; the symmetrised form keeps its single row test)
+template <bool PLAIN>
 __global__ void __launch_bounds__(256) k_split_rowexp(const SplitJob* __restrict__ jobs, const int4* __restrict__ blocks,
                                                       const double* __restrict__ Abase,
                                                       const double* __restrict__ B0, const double* __restrict__ B1,
@@ -289,15 +298,22 @@ __global__ void __launch_bounds__(256) k_split_rowexp(const SplitJob* __restrict
   }
   __syncthreads();
   int ea = 0, eb = 0;
-  const bool arow = i < jb.m, brow = i < jb.n;
-  if (arow || brow) {
-    const double* A = Abase + jb.a_off;
-    const double* B = (jb.bsel ? B1 : B0) + jb.b_off;
-    for (int t = t0 + ty; t < tend; t += 8) {
-      const int col = s_col[t - t0];
-      if (arow) ea = max(ea, dexp(A[(long long)col * jb.lda + i]));
-      if (brow) eb = max(eb, dexp_scaled(B[(long long)col * jb.ldb + i], s_code[t - t0], s_sc[t - t0]));
+  const double* A = Abase + jb.a_off;
+  const double* B = (jb.bsel ? B1 : B0) + jb.b_off;
+  if (!PLAIN) {
+    if (i < jb.m) {
+      for (int t = t0 + ty; t < tend; t += 8) {
+        const int col = s_col[t - t0];
+        ea = max(ea, dexp(A[(long long)col * jb.lda + i]));
+        eb = max(eb, dexp_scaled(B[(long long)col * jb.ldb + i], s_code[t - t0], s_sc[t - t0]));
+      }
     }
+  } else {
+    if (i < jb.m)
+      for (int t = t0 + ty; t < tend; t += 8) ea = max(ea, dexp(A[(long long)s_col[t - t0] * jb.lda + i]));
+    if (i < jb.n)
+      for (int t = t0 + ty; t < tend; t += 8)
+        eb = max(eb, dexp_scaled(B[(long long)s_col[t - t0] * jb.ldb + i], s_code[t - t0], s_sc[t - t0]));
   }
   sa[ty][r] = ea;
   sb[ty][r] = eb;
@@ -369,7 +385,7 @@ __device__ __forceinline__ int job_c(const int* jobmax, int job)
 // arrays
 //   alpha = A digits, beta = B digits, gamma = s phi_i B digits, delta = phi_i A digits
 // (gamma / delta written only when they differ from beta / alpha).
-template <int S>
+template <int S, bool PLAIN>
 __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict__ jobs, const int4* __restrict__ blocks,
                                                      const double* __restrict__ Abase,
                                                      const double* __restrict__ B0, const double* __restrict__ B1,
@@ -394,12 +410,12 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
   const SplitJob jb = jobs[job];
   const int r0 = bk.y * 32;
   const int t0 = bk.z * KB;
-  const int c = jb.nosym ? 0 : job_c(jobmax, job);
+  const int c = PLAIN ? 0 : job_c(jobmax, job);
   const int sign = jb.sign != 0 ? jb.sign : gsign;
   const int* ph = jb.phase_off >= 0 ? phase + jb.phase_off : nullptr;
   if (threadIdx.x < 32) {
     const int i = r0 + threadIdx.x;
-    if (jb.nosym) {
+    if (PLAIN) {
       rowA[threadIdx.x] = own_exp(rexpA[jb.exp_base + i]);
       rowB[threadIdx.x] = own_exp(rexpB[jb.exp_base + i]);
     } else {
@@ -434,10 +450,10 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
     for (int h = 0; h < 2; ++h) {
       const int tt = 2 * tp + h, t = t0 + tt;
       long long qa = 0, qb = 0;
-      if (t < jb.K) {
+      if (!PLAIN ? (i < jb.m && t < jb.K) : (t < jb.K && (i < jb.m || i < jb.n))) {
         const int col = s_col[tt], code = s_code[tt];
-        if (i < jb.m) qa = to_fixed(A[(long long)col * jb.lda + i], rowA[r], P);
-        if (i < jb.n) {
+        if (!PLAIN || i < jb.m) qa = to_fixed(A[(long long)col * jb.lda + i], rowA[r], P);
+        if (!PLAIN || i < jb.n) {
           const double vb = B[(long long)col * jb.ldb + i];
           if (code == SC_GENERAL) {
             qb = to_fixed(vb * s_sc[tt], rowB[r], P);
@@ -802,7 +818,33 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
   }
 }
 
+// Self-test of the bounded wait: one thread waits on an mbarrier that nothing
+// arrives on, through the same wait loop as the products above but with a
+// bound of `limit` iterations; when it runs out the kernel sets the status
+// word (code 105), stores the clock cycles it waited, and returns, so the
+// context stays usable.
+__global__ void k_wait_selftest(int* status, unsigned limit, long long* cycles)
+{
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x != 0) return;
+  const unsigned a = smem_u32(&bar);
+  mbar_init(a, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  const long long c0 = clock64();
+  if (!mbar_wait(a, 0, limit)) set_status(status, 105);
+  *cycles = clock64() - c0;
+}
+
 }  // namespace
+
+cudaError_t launch_wait_selftest(int* status, unsigned limit, long long* cycles, cudaStream_t st)
+{
+  k_wait_selftest<<<1, 32, 0, st>>>(status, limit, cycles);
+  count_launch();
+  return cudaGetLastError();
+}
+
+unsigned wait_limit() { return WAIT_LIMIT; }
 
 // ------------------------------------------------------------------ host
 typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -942,8 +984,13 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
     cudaMemcpy(p->d_tiles, tiles.data(), sizeof(SplitTile) * p->ntiles, cudaMemcpyHostToDevice);
     size_t abytes = (size_t)std::max(row, (long long)TILE_M) * kstride * 2;
     // gamma / delta (the second half of a doubled K) only for symmetrised jobs
-    bool any_sym = false;
-    for (const SplitJob& sj : p->jobs) any_sym = any_sym || !sj.nosym;
+    bool any_sym = false, any_plain = false;
+    for (const SplitJob& sj : p->jobs) {
+      any_sym = any_sym || !sj.nosym;
+      any_plain = any_plain || sj.nosym;
+    }
+    if (any_sym && any_plain) throw std::invalid_argument("a split plan holds plain or symmetrised jobs, not both");
+    p->plain = any_plain;
     for (int a = 0; a < (any_sym ? 4 : 2); ++a) {
       p->arr[a] = (__nv_bfloat16*)dm(abytes);
       cudaMemset(p->arr[a], 0, abytes);
@@ -1044,13 +1091,15 @@ static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, con
     e = cudaMemsetAsync(p->d_rexpB, 0, sizeof(int) * std::max(1ll, p->total_exp_rows), st);
     if (e != cudaSuccess) return e;
     if (p->n_rblk > 0) {
-      k_split_rowexp<<<p->n_rblk, 256, 0, st>>>(p->d_jobs, p->d_rblk, A, B0, B1, kidx, kw, gbscale, p->d_rexpA,
-                                                p->d_rexpB, p->d_jobmax);
+      auto kr = p->plain ? k_split_rowexp<true> : k_split_rowexp<false>;
+      kr<<<p->n_rblk, 256, 0, st>>>(p->d_jobs, p->d_rblk, A, B0, B1, kidx, kw, gbscale, p->d_rexpA, p->d_rexpB,
+                                    p->d_jobmax);
       count_launch();
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if (p->n_dblk > 0) {
-      k_split_digits<S><<<p->n_dblk, 256, 0, st>>>(p->d_jobs, p->d_dblk, A, B0, B1, kidx, kw, phase, gbscale, gsign,
+      auto kd = p->plain ? k_split_digits<S, true> : k_split_digits<S, false>;
+      kd<<<p->n_dblk, 256, 0, st>>>(p->d_jobs, p->d_dblk, A, B0, B1, kidx, kw, phase, gbscale, gsign,
                                                     p->d_rexpA, p->d_rexpB, p->d_jobmax, flags_for(p, gsign),
                                                     p->beta, p->K_stride, p->arr[0], p->arr[1], p->arr[2],
                                                     p->arr[3]);

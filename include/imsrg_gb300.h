@@ -153,6 +153,16 @@ int imsrg_space_tensor_layout(imsrg_space* s, int lam, int trank, int parity, in
 int imsrg_space_ninej(imsrg_space* s, int lam, int ja, int jd, int J1, int jb, int jc, int J2, int Jbra, int Jket,
                       double* out);
 
+/* Self-test of the failure path of the split products' bounded waits: one
+ * kernel waits on an mbarrier that nothing arrives on, through the products'
+ * own wait loop bounded at `limit` iterations (1 .. the production bound,
+ * returned in *production_limit), sets the space's status word and returns;
+ * the call reports it as IMSRG_ERR_KERNEL and clears the word, and *cycles
+ * holds the SM clock cycles the wait took.  The context stays usable.  No
+ * counterpart in the reference. */
+int imsrg_space_wait_selftest(imsrg_space* s, unsigned limit, long long* cycles, unsigned* production_limit,
+                              void* stream);
+
 /* Host <-> device copies of the whole arena (arena_len doubles). */
 int imsrg_op_upload(imsrg_op* op, const double* host, void* stream);
 int imsrg_op_download(const imsrg_op* op, double* host, void* stream);
