@@ -642,82 +642,132 @@ __global__ void k_tzbar(DevSpace S, DevWork W, DevTensor T, const double* __rest
   Zb[T.zb_off[p] + (long long)col * nlo + r] = s;
 }
 
-// sum over the cross-coupled channels (J3 for (i, l), J4 for (k, j)) of
-// hat 9j (-1)^(j_j' + jl + J2 + J4) Zbar(il | kj): one of the two sums of the
-// inverse tensor Pandya transform (src/TensorCommutators.cc:790-900), with the
-// orbits (i, j) of the bra taken as given (the caller swaps them for the
-// other sum).  Zbar of (cbra, cket) is stored in the block of (lo, hi) =
-// (min, max) as n_lo x 2 n_hi; the element's place and phase follow the
-// reference's four cases (src/TensorCommutators.cc:830-852).
-__device__ double tinv_sum(const DevSpace& S, const DevTensor& T, const double* Zb, int hZ, int i, int j, int k,
-                           int l, int J1, int J2)
+// Zbar(al | kb) at (J3, J4) as the inverse transform reads it: the element's
+// place and phase follow the reference's four cases (src/TensorCommutators.cc:
+// 830-852); 0 when the Zbar block is not stored
+__device__ __forceinline__ double zbar_val(const DevSpace& S, const DevTensor& T, const double* Zb, int hZ, int a,
+                                           int b, int k, int l, int J3, int J4)
 {
-  const int ji = S.j2[i], jj = S.j2[j], jk = S.j2[k], jl = S.j2[l], Lam = T.lam;
-  const int pbc = (S.l[i] + S.l[l]) & 1, pkc = (S.l[k] + S.l[j]) & 1;
-  const int tbc = abs(S.tz2[i] - S.tz2[l]) / 2, tkc = abs(S.tz2[k] - S.tz2[j]) / 2;
-  const int kil = ket_index(S.norb, min(i, l), max(i, l)), kkj = ket_index(S.norb, min(j, k), max(j, k));
-  const int sum4 = (ji + jj + jk + jl) >> 1, hneg = hZ < 0;
-  const NineJRow nj = ninej_row(T, ji, jj, jk, jl, J1, J2);
-  const int J3min = abs(ji - jl) >> 1, J3max = (ji + jl) >> 1;
+  const int pbc = (S.l[a] + S.l[l]) & 1, pkc = (S.l[k] + S.l[b]) & 1;
+  const int tbc = abs(S.tz2[a] - S.tz2[l]) / 2, tkc = abs(S.tz2[k] - S.tz2[b]) / 2;
+  const int cbra = chan_index(J3, pbc, tbc), cket = chan_index(J4, pkc, tkc);
+  const int lo = min(cbra, cket), hi = max(cbra, cket);
+  const long long off = T.zb_lookup[lo * S.nch + hi];
+  if (off < 0) return 0.0;
+  const int ixil = S.ccJ_loc[J3 * S.nkets + ket_index(S.norb, min(a, l), max(a, l))];
+  const int ixkj = S.ccJ_loc[J4 * S.nkets + ket_index(S.norb, min(b, k), max(b, k))];
+  const double* M = Zb + off;
+  const int nrow = S.cc_n[lo];
+  const int sum4 = (S.j2[a] + S.j2[b] + S.j2[k] + S.j2[l]) >> 1, hneg = hZ < 0;
+  if (cbra <= cket) {
+    if (a <= l) return M[(long long)(ixkj + (k > b ? S.cc_n[cket] : 0)) * nrow + ixil];
+    return flip(M[(long long)(ixkj + (k > b ? 0 : S.cc_n[cket])) * nrow + ixil], hneg + J3 - J4 + sum4);
+  }
+  if (k <= b) return flip(M[(long long)(ixil + (a > l ? S.cc_n[cbra] : 0)) * nrow + ixkj], hneg + J3 - J4);
+  return flip(M[(long long)(ixil + (a > l ? 0 : S.cc_n[cbra])) * nrow + ixkj], sum4);
+}
+
+// the Zbar values one sum of the inverse transform reads for the quadruple
+// (a, b, k, l): slot (J3 - J3min) w + (J4 - J3 + lam), lanes over slots
+__device__ __forceinline__ void tinv_gather(const DevSpace& S, const DevTensor& T, const double* Zb, int hZ, int a,
+                                            int b, int k, int l, double* in, int lane)
+{
+  const int ja = S.j2[a], jb = S.j2[b], jk = S.j2[k], jl = S.j2[l], Lam = T.lam, w = 2 * Lam + 1;
+  const int J3min = abs(ja - jl) >> 1, nJ3 = ((ja + jl) >> 1) - J3min + 1;
+  const int J4lo = abs(jk - jb) >> 1, J4hi = (jk + jb) >> 1;
+  for (int s = lane; s < nJ3 * w; s += 32) {
+    const int J3 = J3min + s / w, J4 = J3 - Lam + s % w;
+    in[s] = (J4 < J4lo || J4 > J4hi) ? 0.0 : zbar_val(S, T, Zb, hZ, a, b, k, l, J3, J4);
+  }
+}
+
+// one sum over the gathered values: sum_{J3, J4} hat 9j (-1)^(jb + jl + J2 + J4)
+// Zbar (the 9j {ja jb J1; ...} row of (J1, J2))
+__device__ __forceinline__ double tinv_dot(const DevSpace& S, const DevTensor& T, int a, int b, int k, int l, int J1,
+                                           int J2, const double* in)
+{
+  const int ja = S.j2[a], jb = S.j2[b], jk = S.j2[k], jl = S.j2[l], Lam = T.lam, w = 2 * Lam + 1;
+  const NineJRow nj = ninej_row(T, ja, jb, jk, jl, J1, J2);
+  const int J3min = abs(ja - jl) >> 1, J3max = (ja + jl) >> 1;
   double acc = 0.0;
   for (int J3 = J3min; J3 <= J3max; ++J3) {
-    const int cbra = chan_index(J3, pbc, tbc);
-    const int ixil = S.ccJ_loc[J3 * S.nkets + kil];
-    const int nbras = S.cc_n[cbra];
-    const int J4min = max(abs(jk - jj) >> 1, abs(J3 - Lam)), J4max = min((jk + jj) >> 1, J3 + Lam);
+    const int J4min = max(abs(jk - jb) >> 1, abs(J3 - Lam)), J4max = min((jk + jb) >> 1, J3 + Lam);
+    const double* row = in + (J3 - J3min) * w - J3 + Lam;
     for (int J4 = J4min; J4 <= J4max; ++J4) {
       const double nh = nj.get(J3, J4);
       if (is_zero(nh)) continue;
-      const int cket = chan_index(J4, pkc, tkc);
-      const int lo = min(cbra, cket), hi = max(cbra, cket);
-      const long long off = T.zb_lookup[lo * S.nch + hi];
-      if (off < 0) continue;
-      const int ixkj = S.ccJ_loc[J4 * S.nkets + kkj];
-      const double* M = Zb + off;
-      const int nrow = S.cc_n[lo];
-      double z;
-      if (cbra <= cket) {
-        if (i <= l)
-          z = M[(long long)(ixkj + (k > j ? S.cc_n[cket] : 0)) * nrow + ixil];
-        else
-          z = flip(M[(long long)(ixkj + (k > j ? 0 : S.cc_n[cket])) * nrow + ixil], hneg + J3 - J4 + sum4);
-      } else {
-        if (k <= j)
-          z = flip(M[(long long)(ixil + (i > l ? nbras : 0)) * nrow + ixkj], hneg + J3 - J4);
-        else
-          z = flip(M[(long long)(ixil + (i > l ? 0 : nbras)) * nrow + ixkj], sum4);
-      }
-      acc = fma(flip(nh, ((jj + jl) >> 1) + J2 + J4), z, acc);
+      acc = fma(flip(nh, ((jb + jl) >> 1) + J2 + J4), row[J4], acc);
     }
   }
   return acc;
 }
 
-// inverse tensor Pandya transform, AddInverseTensorPandyaTransformation
-// (src/TensorCommutators.cc:754-920): a thread per element (ibra, iket) of a
-// stored block (iket >= ibra in a diagonal block, whose lower triangle takes
-// hZ times the upper)
-__global__ void k_tinv(DevSpace S, DevTensor T, const double* __restrict__ Zb, int hZ, double* __restrict__ Z)
+// Inverse tensor Pandya transform by orbit quadruple (AddInverseTensor-
+// PandyaTransformation, src/TensorCommutators.cc:754-920): a warp per (i <= j,
+// k <= l) of the layout's quadruple list.  The Zbar values of both sums (over
+// J3, J4) are gathered once into shared memory; then the lanes take the
+// (J1, J2) slots whose element the quadruple owns (a stored block, the upper
+// triangle of a diagonal one) and sum over them.  Each stored element is owned
+// by exactly one quadruple and slot, so there are no write conflicts.
+constexpr int kTqWarps = 8;
+
+__global__ void __launch_bounds__(32 * kTqWarps) k_tinv_q(DevSpace S, DevTensor T, const double* __restrict__ Zb,
+                                                         int hZ, double* __restrict__ Z,
+                                                         const int2* __restrict__ tq, long long nq, int slots)
 {
-  const int blk = blockIdx.y;
-  const int chb = T.bra[blk], chk = T.ket[blk];
-  const int nb = S.ch_n[chb], nk = S.ch_n[chk];
-  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (e >= (long long)nb * nk) return;
-  const int ik = (int)(e / nb), ib = (int)(e - (long long)ik * nb);
-  if (chb == chk && ik < ib) return;
-  const int i = S.ket_p[S.ch_kofs[chb] + ib], j = S.ket_q[S.ch_kofs[chb] + ib];
-  const int k = S.ket_p[S.ch_kofs[chk] + ik], l = S.ket_q[S.ch_kofs[chk] + ik];
-  const int J1 = ch_J(chb), J2 = ch_J(chk);
-  const int ji = S.j2[i], jj = S.j2[j];
-  const double commij = tinv_sum(S, T, Zb, hZ, i, j, k, l, J1, J2);
-  const double commji = i == j ? commij : tinv_sum(S, T, Zb, hZ, j, i, k, l, J1, J2);
-  const double z = unnorm(commij + flip(commji, 1 + ((ji + jj) >> 1) - J1), i == j, k == l);
-  Z[T.off[blk] + (long long)ik * nb + ib] += z;
-  if (chb == chk && ik != ib) Z[T.off[blk] + (long long)ib * nb + ik] += flip(z, hZ < 0);
+  extern __shared__ double s_in[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long qi = blockIdx.x * (long long)kTqWarps + warp;
+  if (qi >= nq) return;
+  double* in1 = s_in + (size_t)warp * 2 * slots;
+  double* in2 = in1 + slots;
+  const int2 v = tq[qi];
+  const int i = v.x & 0xFFFF, j = v.x >> 16, k = v.y & 0xFFFF, l = v.y >> 16;
+  tinv_gather(S, T, Zb, hZ, i, j, k, l, in1, lane);
+  if (i != j) tinv_gather(S, T, Zb, hZ, j, i, k, l, in2, lane);
+  __syncwarp();
+  const int ji = S.j2[i], jj = S.j2[j], jk = S.j2[k], jl = S.j2[l], Lam = T.lam, w = 2 * Lam + 1;
+  const int pb = (S.l[i] + S.l[j]) & 1, tb = (S.tz2[i] + S.tz2[j]) / 2;
+  const int pk = (S.l[k] + S.l[l]) & 1, tk = (S.tz2[k] + S.tz2[l]) / 2;
+  const int kb = ket_index(S.norb, i, j), kk = ket_index(S.norb, k, l);
+  const int J1min = abs(ji - jj) >> 1, nJ1 = ((ji + jj) >> 1) - J1min + 1;
+  const int J2lo = abs(jk - jl) >> 1, J2hi = (jk + jl) >> 1;
+  for (int t = lane; t < nJ1 * w; t += 32) {
+    const int J1 = J1min + t / w, J2 = J1 - Lam + t % w;
+    if (J2 < J2lo || J2 > J2hi || J1 >= S.NJ || J2 >= S.NJ) continue;
+    const int ib = S.ketJ_loc[J1 * S.nkets + kb], ik = S.ketJ_loc[J2 * S.nkets + kk];
+    if (ib < 0 || ik < 0) continue;
+    const int chb = chan_index(J1, pb, tb), chk = chan_index(J2, pk, tk);
+    if (chb > chk || (chb == chk && ik < ib)) continue;
+    const int blk = T.lookup[chb * S.nch + chk];
+    if (blk < 0) continue;
+    const double commij = tinv_dot(S, T, i, j, k, l, J1, J2, in1);
+    const double commji = i == j ? commij : tinv_dot(S, T, j, i, k, l, J1, J2, in2);
+    const double z = unnorm(commij + flip(commji, 1 + ((ji + jj) >> 1) - J1), i == j, k == l);
+    const int nb = S.ch_n[chb];
+    Z[T.off[blk] + (long long)ik * nb + ib] += z;
+    if (chb == chk && ik != ib) Z[T.off[blk] + (long long)ib * nb + ik] += flip(z, hZ < 0);
+  }
 }
 
 unsigned grid_for(long long n) { return (unsigned)std::max(1LL, (n + 255) / 256); }
+
+cudaError_t launch_tinv_q(const Space& s, const TensorLayout& t, const double* Zbar, double* Z, int hZ,
+                          cudaStream_t st)
+{
+  const long long nq = (long long)t.tq.size();
+  if (nq == 0) return cudaSuccess;
+  const int slots = t.tq_max_j3 * (2 * t.lam + 1);
+  const size_t smem = (size_t)kTqWarps * 2 * slots * sizeof(double);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_tinv_q, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  k_tinv_q<<<(unsigned)((nq + kTqWarps - 1) / kTqWarps), 32 * kTqWarps, smem, st>>>(s.dev, t.dev, Zbar, hZ, Z, t.d_tq,
+                                                                                     nq, slots);
+  count_launch();
+  return cudaGetLastError();
+}
 
 }  // namespace
 
@@ -786,11 +836,7 @@ cudaError_t launch_tensor_ph(const Space& s, const TensorLayout& t, const double
   k_tzbar<<<gz, 256, 0, st>>>(s.dev, s.work, t.dev, Xbar, Ybar, hX, hY, Zbar, s.work.phase_tab);
   count_launch();
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if (t.bra.empty() || t.max_blk_elems == 0) return cudaSuccess;
-  dim3 gi(grid_for(t.max_blk_elems), (unsigned)t.bra.size());
-  k_tinv<<<gi, 256, 0, st>>>(s.dev, t.dev, Zbar, hZ, Z);
-  count_launch();
-  return cudaGetLastError();
+  return launch_tinv_q(s, t, Zbar, Z, hZ, st);
 }
 
 // ---------------------------------------------------------- split form
@@ -839,11 +885,7 @@ cudaError_t launch_tensor_222_221_split(const Space& s, const TensorLayout& t, c
 cudaError_t launch_tensor_inverse_pandya(const Space& s, const TensorLayout& t, const double* Zbar, double* Z, int hZ,
                                          cudaStream_t st)
 {
-  if (t.bra.empty() || t.max_blk_elems == 0) return cudaSuccess;
-  dim3 gi(grid_for(t.max_blk_elems), (unsigned)t.bra.size());
-  k_tinv<<<gi, 256, 0, st>>>(s.dev, t.dev, Zbar, hZ, Z);
-  count_launch();
-  return cudaGetLastError();
+  return launch_tinv_q(s, t, Zbar, Z, hZ, st);
 }
 
 }  // namespace imsrg

@@ -78,6 +78,69 @@ TensorLayout::~TensorLayout()
   for (void* p : dev_allocs) cudaFree(p);
 }
 
+// The orbit quadruples of the inverse tensor Pandya transform (k_tinv_q): a
+// bra ket (i <= j) and a ket ket (k <= l) with the rank's parity and |dTz|,
+// kept when some (J1, J2) gives a stored element it owns: block (chb, chk)
+// with chb <= chk and, within a diagonal block, ket index >= bra index.
+static void build_quadruples(const Space& s, TensorLayout& t)
+{
+  const int N = s.norb, nk = s.nkets, NJ = s.NJ, d1 = s.d1, lam = t.lam;
+  std::vector<int> kp, kq;
+  for (int p = 0; p < N; ++p)
+    for (int q = p; q < N; ++q) {
+      kp.push_back(p);
+      kq.push_back(q);
+    }
+  struct Item {
+    int key;
+    int2 v;
+  };
+  std::vector<std::vector<Item>> part(nk);
+  int maxj = 0;
+  for (int p = 0; p < N; ++p) maxj = std::max(maxj, s.j2[p]);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int kb = 0; kb < nk; ++kb) {
+    const int i = kp[kb], j = kq[kb];
+    const int pb = (s.l[i] + s.l[j]) & 1, tb = (s.tz2[i] + s.tz2[j]) / 2;
+    const int ji = s.j2[i], jj = s.j2[j];
+    for (int kk = 0; kk < nk; ++kk) {
+      const int k = kp[kk], l = kq[kk];
+      const int pk = (s.l[k] + s.l[l]) & 1, tk = (s.tz2[k] + s.tz2[l]) / 2;
+      if (((pb + pk + t.parity) & 1) || std::abs(tb - tk) != t.trank) continue;
+      const int jk = s.j2[k], jl = s.j2[l];
+      bool owned = false;
+      for (int J1 = std::abs(ji - jj) / 2; J1 <= (ji + jj) / 2 && J1 < NJ && !owned; ++J1) {
+        const int ib = s.ketJ_loc[(size_t)J1 * nk + kb];
+        if (ib < 0) continue;
+        const int chb = 6 * J1 + 2 * (tb + 1) + pb;
+        for (int J2 = std::max(std::abs(jk - jl) / 2, std::abs(J1 - lam)); J2 <= std::min((jk + jl) / 2, J1 + lam) && J2 < NJ;
+             ++J2) {
+          const int ik = s.ketJ_loc[(size_t)J2 * nk + kk];
+          if (ik < 0) continue;
+          const int chk = 6 * J2 + 2 * (tk + 1) + pk;
+          if (chb < chk || (chb == chk && ik >= ib)) {
+            owned = true;
+            break;
+          }
+        }
+      }
+      if (!owned) continue;
+      const int key = ((((ji - 1) / 2) * d1 + (jj - 1) / 2) * d1 + (jk - 1) / 2) * d1 + (jl - 1) / 2;
+      part[kb].push_back({key, make_int2(i | (j << 16), k | (l << 16))});
+    }
+  }
+  // counting sort by class
+  const int nkey = d1 * d1 * d1 * d1;
+  std::vector<long long> cnt(nkey + 1, 0);
+  for (const auto& v : part)
+    for (const Item& it : v) ++cnt[it.key + 1];
+  for (int x = 0; x < nkey; ++x) cnt[x + 1] += cnt[x];
+  t.tq.assign((size_t)cnt[nkey], make_int2(0, 0));
+  for (const auto& v : part)
+    for (const Item& it : v) t.tq[(size_t)cnt[it.key]++] = it.v;
+  t.tq_max_j3 = maxj + 1;
+}
+
 TensorLayout* tensor_layout(Space& s, int lam, int trank, int parity)
 {
   const int key = (lam * 4 + trank) * 2 + parity;
@@ -241,6 +304,7 @@ TensorLayout* tensor_layout(Space& s, int lam, int trank, int parity)
     t->lad_n[c] = jb.K;
     t->lad_maxelems = std::max(t->lad_maxelems, (long long)jb.m * jb.K);
   }
+  build_quadruples(s, *t);
   t->hat2.assign((size_t)t->NJ * t->NJ, 0.0);
   for (int J1 = 0; J1 < t->NJ; ++J1)
     for (int J2 = 0; J2 < t->NJ; ++J2) t->hat2[(size_t)J1 * t->NJ + J2] = std::sqrt((double)((2 * J1 + 1) * (2 * J2 + 1)));
@@ -315,6 +379,7 @@ void tensor_upload(TensorLayout& t)
   d.hat2 = dev_copy(t, t.hat2);
   d.tob_off = dev_copy(t, t.tob_off);
   d.tob_list = dev_copy(t, t.tob_list);
+  t.d_tq = dev_copy(t, t.tq);
   d.lad_koff = dev_copy(t, t.lad_koff);
   d.lad_woff = dev_copy(t, t.lad_woff);
   d.lad_n = dev_copy(t, t.lad_n);

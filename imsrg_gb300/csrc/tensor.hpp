@@ -108,6 +108,12 @@ struct TensorLayout {
   double *d_yt = nullptr, *d_ybt = nullptr, *d_ybtf = nullptr, *d_xbf = nullptr;
   SplitPlan *sp_lad1 = nullptr, *sp_lad2 = nullptr, *sp_zb1 = nullptr, *sp_zb2 = nullptr;
   int max_tiles32 = 0;        // largest block in 32 x 32 tiles (transpose grid)
+  // orbit quadruples of the inverse tensor Pandya transform: (i | j << 16,
+  // k | l << 16) for every bra ket i <= j and ket ket k <= l that own at
+  // least one stored element, ordered by the class (ji, jj, jk, jl)
+  std::vector<int2> tq;
+  int tq_max_j3 = 0;          // largest J3 (or J1) range of a quadruple
+  int2* d_tq = nullptr;
   long long max_xbf = 0;      // largest X bar panel (2 nph x n_cc)
   DevTensor dev;
   bool dev_ready = false;
