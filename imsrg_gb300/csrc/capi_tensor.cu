@@ -62,7 +62,7 @@ int scratch(imsrg_space* sp, TensorLayout* tl)
   if ((rc = alloc(tl, tl->d_mpp, tl->total)) || (rc = alloc(tl, tl->d_mhh, tl->total)) ||
       (rc = alloc(tl, tl->d_xbar, sp->s->xb_total)) || (rc = alloc(tl, tl->d_ybar, tl->yb_total)) ||
       (rc = alloc(tl, tl->d_zbar, tl->zb_total)) || (rc = alloc(tl, tl->d_xw, sp->s->arena)) ||
-      (rc = alloc(tl, tl->d_wx, sp->s->arena)))
+      (rc = alloc(tl, tl->d_wx, sp->s->arena)) || (rc = alloc(tl, tl->d_yt, tl->total)))
     return rc;
   return IMSRG_OK;
 }
@@ -164,7 +164,7 @@ int split_ready(imsrg_space* sp, TensorLayout* tl)
   if (rc) return rc;
   std::lock_guard<std::mutex> g(sp->mu);
   const Space& s = *sp->s;
-  if ((rc = alloc(tl, tl->d_yt, tl->total)) || (rc = alloc(tl, tl->d_ybt, tl->yb_total)) ||
+  if ((rc = alloc(tl, tl->d_ybt, tl->yb_total)) ||
       (rc = alloc(tl, tl->d_ybtf, tl->yb_total)) || (rc = alloc(tl, tl->d_xbf, s.xb_total)))
     return rc;
   try {
@@ -240,8 +240,11 @@ int t121(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
 
 int t122(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st)
 {
+  TensorLayout* tl = Y->tl;
+  int rc = scratch(X->sp, tl);
+  if (rc) return rc;
   ProfScope ps("comm122st", st);
-  T_CUDA(launch_tensor_122(*X->sp->s, *Y->tl, X->d, Y->d, Y->herm, Z->d, st));
+  T_CUDA(launch_tensor_122(*X->sp->s, *tl, X->d, Y->d, X->herm, tl->d_yt, Z->d, st));
   return IMSRG_OK;
 }
 

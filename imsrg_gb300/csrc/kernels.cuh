@@ -90,8 +90,9 @@ struct TensorLayout;
 cudaError_t launch_tensor_111(const Space& s, const double* X, const double* Y, double* Z, cudaStream_t st);
 cudaError_t launch_tensor_121(const Space& s, const TensorLayout& t, const int* dev_holes, const double* X,
                               const double* Y, int hY, double* Z, int hZ, cudaStream_t st);
-cudaError_t launch_tensor_122(const Space& s, const TensorLayout& t, const double* X, const double* Y, int hY,
-                              double* Z, cudaStream_t st);
+// YT: scratch of layout t (Y with its blocks transposed, written here)
+cudaError_t launch_tensor_122(const Space& s, const TensorLayout& t, const double* X, const double* Y, int hX,
+                              double* YT, double* Z, cudaStream_t st);
 // XW, WX: scratch of the space's arena length; D (= Mpp - Mhh), Mhh: scratch
 // arenas of layout t
 cudaError_t launch_tensor_222_221(const Space& s, const TensorLayout& t, const double* X, const double* Y,

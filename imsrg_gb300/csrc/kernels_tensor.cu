@@ -228,117 +228,232 @@ __global__ void k_t121(DevSpace S, DevTensor T, const int* __restrict__ holes, i
 // -------------------------------------------------------------- comm122st
 // src/TensorCommutators.cc:158-312: a thread per element of every stored block
 // (blockIdx.y = block)
-__global__ void k_t122(DevSpace S, DevTensor T, const double* __restrict__ X, const double* __restrict__ Y, int hY,
-                       double* __restrict__ Z)
+// The element Z(ij, kl) of block (chb, chk) is a sum over the bra's
+// partners and a sum over the ket's partners (src/TensorCommutators.cc:
+// 158-312 with the reference's i == j and k == l shortcuts):
+//   bra side:  sum_a X1(a,i) Y(aj, kl) + X1(a,j) Y(ia, kl)   (Y rows: chb kets)
+//            + hat (-1)^.. 6j Y1(a,i) X(aj, kl) ...          (X rows: chk kets)
+//   ket side: -sum_a X1(k,a) Y(ij, al) + ...                 (Y columns: chk kets)
+//            + hat (-1)^.. 6j Y1(k,a) X(ij, la) ...          (X columns: chb kets)
+// Each side is a list of (partner ket, coefficient) per bra or per ket,
+// built once per block tile in shared memory; every element is then one FMA
+// per list entry.  The pair normalisation factorises as (1/sqrt2)^(i==j)
+// (1/sqrt2)^(k==l) and cancels the fixed side's sqrt(2), so each side carries
+// its own factor.  Bra-side values are read as Y^T (the block transposed) and
+// X^T = hX X (symmetry) so that lanes over kets read consecutive addresses.
+struct T122Lists {
+  int* yrow;
+  double* ycoef;
+  int* xrow;
+  double* xcoef;
+  int* ny;
+  int* nx;
+  int LY, LX;
+};
+
+// carve the lists of 32 bras (or kets) out of dynamic shared memory
+__device__ __forceinline__ T122Lists t122_lists(unsigned char* smem, int LY, int LX)
 {
-  const int blk = blockIdx.y;
-  const int chb = T.bra[blk], chk = T.ket[blk];  // chb <= chk: the element's own block is stored
-  const int nb = S.ch_n[chb], nk = S.ch_n[chk];
-  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (e >= (long long)nb * nk) return;
-  (void)hY;
-  const int ik = (int)(e / nb), ib = (int)(e - (long long)ik * nb);
-  const int N = S.norb, Lam = T.lam;
-  const int i = S.ket_p[S.ch_kofs[chb] + ib], j = S.ket_q[S.ch_kofs[chb] + ib];
-  const int k = S.ket_p[S.ch_kofs[chk] + ik], l = S.ket_q[S.ch_kofs[chk] + ik];
+  T122Lists L;
+  L.ycoef = (double*)smem;
+  L.xcoef = L.ycoef + 32 * LY;
+  L.yrow = (int*)(L.xcoef + 32 * LX);
+  L.xrow = L.yrow + 32 * LY;
+  L.ny = L.xrow + 32 * LX;
+  L.nx = L.ny + 32;
+  L.LY = LY;
+  L.LX = LX;
+  return L;
+}
+
+// Entries of one bra (side 0: p = i, q = j; J, J' = J1, J2; Y rows in chb,
+// X rows in chk) or one ket (side 1: p = k, q = l; Y columns in chk, X
+// columns in chb), the lanes of a warp over the candidate partners, compacted
+// by ballot into slot s of the lists.
+__device__ void t122_build(const DevSpace& S, const DevTensor& T, const double* X, const double* Y, int side, int p,
+                           int q, int chb, int chk, int hX, int s, T122Lists& L)
+{
+  const int lane = threadIdx.x & 31, N = S.norb, Lam = T.lam;
   const int J1 = ch_J(chb), J2 = ch_J(chk);
-  const int ji = S.j2[i], jj = S.j2[j], jk = S.j2[k], jl = S.j2[l];
+  const int jp = S.j2[p], jq = S.j2[q];
+  const bool same = p == q;
   const double* X1 = X + 32;
   const double* Y1 = Y + 32;
-  // <ab|Y|kl> for a bra (a, b) of chb: column ik of the element's block;
-  // <ij|Y|cd> for a ket (c, d) of chk: row ib of it (TwoBodyME::GetTBME with
-  // the swap phase and sqrt(2) of the bra or ket that varies; the fixed side's
-  // sqrt(2) is applied to the sums)
-  const double* Yblk = Y + T.off[blk];
-  const double* Ycol = Yblk + (long long)ik * nb;
-  auto y_bra = [&](int a, int b) -> double {
-    const int bi = ket_in(S, chb, a, b);
-    if (bi < 0) return 0.0;
-    double v = flip(Ycol[bi], a > b ? ((S.j2[a] + S.j2[b]) >> 1) + 1 + J1 : 0);
-    return a == b ? v * kSqrt2t : v;
-  };
-  auto y_ket = [&](int c, int d) -> double {
-    const int ki = ket_in(S, chk, c, d);
-    if (ki < 0) return 0.0;
-    double v = flip(Yblk[(long long)ki * nb + ib], c > d ? ((S.j2[c] + S.j2[d]) >> 1) + 1 + J2 : 0);
-    return c == d ? v * kSqrt2t : v;
-  };
-  // scalar <ab|X|kl>_(J2) (column ik of X's chk block) and <ij|X|cd>_(J1)
-  // (row ib of X's chb block)
-  const double* Xk = X + S.ch_off[chk] + (long long)ik * nk;
-  const double* Xb = X + S.ch_off[chb] + ib;
-  auto x_bra = [&](int a, int b) -> double {
-    const int bi = ket_in(S, chk, a, b);
-    if (bi < 0) return 0.0;
-    double v = flip(Xk[bi], a > b ? ((S.j2[a] + S.j2[b]) >> 1) + 1 + J2 : 0);
-    return a == b ? v * kSqrt2t : v;
-  };
-  auto x_ket = [&](int c, int d) -> double {
-    const int ki = ket_in(S, chb, c, d);
-    if (ki < 0) return 0.0;
-    double v = flip(Xb[(long long)ki * nb], c > d ? ((S.j2[c] + S.j2[d]) >> 1) + 1 + J1 : 0);
-    return c == d ? v * kSqrt2t : v;
-  };
-  const double sk = k == l ? kSqrt2t : 1.0, sb = i == j ? kSqrt2t : 1.0;
-  // X one-body, Y two-body
-  double c1 = 0, c2 = 0, c3 = 0, c4 = 0;
-  for (int q = 0; q < S.ob_count[i]; ++q) {
-    const int a = S.ob_list[S.ob_start[i] + q];
-    c1 = fma(X1[(long long)a * N + i], y_bra(a, j), c1);
-  }
-  if (i == j) {
-    c2 = c1;
-  } else {
-    for (int q = 0; q < S.ob_count[j]; ++q) {
-      const int a = S.ob_list[S.ob_start[j] + q];
-      c2 = fma(X1[(long long)a * N + j], y_bra(i, a), c2);
-    }
-  }
-  for (int q = 0; q < S.ob_count[k]; ++q) {
-    const int a = S.ob_list[S.ob_start[k] + q];
-    c3 = fma(X1[(long long)k * N + a], y_ket(a, l), c3);
-  }
-  if (k == l) {
-    c4 = c3;
-  } else {
-    for (int q = 0; q < S.ob_count[l]; ++q) {
-      const int a = S.ob_list[S.ob_start[l] + q];
-      c4 = fma(X1[(long long)l * N + a], y_ket(k, a), c4);
-    }
-  }
-  double cijkl = (c1 + c2) * sk - (c3 + c4) * sb;
-  // Y one-body, X two-body
-  c1 = c2 = c3 = c4 = 0;
-  for (int q = T.tob_off[i]; q < T.tob_off[i + 1]; ++q) {
-    const int a = T.tob_list[q];
-    c1 -= sixjA(T, J2, J1, ji, S.j2[a], jj) * Y1[(long long)a * N + i] * x_bra(a, j);
-  }
-  if (i == j) {
-    c2 = -c1;
-  } else {
-    for (int q = T.tob_off[j]; q < T.tob_off[j + 1]; ++q) {
-      const int a = T.tob_list[q];
-      c2 += sixjA(T, J2, J1, jj, S.j2[a], ji) * Y1[(long long)a * N + j] * x_bra(a, i);
-    }
-  }
-  for (int q = T.tob_off[k]; q < T.tob_off[k + 1]; ++q) {
-    const int a = T.tob_list[q];
-    c3 -= sixjA(T, J1, J2, jk, S.j2[a], jl) * Y1[(long long)k * N + a] * x_ket(l, a);
-  }
-  if (k == l) {
-    c4 = -c3;
-  } else {
-    for (int q = T.tob_off[l]; q < T.tob_off[l + 1]; ++q) {
-      const int a = T.tob_list[q];
-      c4 += sixjA(T, J1, J2, jl, S.j2[a], jk) * Y1[(long long)l * N + a] * x_ket(k, a);
-    }
-  }
-  const int odd1 = ((ji + jj) >> 1) + J2 + Lam;
-  const int odd2 = J1 - J2 + Lam, odd3 = odd2;
-  const int odd4 = ((jk + jl) >> 1) - J1 + Lam;
+  const int n1 = S.ob_count[p], n2 = same ? 0 : S.ob_count[q];
+  const int n3 = T.tob_off[p + 1] - T.tob_off[p], n4 = same ? 0 : T.tob_off[q + 1] - T.tob_off[q];
+  const int ntot = n1 + n2 + n3 + n4;
   const double hat = T.hat2[J1 * T.NJ + J2];
-  cijkl += hat * ((flip(c1, odd1) + flip(c2, odd2)) * sk + (flip(c3, odd3) + flip(c4, odd4)) * sb);
-  Z[T.off[blk] + (long long)ik * nb + ib] += unnorm(cijkl, i == j, k == l);
+  const double fnorm = same ? kInvSqrt2 : 1.0;
+  // the two X-side phases (odd1, odd2 for a bra; odd3, odd4 for a ket)
+  const int oddA = side == 0 ? ((jp + jq) >> 1) + J2 + Lam : J1 - J2 + Lam;
+  const int oddB = side == 0 ? J1 - J2 + Lam : ((jp + jq) >> 1) - J1 + Lam;
+  int ny = 0, nx = 0;
+  for (int c0 = 0; c0 < ntot; c0 += 32) {
+    const int t = c0 + lane;
+    int row = -1;
+    double coef = 0.0;
+    bool isx = false;
+    if (t < n1 + n2) {
+      // X one-body, Y two-body
+      const bool first = t < n1;
+      const int a = first ? S.ob_list[S.ob_start[p] + t] : S.ob_list[S.ob_start[q] + t - n1];
+      const int ja = S.j2[a];
+      if (side == 0) {
+        // bra (a, q) or (p, a) in chb: coefficient X1(a, p) or X1(a, q)
+        const int u = first ? a : p, v = first ? q : a;
+        row = ket_in(S, chb, u, v);
+        coef = X1[(long long)a * N + (first ? p : q)];
+        coef = flip(coef, u > v ? ((S.j2[u] + S.j2[v]) >> 1) + 1 + J1 : 0);
+        if (u == v) coef *= kSqrt2t;
+        if (same) coef *= 2.0;
+      } else {
+        // ket (a, q) or (p, a) in chk: coefficient -X1(p, a) or -X1(q, a)
+        const int u = first ? a : p, v = first ? q : a;
+        row = ket_in(S, chk, u, v);
+        coef = -X1[(long long)(first ? p : q) * N + a];
+        coef = flip(coef, u > v ? ((S.j2[u] + S.j2[v]) >> 1) + 1 + J2 : 0);
+        if (u == v) coef *= kSqrt2t;
+        if (same) coef *= 2.0;
+      }
+      (void)ja;
+      coef *= fnorm;
+    } else if (t < ntot) {
+      // Y one-body, X two-body
+      isx = true;
+      const bool first = t < n1 + n2 + n3;
+      const int a = first ? T.tob_list[T.tob_off[p] + t - n1 - n2] : T.tob_list[T.tob_off[q] + t - n1 - n2 - n3];
+      const int ja = S.j2[a];
+      double sg;
+      if (side == 0) {
+        // bra (a, q) or (a, p) of chk, X rows: -6j{J2 J1 lam; jp ja jq} Y1(a, p), +6j{..; jq ja jp} Y1(a, q)
+        const int u = a, v = first ? q : p;
+        row = ket_in(S, chk, u, v);
+        coef = first ? -sixjA(T, J2, J1, jp, ja, jq) * Y1[(long long)a * N + p]
+                     : sixjA(T, J2, J1, jq, ja, jp) * Y1[(long long)a * N + q];
+        coef = flip(coef, u > v ? ((S.j2[u] + S.j2[v]) >> 1) + 1 + J2 : 0);
+        if (u == v) coef *= kSqrt2t;
+      } else {
+        // ket (q, a) or (p, a) of chb, X columns: -6j{J1 J2 lam; jp ja jq} Y1(p, a), +6j{..; jq ja jp} Y1(q, a)
+        const int u = first ? q : p, v = a;
+        row = ket_in(S, chb, u, v);
+        coef = first ? -sixjA(T, J1, J2, jp, ja, jq) * Y1[(long long)p * N + a]
+                     : sixjA(T, J1, J2, jq, ja, jp) * Y1[(long long)q * N + a];
+        coef = flip(coef, u > v ? ((S.j2[u] + S.j2[v]) >> 1) + 1 + J1 : 0);
+        if (u == v) coef *= kSqrt2t;
+      }
+      // hat (-1)^odd; for p == q the partner list repeats with the opposite
+      // sign, which folds into (-1)^oddA - (-1)^oddB
+      if (same)
+        sg = (double)(iphase(oddA) - iphase(oddB));
+      else
+        sg = (double)iphase(first ? oddA : oddB);
+      coef *= hat * sg * fnorm;
+      if (side == 0 && hX < 0) coef = -coef;  // X^T = hX X
+    }
+    const bool vy = row >= 0 && !isx && coef != 0.0, vx = row >= 0 && isx && coef != 0.0;
+    const unsigned my = __ballot_sync(0xffffffffu, vy), mx = __ballot_sync(0xffffffffu, vx);
+    const unsigned below = (1u << lane) - 1;
+    if (vy) {
+      const int pos = ny + __popc(my & below);
+      L.yrow[s * L.LY + pos] = row;
+      L.ycoef[s * L.LY + pos] = coef;
+    }
+    if (vx) {
+      const int pos = nx + __popc(mx & below);
+      L.xrow[s * L.LX + pos] = row;
+      L.xcoef[s * L.LX + pos] = coef;
+    }
+    ny += __popc(my);
+    nx += __popc(mx);
+  }
+  if (lane == 0) {
+    L.ny[s] = ny;
+    L.nx[s] = nx;
+  }
+}
+
+// bra side: a block per (32 bras, block); warp w builds the lists of bras
+// w, w + 8, ...; then for each 32-ket chunk the warps take 4 bras each, lanes
+// over kets (reads of Y^T and X^T rows), results through a shared tile so the
+// Z update is coalesced over bras
+__global__ void __launch_bounds__(256) k_t122_bra(DevSpace S, DevTensor T, const double* __restrict__ X,
+                                                  const double* __restrict__ Y, const double* __restrict__ YT, int hX,
+                                                  double* __restrict__ Z, int LY, int LX)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double tile[32][33];
+  const int blk = blockIdx.y;
+  const int chb = T.bra[blk], chk = T.ket[blk];
+  const int nb = S.ch_n[chb], nk = S.ch_n[chk];
+  const int ib0 = blockIdx.x * 32;
+  if (ib0 >= nb) return;
+  T122Lists L = t122_lists(smem, LY, LX);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int b = warp; b < 32; b += 8) {
+    const int ib = ib0 + b;
+    if (ib < nb)
+      t122_build(S, T, X, Y, 0, S.ket_p[S.ch_kofs[chb] + ib], S.ket_q[S.ch_kofs[chb] + ib], chb, chk, hX, b, L);
+    else if (lane == 0)
+      L.ny[b] = L.nx[b] = 0;
+  }
+  __syncthreads();
+  const double* yt = YT + T.off[blk];         // nb x nk transposed: yt[row nk + ik]
+  const double* xk = X + S.ch_off[chk];        // symmetric: X(row, ik) = hX xk[row nk + ik]
+  for (int k0 = 0; k0 < nk; k0 += 32) {
+    const int ik = k0 + lane;
+    for (int b = warp; b < 32; b += 8) {
+      double z = 0.0;
+      if (ik < nk) {
+        const int ny = L.ny[b], nx = L.nx[b];
+        for (int e = 0; e < ny; ++e) z = fma(L.ycoef[b * LY + e], yt[(long long)L.yrow[b * LY + e] * nk + ik], z);
+        for (int e = 0; e < nx; ++e) z = fma(L.xcoef[b * LX + e], xk[(long long)L.xrow[b * LX + e] * nk + ik], z);
+      }
+      tile[b][lane] = z;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * 32; e += 256) {
+      const int kk = e >> 5, b = e & 31;
+      if (ib0 + b < nb && k0 + kk < nk) Z[T.off[blk] + (long long)(k0 + kk) * nb + ib0 + b] += tile[b][kk];
+    }
+    __syncthreads();
+  }
+}
+
+// ket side: a block per (32 kets, block); lists per ket, then warps take 4
+// kets each, lanes over bras (reads of Y's and X's columns), Z += directly
+__global__ void __launch_bounds__(256) k_t122_ket(DevSpace S, DevTensor T, const double* __restrict__ X,
+                                                  const double* __restrict__ Y, int hX, double* __restrict__ Z,
+                                                  int LY, int LX)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int blk = blockIdx.y;
+  const int chb = T.bra[blk], chk = T.ket[blk];
+  const int nb = S.ch_n[chb], nk = S.ch_n[chk];
+  const int ik0 = blockIdx.x * 32;
+  if (ik0 >= nk) return;
+  T122Lists L = t122_lists(smem, LY, LX);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int c = warp; c < 32; c += 8) {
+    const int ik = ik0 + c;
+    if (ik < nk)
+      t122_build(S, T, X, Y, 1, S.ket_p[S.ch_kofs[chk] + ik], S.ket_q[S.ch_kofs[chk] + ik], chb, chk, hX, c, L);
+    else if (lane == 0)
+      L.ny[c] = L.nx[c] = 0;
+  }
+  __syncthreads();
+  const double* yb = Y + T.off[blk];   // nb x nk: yb[col nb + ib]
+  const double* xb = X + S.ch_off[chb];  // nb x nb: xb[col nb + ib]
+  for (int c = warp; c < 32; c += 8) {
+    const int ik = ik0 + c;
+    if (ik >= nk) continue;
+    const int ny = L.ny[c], nx = L.nx[c];
+    for (int ib = lane; ib < nb; ib += 32) {
+      double z = 0.0;
+      for (int e = 0; e < ny; ++e) z = fma(L.ycoef[c * LY + e], yb[(long long)L.yrow[c * LY + e] * nb + ib], z);
+      for (int e = 0; e < nx; ++e) z = fma(L.xcoef[c * LX + e], xb[(long long)L.xrow[c * LX + e] * nb + ib], z);
+      Z[T.off[blk] + (long long)ik * nb + ib] += z;
+    }
+  }
 }
 
 // --------------------------------------------------- comm222_pp_hh_221st
@@ -788,12 +903,30 @@ cudaError_t launch_tensor_121(const Space& s, const TensorLayout& t, const int* 
   return cudaGetLastError();
 }
 
-cudaError_t launch_tensor_122(const Space& s, const TensorLayout& t, const double* X, const double* Y, int hY,
-                              double* Z, cudaStream_t st)
+cudaError_t launch_tensor_122(const Space& s, const TensorLayout& t, const double* X, const double* Y, int hX,
+                              double* YT, double* Z, cudaStream_t st)
 {
   if (t.bra.empty() || t.max_blk_elems == 0) return cudaSuccess;
-  dim3 grid(grid_for(t.max_blk_elems), (unsigned)t.bra.size());
-  k_t122<<<grid, 256, 0, st>>>(s.dev, t.dev, X, Y, hY, Z);
+  cudaError_t e;
+  // Y^T for the bra side
+  k_ttranspose<<<dim3((unsigned)t.max_tiles32, (unsigned)t.bra.size()), dim3(32, 8), 0, st>>>(s.dev, t.dev, Y, YT);
+  count_launch();
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  const int LY = std::max(1, 2 * t.max_ob), LX = std::max(1, 2 * t.max_tob);
+  const size_t smem = (size_t)32 * (LY + LX) * (sizeof(double) + sizeof(int)) + 64 * sizeof(int);
+  if (smem > 40 * 1024) {
+    if ((e = cudaFuncSetAttribute(k_t122_bra, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+            cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_t122_ket, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+      return e;
+  }
+  int maxn = 0;
+  for (int c = 0; c < s.nch; ++c) maxn = std::max(maxn, s.ch[c].n());
+  const dim3 grid((unsigned)((maxn + 31) / 32), (unsigned)t.bra.size());
+  k_t122_bra<<<grid, 256, smem, st>>>(s.dev, t.dev, X, Y, YT, hX, Z, LY, LX);
+  count_launch();
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  k_t122_ket<<<grid, 256, smem, st>>>(s.dev, t.dev, X, Y, hX, Z, LY, LX);
   count_launch();
   return cudaGetLastError();
 }

@@ -229,6 +229,10 @@ TensorLayout* tensor_layout(Space& s, int lam, int trank, int parity)
       if (t->ob_ok[(size_t)i * N + j]) t->tob_list.push_back(j);
   }
   t->tob_off[N] = (int)t->tob_list.size();
+  for (int i = 0; i < N; ++i) {
+    t->max_tob = std::max(t->max_tob, t->tob_off[i + 1] - t->tob_off[i]);
+    t->max_ob = std::max(t->max_ob, s.ob_count[i]);
+  }
   // angular tables, half-integers widened by lam (the 9j sums reach j + lam)
   t->NJ = s.NJ;
   t->d1x = s.d1 + lam;

@@ -90,6 +90,7 @@ struct TensorLayout {
   std::vector<double> hat2;
   std::vector<int> lad_koff, lad_woff, lad_n;
   std::vector<int> tob_off, tob_list;
+  int max_ob = 0, max_tob = 0;  // longest one-body partner list (scalar, tensor) of an orbit
   long long lad_maxelems = 0;  // largest n_channel x gather length (grid sizing)
   int64_t zb_total = 0, yb_total = 0;
   int zb_maxelems = 0, yb_maxelems = 0;  // largest block of each list (grid sizing)
