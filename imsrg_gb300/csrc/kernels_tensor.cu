@@ -803,15 +803,23 @@ __device__ __forceinline__ double tinv_dot(const DevSpace& S, const DevTensor& T
 {
   const int ja = S.j2[a], jb = S.j2[b], jk = S.j2[k], jl = S.j2[l], Lam = T.lam, w = 2 * Lam + 1;
   const NineJRow nj = ninej_row(T, ja, jb, jk, jl, J1, J2);
+  if (!nj.p) return 0.0;
+  // the row's J1 window is this sum's J3 range (both |ja - jl| .. ja + jl),
+  // and J4 - J3 + lam stays in [0, w): every slot below is in the table
   const int J3min = abs(ja - jl) >> 1, J3max = (ja + jl) >> 1;
+  const int J4lo = abs(jk - jb) >> 1, J4hi = (jk + jb) >> 1;
+  const long long st = nj.stride;
   double acc = 0.0;
   for (int J3 = J3min; J3 <= J3max; ++J3) {
-    const int J4min = max(abs(jk - jb) >> 1, abs(J3 - Lam)), J4max = min((jk + jb) >> 1, J3 + Lam);
-    const double* row = in + (J3 - J3min) * w - J3 + Lam;
-    for (int J4 = J4min; J4 <= J4max; ++J4) {
-      const double nh = nj.get(J3, J4);
+    const int J4min = max(J4lo, abs(J3 - Lam)), J4max = min(J4hi, J3 + Lam);
+    if (J4min > J4max) continue;
+    long long k9 = ((long long)(J3 - J3min) * w + (J4min - J3 + Lam)) * st;
+    int e = (J3 - J3min) * w + (J4min - J3 + Lam);
+    int odd = ((jb + jl) >> 1) + J2 + J4min;
+    for (int J4 = J4min; J4 <= J4max; ++J4, k9 += st, ++e, ++odd) {
+      const double nh = nj.p[k9];
       if (is_zero(nh)) continue;
-      acc = fma(flip(nh, ((jb + jl) >> 1) + J2 + J4), row[J4], acc);
+      acc = fma(flip(nh, odd), in[e], acc);
     }
   }
   return acc;
@@ -826,7 +834,7 @@ __device__ __forceinline__ double tinv_dot(const DevSpace& S, const DevTensor& T
 // by exactly one quadruple and slot, so there are no write conflicts.
 constexpr int kTqWarps = 8;
 
-__global__ void __launch_bounds__(32 * kTqWarps) k_tinv_q(DevSpace S, DevTensor T, const double* __restrict__ Zb,
+__global__ void __launch_bounds__(32 * kTqWarps, 4) k_tinv_q(DevSpace S, DevTensor T, const double* __restrict__ Zb,
                                                          int hZ, double* __restrict__ Z,
                                                          const int2* __restrict__ tq, long long nq, int slots)
 {

@@ -210,11 +210,16 @@ struct NineJRow {
   const double* p = nullptr;  // slot of (J1min, o2 = 0)
   long long stride = 0;       // between consecutive (J1, o2) slots
   int J1min = 0, J1max = -1, w = 0, L = 0;
-  IMSRG_HD double get(int J1, int J2) const
+  IMSRG_HD long long slot(int J1, int J2) const
   {
     const int o2 = J2 - J1 + L;
-    if (!p || J1 < J1min || J1 > J1max || o2 < 0 || o2 >= w) return 0.0;
-    return p[((long long)(J1 - J1min) * w + o2) * stride];
+    if (!p || J1 < J1min || J1 > J1max || o2 < 0 || o2 >= w) return -1;
+    return ((long long)(J1 - J1min) * w + o2) * stride;
+  }
+  IMSRG_HD double get(int J1, int J2) const
+  {
+    const long long k = slot(J1, J2);
+    return k < 0 ? 0.0 : p[k];
   }
 };
 
@@ -228,7 +233,8 @@ IMSRG_HD NineJRow ninej_row(const DevTensor& T, int ja, int jb, int jc, int jd, 
   const int o4 = Jket - Jbra + L;
   if (Jbra < Jbmin || Jbra > Jbmax || o4 < 0 || o4 >= w) return r;
   const int nJb = Jbmax - Jbmin + 1;
-  r.p = T.nj_hat + T.nj_base[((a * d1 + b) * d1 + c) * d1 + d] + (long long)(Jbra - Jbmin) * w + o4;
+  const long long o = T.nj_base[((a * d1 + b) * d1 + c) * d1 + d] + (long long)(Jbra - Jbmin) * w + o4;
+  r.p = T.nj_hat + o;
   r.stride = (long long)nJb * w;
   r.J1min = (ja > jd ? ja - jd : jd - ja) >> 1;
   r.J1max = (ja + jd) >> 1;
