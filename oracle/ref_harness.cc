@@ -203,14 +203,15 @@ static std::vector<double> store_tensor(const Operator& op, size_t n_orb) {
 }
 
 static int tensor_main(int argc, char** argv) {
-  if (argc != 10) {
-    std::cerr << "usage: ref_harness tensor <emax> <lam> <trank> <parity> <herm> <X.bin> <T.bin> <outdir>\n";
+  if (argc != 10 && argc != 11) {
+    std::cerr << "usage: ref_harness tensor <emax> <lam> <trank> <parity> <herm> <X.bin> <T.bin> <outdir> [nucleus]\n";
     return 1;
   }
   int emax = std::atoi(argv[2]), lam = std::atoi(argv[3]), trank = std::atoi(argv[4]), parity = std::atoi(argv[5]);
   int herm = std::atoi(argv[6]);
   std::string outdir = argv[9];
-  ModelSpace ms(emax, "O16", "O16");
+  const std::string nucleus = argc == 11 ? argv[10] : "O16";
+  ModelSpace ms(emax, nucleus, nucleus);
   ArenaLayout L = make_layout(ms);
   size_t N = L.n_orb;
   Operator X(ms, 0, 0, 0, 2);

@@ -37,6 +37,10 @@ Fixtures (arena layout: see oracle/modelspace_ref.py):
                      random_tensor) of rank (J, T, parity) = (2, 0, 0)
                      hermitian, (1, 0, 1) hermitian and (1, 1, 0)
                      anti-hermitian at emax 2; the first case only at emax 3.
+  golden_tensor_emax3_O18.npz
+                     the same on O18's space (fractional 0d5/2 neutron
+                     occupations) for the ranks (2, 0, 0) hermitian and
+                     (1, 1, 0) anti-hermitian.
   sixj_exact.npz     6j symbols {j1 j2 J3; j4 j5 J6} for half-integer
                      j <= 9/2 and integer J <= 9, evaluated in exact rational
                      arithmetic (Racah formula with Python integers), the pin for
@@ -127,8 +131,11 @@ TENSOR_CASES = {"e2": (2, 0, 0, 1), "e1": (1, 0, 1, 1), "gt": (1, 1, 0, -1)}
 TENSOR_TERMS = ["comm111st", "comm121st", "comm122st", "comm222_pp_hh_221st", "comm222_phst", "full"]
 
 
-def run_reference_tensor(emax, cases):
-    ms = RefModelSpace(emax)
+def run_reference_tensor(emax, cases, nucleus=None):
+    """nucleus: None for O16, else (name, A, Z) of the reference the space
+    is built on (its occupations enter the terms; the arenas' layout does
+    not change)."""
+    ms = RefModelSpace(emax) if nucleus is None else RefModelSpace(emax, nucleus[1], nucleus[2])
     X = ms.random_operator(1000 + emax, hermitian=True)
     harness = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
     out = {"X": X, "emax": np.array(emax)}
@@ -138,9 +145,11 @@ def run_reference_tensor(emax, cases):
             lam, trank, par, herm = TENSOR_CASES[name]
             T = ms.random_tensor(8000 + 10 * emax + i, lam, trank, par, hermitian=herm > 0)
             T.tofile(os.path.join(td, "T.bin"))
-            subprocess.run([harness, "tensor", str(emax), str(lam), str(trank), str(par), str(herm),
-                            os.path.join(td, "X.bin"), os.path.join(td, "T.bin"), td], check=True,
-                           stdout=subprocess.DEVNULL, env=dict(os.environ, OMP_NUM_THREADS="1"))
+            cmd = [harness, "tensor", str(emax), str(lam), str(trank), str(par), str(herm),
+                   os.path.join(td, "X.bin"), os.path.join(td, "T.bin"), td]
+            if nucleus is not None:
+                cmd.append(nucleus[0])
+            subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, env=dict(os.environ, OMP_NUM_THREADS="1"))
             out[name + "_T"] = T
             out[name + "_rank"] = np.array([lam, trank, par, herm])
             for t in TENSOR_TERMS:
@@ -204,10 +213,12 @@ def main():
         np.savez_compressed(os.path.join(HERE, "golden_flow_emax%d.npz" % e), **run_reference_flow(e))
     np.savez_compressed(os.path.join(HERE, "golden_tensor_emax2.npz"), **run_reference_tensor(2, ["e2", "e1", "gt"]))
     np.savez_compressed(os.path.join(HERE, "golden_tensor_emax3.npz"), **run_reference_tensor(3, ["e2"]))
+    np.savez_compressed(os.path.join(HERE, "golden_tensor_emax3_O18.npz"),
+                        **run_reference_tensor(3, ["e2", "gt"], ("O18", 18, 8)))
     keys, vals = make_sixj_table()
     np.savez_compressed(os.path.join(HERE, "sixj_exact.npz"), keys=keys, values=vals)
     for f in ("golden_emax2.npz", "golden_emax3.npz", "golden_flow_emax2.npz", "golden_flow_emax3.npz",
-              "golden_tensor_emax2.npz", "golden_tensor_emax3.npz", "sixj_exact.npz"):
+              "golden_tensor_emax2.npz", "golden_tensor_emax3.npz", "golden_tensor_emax3_O18.npz", "sixj_exact.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 
@@ -219,6 +230,8 @@ if __name__ == "__main__":
         np.savez_compressed(os.path.join(HERE, "golden_tensor_emax2.npz"),
                             **run_reference_tensor(2, ["e2", "e1", "gt"]))
         np.savez_compressed(os.path.join(HERE, "golden_tensor_emax3.npz"), **run_reference_tensor(3, ["e2"]))
+        np.savez_compressed(os.path.join(HERE, "golden_tensor_emax3_O18.npz"),
+                            **run_reference_tensor(3, ["e2", "gt"], ("O18", 18, 8)))
     elif sys.argv[1:] == ["--flow"]:
         for e in (2, 3):
             np.savez_compressed(os.path.join(HERE, "golden_flow_emax%d.npz" % e), **run_reference_flow(e))

@@ -45,8 +45,9 @@ def load_flow_golden(emax):
     return dict(np.load(os.path.join(GOLDEN, "golden_flow_emax%d.npz" % emax)))
 
 
-def load_tensor_golden(emax):
-    return dict(np.load(os.path.join(GOLDEN, "golden_tensor_emax%d.npz" % emax)))
+def load_tensor_golden(emax, nucleus=None):
+    suffix = "" if nucleus is None else "_" + nucleus
+    return dict(np.load(os.path.join(GOLDEN, "golden_tensor_emax%d%s.npz" % (emax, suffix))))
 
 
 def tensor_rel_errors(ms, rank, Z, R):

@@ -120,3 +120,35 @@ def test_tensor_split_vs_fp64_emax5(rank, herm):
         F, S = dF.download(), dS.download()
     errs = tensor_rel_errors(ref_space(5), rank, S, F)
     assert max(errs) < SPLIT_TOL, errs
+
+
+# ------------------------------------------------- O18 (fractional occupations)
+# The reference's terms on O18's space (0d5/2 neutrons at 1/3): the hole /
+# particle branches of the one-body terms and the ladder weights see
+# fractional occupations (golden_tensor_emax3_O18.npz).
+@pytest.mark.parametrize("case", ["e2", "gt"])
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL), ("split", SPLIT_TOL)])
+def test_tensor_o18_vs_reference(case, prec, tol):
+    g = load_tensor_golden(3, "O18")
+    lam, trank, par, herm = (int(x) for x in g[case + "_rank"])
+    rank = (lam, trank, par)
+    ms = ig.ModelSpace(3, "O18", "O18")
+    with ig.DeviceOperator(ms, 1) as dX, ig.DeviceOperator(ms, herm, rank) as dT, \
+            ig.DeviceOperator(ms, 1, rank) as dZ:
+        dX.upload(g["X"])
+        dT.upload(g[case + "_T"])
+        ig.Commutator.device_scalar_tensor(dX, dT, dZ, precision=prec)
+        Z = dZ.download()
+    errs = tensor_rel_errors(ref_space(3), rank, Z, g[case + "_full"])
+    assert max(errs) < tol, (case, prec, errs)
+    if prec == "fp64":
+        hz = -1 if herm == 1 else 1
+        for term in TERMS:
+            with ig.DeviceOperator(ms, 1) as dX, ig.DeviceOperator(ms, herm, rank) as dT, \
+                    ig.DeviceOperator(ms, hz, rank) as dZ:
+                dX.upload(g["X"])
+                dT.upload(g[case + "_T"])
+                ig.Commutator.device_tensor_term(term, dX, dT, dZ)
+                R = g["%s_%s" % (case, term)]
+                errs = tensor_rel_errors(ref_space(3), rank, dZ.download(), R)
+            assert max(errs) < TOL, (case, term, errs)

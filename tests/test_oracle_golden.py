@@ -128,3 +128,12 @@ def test_reference_binary_layout(emax):
         assert np.array_equal(a, g[name])
         assert flags == ((h == 1), (h == -1), (h == 1), (h == -1))
         assert hdr == (0, 0, 0, 2, 4, min(14, 3 * emax), ms.nch, ms.nch, 0, 0, 0)
+
+
+def test_tensor_golden_o18_differs_from_o16():
+    # the same X and T on O16's and O18's spaces: the fractional 0d5/2
+    # occupations change the reference's scalar-tensor commutator
+    from helpers import load_tensor_golden
+    g16, g18 = load_tensor_golden(3), load_tensor_golden(3, "O18")
+    assert np.array_equal(g16["X"], g18["X"]) and np.array_equal(g16["e2_T"], g18["e2_T"])
+    assert np.abs(g16["e2_full"] - g18["e2_full"]).max() > 1e-3
