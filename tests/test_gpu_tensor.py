@@ -106,10 +106,12 @@ def test_tensor_term_split_vs_reference(emax, case, term):
     assert max(errs) < SPLIT_TOL, (term, errs)
 
 
-@pytest.mark.parametrize("rank,herm", [((2, 0, 0), 1), ((1, 1, 0), -1), ((3, 0, 1), 1)])
+@pytest.mark.parametrize("rank,herm", [((2, 0, 0), 1), ((1, 1, 0), -1), ((3, 0, 1), 1), ((0, 1, 0), 1),
+                                       ((4, 0, 0), -1), ((2, 1, 1), 1)])
 def test_tensor_split_vs_fp64_emax5(rank, herm):
     # larger channels than the golden spaces (several 128-row tiles, ragged
-    # edges, K past one pipeline stage): the split form against the FP64 one
+    # edges, K past one pipeline stage): the split form against the FP64 one,
+    # for ranks from lambda = 0 (isovector, |dTz| = 1) to lambda = 4
     ms = ig.ModelSpace(5, "O16", "O16")
     with ig.DeviceOperator(ms, 1) as dX, ig.DeviceOperator(ms, herm, rank) as dT, \
             ig.DeviceOperator(ms, 1, rank) as dF, ig.DeviceOperator(ms, 1, rank) as dS:
