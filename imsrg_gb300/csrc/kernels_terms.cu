@@ -710,7 +710,10 @@ __device__ __forceinline__ int warp_compact64(bool v0, bool v1, unsigned char x0
 // product's rounding error (2^-11)
 __device__ __forceinline__ int small_div(int r, float rcp) { return __float2int_rz(__fmul_rn((float)r + 0.5f, rcp)); }
 
-__global__ void __launch_bounds__(kInvqThreads) k_pandya_inv_ff(DevSpace S, DevWork W, const double* __restrict__ Zb,
+// (four blocks per SM: the shared-memory budget admits four, and the register
+// bound that fits them measured 3% faster than the compiler's own choice;
+// smaller or larger budgets measured slower)
+__global__ void __launch_bounds__(kInvqThreads, 4) k_pandya_inv_ff(DevSpace S, DevWork W, const double* __restrict__ Zb,
                                                              double* __restrict__ Z, int hZ,
                                                              const int4* __restrict__ tasks,
                                                              const int* __restrict__ clist,
