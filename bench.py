@@ -454,7 +454,11 @@ def run_gb300(args):
     # ---- plain FP64 form (the metric compares split vs FP64)
     fp64 = None
     if prec == "split":
+        Zs = dZ.download()  # the split result of the timed region's inputs
         step("fp64")
+        Zf = dZ.download()
+        fp64_err = split_vs_fp64(ms, Zs, Zf)
+        del Zs, Zf
         barrier()
         f0 = torch.cuda.Event(enable_timing=True)
         f1 = torch.cuda.Event(enable_timing=True)
@@ -465,7 +469,8 @@ def run_gb300(args):
         f1.record()
         torch.cuda.synchronize()
         fms = max_ms(f0.elapsed_time(f1)) / nf
-        fp64 = {"value": world * 1000.0 / fms, "unit": UNIT, "ms_per_step": fms, "steps": nf}
+        fp64 = {"value": world * 1000.0 / fms, "unit": UNIT, "ms_per_step": fms, "steps": nf,
+                "split_vs_fp64_rel_err": fp64_err}
     # ---- end to end: host buffers, H2D + commutator + D2H per step, through the C ABI
     A = ms.arena_size
     hX = torch.empty(A, dtype=torch.float64, pin_memory=True)
@@ -524,6 +529,7 @@ def run_gb300(args):
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "working set > L2 every step (X2, Y2 280 MiB each; Zbar 761 MiB)"},
         "plain_fp64": fp64,
+        "split_vs_fp64_rel_err": fp64["split_vs_fp64_rel_err"] if fp64 else None,
         "e2e": e2e,
         "roofline": roof,
         "phases_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in sorted(phases.items())},
@@ -750,6 +756,20 @@ def run_batch(args):
         "split": sp, "plain_fp64": res["fp64"], "gpu_launches": sp["launches_per_step"] * K,
     }
     print(json.dumps(out))
+
+
+def split_vs_fp64(ms, Zs, Zf):
+    """Relative Frobenius difference per body rank (zero-, one-, two-body) of
+    the split and FP64 results of the same commutator."""
+    import numpy as np
+    N = ms.norb
+    o2 = (32 + N * N + 31) // 32 * 32
+    out = {}
+    for name, a, b in (("zero_body", Zs[:1], Zf[:1]), ("one_body", Zs[32:32 + N * N], Zf[32:32 + N * N]),
+                       ("two_body", Zs[o2:], Zf[o2:])):
+        nb = float(np.linalg.norm(b))
+        out[name] = float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a - b))
+    return out
 
 
 TENSOR_METRIC = ("ms per scalar-tensor commutator [X,T], rank (J,dTz,parity)=(2,0,+), emax={emax}: {form} form "
