@@ -622,10 +622,13 @@ class _BCHNamespace:
         return n.value
 
     def BCH_Transform(self, OpIn, Omega, precision=None):
+        """BCH::BCH_Transform(OpIn, Omega): OpIn scalar or a reduced tensor,
+        Omega scalar."""
         ms = OpIn.modelspace
-        out = Operator(ms)
+        rank = getattr(OpIn, "rank", (0, 0, 0))
+        out = Operator(ms, *rank) if rank != (0, 0, 0) else Operator(ms)
         with DeviceOperator.from_host(OpIn) as di, DeviceOperator.from_host(Omega) as dom, \
-                DeviceOperator(ms) as do:
+                DeviceOperator(ms, 1, rank) as do:
             self.last_n_nested = self.device_transform(di, dom, do, precision)
             do.download(out.arena)
             out.hermitian = do.hermiticity
@@ -829,18 +832,19 @@ class IMSRGSolver:
         check(self._L.imsrg_solver_history(self._h, m, _ip(it), *[_dp(c) for c in cols], ctypes.byref(n)))
         return it[:m], cols[0][:m], cols[1][:m], cols[2][:m], cols[3][:m]
 
-    def Transform(self, op):
-        out = Operator(op.modelspace)
-        with DeviceOperator.from_host(op) as di, DeviceOperator(op.modelspace, op.hermitian) as do:
-            check(self._L.imsrg_solver_transform(self._h, di._h, do._h, _precision(self.precision), None))
+    def _transform(self, fn, op):
+        # scalar operators or reduced tensors (observables) alike
+        rank = getattr(op, "rank", (0, 0, 0))
+        out = Operator(op.modelspace, *rank) if rank != (0, 0, 0) else Operator(op.modelspace)
+        with DeviceOperator.from_host(op) as di, DeviceOperator(op.modelspace, op.hermitian, rank) as do:
+            check(fn(self._h, di._h, do._h, _precision(self.precision), None))
             do.download(out.arena)
             out.hermitian = do.hermiticity
         return out
 
+    def Transform(self, op):
+        """IMSRGSolver::Transform: e^Omega op e^-Omega through every Omega."""
+        return self._transform(self._L.imsrg_solver_transform, op)
+
     def InverseTransform(self, op):
-        out = Operator(op.modelspace)
-        with DeviceOperator.from_host(op) as di, DeviceOperator(op.modelspace, op.hermitian) as do:
-            check(self._L.imsrg_solver_inverse_transform(self._h, di._h, do._h, _precision(self.precision), None))
-            do.download(out.arena)
-            out.hermitian = do.hermiticity
-        return out
+        return self._transform(self._L.imsrg_solver_inverse_transform, op)

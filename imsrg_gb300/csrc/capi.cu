@@ -851,7 +851,7 @@ int imsrg_op_axpy(imsrg_op* y, double a, const imsrg_op* x, void* stream)
 int imsrg_op_norm(const imsrg_op* op, double* out, void* stream)
 {
   if (!op || !out) return fail(IMSRG_ERR_ARG, "bad arguments");
-  if (op->tl) return fail(IMSRG_ERR_UNSUPPORTED, "norm of a tensor operator is not on the GPU path");
+  if (op->tl) return tensor_norm_dev(op, out, S_(stream));
   return norm_impl(op, out, S_(stream));
 }
 
@@ -1018,9 +1018,13 @@ int imsrg_bch_transform(const imsrg_op* OpIn, const imsrg_op* Omega, imsrg_op* O
 {
   if (!OpIn || !Omega || !OpOut) return fail(IMSRG_ERR_ARG, "null operator");
   if (OpIn->sp != Omega->sp || OpIn->sp != OpOut->sp) return fail(IMSRG_ERR_ARG, "different model spaces");
-  if (OpIn->tl || Omega->tl || OpOut->tl) return fail(IMSRG_ERR_UNSUPPORTED, "BCH_Transform of tensor operators is not on the GPU path");
+  if (Omega->tl) return fail(IMSRG_ERR_UNSUPPORTED, "Omega must be a scalar operator");
+  if (OpOut->tl != OpIn->tl) return fail(IMSRG_ERR_ARG, "OpIn and OpOut must have the same rank");
   if (OpOut == Omega) return fail(IMSRG_ERR_ARG, "OpOut must not alias Omega");
+  if ((Omega->herm != 1 && Omega->herm != -1) || (OpIn->herm != 1 && OpIn->herm != -1))
+    return fail(IMSRG_ERR_UNSUPPORTED, "operators must be hermitian or anti-hermitian");
   cudaStream_t st = S_(stream);
+  if (OpIn->tl) return tensor_bch_transform(OpIn, Omega, OpOut, threshold, precision, n_nested, st);
   imsrg_space* sp = OpIn->sp;
   if (n_nested) *n_nested = 0;
   int rc;

@@ -479,7 +479,7 @@ int imsrg_solver_transform(const imsrg_solver* sv, const imsrg_op* OpIn, imsrg_o
 {
   if (!sv || !OpIn || !OpOut) return err(IMSRG_ERR_ARG, "bad arguments");
   if (OpIn->sp != sv->sp || OpOut->sp != sv->sp) return err(IMSRG_ERR_ARG, "operator from another model space");
-  if (OpIn->tl || OpOut->tl) return err(IMSRG_ERR_UNSUPPORTED, "transforms of tensor operators are not on the GPU path");
+  if (OpIn->tl != OpOut->tl) return err(IMSRG_ERR_ARG, "OpIn and OpOut must have the same rank");
   cudaStream_t st = S_(stream);
   // IMSRGSolver::Transform_Partial(OpIn, 0), src/IMSRGSolver.cc:957-1002:
   // the Omegas written to scratch files first, then those in device memory
@@ -506,7 +506,7 @@ int imsrg_solver_inverse_transform(const imsrg_solver* sv, const imsrg_op* OpIn,
 {
   if (!sv || !OpIn || !OpOut) return err(IMSRG_ERR_ARG, "bad arguments");
   if (OpIn->sp != sv->sp || OpOut->sp != sv->sp) return err(IMSRG_ERR_ARG, "operator from another model space");
-  if (OpIn->tl || OpOut->tl) return err(IMSRG_ERR_UNSUPPORTED, "transforms of tensor operators are not on the GPU path");
+  if (OpIn->tl != OpOut->tl) return err(IMSRG_ERR_ARG, "OpIn and OpOut must have the same rank");
   cudaStream_t st = S_(stream);
   // IMSRGSolver::InverseTransform, src/IMSRGSolver.cc:939-952: Omegas in
   // reverse order, each negated

@@ -29,6 +29,11 @@ int set_error(int code, const char* msg);
 int commutator_dev(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStream_t st);
 int norm_dev(const imsrg_op* op, double* out, cudaStream_t st);
 int status_dev(imsrg_space* sp, cudaStream_t st);
+// tensor operators (capi_tensor.cu): Operator::Norm, and BCH_Transform by a
+// scalar Omega
+int tensor_norm_dev(const imsrg_op* op, double* out, cudaStream_t st);
+int tensor_bch_transform(const imsrg_op* OpIn, const imsrg_op* Omega, imsrg_op* OpOut, double threshold,
+                         int precision, int* n_nested, cudaStream_t st);
 // the split-form commutator of a group of same-structure pairs, one launch
 // per kernel for the whole group: usable only with every term switched on
 bool batch_phases_usable();

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <exception>
 #include <mutex>
 #include <string>
@@ -218,6 +219,15 @@ int tph_split(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st
   return IMSRG_OK;
 }
 
+// BCH_Transform's work arenas of a rank
+int bch_scratch(imsrg_space* sp, TensorLayout* tl)
+{
+  std::lock_guard<std::mutex> g(sp->mu);
+  int rc;
+  if ((rc = alloc(tl, tl->d_bch_nested, tl->total)) || (rc = alloc(tl, tl->d_bch_next, tl->total))) return rc;
+  return IMSRG_OK;
+}
+
 int check_prec(int precision)
 {
   if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_SPLIT) return terr(IMSRG_ERR_ARG, "bad precision");
@@ -342,3 +352,63 @@ int imsrg_commutator_scalar_tensor(const imsrg_op* X, const imsrg_op* Y, imsrg_o
 }
 
 }  // extern "C"
+
+namespace imsrg {
+
+// Operator::Norm of a tensor operator (src/Operator.cc:1610-1646 with
+// TwoBodyME::Norm, src/TwoBodyME.cc:703-725)
+int tensor_norm_dev(const imsrg_op* op, double* out, cudaStream_t st)
+{
+  TensorLayout* tl = op->tl;
+  const size_t n2 = tl->nrm2_off.size();
+  T_CUDA(launch_tensor_norm(*tl, op->d, tl->d_nrm_partial, st));
+  T_CUDA(cudaMemcpyAsync(tl->h_nrm_partial.data(), tl->d_nrm_partial, (n2 + 1) * sizeof(double),
+                         cudaMemcpyDeviceToHost, st));
+  T_CUDA(cudaStreamSynchronize(st));
+  double s2 = 0.0;
+  for (size_t c = 0; c < n2; ++c) s2 += tl->h_nrm_partial[c];
+  *out = std::sqrt(tl->h_nrm_partial[n2] + s2);
+  return IMSRG_OK;
+}
+
+// BCH::Standard_BCH_Transform (src/BCH.cc:87-201) of a tensor operator by a
+// scalar Omega: the same series and stopping rule as the scalar form, with
+// the nested commutators [Omega, .] from CommutatorScalarTensor
+int tensor_bch_transform(const imsrg_op* OpIn, const imsrg_op* Omega, imsrg_op* OpOut, double threshold,
+                         int precision, int* n_nested, cudaStream_t st)
+{
+  TensorLayout* tl = OpIn->tl;
+  imsrg_space* sp = OpIn->sp;
+  if (n_nested) *n_nested = 0;
+  int rc;
+  double nx = 0, ny = 0;
+  if ((rc = tensor_norm_dev(OpIn, &nx, st)) || (rc = norm_dev(Omega, &ny, st))) return rc;
+  if ((rc = imsrg_op_copy(OpOut, OpIn, st))) return rc;
+  if (!(nx > threshold)) return IMSRG_OK;
+  if ((rc = bch_scratch(sp, tl))) return rc;
+  imsrg_op nested, next;
+  nested.sp = next.sp = sp;
+  nested.tl = next.tl = tl;
+  nested.len = next.len = tl->total;
+  nested.d = tl->d_bch_nested;
+  next.d = tl->d_bch_next;
+  T_CUDA(cudaMemcpyAsync(nested.d, OpOut->d, tl->total * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  nested.herm = OpOut->herm;
+  double epsilon = nx * std::exp(-2 * ny) * threshold / (2 * ny);
+  double fden = 1.0;
+  for (int i = 1; i <= 40; ++i) {
+    if ((rc = imsrg_commutator_scalar_tensor(Omega, &nested, &next, precision, st))) return rc;
+    std::swap(nested.d, next.d);
+    std::swap(nested.herm, next.herm);
+    fden /= i;
+    T_CUDA(launch_axpy(OpOut->d, nested.d, fden, tl->total, st));
+    if (n_nested) *n_nested = i;
+    epsilon *= i + 1;
+    double nn = 0;
+    if ((rc = tensor_norm_dev(&nested, &nn, st))) return rc;
+    if (nn < epsilon) break;
+  }
+  return IMSRG_OK;
+}
+
+}  // namespace imsrg

@@ -101,6 +101,9 @@ cudaError_t launch_tensor_222_221(const Space& s, const TensorLayout& t, const d
 // Ybar, Zbar: scratch of t's yb_total and zb_total doubles
 cudaError_t launch_tensor_ph(const Space& s, const TensorLayout& t, const double* Xbar, const double* Y, int hX,
                              int hY, double* Ybar, double* Zbar, double* Z, int hZ, cudaStream_t st);
+// Operator::Norm of a tensor of layout t: partial[0 .. nrm2_off.size()] are
+// the two-body chunks' weighted sums of squares, then the one-body one
+cudaError_t launch_tensor_norm(const TensorLayout& t, const double* A, double* partial, cudaStream_t st);
 // split form: the operands the split products read (Y with its blocks
 // transposed, the tensor Pandya panels transposed and half-swapped, X bar
 // half-swapped); the ladder's remainder (Mhh, Z2 += D, the one-body part) once

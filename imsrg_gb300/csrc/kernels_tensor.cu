@@ -1029,4 +1029,42 @@ cudaError_t launch_tensor_inverse_pandya(const Space& s, const TensorLayout& t, 
   return launch_tinv_q(s, t, Zbar, Z, hZ, st);
 }
 
+// Operator::Norm of a tensor operator: blocks 0 .. n2-1 sum their chunk's
+// squares times its weight; block n2 sums the weighted one-body squares
+__global__ void k_tnorm(const double* __restrict__ A, const long long* __restrict__ off,
+                        const int* __restrict__ len, const double* __restrict__ w2, int n2,
+                        const int* __restrict__ idx1, const double* __restrict__ w1, int n1,
+                        double* __restrict__ partial)
+{
+  __shared__ double red[32];
+  const int c = blockIdx.x;
+  double s = 0.0;
+  if (c < n2) {
+    const double* p = A + off[c];
+    for (int t = threadIdx.x; t < len[c]; t += blockDim.x) s = fma(p[t], p[t], s);
+  } else {
+    for (int t = threadIdx.x; t < n1; t += blockDim.x) {
+      const double v = A[idx1[t]];
+      s = fma(v * v, w1[t], s);
+    }
+  }
+  s = wsum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    v = wsum(v);
+    if (threadIdx.x == 0) partial[c] = c < n2 ? v * w2[c] : v;
+  }
+}
+
+cudaError_t launch_tensor_norm(const TensorLayout& t, const double* A, double* partial, cudaStream_t st)
+{
+  const int n2 = (int)t.nrm2_off.size();
+  k_tnorm<<<n2 + 1, 256, 0, st>>>(A, t.d_nrm2_off, t.d_nrm2_len, t.d_nrm2_w, n2, t.d_nrm1_idx, t.d_nrm1_w,
+                                  (int)t.nrm1_idx.size(), partial);
+  count_launch();
+  return cudaGetLastError();
+}
+
 }  // namespace imsrg

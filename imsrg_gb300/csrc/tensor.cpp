@@ -233,6 +233,34 @@ TensorLayout* tensor_layout(Space& s, int lam, int trank, int parity)
     t->max_tob = std::max(t->max_tob, t->tob_off[i + 1] - t->tob_off[i]);
     t->max_ob = std::max(t->max_ob, s.ob_count[i]);
   }
+  // norm weights (the reference's integer arithmetic, including its mix of
+  // doubled j and integer rank_J in the one-body degeneracy)
+  t->nrm1_idx.clear();
+  t->nrm1_w.clear();
+  for (int p = 0; p < N; ++p)
+    for (int q = 0; q < N; ++q) {
+      if (!t->ob_ok[(size_t)q * N + p]) continue;
+      const int jp = s.j2[p], jq = s.j2[q];
+      const int dfac = (jp + 1) * ((std::min(jq, jp + lam) - std::max(-jq, jp - lam)) / 2 + 1);
+      if (dfac == 0) continue;
+      t->nrm1_idx.push_back(32 + q * N + p);  // OneBody(p, q), column-major
+      t->nrm1_w.push_back((double)dfac);
+    }
+  t->nrm2_off.clear();
+  t->nrm2_len.clear();
+  t->nrm2_w.clear();
+  for (size_t b = 0; b < t->bra.size(); ++b) {
+    const int Jb = s.ch[t->bra[b]].J, Jk = s.ch[t->ket[b]].J;
+    const long long nn = (long long)s.ch[t->bra[b]].n() * s.ch[t->ket[b]].n();
+    const double deg = (double)((2 * Jk + 1) * (std::min(Jb, Jk + lam) - std::max(-Jb, Jk - lam) + 1));
+    const double w = deg * deg * (t->bra[b] == t->ket[b] ? 1.0 : 2.0);
+    for (long long o = 0; o < nn; o += 65536) {
+      t->nrm2_off.push_back(t->off[b] + o);
+      t->nrm2_len.push_back((int)std::min<long long>(65536, nn - o));
+      t->nrm2_w.push_back(w);
+    }
+  }
+  t->h_nrm_partial.assign(t->nrm2_off.size() + 1, 0.0);
   // angular tables, half-integers widened by lam (the 9j sums reach j + lam)
   t->NJ = s.NJ;
   t->d1x = s.d1 + lam;
@@ -381,6 +409,12 @@ void tensor_upload(TensorLayout& t)
   d.nj_hat = dev_copy(t, t.nj_hat);
   d.d1 = t.nj_d1;
   d.hat2 = dev_copy(t, t.hat2);
+  t.d_nrm1_idx = dev_copy(t, t.nrm1_idx);
+  t.d_nrm1_w = dev_copy(t, t.nrm1_w);
+  t.d_nrm2_off = dev_copy(t, t.nrm2_off);
+  t.d_nrm2_len = dev_copy(t, t.nrm2_len);
+  t.d_nrm2_w = dev_copy(t, t.nrm2_w);
+  t.d_nrm_partial = dev_copy(t, t.h_nrm_partial);
   d.tob_off = dev_copy(t, t.tob_off);
   d.tob_list = dev_copy(t, t.tob_list);
   t.d_tq = dev_copy(t, t.tq);

@@ -91,6 +91,23 @@ struct TensorLayout {
   std::vector<int> lad_koff, lad_woff, lad_n;
   std::vector<int> tob_off, tob_list;
   int max_ob = 0, max_tob = 0;  // longest one-body partner list (scalar, tensor) of an orbit
+  // Operator::Norm of a tensor (src/Operator.cc:1610-1646, src/TwoBodyME.cc:
+  // 703-725): the one-body elements with their degeneracy weights, and every
+  // stored block in chunks with its weight (degeneracy^2, doubled when the
+  // bra and ket channels differ)
+  std::vector<int> nrm1_idx;
+  std::vector<double> nrm1_w;
+  std::vector<long long> nrm2_off;
+  std::vector<int> nrm2_len;
+  std::vector<double> nrm2_w;
+  int* d_nrm1_idx = nullptr;
+  double* d_nrm1_w = nullptr;
+  long long* d_nrm2_off = nullptr;
+  int* d_nrm2_len = nullptr;
+  double *d_nrm2_w = nullptr, *d_nrm_partial = nullptr;
+  std::vector<double> h_nrm_partial;
+  // BCH_Transform's work operators of this rank (layout total each)
+  double *d_bch_nested = nullptr, *d_bch_next = nullptr;
   long long lad_maxelems = 0;  // largest n_channel x gather length (grid sizing)
   int64_t zb_total = 0, yb_total = 0;
   int zb_maxelems = 0, yb_maxelems = 0;  // largest block of each list (grid sizing)

@@ -188,8 +188,10 @@ int imsrg_op_axpy(imsrg_op* y, double a, const imsrg_op* x, void* stream);
 int imsrg_op_write_binary(const imsrg_op* op, const char* path, void* stream);
 int imsrg_op_read_binary(imsrg_op* op, const char* path, void* stream);
 
-/* Operator::Norm of a scalar operator (src/Operator.cc:1610-1651,
- * src/TwoBodyME.cc:703-723); synchronises the stream. */
+/* Operator::Norm (src/Operator.cc:1610-1651, src/TwoBodyME.cc:703-723) of a
+ * scalar or tensor operator (a tensor's one-body elements weighted by the
+ * reference's degeneracy factor, its blocks by (2Jket+1)(..)^2 and twice when
+ * the bra and ket channels differ); synchronises the stream. */
 int imsrg_op_norm(const imsrg_op* op, double* out, void* stream);
 
 /* Seeded random operator: uniform[-1,1] on symmetry-allowed entries,
@@ -313,9 +315,11 @@ int imsrg_get_default_precision(int* precision);
 /* BCH::Standard_BCH_Transform (src/BCH.cc:87-201): OpOut = e^Omega OpIn e^-Omega
  * by nested commutators, stopping as the reference does (threshold:
  * BCH::bch_transform_threshold, default 1e-9, src/BCH.cc:8-69; at most 40
- * nested commutators).  n_nested (may be NULL) receives the number of nested
- * commutators evaluated.  Synchronises the stream once per nested commutator
- * for the convergence test. */
+ * nested commutators).  Omega is scalar; OpIn and OpOut are scalar or tensor
+ * operators of one rank (a tensor's nested commutators are
+ * CommutatorScalarTensor).  n_nested (may be NULL) receives the number of
+ * nested commutators evaluated.  Synchronises the stream once per nested
+ * commutator for the convergence test. */
 int imsrg_bch_transform(const imsrg_op* OpIn, const imsrg_op* Omega, imsrg_op* OpOut, double threshold,
                         int precision, int* n_nested, void* stream);
 
@@ -397,7 +401,8 @@ int imsrg_solver_history(const imsrg_solver* solver, int cap, int* istep, double
 /* IMSRGSolver::Transform (src/IMSRGSolver.cc:928-1002): OpOut = e^Omega OpIn
  * e^-Omega through every Omega in order (scratch files first); InverseTransform
  * (:939-952) undoes the Omegas held in device memory (as the reference, it
- * does not read scratch files).  OpOut may alias OpIn. */
+ * does not read scratch files).  OpIn and OpOut are scalar or tensor
+ * operators of one rank (observables); OpOut may alias OpIn. */
 int imsrg_solver_transform(const imsrg_solver* solver, const imsrg_op* OpIn, imsrg_op* OpOut, int precision,
                            void* stream);
 int imsrg_solver_inverse_transform(const imsrg_solver* solver, const imsrg_op* OpIn, imsrg_op* OpOut, int precision,

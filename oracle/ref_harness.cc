@@ -241,6 +241,16 @@ static int tensor_main(int argc, char** argv) {
   }
   Operator Zf = Commutator::CommutatorScalarTensor(X, T);
   write_file(outdir + "/st_full.bin", store_tensor(Zf, N));
+  // BCH_Transform of the tensor by Omega = 0.2 X / |X|, and the norms
+  {
+    Operator Omega = X * (0.2 / X.Norm());
+    write_file(outdir + "/st_omega.bin", store(Omega, L));
+    Operator B = BCH::BCH_Transform(T, Omega);
+    write_file(outdir + "/st_bch.bin", store_tensor(B, N));
+    std::ofstream nf(outdir + "/st_norms.txt");
+    nf << std::setprecision(17) << T.Norm() << " " << Zf.Norm() << " " << B.Norm() << " " << T.OneBodyNorm() << " "
+       << T.TwoBodyNorm() << "\n";
+  }
   return 0;
 }
 

@@ -37,6 +37,10 @@ Fixtures (arena layout: see oracle/modelspace_ref.py):
                      random_tensor) of rank (J, T, parity) = (2, 0, 0)
                      hermitian, (1, 0, 1) hermitian and (1, 1, 0)
                      anti-hermitian at emax 2; the first case only at emax 3.
+                     Per case also BCH::BCH_Transform(T, Omega) for the
+                     scalar Omega = 0.2 X / |X| (with Omega itself), and the
+                     Operator::Norm of T, of [X, T] and of the transform, with
+                     T's one- and two-body norms.
   golden_tensor_emax3_O18.npz
                      the same on O18's space (fractional 0d5/2 neutron
                      occupations) for the ranks (2, 0, 0) hermitian and
@@ -154,6 +158,9 @@ def run_reference_tensor(emax, cases, nucleus=None):
             out[name + "_rank"] = np.array([lam, trank, par, herm])
             for t in TENSOR_TERMS:
                 out["%s_%s" % (name, t)] = np.fromfile(os.path.join(td, "st_%s.bin" % t))
+            out[name + "_omega"] = np.fromfile(os.path.join(td, "st_omega.bin"))
+            out[name + "_bch"] = np.fromfile(os.path.join(td, "st_bch.bin"))
+            out[name + "_norms"] = np.loadtxt(os.path.join(td, "st_norms.txt"))
             out[name + "_blocks"] = np.loadtxt(os.path.join(td, "tensor_blocks.txt"), dtype=np.int64).reshape(-1, 4)
     return out
 

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import imsrg_gb300 as ig
-from helpers import load_tensor_golden, ref_space, tensor_rel_errors
+from helpers import load_flow_golden, load_tensor_golden, ref_space, tensor_rel_errors
 
 pytestmark = pytest.mark.gpu
 
@@ -72,8 +72,8 @@ def test_tensor_rejected_by_scalar_paths():
             ig.DeviceOperator(ms, -1) as dZ:
         with pytest.raises(ig.IMSRGError):
             ig.Commutator.device_commutator(dX, dT, dZ)
-        with pytest.raises(ig.IMSRGError):
-            dT.norm()
+        with pytest.raises(ig.IMSRGError):  # Omega must be scalar
+            ig.BCH.device_transform(dX, dT, dZ)
 
 
 # ------------------------------------------------------------- split form
@@ -154,3 +154,60 @@ def test_tensor_o18_vs_reference(case, prec, tol):
                 R = g["%s_%s" % (case, term)]
                 errs = tensor_rel_errors(ref_space(3), rank, dZ.download(), R)
             assert max(errs) < TOL, (case, term, errs)
+
+
+# ------------------------------------------ norms, BCH_Transform, Transform
+# Operator::Norm of a tensor, BCH::BCH_Transform of a tensor by a scalar
+# Omega (the reference's own: Omega = 0.2 X / |X| and its transform of T are
+# in the golden files), and IMSRGSolver::Transform of an observable.
+@pytest.mark.parametrize("emax,case", CASES)
+def test_tensor_norm_vs_reference(emax, case):
+    g, ms, dX, dT, rank, herm = setup(emax, case)
+    nT, nZ, nB, n1, n2 = g[case + "_norms"]
+    assert abs(dT.norm() - nT) <= 1e-13 * nT
+    with ig.DeviceOperator(ms, 1, rank) as dZ:
+        ig.Commutator.device_scalar_tensor(dX, dT, dZ, precision="fp64")
+        assert abs(dZ.norm() - nZ) <= 1e-12 * nZ
+
+
+@pytest.mark.parametrize("emax,case", CASES)
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL), ("split", SPLIT_TOL)])
+def test_tensor_bch_transform_vs_reference(emax, case, prec, tol):
+    g, ms, dX, dT, rank, herm = setup(emax, case)
+    with ig.DeviceOperator(ms, 1) as dOm, ig.DeviceOperator(ms, herm, rank) as dB:
+        dOm.upload(g[case + "_omega"])
+        n = ig.BCH.device_transform(dT, dOm, dB, prec)
+        assert n >= 3
+        B = dB.download()
+        assert abs(dB.norm() - g[case + "_norms"][2]) <= 10 * tol * g[case + "_norms"][2]
+    errs = tensor_rel_errors(ref_space(emax), rank, B, g[case + "_bch"])
+    assert max(errs) < tol, (case, prec, errs)
+    # host API: BCH.BCH_Transform keeps the tensor's rank
+    T = ig.Operator(ms, *rank, arena=g[case + "_T"], hermitian=herm == 1)
+    Om = ig.Operator(ms, arena=g[case + "_omega"])
+    Bh = ig.BCH.BCH_Transform(T, Om, prec)
+    assert Bh.rank == rank
+    assert max(tensor_rel_errors(ref_space(emax), rank, Bh.arena, g[case + "_bch"])) < tol
+
+
+def test_solver_transform_of_a_tensor_observable():
+    # Transform(T) after a flow with several Omegas is the chain of
+    # BCH_Transforms through them, and InverseTransform undoes it
+    gf = load_flow_golden(3)
+    g = load_tensor_golden(3)
+    ms = ig.ModelSpace(3, "O16", "O16")
+    rank = (2, 0, 0)
+    H = ig.Operator(ms, arena=gf["H"])
+    solver = ig.IMSRGSolver(H, precision="fp64")
+    solver.SetOmegaNormMax(0.3)
+    solver.SetSmax(2.0)
+    solver.Solve()
+    assert solver.GetOmegaSize() > 1
+    T = ig.Operator(ms, *rank, arena=g["e2_T"], hermitian=True)
+    Tt = solver.Transform(T)
+    ref = T
+    for i in range(solver.GetOmegaSize()):
+        ref = ig.BCH.BCH_Transform(ref, solver.GetOmega(i), "fp64")
+    assert max(tensor_rel_errors(ref_space(3), rank, Tt.arena, ref.arena)) < 1e-12
+    back = solver.InverseTransform(Tt)
+    assert max(tensor_rel_errors(ref_space(3), rank, back.arena, T.arena)) < 1e-8
