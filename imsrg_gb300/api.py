@@ -247,7 +247,7 @@ class Operator:
 
     def ReadBinary(self, path):
         """Operator::ReadBinary from a file path (hermiticity from the file)."""
-        with DeviceOperator(self.modelspace, self.hermitian) as d:
+        with DeviceOperator(self.modelspace, self.hermitian, getattr(self, "rank", (0, 0, 0))) as d:
             d.read_binary(path)
             d.download(self.arena)
             self.hermitian = d.hermiticity

@@ -1,5 +1,6 @@
 // extern "C" boundary, operator files (include/imsrg_gb300.h): a device
-// operator written to / read from the reference's binary Operator layout
+// operator (scalar or reduced tensor) written to / read from the reference's
+// binary Operator layout
 // (Operator::WriteBinary / ReadBinary, src/Operator.cc:341-388, with
 // TwoBodyME::WriteBinary / ReadBinary, src/TwoBodyME.cc:812-836), so files
 // interchange with IMSRG++.  The arena streams through two pinned staging
@@ -15,6 +16,7 @@
 
 #include "../../include/imsrg_gb300.h"
 #include "capi_internal.hpp"
+#include "tensor.hpp"
 
 using namespace imsrg;
 
@@ -30,11 +32,19 @@ struct Piece {
   int64_t off, len;
 };
 
-std::vector<Piece> pieces(const Space& s)
+std::vector<Piece> pieces(const Space& s, const TensorLayout* t)
 {
   std::vector<Piece> v;
   v.push_back({0, 1});
   v.push_back({32, (int64_t)s.norb * s.norb});
+  if (t) {
+    // a tensor's blocks in TwoBodyME::MatEl order (the layout's order)
+    for (size_t b = 0; b < t->bra.size(); ++b) {
+      int64_t n = (int64_t)s.ch[t->bra[b]].n() * s.ch[t->ket[b]].n();
+      if (n) v.push_back({t->off[b], n});
+    }
+    return v;
+  }
   for (int c = 0; c < s.nch; ++c) {
     int64_t n = s.ch[c].n();
     if (n) v.push_back({s.ch[c].off, n * n});
@@ -100,9 +110,10 @@ extern "C" {
 int imsrg_op_write_binary(const imsrg_op* op, const char* path, void* stream)
 {
   if (!op || !path) return ioerr(IMSRG_ERR_ARG, "bad arguments");
-  if (op->tl) return ioerr(IMSRG_ERR_UNSUPPORTED, "tensor operator files are not on the GPU path");
   if (op->herm != 1 && op->herm != -1) return ioerr(IMSRG_ERR_UNSUPPORTED, "hermiticity must be +1 or -1");
   const Space& s = *op->sp->s;
+  const TensorLayout* t = op->tl;
+  const int rJ = t ? t->lam : 0, rT = t ? t->trank : 0, par = t ? t->parity : 0;
   cudaStream_t st = (cudaStream_t)stream;
   Staging stg;
   int rc = stg.init();
@@ -110,11 +121,11 @@ int imsrg_op_write_binary(const imsrg_op* op, const char* path, void* stream)
   File fh;
   fh.f = std::fopen(path, "wb");
   if (!fh.f) return ioerr(IMSRG_ERR_IO, std::string("cannot open ") + path + " for writing");
-  OpHeader oh{0, 0, 0, 2, 4, 2 * s.emax, std::min(14, 3 * s.emax), (uint8_t)(op->herm == 1),
+  OpHeader oh{rJ, rT, par, 2, 4, 2 * s.emax, std::min(14, 3 * s.emax), (uint8_t)(op->herm == 1),
               (uint8_t)(op->herm == -1), s.nch};
-  TbHeader th{(uint64_t)s.nch, oh.hermitian, oh.antihermitian, 0, 0, 0};
+  TbHeader th{(uint64_t)s.nch, oh.hermitian, oh.antihermitian, rJ, rT, par};
   if (std::fwrite(&oh, sizeof(oh), 1, fh.f) != 1) return ioerr(IMSRG_ERR_IO, "write failed");
-  std::vector<Piece> pcs = pieces(s);
+  std::vector<Piece> pcs = pieces(s, t);
   // chunks of the arena [lo, hi) stream through the two staging buffers; the
   // pieces are in increasing arena order, so each chunk writes the parts of
   // the pieces it covers, in order
@@ -161,16 +172,17 @@ int imsrg_op_write_binary(const imsrg_op* op, const char* path, void* stream)
 int imsrg_op_read_binary(imsrg_op* op, const char* path, void* stream)
 {
   if (!op || !path) return ioerr(IMSRG_ERR_ARG, "bad arguments");
-  if (op->tl) return ioerr(IMSRG_ERR_UNSUPPORTED, "tensor operator files are not on the GPU path");
   const Space& s = *op->sp->s;
+  const TensorLayout* t = op->tl;
+  const int rJ = t ? t->lam : 0, rT = t ? t->trank : 0, par = t ? t->parity : 0;
   cudaStream_t st = (cudaStream_t)stream;
   File fh;
   fh.f = std::fopen(path, "rb");
   if (!fh.f) return ioerr(IMSRG_ERR_IO, std::string("cannot open ") + path);
   OpHeader oh;
   if (std::fread(&oh, sizeof(oh), 1, fh.f) != 1) return ioerr(IMSRG_ERR_IO, "file too short");
-  if (oh.rank_J != 0 || oh.rank_T != 0 || oh.parity != 0)
-    return ioerr(IMSRG_ERR_UNSUPPORTED, "not a scalar operator (J, T or parity rank set)");
+  if (oh.rank_J != rJ || oh.rank_T != rT || oh.parity != par)
+    return ioerr(IMSRG_ERR_ARG, "the file's rank (J, T, parity) is not the operator's");
   if (oh.legs != 4 || oh.particle_rank != 2)
     return ioerr(IMSRG_ERR_UNSUPPORTED, "only two-body operators (legs = 4) are on the GPU path");
   if (oh.nChannels != s.nch) return ioerr(IMSRG_ERR_ARG, "file is for a model space with another channel count");
@@ -179,9 +191,9 @@ int imsrg_op_read_binary(imsrg_op* op, const char* path, void* stream)
   Staging stg;
   int rc = stg.init();
   if (rc) return rc;
-  if (cudaMemsetAsync(op->d, 0, s.arena * sizeof(double), st) != cudaSuccess)
+  if (cudaMemsetAsync(op->d, 0, op->len * sizeof(double), st) != cudaSuccess)
     return ioerr(IMSRG_ERR_CUDA, "arena memset failed");
-  std::vector<Piece> pcs = pieces(s);
+  std::vector<Piece> pcs = pieces(s, t);
   // file pieces fill a staging buffer; a full buffer goes to the device as one
   // copy per piece, and the other buffer fills meanwhile
   struct Pending {
@@ -211,7 +223,7 @@ int imsrg_op_read_binary(imsrg_op* op, const char* path, void* stream)
     if (ip == 2) {
       TbHeader th;
       if (std::fread(&th, sizeof(th), 1, fh.f) != 1) return ioerr(IMSRG_ERR_IO, "file too short");
-      if (th.nChannels != (uint64_t)s.nch || th.rank_J || th.rank_T || th.parity)
+      if (th.nChannels != (uint64_t)s.nch || th.rank_J != rJ || th.rank_T != rT || th.parity != par)
         return ioerr(IMSRG_ERR_ARG, "two-body header does not match the model space");
     }
     int64_t got = 0;

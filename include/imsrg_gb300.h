@@ -181,9 +181,10 @@ int imsrg_op_axpy(imsrg_op* y, double a, const imsrg_op* x, void* stream);
  * (Operator header, ZeroBody, OneBody, TwoBodyME header, every channel block
  * column-major in channel order), so files interchange with IMSRG++.  The
  * E2max field is written as 2 emax (the reference writes an uninitialised
- * value there) and ignored on reading.  Reading checks the header against the
- * space (scalar, two-body, channel count, exact length) and sets the
- * operator's hermiticity from the file.  Both stream the arena through pinned
+ * value there) and ignored on reading.  Tensor operators write their rank in
+ * both headers and their blocks in TwoBodyME::MatEl order.  Reading checks the
+ * header against the operator (rank (J, T, parity), two-body, channel count,
+ * exact length) and sets the operator's hermiticity from the file.  Both stream the arena through pinned
  * staging buffers on stream and return when the file is complete. */
 int imsrg_op_write_binary(const imsrg_op* op, const char* path, void* stream);
 int imsrg_op_read_binary(imsrg_op* op, const char* path, void* stream);

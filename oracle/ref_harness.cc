@@ -251,6 +251,11 @@ static int tensor_main(int argc, char** argv) {
     nf << std::setprecision(17) << T.Norm() << " " << Zf.Norm() << " " << B.Norm() << " " << T.OneBodyNorm() << " "
        << T.TwoBodyNorm() << "\n";
   }
+  {
+    // Operator::WriteBinary of the tensor
+    std::ofstream ot(outdir + "/st_T_op.bin", std::ios::binary);
+    T.WriteBinary(ot);
+  }
   return 0;
 }
 

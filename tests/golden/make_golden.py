@@ -40,7 +40,7 @@ Fixtures (arena layout: see oracle/modelspace_ref.py):
                      Per case also BCH::BCH_Transform(T, Omega) for the
                      scalar Omega = 0.2 X / |X| (with Omega itself), and the
                      Operator::Norm of T, of [X, T] and of the transform, with
-                     T's one- and two-body norms.
+                     T's one- and two-body norms, and Operator::WriteBinary of T.
   golden_tensor_emax3_O18.npz
                      the same on O18's space (fractional 0d5/2 neutron
                      occupations) for the ranks (2, 0, 0) hermitian and
@@ -161,6 +161,7 @@ def run_reference_tensor(emax, cases, nucleus=None):
             out[name + "_omega"] = np.fromfile(os.path.join(td, "st_omega.bin"))
             out[name + "_bch"] = np.fromfile(os.path.join(td, "st_bch.bin"))
             out[name + "_norms"] = np.loadtxt(os.path.join(td, "st_norms.txt"))
+            out[name + "_binary"] = np.fromfile(os.path.join(td, "st_T_op.bin"), dtype=np.uint8)
             out[name + "_blocks"] = np.loadtxt(os.path.join(td, "tensor_blocks.txt"), dtype=np.int64).reshape(-1, 4)
     return out
 

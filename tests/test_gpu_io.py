@@ -107,3 +107,31 @@ def test_solver_scratch_omegas(tmp_path):
     assert max(rel_errors(r, T.arena, Hd.arena)) < 1e-12
     disk.close()
     assert os.listdir(tmp_path) == []
+
+
+# Tensor operators: the reference's Operator::WriteBinary of T (golden_tensor_*)
+@pytest.mark.parametrize("emax,case", [(2, "e2"), (2, "e1"), (2, "gt"), (3, "e2")])
+def test_tensor_files_interchange(tmp_path, emax, case):
+    from helpers import load_tensor_golden
+    g = load_tensor_golden(emax)
+    lam, trank, par, herm = (int(x) for x in g[case + "_rank"])
+    ms = ig.ModelSpace(emax, "O16", "O16")
+    ref = g[case + "_binary"]
+    f = tmp_path / "t.bin"
+    ref.tofile(f)
+    with ig.DeviceOperator(ms, 1, (lam, trank, par)) as d:
+        d.upload(np.full(d.size, 7.0))  # padding must come back zero
+        d.read_binary(str(f))
+        assert d.hermiticity == herm
+        assert np.array_equal(d.download(), g[case + "_T"])
+        out = tmp_path / "mine.bin"
+        d.write_binary(str(out))
+    mine = np.fromfile(out, dtype=np.uint8)
+    assert mine.size == ref.size
+    keep = np.ones(ref.size, bool)
+    keep[E2MAX] = False
+    assert np.array_equal(mine[keep], ref[keep])
+    # a file of another rank is refused
+    with ig.DeviceOperator(ms, 1, (lam + 1, trank, par)) as d2:
+        with pytest.raises(ig.IMSRGError):
+            d2.read_binary(str(f))
