@@ -756,6 +756,16 @@ class IMSRGSolver:
     def SetHunterGatherer(self, b=True):
         self._set("hunter_gatherer", 1 if b else 0)
 
+    _METHODS = {"magnus_euler": 0, "magnus": 0, "magnus_modified_euler": 1, "magnus_backoff": 2}
+
+    def SetMethod(self, m):
+        """IMSRGSolver::SetMethod: magnus_euler (magnus), magnus_modified_euler
+        or magnus_backoff; the ODE methods are not on the GPU path."""
+        if m not in self._METHODS:
+            raise _lib.IMSRGError(_lib.ERR_UNSUPPORTED, "method %s is not on the GPU path" % m)
+        self._set("method", self._METHODS[m])
+        self.method = m
+
     def SetDenominatorCutoff(self, c):
         self._set("denominator_cutoff", c)
 
@@ -776,11 +786,6 @@ class IMSRGSolver:
 
     def SetDenominatorPartitioning(self, dp):
         check(self._L.imsrg_solver_set_denominator_partitioning(self._h, dp.encode()))
-
-    def SetMethod(self, m):
-        if m not in ("magnus_euler", "magnus"):
-            raise NotImplementedError("solver method %r is not on the GPU path" % m)
-        self.method = m
 
     def SetBCHTransformThreshold(self, x):
         self._set("bch_transform_threshold", x)

@@ -173,12 +173,20 @@ struct imsrg_solver {
   std::string scratch;
   int n_written = 0, max_omega_written = 500;
   std::vector<std::string> files;
+  // IMSRGSolver::method (src/IMSRGSolver.cc:201-234): 0 magnus_euler,
+  // 1 magnus_modified_euler, 2 magnus_backoff; the back-off parameters and
+  // state (src/IMSRGSolver.hh:73-78)
+  int method = 0;
+  double ds_backoff_factor = 0.5, ds_max_growth_factor = 1.2;
+  bool soft_landing = false;
+  imsrg_op* Htemp = nullptr;  // modified Euler's predicted H
 
   ~imsrg_solver()
   {
     imsrg_op_destroy(Hs);
     imsrg_op_destroy(Eta);
     imsrg_op_destroy(Hsaved);
+    imsrg_op_destroy(Htemp);
     for (imsrg_op* o : omega) imsrg_op_destroy(o);
     for (const std::string& f : files) std::remove(f.c_str());  // CleanupScratch
   }
@@ -285,6 +293,95 @@ int solve_magnus_euler(imsrg_solver* sv, int prec, cudaStream_t st)
   return IMSRG_OK;
 }
 
+// IMSRGSolver::Solve_magnus_modified_euler, src/IMSRGSolver.cc:449-504: the
+// generator at the Euler-predicted H_temp = H + ds [eta, H] (Generator::
+// AddToEta overwrites the elements Update wrote, so Eta becomes G(H_temp)),
+// times ds / 2; no eta criterion, no Omega gathering
+int solve_magnus_modified_euler(imsrg_solver* sv, int prec, cudaStream_t st)
+{
+  sv->istep = 0;
+  FLOW_TRY(generator_impl(sv->Hs, sv->Eta, sv->gen, st));
+  if (!sv->Htemp) FLOW_TRY(imsrg_op_create(sv->sp, 1, &sv->Htemp));
+  int rc = IMSRG_OK;
+  for (sv->istep = 1; sv->s < sv->smax; ++sv->istep) {
+    double norm_eta = 0, norm_omega = 0;
+    FLOW_TRY(norm_dev(sv->Eta, &norm_eta, st));
+    FLOW_TRY(norm_dev(sv->omega.back(), &norm_omega, st));
+    if (norm_omega > sv->omega_norm_max) {
+      FLOW_TRY(new_omega(sv, st));
+      norm_omega = 0;
+    }
+    sv->ds = std::min(std::min(sv->norm_domega / norm_eta, sv->norm_domega / norm_eta / (norm_omega + 1.0e-9)),
+                      sv->ds_max);
+    if (sv->s + sv->ds > sv->smax) sv->ds = sv->smax - sv->s;
+    sv->s += sv->ds;
+    FLOW_TRY(commutator_dev(sv->Eta, sv->Hs, sv->Htemp, prec, st));
+    FLOW_TRY(imsrg_op_scale(sv->Htemp, sv->ds, st));
+    FLOW_TRY(imsrg_op_axpy(sv->Htemp, 1.0, sv->Hs, st));
+    sv->Htemp->herm = sv->Hs->herm;
+    FLOW_TRY(generator_impl(sv->Htemp, sv->Eta, sv->gen, st));
+    FLOW_TRY(imsrg_op_scale(sv->Eta, sv->ds * 0.5, st));
+    FLOW_TRY(bch_product_impl(sv->Eta, sv->omega.back(), sv->omega.back(), sv->bch_product_threshold, prec, nullptr,
+                              st));
+    const imsrg_op* Hin = sv->omega.size() + sv->n_written < 2 ? sv->H0 : sv->Hsaved;
+    FLOW_TRY(imsrg_bch_transform(Hin, sv->omega.back(), sv->Hs, sv->bch_transform_threshold, prec, nullptr, st));
+    FLOW_TRY(generator_impl(sv->Hs, sv->Eta, sv->gen, st));
+    const double e0 = zero_body(sv->Hs, st, &rc);
+    if (rc) return rc;
+    sv->history.push_back({sv->istep, sv->s, e0, norm_eta, norm_omega});
+  }
+  return IMSRG_OK;
+}
+
+// IMSRGSolver::Solve_magnus_backoff, src/IMSRGSolver.cc:324-447: Euler steps
+// whose ds backs off (by ds_backoff_factor) while ds |eta| > pi/4 or when
+// |eta| grew over the step, and grows (by ds_max_growth_factor, up to ds_max)
+// otherwise, except in the soft-landing phase (|eta| < 20 eta_criterion)
+int solve_magnus_backoff(imsrg_solver* sv, int prec, cudaStream_t st)
+{
+  sv->istep = 0;
+  FLOW_TRY(generator_impl(sv->Hs, sv->Eta, sv->gen, st));
+  int rc = IMSRG_OK;
+  for (sv->istep = 1; sv->s < sv->smax; ++sv->istep) {
+    double norm_eta = 0;
+    FLOW_TRY(norm_dev(sv->Eta, &norm_eta, st));
+    if (!sv->soft_landing && std::fabs(norm_eta) < sv->eta_criterion * 20.0) sv->soft_landing = true;
+    if (norm_eta < sv->eta_criterion) break;
+    while (sv->magnus_adaptive && sv->ds * norm_eta > M_PI_4) sv->ds = sv->ds * sv->ds_backoff_factor;
+    double norm_omega = 0;
+    FLOW_TRY(norm_dev(sv->omega.back(), &norm_omega, st));
+    if (norm_omega > sv->omega_norm_max) {
+      if (sv->hunter_gatherer)
+        FLOW_TRY(gather_omega(sv, prec, st));
+      else
+        FLOW_TRY(new_omega(sv, st));
+      norm_omega = 0;
+    }
+    sv->ds = std::min(sv->ds, sv->smax - sv->s);
+    sv->s += sv->ds;
+    FLOW_TRY(imsrg_op_scale(sv->Eta, sv->ds, st));
+    FLOW_TRY(bch_product_impl(sv->Eta, sv->omega.back(), sv->omega.back(), sv->bch_product_threshold, prec, nullptr,
+                              st));
+    const imsrg_op* Hin = sv->omega.size() + sv->n_written < 2 ? sv->H0 : sv->Hsaved;
+    FLOW_TRY(imsrg_bch_transform(Hin, sv->omega.back(), sv->Hs, sv->bch_transform_threshold, prec, nullptr, st));
+    FLOW_TRY(generator_impl(sv->Hs, sv->Eta, sv->gen, st));
+    if (sv->magnus_adaptive) {
+      double norm_eta_new = 0;
+      FLOW_TRY(norm_dev(sv->Eta, &norm_eta_new, st));
+      if (norm_eta_new > norm_eta) {
+        sv->ds = sv->ds * sv->ds_backoff_factor;
+      } else if (!sv->soft_landing) {
+        const double ds_new = std::min(sv->ds_max, sv->ds * sv->ds_max_growth_factor);
+        if (ds_new > sv->ds) sv->ds = ds_new;
+      }
+    }
+    const double e0 = zero_body(sv->Hs, st, &rc);
+    if (rc) return rc;
+    sv->history.push_back({sv->istep, sv->s, e0, norm_eta, norm_omega});
+  }
+  return IMSRG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -360,6 +457,12 @@ int imsrg_solver_set(imsrg_solver* sv, const char* name, double v)
   else if (n == "bch_transform_threshold") sv->bch_transform_threshold = v;
   else if (n == "bch_product_threshold") sv->bch_product_threshold = v;
   else if (n == "max_omega_written") sv->max_omega_written = (int)v;
+  else if (n == "method") {
+    if (v != 0 && v != 1 && v != 2) return err(IMSRG_ERR_ARG, "method: 0 magnus_euler, 1 magnus_modified_euler, 2 magnus_backoff");
+    sv->method = (int)v;
+  }
+  else if (n == "ds_backoff_factor") sv->ds_backoff_factor = v;
+  else if (n == "ds_max_growth_factor") sv->ds_max_growth_factor = v;
   else return err(IMSRG_ERR_ARG, "unknown solver setting " + n);
   return IMSRG_OK;
 }
@@ -415,7 +518,10 @@ int imsrg_solver_set_generator(imsrg_solver* sv, const char* type, void* stream)
     else
       FLOW_TRY(new_omega(sv, st));
   }
-  if (sv->magnus_adaptive) sv->ds = sv->ds_0;
+  if (sv->magnus_adaptive) {
+    sv->ds = sv->ds_0;
+    sv->soft_landing = false;
+  }
   return IMSRG_OK;
 }
 
@@ -432,6 +538,14 @@ int imsrg_solver_solve(imsrg_solver* sv, int precision, void* stream)
 {
   if (!sv) return err(IMSRG_ERR_ARG, "null solver");
   if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_SPLIT) return err(IMSRG_ERR_ARG, "bad precision");
+  if (sv->method == 1) {
+    ProfScope ps("Solve_magnus_modified_euler", S_(stream));
+    return solve_magnus_modified_euler(sv, precision, S_(stream));
+  }
+  if (sv->method == 2) {
+    ProfScope ps("Solve_magnus_backoff", S_(stream));
+    return solve_magnus_backoff(sv, precision, S_(stream));
+  }
   ProfScope ps("Solve_magnus_euler", S_(stream));
   return solve_magnus_euler(sv, precision, S_(stream));
 }

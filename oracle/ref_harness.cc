@@ -330,6 +330,22 @@ static int flow_main(int argc, char** argv) {
     write_file(outdir + "/flow2_Hs.bin", store(solver.GetH_s(), L));
     write_file(outdir + "/flow2_Omega.bin", store(solver.GetOmega(solver.GetOmegaSize() - 1), L));
   }
+  // the other Magnus methods: modified Euler and back-off, with Omega splits
+  struct MethodCase { const char* name; const char* method; };
+  const MethodCase methods[] = {{"flow_me", "magnus_modified_euler"}, {"flow_bo", "magnus_backoff"}};
+  for (const MethodCase& mc : methods) {
+    IMSRGSolver solver(H);
+    solver.SetGenerator("white");
+    solver.SetMethod(mc.method);
+    solver.SetOmegaNormMax(0.3);
+    solver.SetEtaCriterion(1e-20);
+    solver.SetSmax(2.0);
+    solver.Solve();
+    std::ofstream f(outdir + "/" + mc.name + ".txt");
+    f << std::setprecision(17) << solver.GetS() << " " << solver.GetOmegaSize() << " " << solver.GetH_s().ZeroBody
+      << "\n";
+    write_file(outdir + "/" + mc.name + "_Hs.bin", store(solver.GetH_s(), L));
+  }
   return 0;
 }
 

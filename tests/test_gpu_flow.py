@@ -209,3 +209,35 @@ def test_solver_settings_and_errors():
     with pytest.raises(ig.IMSRGError):
         solver.SetDenominatorPartitioning("MP_isospin")
     assert solver.GetS() == 0.0 and solver.GetOmegaSize() == 1
+
+
+@pytest.mark.parametrize("emax", [2, 3])
+@pytest.mark.parametrize("method,key", [("magnus_modified_euler", "flow_me"), ("magnus_backoff", "flow_bo")])
+@pytest.mark.parametrize("prec", ["fp64", "split"])
+def test_other_magnus_methods_vs_reference(emax, method, key, prec):
+    # IMSRGSolver::Solve_magnus_modified_euler and Solve_magnus_backoff
+    # (src/IMSRGSolver.cc:324-504) to s = 2 with Omega splits, against the
+    # reference's own runs
+    g = load_flow_golden(emax)
+    ms = ig.ModelSpace(emax, "O16", "O16")
+    r = ref_space(emax)
+    s_ref, n_omega_ref, e0_ref = g[key]
+    solver = ig.IMSRGSolver(ig.Operator(ms, arena=g["H"]), precision=prec)
+    solver.SetGenerator("white")
+    solver.SetMethod(method)
+    solver.SetOmegaNormMax(0.3)
+    solver.SetEtaCriterion(1e-20)
+    solver.SetSmax(2.0)
+    solver.Solve()
+    assert abs(solver.GetS() - s_ref) <= 1e-12
+    assert solver.GetOmegaSize() == int(n_omega_ref)
+    Hs = solver.GetH_s()
+    assert abs(Hs.ZeroBody - e0_ref) <= TOL_E0[prec] * abs(e0_ref)
+    assert max(rel_errors(r, Hs.arena, g[key + "_Hs"])) < TOL_OPS[prec]
+
+
+def test_unknown_method_refused():
+    ms = ig.ModelSpace(2, "O16", "O16")
+    solver = ig.IMSRGSolver(ig.Operator(ms, arena=load_flow_golden(2)["H"]))
+    with pytest.raises(ig.IMSRGError):
+        solver.SetMethod("flow_RK4")
