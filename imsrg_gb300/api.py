@@ -644,7 +644,8 @@ class _BCHNamespace:
 BCH = _BCHNamespace()
 
 
-_GENERATOR_TYPES = {"white": 0, "atan": 1, "wegner": 2, "imaginary-time": 3}
+_GENERATOR_TYPES = {"white": 0, "atan": 1, "wegner": 2, "imaginary-time": 3, "qtransfer-atan": 101}
+_GENERATOR_TYPES.update({"qtransfer-atan_%d" % n: 100 + n for n in range(1, 17)})
 DELTA_ALL = -12345
 
 

@@ -10,6 +10,7 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -142,6 +143,18 @@ int gen_type(const char* t, int* out)
       *out = i;
       return IMSRG_OK;
     }
+  // qtransfer-atan and qtransfer-atan_<n> (src/Generator.cc:55, :63-69)
+  if (!std::strcmp(t, "qtransfer-atan")) {
+    *out = GEN_QTRANSFER_BASE + 1;
+    return IMSRG_OK;
+  }
+  if (!std::strncmp(t, "qtransfer-atan_", 15)) {
+    const int n = std::atoi(t + 15);
+    if (n >= 1 && n <= 16) {
+      *out = GEN_QTRANSFER_BASE + n;
+      return IMSRG_OK;
+    }
+  }
   return err(IMSRG_ERR_UNSUPPORTED, std::string("generator type not on the GPU path: ") + t);
 }
 
@@ -392,7 +405,9 @@ int imsrg_generator_update(const imsrg_op* H, imsrg_op* Eta, int type, int parti
   if (!H || !Eta || H == Eta) return err(IMSRG_ERR_ARG, "bad operators");
   if (H->tl || Eta->tl) return err(IMSRG_ERR_UNSUPPORTED, "the generator takes scalar operators");
   if (H->sp != Eta->sp) return err(IMSRG_ERR_ARG, "operators belong to different model spaces");
-  if (type < IMSRG_GEN_WHITE || type > IMSRG_GEN_IMAGINARY_TIME) return err(IMSRG_ERR_ARG, "bad generator type");
+  if ((type < IMSRG_GEN_WHITE || type > IMSRG_GEN_IMAGINARY_TIME) &&
+      (type <= GEN_QTRANSFER_BASE || type > GEN_QTRANSFER_BASE + 16))
+    return err(IMSRG_ERR_ARG, "bad generator type");
   if (partitioning != IMSRG_DENOM_EPSTEIN_NESBET && partitioning != IMSRG_DENOM_MOLLER_PLESSET)
     return err(IMSRG_ERR_ARG, "bad denominator partitioning");
   GenParams p;

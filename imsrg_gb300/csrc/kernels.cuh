@@ -71,6 +71,8 @@ cudaError_t launch_pandya_single(const Space& s, const double* Z, int herm, int 
 // imaginary-time functions, Epstein-Nesbet or Moller-Plesset denominators):
 // Eta is overwritten; mono is norb^2 doubles of scratch
 enum { GEN_WHITE = 0, GEN_ATAN = 1, GEN_WEGNER = 2, GEN_IMAGINARY_TIME = 3 };
+// qtransfer-atan_n: type GEN_QTRANSFER_BASE + n (qtransfer-atan is n = 1)
+constexpr int GEN_QTRANSFER_BASE = 100;
 enum { DENOM_EPSTEIN_NESBET = 0, DENOM_MOLLER_PLESSET = 1 };
 constexpr int kDeltaAll = -12345;  // denominator_delta_index that adds the delta everywhere
 struct GenParams {

@@ -1079,8 +1079,18 @@ __global__ void k_pandya_single(DevSpace S, DevWork W, const double* __restrict_
 constexpr double kGenOccCut = 1e-6;  // ModelSpace::OCC_CUT (src/ModelSpace.cc:14)
 
 // the generator functions of src/Generator.cc:12-15
+// the reference's q-transfer generators (src/Generator.cc:18, :63-69):
+// atan(2 Hod / d) / 2 times (|d| M_N / (hbar c)^2)^(n/2), with the reference's
+// constants (src/PhysicalConstants.hh: hbar c = 197.3269718 MeV fm, M_N the
+// mean of 938.2720813 and 939.5654133 MeV)
+constexpr double kHbarc = 197.3269718;
+constexpr double kMNucleon = (938.2720813 + 939.5654133) / 2.0;
+
 __device__ __forceinline__ double eta_value(int type, double hod, double den)
 {
+  if (type > GEN_QTRANSFER_BASE)
+    return pow(fabs(den) * kMNucleon / kHbarc / kHbarc, 0.5 * (type - GEN_QTRANSFER_BASE)) *
+           (0.5 * atan(2 * hod / den));
   switch (type) {
     case GEN_ATAN: return 0.5 * atan(2 * hod / den);
     case GEN_WEGNER: return hod * den;

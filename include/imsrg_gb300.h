@@ -54,6 +54,9 @@ extern "C" {
 #define IMSRG_GEN_ATAN 1           /* atan(2 Hod / denominator) / 2 */
 #define IMSRG_GEN_WEGNER 2         /* Hod * denominator */
 #define IMSRG_GEN_IMAGINARY_TIME 3 /* Hod * sign(denominator) */
+/* qtransfer-atan_n (qtransfer-atan is n = 1): the atan generator times
+ * (|denominator| M_N / (hbar c)^2)^(n/2), 1 <= n <= 16 */
+#define IMSRG_GEN_QTRANSFER_ATAN(n) (100 + (n))
 #define IMSRG_DENOM_EPSTEIN_NESBET 0
 #define IMSRG_DENOM_MOLLER_PLESSET 1
 /* denominator_delta_index that adds denominator_delta to every denominator */

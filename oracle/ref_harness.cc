@@ -287,7 +287,9 @@ static int flow_main(int argc, char** argv) {
   struct GenCase { const char* file; const char* type; const char* part; };
   const GenCase gens[] = {{"eta_white", "white", "Epstein_Nesbet"},
                           {"eta_atan", "atan", "Epstein_Nesbet"},
-                          {"eta_white_mp", "white", "Moller_Plesset"}};
+                          {"eta_white_mp", "white", "Moller_Plesset"},
+                          {"eta_qt", "qtransfer-atan", "Epstein_Nesbet"},
+                          {"eta_qt2", "qtransfer-atan_2", "Epstein_Nesbet"}};
   for (const GenCase& g : gens) {
     Generator gen;
     gen.SetType(g.type);

@@ -22,9 +22,9 @@ Fixtures (arena layout: see oracle/modelspace_ref.py):
   golden_flow_emax2.npz, golden_flow_emax3.npz
                      H (flow Hamiltonian, RefModelSpace.flow_hamiltonian with
                      two-body scale 0.5), A = 0.05 V/|V| and B = 0.5 U/|U|
-                     (anti-hermitian); BCH::BCH_Product(A, B) and of (6A, 2B); the White and
-                     atan generators of H (Epstein-Nesbet) and White with
-                     Moller-Plesset denominators; ten fixed Magnus-Euler steps
+                     (anti-hermitian); BCH::BCH_Product(A, B) and of (6A, 2B); the White,
+                     atan, qtransfer-atan and qtransfer-atan_2 generators of H
+                     (Epstein-Nesbet) and White with Moller-Plesset denominators; ten fixed Magnus-Euler steps
                      (ds 0.5, White generator) with s and E0 after each step and
                      the final H(s), Omega; an adaptive flow to s = 2 with Omega
                      split at |Omega| > 0.3 (final s, number of Omegas, E0,
@@ -126,7 +126,7 @@ def run_reference_flow(emax):
                        env=dict(os.environ, OMP_NUM_THREADS="1"))
         out = {"H": H, "A": A, "B": B, "emax": np.array(emax), "v2": np.array(FLOW_V2)}
         for k in ("bchp", "bchp_big", "eta_white", "eta_atan", "eta_white_mp", "flow_Hs", "flow_Omega", "flow2_Hs",
-                  "flow2_Omega", "flow_me_Hs", "flow_bo_Hs"):
+                  "flow2_Omega", "flow_me_Hs", "flow_bo_Hs", "eta_qt", "eta_qt2"):
             out[k] = np.fromfile(os.path.join(td, k + ".bin"))
         out["flow_steps"] = np.loadtxt(os.path.join(td, "flow_steps.txt"))
         out["flow2"] = np.loadtxt(os.path.join(td, "flow2.txt"))

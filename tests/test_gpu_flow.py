@@ -72,7 +72,9 @@ def test_bch_product_host_api():
 
 @pytest.mark.parametrize("emax", [2, 3])
 @pytest.mark.parametrize("case", [("eta_white", "white", "Epstein_Nesbet"), ("eta_atan", "atan", "Epstein_Nesbet"),
-                                  ("eta_white_mp", "white", "Moller_Plesset")])
+                                  ("eta_white_mp", "white", "Moller_Plesset"),
+                                  ("eta_qt", "qtransfer-atan", "Epstein_Nesbet"),
+                                  ("eta_qt2", "qtransfer-atan_2", "Epstein_Nesbet")])
 def test_generator_vs_reference(emax, case):
     key, kind, part = case
     g = load_flow_golden(emax)
