@@ -38,11 +38,20 @@ int fail(int code, const std::string& msg)
       return fail(IMSRG_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
   } while (0)
 
-enum Term { T110 = 0, T220, T111, T121, T122, T221, T222PPHH, T222PH, NTERMS };
-const char* kTermNames[NTERMS] = {"comm110ss", "comm220ss",      "comm111ss",   "comm121ss",
-                                  "comm122ss", "comm221ss", "comm222_pp_hhss", "comm222_phss"};
+// Commutator::comm_term_on (src/Commutator.cc): the scalar terms, then the
+// scalar-tensor terms CommutatorScalarTensor consults (src/Commutator.cc:
+// 459-482; comm222_pp_hh_221st runs when both comm222_pp_hhst and comm221st
+// are on)
+enum Term {
+  T110 = 0, T220, T111, T121, T122, T221, T222PPHH, T222PH, NSCALAR_TERMS,
+  TS111 = NSCALAR_TERMS, TS121, TS122, TS222PPHH, TS221, TS222PH, NTERMS
+};
+const char* kTermNames[NTERMS] = {"comm110ss",  "comm220ss",  "comm111ss",       "comm121ss",
+                                  "comm122ss",  "comm221ss",  "comm222_pp_hhss", "comm222_phss",
+                                  "comm111st",  "comm121st",  "comm122st",       "comm222_pp_hhst",
+                                  "comm221st",  "comm222_phst"};
 std::mutex g_mu;
-bool g_term_on[NTERMS] = {true, true, true, true, true, true, true, true};
+bool g_term_on[NTERMS] = {true, true, true, true, true, true, true, true, true, true, true, true, true, true};
 int g_default_precision = IMSRG_PREC_FP64;
 
 template <class T>
@@ -1086,9 +1095,19 @@ namespace imsrg {
 bool batch_phases_usable()
 {
   std::lock_guard<std::mutex> g(g_mu);
-  for (int t = 0; t < NTERMS; ++t)
+  for (int t = 0; t < NSCALAR_TERMS; ++t)
     if (!g_term_on[t]) return false;
   return true;
+}
+
+void tensor_terms_on(bool on[5])
+{
+  std::lock_guard<std::mutex> g(g_mu);
+  on[0] = g_term_on[TS111];
+  on[1] = g_term_on[TS121];
+  on[2] = g_term_on[TS122];
+  on[3] = g_term_on[TS222PPHH] && g_term_on[TS221];
+  on[4] = g_term_on[TS222PH];
 }
 
 // Products of several pairs whose spaces have the same structure (equal

@@ -37,6 +37,9 @@ int tensor_bch_transform(const imsrg_op* OpIn, const imsrg_op* Omega, imsrg_op* 
 // the split-form commutator of a group of same-structure pairs, one launch
 // per kernel for the whole group: usable only with every term switched on
 bool batch_phases_usable();
+// the scalar-tensor term switches: comm111st, comm121st, comm122st,
+// comm222_pp_hh_221st (comm222_pp_hhst and comm221st), comm222_phst
+void tensor_terms_on(bool on[5]);
 // the ladder and Zbar products of same-structure pairs as one launch each
 struct GroupedProducts;
 GroupedProducts* grouped_products_create(const std::vector<const imsrg_op*>& X, const std::vector<const imsrg_op*>& Y,

@@ -339,13 +339,19 @@ int imsrg_commutator_scalar_tensor(const imsrg_op* X, const imsrg_op* Y, imsrg_o
   if ((rc = check_st(X, Y, Z))) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   if (precision == IMSRG_PREC_SPLIT && (rc = split_ready(X->sp, Y->tl))) return rc;
+  bool on[5];
+  tensor_terms_on(on);  // Commutator::comm_term_on, as CommutatorScalarTensor consults it
   ProfScope ps("CommutatorScalarTensor", st);
   T_CUDA(cudaMemsetAsync(Z->d, 0, Z->len * sizeof(double), st));
-  if ((rc = t111(X, Y, Z, st)) || (rc = t121(X, Y, Z, st)) || (rc = t122(X, Y, Z, st))) return rc;
+  if ((on[0] && (rc = t111(X, Y, Z, st))) || (on[1] && (rc = t121(X, Y, Z, st))) ||
+      (on[2] && (rc = t122(X, Y, Z, st))))
+    return rc;
   if (precision == IMSRG_PREC_FP64) {
-    if ((rc = t222(X, Y, Z, st)) || (rc = tph(X, Y, Z, st))) return rc;
-  } else {
-    if ((rc = split_operands(X, Y, st)) || (rc = t222_split(X, Y, Z, st)) || (rc = tph_split(X, Y, Z, st))) return rc;
+    if ((on[3] && (rc = t222(X, Y, Z, st))) || (on[4] && (rc = tph(X, Y, Z, st)))) return rc;
+  } else if (on[3] || on[4]) {
+    if ((rc = split_operands(X, Y, st)) || (on[3] && (rc = t222_split(X, Y, Z, st))) ||
+        (on[4] && (rc = tph_split(X, Y, Z, st))))
+      return rc;
     return status_dev(X->sp, st);
   }
   return IMSRG_OK;

@@ -282,7 +282,11 @@ int imsrg_commutator_scalar_scalar(const imsrg_op* X, const imsrg_op* Y, imsrg_o
 
 /* Commutator::TurnOnTerm / TurnOffTerm (src/Commutator.cc:77-78) for the
  * IMSRG(2) names "comm110ss", "comm220ss", "comm111ss", "comm121ss",
- * "comm122ss", "comm221ss", "comm222_pp_hhss", "comm222_phss". Process-wide. */
+ * "comm122ss", "comm221ss", "comm222_pp_hhss", "comm222_phss", and the
+ * scalar-tensor names "comm111st", "comm121st", "comm122st",
+ * "comm222_pp_hhst", "comm221st", "comm222_phst" (comm222_pp_hh_221st runs
+ * when both comm222_pp_hhst and comm221st are on, as in the reference).
+ * Process-wide. */
 int imsrg_set_term(const char* name, int on);
 int imsrg_get_term(const char* name, int* on);
 

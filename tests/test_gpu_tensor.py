@@ -211,3 +211,26 @@ def test_solver_transform_of_a_tensor_observable():
     assert max(tensor_rel_errors(ref_space(3), rank, Tt.arena, ref.arena)) < 1e-12
     back = solver.InverseTransform(Tt)
     assert max(tensor_rel_errors(ref_space(3), rank, back.arena, T.arena)) < 1e-8
+
+
+@pytest.mark.parametrize("off,dropped", [("comm222_phst", ["comm222_phst"]),
+                                         ("comm221st", ["comm222_pp_hh_221st"]),
+                                         ("comm122st", ["comm122st"])])
+def test_tensor_term_switches(off, dropped):
+    # Commutator::TurnOffTerm, as CommutatorScalarTensor consults it
+    # (comm222_pp_hh_221st needs both comm222_pp_hhst and comm221st)
+    g, ms, dX, dT, rank, herm = setup(2, "e2")
+    R = g["e2_full"].copy()
+    for t in dropped:
+        R -= g["e2_" + t]
+    ig.Commutator.TurnOffTerm(off)
+    try:
+        for prec in ("fp64", "split"):
+            with ig.DeviceOperator(ms, 1, rank) as dZ:
+                ig.Commutator.device_scalar_tensor(dX, dT, dZ, precision=prec)
+                Z = dZ.download()
+            errs = tensor_rel_errors(ref_space(2), rank, Z, R)
+            assert max(errs) < (TOL if prec == "fp64" else SPLIT_TOL), (off, prec, errs)
+    finally:
+        ig.Commutator.TurnOnTerm(off)
+    assert ig.Commutator.IsTermOn(off)
