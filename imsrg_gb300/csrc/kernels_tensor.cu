@@ -840,8 +840,10 @@ __global__ void __launch_bounds__(32 * kTqWarps, 4) k_tinv_q(DevSpace S, DevTens
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long qi = blockIdx.x * (long long)kTqWarps + warp;
   if (qi >= nq) return;
-  double* in1 = s_in + (size_t)warp * 2 * slots;
+  // per warp: the two sums' gathered values, then the owned output slots
+  double* in1 = s_in + (size_t)warp * 3 * slots;
   double* in2 = in1 + slots;
+  int* own = reinterpret_cast<int*>(in2 + slots);
   const int2 v = tq[qi];
   const int i = v.x & 0xFFFF, j = v.x >> 16, k = v.y & 0xFFFF, l = v.y >> 16;
   tinv_gather(S, T, Zb, hZ, i, j, k, l, in1, lane);
@@ -853,15 +855,31 @@ __global__ void __launch_bounds__(32 * kTqWarps, 4) k_tinv_q(DevSpace S, DevTens
   const int kb = ket_index(S.norb, i, j), kk = ket_index(S.norb, k, l);
   const int J1min = abs(ji - jj) >> 1, nJ1 = ((ji + jj) >> 1) - J1min + 1;
   const int J2lo = abs(jk - jl) >> 1, J2hi = (jk + jl) >> 1;
-  for (int t = lane; t < nJ1 * w; t += 32) {
+  // the slots this quadruple owns, compacted (ballot) so every lane of the
+  // sums below has one
+  int nown = 0;
+  for (int c0 = 0; c0 < nJ1 * w; c0 += 32) {
+    const int t = c0 + lane;
+    bool ok = false;
+    if (t < nJ1 * w) {
+      const int J1 = J1min + t / w, J2 = J1 - Lam + t % w;
+      if (J2 >= J2lo && J2 <= J2hi && J1 < S.NJ && J2 < S.NJ) {
+        const int ib = S.ketJ_loc[J1 * S.nkets + kb], ik = S.ketJ_loc[J2 * S.nkets + kk];
+        const int chb = chan_index(J1, pb, tb), chk = chan_index(J2, pk, tk);
+        ok = ib >= 0 && ik >= 0 && !(chb > chk || (chb == chk && ik < ib)) && T.lookup[chb * S.nch + chk] >= 0;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, ok);
+    if (ok) own[nown + __popc(m & ((1u << lane) - 1))] = t;
+    nown += __popc(m);
+  }
+  __syncwarp();
+  for (int x = lane; x < nown; x += 32) {
+    const int t = own[x];
     const int J1 = J1min + t / w, J2 = J1 - Lam + t % w;
-    if (J2 < J2lo || J2 > J2hi || J1 >= S.NJ || J2 >= S.NJ) continue;
     const int ib = S.ketJ_loc[J1 * S.nkets + kb], ik = S.ketJ_loc[J2 * S.nkets + kk];
-    if (ib < 0 || ik < 0) continue;
     const int chb = chan_index(J1, pb, tb), chk = chan_index(J2, pk, tk);
-    if (chb > chk || (chb == chk && ik < ib)) continue;
     const int blk = T.lookup[chb * S.nch + chk];
-    if (blk < 0) continue;
     const double commij = tinv_dot(S, T, i, j, k, l, J1, J2, in1);
     const double commji = i == j ? commij : tinv_dot(S, T, j, i, k, l, J1, J2, in2);
     const double z = unnorm(commij + flip(commji, 1 + ((ji + jj) >> 1) - J1), i == j, k == l);
@@ -878,8 +896,9 @@ cudaError_t launch_tinv_q(const Space& s, const TensorLayout& t, const double* Z
 {
   const long long nq = (long long)t.tq.size();
   if (nq == 0) return cudaSuccess;
+  // slots bounds a sum's gathered values and the output slots alike
   const int slots = t.tq_max_j3 * (2 * t.lam + 1);
-  const size_t smem = (size_t)kTqWarps * 2 * slots * sizeof(double);
+  const size_t smem = (size_t)kTqWarps * 3 * slots * sizeof(double);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_tinv_q, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
