@@ -757,11 +757,13 @@ class IMSRGSolver:
     def SetHunterGatherer(self, b=True):
         self._set("hunter_gatherer", 1 if b else 0)
 
-    _METHODS = {"magnus_euler": 0, "magnus": 0, "magnus_modified_euler": 1, "magnus_backoff": 2}
+    _METHODS = {"magnus_euler": 0, "magnus": 0, "magnus_modified_euler": 1, "magnus_backoff": 2, "flow_RK4": 3}
 
     def SetMethod(self, m):
-        """IMSRGSolver::SetMethod: magnus_euler (magnus), magnus_modified_euler
-        or magnus_backoff; the ODE methods are not on the GPU path."""
+        """IMSRGSolver::SetMethod: magnus_euler (magnus), magnus_modified_euler,
+        magnus_backoff or flow_RK4 (fixed RK4 steps of ds_max on H(s), no
+        Omega); the boost::odeint methods (flow, flow_adaptive, flow_euler,
+        magnus_adaptive, restore_4th_order) are not on the GPU path."""
         if m not in self._METHODS:
             raise _lib.IMSRGError(_lib.ERR_UNSUPPORTED, "method %s is not on the GPU path" % m)
         self._set("method", self._METHODS[m])

@@ -187,12 +187,14 @@ struct imsrg_solver {
   int n_written = 0, max_omega_written = 500;
   std::vector<std::string> files;
   // IMSRGSolver::method (src/IMSRGSolver.cc:201-234): 0 magnus_euler,
-  // 1 magnus_modified_euler, 2 magnus_backoff; the back-off parameters and
+  // 1 magnus_modified_euler, 2 magnus_backoff, 3 flow_RK4; the back-off parameters and
   // state (src/IMSRGSolver.hh:73-78)
   int method = 0;
   double ds_backoff_factor = 0.5, ds_max_growth_factor = 1.2;
   bool soft_landing = false;
-  imsrg_op* Htemp = nullptr;  // modified Euler's predicted H
+  imsrg_op* Htemp = nullptr;  // modified Euler's predicted H; RK4's stage H
+  imsrg_op* Kstage = nullptr;  // RK4: [eta, H] of the current stage
+  imsrg_op* Ksum = nullptr;    // RK4: K1 + 2 K2 + 2 K3 + K4
 
   ~imsrg_solver()
   {
@@ -200,6 +202,8 @@ struct imsrg_solver {
     imsrg_op_destroy(Eta);
     imsrg_op_destroy(Hsaved);
     imsrg_op_destroy(Htemp);
+    imsrg_op_destroy(Kstage);
+    imsrg_op_destroy(Ksum);
     for (imsrg_op* o : omega) imsrg_op_destroy(o);
     for (const std::string& f : files) std::remove(f.c_str());  // CleanupScratch
   }
@@ -395,6 +399,50 @@ int solve_magnus_backoff(imsrg_solver* sv, int prec, cudaStream_t st)
   return IMSRG_OK;
 }
 
+// IMSRGSolver::Solve_flow_RK4, src/IMSRGSolver.cc:505-636: the classical
+// fixed-step RK4 rule for dH/ds = [eta(H), H] with steps of ds_max (the last
+// one cut to end at smax), the generator re-evaluated at every stage's H;
+// no Omega, one flowing operator, no goose-tank term (BCH's
+// use_goose_tank_correction is off by default)
+int solve_flow_rk4(imsrg_solver* sv, int prec, cudaStream_t st)
+{
+  sv->istep = 0;
+  FLOW_TRY(generator_impl(sv->Hs, sv->Eta, sv->gen, st));
+  if (!sv->Htemp) FLOW_TRY(imsrg_op_create(sv->sp, 1, &sv->Htemp));
+  if (!sv->Kstage) FLOW_TRY(imsrg_op_create(sv->sp, 1, &sv->Kstage));
+  if (!sv->Ksum) FLOW_TRY(imsrg_op_create(sv->sp, 1, &sv->Ksum));
+  // weight of stage k's K in the sum, and the step fraction of the H that
+  // feeds stage k + 1 (H + ds/2 K1, H + ds/2 K2, H + ds K3)
+  const double wsum[4] = {1.0, 2.0, 2.0, 1.0};
+  const double shift[3] = {0.5, 0.5, 1.0};
+  int rc = IMSRG_OK;
+  for (sv->istep = 1; sv->s < sv->smax; ++sv->istep) {
+    double norm_eta = 0;
+    FLOW_TRY(norm_dev(sv->Eta, &norm_eta, st));
+    if (norm_eta < sv->eta_criterion) break;
+    sv->ds = std::min(sv->ds_max, sv->smax - sv->s);
+    sv->s += sv->ds;
+    for (int k = 0; k < 4; ++k) {
+      FLOW_TRY(commutator_dev(sv->Eta, k == 0 ? sv->Hs : sv->Htemp, sv->Kstage, prec, st));
+      if (k == 0)
+        FLOW_TRY(imsrg_op_copy(sv->Ksum, sv->Kstage, st));
+      else
+        FLOW_TRY(imsrg_op_axpy(sv->Ksum, wsum[k], sv->Kstage, st));
+      if (k < 3) {
+        FLOW_TRY(imsrg_op_copy(sv->Htemp, sv->Hs, st));
+        FLOW_TRY(imsrg_op_axpy(sv->Htemp, shift[k] * sv->ds, sv->Kstage, st));
+        FLOW_TRY(generator_impl(sv->Htemp, sv->Eta, sv->gen, st));
+      }
+    }
+    FLOW_TRY(imsrg_op_axpy(sv->Hs, sv->ds / 6.0, sv->Ksum, st));
+    FLOW_TRY(generator_impl(sv->Hs, sv->Eta, sv->gen, st));
+    const double e0 = zero_body(sv->Hs, st, &rc);
+    if (rc) return rc;
+    sv->history.push_back({sv->istep, sv->s, e0, norm_eta, 0.0});
+  }
+  return IMSRG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -473,7 +521,8 @@ int imsrg_solver_set(imsrg_solver* sv, const char* name, double v)
   else if (n == "bch_product_threshold") sv->bch_product_threshold = v;
   else if (n == "max_omega_written") sv->max_omega_written = (int)v;
   else if (n == "method") {
-    if (v != 0 && v != 1 && v != 2) return err(IMSRG_ERR_ARG, "method: 0 magnus_euler, 1 magnus_modified_euler, 2 magnus_backoff");
+    if (v != 0 && v != 1 && v != 2 && v != 3)
+      return err(IMSRG_ERR_ARG, "method: 0 magnus_euler, 1 magnus_modified_euler, 2 magnus_backoff, 3 flow_RK4");
     sv->method = (int)v;
   }
   else if (n == "ds_backoff_factor") sv->ds_backoff_factor = v;
@@ -560,6 +609,10 @@ int imsrg_solver_solve(imsrg_solver* sv, int precision, void* stream)
   if (sv->method == 2) {
     ProfScope ps("Solve_magnus_backoff", S_(stream));
     return solve_magnus_backoff(sv, precision, S_(stream));
+  }
+  if (sv->method == 3) {
+    ProfScope ps("Solve_flow_RK4", S_(stream));
+    return solve_flow_rk4(sv, precision, S_(stream));
   }
   ProfScope ps("Solve_magnus_euler", S_(stream));
   return solve_magnus_euler(sv, precision, S_(stream));

@@ -376,8 +376,8 @@ void imsrg_solver_destroy(imsrg_solver* solver);
  * does), "magnus_adaptive", "hunter_gatherer" (0/1), "denominator_cutoff",
  * "denominator_delta", "denominator_delta_index", "bch_transform_threshold",
  * "bch_product_threshold", "max_omega_written", "method" (SetMethod: 0
- * magnus_euler, 1 magnus_modified_euler, 2 magnus_backoff; the ODE methods
- * are not on the GPU path), "ds_backoff_factor" (0.5) and
+ * magnus_euler, 1 magnus_modified_euler, 2 magnus_backoff, 3 flow_RK4; the
+ * boost::odeint methods are not on the GPU path), "ds_backoff_factor" (0.5) and
  * "ds_max_growth_factor" (1.2) of magnus_backoff.  imsrg_solver_get also reads "s" (flow parameter),
  * "n_omega" (Omegas kept) and "istep" (steps of the last solve, + 1). */
 int imsrg_solver_set(imsrg_solver* solver, const char* name, double value);
@@ -399,7 +399,9 @@ int imsrg_solver_set_denominator_partitioning(imsrg_solver* solver, const char* 
  * magnus_euler (the default) flows from the current s to smax or until |eta| <
  * eta_criterion, with IMSRG_ERR_DIVERGED when the reference's give-up test
  * fires (H(s) is then multiplied by 1/0, as there); magnus_modified_euler and
- * magnus_backoff follow Solve_magnus_modified_euler and Solve_magnus_backoff. */
+ * magnus_backoff follow Solve_magnus_modified_euler and Solve_magnus_backoff;
+ * flow_RK4 follows Solve_flow_RK4 (src/IMSRGSolver.cc:505-636): fixed RK4
+ * steps of ds_max on H(s) itself, no Omega. */
 int imsrg_solver_solve(imsrg_solver* solver, int precision, void* stream);
 /* GetH_s, GetEta and GetOmega(i) (0 <= i < n_omega): the solver's operators */
 int imsrg_solver_hs(imsrg_solver* solver, imsrg_op** out);

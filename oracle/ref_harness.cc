@@ -332,9 +332,11 @@ static int flow_main(int argc, char** argv) {
     write_file(outdir + "/flow2_Hs.bin", store(solver.GetH_s(), L));
     write_file(outdir + "/flow2_Omega.bin", store(solver.GetOmega(solver.GetOmegaSize() - 1), L));
   }
-  // the other Magnus methods: modified Euler and back-off, with Omega splits
+  // the other solver methods: Magnus modified Euler and back-off, with Omega
+  // splits, and the fixed-step RK4 flow of H itself
   struct MethodCase { const char* name; const char* method; };
-  const MethodCase methods[] = {{"flow_me", "magnus_modified_euler"}, {"flow_bo", "magnus_backoff"}};
+  const MethodCase methods[] = {
+      {"flow_me", "magnus_modified_euler"}, {"flow_bo", "magnus_backoff"}, {"flow_rk4", "flow_RK4"}};
   for (const MethodCase& mc : methods) {
     IMSRGSolver solver(H);
     solver.SetGenerator("white");

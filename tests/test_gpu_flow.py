@@ -214,12 +214,13 @@ def test_solver_settings_and_errors():
 
 
 @pytest.mark.parametrize("emax", [2, 3])
-@pytest.mark.parametrize("method,key", [("magnus_modified_euler", "flow_me"), ("magnus_backoff", "flow_bo")])
+@pytest.mark.parametrize("method,key", [("magnus_modified_euler", "flow_me"), ("magnus_backoff", "flow_bo"),
+                                        ("flow_RK4", "flow_rk4")])
 @pytest.mark.parametrize("prec", ["fp64", "split"])
-def test_other_magnus_methods_vs_reference(emax, method, key, prec):
-    # IMSRGSolver::Solve_magnus_modified_euler and Solve_magnus_backoff
-    # (src/IMSRGSolver.cc:324-504) to s = 2 with Omega splits, against the
-    # reference's own runs
+def test_other_solver_methods_vs_reference(emax, method, key, prec):
+    # IMSRGSolver::Solve_magnus_modified_euler, Solve_magnus_backoff (with
+    # Omega splits) and Solve_flow_RK4 (src/IMSRGSolver.cc:324-636) to s = 2,
+    # against the reference's own runs
     g = load_flow_golden(emax)
     ms = ig.ModelSpace(emax, "O16", "O16")
     r = ref_space(emax)
@@ -241,5 +242,8 @@ def test_other_magnus_methods_vs_reference(emax, method, key, prec):
 def test_unknown_method_refused():
     ms = ig.ModelSpace(2, "O16", "O16")
     solver = ig.IMSRGSolver(ig.Operator(ms, arena=load_flow_golden(2)["H"]))
+    for m in ("flow_adaptive", "flow_euler", "magnus_adaptive", "restore_4th_order"):
+        with pytest.raises(ig.IMSRGError):
+            solver.SetMethod(m)
     with pytest.raises(ig.IMSRGError):
-        solver.SetMethod("flow_RK4")
+        solver._set("method", 4.0)
