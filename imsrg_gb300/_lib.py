@@ -108,6 +108,8 @@ SIGNATURES = {
     "imsrg_solver_hs": (I, [P, ctypes.POINTER(P)]),
     "imsrg_solver_eta": (I, [P, ctypes.POINTER(P)]),
     "imsrg_solver_omega": (I, [P, I, ctypes.POINTER(P)]),
+    "imsrg_solver_add_operator": (I, [P, P, IP, P]),
+    "imsrg_solver_get_operator": (I, [P, I, ctypes.POINTER(P)]),
     "imsrg_solver_history": (I, [P, I, IP, DP, DP, DP, DP, IP]),
     "imsrg_solver_transform": (I, [P, P, P, I, P]),
     "imsrg_solver_inverse_transform": (I, [P, P, P, I, P]),

@@ -289,16 +289,17 @@ class DeviceOperator:
             self.size = ms.tensor_size(*self.rank)
 
     @classmethod
-    def _view(cls, ms, handle, owner):
-        """An operator owned by another object (a solver's H(s), Eta, Omega)."""
+    def _view(cls, ms, handle, owner, rank=(0, 0, 0)):
+        """An operator owned by another object (a solver's H(s), Eta, Omega,
+        added operators)."""
         d = cls.__new__(cls)
         d.modelspace = ms
         d._L = _lib.lib()
         d._owned = False
         d._owner = owner
         d._h = handle
-        d.rank = (0, 0, 0)
-        d.size = ms.arena_size
+        d.rank = tuple(int(x) for x in rank)
+        d.size = ms.arena_size if d.rank == (0, 0, 0) else ms.tensor_size(*d.rank)
         return d
 
     @classmethod
@@ -820,6 +821,27 @@ class IMSRGSolver:
         h = ctypes.c_void_p()
         check(self._L.imsrg_solver_omega(self._h, int(i), ctypes.byref(h)))
         return DeviceOperator._view(self.modelspace, h, self)
+
+    def AddOperator(self, op):
+        """IMSRGSolver::AddOperator: a copy of op (scalar or reduced tensor)
+        joins the flowing operators (flow_RK4 flows it with H(s)); returns
+        its index for GetOperator."""
+        rank = getattr(op, "rank", (0, 0, 0))
+        idx = ctypes.c_int()
+        with DeviceOperator.from_host(op) as d:
+            check(self._L.imsrg_solver_add_operator(self._h, d._h, ctypes.byref(idx), None))
+        self._ranks = getattr(self, "_ranks", [(0, 0, 0)]) + [tuple(rank)]
+        return idx.value
+
+    def device_operator(self, i):
+        h = ctypes.c_void_p()
+        check(self._L.imsrg_solver_get_operator(self._h, int(i), ctypes.byref(h)))
+        ranks = getattr(self, "_ranks", [(0, 0, 0)])
+        return DeviceOperator._view(self.modelspace, h, self, ranks[i] if 0 <= i < len(ranks) else (0, 0, 0))
+
+    def GetOperator(self, i):
+        """IMSRGSolver::GetOperator: flowing operator i (0 is H(s))."""
+        return self.device_operator(i).to_host()
 
     def GetH_s(self):
         return self.device_hs().to_host()

@@ -195,6 +195,13 @@ struct imsrg_solver {
   imsrg_op* Htemp = nullptr;  // modified Euler's predicted H; RK4's stage H
   imsrg_op* Kstage = nullptr;  // RK4: [eta, H] of the current stage
   imsrg_op* Ksum = nullptr;    // RK4: K1 + 2 K2 + 2 K3 + K4
+  // IMSRGSolver::AddOperator (src/IMSRGSolver.hh:94): flowing operators after
+  // H(s), copies owned by the solver, each with RK4's stage operator, stage
+  // [eta, O] and stage sum (allocated by the first RK4 solve)
+  struct Flowing {
+    imsrg_op *op = nullptr, *tmp = nullptr, *k = nullptr, *sum = nullptr;
+  };
+  std::vector<Flowing> flowing;
 
   ~imsrg_solver()
   {
@@ -204,6 +211,12 @@ struct imsrg_solver {
     imsrg_op_destroy(Htemp);
     imsrg_op_destroy(Kstage);
     imsrg_op_destroy(Ksum);
+    for (Flowing& f : flowing) {
+      imsrg_op_destroy(f.op);
+      imsrg_op_destroy(f.tmp);
+      imsrg_op_destroy(f.k);
+      imsrg_op_destroy(f.sum);
+    }
     for (imsrg_op* o : omega) imsrg_op_destroy(o);
     for (const std::string& f : files) std::remove(f.c_str());  // CleanupScratch
   }
@@ -399,10 +412,27 @@ int solve_magnus_backoff(imsrg_solver* sv, int prec, cudaStream_t st)
   return IMSRG_OK;
 }
 
+// an operator of src's kind (scalar, or a reduced tensor of src's rank)
+int create_like(const imsrg_op* src, imsrg_op** out)
+{
+  if (src->tl)
+    return imsrg_op_create_tensor(src->sp, src->tl->lam, src->tl->trank, src->tl->parity, src->herm, out);
+  return imsrg_op_create(src->sp, src->herm, out);
+}
+
+// [eta, O] for a scalar or tensor O, Commutator::Commutator's dispatch
+// (src/Commutator.cc:106-160)
+int flow_commutator(const imsrg_op* eta, const imsrg_op* O, imsrg_op* Z, int prec, cudaStream_t st)
+{
+  if (O->tl) return imsrg_commutator_scalar_tensor(eta, O, Z, prec, st);
+  return commutator_dev(eta, O, Z, prec, st);
+}
+
 // IMSRGSolver::Solve_flow_RK4, src/IMSRGSolver.cc:505-636: the classical
 // fixed-step RK4 rule for dH/ds = [eta(H), H] with steps of ds_max (the last
 // one cut to end at smax), the generator re-evaluated at every stage's H;
-// no Omega, one flowing operator, no goose-tank term (BCH's
+// the operators added with AddOperator flow with the same stage generators
+// (evaluated from H's stages only); no Omega, no goose-tank term (BCH's
 // use_goose_tank_correction is off by default)
 int solve_flow_rk4(imsrg_solver* sv, int prec, cudaStream_t st)
 {
@@ -411,6 +441,18 @@ int solve_flow_rk4(imsrg_solver* sv, int prec, cudaStream_t st)
   if (!sv->Htemp) FLOW_TRY(imsrg_op_create(sv->sp, 1, &sv->Htemp));
   if (!sv->Kstage) FLOW_TRY(imsrg_op_create(sv->sp, 1, &sv->Kstage));
   if (!sv->Ksum) FLOW_TRY(imsrg_op_create(sv->sp, 1, &sv->Ksum));
+  for (imsrg_solver::Flowing& f : sv->flowing) {
+    if (!f.tmp) FLOW_TRY(create_like(f.op, &f.tmp));
+    if (!f.k) FLOW_TRY(create_like(f.op, &f.k));
+    if (!f.sum) FLOW_TRY(create_like(f.op, &f.sum));
+  }
+  // operator i of the flow: H(s) (i = 0) or an added one, with its stage
+  // operator, stage [eta, O] and stage sum
+  const size_t nops = sv->flowing.size() + 1;
+  auto ops = [&](size_t i) {
+    if (i == 0) return imsrg_solver::Flowing{sv->Hs, sv->Htemp, sv->Kstage, sv->Ksum};
+    return sv->flowing[i - 1];
+  };
   // weight of stage k's K in the sum, and the step fraction of the H that
   // feeds stage k + 1 (H + ds/2 K1, H + ds/2 K2, H + ds K3)
   const double wsum[4] = {1.0, 2.0, 2.0, 1.0};
@@ -423,18 +465,21 @@ int solve_flow_rk4(imsrg_solver* sv, int prec, cudaStream_t st)
     sv->ds = std::min(sv->ds_max, sv->smax - sv->s);
     sv->s += sv->ds;
     for (int k = 0; k < 4; ++k) {
-      FLOW_TRY(commutator_dev(sv->Eta, k == 0 ? sv->Hs : sv->Htemp, sv->Kstage, prec, st));
-      if (k == 0)
-        FLOW_TRY(imsrg_op_copy(sv->Ksum, sv->Kstage, st));
-      else
-        FLOW_TRY(imsrg_op_axpy(sv->Ksum, wsum[k], sv->Kstage, st));
-      if (k < 3) {
-        FLOW_TRY(imsrg_op_copy(sv->Htemp, sv->Hs, st));
-        FLOW_TRY(imsrg_op_axpy(sv->Htemp, shift[k] * sv->ds, sv->Kstage, st));
-        FLOW_TRY(generator_impl(sv->Htemp, sv->Eta, sv->gen, st));
+      for (size_t i = 0; i < nops; ++i) {
+        const imsrg_solver::Flowing f = ops(i);
+        FLOW_TRY(flow_commutator(sv->Eta, k == 0 ? f.op : f.tmp, f.k, prec, st));
+        if (k == 0)
+          FLOW_TRY(imsrg_op_copy(f.sum, f.k, st));
+        else
+          FLOW_TRY(imsrg_op_axpy(f.sum, wsum[k], f.k, st));
+        if (k < 3) {
+          FLOW_TRY(imsrg_op_copy(f.tmp, f.op, st));
+          FLOW_TRY(imsrg_op_axpy(f.tmp, shift[k] * sv->ds, f.k, st));
+        }
       }
+      if (k < 3) FLOW_TRY(generator_impl(sv->Htemp, sv->Eta, sv->gen, st));
     }
-    FLOW_TRY(imsrg_op_axpy(sv->Hs, sv->ds / 6.0, sv->Ksum, st));
+    for (size_t i = 0; i < nops; ++i) FLOW_TRY(imsrg_op_axpy(ops(i).op, sv->ds / 6.0, ops(i).sum, st));
     FLOW_TRY(generator_impl(sv->Hs, sv->Eta, sv->gen, st));
     const double e0 = zero_body(sv->Hs, st, &rc);
     if (rc) return rc;
@@ -629,6 +674,32 @@ int imsrg_solver_eta(imsrg_solver* sv, imsrg_op** out)
 {
   if (!sv || !out) return err(IMSRG_ERR_ARG, "bad arguments");
   *out = sv->Eta;
+  return IMSRG_OK;
+}
+
+int imsrg_solver_add_operator(imsrg_solver* sv, const imsrg_op* op, int* index, void* stream)
+{
+  if (!sv || !op) return err(IMSRG_ERR_ARG, "bad arguments");
+  if (op->sp != sv->sp) return err(IMSRG_ERR_ARG, "the operator belongs to another model space");
+  imsrg_solver::Flowing f;
+  FLOW_TRY(create_like(op, &f.op));
+  // the copy is complete on return, so the caller may free op
+  int rc = imsrg_op_copy(f.op, op, S_(stream));
+  if (!rc && cudaStreamSynchronize(S_(stream)) != cudaSuccess) rc = err(IMSRG_ERR_CUDA, "operator copy failed");
+  if (rc) {
+    imsrg_op_destroy(f.op);
+    return rc;
+  }
+  sv->flowing.push_back(f);
+  if (index) *index = (int)sv->flowing.size();
+  return IMSRG_OK;
+}
+
+int imsrg_solver_get_operator(imsrg_solver* sv, int i, imsrg_op** out)
+{
+  if (!sv || !out) return err(IMSRG_ERR_ARG, "bad arguments");
+  if (i < 0 || i > (int)sv->flowing.size()) return err(IMSRG_ERR_ARG, "operator index out of range");
+  *out = i == 0 ? sv->Hs : sv->flowing[i - 1].op;
   return IMSRG_OK;
 }
 

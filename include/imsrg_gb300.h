@@ -407,6 +407,15 @@ int imsrg_solver_solve(imsrg_solver* solver, int precision, void* stream);
 int imsrg_solver_hs(imsrg_solver* solver, imsrg_op** out);
 int imsrg_solver_eta(imsrg_solver* solver, imsrg_op** out);
 int imsrg_solver_omega(imsrg_solver* solver, int i, imsrg_op** out);
+/* IMSRGSolver::AddOperator / GetOperator (src/IMSRGSolver.hh:94-95): a copy
+ * of op (scalar or reduced tensor, of the solver's model space) joins the
+ * flowing operators (the copy is complete on return); *index (may be NULL)
+ * receives its index.  Operator 0 is
+ * H(s).  flow_RK4 flows every added operator with the stage generators of
+ * H(s); the Magnus methods leave them as added, as the reference does (their
+ * observables go through imsrg_solver_transform). */
+int imsrg_solver_add_operator(imsrg_solver* solver, const imsrg_op* op, int* index, void* stream);
+int imsrg_solver_get_operator(imsrg_solver* solver, int i, imsrg_op** out);
 /* Flow record, one entry per step of every solve (WriteFlowStatus columns,
  * src/IMSRGSolver.cc:1206-1231): step, s, H(s).ZeroBody, |eta| and |Omega|
  * before the step.  Arrays may be NULL; *n receives the number of entries,

@@ -337,18 +337,26 @@ static int flow_main(int argc, char** argv) {
   struct MethodCase { const char* name; const char* method; };
   const MethodCase methods[] = {
       {"flow_me", "magnus_modified_euler"}, {"flow_bo", "magnus_backoff"}, {"flow_rk4", "flow_RK4"}};
+  // flow_RK4 also flows an added observable, the hermitian [A, H]
+  Operator obs = Commutator::Commutator(A, H);
   for (const MethodCase& mc : methods) {
+    const bool rk4 = std::string(mc.method) == "flow_RK4";
     IMSRGSolver solver(H);
     solver.SetGenerator("white");
     solver.SetMethod(mc.method);
     solver.SetOmegaNormMax(0.3);
     solver.SetEtaCriterion(1e-20);
     solver.SetSmax(2.0);
+    if (rk4) solver.AddOperator(obs);
     solver.Solve();
     std::ofstream f(outdir + "/" + mc.name + ".txt");
     f << std::setprecision(17) << solver.GetS() << " " << solver.GetOmegaSize() << " " << solver.GetH_s().ZeroBody
       << "\n";
     write_file(outdir + "/" + mc.name + "_Hs.bin", store(solver.GetH_s(), L));
+    if (rk4) {
+      write_file(outdir + "/flow_rk4_obs_in.bin", store(obs, L));
+      write_file(outdir + "/flow_rk4_obs.bin", store(solver.GetOperator(1), L));
+    }
   }
   return 0;
 }

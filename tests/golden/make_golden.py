@@ -31,7 +31,8 @@ Fixtures (arena layout: see oracle/modelspace_ref.py):
                      H(s), last Omega); the same flow with the
                      magnus_modified_euler and magnus_backoff methods, and
                      the fixed-step flow_RK4 flow of H (final s, number of
-                     Omegas, E0 and H(s)).
+                     Omegas, E0 and H(s)); flow_RK4 also flows an added
+                     observable [A, H] (AddOperator; the input and GetOperator(1)).
   golden_tensor_emax2.npz, golden_tensor_emax3.npz
                      Commutator::CommutatorScalarTensor [X, T] and its five
                      IMSRG(2) terms (comm111st, comm121st, comm122st,
@@ -127,7 +128,8 @@ def run_reference_flow(emax):
                        env=dict(os.environ, OMP_NUM_THREADS="1"))
         out = {"H": H, "A": A, "B": B, "emax": np.array(emax), "v2": np.array(FLOW_V2)}
         for k in ("bchp", "bchp_big", "eta_white", "eta_atan", "eta_white_mp", "flow_Hs", "flow_Omega", "flow2_Hs",
-                  "flow2_Omega", "flow_me_Hs", "flow_bo_Hs", "flow_rk4_Hs", "eta_qt", "eta_qt2"):
+                  "flow2_Omega", "flow_me_Hs", "flow_bo_Hs", "flow_rk4_Hs", "flow_rk4_obs_in", "flow_rk4_obs",
+                  "eta_qt", "eta_qt2"):
             out[k] = np.fromfile(os.path.join(td, k + ".bin"))
         out["flow_steps"] = np.loadtxt(os.path.join(td, "flow_steps.txt"))
         out["flow2"] = np.loadtxt(os.path.join(td, "flow2.txt"))
