@@ -74,3 +74,36 @@ def test_oracle_flow_resumes():
     b = o.magnus_euler(g["H"], p, state=a)
     assert a["steps"] + b["steps"] == one["steps"] == 5
     assert np.array_equal(b["Hs"], one["Hs"])
+
+
+@pytest.mark.parametrize("emax", [2, 3])
+def test_oracle_rk4_flow_matches_reference(emax):
+    # IMSRGSolver::Solve_flow_RK4 (src/IMSRGSolver.cc:505-636) restated over
+    # the oracle's commutator and White generator: four RK4 steps of ds_max
+    # = 0.5 to s = 2, flowing H and the added observable [A, H] with the
+    # stage generators of H
+    g = load_flow_golden(emax)
+    o = Oracle(emax)
+    s_ref, n_omega_ref, e0_ref = g["flow_rk4"]
+    H, O = g["H"].copy(), g["flow_rk4_obs_in"].copy()
+    s, ds = 0.0, 0.5
+    eta = o.generator(H)
+    while s < 2.0:
+        assert o.norm(eta) >= 1e-20
+        ds = min(0.5, 2.0 - s)
+        s += ds
+        sums = [np.zeros_like(H), np.zeros_like(O)]
+        stage = [H, O]
+        for wk, sk in zip((1.0, 2.0, 2.0, 1.0), (0.5, 0.5, 1.0, None)):
+            K = [o.commutator(eta, X, -1, 1) for X in stage]
+            sums = [acc + wk * k for acc, k in zip(sums, K)]
+            if sk is not None:
+                stage = [X0 + sk * ds * k for X0, k in zip((H, O), K)]
+                eta = o.generator(stage[0])
+        H = H + ds / 6.0 * sums[0]
+        O = O + ds / 6.0 * sums[1]
+        eta = o.generator(H)
+    assert s == s_ref and int(n_omega_ref) == 1
+    assert abs(H[0] - e0_ref) <= 1e-12 * abs(e0_ref)
+    assert max(rel_errors(o.ms, H, g["flow_rk4_Hs"])) < 1e-12
+    assert max(rel_errors(o.ms, O, g["flow_rk4_obs"])) < 1e-12
