@@ -832,7 +832,7 @@ __device__ __forceinline__ double tinv_dot(const DevSpace& S, const DevTensor& T
 // by exactly one quadruple and slot, so there are no write conflicts.
 constexpr int kTqWarps = 8;
 
-__global__ void __launch_bounds__(32 * kTqWarps, 4) k_tinv_q(DevSpace S, DevTensor T, const double* __restrict__ Zb,
+__global__ void __launch_bounds__(32 * kTqWarps, 6) k_tinv_q(DevSpace S, DevTensor T, const double* __restrict__ Zb,
                                                          int hZ, double* __restrict__ Z,
                                                          const int2* __restrict__ tq, long long nq, int slots)
 {
