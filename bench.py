@@ -74,6 +74,8 @@ def parse_args():
     p.add_argument("--pairs", type=int, default=64, help="batch workload: independent (X, Y) pairs")
     p.add_argument("--batch-emax", type=int, default=None, help="batch workload: every pair at this emax")
     p.add_argument("--fp64-steps", type=int, default=None, help="flow steps timed in the FP64 form")
+    p.add_argument("--cpu-flow-steps", type=int, default=1,
+                   help="flow workload: steps of the C oracle's flow compared with the GPU flows' zero-body value")
     p.add_argument("--precision", default="split", choices=["split", "fp64"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -235,28 +237,79 @@ def kernel_work(name, w):
     return None
 
 
-def cpu_oracle_rate(emax, seconds, threads):
-    """The C oracle on `threads` host threads: commutators/s over a bounded sample."""
-    code = r"""
+def rank_errors(a, b, norb):
+    """Relative Frobenius difference per body rank (zero-, one-, two-body) of
+    arena a against arena b."""
+    import numpy as np
+    N = norb
+    o2 = (32 + N * N + 31) // 32 * 32
+    out = {}
+    for name, x, y in (("zero_body", a[:1], b[:1]), ("one_body", a[32:32 + N * N], b[32:32 + N * N]),
+                       ("two_body", a[o2:], b[o2:])):
+        ny = float(np.linalg.norm(y))
+        out[name] = float(np.linalg.norm(x - y) / ny) if ny > 0 else float(np.linalg.norm(x - y))
+    return out
+
+
+# The CPU leg (rank 0, N=1): the C oracle, a restatement of the reference's
+# OpenMP + BLAS path, run in a child process on all host cores.  It evaluates
+# [X, Y] and BCH_Transform(X, c Y) on the benchmark's own operators (read from
+# .npy files), which serves twice: as the reference result the GPU results are
+# checked against per body rank, and as the timed CPU baseline (a bounded
+# sample of commutators, one BCH step).
+CPU_LEG = r"""
 import sys, time, json
-sys.path.insert(0, %r)
+import numpy as np
+sys.path.insert(0, %(oracle)r)
+sys.path.insert(0, %(root)r)
 from oracle import Oracle
-o = Oracle(%d)
-X = o.ms.random_operator(1, True); Y = o.ms.random_operator(2, False)
-o.commutator(X, Y, 1, -1)
-n = 0; t0 = time.perf_counter()
-while True:
+from bench import rank_errors
+d = %(dir)r
+o = Oracle(%(emax)d)
+N = o.ms.norb
+X = np.load(d + "/X.npy"); Y = np.load(d + "/Y.npy")
+t0 = time.perf_counter()
+R = o.commutator(X, Y, 1, -1)
+t_first = time.perf_counter() - t0
+out = {"threads": o.num_threads(), "rel_err_vs_oracle": {}}
+for form in ("split", "fp64"):
+    out["rel_err_vs_oracle"][form] = rank_errors(np.load(d + "/Z_%%s.npy" %% form), R, N)
+del R
+n = 1; t = t_first
+t0 = time.perf_counter()
+while t < %(seconds)f and n < 50:
     o.commutator(X, Y, 1, -1); n += 1
-    t = time.perf_counter() - t0
-    if t >= %f or n >= 50: break
-print(json.dumps({"n": n, "t": t, "threads": o.num_threads()}))
-""" % (os.path.join(ROOT, "oracle"), emax, seconds)
-    env = dict(os.environ, OMP_NUM_THREADS=str(threads), OPENBLAS_NUM_THREADS="1", OMP_PROC_BIND="false")
-    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=1800)
+    t = t_first + time.perf_counter() - t0
+out["n"] = n; out["t"] = t
+c = float(np.load(d + "/c.npy"))
+if c > 0:
+    t0 = time.perf_counter()
+    B, it = o.bch_transform(X, 1, c * Y, -1)
+    out["bch_ms"] = 1000.0 * (time.perf_counter() - t0)
+    out["bch_nested"] = int(it)
+    out["bch_rel_err_vs_oracle"] = {}
+    for form in ("split", "fp64"):
+        out["bch_rel_err_vs_oracle"][form] = rank_errors(np.load(d + "/B_%%s.npy" %% form), B, N)
+print(json.dumps(out))
+"""
+
+
+def cpu_leg(emax, seconds, threads, arrays):
+    """Run CPU_LEG on the arrays (dict name -> numpy array, written as .npy to
+    a temporary directory); returns its JSON result."""
+    import tempfile
+
+    import numpy as np
+    with tempfile.TemporaryDirectory() as td:
+        for name, a in arrays.items():
+            np.save(os.path.join(td, name + ".npy"), a)
+        code = CPU_LEG % {"oracle": os.path.join(ROOT, "oracle"), "root": ROOT, "dir": td, "emax": emax,
+                          "seconds": seconds}
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads), OPENBLAS_NUM_THREADS="1", OMP_PROC_BIND="false")
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=3600)
     if r.returncode != 0:
         raise RuntimeError("CPU oracle failed: " + r.stderr[-500:])
-    d = json.loads(r.stdout.strip().splitlines()[-1])
-    return d["n"] / d["t"], d["threads"], d["n"]
+    return json.loads(r.stdout.strip().splitlines()[-1])
 
 
 # --------------------------------------------------------------- arms
@@ -357,7 +410,101 @@ def e2e_streamed(ig, ms, prec, hX, hY, hZ, steps, barrier, max_ms):
     return max_ms(ms_total)
 
 
+def timed_steps(step, steps, barrier, max_ms):
+    """CUDA-event time (ms, max over ranks) of `steps` calls of step(), with an
+    event after every step; returns (total, per-step list)."""
+    import torch
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    barrier()
+    ev[0].record()
+    for k in range(steps):
+        step()
+        ev[k + 1].record()
+    torch.cuda.synchronize()
+    barrier()
+    per = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
+    return max_ms(ev[0].elapsed_time(ev[-1])), per
+
+
+def profiled_phases(L, step, nsteps):
+    """The library's per-phase CUDA-event timers over nsteps calls of step()
+    (a separate pass: the headline timing runs with the timers off)."""
+    import torch
+    torch.cuda.synchronize()
+    L.imsrg_profiler_reset()
+    L.imsrg_profiler_enable(1)
+    for _ in range(nsteps):
+        step()
+    torch.cuda.synchronize()
+    L.imsrg_profiler_enable(0)
+    n = L.imsrg_profiler_names(None, 0)
+    buf = ctypes.create_string_buffer(n)
+    L.imsrg_profiler_names(buf, n)
+    phases = {}
+    for name in [x for x in buf.value.decode().split("\n") if x]:
+        t = ctypes.c_double()
+        c = ctypes.c_longlong()
+        L.imsrg_profiler_get(name.encode(), ctypes.byref(t), ctypes.byref(c))
+        phases[name] = (t.value, c.value)
+    return phases
+
+
+def roofline(phases, work, emax):
+    """Roofline entry of the dominant profiled phase."""
+    hbm_peak, bf16_peak, peak_src = measured_peaks()
+    best = None
+    for name, (tot, cnt) in phases.items():
+        kw = kernel_work(name, work)
+        if kw and cnt and (best is None or tot > phases[best][0]):
+            best = name
+    if not best:
+        return None
+    bound, amount, unit = kernel_work(best, work)
+    avg_s = phases[best][0] / phases[best][1] / 1000.0
+    if bound == "tensor":
+        ach = amount / avg_s / 1e12
+        roof = {"kernel": best, "bound": "tensor", "achieved": ach, "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": ach / bf16_peak, "traffic": None,
+                "issued_bf16_tflops": 21 * ach, "issued_frac": 21 * ach / bf16_peak,
+                "note": "achieved counts FP64-equivalent algorithmic flops (the digit products issue 21x "
+                        "as many BF16 flops); peak = bf16 dense burst, %s" % peak_src}
+    else:
+        ach = amount / avg_s / 1e9
+        roof = {"kernel": best, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                "frac": ach / hbm_peak, "traffic": None, "note": "peak = HBM copy, %s" % peak_src}
+    roof["launch_ms"] = avg_s * 1000.0
+    if "CommutatorScalarScalar" in phases:
+        roof["share"] = phases[best][0] / max(1e-9, phases["CommutatorScalarScalar"][0])
+    tr = profiled_traffic(best, emax)
+    if tr:
+        roof["traffic"] = tr[0]
+        roof["traffic_source"] = "dram__bytes_read.sum + dram__bytes_write.sum per launch, ncu capture of " \
+                                 "the same kernel at this emax, summarised in " + tr[1]
+    return roof
+
+
+def calibrate_omega(ig, dX, dY, dOut, prec, lo=10, hi=20):
+    """Scale c of Omega = c Y / |Y| for which BCH_Transform(X, Omega) runs a
+    number of nested commutators in [lo, hi] (geometric search on |Omega|);
+    returns (|Omega|, nested)."""
+    ny = dY.norm()
+    best = None
+    t = 2.0
+    for _ in range(16):
+        with ig.DeviceOperator(dY.modelspace, -1) as dOm:
+            dOm.copy_from(dY)
+            dOm.scale(t / ny)
+            n = ig.BCH.device_transform(dX, dOm, dOut, prec)
+        if best is None or abs(n - (lo + hi) / 2) < abs(best[1] - (lo + hi) / 2):
+            best = (t, n)
+        if lo <= n <= hi:
+            break
+        t = t * 1.6 if n < lo else t / 1.3
+    return best
+
+
 def run_gb300(args):
+    import numpy as np
     import torch
 
     import imsrg_gb300 as ig
@@ -375,6 +522,9 @@ def run_gb300(args):
     dX.fill_random(sx)
     dY.fill_random(sy)
     prec = args.precision
+    # commutators queue on the stream without a host round trip each; the
+    # kernels' status word is read once per timed region
+    ms.defer_status(True)
 
     def step(p=prec):
         ig.Commutator.device_commutator(dX, dY, dZ, p)
@@ -388,89 +538,66 @@ def run_gb300(args):
     def max_ms(x):
         return max_over_ranks(x, device="cuda")
 
-    for _ in range(max(args.warmup, 3)):
+    warm = max(args.warmup, 3)
+    for _ in range(warm):
         step()
+    ms.check_status()
     barrier()
-    # ---- timed region (device-resident operands)
+    # ---- timed region: device-resident operands, phase timers off
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    L.imsrg_profiler_reset()
-    L.imsrg_profiler_enable(1)
     launches0 = L.imsrg_kernel_launches()
-    barrier()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        step()
-    e1.record()
-    torch.cuda.synchronize()
-    barrier()
+    elapsed_ms, per_step = timed_steps(step, args.steps, barrier, max_ms)
     launches = L.imsrg_kernel_launches() - launches0
-    L.imsrg_profiler_enable(0)
     clocks.stop()
-    elapsed_ms = max_ms(e0.elapsed_time(e1))
+    ms.check_status()
     value = whole_job_value(world, args.steps, elapsed_ms)
-    # per-phase CUDA-event timers over the timed region
-    n = L.imsrg_profiler_names(None, 0)
-    buf = ctypes.create_string_buffer(n)
-    L.imsrg_profiler_names(buf, n)
-    phases = {}
-    for name in [x for x in buf.value.decode().split("\n") if x]:
-        t = ctypes.c_double()
-        c = ctypes.c_longlong()
-        L.imsrg_profiler_get(name.encode(), ctypes.byref(t), ctypes.byref(c))
-        phases[name] = (t.value, c.value)
-    # ---- roofline of the dominant kernel
+    # ---- per-phase CUDA-event timers: a separate pass over the same steps
+    nprof = max(1, min(args.steps, 10))
+    phases = profiled_phases(L, step, nprof)
+    ms.check_status()
     work = algorithmic_work(ms)
-    hbm_peak, bf16_peak, peak_src = measured_peaks()
-    roof = None
-    best = None
-    for name, (tot, cnt) in phases.items():
-        kw = kernel_work(name, work)
-        if kw and cnt and (best is None or tot > phases[best][0]):
-            best = name
-    if best:
-        bound, amount, unit = kernel_work(best, work)
-        avg_s = phases[best][0] / phases[best][1] / 1000.0
-        if bound == "tensor":
-            ach = amount / avg_s / 1e12
-            roof = {"kernel": best, "bound": "tensor", "achieved": ach, "peak": bf16_peak, "unit": "TFLOP/s",
-                    "frac": ach / bf16_peak, "traffic": None,
-                    "issued_bf16_tflops": 21 * ach, "issued_frac": 21 * ach / bf16_peak,
-                    "note": "achieved counts FP64-equivalent algorithmic flops (the digit products issue 21x "
-                            "as many BF16 flops); peak = bf16 dense, %s" % peak_src}
-        else:
-            ach = amount / avg_s / 1e9
-            roof = {"kernel": best, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
-                    "frac": ach / hbm_peak, "traffic": None, "note": "peak = HBM copy, %s" % peak_src}
-        roof["share"] = phases[best][0] / max(1e-9, phases["CommutatorScalarScalar"][0]) \
-            if "CommutatorScalarScalar" in phases else None
-        tr = profiled_traffic(best, args.emax)
-        if tr:
-            roof["traffic"] = tr[0]
-            roof["traffic_source"] = "dram__bytes_read.sum + dram__bytes_write.sum per launch, ncu, " + tr[1]
+    roof = roofline(phases, work, args.emax)
+    Zs = dZ.download()  # the split result of the timed region's inputs
     # ---- plain FP64 form (the metric compares split vs FP64)
     fp64 = None
+    Zf = None
     if prec == "split":
-        Zs = dZ.download()  # the split result of the timed region's inputs
         step("fp64")
         Zf = dZ.download()
-        fp64_err = split_vs_fp64(ms, Zs, Zf)
-        del Zs, Zf
-        barrier()
-        f0 = torch.cuda.Event(enable_timing=True)
-        f1 = torch.cuda.Event(enable_timing=True)
+        fp64_err = rank_errors(Zs, Zf, ms.norb)
         nf = 3
-        f0.record()
-        for _ in range(nf):
-            step("fp64")
-        f1.record()
-        torch.cuda.synchronize()
-        fms = max_ms(f0.elapsed_time(f1)) / nf
+        fms, _ = timed_steps(lambda: step("fp64"), nf, barrier, max_ms)
+        fms /= nf
         fp64 = {"value": world * 1000.0 / fms, "unit": UNIT, "ms_per_step": fms, "steps": nf,
                 "split_vs_fp64_rel_err": fp64_err}
+    # ---- ms per BCH step: BCH_Transform(X, Omega), Omega = c Y with |Omega|
+    # chosen so that 10-20 nested commutators run
+    bch = None
+    Bs = Bf = None
+    c_omega = 0.0
+    if prec == "split":
+        with ig.DeviceOperator(ms, 1) as dB, ig.DeviceOperator(ms, -1) as dOm:
+            om_norm, _ = calibrate_omega(ig, dX, dY, dB, "split")
+            c_omega = om_norm / dY.norm()
+            dOm.copy_from(dY)
+            dOm.scale(c_omega)
+            bch = {"omega_norm": om_norm, "h_norm": dX.norm()}
+            for form, reps in (("split", 3), ("fp64", 1)):
+                ig.BCH.device_transform(dX, dOm, dB, form)  # warm-up
+                nested = []
+
+                def bstep(f=form):
+                    nested.append(ig.BCH.device_transform(dX, dOm, dB, f))
+                bms, _ = timed_steps(bstep, reps, barrier, max_ms)
+                bch[form] = {"ms_per_bch_step": bms / reps, "nested_commutators": nested[-1], "steps": reps}
+                if form == "split":
+                    Bs = dB.download()
+                else:
+                    Bf = dB.download()
+        bch["split_vs_fp64_rel_err"] = rank_errors(Bs, Bf, ms.norb)
+        bch["fp64_over_split"] = bch["fp64"]["ms_per_bch_step"] / bch["split"]["ms_per_bch_step"]
     # ---- end to end: host buffers, H2D + commutator + D2H per step, through the C ABI
     A = ms.arena_size
     hX = torch.empty(A, dtype=torch.float64, pin_memory=True)
@@ -479,22 +606,17 @@ def run_gb300(args):
     dX.download_ptr(hX.data_ptr())
     dY.download_ptr(hY.data_ptr())
     ne = max(1, min(args.steps, 10))
-    # serial: upload, commutator, download, one step after the other
-    barrier()
-    g0 = torch.cuda.Event(enable_timing=True)
-    g1 = torch.cuda.Event(enable_timing=True)
-    g0.record()
-    for _ in range(ne):
+
+    def serial_step():
         dX.upload_ptr(hX.data_ptr())
         dY.upload_ptr(hY.data_ptr())
         step()
         dZ.download_ptr(hZ.data_ptr())
-    g1.record()
-    torch.cuda.synchronize()
-    serial_ms = max_ms(g0.elapsed_time(g1))
+    serial_ms, _ = timed_steps(serial_step, ne, barrier, max_ms)
     # streamed: independent commutators with two operator sets; step k+1's
     # upload and step k-1's download overlap step k's commutator
     pipe_ms = e2e_streamed(ig, ms, prec, hX, hY, hZ, ne, barrier, max_ms)
+    ms.check_status()
     ems = min(serial_ms, pipe_ms)
     e2e = {"value": world * ne / (ems / 1000.0), "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * A,
            "d2h_bytes_per_step": 8 * A,
@@ -507,32 +629,51 @@ def run_gb300(args):
         if world > 1:
             torch.distributed.destroy_process_group()
         return
-    # ---- CPU baseline (rank 0, N=1 only)
+    # ---- CPU leg (rank 0, N=1 only): baseline and the oracle check
     cpu = None
+    oracle_err = None
     if world == 1 and not args.no_cpu_baseline:
         try:
             threads = os.cpu_count() or 1
-            rate, used, nsamp = cpu_oracle_rate(args.emax, args.cpu_seconds, threads)
-            cpu = {"value": rate, "unit": UNIT, "cores": used, "kind": "port",
-                   "sample": "%d commutator(s) at emax=%d, C oracle (OpenMP over channels + SciPy BLAS dgemm)"
-                             % (nsamp, args.emax)}
+            arrays = {"X": hX.numpy(), "Y": hY.numpy(), "Z_split": Zs,
+                      "Z_fp64": Zf if Zf is not None else Zs, "c": np.array(c_omega)}
+            if Bs is not None:
+                arrays.update(B_split=Bs, B_fp64=Bf)
+            d = cpu_leg(args.emax, args.cpu_seconds, threads, arrays)
+            cpu = {"value": d["n"] / d["t"], "unit": UNIT, "cores": d["threads"], "kind": "port",
+                   "sample": "%d commutator(s) at emax=%d on the benchmark's X, Y, C oracle (OpenMP over channels + "
+                             "SciPy BLAS dgemm)" % (d["n"], args.emax)}
+            if "bch_ms" in d:
+                cpu["ms_per_bch_step"] = d["bch_ms"]
+                cpu["bch_nested_commutators"] = d["bch_nested"]
+                bch["cpu"] = {"ms_per_bch_step": d["bch_ms"], "nested_commutators": d["bch_nested"],
+                              "cores": d["threads"], "kind": "port"}
+                bch["rel_err_vs_oracle"] = d["bch_rel_err_vs_oracle"]
+            oracle_err = d["rel_err_vs_oracle"]
         except Exception as ex:  # reported, not fatal
             cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": "failed: %s" % ex}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": max(args.warmup, 3), "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+        "warmup": warm, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD.format(emax=args.emax), "emax": args.emax, "orbits": ms.norb,
                    "largest_2b_channel": max(c["nkets"] for c in ms.channels), "precision": prec,
                    "gemm": "Ozaki BF16 digits on tcgen05, FP32 accumulate, int64/FP64 recombination"
                    if prec == "split" else "FP64 CUDA cores",
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "working set > L2 every step (X2, Y2 280 MiB each; Zbar 761 MiB)"},
+                   "l2": "working set > L2 every step (X2, Y2 280 MiB each; Zbar 761 MiB)",
+                   "timing": "phase timers off; kernels' status word read once after the K steps"},
+        "step_ms": {"min": min(per_step), "median": statistics.median(per_step), "max": max(per_step)},
         "plain_fp64": fp64,
         "split_vs_fp64_rel_err": fp64["split_vs_fp64_rel_err"] if fp64 else None,
+        "rel_err_vs_oracle": oracle_err,
+        "bch": bch,
+        "bch_ms_per_step": {k: bch[k]["ms_per_bch_step"] for k in ("split", "fp64", "cpu") if k in bch}
+        if bch else None,
         "e2e": e2e,
         "roofline": roof,
-        "phases_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in sorted(phases.items())},
+        "phases_ms_per_step": {k: v[0] / nprof for k, v in sorted(phases.items())},
+        "phases_steps": nprof,
         "cpu_baseline": cpu,
         "clocks": clocks.summary(),
         "gpu_launches": int(launches),
@@ -636,6 +777,7 @@ def run_flow(args):
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         import tempfile
+        ncpu = max(1, args.cpu_flow_steps)
         ha = H.download()
         with tempfile.TemporaryDirectory() as td:
             fn = os.path.join(td, "H.npy")
@@ -648,12 +790,13 @@ sys.path.insert(0, %r)
 from oracle import Oracle, FlowParams
 o = Oracle(%d)
 H = np.load(%r)
-p = FlowParams(ds=0.5, ds_max=0.5, smax=0.5, magnus_adaptive=0, omega_norm_max=1e9, eta_criterion=1e-20)
+p = FlowParams(ds=0.5, ds_max=0.5, smax=0.5 * %d, magnus_adaptive=0, omega_norm_max=1e9, eta_criterion=1e-20)
 t0 = time.perf_counter()
 st = o.magnus_euler(H, p)
 t = time.perf_counter() - t0
-print(json.dumps({"t": t, "steps": st["steps"], "e0": list(st["e0_hist"]), "threads": o.num_threads()}))
-""" % (os.path.join(ROOT, "oracle"), emax, fn)
+print(json.dumps({"t": t, "steps": st["steps"], "e0": list(st["e0_hist"]), "e0_final": float(st["Hs"][0]),
+                  "threads": o.num_threads()}))
+""" % (os.path.join(ROOT, "oracle"), emax, fn, ncpu)
             threads = os.cpu_count() or 1
             env = dict(os.environ, OMP_NUM_THREADS=str(threads), OPENBLAS_NUM_THREADS="1")
             try:
@@ -662,11 +805,19 @@ print(json.dumps({"t": t, "steps": st["steps"], "e0": list(st["e0_hist"]), "thre
                 d = json.loads(r.stdout.strip().splitlines()[-1])
                 e_cpu = d["e0"][0]
                 cpu = {"value": 1000.0 * d["t"] / d["steps"], "unit": "ms/step", "cores": d["threads"],
-                       "kind": "port", "sample": "first flow step at emax=%d, C oracle (OpenMP + SciPy BLAS); "
-                                                 "table setup excluded" % emax,
+                       "kind": "port", "sample": "%d flow step(s) at emax=%d, C oracle (OpenMP + SciPy BLAS); "
+                                                 "table setup excluded" % (d["steps"], emax),
                        "e0_step1": e_cpu,
                        "e0_step1_rel_split": abs(e_split[0] - e_cpu) / abs(e_cpu),
-                       "e0_step1_rel_fp64": abs(e_fp64[0] - e_cpu) / abs(e_cpu)}
+                       "e0_step1_rel_fp64": abs(e_fp64[0] - e_cpu) / abs(e_cpu),
+                       "steps": d["steps"], "e0_final": d["e0_final"]}
+                # the zero-body value after the CPU flow's last step against
+                # each GPU flow after the same step (history entry k holds
+                # H(s).ZeroBody after step k + 1, in both flows)
+                n = d["steps"]
+                for form, e_hist in (("split", e_split), ("fp64", e_fp64)):
+                    if 0 < n <= len(e_hist):
+                        cpu["e0_final_rel_" + form] = abs(e_hist[n - 1] - d["e0_final"]) / abs(d["e0_final"])
             except Exception as ex:  # reported, not fatal
                 cpu = {"value": None, "unit": "ms/step", "kind": "port", "sample": "failed: %s" % ex}
     out = {
@@ -756,20 +907,6 @@ def run_batch(args):
         "split": sp, "plain_fp64": res["fp64"], "gpu_launches": sp["launches_per_step"] * K,
     }
     print(json.dumps(out))
-
-
-def split_vs_fp64(ms, Zs, Zf):
-    """Relative Frobenius difference per body rank (zero-, one-, two-body) of
-    the split and FP64 results of the same commutator."""
-    import numpy as np
-    N = ms.norb
-    o2 = (32 + N * N + 31) // 32 * 32
-    out = {}
-    for name, a, b in (("zero_body", Zs[:1], Zf[:1]), ("one_body", Zs[32:32 + N * N], Zf[32:32 + N * N]),
-                       ("two_body", Zs[o2:], Zf[o2:])):
-        nb = float(np.linalg.norm(b))
-        out[name] = float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a - b))
-    return out
 
 
 TENSOR_METRIC = ("ms per scalar-tensor commutator [X,T], rank (J,dTz,parity)=(2,0,+), emax={emax}: {form} form "

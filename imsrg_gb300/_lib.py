@@ -92,6 +92,10 @@ SIGNATURES = {
     "imsrg_batch_launch": (I, [P, P]),
     "imsrg_batch_sync": (I, [P, P]),
     "imsrg_batch_info": (I, [P, IP, IP, IP, LLP]),
+    "imsrg_space_zbar_layout": (I, [P, I, IP, IP, LLP, LLP]),
+    "imsrg_add_inverse_pandya": (I, [P, P, I, P]),
+    "imsrg_space_defer_status": (I, [P, I]),
+    "imsrg_space_check_status": (I, [P, P]),
     "imsrg_set_default_precision": (I, [I]),
     "imsrg_get_default_precision": (I, [IP]),
     "imsrg_bch_transform": (I, [P, P, P, D, I, IP, P]),

@@ -101,6 +101,17 @@ class ModelSpace:
         except Exception:
             pass
 
+    def defer_status(self, on=True):
+        """Split-precision commutators and terms on this space return without
+        reading the kernels' status word (no stream synchronisation);
+        check_status() reads it once for all of them."""
+        check(self._L.imsrg_space_defer_status(self._h, 1 if on else 0))
+
+    def check_status(self, stream=None):
+        """Synchronise the stream and raise if a kernel reported an error since
+        the last read."""
+        check(self._L.imsrg_space_check_status(self._h, stream))
+
     def GetNumberOrbits(self):
         return self.norb
 

@@ -245,11 +245,16 @@ int ensure_device(imsrg_space* sp)
 {
   std::lock_guard<std::mutex> g(sp->mu);
   if (sp->dev_ready) return IMSRG_OK;
+  int dev = -1;
+  CUDA_TRY(cudaGetDevice(&dev));
   try {
     setup_device_lists(sp);
   } catch (std::exception& e) {
     return fail(IMSRG_ERR_CUDA, std::string("device tables: ") + e.what());
   }
+  sp->device = dev;
+  int rc = noalloc_setup(sp, dev);
+  if (rc) return rc;
   sp->dev_ready = true;
   return IMSRG_OK;
 }
@@ -954,7 +959,7 @@ int imsrg_comm222_pp_hhss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int
 {
   TERM_PROLOGUE
   rc = do_ladder(X, Y, Z, precision, st);
-  if (rc == IMSRG_OK && precision == IMSRG_PREC_SPLIT) rc = check_status(X->sp, st);
+  if (rc == IMSRG_OK && precision == IMSRG_PREC_SPLIT) rc = end_status(X->sp, st);
   return rc;
 }
 
@@ -963,7 +968,7 @@ int imsrg_comm222_pp_hh_221ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z,
   TERM_PROLOGUE
   if ((rc = do_ladder(X, Y, Z, precision, st))) return rc;
   if ((rc = do_221_1b(X, Y, Z, st))) return rc;
-  if (precision == IMSRG_PREC_SPLIT) rc = check_status(X->sp, st);
+  if (precision == IMSRG_PREC_SPLIT) rc = end_status(X->sp, st);
   return rc;
 }
 
@@ -971,15 +976,61 @@ int imsrg_comm222_phss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int pr
 {
   TERM_PROLOGUE
   rc = do_ph(X, Y, Z, precision, st);
-  if (rc == IMSRG_OK && precision == IMSRG_PREC_SPLIT) rc = check_status(X->sp, st);
+  if (rc == IMSRG_OK && precision == IMSRG_PREC_SPLIT) rc = end_status(X->sp, st);
   return rc;
 }
 
 int imsrg_commutator_scalar_scalar(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream)
 {
   int rc = commutator_impl(X, Y, Z, precision, S_(stream));
-  if (rc == IMSRG_OK && precision == IMSRG_PREC_SPLIT) rc = check_status(X->sp, S_(stream));
+  if (rc == IMSRG_OK && precision == IMSRG_PREC_SPLIT) rc = end_status(X->sp, S_(stream));
   return rc;
+}
+
+int imsrg_space_zbar_layout(const imsrg_space* sp, int ch_cc, int* rows, int* cols, long long* offset,
+                            long long* total)
+{
+  if (!sp) return fail(IMSRG_ERR_ARG, "bad arguments");
+  const Space& s = *sp->s;
+  if (total) *total = std::max<int64_t>(1, s.zb_total);
+  if (ch_cc < 0) return IMSRG_OK;
+  if (ch_cc >= s.nch) return fail(IMSRG_ERR_ARG, "channel index out of range");
+  if (rows) *rows = s.cc[ch_cc].n();
+  if (cols) *cols = 2 * s.cc[ch_cc].n();
+  if (offset) *offset = s.zb_off[ch_cc];
+  return IMSRG_OK;
+}
+
+int imsrg_add_inverse_pandya(const double* zbar, imsrg_op* Z, int precision, void* stream)
+{
+  if (!zbar || !Z) return fail(IMSRG_ERR_ARG, "bad arguments");
+  if (Z->tl) return fail(IMSRG_ERR_UNSUPPORTED, "Z must be a scalar operator");
+  if (Z->herm != 1 && Z->herm != -1) return fail(IMSRG_ERR_UNSUPPORTED, "Z must be hermitian or anti-hermitian");
+  if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_SPLIT) return fail(IMSRG_ERR_ARG, "bad precision");
+  imsrg_space* sp = Z->sp;
+  Space& s = *sp->s;
+  cudaStream_t st = S_(stream);
+  ProfScope ps("InversePandyaTransformation", st);
+  if (precision == IMSRG_PREC_SPLIT && sp->n_invq > 0)
+    CUDA_TRY(launch_pandya_inv_ff(s, zbar, Z->d, Z->herm, sp->d_invq, sp->n_invq, sp->d_cls_list, sp->d_cls_off,
+                                  sp->d_cls_sort, s.invq_smem, st));
+  else
+    CUDA_TRY(launch_pandya_inv(s, zbar, Z->d, Z->herm, sp->d_pinv, sp->n_pinv, st));
+  return IMSRG_OK;
+}
+
+int imsrg_space_defer_status(imsrg_space* sp, int defer)
+{
+  if (!sp) return fail(IMSRG_ERR_ARG, "null space");
+  sp->defer_status = defer != 0;
+  return IMSRG_OK;
+}
+
+int imsrg_space_check_status(imsrg_space* sp, void* stream)
+{
+  if (!sp) return fail(IMSRG_ERR_ARG, "null space");
+  if (!sp->dev_ready) return IMSRG_OK;  // nothing has run on the device
+  return check_status(sp, S_(stream));
 }
 
 int imsrg_set_term(const char* name, int on)
@@ -1082,6 +1133,7 @@ int commutator_dev(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, 
 }
 int norm_dev(const imsrg_op* op, double* out, cudaStream_t st) { return norm_impl(op, out, st); }
 int status_dev(imsrg_space* sp, cudaStream_t st) { return check_status(sp, st); }
+int end_status(imsrg_space* sp, cudaStream_t st) { return sp->defer_status ? IMSRG_OK : check_status(sp, st); }
 }  // namespace imsrg
 
 // ------------------------------------------------------------- batch phases

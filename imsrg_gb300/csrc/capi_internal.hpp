@@ -29,6 +29,11 @@ int set_error(int code, const char* msg);
 int commutator_dev(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStream_t st);
 int norm_dev(const imsrg_op* op, double* out, cudaStream_t st);
 int status_dev(imsrg_space* sp, cudaStream_t st);
+// imsrg_comm122ss_noalloc's set-up on the current device (noalloc.cu)
+int noalloc_setup(imsrg_space* sp, int device);
+// the status read that ends a commutator or term entry point: status_dev, or
+// nothing when the space defers it to imsrg_space_check_status
+int end_status(imsrg_space* sp, cudaStream_t st);
 // tensor operators (capi_tensor.cu): Operator::Norm, and BCH_Transform by a
 // scalar Omega
 int tensor_norm_dev(const imsrg_op* op, double* out, cudaStream_t st);
@@ -56,6 +61,9 @@ int group_post(GroupedProducts* g, cudaStream_t st);
 struct imsrg_space {
   Space* s = nullptr;
   bool dev_ready = false;
+  int device = -1;            // CUDA device the tables (and every operator) live on
+  bool defer_status = false;  // imsrg_space_defer_status
+  double* noalloc_w2 = nullptr;  // device address of the no-alloc entry's static W2 array on that device
   std::mutex mu;
   std::vector<void*> allocs;
   int* d_holes = nullptr;

@@ -315,7 +315,7 @@ int imsrg_comm222_pp_hh_221st(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z,
   if (precision == IMSRG_PREC_FP64) return t222(X, Y, Z, st);
   if ((rc = split_ready(X->sp, Y->tl)) || (rc = split_operands(X, Y, st)) || (rc = t222_split(X, Y, Z, st)))
     return rc;
-  return status_dev(X->sp, st);
+  return end_status(X->sp, st);
 }
 
 int imsrg_comm222_phst(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream)
@@ -326,7 +326,7 @@ int imsrg_comm222_phst(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int pr
   if (precision == IMSRG_PREC_FP64) return tph(X, Y, Z, st);
   if ((rc = split_ready(X->sp, Y->tl)) || (rc = split_operands(X, Y, st)) || (rc = tph_split(X, Y, Z, st)))
     return rc;
-  return status_dev(X->sp, st);
+  return end_status(X->sp, st);
 }
 
 int imsrg_commutator_scalar_tensor(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int precision, void* stream)
@@ -352,7 +352,7 @@ int imsrg_commutator_scalar_tensor(const imsrg_op* X, const imsrg_op* Y, imsrg_o
     if ((rc = split_operands(X, Y, st)) || (on[3] && (rc = t222_split(X, Y, Z, st))) ||
         (on[4] && (rc = tph_split(X, Y, Z, st))))
       return rc;
-    return status_dev(X->sp, st);
+    return end_status(X->sp, st);
   }
   return IMSRG_OK;
 }

@@ -42,6 +42,9 @@ cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, 
                               const double* Mz, cudaStream_t st, const long long* zo = nullptr, int nz = 1);
 cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, double* Z, double* W2, int hZ,
                            const int* sym_tiles, int nsym_tiles, cudaStream_t st);
+// loads launch_comm122's kernels on the current device (they are otherwise
+// loaded at their first launch under lazy module loading)
+cudaError_t load_comm122_kernels();
 // (hi, lo) float-pair copy of an arena (integer instructions); (grouped, with
 // the roles of A and Af)
 cudaError_t launch_to_ff(const Space& s, const double* A, float2* Af, cudaStream_t st, const long long* zo = nullptr,

@@ -1293,6 +1293,15 @@ cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, dou
   return cudaGetLastError();
 }
 
+cudaError_t load_comm122_kernels()
+{
+  // cudaFuncGetAttributes loads a kernel's module under lazy module loading
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, k_comm122_w);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_sym_subtract);
+  return e;
+}
+
 // grid of a grid-stride elementwise kernel over n elements: at most cap blocks
 // (a few waves at emax >= 8), fewer for small arenas, so that small operators
 // do not fill the GPU with idle blocks (commutators of different spaces run

@@ -18,11 +18,14 @@
 // clearing.  Calls that overlap on the GPU (different streams, no ordering)
 // race on the array.
 //
-// Host code never passes g_w2_scratch itself to a kernel: in host code that
-// name is a host-side stand-in, not a device address.  The device address is
-// looked up once per device with cudaGetSymbolAddress, with that device
-// current, on the first call made on that device; make that first call before
-// any stream capture.
+// Set-up happens when the space's device tables are built (its first
+// operator, imsrg_op_create), with the space's device current: host code never
+// passes g_w2_scratch itself to a kernel (in host code that name is a
+// host-side stand-in, not a device address), so the device address is looked
+// up there with cudaGetSymbolAddress, once per device, and the comm122ss
+// kernels are loaded.  Under lazy module loading that step is what commits
+// the array's 16 MiB on the device; the entry point itself then neither
+// allocates nor loads anything.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -40,44 +43,57 @@ constexpr int kMaxDevices = 64;
 std::mutex g_sym_mu;
 double* g_sym_addr[kMaxDevices] = {};
 
-// device address of g_w2_scratch on the current device (looked up once)
-int scratch_address(double** out)
+}  // namespace
+
+namespace imsrg {
+
+// the set-up of imsrg_comm122ss_noalloc on the current device (device), run
+// while a space's device tables are built
+int noalloc_setup(imsrg_space* sp, int device)
 {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return imsrg::set_error(IMSRG_ERR_CUDA, "cudaGetDevice failed");
-  if (dev < 0 || dev >= kMaxDevices) return imsrg::set_error(IMSRG_ERR_ARG, "device ordinal out of range");
+  if (device < 0 || device >= kMaxDevices) return set_error(IMSRG_ERR_ARG, "device ordinal out of range");
   std::lock_guard<std::mutex> g(g_sym_mu);
-  if (!g_sym_addr[dev]) {
+  if (!g_sym_addr[device]) {
     void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_w2_scratch);
+    cudaError_t e = cudaGetSymbolAddress(&p, g_w2_scratch);
     if (e != cudaSuccess || !p) {
       cudaGetLastError();
-      return imsrg::set_error(IMSRG_ERR_CUDA, "cudaGetSymbolAddress of the comm122ss scratch failed");
+      return set_error(IMSRG_ERR_CUDA, "cudaGetSymbolAddress of the comm122ss scratch failed");
     }
-    g_sym_addr[dev] = (double*)p;
+    e = load_comm122_kernels();
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(IMSRG_ERR_CUDA, "loading the comm122ss kernels failed");
+    }
+    g_sym_addr[device] = (double*)p;
   }
-  *out = g_sym_addr[dev];
+  sp->noalloc_w2 = g_sym_addr[device];
   return IMSRG_OK;
 }
 
-}  // namespace
+}  // namespace imsrg
 
 extern "C" int imsrg_comm122ss_noalloc(const imsrg_space* s, const double* X, const double* Y, double* Z, int hZ,
                                        void* stream)
 {
   if (!s || !X || !Y || !Z) return imsrg::set_error(IMSRG_ERR_ARG, "null argument");
   if (hZ != 1 && hZ != -1) return imsrg::set_error(IMSRG_ERR_UNSUPPORTED, "Z must be hermitian or anti-hermitian");
-  if (!s->dev_ready)
+  if (!s->dev_ready || !s->noalloc_w2)
     return imsrg::set_error(IMSRG_ERR_ARG,
                             "the space has no device tables yet: create an operator on it first (imsrg_op_create)");
   if (s->s->arena > kScratchDoubles)
     return imsrg::set_error(IMSRG_ERR_ARG,
                             "model space too large for imsrg_comm122ss_noalloc: arena above 2^21 doubles (16 MiB)");
-  double* w2 = nullptr;
-  int rc = scratch_address(&w2);
-  if (rc) return rc;
-  cudaError_t e = imsrg::launch_comm122(*s->s, X, Y, Z, w2, hZ, s->d_sym122, s->n_sym122, (cudaStream_t)stream);
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return imsrg::set_error(IMSRG_ERR_CUDA, "cudaGetDevice failed");
+  }
+  if (dev != s->device)
+    return imsrg::set_error(IMSRG_ERR_ARG,
+                            "the current CUDA device is not the one the space's tables live on: make it current");
+  cudaError_t e =
+      imsrg::launch_comm122(*s->s, X, Y, Z, s->noalloc_w2, hZ, s->d_sym122, s->n_sym122, (cudaStream_t)stream);
   if (e != cudaSuccess) return imsrg::set_error(IMSRG_ERR_CUDA, cudaGetErrorString(e));
   return IMSRG_OK;
 }

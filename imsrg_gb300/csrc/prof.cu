@@ -84,6 +84,13 @@ int imsrg_profiler_enable(int on)
 {
   std::lock_guard<std::mutex> g(g_pmu);
   g_on = on != 0;
+  // events are created here, not inside the timed phases (a phase takes two
+  // and they return to the pool only when the timers are read)
+  while (g_on && g_free.size() < 1024) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) break;
+    g_free.push_back(e);
+  }
   return IMSRG_OK;
 }
 

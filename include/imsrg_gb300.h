@@ -18,7 +18,7 @@
  *                         reference's local order; every block starts on a
  *                         multiple of 32 doubles.
  * Column-major n x n blocks are exactly arma::mat, so packing a reference
- * Operator is one memcpy per block (see INTEGRATION.md).
+ * Operator is one memcpy per block.
  *
  * Term entry points accumulate into Z, as the reference's
  * Commutator::comm*ss(X, Y, Z) do; Z's hermiticity flag selects the
@@ -221,17 +221,19 @@ int imsrg_comm121ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* str
 /* Commutator::comm122ss, src/Commutator.cc:837-932 */
 int imsrg_comm122ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
 /* comm122ss (plain FP64 form) that allocates no device memory, for callers
- * that cannot call cudaMalloc where they evaluate the term (fixed device
- * budgets, allocators that own all device memory, regions where allocation
- * is not allowed).  X, Y, Z are caller-owned device arenas of the space's
- * layout (Z accumulates); hZ is Z's hermiticity.  The W2 intermediate lives
- * in a static device array of 2^21 doubles (16 MiB) that every GPU loading
- * the library holds until exit, so spaces with a longer arena are rejected
- * (IMSRG_ERR_ARG); the space's device tables must already exist (they are
- * built with its first operator).  The first call on a device looks up the
- * array's device address; make it before any stream capture.  All calls share
- * the array: calls that overlap on the GPU race.  No counterpart in the
- * reference (its comm122ss, src/Commutator.cc:837-932, allocates W2 per call). */
+ * that cannot call cudaMalloc where they evaluate the term: code under a fixed
+ * device-memory budget, a caching allocator that owns all device memory, or a
+ * region where allocating is not allowed.  X, Y, Z are caller-owned device
+ * arenas of the space's layout (Z accumulates); hZ is Z's hermiticity.  The
+ * W2 intermediate lives in a static device array of 2^21 doubles (16 MiB)
+ * that every GPU loading the library holds until exit, so spaces with a
+ * longer arena are rejected (IMSRG_ERR_ARG).  Set-up is done when the space's
+ * device tables are built (its first imsrg_op_create, with that device
+ * current): it looks up the array's device address and loads the kernels,
+ * and under lazy module loading that step may commit the array's 16 MiB.
+ * Calls must be made with that same device current (IMSRG_ERR_ARG otherwise).
+ * All calls share the array: calls that overlap on the GPU race.  No
+ * counterpart in the reference. */
 int imsrg_comm122ss_noalloc(const imsrg_space* s, const double* X, const double* Y, double* Z, int hZ, void* stream);
 /* Commutator::comm221ss, src/Commutator.cc:760-819 */
 int imsrg_comm221ss(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, void* stream);
@@ -275,6 +277,22 @@ int imsrg_comm222_phst(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int pr
  * (comm222_phss transforms X and Y together, in its own layout). */
 int imsrg_pandya_transform(const imsrg_op* Z, int transpose, double* out, void* stream);
 
+/* Layout of a Z bar buffer (imsrg_add_inverse_pandya): total length in
+ * doubles, and for cross-coupled channel ch_cc (ch_cc < 0: total only) its
+ * matrix's rows = the channel's kets and cols = twice that (the "head" half
+ * [0, rows) and the "tail" half [rows, 2 rows) of comm222_phss's Z bar,
+ * src/Commutator.cc:1789-1805), column-major from offset. */
+int imsrg_space_zbar_layout(const imsrg_space* s, int ch_cc, int* rows, int* cols, long long* offset,
+                            long long* total);
+
+/* Commutator::AddInversePandyaTransformation (src/Commutator.cc:1501-1616):
+ * Z += the inverse Pandya transform of zbar, a device buffer of the
+ * imsrg_space_zbar_layout layout; Z's hermiticity selects the symmetrisation.
+ * precision selects the kernel that comm222_phss uses in that form:
+ * IMSRG_PREC_FP64 sums the J' terms in FP64 by channel tile,
+ * IMSRG_PREC_SPLIT by orbit quadruple in double-float arithmetic. */
+int imsrg_add_inverse_pandya(const double* zbar, imsrg_op* Z, int precision, void* stream);
+
 /* Commutator::CommutatorScalarScalar, src/Commutator.cc:280-428 (IMSRG(2)
  * terms): Z is overwritten with [X,Y] and its hermiticity set from X and Y;
  * the terms switched on by imsrg_set_term run in the reference's order. */
@@ -315,6 +333,20 @@ int imsrg_batch_sync(imsrg_batch* batch, void* stream);
  * per replay. */
 int imsrg_batch_info(const imsrg_batch* batch, int* n_pairs, int* n_branches, int* n_product_groups,
                      long long* kernel_nodes);
+
+/* Status reads of the split-precision kernels.  By default every commutator
+ * and term entry point that runs a split-precision product ends by reading
+ * the space's kernel status word (a 4-byte device-to-host copy and a stream
+ * synchronisation), so a bounded wait that gave up is reported by the call
+ * that ran it.  With defer = 1 those entry points return without the read and
+ * without synchronising, so a caller can queue many commutators on a stream;
+ * imsrg_space_check_status then synchronises the stream and returns
+ * IMSRG_ERR_KERNEL if any kernel reported an error since the last read
+ * (clearing the word).  BCH, BCH_Product, the batch and the solver read the
+ * word with the norms they synchronise for anyway, whatever the setting.  No
+ * counterpart in the reference (it has no device status). */
+int imsrg_space_defer_status(imsrg_space* s, int defer);
+int imsrg_space_check_status(imsrg_space* s, void* stream);
 
 /* Default precision used by the reference-signature shim (process-wide). */
 int imsrg_set_default_precision(int precision);

@@ -10,9 +10,15 @@
 # Every output goes to oracle/_ref/.  Used only in the build container (the
 # reference sources do not exist elsewhere).
 #
-#   make -f oracle/ref_build.mk [REF=/root/reference] -j8
+#   make -f oracle/ref_build.mk REF=<IMSRG++ checkout> -j8
+#   make -f oracle/ref_build.mk REF=<checkout> SCIPY_OPENBLAS=<libscipy_openblas .so> blas -j8
+#
+# REF defaults to the environment variable IMSRG_REFERENCE.
 
-REF ?= /root/reference
+REF ?= $(IMSRG_REFERENCE)
+ifeq ($(strip $(REF)),)
+$(error set REF (or IMSRG_REFERENCE) to the IMSRG++ checkout)
+endif
 SRC := $(REF)/src
 ORACLE := $(dir $(lastword $(MAKEFILE_LIST)))
 OUT := $(ORACLE)_ref
@@ -54,7 +60,39 @@ $(OBJ)/ref_harness.o: $(ORACLE)ref_harness.cc | $(OBJ)
 $(OUT)/ref_harness: $(REF_OBJS) $(OBJ)/coupling_stub.o $(OBJ)/ode_stub.o $(OBJ)/ref_harness.o
 	$(CXX) -fopenmp -o $@ $^ -lm
 
-clean:
-	rm -rf $(OUT)/obj $(OUT)/ref_harness
+# The same closure with Armadillo's BLAS path on (LAPACK stays off: the path
+# calls none), BLAS from SciPy's OpenBLAS through ref_stubs/blas_forward.c:
+# the reference as its own build runs it, for timing against the C oracle.
+# Built only on request (target blas).
+SCIPY_OPENBLAS ?=
+OBJB := $(OUT)/obj_blas
+DEFS_BLAS := -DARMA_DONT_USE_WRAPPER -DARMA_DONT_USE_LAPACK -DARMA_NO_DEBUG -DNO_ODE
+CXXFLAGS_BLAS := -std=c++17 -O2 -fopenmp -w $(DEFS_BLAS) $(INCS)
+REF_OBJS_BLAS := $(addprefix $(OBJB)/,$(addsuffix .o,$(REF_UNITS)))
 
-.PHONY: all clean
+blas: $(OUT)/ref_harness_blas
+
+$(OBJB):
+	mkdir -p $(OBJB)
+
+$(OBJB)/%.o: $(SRC)/%.cc | $(OBJB)
+	$(CXX) $(CXXFLAGS_BLAS) -c $< -o $@
+
+$(OBJB)/ode_stub.o: $(ORACLE)ref_stubs/ode_stub.cc | $(OBJB)
+	$(CXX) $(CXXFLAGS_BLAS) -c $< -o $@
+
+$(OBJB)/ref_harness.o: $(ORACLE)ref_harness.cc | $(OBJB)
+	$(CXX) $(CXXFLAGS_BLAS) -c $< -o $@
+
+$(OBJB)/blas_forward.o: $(ORACLE)ref_stubs/blas_forward.c | $(OBJB)
+	$(CC) -O2 -fPIC -c $< -o $@
+
+$(OUT)/ref_harness_blas: $(REF_OBJS_BLAS) $(OBJ)/coupling_stub.o $(OBJB)/ode_stub.o $(OBJB)/ref_harness.o \
+		$(OBJB)/blas_forward.o
+	@test -n "$(SCIPY_OPENBLAS)" || (echo "set SCIPY_OPENBLAS to SciPy's libscipy_openblas .so" && false)
+	$(CXX) -fopenmp -o $@ $^ $(SCIPY_OPENBLAS) -Wl,-rpath,$(dir $(SCIPY_OPENBLAS)) -lm
+
+clean:
+	rm -rf $(OUT)/obj $(OUT)/obj_blas $(OUT)/ref_harness $(OUT)/ref_harness_blas
+
+.PHONY: all blas clean

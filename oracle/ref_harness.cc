@@ -51,6 +51,9 @@
 #include "Generator.hh"
 #include "IMSRGSolver.hh"
 
+#include <omp.h>
+
+#include <algorithm>
 #include <cstdio>
 #include <deque>
 #include <cstdlib>
@@ -361,7 +364,34 @@ static int flow_main(int argc, char** argv) {
   return 0;
 }
 
+// usage: ref_harness time <emax> <X.bin> <Y.bin> <reps>
+//   Commutator::CommutatorScalarScalar(X, Y) once untimed (6j tables, first
+//   touches), then reps times; prints "seconds_per_commutator <t> threads <n>".
+static int time_main(int argc, char** argv) {
+  if (argc != 6) {
+    std::cerr << "usage: ref_harness time <emax> <X.bin> <Y.bin> <reps>\n";
+    return 1;
+  }
+  int emax = std::atoi(argv[2]);
+  int reps = std::atoi(argv[5]);
+  ModelSpace ms(emax, "O16", "O16");
+  ArenaLayout L = make_layout(ms);
+  Operator X(ms, 0, 0, 0, 2), Y(ms, 0, 0, 0, 2);
+  X.SetHermitian();
+  Y.SetAntiHermitian();
+  load(X, read_file(argv[3], L.total), L);
+  load(Y, read_file(argv[4], L.total), L);
+  Operator Z = Commutator::CommutatorScalarScalar(X, Y);
+  double t0 = omp_get_wtime();
+  for (int r = 0; r < reps; ++r) Z = Commutator::CommutatorScalarScalar(X, Y);
+  double t = (omp_get_wtime() - t0) / std::max(1, reps);
+  std::cout << "seconds_per_commutator " << std::setprecision(6) << t << " threads " << omp_get_max_threads()
+            << "\n";
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc > 1 && std::string(argv[1]) == "time") return time_main(argc, argv);
   if (argc > 1 && std::string(argv[1]) == "flow") return flow_main(argc, argv);
   if (argc > 1 && std::string(argv[1]) == "tensor") return tensor_main(argc, argv);
   if (argc != 6) {

@@ -4,6 +4,9 @@ import sys
 
 import pytest
 
+# the C oracle calls BLAS from inside its OpenMP loops: one BLAS thread each
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 for p in (ROOT, os.path.join(ROOT, "oracle")):
     if p not in sys.path:

@@ -1,13 +1,15 @@
 """imsrg_comm122ss_noalloc: the comm122ss variant for callers that cannot
-allocate device memory (its W2 intermediate lives in a static device array).
+allocate device memory where they evaluate the term (its W2 intermediate lives
+in a static device array, set up when the space's device tables are built).
 
-Through the C ABI, with caller-owned device buffers (torch tensors), it must
-give the same result as the regular imsrg_comm122ss, call after call, and
-refuse spaces whose arena exceeds its static array.  This file is collected
-last so a failure here comes after every other test has run."""
+Through the C ABI, with caller-owned device buffers (torch tensors), on a
+fresh model space: two calls in a row must leave the device's free memory
+unchanged and give the same result as the regular imsrg_comm122ss (which
+allocates its own scratch, so it runs last).  Spaces whose arena exceeds the
+static array are refused.  This file is collected last so a failure here
+comes after every other test has run."""
 import ctypes
 
-import numpy as np
 import pytest
 
 import imsrg_gb300 as ig
@@ -27,23 +29,30 @@ def test_noalloc_matches_regular_entry_point_twice():
     X = r.random_operator(71, True)
     Y = r.random_operator(72, False)
     L = _lib.lib()
-    # regular entry point (library-allocated scratch)
+    # set-up: the space's device tables (with them the no-alloc entry's
+    # scratch address), and every caller-owned buffer
+    with ig.DeviceOperator(ms, 1):
+        pass
+    tX = torch.from_numpy(X).cuda()
+    tY = torch.from_numpy(Y).cuda()
+    tZ = [torch.zeros(ms.arena_size, dtype=torch.float64, device="cuda") for _ in range(2)]
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for call in range(2):
+        rc = L.imsrg_comm122ss_noalloc(ms._h, ctypes.c_void_p(tX.data_ptr()), ctypes.c_void_p(tY.data_ptr()),
+                                       ctypes.c_void_p(tZ[call].data_ptr()), 1, None)
+        assert rc == _lib.OK, L.imsrg_last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    # the regular entry point (library-allocated scratch) on the same inputs
     with ig.DeviceOperator(ms, 1) as dX, ig.DeviceOperator(ms, -1) as dY, ig.DeviceOperator(ms, 1) as dZ:
         dX.upload(X)
         dY.upload(Y)
         ig.Commutator.device_term("comm122ss", dX, dY, dZ)
         ref = dZ.download()
-    # caller-owned device buffers
-    tX = torch.from_numpy(X).cuda()
-    tY = torch.from_numpy(Y).cuda()
     for call in range(2):
-        tZ = torch.zeros(ms.arena_size, dtype=torch.float64, device="cuda")
-        rc = L.imsrg_comm122ss_noalloc(ms._h, ctypes.c_void_p(tX.data_ptr()), ctypes.c_void_p(tY.data_ptr()),
-                                       ctypes.c_void_p(tZ.data_ptr()), 1, None)
-        assert rc == _lib.OK, L.imsrg_last_error()
-        torch.cuda.synchronize()
-        Z = tZ.cpu().numpy()
-        errs = rel_errors(r, Z, ref)
+        errs = rel_errors(r, tZ[call].cpu().numpy(), ref)
         assert max(errs) < TOL_FP64, (call, errs)
 
 
