@@ -92,7 +92,41 @@ $(OUT)/ref_harness_blas: $(REF_OBJS_BLAS) $(OBJ)/coupling_stub.o $(OBJB)/ode_stu
 	@test -n "$(SCIPY_OPENBLAS)" || (echo "set SCIPY_OPENBLAS to SciPy's libscipy_openblas .so" && false)
 	$(CXX) -fopenmp -o $@ $^ $(SCIPY_OPENBLAS) -Wl,-rpath,$(dir $(SCIPY_OPENBLAS)) -lm
 
-clean:
-	rm -rf $(OUT)/obj $(OUT)/obj_blas $(OUT)/ref_harness $(OUT)/ref_harness_blas
+# The drop-in link: imsrg_gb300/shim/imsrg_gpu_shim.cc in place of the
+# reference's IMSRG(2) terms, CommutatorScalarScalar and
+# Standard_BCH_Transform.  Copies of Commutator.o and BCH.o get those symbols
+# made weak (objcopy), so the shim's definitions are the ones linked; every
+# other object is the reference's own.  Needs the built library (LIB).
+# Built only on request (target shim); oracle/shim_harness.cc is the driver.
+REPO := $(abspath $(ORACLE)..)
+LIB ?= $(REPO)/imsrg_gb300/_build/libimsrg_gb300.so
+SHIM_COMM_SYMS := _ZN10Commutator9comm110ssERK8OperatorS2_RS0_ _ZN10Commutator9comm220ssERK8OperatorS2_RS0_ \
+  _ZN10Commutator9comm111ssERK8OperatorS2_RS0_ _ZN10Commutator9comm121ssERK8OperatorS2_RS0_ \
+  _ZN10Commutator9comm122ssERK8OperatorS2_RS0_ _ZN10Commutator9comm221ssERK8OperatorS2_RS0_ \
+  _ZN10Commutator15comm222_pp_hhssERK8OperatorS2_RS0_ _ZN10Commutator19comm222_pp_hh_221ssERK8OperatorS2_RS0_ \
+  _ZN10Commutator12comm222_phssERK8OperatorS2_RS0_ _ZN10Commutator22CommutatorScalarScalarERK8OperatorS2_
+SHIM_BCH_SYMS := _ZN3BCH22Standard_BCH_TransformERK8OperatorS2_
+SHIM_BASE_OBJS := $(filter-out $(OBJ)/Commutator.o $(OBJ)/BCH.o,$(REF_OBJS))
 
-.PHONY: all blas clean
+shim: $(OUT)/shim_harness
+
+$(OBJ)/Commutator_weak.o: $(OBJ)/Commutator.o
+	objcopy $(addprefix --weaken-symbol=,$(SHIM_COMM_SYMS)) $< $@
+
+$(OBJ)/BCH_weak.o: $(OBJ)/BCH.o
+	objcopy $(addprefix --weaken-symbol=,$(SHIM_BCH_SYMS)) $< $@
+
+$(OBJ)/imsrg_gpu_shim.o: $(REPO)/imsrg_gb300/shim/imsrg_gpu_shim.cc $(REPO)/include/imsrg_gb300.h | $(OBJ)
+	$(CXX) $(CXXFLAGS) -I$(REPO)/include -c $< -o $@
+
+$(OBJ)/shim_harness.o: $(ORACLE)shim_harness.cc | $(OBJ)
+	$(CXX) $(CXXFLAGS) -c $< -o $@
+
+$(OUT)/shim_harness: $(SHIM_BASE_OBJS) $(OBJ)/Commutator_weak.o $(OBJ)/BCH_weak.o $(OBJ)/imsrg_gpu_shim.o \
+		$(OBJ)/coupling_stub.o $(OBJ)/ode_stub.o $(OBJ)/shim_harness.o $(LIB)
+	$(CXX) -fopenmp -o $@ $^ -Wl,-rpath,$(dir $(LIB)) -lm
+
+clean:
+	rm -rf $(OUT)/obj $(OUT)/obj_blas $(OUT)/ref_harness $(OUT)/ref_harness_blas $(OUT)/shim_harness
+
+.PHONY: all blas shim clean
