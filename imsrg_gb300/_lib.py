@@ -94,6 +94,9 @@ SIGNATURES = {
     "imsrg_batch_info": (I, [P, IP, IP, IP, LLP]),
     "imsrg_space_zbar_layout": (I, [P, I, IP, IP, LLP, LLP]),
     "imsrg_add_inverse_pandya": (I, [P, P, I, P]),
+    "imsrg_space_set_tuning": (I, [P, ctypes.c_char_p, I]),
+    "imsrg_space_get_tuning": (I, [P, ctypes.c_char_p, IP]),
+    "imsrg_space_describe_tuning": (I, [P, ctypes.c_char_p, I]),
     "imsrg_space_defer_status": (I, [P, I]),
     "imsrg_space_check_status": (I, [P, P]),
     "imsrg_set_default_precision": (I, [I]),

@@ -1,9 +1,13 @@
 // extern "C" boundary (include/imsrg_gb300.h): model spaces, device-resident
 // operators, the IMSRG(2) terms, CommutatorScalarScalar and the BCH transform.
 #include <cuda_runtime.h>
+#include <dlfcn.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <fstream>
+#include <sstream>
 #include <cstdint>
 #include <cstring>
 #include <exception>
@@ -208,7 +212,7 @@ void setup_device_lists(imsrg_space* sp)
   sp->d_sym122 = sp->track(dcopy(t122));
   sp->n_pinv = (int)tinv.size() / 3;
   sp->d_pinv = sp->track(dcopy(tinv));
-  build_invq_tasks(s, kInvqBudget);
+  build_invq_tasks(s, sp->invq_budget);
   sp->n_invq = (int)s.invq_tasks.size() / 4;
   sp->d_invq = sp->track(dcopy(s.invq_tasks));
   sp->d_cls_list = sp->track(dcopy(s.cls_list));
@@ -239,6 +243,132 @@ void setup_device_lists(imsrg_space* sp)
   cudaMemset(sp->d_status, 0, 16 * sizeof(int));
 }
 
+// ------------------------------------------------------------------ tuning
+int rebuild_invq(imsrg_space* sp);
+void drop_invd(imsrg_space* sp);
+
+// Names of the tunable parameters of a space (imsrg_space_set_tuning).
+const char* kTuneNames[] = {"ladder.tile",  "ladder.stages", "ladder.schedule",     "zbar.tile",
+                            "zbar.stages",  "zbar.schedule", "inverse.split",       "inverse.fp64",
+                            "inverse.quad_budget", "inverse.desc_stage", "inverse.desc_results",
+                            "inverse.desc_weights"};
+constexpr int kNTune = sizeof(kTuneNames) / sizeof(kTuneNames[0]);
+
+int* tune_slot(imsrg_space* sp, int t)
+{
+  switch (t) {
+    case 0: return &sp->opt_ladder.tn;
+    case 1: return &sp->opt_ladder.stages;
+    case 2: return &sp->opt_ladder.sched;
+    case 3: return &sp->opt_zbar.tn;
+    case 4: return &sp->opt_zbar.stages;
+    case 5: return &sp->opt_zbar.sched;
+    case 6: return &sp->inv_split;
+    case 7: return &sp->inv_fp64;
+    case 8: return &sp->invq_budget;
+    case 9: return &sp->invd_stage;
+    case 10: return &sp->invd_res;
+    case 11: return &sp->invd_weights;
+  }
+  return nullptr;
+}
+
+bool tune_valid(int t, int v)
+{
+  switch (t) {
+    case 0: case 3: return v == 0 || v == 32 || v == 64;
+    case 1: case 4: return v == 0 || (v >= 2 && v <= 6);
+    case 2: case 5: return v == 0 || v == 1;
+    case 6: return v >= 0 && v <= 2;
+    case 7: return v == 0 || v == 1;
+    case 8: return v >= 8192 && v <= 160 * 1024;
+    case 9: return v >= 64 && v <= 8192;
+    case 10: return v >= 64 && v <= (1 << 20);
+    case 11: return v == 0 || v == 1;
+  }
+  return false;
+}
+
+// sets parameter t; with the device tables built, the plans it shapes are
+// dropped (and rebuilt on next use)
+int tune_apply(imsrg_space* sp, int t, int v)
+{
+  if (!tune_valid(t, v)) return fail(IMSRG_ERR_ARG, std::string("bad value for ") + kTuneNames[t]);
+  int* slot = tune_slot(sp, t);
+  if (*slot == v) return IMSRG_OK;
+  *slot = v;
+  if (t == 0 || t == 3) (t == 0 ? sp->opt_ladder : sp->opt_zbar).nacc = v == 64 ? 1 : (v == 32 ? 2 : 0);
+  if (!sp->dev_ready) return IMSRG_OK;
+  if (t <= 2 && sp->split_ladder) {
+    split_plan_destroy(sp->split_ladder);
+    sp->split_ladder = nullptr;
+  }
+  if (t >= 3 && t <= 5 && sp->split_zbar) {
+    split_plan_destroy(sp->split_zbar);
+    sp->split_zbar = nullptr;
+  }
+  if (t == 8) return rebuild_invq(sp);
+  if (t >= 9 && t <= 11) drop_invd(sp);
+  return IMSRG_OK;
+}
+
+int tune_index(const char* name)
+{
+  for (int t = 0; t < kNTune; ++t)
+    if (name && std::strcmp(name, kTuneNames[t]) == 0) return t;
+  return -1;
+}
+
+// The tuning file: one line per tuned space, "arena=<len> norb=<n>
+// name=value ...", written by imsrg_gb300.autotune.  Found at
+// $IMSRG_GB300_TUNING ("off": none), else tuning/gb300.txt beside the
+// library's directory (imsrg_gb300/tuning/ for the in-tree build).
+std::string tuning_file_path()
+{
+  const char* env = std::getenv("IMSRG_GB300_TUNING");
+  if (env && *env) return std::strcmp(env, "off") == 0 ? std::string() : std::string(env);
+  Dl_info info;
+  if (!dladdr((void*)&tuning_file_path, &info) || !info.dli_fname) return std::string();
+  std::string so(info.dli_fname);
+  size_t cut = so.find_last_of('/');
+  std::string dir = cut == std::string::npos ? std::string(".") : so.substr(0, cut);
+  return dir + "/../tuning/gb300.txt";
+}
+
+void apply_tuning_file(imsrg_space* sp)
+{
+  std::string path = tuning_file_path();
+  if (path.empty()) return;
+  std::ifstream in(path);
+  if (!in) return;
+  std::string line;
+  int lineno = 0;
+  while (std::getline(in, line)) {
+    ++lineno;
+    if (line.empty() || line[0] == '#') continue;
+    std::istringstream ls(line);
+    std::string tok;
+    std::vector<std::pair<std::string, long long>> kv;
+    while (ls >> tok) {
+      size_t eq = tok.find('=');
+      if (eq == std::string::npos) continue;
+      kv.push_back({tok.substr(0, eq), std::atoll(tok.c_str() + eq + 1)});
+    }
+    long long arena = -1, norb = -1;
+    for (auto& p : kv) {
+      if (p.first == "arena") arena = p.second;
+      if (p.first == "norb") norb = p.second;
+    }
+    if (arena != sp->s->arena || norb != sp->s->norb) continue;
+    for (auto& p : kv) {
+      int t = tune_index(p.first.c_str());
+      if (t >= 0 && tune_valid(t, (int)p.second)) tune_apply(sp, t, (int)p.second);
+    }
+    sp->tuning_source = path + ":" + std::to_string(lineno);
+    return;
+  }
+}
+
 // device tables are built on first device use, so a space can be created and
 // queried on a machine without a GPU
 int ensure_device(imsrg_space* sp)
@@ -247,6 +377,7 @@ int ensure_device(imsrg_space* sp)
   if (sp->dev_ready) return IMSRG_OK;
   int dev = -1;
   CUDA_TRY(cudaGetDevice(&dev));
+  apply_tuning_file(sp);
   try {
     setup_device_lists(sp);
   } catch (std::exception& e) {
@@ -274,6 +405,103 @@ int ensure_scratch(imsrg_space* sp, bool pandya, bool w2)
   } catch (std::exception& e) {
     return fail(IMSRG_ERR_NOMEM, std::string("scratch allocation failed: ") + e.what());
   }
+  return IMSRG_OK;
+}
+
+// untracks and frees one device allocation of the space
+void drop_alloc(imsrg_space* sp, void* p)
+{
+  if (!p) return;
+  auto it = std::find(sp->allocs.begin(), sp->allocs.end(), p);
+  if (it != sp->allocs.end()) sp->allocs.erase(it);
+  cudaFree(p);
+}
+
+// the quadruple blocks of the split form's inverse Pandya transform, rebuilt
+// for the space's shared-memory budget
+int rebuild_invq(imsrg_space* sp)
+{
+  Space& s = *sp->s;
+  drop_alloc(sp, sp->d_invq);
+  drop_alloc(sp, sp->d_cls_list);
+  drop_alloc(sp, sp->d_cls_off);
+  drop_alloc(sp, sp->d_cls_sort);
+  sp->d_invq = nullptr;
+  sp->d_cls_list = sp->d_cls_off = nullptr;
+  sp->d_cls_sort = nullptr;
+  try {
+    build_invq_tasks(s, sp->invq_budget);
+    sp->n_invq = (int)s.invq_tasks.size() / 4;
+    sp->d_invq = sp->track(dcopy(s.invq_tasks));
+    sp->d_cls_list = sp->track(dcopy(s.cls_list));
+    sp->d_cls_off = sp->track(dcopy(s.cls_off));
+    sp->d_cls_sort = sp->track(dcopy(s.cls_sort));
+  } catch (std::exception& e) {
+    sp->n_invq = 0;
+    return fail(IMSRG_ERR_NOMEM, std::string("inverse Pandya blocks: ") + e.what());
+  }
+  return IMSRG_OK;
+}
+
+void drop_invd(imsrg_space* sp)
+{
+  for (void* p : sp->invd_allocs) cudaFree(p);
+  sp->invd_allocs.clear();
+  sp->invd = InvdDev{};
+  sp->invd_ready = false;
+}
+
+// the inverse Pandya descriptors of the space (built on first use)
+int ensure_invd(imsrg_space* sp)
+{
+  if (sp->invd_ready) return IMSRG_OK;
+  drop_invd(sp);
+  try {
+    InvdPlan plan;
+    build_invd(*sp->s, plan, sp->invd_stage, sp->invd_res, sp->invd_weights != 0);
+    auto up = [&](const auto& v) {
+      auto* p = dcopy(v);
+      sp->invd_allocs.push_back((void*)p);
+      return p;
+    };
+    sp->invd.blocks = up(plan.blocks);
+    sp->invd.wblk = up(plan.wblk);
+    sp->invd.wrow = up(plan.wrow);
+    sp->invd.sslot = up(plan.sslot);
+    sp->invd.sidx = up(plan.sidx);
+    sp->invd.dA = up(plan.dA);
+    sp->invd.dB = up(plan.dB);
+    sp->invd.nblocks = (int)plan.blocks.size();
+    sp->invd.stage_max = plan.stage_max;
+    sp->invd.staged_weights = sp->invd_weights != 0;
+  } catch (std::exception& e) {
+    drop_invd(sp);
+    return fail(IMSRG_ERR_NOMEM, std::string("inverse Pandya descriptors: ") + e.what());
+  }
+  sp->invd_ready = true;
+  return IMSRG_OK;
+}
+
+// AddInversePandyaTransformation of zb into Z with the kernel the space's
+// tuning selects for the form (grouped: nz pairs at the offsets zo)
+int inverse_pandya(imsrg_space* sp, const double* zb, double* Z, int hZ, int prec, cudaStream_t st,
+                   const long long* zo = nullptr, int nz = 1)
+{
+  Space& s = *sp->s;
+  const int variant = prec == IMSRG_PREC_SPLIT ? sp->inv_split : (sp->inv_fp64 ? 2 : 0);
+  if (variant == 1 || variant == 2) {
+    int rc = ensure_invd(sp);
+    if (rc) return rc;
+    CUDA_TRY(launch_pandya_inv_desc(s, sp->invd, variant == 1, zb, Z, hZ, st, zo, nz));
+    return IMSRG_OK;
+  }
+  if (prec == IMSRG_PREC_SPLIT && sp->n_invq > 0) {
+    CUDA_TRY(launch_pandya_inv_ff(s, zb, Z, hZ, sp->d_invq, sp->n_invq, sp->d_cls_list, sp->d_cls_off, sp->d_cls_sort,
+                                  s.invq_smem, st, zo, nz));
+    return IMSRG_OK;
+  }
+  if (zo) return fail(IMSRG_ERR_UNSUPPORTED, "grouped inverse Pandya needs the quadruple or descriptor kernel");
+  CUDA_TRY(launch_pandya_inv(s, zb, Z, hZ, sp->d_pinv, sp->n_pinv, st));
   return IMSRG_OK;
 }
 
@@ -380,8 +608,8 @@ int check_status(imsrg_space* sp, cudaStream_t st)
 int ensure_split(imsrg_space* sp)
 {
   try {
-    if (!sp->split_ladder) sp->split_ladder = split_plan_create(*sp->s, sp->ladder_jobs, 0);
-    if (!sp->split_zbar) sp->split_zbar = split_plan_create(*sp->s, sp->zbar_jobs, 1);
+    if (!sp->split_ladder) sp->split_ladder = split_plan_create(*sp->s, sp->ladder_jobs, 0, sp->opt_ladder);
+    if (!sp->split_zbar) sp->split_zbar = split_plan_create(*sp->s, sp->zbar_jobs, 1, sp->opt_zbar);
   } catch (std::exception& e) {
     return fail(IMSRG_ERR_NOMEM, std::string("split-precision plan: ") + e.what());
   }
@@ -436,6 +664,8 @@ int do_ph(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStrea
   if (prec == IMSRG_PREC_SPLIT) {
     rc = ensure_split(sp);
     if (rc) return rc;
+    // the descriptor inverse kernels read only Zbar's upper triangle
+    split_plan_set_mirror(sp->split_zbar, sp->inv_split == 0 ? 1 : 0);
     CUDA_TRY(launch_symgemm_split(sp->split_zbar, sp->d_xb, sp->d_yt, sp->d_yf, sp->d_zb, s.work.kidx,
                                   s.work.kweight, s.work.phase_tab, sp->d_status, Z->herm, 1.0, st));
   } else if (prec == IMSRG_PREC_FP64) {
@@ -446,12 +676,7 @@ int do_ph(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStrea
   }
   prof_end(slot, st);
   ProfScope pinv("InversePandyaTransformation", st);
-  if (prec == IMSRG_PREC_SPLIT && sp->n_invq > 0)
-    CUDA_TRY(launch_pandya_inv_ff(s, sp->d_zb, Z->d, Z->herm, sp->d_invq, sp->n_invq, sp->d_cls_list, sp->d_cls_off,
-                                  sp->d_cls_sort, s.invq_smem, st));
-  else
-    CUDA_TRY(launch_pandya_inv(s, sp->d_zb, Z->d, Z->herm, sp->d_pinv, sp->n_pinv, st));
-  return IMSRG_OK;
+  return inverse_pandya(sp, sp->d_zb, Z->d, Z->herm, prec, st);
 }
 
 int z_herm(int hx, int hy) { return (hx == hy) ? -1 : 1; }
@@ -1007,15 +1232,47 @@ int imsrg_add_inverse_pandya(const double* zbar, imsrg_op* Z, int precision, voi
   if (Z->tl) return fail(IMSRG_ERR_UNSUPPORTED, "Z must be a scalar operator");
   if (Z->herm != 1 && Z->herm != -1) return fail(IMSRG_ERR_UNSUPPORTED, "Z must be hermitian or anti-hermitian");
   if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_SPLIT) return fail(IMSRG_ERR_ARG, "bad precision");
-  imsrg_space* sp = Z->sp;
-  Space& s = *sp->s;
   cudaStream_t st = S_(stream);
   ProfScope ps("InversePandyaTransformation", st);
-  if (precision == IMSRG_PREC_SPLIT && sp->n_invq > 0)
-    CUDA_TRY(launch_pandya_inv_ff(s, zbar, Z->d, Z->herm, sp->d_invq, sp->n_invq, sp->d_cls_list, sp->d_cls_off,
-                                  sp->d_cls_sort, s.invq_smem, st));
-  else
-    CUDA_TRY(launch_pandya_inv(s, zbar, Z->d, Z->herm, sp->d_pinv, sp->n_pinv, st));
+  return inverse_pandya(Z->sp, zbar, Z->d, Z->herm, precision, st);
+}
+
+int imsrg_space_set_tuning(imsrg_space* sp, const char* name, int value)
+{
+  if (!sp || !name) return fail(IMSRG_ERR_ARG, "bad arguments");
+  int t = tune_index(name);
+  if (t < 0) return fail(IMSRG_ERR_ARG, std::string("unknown tuning parameter ") + name);
+  std::lock_guard<std::mutex> g(sp->mu);
+  int rc = tune_apply(sp, t, value);
+  if (rc == IMSRG_OK) sp->tuning_source = "set";
+  return rc;
+}
+
+int imsrg_space_get_tuning(const imsrg_space* sp, const char* name, int* value)
+{
+  if (!sp || !name || !value) return fail(IMSRG_ERR_ARG, "bad arguments");
+  int t = tune_index(name);
+  if (t < 0) return fail(IMSRG_ERR_ARG, std::string("unknown tuning parameter ") + name);
+  int v = *tune_slot(const_cast<imsrg_space*>(sp), t);
+  if (t == 0 && v == 0) v = 64;
+  if (t == 3 && v == 0) v = 32;
+  *value = v;
+  return IMSRG_OK;
+}
+
+int imsrg_space_describe_tuning(const imsrg_space* sp, char* buf, int buflen)
+{
+  if (!sp) return fail(IMSRG_ERR_ARG, "null space");
+  std::string all = "source=" + sp->tuning_source;
+  for (int t = 0; t < kNTune; ++t) {
+    int v = 0;
+    imsrg_space_get_tuning(sp, kTuneNames[t], &v);
+    all += std::string(" ") + kTuneNames[t] + "=" + std::to_string(v);
+  }
+  if (!buf || buflen <= 0) return (int)all.size() + 1;
+  int n = std::min<int>((int)all.size(), buflen - 1);
+  all.copy(buf, n);
+  buf[n] = 0;
   return IMSRG_OK;
 }
 
@@ -1247,8 +1504,8 @@ GroupedProducts* grouped_products_create(const std::vector<const imsrg_op*>& X, 
     zo.insert(zo.end(), r, r + kZRoles);
   }
   try {
-    g->ladder = split_plan_create(*s0->s, lj, 0);
-    g->zbar = split_plan_create(*s0->s, zj, 1);
+    g->ladder = split_plan_create(*s0->s, lj, 0, s0->opt_ladder);
+    g->zbar = split_plan_create(*s0->s, zj, 1, s0->opt_zbar);
     g->d_zoff = dcopy(zo);
   } catch (std::exception& e) {
     if (why) *why = std::string("grouped product plans: ") + e.what();
@@ -1302,9 +1559,9 @@ int group_post(GroupedProducts* g, cudaStream_t st)
   imsrg_op* Z = g->Z[0];
   imsrg_space* sp = g->X[0]->sp;
   const Space& s = *sp->s;
-  if (sp->n_invq > 0) {
-    CUDA_TRY(launch_pandya_inv_ff(s, sp->d_zb, Z->d, Z->herm, sp->d_invq, sp->n_invq, sp->d_cls_list, sp->d_cls_off,
-                                  sp->d_cls_sort, s.invq_smem, st, g->d_zoff, nz));
+  if (sp->inv_split != 0 || sp->n_invq > 0) {
+    int rc = inverse_pandya(sp, sp->d_zb, Z->d, Z->herm, IMSRG_PREC_SPLIT, st, g->d_zoff, nz);
+    if (rc) return rc;
   } else {
     for (int p = 0; p < nz; ++p) {
       imsrg_space* q = g->X[p]->sp;
@@ -1331,6 +1588,7 @@ int grouped_zbar(GroupedProducts* g, cudaStream_t st)
 {
   imsrg_space* s0 = g->X[0]->sp;
   const Space& s = *s0->s;
+  split_plan_set_mirror(g->zbar, s0->inv_split == 0 ? 1 : 0);  // as group_post reads Zbar
   CUDA_TRY(launch_symgemm_split(g->zbar, s0->d_xb, s0->d_yt, s0->d_yf, s0->d_zb, s.work.kidx, s.work.kweight,
                                 s.work.phase_tab, s0->d_status, g->Z[0]->herm, 1.0, st));
   return IMSRG_OK;

@@ -106,6 +106,19 @@ struct imsrg_space {
   double *d_nested = nullptr, *d_next = nullptr, *d_prod = nullptr;
   // generator scratch: monopoles V(ab, ab) of H, norb^2
   double* d_mono = nullptr;
+  // tuning (imsrg_space_set_tuning, or this space's entry of the tuning file)
+  imsrg::SplitOpts opt_ladder, opt_zbar;
+  int inv_split = 0;  // split form's inverse Pandya: 0 quadruple blocks (double-float), 1 descriptors
+                      // (double-float), 2 descriptors (FP64)
+  int inv_fp64 = 0;   // FP64 form's inverse Pandya: 0 channel tiles, 1 descriptors (FP64)
+  int invq_budget = imsrg::kInvqBudget;
+  int invd_stage = 2048, invd_res = 2048;
+  int invd_weights = 0;  // descriptor kernel: 1 stages the 6j weight rows per block
+  std::string tuning_source = "default";
+  // inverse Pandya descriptors (built on first use)
+  imsrg::InvdDev invd;
+  bool invd_ready = false;
+  std::vector<void*> invd_allocs;
   // second stream of CommutatorScalarScalar (work independent of the ladder
   // product) and the events that fork it from and join it to the caller's
   cudaStream_t side = nullptr;
@@ -125,6 +138,7 @@ struct imsrg_space {
     if (ev_join) cudaEventDestroy(ev_join);
     if (side) cudaStreamDestroy(side);
     for (void* p : allocs) cudaFree(p);
+    for (void* p : invd_allocs) cudaFree(p);
     delete s;
   }
 };

@@ -67,6 +67,36 @@ cudaError_t launch_pandya_inv_ff(const Space& s, const double* Zb, double* Z, in
                                  cudaStream_t st, const long long* zo = nullptr, int nz = 1);
 // shared-memory budget of one quadruple block (dynamic part)
 constexpr int kInvqBudget = 36864;
+
+// kernels_invd.cu: the inverse Pandya transform from per-space descriptors
+// (both forms; FP64 or double-float J' sums)
+struct InvdPlan {
+  std::vector<int4> blocks;  // per block: first staged index, staged count, first result, result count
+  std::vector<int2> wblk;    // per block: first weight row, row count
+  std::vector<int2> wrow;    // per 6j weight row: first sixj_wval / sixj_wf index, offset | length << 20
+  std::vector<int> sidx;     // Zbar element (and sign bits) of every staged value, in address order
+  std::vector<unsigned short> sslot;  // its slot in the block's shared memory
+  std::vector<int4> dA;      // per result: staged weight rows of both sums, Z element, mirror element (-1: none)
+  std::vector<int2> dB;      // per result: staged offsets, counts and combination bits
+  int stage_max = 0;         // most staged values + weights in one block (shared-memory words)
+};
+struct InvdDev {
+  const int4* blocks = nullptr;
+  const int2* wblk = nullptr;
+  const int2* wrow = nullptr;
+  const int* sidx = nullptr;
+  const unsigned short* sslot = nullptr;
+  const int4* dA = nullptr;
+  const int2* dB = nullptr;
+  int nblocks = 0, stage_max = 0;
+  bool staged_weights = false;  // the 6j weight rows are staged per block (else read from the table)
+};
+// blocks of at most stage_max staged values (and, staging weights, as many
+// weights) and res_max results
+void build_invd(const Space& s, InvdPlan& out, int stage_max, int res_max, bool stage_weights);
+// (grouped)
+cudaError_t launch_pandya_inv_desc(const Space& s, const InvdDev& d, bool df, const double* Zb, double* Z, int hZ,
+                                   cudaStream_t st, const long long* zo = nullptr, int nz = 1);
 // single-operator Pandya transform into the Xbar panel layout (xb_off)
 cudaError_t launch_pandya_single(const Space& s, const double* Z, int herm, int transpose, double* out,
                                  cudaStream_t st);
@@ -129,10 +159,24 @@ cudaError_t launch_symgemm_fp64(const GemmJobDev* jobs, const int* pairs, int np
 
 // kernels_split.cu (Ozaki-style sliced BF16 products on tcgen05)
 struct SplitPlan;
-SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs, int family);
+// Tile shape and schedule of a plan: tn x nacc in {64 x 1, 32 x 2} (tile
+// columns, TMEM accumulator sets; 0 = the family's default), pipeline stages
+// (0 = as many as shared memory holds), schedule 0 = tiles dealt round-robin
+// to the persistent CTAs in size order, 1 = longest-first greedy (LPT) lists
+// per CTA on the tiles' K-block counts.
+struct SplitOpts {
+  int tn = 0, nacc = 0, stages = 0, sched = 0;
+};
+SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs, int family,
+                             const SplitOpts& opts = SplitOpts());
+// the options a plan was built with (defaults resolved)
+SplitOpts split_plan_opts(const SplitPlan* p);
 void split_plan_destroy(SplitPlan* p);
 // -1: each job's own accumulate flag; 0: overwrite the output; 1: accumulate
 void split_plan_set_accumulate(SplitPlan* p, int mode);
+// 0: symmetrised jobs store only their upper triangle (for a reader of the
+// upper triangle alone, e.g. the descriptor inverse Pandya kernel); 1: both
+void split_plan_set_mirror(SplitPlan* p, int mirror);
 // one bounded mbarrier wait of `limit` iterations that runs out (no arrival):
 // status = 105, *cycles = the SM clock cycles it waited (device pointer)
 cudaError_t launch_wait_selftest(int* status, unsigned limit, long long* cycles, cudaStream_t st);

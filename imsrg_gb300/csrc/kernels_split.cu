@@ -105,7 +105,10 @@ struct SplitPlan {
   size_t smem = 0;
   int nstages = 0;
   int accum_override = -1;
+  int mirror = 1;  // 0: symmetrised jobs write only their upper triangle
   int tn = 64, nacc = 1, epiw = 4;  // tile columns, accumulator sets, epilogue warps
+  int stages_opt = 0, sched = 0;    // requested pipeline stages (0: most that fit), tile schedule
+  int* d_cta = nullptr;             // [grid + 1]: each CTA's tiles are tiles[d_cta[b] .. d_cta[b + 1])
   bool shared_gd = false;           // gamma / delta alias beta / alpha (plain jobs only)
   bool plain = false;               // every job is a plain product (a plan holds one kind)
 };
@@ -541,6 +544,7 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
 struct GemmArgs {
   const SplitJob* jobs;
   const SplitTile* tiles;
+  const int* cta_first;  // [gridDim.x + 1]: the CTA's run of tiles
   int ntiles;
   const int* rexpA;
   const int* rexpB;
@@ -551,6 +555,7 @@ struct GemmArgs {
   int* status;
   int S, beta, nstages, gsign;
   int accum;  // -1: each job's flag; 0: overwrite; 1: accumulate
+  int nomirror;  // 1: symmetrised jobs skip the mirror (lower-triangle) stores
 };
 
 // TN: tile columns (UMMA N); NACC: TMEM accumulator sets (2 lets the
@@ -620,7 +625,8 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
     // ------------------------------------------------ TMA producer
     if (lane == 0) {
       int it = 0;
-      for (int tix = blockIdx.x; tix < g.ntiles && !s_err; tix += gridDim.x) {
+      const int tend = g.cta_first[blockIdx.x + 1];
+      for (int tix = g.cta_first[blockIdx.x]; tix < tend && !s_err; ++tix) {
         const SplitTile tl = g.tiles[tix];
         const SplitJob& jb = g.jobs[tl.job];
         const bool useG = g.flags[2 * tl.job] != 0, useD = g.flags[2 * tl.job + 1] != 0;
@@ -658,7 +664,8 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
     if (lane == 0) {
       constexpr int MAXT = 256 / TN;  // B digit tiles per MMA (UMMA N <= 256)
       int it = 0, tc = 0;
-      for (int tix = blockIdx.x; tix < g.ntiles && !s_err; tix += gridDim.x, ++tc) {
+      const int tend = g.cta_first[blockIdx.x + 1];
+      for (int tix = g.cta_first[blockIdx.x]; tix < tend && !s_err; ++tix, ++tc) {
         const SplitJob& jb = g.jobs[g.tiles[tix].job];
         const int b = tc % NACC;
         if (!mbar_wait(acc_empty(b), (unsigned)(((tc / NACC) & 1) ^ 1))) {
@@ -717,7 +724,8 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
     const int cbeg = ((warp - 2) >> 2) * COLS_W;  // first column of this warp
     const int et = threadIdx.x - 64;         // 0 .. EPI_T-1
     int tc = 0;
-    for (int tix = blockIdx.x; tix < g.ntiles; tix += gridDim.x, ++tc) {
+    const int tend = g.cta_first[blockIdx.x + 1];
+    for (int tix = g.cta_first[blockIdx.x]; tix < tend; ++tix, ++tc) {
       const SplitTile tl = g.tiles[tix];
       const SplitJob& jb = g.jobs[tl.job];
       const int b = tc % NACC;
@@ -769,7 +777,7 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
         for (int cc = 0; cc < EPI_COLS; ++cc) {
           const int j = tl.J * TN + c0 + cc;
           wd[cc] = rowok && j < jb.n && !(tl.diag && i > j);
-          wm[cc] = wd[cc] && i != j && !jb.nosym;
+          wm[cc] = wd[cc] && i != j && !jb.nosym && !g.nomirror;
           // exact merge of the weight groups: Horner in base 2^beta
           long long I64 = __float2int_rn(__uint_as_float(r[0][cc]));
 #pragma unroll
@@ -899,16 +907,44 @@ static void choose_digits(int Kmax, int& beta, int& S)
   if (S > MAX_S) S = MAX_S;
 }
 
-SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs_in, int family)
+SplitOpts split_plan_opts(const SplitPlan* p)
+{
+  SplitOpts o;
+  o.tn = p->tn;
+  o.nacc = p->nacc;
+  o.stages = p->nstages;
+  o.sched = p->sched;
+  return o;
+}
+
+SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs_in, int family,
+                             const SplitOpts& opts)
 {
   (void)s;
   SplitPlan* p = new SplitPlan();
   p->family = family;
-  // the ladder products have long K (MMA-bound tiles): 64-column tiles, one
-  // accumulator set; the Pandya-space products have short K (epilogue-bound
-  // tiles): 32-column tiles and two accumulator sets; eight epilogue warps
+  // defaults: the ladder products have long K (MMA-bound tiles): 64-column
+  // tiles, one accumulator set; the Pandya-space products have short K
+  // (epilogue-bound tiles): 32-column tiles and two accumulator sets; eight
+  // epilogue warps
   p->tn = family == 0 ? 64 : 32;
   p->nacc = family == 0 ? 1 : 2;
+  if (opts.tn == 64 && (opts.nacc == 0 || opts.nacc == 1)) {
+    p->tn = 64;
+    p->nacc = 1;
+  } else if (opts.tn == 32 && (opts.nacc == 0 || opts.nacc == 2)) {
+    p->tn = 32;
+    p->nacc = 2;
+  } else if (opts.tn != 0 || opts.nacc != 0) {
+    delete p;
+    throw std::invalid_argument("split plan: tile shape must be 64 x 1 or 32 x 2");
+  }
+  if (opts.sched < 0 || opts.sched > 1 || opts.stages < 0) {
+    delete p;
+    throw std::invalid_argument("split plan: bad schedule or stage count");
+  }
+  p->stages_opt = opts.stages;
+  p->sched = opts.sched;
   p->epiw = 8;
   int Kmax = 1;
   for (const GemmJobDev& j : jobs_in) Kmax = std::max(Kmax, j.K);
@@ -977,11 +1013,56 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
     if (cudaMalloc(&q, std::max<size_t>(bytes, 16)) != cudaSuccess) throw std::runtime_error("cudaMalloc");
     return q;
   };
+  // persistent grid: one CTA per SM; each CTA works through its own run of
+  // tiles, dealt round-robin in size order (sched 0) or by longest-first
+  // greedy assignment of the tiles' K-block counts (sched 1)
+  {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    p->grid = std::max(1, std::min(nsm, p->ntiles));
+  }
+  std::vector<int> cta_first(p->grid + 1, 0);
+  {
+    const int G = p->grid;
+    std::vector<int> owner(tiles.size());
+    if (p->sched == 0) {
+      for (size_t t = 0; t < tiles.size(); ++t) owner[t] = (int)(t % G);
+    } else {
+      std::vector<int> ord(tiles.size());
+      for (size_t t = 0; t < ord.size(); ++t) ord[t] = (int)t;
+      auto cost = [&](int t) { return (long long)p->jobs[tiles[t].job].nkt + 4; };
+      std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return cost(a) > cost(b); });
+      std::vector<std::pair<long long, int>> heap;  // (load, cta), min-heap
+      for (int b = 0; b < G; ++b) heap.push_back({0, b});
+      auto gt = [](const std::pair<long long, int>& x, const std::pair<long long, int>& y) { return x > y; };
+      std::make_heap(heap.begin(), heap.end(), gt);
+      for (int t : ord) {
+        std::pop_heap(heap.begin(), heap.end(), gt);
+        heap.back().first += cost(t);
+        owner[t] = heap.back().second;
+        std::push_heap(heap.begin(), heap.end(), gt);
+      }
+    }
+    // tiles of one CTA contiguous, in their original (size) order
+    std::vector<SplitTile> sorted;
+    sorted.reserve(tiles.size());
+    std::vector<std::vector<int>> lists(G);
+    for (size_t t = 0; t < tiles.size(); ++t) lists[owner[t]].push_back((int)t);
+    for (int b = 0; b < G; ++b) {
+      cta_first[b] = (int)sorted.size();
+      for (int t : lists[b]) sorted.push_back(tiles[t]);
+    }
+    cta_first[G] = (int)sorted.size();
+    tiles.swap(sorted);
+  }
   try {
     p->d_jobs = (SplitJob*)dm(sizeof(SplitJob) * std::max(1, p->njobs));
     p->d_tiles = (SplitTile*)dm(sizeof(SplitTile) * std::max(1, p->ntiles));
+    p->d_cta = (int*)dm(sizeof(int) * cta_first.size());
     cudaMemcpy(p->d_jobs, p->jobs.data(), sizeof(SplitJob) * p->njobs, cudaMemcpyHostToDevice);
     cudaMemcpy(p->d_tiles, tiles.data(), sizeof(SplitTile) * p->ntiles, cudaMemcpyHostToDevice);
+    cudaMemcpy(p->d_cta, cta_first.data(), sizeof(int) * cta_first.size(), cudaMemcpyHostToDevice);
     size_t abytes = (size_t)std::max(row, (long long)TILE_M) * kstride * 2;
     // gamma / delta (the second half of a doubled K) only for symmetrised jobs
     bool any_sym = false, any_plain = false;
@@ -1044,15 +1125,16 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
     split_plan_destroy(p);
     throw;
   }
-  int dev = 0, nsm = 0;
+  int dev = 0, maxsm = 0;
   cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  p->grid = std::max(1, std::min(nsm, p->ntiles));
-  int maxsm = 0;
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   size_t stage = (size_t)p->S * (TILE_M + p->tn) * KB * 2;
   p->nstages = (int)std::min<size_t>(6, ((size_t)maxsm - 3072) / stage);
-  if (p->nstages < 2) throw std::runtime_error("not enough shared memory for the split GEMM pipeline");
+  if (p->stages_opt > 0) p->nstages = std::min(p->nstages, p->stages_opt);
+  if (p->nstages < 2) {
+    split_plan_destroy(p);
+    throw std::runtime_error("not enough shared memory for the split GEMM pipeline (or fewer than 2 stages asked)");
+  }
   p->smem = 1024 + p->nstages * stage + (2 * p->nstages + 2 * p->nacc) * 8 + 16;
   return p;
 }
@@ -1062,6 +1144,7 @@ void split_plan_destroy(SplitPlan* p)
   if (!p) return;
   cudaFree(p->d_jobs);
   cudaFree(p->d_tiles);
+  cudaFree(p->d_cta);
   for (int a = 0; a < (p->shared_gd ? 2 : 4); ++a) cudaFree(p->arr[a]);
   cudaFree(p->d_rexpA);
   cudaFree(p->d_rexpB);
@@ -1112,6 +1195,7 @@ static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, con
     GemmArgs ga;
     ga.jobs = p->d_jobs;
     ga.tiles = p->d_tiles;
+    ga.cta_first = p->d_cta;
     ga.ntiles = p->ntiles;
     ga.rexpA = p->d_rexpA;
     ga.rexpB = p->d_rexpB;
@@ -1125,6 +1209,7 @@ static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, con
     ga.nstages = p->nstages;
     ga.gsign = gsign;
     ga.accum = p->accum_override;
+    ga.nomirror = p->mirror ? 0 : 1;
     if (p->tn == 64) {
       auto kern = k_split_gemm<S, 64, 1, 8>;
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
@@ -1143,6 +1228,7 @@ static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, con
 }
 
 void split_plan_set_accumulate(SplitPlan* p, int mode) { p->accum_override = mode; }
+void split_plan_set_mirror(SplitPlan* p, int mirror) { p->mirror = mirror ? 1 : 0; }
 
 cudaError_t launch_symgemm_split(SplitPlan* p, const double* A, const double* B0, const double* B1, double* O,
                                  const int* kidx, const double* kw, const int* phase, int* dev_status, int gsign,

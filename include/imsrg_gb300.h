@@ -288,9 +288,12 @@ int imsrg_space_zbar_layout(const imsrg_space* s, int ch_cc, int* rows, int* col
 /* Commutator::AddInversePandyaTransformation (src/Commutator.cc:1501-1616):
  * Z += the inverse Pandya transform of zbar, a device buffer of the
  * imsrg_space_zbar_layout layout; Z's hermiticity selects the symmetrisation.
- * precision selects the kernel that comm222_phss uses in that form:
- * IMSRG_PREC_FP64 sums the J' terms in FP64 by channel tile,
- * IMSRG_PREC_SPLIT by orbit quadruple in double-float arithmetic. */
+ * precision selects the kernel that comm222_phss uses in that form
+ * (imsrg_space_set_tuning "inverse.split" / "inverse.fp64").  zbar must have
+ * the symmetry of comm222_phss's Z bar, which every kernel relies on: head
+ * Zbar(r, c) = hZ Zbar(c, r), tail Zbar(r, n + c) = phi_r phi_c Zbar(c, n + r)
+ * with phi of a ket (p, q) = (-1)^((j_p + j_q) / 2); the descriptor kernels
+ * read only each block's upper triangle. */
 int imsrg_add_inverse_pandya(const double* zbar, imsrg_op* Z, int precision, void* stream);
 
 /* Commutator::CommutatorScalarScalar, src/Commutator.cc:280-428 (IMSRG(2)
@@ -333,6 +336,39 @@ int imsrg_batch_sync(imsrg_batch* batch, void* stream);
  * per replay. */
 int imsrg_batch_info(const imsrg_batch* batch, int* n_pairs, int* n_branches, int* n_product_groups,
                      long long* kernel_nodes);
+
+/* Tuning of a space's kernels: tile shapes, pipeline depth and tile-to-CTA
+ * schedules of the split products, and the inverse Pandya kernel and its
+ * block sizes.  Parameters (value 0 = the built-in default where allowed):
+ *   "ladder.tile", "zbar.tile"          64 (64 columns, one accumulator set)
+ *                                       or 32 (32 columns, two sets)
+ *   "ladder.stages", "zbar.stages"      pipeline stages, 2..6 (0: most that fit)
+ *   "ladder.schedule", "zbar.schedule"  0: tiles dealt round-robin to the
+ *                                       persistent CTAs in size order, 1:
+ *                                       longest-first greedy lists per CTA
+ *   "inverse.split"                     split form: 0 orbit-quadruple blocks,
+ *                                       1 descriptors with double-float sums,
+ *                                       2 descriptors with FP64 sums
+ *   "inverse.fp64"                      FP64 form: 0 channel tiles, 1
+ *                                       descriptors (FP64 sums)
+ *   "inverse.quad_budget"               shared-memory bytes per quadruple block
+ *   "inverse.desc_stage", "inverse.desc_results"
+ *                                       staged values / results per descriptor block
+ *   "inverse.desc_weights"              1: descriptor blocks stage their 6j
+ *                                       weight rows in shared memory
+ * When the space's device tables are built (its first operator), the line of
+ * the tuning file whose "arena=" and "norb=" match the space is applied: the
+ * file is $IMSRG_GB300_TUNING ("off" for none), else tuning/gb300.txt in the
+ * directory above the library's (written by python -m imsrg_gb300.autotune).
+ * Setting a parameter drops the plans it shapes (rebuilt on next use); no
+ * call on the space may be running.  The reference has no counterpart (its
+ * schedule is OpenMP's dynamic one over size-sorted channels,
+ * src/ModelSpace.cc:1183-1198, src/Commutator.cc:1113-1115). */
+int imsrg_space_set_tuning(imsrg_space* s, const char* name, int value);
+int imsrg_space_get_tuning(const imsrg_space* s, const char* name, int* value);
+/* "source=<file:line | set | default> name=value ..."; with buf == NULL
+ * returns the size needed */
+int imsrg_space_describe_tuning(const imsrg_space* s, char* buf, int buflen);
 
 /* Status reads of the split-precision kernels.  By default every commutator
  * and term entry point that runs a split-precision product ends by reading

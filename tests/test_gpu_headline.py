@@ -8,8 +8,9 @@
 - A 50-step Magnus-Euler flow (White generator, ds = 0.5): the zero-body value
   after the last step against the oracle's flow, <= 1e-8 relative, both forms.
 - The double-float kernels of the split form against their FP64 twins on the
-  same input: the inverse Pandya transform (same Z bar) and comm122ss (same X,
-  Y), relative Frobenius <= 1e-13 at emax=8."""
+  same input: the inverse Pandya transform (same Z bar; every kernel variant)
+  and comm122ss (same X, Y), relative Frobenius <= 1e-13 at emax=8.
+- The full commutator under every tuning choice against the oracle."""
 import ctypes
 
 import numpy as np
@@ -103,26 +104,99 @@ def test_flow_50_steps_final_e0_vs_oracle(prec):
     assert abs(e_final - ref) <= TOL_FLOW_E0 * abs(ref), (prec, e_final, ref)
 
 
-def test_inverse_pandya_double_float_vs_fp64():
-    emax = 8
-    ms = ig.ModelSpace(emax, "O16", "O16")
+def symmetric_zbar(ms, hz, seed):
+    """A random Z bar with the symmetry of comm222_phss's (which the inverse
+    transforms rely on): per cross-coupled channel, head H = R + hZ R^T and
+    tail T = S + Phi S^T Phi, Phi = diag((-1)^((j_p + j_q) / 2)) of its kets."""
+    import torch
     L = ig.lib()
     total = ctypes.c_longlong()
     assert L.imsrg_space_zbar_layout(ms._h, -1, None, None, None, ctypes.byref(total)) == 0
-    import torch
-    g = torch.Generator().manual_seed(88)
-    zbar = (torch.rand(total.value, generator=g, dtype=torch.float64) * 2 - 1).cuda()
-    out = {}
+    z = np.zeros(total.value)
+    rng = np.random.default_rng(seed)
+    for ch in range(ms.nch):
+        rows, cols, off = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+        assert L.imsrg_space_zbar_layout(ms._h, ch, ctypes.byref(rows), ctypes.byref(cols), ctypes.byref(off),
+                                         None) == 0
+        n = rows.value
+        if n == 0:
+            continue
+        kets = ms.cc_channel(ch)["kets"]
+        phi = np.array([(-1) ** ((ms.orbits[p][2] + ms.orbits[q][2]) // 2) for (p, q) in kets], dtype=float)
+        R = rng.uniform(-1, 1, (n, n))
+        S = rng.uniform(-1, 1, (n, n))
+        H = R + hz * R.T
+        T = S + phi[:, None] * S.T * phi[None, :]
+        z[off.value:off.value + 2 * n * n] = np.concatenate([H.ravel(order="F"), T.ravel(order="F")])
+    return torch.from_numpy(z).cuda()
+
+
+def set_tuning(ms, name, value):
+    L = ig.lib()
+    assert L.imsrg_space_set_tuning(ms._h, name.encode(), value) == 0, L.imsrg_last_error()
+
+
+@pytest.mark.parametrize("emax", [4, 8])
+def test_inverse_pandya_kernels_vs_fp64(emax):
+    """Every inverse Pandya kernel against the FP64 channel-tiled one on the
+    same Z bar: the FP64 descriptor kernel to rounding (1e-15), the
+    double-float ones to 1e-13."""
+    ms = ig.ModelSpace(emax, "O16", "O16")
+    L = ig.lib()
+    r = ref_space(emax)
+    # (form, tuning parameter, value, tolerance)
+    variants = [("split", "inverse.split", 0, TOL_DF), ("split", "inverse.split", 1, TOL_DF),
+                ("split", "inverse.split", 2, 1e-15), ("fp64", "inverse.fp64", 1, 1e-15),
+                ("split", "inverse.desc_weights", 1, 1e-15), ("split", "inverse.split", 1, TOL_DF)]
     for hz in (1, -1):
-        for prec, code in (("fp64", 0), ("split", 1)):
-            with ig.DeviceOperator(ms, hz) as dZ:
+        zbar = symmetric_zbar(ms, hz, 88 + emax)
+        with ig.DeviceOperator(ms, hz) as dZ:
+            set_tuning(ms, "inverse.fp64", 0)
+            assert L.imsrg_add_inverse_pandya(ctypes.c_void_p(zbar.data_ptr()), dZ._h, 0, None) == 0
+            ref = dZ.download()
+            assert np.linalg.norm(ref) > 0
+            for form, name, value, tol in variants:
+                set_tuning(ms, name, value)
+                dZ.zero()
+                code = 1 if form == "split" else 0
                 rc = L.imsrg_add_inverse_pandya(ctypes.c_void_p(zbar.data_ptr()), dZ._h, code, None)
                 assert rc == 0, L.imsrg_last_error()
-                out[(hz, prec)] = dZ.download()
-        r = ref_space(emax)
-        errs = rel_errors(r, out[(hz, "split")], out[(hz, "fp64")])
-        assert max(errs[1:]) < TOL_DF, (hz, errs)
-        assert np.linalg.norm(out[(hz, "fp64")]) > 0
+                errs = rel_errors(r, dZ.download(), ref)
+                assert max(errs[1:]) < tol, (hz, name, value, errs)
+        set_tuning(ms, "inverse.split", 0)
+        set_tuning(ms, "inverse.fp64", 0)
+        set_tuning(ms, "inverse.desc_weights", 0)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "split"])
+def test_commutator_with_every_tuning(prec):
+    """The full commutator with each tile shape, stage count, schedule and
+    inverse Pandya kernel against the oracle."""
+    emax = 5
+    o = Oracle(emax)
+    ms = ig.ModelSpace(emax, "O16", "O16")
+    X = o.ms.random_operator(505, True)
+    Y = o.ms.random_operator(606, False)
+    R = o.commutator(X, Y, 1, -1)
+    settings = [{}, {"ladder.tile": 32, "zbar.tile": 64}, {"ladder.stages": 2, "zbar.stages": 2},
+                {"ladder.schedule": 1, "zbar.schedule": 1}, {"inverse.split": 1, "inverse.fp64": 1},
+                {"inverse.split": 2, "inverse.desc_stage": 256, "inverse.desc_results": 128},
+                {"inverse.split": 1, "inverse.desc_weights": 1}, {"inverse.split": 2, "inverse.desc_weights": 1},
+                {"inverse.quad_budget": 16384}]
+    with ig.DeviceOperator(ms, 1) as dX, ig.DeviceOperator(ms, -1) as dY, ig.DeviceOperator(ms, 1) as dZ:
+        dX.upload(X)
+        dY.upload(Y)
+        for st in settings:
+            for k, v in st.items():
+                set_tuning(ms, k, v)
+            ig.Commutator.device_commutator(dX, dY, dZ, prec)
+            errs = rel_errors(o.ms, dZ.download(), R)
+            assert max(errs) < TOL[prec], (st, errs)
+            for k in st:
+                set_tuning(ms, k, 0 if k not in ("inverse.quad_budget", "inverse.desc_stage",
+                                                 "inverse.desc_results") else
+                           {"inverse.quad_budget": 36864, "inverse.desc_stage": 2048,
+                            "inverse.desc_results": 2048}[k])
 
 
 def test_comm122_double_float_vs_fp64():
