@@ -662,7 +662,8 @@ def run_gb300(args):
                    if prec == "split" else "FP64 CUDA cores",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "working set > L2 every step (X2, Y2 280 MiB each; Zbar 761 MiB)",
-                   "timing": "phase timers off; kernels' status word read once after the K steps"},
+                   "timing": "phase timers off; kernels' status word read once after the K steps",
+                   "tuning": ms.tuning()},
         "step_ms": {"min": min(per_step), "median": statistics.median(per_step), "max": max(per_step)},
         "plain_fp64": fp64,
         "split_vs_fp64_rel_err": fp64["split_vs_fp64_rel_err"] if fp64 else None,

@@ -112,6 +112,21 @@ class ModelSpace:
         the last read."""
         check(self._L.imsrg_space_check_status(self._h, stream))
 
+    def tuning(self):
+        """The space's kernel tuning, {"source": ..., name: value}
+        (imsrg_space_describe_tuning)."""
+        n = self._L.imsrg_space_describe_tuning(self._h, None, 0)
+        buf = ctypes.create_string_buffer(n)
+        check(self._L.imsrg_space_describe_tuning(self._h, buf, n))
+        out = {}
+        for tok in buf.value.decode().split():
+            k, v = tok.split("=", 1)
+            out[k] = v if k == "source" else int(v)
+        return out
+
+    def set_tuning(self, name, value):
+        check(self._L.imsrg_space_set_tuning(self._h, name.encode(), int(value)))
+
     def GetNumberOrbits(self):
         return self.norb
 

@@ -32,7 +32,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 DEFAULTS = {"ladder.tile": 64, "ladder.stages": 0, "ladder.schedule": 0, "zbar.tile": 32, "zbar.stages": 0,
             "zbar.schedule": 0, "inverse.split": 0, "inverse.fp64": 0, "inverse.quad_budget": 36864,
-            "inverse.desc_stage": 2048, "inverse.desc_results": 2048, "inverse.desc_weights": 0}
+            "inverse.desc_stage": 2048, "inverse.desc_results": 2048, "inverse.desc_weights": 0,
+            "inverse.desc_ilp": 1}
 
 
 def _set(L, ms, name, value):
@@ -109,20 +110,22 @@ def tune_space(ig, emax, reps, fp64_margin, log):
             _set(L, ms, "inverse.desc_stage", stage)
             _set(L, ms, "inverse.desc_results", stage)
             for variant in (1, 2):
-                _set(L, ms, "inverse.split", variant)
-                t = inverse_ms(1)
-                cfg = {"inverse.split": variant, "inverse.desc_stage": stage, "inverse.desc_results": stage,
-                       "inverse.desc_weights": weights}
-                rec["trials"].append({"what": "inverse split", **cfg, "ms": t})
-                if variant not in cands or t < cands[variant][0]:
-                    cands[variant] = (t, cfg)
+                for ilp in (1, 2):
+                    _set(L, ms, "inverse.split", variant)
+                    _set(L, ms, "inverse.desc_ilp", ilp)
+                    t = inverse_ms(1)
+                    cfg = {"inverse.split": variant, "inverse.desc_stage": stage, "inverse.desc_results": stage,
+                           "inverse.desc_weights": weights, "inverse.desc_ilp": ilp}
+                    rec["trials"].append({"what": "inverse split", **cfg, "ms": t})
+                    if variant not in cands or t < cands[variant][0]:
+                        cands[variant] = (t, cfg)
     # FP64 sums unless a double-float kernel wins by more than the margin
     fastest = min(cands.values(), key=lambda c: c[0])
     pick = cands[2] if cands[2][0] <= fastest[0] * (1.0 + fp64_margin) else fastest
     for k, v in pick[1].items():
         chosen[k] = v
     for k in ("inverse.split", "inverse.desc_stage", "inverse.desc_results", "inverse.desc_weights",
-              "inverse.quad_budget"):
+              "inverse.desc_ilp", "inverse.quad_budget"):
         _set(L, ms, k, chosen[k])
     # the FP64 form's kernel: channel tiles or descriptors (same block sizes)
     f64 = {}

@@ -251,7 +251,7 @@ void drop_invd(imsrg_space* sp);
 const char* kTuneNames[] = {"ladder.tile",  "ladder.stages", "ladder.schedule",     "zbar.tile",
                             "zbar.stages",  "zbar.schedule", "inverse.split",       "inverse.fp64",
                             "inverse.quad_budget", "inverse.desc_stage", "inverse.desc_results",
-                            "inverse.desc_weights"};
+                            "inverse.desc_weights", "inverse.desc_ilp"};
 constexpr int kNTune = sizeof(kTuneNames) / sizeof(kTuneNames[0]);
 
 int* tune_slot(imsrg_space* sp, int t)
@@ -269,6 +269,7 @@ int* tune_slot(imsrg_space* sp, int t)
     case 9: return &sp->invd_stage;
     case 10: return &sp->invd_res;
     case 11: return &sp->invd_weights;
+    case 12: return &sp->invd_ilp;
   }
   return nullptr;
 }
@@ -285,6 +286,7 @@ bool tune_valid(int t, int v)
     case 9: return v >= 64 && v <= 8192;
     case 10: return v >= 64 && v <= (1 << 20);
     case 11: return v == 0 || v == 1;
+    case 12: return v == 1 || v == 2 || v == 4;
   }
   return false;
 }
@@ -492,6 +494,7 @@ int inverse_pandya(imsrg_space* sp, const double* zb, double* Z, int hZ, int pre
   if (variant == 1 || variant == 2) {
     int rc = ensure_invd(sp);
     if (rc) return rc;
+    sp->invd.ilp = sp->invd_ilp;
     CUDA_TRY(launch_pandya_inv_desc(s, sp->invd, variant == 1, zb, Z, hZ, st, zo, nz));
     return IMSRG_OK;
   }

@@ -114,6 +114,7 @@ struct imsrg_space {
   int invq_budget = imsrg::kInvqBudget;
   int invd_stage = 2048, invd_res = 2048;
   int invd_weights = 0;  // descriptor kernel: 1 stages the 6j weight rows per block
+  int invd_ilp = 1;      // descriptor kernel: results in flight per thread (1, 2, 4)
   std::string tuning_source = "default";
   // inverse Pandya descriptors (built on first use)
   imsrg::InvdDev invd;

@@ -90,6 +90,7 @@ struct InvdDev {
   const int2* dB = nullptr;
   int nblocks = 0, stage_max = 0;
   bool staged_weights = false;  // the 6j weight rows are staged per block (else read from the table)
+  int ilp = 1;                  // results each thread keeps in flight (1, 2 or 4)
 };
 // blocks of at most stage_max staged values (and, staging weights, as many
 // weights) and res_max results

@@ -327,7 +327,74 @@ void build_invd(const Space& s, InvdPlan& out, int stage_max, int res_max, bool 
 // ----------------------------------------------------------------- device
 namespace {
 
+// the value z one descriptor adds to Z(ij, kl) (and hZ z to Z(kl, ij))
 template <bool DF, bool SW>
+__device__ __forceinline__ double invd_value(const int4 a, const int2 b, int hZ, const unsigned char* smem, int nstage,
+                                           const double* __restrict__ wval, const float2* __restrict__ wf)
+{
+  const int n1 = (b.x >> kNShift) & 31, n2 = (b.y >> kNShift) & 31;
+  const int c1 = (b.x >> kCShift) & 3, c2c = (b.y >> kCShift) & 3;
+  const int scode = (b.x >> kFShift) & 3;
+  int c2 = c2c == 0 ? 0 : (c2c == 1 ? 1 : -1);
+  if ((b.y >> kFShift) & 1) c2 *= hZ;
+  const int z1 = b.x & 0xFFFF, z2 = b.y & 0xFFFF;
+  double z;
+  if (DF) {
+    const float2* zs = (const float2*)smem;
+    const float2* ws = SW ? zs + nstage : wf;
+    float s1 = 0.f, e1 = 0.f, s1b = 0.f, e1b = 0.f;
+    if (c1) {
+      int x = 0;
+      for (; x + 1 < n1; x += 2) {
+        df_fma(ws[a.x + x], zs[z1 + x], s1, e1);
+        df_fma(ws[a.x + x + 1], zs[z1 + x + 1], s1b, e1b);
+      }
+      if (x < n1) df_fma(ws[a.x + x], zs[z1 + x], s1, e1);
+      df_add(s1, e1, s1b, e1b, s1, e1);
+      if (c1 == 2) {
+        s1 = __fmul_rn(s1, 2.f);
+        e1 = __fmul_rn(e1, 2.f);
+      }
+    }
+    float hi = s1, lo = e1;
+    if (c2) {
+      float s2 = 0.f, e2 = 0.f, s2b = 0.f, e2b = 0.f;
+      int x = 0;
+      for (; x + 1 < n2; x += 2) {
+        df_fma(ws[a.y + x], zs[z2 + x], s2, e2);
+        df_fma(ws[a.y + x + 1], zs[z2 + x + 1], s2b, e2b);
+      }
+      if (x < n2) df_fma(ws[a.y + x], zs[z2 + x], s2, e2);
+      df_add(s2, e2, s2b, e2b, s2, e2);
+      if (c2 < 0) {
+        s2 = -s2;
+        e2 = -e2;
+      }
+      df_add(s1, e1, s2, e2, hi, lo);
+    }
+    z = ff2d(hi, lo);
+  } else {
+    const double* zs = (const double*)smem;
+    const double* ws = SW ? zs + nstage : wval;
+    double s1 = 0.0, s2 = 0.0;
+    if (c1) {
+      for (int x = 0; x < n1; ++x) s1 = fma(ws[a.x + x], zs[z1 + x], s1);
+      if (c1 == 2) s1 *= 2.0;
+    }
+    if (c2) {
+      for (int x = 0; x < n2; ++x) s2 = fma(ws[a.y + x], zs[z2 + x], s2);
+      s1 = c2 > 0 ? s1 + s2 : s1 - s2;
+    }
+    z = s1;
+  }
+  if (scode == 1)
+    z *= 0.5;
+  else if (scode == 2)
+    z *= 0.70710678118654752440;
+  return z;
+}
+
+template <bool DF, bool SW, int R>
 __global__ void __launch_bounds__(kThreads) k_pandya_inv_desc(const int4* __restrict__ blocks,
                                                               const int2* __restrict__ wblk,
                                                               const int2* __restrict__ wrow,
@@ -388,72 +455,37 @@ __global__ void __launch_bounds__(kThreads) k_pandya_inv_desc(const int4* __rest
     }
   }
   __syncthreads();
-  // 2. a thread per result
-  for (int e = tid; e < bk.w; e += kThreads) {
-    const int4 a = __ldg(dA + bk.z + e);
-    const int2 b = __ldg(dB + bk.z + e);
-    if (((b.x >> kDiagBit) & 1) && hZ < 0) continue;
-    const int n1 = (b.x >> kNShift) & 31, n2 = (b.y >> kNShift) & 31;
-    const int c1 = (b.x >> kCShift) & 3, c2c = (b.y >> kCShift) & 3;
-    const int scode = (b.x >> kFShift) & 3;
-    int c2 = c2c == 0 ? 0 : (c2c == 1 ? 1 : -1);
-    if ((b.y >> kFShift) & 1) c2 *= hZ;
-    const int z1 = b.x & 0xFFFF, z2 = b.y & 0xFFFF;
-    double z;
-    if (DF) {
-      const float2* zs = (const float2*)smem;
-      const float2* ws = SW ? zs + bk.y : wf;
-      float s1 = 0.f, e1 = 0.f, s1b = 0.f, e1b = 0.f;
-      if (c1) {
-        int x = 0;
-        for (; x + 1 < n1; x += 2) {
-          df_fma(ws[a.x + x], zs[z1 + x], s1, e1);
-          df_fma(ws[a.x + x + 1], zs[z1 + x + 1], s1b, e1b);
-        }
-        if (x < n1) df_fma(ws[a.x + x], zs[z1 + x], s1, e1);
-        df_add(s1, e1, s1b, e1b, s1, e1);
-        if (c1 == 2) {
-          s1 = __fmul_rn(s1, 2.f);
-          e1 = __fmul_rn(e1, 2.f);
-        }
+  // 2. a thread per result, R results in flight per thread: descriptors,
+  //    then the old Z values, then the sums and the updates
+  for (int e0 = tid; e0 < bk.w; e0 += R * kThreads) {
+    int4 a[R];
+    int2 b[R];
+    double o1[R], o2[R];
+    bool ok[R];
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const int e = e0 + u * kThreads;
+      ok[u] = e < bk.w;
+      if (ok[u]) {
+        a[u] = __ldg(dA + bk.z + e);
+        b[u] = __ldg(dB + bk.z + e);
+        ok[u] = !(((b[u].x >> kDiagBit) & 1) && hZ < 0);
       }
-      float hi = s1, lo = e1;
-      if (c2) {
-        float s2 = 0.f, e2 = 0.f, s2b = 0.f, e2b = 0.f;
-        int x = 0;
-        for (; x + 1 < n2; x += 2) {
-          df_fma(ws[a.y + x], zs[z2 + x], s2, e2);
-          df_fma(ws[a.y + x + 1], zs[z2 + x + 1], s2b, e2b);
-        }
-        if (x < n2) df_fma(ws[a.y + x], zs[z2 + x], s2, e2);
-        df_add(s2, e2, s2b, e2b, s2, e2);
-        if (c2 < 0) {
-          s2 = -s2;
-          e2 = -e2;
-        }
-        df_add(s1, e1, s2, e2, hi, lo);
-      }
-      z = ff2d(hi, lo);
-    } else {
-      const double* zs = (const double*)smem;
-      const double* ws = SW ? zs + bk.y : wval;
-      double s1 = 0.0, s2 = 0.0;
-      if (c1) {
-        for (int x = 0; x < n1; ++x) s1 = fma(ws[a.x + x], zs[z1 + x], s1);
-        if (c1 == 2) s1 *= 2.0;
-      }
-      if (c2) {
-        for (int x = 0; x < n2; ++x) s2 = fma(ws[a.y + x], zs[z2 + x], s2);
-        s1 = c2 > 0 ? s1 + s2 : s1 - s2;
-      }
-      z = s1;
     }
-    if (scode == 1)
-      z *= 0.5;
-    else if (scode == 2)
-      z *= 0.70710678118654752440;
-    Z[a.z] += z;
-    if (a.w >= 0) Z[a.w] += hZ > 0 ? z : -z;
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      if (ok[u]) {
+        o1[u] = Z[a[u].z];
+        o2[u] = a[u].w >= 0 ? Z[a[u].w] : 0.0;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      if (!ok[u]) continue;
+      const double z = invd_value<DF, SW>(a[u], b[u], hZ, smem, bk.y, wval, wf);
+      Z[a[u].z] = o1[u] + z;
+      if (a[u].w >= 0) Z[a[u].w] = o2[u] + (hZ > 0 ? z : -z);
+    }
   }
 }
 
@@ -464,8 +496,16 @@ cudaError_t launch_pandya_inv_desc(const Space& s, const InvdDev& d, bool df, co
 {
   if (d.nblocks == 0) return cudaSuccess;
   const size_t smem = (size_t)d.stage_max * 8;
-  auto kern = df ? (d.staged_weights ? k_pandya_inv_desc<true, true> : k_pandya_inv_desc<true, false>)
-                 : (d.staged_weights ? k_pandya_inv_desc<false, true> : k_pandya_inv_desc<false, false>);
+  using Kern = void (*)(const int4*, const int2*, const int2*, const int*, const unsigned short*, const int4*,
+                       const int2*, const double*, const float2*, const double*, double*, int, const long long*);
+  // [df][staged weights][results in flight: 1, 2, 4]
+  static const Kern kerns[2][2][3] = {
+      {{k_pandya_inv_desc<false, false, 1>, k_pandya_inv_desc<false, false, 2>, k_pandya_inv_desc<false, false, 4>},
+       {k_pandya_inv_desc<false, true, 1>, k_pandya_inv_desc<false, true, 2>, k_pandya_inv_desc<false, true, 4>}},
+      {{k_pandya_inv_desc<true, false, 1>, k_pandya_inv_desc<true, false, 2>, k_pandya_inv_desc<true, false, 4>},
+       {k_pandya_inv_desc<true, true, 1>, k_pandya_inv_desc<true, true, 2>, k_pandya_inv_desc<true, true, 4>}}};
+  const int ri = d.ilp >= 4 ? 2 : (d.ilp >= 2 ? 1 : 0);
+  Kern kern = kerns[df ? 1 : 0][d.staged_weights ? 1 : 0][ri];
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   kern<<<dim3(d.nblocks, 1, nz), kThreads, smem, st>>>(d.blocks, d.wblk, d.wrow, d.sidx, d.sslot, d.dA, d.dB,

@@ -147,7 +147,8 @@ def test_inverse_pandya_kernels_vs_fp64(emax):
     # (form, tuning parameter, value, tolerance)
     variants = [("split", "inverse.split", 0, TOL_DF), ("split", "inverse.split", 1, TOL_DF),
                 ("split", "inverse.split", 2, 1e-15), ("fp64", "inverse.fp64", 1, 1e-15),
-                ("split", "inverse.desc_weights", 1, 1e-15), ("split", "inverse.split", 1, TOL_DF)]
+                ("split", "inverse.desc_weights", 1, 1e-15), ("split", "inverse.split", 1, TOL_DF),
+                ("split", "inverse.desc_ilp", 4, TOL_DF), ("split", "inverse.split", 2, 1e-15)]
     for hz in (1, -1):
         zbar = symmetric_zbar(ms, hz, 88 + emax)
         with ig.DeviceOperator(ms, hz) as dZ:
@@ -166,6 +167,7 @@ def test_inverse_pandya_kernels_vs_fp64(emax):
         set_tuning(ms, "inverse.split", 0)
         set_tuning(ms, "inverse.fp64", 0)
         set_tuning(ms, "inverse.desc_weights", 0)
+        set_tuning(ms, "inverse.desc_ilp", 1)
 
 
 @pytest.mark.parametrize("prec", ["fp64", "split"])
@@ -182,6 +184,7 @@ def test_commutator_with_every_tuning(prec):
                 {"ladder.schedule": 1, "zbar.schedule": 1}, {"inverse.split": 1, "inverse.fp64": 1},
                 {"inverse.split": 2, "inverse.desc_stage": 256, "inverse.desc_results": 128},
                 {"inverse.split": 1, "inverse.desc_weights": 1}, {"inverse.split": 2, "inverse.desc_weights": 1},
+                {"inverse.split": 1, "inverse.desc_ilp": 4}, {"inverse.split": 2, "inverse.desc_ilp": 2},
                 {"inverse.quad_budget": 16384}]
     with ig.DeviceOperator(ms, 1) as dX, ig.DeviceOperator(ms, -1) as dY, ig.DeviceOperator(ms, 1) as dZ:
         dX.upload(X)
@@ -194,9 +197,9 @@ def test_commutator_with_every_tuning(prec):
             assert max(errs) < TOL[prec], (st, errs)
             for k in st:
                 set_tuning(ms, k, 0 if k not in ("inverse.quad_budget", "inverse.desc_stage",
-                                                 "inverse.desc_results") else
+                                                 "inverse.desc_results", "inverse.desc_ilp") else
                            {"inverse.quad_budget": 36864, "inverse.desc_stage": 2048,
-                            "inverse.desc_results": 2048}[k])
+                            "inverse.desc_results": 2048, "inverse.desc_ilp": 1}[k])
 
 
 def test_comm122_double_float_vs_fp64():
@@ -223,3 +226,37 @@ def test_comm122_double_float_vs_fp64():
     finally:
         for n, on in saved.items():
             (ig.Commutator.TurnOnTerm if on else ig.Commutator.TurnOffTerm)(n)
+
+
+def test_tuning_file_applied():
+    """A space whose size has a line in imsrg_gb300/tuning/gb300.txt gets that
+    line's parameters when it builds its device tables; IMSRG_GB300_TUNING=off
+    leaves the built-in defaults."""
+    import os
+    path = os.path.join(os.path.dirname(ig.__file__), "tuning", "gb300.txt")
+    lines = {}
+    for ln in open(path):
+        if ln.startswith("#") or not ln.strip():
+            continue
+        kv = dict(tok.split("=") for tok in ln.split())
+        lines[int(kv["emax"])] = {k: int(v) for k, v in kv.items() if k not in ("arena", "norb", "emax")}
+    emax = 6
+    ms = ig.ModelSpace(emax, "O16", "O16")
+    with ig.DeviceOperator(ms, 1):
+        t = ms.tuning()
+    assert t["source"].endswith(".txt:%d" % ([i + 1 for i, ln in enumerate(open(path))
+                                             if ln.startswith("arena=%d " % ms.arena_size)][0])), t
+    for k, v in lines[emax].items():
+        assert t[k] == v, (k, t[k], v)
+    old = os.environ.get("IMSRG_GB300_TUNING")
+    os.environ["IMSRG_GB300_TUNING"] = "off"
+    try:
+        ms2 = ig.ModelSpace(emax, "O16", "O16")
+        with ig.DeviceOperator(ms2, 1):
+            t2 = ms2.tuning()
+        assert t2["source"] == "default" and t2["inverse.split"] == 0, t2
+    finally:
+        if old is None:
+            del os.environ["IMSRG_GB300_TUNING"]
+        else:
+            os.environ["IMSRG_GB300_TUNING"] = old
