@@ -10,6 +10,8 @@ the choices that imsrg_space_set_tuning exposes and keeps the fastest:
   pipeline depth and tile-to-CTA schedule (round-robin in size order, or
   longest-first greedy lists), ladder and Z bar product each, timed as whole
   split-form commutators (the products share the GPU with the second stream);
+- the split form's comm122ss with W2 through memory or fused tile pairs,
+  timed as whole split-form commutators;
 - the inverse Pandya kernel of each form and its block sizes, timed alone
   (imsrg_add_inverse_pandya on a Z bar of the space's layout).  Among the
   split form's kernels, the FP64 descriptor kernel (the reference's FP64
@@ -33,7 +35,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 DEFAULTS = {"ladder.tile": 64, "ladder.stages": 0, "ladder.schedule": 0, "zbar.tile": 32, "zbar.stages": 0,
             "zbar.schedule": 0, "inverse.split": 0, "inverse.fp64": 0, "inverse.quad_budget": 36864,
             "inverse.desc_stage": 2048, "inverse.desc_results": 2048, "inverse.desc_weights": 0,
-            "inverse.desc_ilp": 1}
+            "inverse.desc_ilp": 1, "comm122.fused": 0}
 
 
 def _set(L, ms, name, value):
@@ -135,7 +137,17 @@ def tune_space(ig, emax, reps, fp64_margin, log):
         rec["trials"].append({"what": "inverse fp64", "inverse.fp64": variant, "ms": f64[variant]})
     chosen["inverse.fp64"] = min(f64, key=f64.get)
     _set(L, ms, "inverse.fp64", chosen["inverse.fp64"])
-    # 2. the split products: each family's (tile, stages, schedule), with the
+    # 2. the split form's comm122ss: W2 through memory, or fused tile pairs
+    best = None
+    for fused in (0, 1):
+        _set(L, ms, "comm122.fused", fused)
+        t = commutator_ms()
+        rec["trials"].append({"what": "split commutator", "comm122.fused": fused, "ms": t})
+        if best is None or t < best[0]:
+            best = (t, fused)
+    chosen["comm122.fused"] = best[1]
+    _set(L, ms, "comm122.fused", best[1])
+    # 3. the split products: each family's (tile, stages, schedule), with the
     # inverse kernel chosen above (the descriptor kernels let the Z bar
     # product skip its mirror stores)
     for fam, tiles in (("ladder", (64, 32)), ("zbar", (32, 64))):

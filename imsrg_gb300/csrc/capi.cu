@@ -210,6 +210,21 @@ void setup_device_lists(imsrg_space* sp)
   }
   sp->n_sym122 = (int)t122.size() / 3;
   sp->d_sym122 = sp->track(dcopy(t122));
+  // tile pairs (a <= b) of the fused split-form comm122ss
+  {
+    std::vector<int> tu;
+    for (int c = 0; c < s.nch; ++c) {
+      int nt = (s.ch[c].n() + 31) / 32;
+      for (int a = 0; a < nt; ++a)
+        for (int b = a; b < nt; ++b) {
+          tu.push_back(c);
+          tu.push_back(a);
+          tu.push_back(b);
+        }
+    }
+    sp->n_sym122u = (int)tu.size() / 3;
+    sp->d_sym122u = sp->track(dcopy(tu));
+  }
   sp->n_pinv = (int)tinv.size() / 3;
   sp->d_pinv = sp->track(dcopy(tinv));
   build_invq_tasks(s, sp->invq_budget);
@@ -251,7 +266,7 @@ void drop_invd(imsrg_space* sp);
 const char* kTuneNames[] = {"ladder.tile",  "ladder.stages", "ladder.schedule",     "zbar.tile",
                             "zbar.stages",  "zbar.schedule", "inverse.split",       "inverse.fp64",
                             "inverse.quad_budget", "inverse.desc_stage", "inverse.desc_results",
-                            "inverse.desc_weights", "inverse.desc_ilp"};
+                            "inverse.desc_weights", "inverse.desc_ilp", "comm122.fused"};
 constexpr int kNTune = sizeof(kTuneNames) / sizeof(kTuneNames[0]);
 
 int* tune_slot(imsrg_space* sp, int t)
@@ -270,6 +285,7 @@ int* tune_slot(imsrg_space* sp, int t)
     case 10: return &sp->invd_res;
     case 11: return &sp->invd_weights;
     case 12: return &sp->invd_ilp;
+    case 13: return &sp->comm122_fused;
   }
   return nullptr;
 }
@@ -287,6 +303,7 @@ bool tune_valid(int t, int v)
     case 10: return v >= 64 && v <= (1 << 20);
     case 11: return v == 0 || v == 1;
     case 12: return v == 1 || v == 2 || v == 4;
+    case 13: return v == 0 || v == 1;
   }
   return false;
 }
@@ -578,8 +595,12 @@ int do_122(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st, i
   if (prec == IMSRG_PREC_SPLIT) {
     if (!prepared && (rc = prep_122_df(X, Y, st))) return rc;
     ProfScope ps("comm122ss", st);
-    CUDA_TRY(launch_comm122_df(*sp->s, X->d, Y->d, Z->d, sp->d_xf, sp->d_yff, (float2*)sp->d_w2, Z->herm,
-                               sp->d_sym122, sp->n_sym122, st));
+    if (sp->comm122_fused)
+      CUDA_TRY(launch_comm122_fused_df(*sp->s, X->d, Y->d, Z->d, sp->d_xf, sp->d_yff, Z->herm, sp->d_sym122u,
+                                       sp->n_sym122u, st));
+    else
+      CUDA_TRY(launch_comm122_df(*sp->s, X->d, Y->d, Z->d, sp->d_xf, sp->d_yff, (float2*)sp->d_w2, Z->herm,
+                                 sp->d_sym122, sp->n_sym122, st));
     return IMSRG_OK;
   }
   ProfScope ps("comm122ss", st);
@@ -1551,8 +1572,12 @@ int group_mid(GroupedProducts* g, cudaStream_t st)
   const Space& s = *sp->s;
   const long long* zo = g->d_zoff;
   CUDA_TRY(launch_comm221_1b(s, X->d, Y->d, Z->d, X->herm, Z->herm, Z->d, st, zo, nz));
-  CUDA_TRY(launch_comm122_df(s, X->d, Y->d, Z->d, sp->d_xf, sp->d_yff, (float2*)sp->d_w2, Z->herm, sp->d_sym122,
-                             sp->n_sym122, st, zo, nz));
+  if (sp->comm122_fused)
+    CUDA_TRY(launch_comm122_fused_df(s, X->d, Y->d, Z->d, sp->d_xf, sp->d_yff, Z->herm, sp->d_sym122u, sp->n_sym122u,
+                                     st, zo, nz));
+  else
+    CUDA_TRY(launch_comm122_df(s, X->d, Y->d, Z->d, sp->d_xf, sp->d_yff, (float2*)sp->d_w2, Z->herm, sp->d_sym122,
+                               sp->n_sym122, st, zo, nz));
   return IMSRG_OK;
 }
 

@@ -78,6 +78,8 @@ struct imsrg_space {
   // other tile lists
   int* d_sym122 = nullptr;
   int n_sym122 = 0;
+  int* d_sym122u = nullptr;  // tile pairs a <= b (fused split-form comm122ss)
+  int n_sym122u = 0;
   int* d_pfwd = nullptr;
   int n_pfwd = 0;
   int* d_pinv = nullptr;
@@ -115,6 +117,7 @@ struct imsrg_space {
   int invd_stage = 2048, invd_res = 2048;
   int invd_weights = 0;  // descriptor kernel: 1 stages the 6j weight rows per block
   int invd_ilp = 1;      // descriptor kernel: results in flight per thread (1, 2, 4)
+  int comm122_fused = 0;  // split-form comm122ss: 1 forms W2 tiles in shared memory (no W2 round trip)
   std::string tuning_source = "default";
   // inverse Pandya descriptors (built on first use)
   imsrg::InvdDev invd;

@@ -54,6 +54,12 @@ cudaError_t launch_to_ff(const Space& s, const double* A, float2* Af, cudaStream
 cudaError_t launch_comm122_df(const Space& s, const double* X, const double* Y, double* Z, const float2* Xf,
                               const float2* Yf, float2* W2, int hZ, const int* sym_tiles, int nsym_tiles,
                               cudaStream_t st, const long long* zo = nullptr, int nz = 1);
+// the same without the W2 round trip: tile pairs (ch, a, b), a <= b, each
+// forming both W2 tiles in shared memory and updating Z(a, b) and Z(b, a)
+// (grouped)
+cudaError_t launch_comm122_fused_df(const Space& s, const double* X, const double* Y, double* Z, const float2* Xf,
+                                    const float2* Yf, int hZ, const int* tiles, int ntiles, cudaStream_t st,
+                                    const long long* zo = nullptr, int nz = 1);
 // (grouped)
 cudaError_t launch_pandya_fwd(const Space& s, const double* X, const double* Y, int hY, double* Xb, double* Yt,
                               double* Yf, const int* tiles, int ntiles, cudaStream_t st, const long long* zo = nullptr,

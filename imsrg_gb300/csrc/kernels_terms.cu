@@ -1320,6 +1320,117 @@ cudaError_t launch_to_ff(const Space& s, const double* A, float2* Af, cudaStream
   return cudaGetLastError();
 }
 
+// comm122ss in the split form without the W2 round trip: one block per pair
+// of 32 x 32 tiles (a, b), a <= b, of a channel block.  It forms W2's tile
+// (rows a, columns b) and, for a != b, its tile (rows b, columns a) in shared
+// memory -- each element the same double-float sum over the column's gather
+// list as k_comm122_w_df -- and subtracts
+//   Z(a, b) -= W2(a, b) + hZ W2(b, a)^T,  Z(b, a) -= W2(b, a) + hZ W2(a, b)^T
+// directly (src/Commutator.cc:837-932; the symmetrisation of :927-929).
+__global__ void __launch_bounds__(256) k_comm122_fused_df(DevSpace S, DevWork W, const double* __restrict__ X,
+                                                          const double* __restrict__ Y,
+                                                          const float2* __restrict__ Xf,
+                                                          const float2* __restrict__ Yf, double* __restrict__ Z,
+                                                          int hZ, const int* __restrict__ tiles, int ntiles,
+                                                          const long long* __restrict__ zo)
+{
+  X = zsh(X, zo, ZR_X);
+  Y = zsh(Y, zo, ZR_Y);
+  Xf = zsh(Xf, zo, ZR_XF);
+  Yf = zsh(Yf, zo, ZR_YF);
+  Z = zsh(Z, zo, ZR_Z);
+  __shared__ float2 cx[32][32], cy[32][32];  // per column of the tile being formed: coefficients
+  __shared__ int cl[32][32], ccnt[32];       // and source columns
+  __shared__ float2 wab[32][33], wba[32][33];
+  const int t = blockIdx.x;
+  if (t >= ntiles) return;
+  const int ch = tiles[3 * t], ta = tiles[3 * t + 1], tb = tiles[3 * t + 2];
+  const int n = S.ch_n[ch];
+  const long long off = S.ch_off[ch];
+  const int N = S.norb;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int col0 = S.ch_kofs[ch];  // the channel's first entry in the column list
+  // one tile of W2: rows from tile tr, columns from tile tc, into w
+  auto form = [&](int tr, int tc, float2 (*w)[33]) {
+    // gather lists of the tile's columns (a warp per 4 columns, a lane per item)
+    for (int cc = warp; cc < 32; cc += 8) {
+      const int c = tc * 32 + cc;
+      int cnt = 0, first = 0;
+      if (c < n) {
+        first = W.cols122[4 * (col0 + c) + 2];
+        cnt = min(W.cols122[4 * (col0 + c) + 3], 32);
+      }
+      if (lane < cnt) {
+        const int a = W.it122_a[first + lane], src = W.it122_src[first + lane];
+        const double f = W.it122_f[first + lane];
+        cx[cc][lane] = d2ff(X[32 + (size_t)src * N + a] * f);   //  X1(a, src) f multiplies Y2
+        cy[cc][lane] = d2ff(-Y[32 + (size_t)src * N + a] * f);  // -Y1(a, src) f multiplies X2
+        cl[cc][lane] = W.it122_loc[first + lane];
+      }
+      if (lane == 0) ccnt[cc] = cnt;
+    }
+    __syncthreads();
+    const int r = tr * 32 + lane;
+    for (int cc = warp; cc < 32; cc += 8) {
+      float s = 0.f, e = 0.f;
+      if (r < n) {
+        const int cnt = ccnt[cc];
+        for (int k = 0; k < cnt; ++k) {
+          const long long el = off + (long long)cl[cc][k] * n + r;
+          df_fma(cx[cc][k], Yf[el], s, e);
+          df_fma(cy[cc][k], Xf[el], s, e);
+        }
+      }
+      w[lane][cc] = make_float2(s, e);  // w[row][column]
+    }
+    __syncthreads();
+  };
+  form(ta, tb, wab);
+  if (ta != tb) form(tb, ta, wba);
+  const float2(*wt)[33] = ta != tb ? wba : wab;  // the tile holding W2(b-rows, a-columns)
+  // Z(a, b) -= W2(a, b) + hZ W2(b, a)^T: lanes over rows of tile a
+  for (int cc = warp; cc < 32; cc += 8) {
+    const int r = ta * 32 + lane, c = tb * 32 + cc;
+    if (r < n && c < n) {
+      const float2 w = wab[lane][cc];
+      float2 u = wt[cc][lane];
+      if (hZ < 0) {
+        u.x = -u.x;
+        u.y = -u.y;
+      }
+      float hi, lo;
+      df_add(w.x, w.y, u.x, u.y, hi, lo);
+      Z[off + (long long)c * n + r] -= ff2d(hi, lo);
+    }
+  }
+  if (ta == tb) return;
+  // Z(b, a) -= W2(b, a) + hZ W2(a, b)^T: lanes over rows of tile b
+  for (int cc = warp; cc < 32; cc += 8) {
+    const int r = tb * 32 + lane, c = ta * 32 + cc;
+    if (r < n && c < n) {
+      const float2 w = wba[lane][cc];
+      float2 u = wab[cc][lane];
+      if (hZ < 0) {
+        u.x = -u.x;
+        u.y = -u.y;
+      }
+      float hi, lo;
+      df_add(w.x, w.y, u.x, u.y, hi, lo);
+      Z[off + (long long)c * n + r] -= ff2d(hi, lo);
+    }
+  }
+}
+
+cudaError_t launch_comm122_fused_df(const Space& s, const double* X, const double* Y, double* Z, const float2* Xf,
+                                    const float2* Yf, int hZ, const int* tiles, int ntiles, cudaStream_t st,
+                                    const long long* zo, int nz)
+{
+  if (ntiles == 0) return cudaSuccess;
+  k_comm122_fused_df<<<dim3(ntiles, 1, nz), 256, 0, st>>>(s.dev, s.work, X, Y, Xf, Yf, Z, hZ, tiles, ntiles, zo);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_comm122_df(const Space& s, const double* X, const double* Y, double* Z, const float2* Xf,
                               const float2* Yf, float2* W2, int hZ, const int* sym_tiles, int nsym_tiles,
                               cudaStream_t st, const long long* zo, int nz)

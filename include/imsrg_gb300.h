@@ -358,6 +358,9 @@ int imsrg_batch_info(const imsrg_batch* batch, int* n_pairs, int* n_branches, in
  *                                       weight rows in shared memory
  *   "inverse.desc_ilp"                  results each thread of the descriptor
  *                                       kernel keeps in flight: 1, 2 or 4
+ *   "comm122.fused"                     split-form comm122ss: 1 forms W2 tile
+ *                                       pairs in shared memory and updates Z
+ *                                       directly (no W2 array)
  * When the space's device tables are built (its first operator), the line of
  * the tuning file whose "arena=" and "norb=" match the space is applied: the
  * file is $IMSRG_GB300_TUNING ("off" for none), else tuning/gb300.txt in the

@@ -185,7 +185,7 @@ def test_commutator_with_every_tuning(prec):
                 {"inverse.split": 2, "inverse.desc_stage": 256, "inverse.desc_results": 128},
                 {"inverse.split": 1, "inverse.desc_weights": 1}, {"inverse.split": 2, "inverse.desc_weights": 1},
                 {"inverse.split": 1, "inverse.desc_ilp": 4}, {"inverse.split": 2, "inverse.desc_ilp": 2},
-                {"inverse.quad_budget": 16384}]
+                {"inverse.quad_budget": 16384}, {"comm122.fused": 1}]
     with ig.DeviceOperator(ms, 1) as dX, ig.DeviceOperator(ms, -1) as dY, ig.DeviceOperator(ms, 1) as dZ:
         dX.upload(X)
         dY.upload(Y)
@@ -202,9 +202,11 @@ def test_commutator_with_every_tuning(prec):
                             "inverse.desc_results": 2048, "inverse.desc_ilp": 1}[k])
 
 
-def test_comm122_double_float_vs_fp64():
+@pytest.mark.parametrize("fused", [0, 1])
+def test_comm122_double_float_vs_fp64(fused):
     emax = 8
     ms = ig.ModelSpace(emax, "O16", "O16")
+    ms.set_tuning("comm122.fused", fused)
     r = ref_space(emax)
     names = ["comm110ss", "comm220ss", "comm111ss", "comm121ss", "comm122ss", "comm221ss", "comm222_pp_hhss",
              "comm222_phss"]
