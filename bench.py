@@ -11,15 +11,22 @@ scaled to unit Frobenius norm (synthetic; the reference publishes no dataset).
 
 gb300 arm (default): value = whole-job commutators/s of the split-precision form
 with operands resident in HBM, timed with CUDA events over K steps between
-barriers + synchronisations (max over ranks).  Every step reads X2, Y2 (280 MiB
-each) and writes Zbar (761 MiB), so the working set exceeds the 129 MB L2
-between steps.  Also reported: the plain FP64 form ("plain_fp64"), e2e (host
-buffers in pinned memory, H2D of X and Y + commutator + D2H of Z per step,
-through the C ABI; independent steps streamed over two operator sets, with the
-serial figure beside it), the roofline of the dominant kernel (from the library's
-CUDA-event phase timers over the timed region), SM clocks sampled during the
-timed region, the number of kernel launches, and a CPU baseline (the C oracle,
-a restatement of the reference's OpenMP + BLAS path, on all host cores).
+barriers + synchronisations (max over ranks), the library's phase timers off and
+the kernels' status word read once after the K steps.  Every step reads X2, Y2
+(280 MiB each) and writes Zbar (upper triangle, 380 MiB), so the working set
+exceeds the 129 MB L2 between steps.  Also reported: per-step event times; the
+plain FP64 form ("plain_fp64"); the per-body-rank error of both forms against
+the C oracle on the same X, Y ("rel_err_vs_oracle"); ms per BCH step
+(BCH_Transform(X, Omega) with |Omega| set so that 10-20 nested commutators run;
+split, FP64 and CPU); e2e (host buffers in pinned memory, H2D of X and Y +
+commutator + D2H of Z per step, through the C ABI; independent steps streamed
+over two operator sets, with the serial figure beside it); the 64-pair batch
+(emax 2..6, one CUDA graph, both forms); the roofline of the dominant kernel
+(from the library's CUDA-event phase timers, in a separate pass over the same
+steps); the applied kernel tuning; SM clocks sampled during the timed region;
+the number of kernel launches; and a CPU baseline (the C oracle, a restatement
+of the reference's OpenMP + BLAS path, on all host cores, on the benchmark's
+own X and Y).
 
 reference arm: the reference's CPU implementation of the path, here the C
 oracle port (the reference's own build needs the reference sources, absent on
@@ -79,6 +86,7 @@ def parse_args():
     p.add_argument("--precision", default="split", choices=["split", "fp64"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-batch", action="store_true", help="commutator workload: skip the 64-pair batch key")
     return p.parse_args()
 
 
@@ -625,6 +633,16 @@ def run_gb300(args):
            "streamed": {"value": world * ne / (pipe_ms / 1000.0), "ms_per_step": pipe_ms / ne},
            "note": "per step: H2D of X and Y from pinned host memory, the commutator, D2H of Z, through the C ABI; "
                    "streamed = uploads / downloads on their own streams, two device operator sets"}
+    # ---- the 64-pair batch (emax 2..6, one CUDA graph, both forms)
+    batch = None
+    if not args.no_batch:
+        bres, bes, _ = batch_measure(ig, L, 64, 5, 3, 4 + rank)
+        batch = {"pairs": 64, "emax_counts": {str(e): bes.count(e) for e in sorted(set(bes))},
+                 "unit": "commutators/s",
+                 "split": {k: bres["split"][k] for k in ("batched", "sequential", "speedup",
+                                                         "grouped_product_launches", "kernel_nodes")},
+                 "fp64": {k: bres["fp64"][k] for k in ("batched", "sequential", "speedup",
+                                                       "grouped_product_launches", "kernel_nodes")}}
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -672,6 +690,7 @@ def run_gb300(args):
         "bch_ms_per_step": {k: bch[k]["ms_per_bch_step"] for k in ("split", "fp64", "cpu") if k in bch}
         if bch else None,
         "e2e": e2e,
+        "batch_64_pairs": batch,
         "roofline": roof,
         "phases_ms_per_step": {k: v[0] / nprof for k, v in sorted(phases.items())},
         "phases_steps": nprof,
@@ -840,18 +859,17 @@ print(json.dumps({"t": t, "steps": st["steps"], "e0": list(st["e0_hist"]), "e0_f
 BATCH_METRIC = "[X,Y] commutators/sec, {n} independent pairs with emax drawn from {{2..6}}, one CUDA graph"
 
 
-def run_batch(args):
+def batch_measure(ig, L, npairs, K, W, seed, batch_emax=None):
+    """The 64-pair configuration: npairs independent (X, Y) pairs, emax drawn
+    from {2..6} by seed, one model space per pair; both forms timed as one
+    CUDA-graph batch and as one-by-one calls.  Returns (per form results,
+    emax list, operator bytes)."""
     import numpy as np
     import torch
-
-    import imsrg_gb300 as ig
-    world, rank, local = dist_env()
-    torch.cuda.set_device(local)
-    L = ig.lib()
-    rng = np.random.Generator(np.random.PCG64(4 + rank))
-    es = [int(e) for e in rng.choice([2, 3, 4, 5, 6], size=args.pairs)]
-    if args.batch_emax is not None:
-        es = [args.batch_emax] * args.pairs
+    rng = np.random.Generator(np.random.PCG64(seed))
+    es = [int(e) for e in rng.choice([2, 3, 4, 5, 6], size=npairs)]
+    if batch_emax is not None:
+        es = [batch_emax] * npairs
     pairs = []
     arena_bytes = 0
     for i, e in enumerate(es):
@@ -861,7 +879,6 @@ def run_batch(args):
         dY.fill_random(1001 + 2 * i)
         pairs.append((dX, dY, dZ))
         arena_bytes += 3 * 8 * ms.arena_size
-    K, W = args.steps, max(3, args.warmup)
 
     def timed(fn):
         for _ in range(W):
@@ -889,11 +906,23 @@ def run_batch(args):
         b.sync()
         launches = (L.imsrg_kernel_launches() - l0) // (K + W)
         res[prec] = {"batched_ms": bat_ms, "sequential_ms": seq_ms,
-                     "batched": args.pairs * 1000.0 / bat_ms, "sequential": args.pairs * 1000.0 / seq_ms,
+                     "batched": npairs * 1000.0 / bat_ms, "sequential": npairs * 1000.0 / seq_ms,
                      "speedup": seq_ms / bat_ms, "graph_branches": groups, "grouped_product_launches": grouped,
                      "kernel_nodes": nodes,
                      "launches_per_step": int(launches)}
         b.close()
+    return res, es, arena_bytes
+
+
+def run_batch(args):
+    import torch
+
+    import imsrg_gb300 as ig
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    L = ig.lib()
+    K, W = args.steps, max(3, args.warmup)
+    res, es, arena_bytes = batch_measure(ig, L, args.pairs, K, W, 4 + rank, args.batch_emax)
     if rank != 0:
         return
     sp = res["split"]

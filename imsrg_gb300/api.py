@@ -121,7 +121,7 @@ class ModelSpace:
         out = {}
         for tok in buf.value.decode().split():
             k, v = tok.split("=", 1)
-            out[k] = v if k == "source" else int(v)
+            out[k] = os.path.basename(v) if k == "source" else int(v)
         return out
 
     def set_tuning(self, name, value):

@@ -1454,8 +1454,13 @@ void tensor_terms_on(bool on[5])
 struct GroupedProducts {
   std::vector<const imsrg_op*> X, Y;
   std::vector<imsrg_op*> Z;
-  SplitPlan* ladder = nullptr;
+  int prec = IMSRG_PREC_SPLIT;
+  SplitPlan* ladder = nullptr;  // split form
   SplitPlan* zbar = nullptr;
+  // FP64 form: every pair's jobs and tile pairs in one list per product
+  GemmJobDev *d_lj = nullptr, *d_zj = nullptr;
+  int *d_lp = nullptr, *d_zp = nullptr;
+  int n_lp = 0, n_zp = 0;
   // byte offsets of every pair's operands and scratch from pair 0's, for
   // the grouped launches of the other kernels (kZRoles per pair)
   long long* d_zoff = nullptr;
@@ -1464,6 +1469,8 @@ struct GroupedProducts {
     if (ladder) split_plan_destroy(ladder);
     if (zbar) split_plan_destroy(zbar);
     if (d_zoff) cudaFree(d_zoff);
+    for (void* p : {(void*)d_lj, (void*)d_zj, (void*)d_lp, (void*)d_zp})
+      if (p) cudaFree(p);
   }
 };
 
@@ -1475,7 +1482,7 @@ static long long dist(const void* a, const void* b)
 }
 
 GroupedProducts* grouped_products_create(const std::vector<const imsrg_op*>& X, const std::vector<const imsrg_op*>& Y,
-                                         const std::vector<imsrg_op*>& Z, std::string* why)
+                                         const std::vector<imsrg_op*>& Z, int prec, std::string* why)
 {
   if (X.empty()) return nullptr;
   imsrg_space* s0 = X[0]->sp;
@@ -1507,10 +1514,15 @@ GroupedProducts* grouped_products_create(const std::vector<const imsrg_op*>& X, 
       zj.push_back(j);
     }
   }
+  if (prec == IMSRG_PREC_FP64 && s0->inv_fp64 == 0) {
+    if (why) *why = "the FP64 form's grouped inverse Pandya needs the descriptor kernel (inverse.fp64 = 1)";
+    return nullptr;
+  }
   GroupedProducts* g = new GroupedProducts();
   g->X = X;
   g->Y = Y;
   g->Z = Z;
+  g->prec = prec;
   std::vector<long long> zo;
   for (size_t p = 0; p < X.size(); ++p) {
     imsrg_space* sp = X[p]->sp;
@@ -1528,8 +1540,19 @@ GroupedProducts* grouped_products_create(const std::vector<const imsrg_op*>& X, 
     zo.insert(zo.end(), r, r + kZRoles);
   }
   try {
-    g->ladder = split_plan_create(*s0->s, lj, 0, s0->opt_ladder);
-    g->zbar = split_plan_create(*s0->s, zj, 1, s0->opt_zbar);
+    if (prec == IMSRG_PREC_SPLIT) {
+      g->ladder = split_plan_create(*s0->s, lj, 0, s0->opt_ladder);
+      g->zbar = split_plan_create(*s0->s, zj, 1, s0->opt_zbar);
+    } else {
+      // the FP64 products' tile pairs over every pair's jobs (offsets from pair 0's arrays)
+      std::vector<int> lp = tile_pairs(lj, symgemm_fp64_tile()), zp = tile_pairs(zj, symgemm_fp64_tile());
+      g->d_lj = dcopy(lj);
+      g->d_zj = dcopy(zj);
+      g->d_lp = dcopy(lp);
+      g->d_zp = dcopy(zp);
+      g->n_lp = (int)lp.size() / 3;
+      g->n_zp = (int)zp.size() / 3;
+    }
     g->d_zoff = dcopy(zo);
   } catch (std::exception& e) {
     if (why) *why = std::string("grouped product plans: ") + e.what();
@@ -1554,8 +1577,10 @@ int group_pre(GroupedProducts* g, cudaStream_t st)
   imsrg_space* sp = X->sp;
   const Space& s = *sp->s;
   const long long* zo = g->d_zoff;
-  CUDA_TRY(launch_to_ff(s, X->d, sp->d_xf, st, zo, nz, ZR_X, ZR_XF));
-  CUDA_TRY(launch_to_ff(s, Y->d, sp->d_yff, st, zo, nz, ZR_Y, ZR_YF));
+  if (g->prec == IMSRG_PREC_SPLIT) {
+    CUDA_TRY(launch_to_ff(s, X->d, sp->d_xf, st, zo, nz, ZR_X, ZR_XF));
+    CUDA_TRY(launch_to_ff(s, Y->d, sp->d_yff, st, zo, nz, ZR_Y, ZR_YF));
+  }
   CUDA_TRY(launch_pandya_fwd(s, X->d, Y->d, Y->herm, sp->d_xb, sp->d_yt, sp->d_yf, sp->d_pfwd, sp->n_pfwd, st, zo, nz));
   CUDA_TRY(launch_comm111_110(s, X->d, Y->d, Z->d, true, X->herm != Y->herm, st, zo, nz));
   if (X->herm != Y->herm) CUDA_TRY(launch_comm220(s, X->d, Y->d, Z->d, X->herm, st, zo, nz));
@@ -1572,7 +1597,9 @@ int group_mid(GroupedProducts* g, cudaStream_t st)
   const Space& s = *sp->s;
   const long long* zo = g->d_zoff;
   CUDA_TRY(launch_comm221_1b(s, X->d, Y->d, Z->d, X->herm, Z->herm, Z->d, st, zo, nz));
-  if (sp->comm122_fused)
+  if (g->prec == IMSRG_PREC_FP64)
+    CUDA_TRY(launch_comm122(s, X->d, Y->d, Z->d, sp->d_w2, Z->herm, sp->d_sym122, sp->n_sym122, st, zo, nz));
+  else if (sp->comm122_fused)
     CUDA_TRY(launch_comm122_fused_df(s, X->d, Y->d, Z->d, sp->d_xf, sp->d_yff, Z->herm, sp->d_sym122u, sp->n_sym122u,
                                      st, zo, nz));
   else
@@ -1587,8 +1614,8 @@ int group_post(GroupedProducts* g, cudaStream_t st)
   imsrg_op* Z = g->Z[0];
   imsrg_space* sp = g->X[0]->sp;
   const Space& s = *sp->s;
-  if (sp->inv_split != 0 || sp->n_invq > 0) {
-    int rc = inverse_pandya(sp, sp->d_zb, Z->d, Z->herm, IMSRG_PREC_SPLIT, st, g->d_zoff, nz);
+  if (g->prec == IMSRG_PREC_FP64 || sp->inv_split != 0 || sp->n_invq > 0) {
+    int rc = inverse_pandya(sp, sp->d_zb, Z->d, Z->herm, g->prec, st, g->d_zoff, nz);
     if (rc) return rc;
   } else {
     for (int p = 0; p < nz; ++p) {
@@ -1605,6 +1632,12 @@ int grouped_ladder(GroupedProducts* g, cudaStream_t st)
 {
   imsrg_space* s0 = g->X[0]->sp;
   const Space& s = *s0->s;
+  if (g->prec == IMSRG_PREC_FP64) {
+    CUDA_TRY(launch_symgemm_fp64(g->d_lj, g->d_lp, g->n_lp, g->X[0]->d, g->Y[0]->d, g->Y[0]->d, g->Z[0]->d,
+                                 s.work.kidx, s.work.kweight, s.work.phase_tab, g->Z[0]->herm,
+                                 (double)g->Y[0]->herm, st));
+    return IMSRG_OK;
+  }
   split_plan_set_accumulate(g->ladder, 0);  // Z was zeroed in the pre phase
   CUDA_TRY(launch_symgemm_split(g->ladder, g->X[0]->d, g->Y[0]->d, g->Y[0]->d, g->Z[0]->d, s.work.kidx,
                                 s.work.kweight, s.work.phase_tab, s0->d_status, g->Z[0]->herm,
@@ -1616,6 +1649,11 @@ int grouped_zbar(GroupedProducts* g, cudaStream_t st)
 {
   imsrg_space* s0 = g->X[0]->sp;
   const Space& s = *s0->s;
+  if (g->prec == IMSRG_PREC_FP64) {
+    CUDA_TRY(launch_symgemm_fp64(g->d_zj, g->d_zp, g->n_zp, s0->d_xb, s0->d_yt, s0->d_yf, s0->d_zb, s.work.kidx,
+                                 s.work.kweight, s.work.phase_tab, g->Z[0]->herm, 1.0, st));
+    return IMSRG_OK;
+  }
   split_plan_set_mirror(g->zbar, s0->inv_split == 0 ? 1 : 0);  // as group_post reads Zbar
   CUDA_TRY(launch_symgemm_split(g->zbar, s0->d_xb, s0->d_yt, s0->d_yf, s0->d_zb, s.work.kidx, s.work.kweight,
                                 s.work.phase_tab, s0->d_status, g->Z[0]->herm, 1.0, st));

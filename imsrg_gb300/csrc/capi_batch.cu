@@ -4,7 +4,7 @@
 // commutators at small emax (a few microseconds of work per kernel).
 //
 // Two graph shapes:
-//  - grouped (split form, every term on, one model space per pair): pairs of
+//  - grouped (either form, every term on, one model space per pair): pairs of
 //    the same structure form a group, and each group is one chain of
 //    launches in which every kernel of the commutator runs once for all the
 //    group's pairs (the grid's z runs over pairs; the two dense products are
@@ -104,7 +104,7 @@ int setup_grouped(imsrg_batch* b)
       Z.push_back(b->Z[i]);
     }
     std::string why;
-    GroupedProducts* g = grouped_products_create(X, Y, Z, &why);
+    GroupedProducts* g = grouped_products_create(X, Y, Z, b->prec, &why);
     if (!g) return berr(IMSRG_ERR_UNSUPPORTED, why);
     b->products.push_back(g);
     cudaStream_t s = nullptr;
@@ -204,7 +204,7 @@ int imsrg_batch_create(int n, const imsrg_op* const* X, const imsrg_op* const* Y
       }
     }
   // the grouped shape when it applies; the branch shape otherwise
-  if (precision == IMSRG_PREC_SPLIT && batch_phases_usable() && (int)b->groups.size() == n) {
+  if (batch_phases_usable() && (int)b->groups.size() == n) {
     b->grouped = true;
     if (setup_grouped(b) != IMSRG_OK) {
       for (GroupedProducts* g : b->products) grouped_products_destroy(g);

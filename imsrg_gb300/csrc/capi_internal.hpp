@@ -39,16 +39,17 @@ int end_status(imsrg_space* sp, cudaStream_t st);
 int tensor_norm_dev(const imsrg_op* op, double* out, cudaStream_t st);
 int tensor_bch_transform(const imsrg_op* OpIn, const imsrg_op* Omega, imsrg_op* OpOut, double threshold,
                          int precision, int* n_nested, cudaStream_t st);
-// the split-form commutator of a group of same-structure pairs, one launch
-// per kernel for the whole group: usable only with every term switched on
+// the commutator of a group of same-structure pairs, one launch per kernel
+// for the whole group (either form): usable only with every term switched on
 bool batch_phases_usable();
 // the scalar-tensor term switches: comm111st, comm121st, comm122st,
 // comm222_pp_hh_221st (comm222_pp_hhst and comm221st), comm222_phst
 void tensor_terms_on(bool on[5]);
 // the ladder and Zbar products of same-structure pairs as one launch each
+// (split plans, or FP64 job lists over every pair)
 struct GroupedProducts;
 GroupedProducts* grouped_products_create(const std::vector<const imsrg_op*>& X, const std::vector<const imsrg_op*>& Y,
-                                         const std::vector<imsrg_op*>& Z, std::string* why);
+                                         const std::vector<imsrg_op*>& Z, int prec, std::string* why);
 void grouped_products_destroy(GroupedProducts* g);
 int grouped_ladder(GroupedProducts* g, cudaStream_t st);
 int grouped_zbar(GroupedProducts* g, cudaStream_t st);

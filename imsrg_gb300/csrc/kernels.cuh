@@ -40,8 +40,10 @@ cudaError_t launch_comm121(const Space& s, const int* dev_holes, const double* X
 // (grouped with Mz)
 cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, double* Z, int hX, int hZ,
                               const double* Mz, cudaStream_t st, const long long* zo = nullptr, int nz = 1);
+// (grouped)
 cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, double* Z, double* W2, int hZ,
-                           const int* sym_tiles, int nsym_tiles, cudaStream_t st);
+                           const int* sym_tiles, int nsym_tiles, cudaStream_t st, const long long* zo = nullptr,
+                           int nz = 1);
 // loads launch_comm122's kernels on the current device (they are otherwise
 // loaded at their first launch under lazy module loading)
 cudaError_t load_comm122_kernels();

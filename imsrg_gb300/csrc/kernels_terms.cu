@@ -407,8 +407,11 @@ __global__ void k_comm221_1b_mz(DevSpace S, DevWork W, const double* __restrict_
 // comm122ss, src/Commutator.cc:837-932.  W2(:, ij) = sum_items f (Y2(:,loc) X1(a,src)
 // - X2(:,loc) Y1(a,src)); one block per column, threads over rows (FP64).
 __global__ void k_comm122_w(DevSpace S, DevWork W, const double* __restrict__ X, const double* __restrict__ Y,
-                            double* __restrict__ W2)
+                            double* __restrict__ W2, const long long* __restrict__ zo)
 {
+  X = zsh(X, zo, ZR_X);
+  Y = zsh(Y, zo, ZR_Y);
+  W2 = zsh(W2, zo, ZR_W2);
   int col = blockIdx.x;
   if (col >= W.ncols122) return;
   int ch = W.cols122[4 * col], ij = W.cols122[4 * col + 1];
@@ -433,8 +436,10 @@ __global__ void k_comm122_w(DevSpace S, DevWork W, const double* __restrict__ X,
 
 // Z2 -= W2 + hZ W2^T, per channel in 32x32 tiles
 __global__ void k_sym_subtract(DevSpace S, const double* __restrict__ W2, double* __restrict__ Z, int hZ,
-                               const int* __restrict__ tiles, int ntiles)
+                               const int* __restrict__ tiles, int ntiles, const long long* __restrict__ zo)
 {
+  W2 = zsh(W2, zo, ZR_W2);
+  Z = zsh(Z, zo, ZR_Z);
   __shared__ double tt[32][33];
   int t = blockIdx.x;
   if (t >= ntiles) return;
@@ -1281,14 +1286,14 @@ cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, 
 }
 
 cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, double* Z, double* W2, int hZ,
-                           const int* sym_tiles, int nsym_tiles, cudaStream_t st)
+                           const int* sym_tiles, int nsym_tiles, cudaStream_t st, const long long* zo, int nz)
 {
   if (s.work.ncols122 == 0) return cudaSuccess;
-  k_comm122_w<<<s.work.ncols122, 128, 0, st>>>(s.dev, s.work, X, Y, W2);
+  k_comm122_w<<<dim3(s.work.ncols122, 1, nz), 128, 0, st>>>(s.dev, s.work, X, Y, W2, zo);
   count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_sym_subtract<<<nsym_tiles, 256, 0, st>>>(s.dev, W2, Z, hZ, sym_tiles, nsym_tiles);
+  k_sym_subtract<<<dim3(nsym_tiles, 1, nz), 256, 0, st>>>(s.dev, W2, Z, hZ, sym_tiles, nsym_tiles, zo);
   count_launch();
   return cudaGetLastError();
 }

@@ -315,10 +315,12 @@ int imsrg_get_term(const char* name, int* on);
  * imsrg_commutator_scalar_scalar), of any mix of model spaces and sizes,
  * recorded once into a CUDA graph and replayed by imsrg_batch_launch.  Pairs
  * that share a model space run one after the other (they share its scratch);
- * pairs of different spaces run concurrently, one graph branch per space.  In
- * the split form with every term on and one model space per pair, the two
- * dense products of all pairs whose spaces have the same orbits (and whose
- * operators the same hermiticities) run as one grouped launch each.
+ * pairs of different spaces run concurrently, one graph branch per space.
+ * With every term on and one model space per pair, every kernel of the
+ * commutator (both dense products included) runs as one grouped launch for
+ * all pairs whose spaces have the same orbits and whose operators the same
+ * hermiticities, in either precision (the FP64 form needs the descriptor
+ * inverse Pandya kernel, "inverse.fp64" = 1, as tuned).
  * Creating a batch evaluates every pair once (allocating all scratch) and
  * captures the graph; the operators, their spaces and the term switches are
  * fixed from then on, and every operator must outlive the batch.  No Z may

@@ -42,8 +42,9 @@ def test_batch_matches_single_launches(prec):
     b = ig.CommutatorBatch(pairs, prec)
     n, branches, grouped, nodes = b.info()
     assert (n, branches) == (64, 64) and nodes > 64
-    # split form: the products of the pairs of each emax run as one launch
-    assert grouped == (5 if prec == "split" else 0)
+    # both forms: the products (and every other kernel) of the pairs of each
+    # emax run as one launch
+    assert grouped == 5
     for _, _, dZ in pairs:
         dZ.zero()
     for _ in range(2):
