@@ -12,6 +12,9 @@ the choices that imsrg_space_set_tuning exposes and keeps the fastest:
   split-form commutators (the products share the GPU with the second stream);
 - the split form's comm122ss with W2 through memory or fused tile pairs,
   timed as whole split-form commutators;
+- the digits per operand of each product family (the precision), kept only
+  when the split commutator stays within a third of the 1e-10 error bound
+  against the FP64 one on the same operators;
 - the inverse Pandya kernel of each form and its block sizes, timed alone
   (imsrg_add_inverse_pandya on a Z bar of the space's layout).  Among the
   split form's kernels, the FP64 descriptor kernel (the reference's FP64
@@ -35,7 +38,23 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 DEFAULTS = {"ladder.tile": 64, "ladder.stages": 0, "ladder.schedule": 0, "zbar.tile": 32, "zbar.stages": 0,
             "zbar.schedule": 0, "inverse.split": 0, "inverse.fp64": 0, "inverse.quad_budget": 36864,
             "inverse.desc_stage": 2048, "inverse.desc_results": 2048, "inverse.desc_weights": 0,
-            "inverse.desc_ilp": 1, "comm122.fused": 0}
+            "inverse.desc_ilp": 1, "comm122.fused": 0, "ladder.digits": 0, "zbar.digits": 0}
+
+
+ERR_GATE = 1e-10 / 3
+
+
+def _rank_error(a, b, norb):
+    """Largest relative Frobenius difference of arena a against b over the
+    zero-, one- and two-body parts."""
+    import numpy as np
+    o2 = (32 + norb * norb + 31) // 32 * 32
+    worst = 0.0
+    for x, y in ((a[:1], b[:1]), (a[32:32 + norb * norb], b[32:32 + norb * norb]), (a[o2:], b[o2:])):
+        ny = float(np.linalg.norm(y))
+        d = float(np.linalg.norm(x - y))
+        worst = max(worst, d / ny if ny > 0 else d)
+    return worst
 
 
 def _set(L, ms, name, value):
@@ -165,6 +184,29 @@ def tune_space(ig, emax, reps, fp64_margin, log):
         for k, v in best[1].items():
             _set(L, ms, k, v)
             chosen[k] = v
+    # 4. digits per operand of each product family, under the accuracy gate:
+    # the split commutator's error against the FP64 one on the same X, Y
+    # (per body rank) stays within a third of the 1e-10 bound
+    ig.Commutator.device_commutator(dX, dY, dZ, "fp64")
+    zf = dZ.download()
+
+    def split_error():
+        ig.Commutator.device_commutator(dX, dY, dZ, "split")
+        ms.check_status()
+        return _rank_error(dZ.download(), zf, ms.norb)
+
+    for fam in ("zbar", "ladder"):
+        best = None
+        for digits in (0, 5):
+            _set(L, ms, fam + ".digits", digits)
+            err = split_error()
+            t = commutator_ms()
+            rec["trials"].append({"what": "split commutator", fam + ".digits": digits, "ms": t, "max_rel_err": err})
+            if err <= ERR_GATE and (best is None or t < best[0]):
+                best = (t, digits)
+        chosen[fam + ".digits"] = best[1] if best else 0
+        _set(L, ms, fam + ".digits", chosen[fam + ".digits"])
+    rec["split_max_rel_err_tuned"] = split_error()
     rec["inverse_split_candidates_ms"] = {str(k): v[0] for k, v in cands.items()}
     rec["commutator_ms_tuned"] = commutator_ms()
     for k, v in DEFAULTS.items():

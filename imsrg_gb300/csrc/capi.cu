@@ -266,7 +266,8 @@ void drop_invd(imsrg_space* sp);
 const char* kTuneNames[] = {"ladder.tile",  "ladder.stages", "ladder.schedule",     "zbar.tile",
                             "zbar.stages",  "zbar.schedule", "inverse.split",       "inverse.fp64",
                             "inverse.quad_budget", "inverse.desc_stage", "inverse.desc_results",
-                            "inverse.desc_weights", "inverse.desc_ilp", "comm122.fused"};
+                            "inverse.desc_weights", "inverse.desc_ilp", "comm122.fused", "ladder.digits",
+                            "zbar.digits"};
 constexpr int kNTune = sizeof(kTuneNames) / sizeof(kTuneNames[0]);
 
 int* tune_slot(imsrg_space* sp, int t)
@@ -286,6 +287,8 @@ int* tune_slot(imsrg_space* sp, int t)
     case 11: return &sp->invd_weights;
     case 12: return &sp->invd_ilp;
     case 13: return &sp->comm122_fused;
+    case 14: return &sp->opt_ladder.digits;
+    case 15: return &sp->opt_zbar.digits;
   }
   return nullptr;
 }
@@ -304,6 +307,7 @@ bool tune_valid(int t, int v)
     case 11: return v == 0 || v == 1;
     case 12: return v == 1 || v == 2 || v == 4;
     case 13: return v == 0 || v == 1;
+    case 14: case 15: return v == 0 || (v >= 5 && v <= 7);
   }
   return false;
 }
@@ -318,11 +322,11 @@ int tune_apply(imsrg_space* sp, int t, int v)
   *slot = v;
   if (t == 0 || t == 3) (t == 0 ? sp->opt_ladder : sp->opt_zbar).nacc = v == 64 ? 1 : (v == 32 ? 2 : 0);
   if (!sp->dev_ready) return IMSRG_OK;
-  if (t <= 2 && sp->split_ladder) {
+  if ((t <= 2 || t == 14) && sp->split_ladder) {
     split_plan_destroy(sp->split_ladder);
     sp->split_ladder = nullptr;
   }
-  if (t >= 3 && t <= 5 && sp->split_zbar) {
+  if (((t >= 3 && t <= 5) || t == 15) && sp->split_zbar) {
     split_plan_destroy(sp->split_zbar);
     sp->split_zbar = nullptr;
   }

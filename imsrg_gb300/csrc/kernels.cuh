@@ -175,6 +175,7 @@ struct SplitPlan;
 // per CTA on the tiles' K-block counts.
 struct SplitOpts {
   int tn = 0, nacc = 0, stages = 0, sched = 0;
+  int digits = 0;  // digits per operand (5..7; 0: enough for 36 bits at the width exactness allows)
 };
 SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs, int family,
                              const SplitOpts& opts = SplitOpts());

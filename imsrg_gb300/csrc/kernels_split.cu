@@ -913,6 +913,7 @@ SplitOpts split_plan_opts(const SplitPlan* p)
   o.tn = p->tn;
   o.nacc = p->nacc;
   o.stages = p->nstages;
+  o.digits = p->S;
   o.sched = p->sched;
   return o;
 }
@@ -949,6 +950,19 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
   int Kmax = 1;
   for (const GemmJobDev& j : jobs_in) Kmax = std::max(Kmax, j.K);
   choose_digits(Kmax, p->beta, p->S);
+  // a requested digit count keeps the digit width (set by exactness) and
+  // changes the precision: beta * S bits per operand row
+  if (opts.digits != 0) {
+    if (opts.digits < 5 || opts.digits > MAX_S) {
+      delete p;
+      throw std::invalid_argument("split plan: digits must be 5, 6 or 7");
+    }
+    if (p->beta * opts.digits > 42) {
+      delete p;
+      throw std::invalid_argument("split plan: digits x digit width above 42 bits");
+    }
+    p->S = opts.digits;
+  }
   long long row = 0, erow = 0;
   int kstride = KB;
   std::vector<SplitTile> tiles;

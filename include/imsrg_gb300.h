@@ -360,6 +360,11 @@ int imsrg_batch_info(const imsrg_batch* batch, int* n_pairs, int* n_branches, in
  *                                       weight rows in shared memory
  *   "inverse.desc_ilp"                  results each thread of the descriptor
  *                                       kernel keeps in flight: 1, 2 or 4
+ *   "ladder.digits", "zbar.digits"      digits per operand of the split
+ *                                       products, 5..7 (0: as many as 36 bits
+ *                                       need at the digit width that keeps the
+ *                                       leading FP32 sums exact); the width
+ *                                       times the count is the precision
  *   "comm122.fused"                     split-form comm122ss: 1 forms W2 tile
  *                                       pairs in shared memory and updates Z
  *                                       directly (no W2 array)
