@@ -64,7 +64,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "[X,Y] commutators/sec at emax=10: split-prec vs FP64 on 1 GB300, <=1e-10 rel err"
+METRIC = "[X,Y] commutators/sec at emax={emax}: split-prec vs FP64 on 1 GB300, <=1e-10 rel err"
 UNIT = "commutators/s"
 WORKLOAD = ("IMSRG(2) CommutatorScalarScalar [X,Y], emax={emax} O16, X hermitian / Y anti-hermitian, "
             "uniform[-1,1], unit Frobenius per channel")
@@ -349,7 +349,7 @@ print(json.dumps({"t": t, "threads": o.num_threads()}))
     d = json.loads(r.stdout.strip().splitlines()[-1])
     value = args.steps / d["t"]
     out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "metric": METRIC.format(emax=args.emax), "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * d["t"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
@@ -671,7 +671,7 @@ def run_gb300(args):
         except Exception as ex:  # reported, not fatal
             cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": "failed: %s" % ex}
     out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": METRIC.format(emax=args.emax), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": warm, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD.format(emax=args.emax), "emax": args.emax, "orbits": ms.norb,
