@@ -186,7 +186,7 @@ def test_commutator_with_every_tuning(prec):
                 {"inverse.split": 1, "inverse.desc_weights": 1}, {"inverse.split": 2, "inverse.desc_weights": 1},
                 {"inverse.split": 1, "inverse.desc_ilp": 4}, {"inverse.split": 2, "inverse.desc_ilp": 2},
                 {"inverse.quad_budget": 16384}, {"comm122.fused": 1}, {"zbar.digits": 5},
-                {"ladder.digits": 7}]
+                {"ladder.digits": 5}]
     with ig.DeviceOperator(ms, 1) as dX, ig.DeviceOperator(ms, -1) as dY, ig.DeviceOperator(ms, 1) as dZ:
         dX.upload(X)
         dY.upload(Y)
