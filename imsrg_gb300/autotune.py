@@ -14,7 +14,7 @@ the choices that imsrg_space_set_tuning exposes and keeps the fastest:
   timed as whole split-form commutators;
 - the digits per operand of each product family (the precision), kept only
   when the split commutator stays within a third of the 1e-10 error bound
-  against the FP64 one on the same operators;
+  against the FP64 one on the same operators, in every two-body channel block;
 - the inverse Pandya kernel of each form and its block sizes, timed alone
   (imsrg_add_inverse_pandya on a Z bar of the space's layout).  Among the
   split form's kernels, the FP64 descriptor kernel (the reference's FP64
@@ -44,16 +44,24 @@ DEFAULTS = {"ladder.tile": 64, "ladder.stages": 0, "ladder.schedule": 0, "zbar.t
 ERR_GATE = 1e-10 / 3
 
 
-def _rank_error(a, b, norb):
+def _rank_error(a, b, ms):
     """Largest relative Frobenius difference of arena a against b over the
-    zero-, one- and two-body parts."""
+    zero- and one-body parts and every two-body channel block (blocks whose
+    reference norm is below 1e-12 of the whole are compared against the
+    whole)."""
     import numpy as np
-    o2 = (32 + norb * norb + 31) // 32 * 32
+    N = ms.norb
+    tot = max(float(np.linalg.norm(b)), 1e-300)
+    parts = [(a[:1], b[:1]), (a[32:32 + N * N], b[32:32 + N * N])]
+    for c in ms.channels:
+        n, o = c["nkets"], c["offset"]
+        if n:
+            parts.append((a[o:o + n * n], b[o:o + n * n]))
     worst = 0.0
-    for x, y in ((a[:1], b[:1]), (a[32:32 + norb * norb], b[32:32 + norb * norb]), (a[o2:], b[o2:])):
+    for x, y in parts:
         ny = float(np.linalg.norm(y))
         d = float(np.linalg.norm(x - y))
-        worst = max(worst, d / ny if ny > 0 else d)
+        worst = max(worst, d / ny if ny > 1e-12 * tot else d / tot)
     return worst
 
 
@@ -186,14 +194,15 @@ def tune_space(ig, emax, reps, fp64_margin, log):
             chosen[k] = v
     # 4. digits per operand of each product family, under the accuracy gate:
     # the split commutator's error against the FP64 one on the same X, Y
-    # (per body rank) stays within a third of the 1e-10 bound
+    # (zero- and one-body parts and every two-body channel block) stays within
+    # a third of the 1e-10 bound
     ig.Commutator.device_commutator(dX, dY, dZ, "fp64")
     zf = dZ.download()
 
     def split_error():
         ig.Commutator.device_commutator(dX, dY, dZ, "split")
         ms.check_status()
-        return _rank_error(dZ.download(), zf, ms.norb)
+        return _rank_error(dZ.download(), zf, ms)
 
     for fam in ("zbar", "ladder"):
         best = None
