@@ -194,15 +194,24 @@ def tune_space(ig, emax, reps, fp64_margin, log):
             chosen[k] = v
     # 4. digits per operand of each product family, under the accuracy gate:
     # the split commutator's error against the FP64 one on the same X, Y
-    # (zero- and one-body parts and every two-body channel block) stays within
-    # a third of the 1e-10 bound
-    ig.Commutator.device_commutator(dX, dY, dZ, "fp64")
-    zf = dZ.download()
+    # (zero- and one-body parts and every two-body channel block, for a
+    # hermitian and an anti-hermitian Z) stays within a third of the 1e-10 bound
+    # both symmetry cases of Z: [X, Y] (X hermitian, Y anti-hermitian) and
+    # [X, W] (both hermitian)
+    dW = ig.DeviceOperator(ms, 1)
+    dW.fill_random(13)
+    refs = []
+    for dB in (dY, dW):
+        ig.Commutator.device_commutator(dX, dB, dZ, "fp64")
+        refs.append((dB, dZ.download()))
 
     def split_error():
-        ig.Commutator.device_commutator(dX, dY, dZ, "split")
-        ms.check_status()
-        return _rank_error(dZ.download(), zf, ms)
+        worst = 0.0
+        for dB, zf in refs:
+            ig.Commutator.device_commutator(dX, dB, dZ, "split")
+            ms.check_status()
+            worst = max(worst, _rank_error(dZ.download(), zf, ms))
+        return worst
 
     for fam in ("zbar", "ladder"):
         best = None
@@ -224,7 +233,7 @@ def tune_space(ig, emax, reps, fp64_margin, log):
     rec["chosen"] = chosen
     log.append(rec)
     del zbar
-    for d in (dX, dY, dZ):
+    for d in (dX, dY, dZ, dW):
         d.close()
     return ms.arena_size, ms.norb, chosen
 
