@@ -443,6 +443,9 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
   const double* B = (jb.bsel ? B1 : B0) + jb.b_off;
   const int P = beta * S;
   const long long half = 1ll << (beta - 1), mask = (1ll << beta) - 1;
+  long long bias = 0;
+#pragma unroll
+  for (int s = 1; s < S; ++s) bias += half << (beta * (S - 1 - s));
   // column pair (tt, tt + 1) of row r: thread layout r fastest (coalesced
   // column reads), the two digits of a pair packed in one 32-bit word
   for (int e = threadIdx.x; e < 32 * (KB / 2); e += 256) {
@@ -466,37 +469,23 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
           }
         }
       }
-      // digits of |q| by shifts (32-bit digit arithmetic), then the carry that
-      // makes them balanced, then the sign: |d| <= 2^(beta-1) below the top
-      // digit, |d_1| <= 2^beta + 1
-      const unsigned long long ua = (unsigned long long)(qa < 0 ? -qa : qa);
-      const unsigned long long ub = (unsigned long long)(qb < 0 ? -qb : qb);
-      int da[S], db[S];
+      // balanced digits by one biased add: the lower digits are the beta-bit
+      // fields of q + bias minus half, the top digit the arithmetic shift of
+      // the rest (bias = half * sum_{s >= 1} 2^(beta (S-1-s)), so the digits
+      // still sum to q): |d| <= 2^(beta-1) below the top digit,
+      // |d_1| <= 2^beta + 1
+      const long long qa2 = qa + bias, qb2 = qb + bias;
 #pragma unroll
       for (int s = 0; s < S; ++s) {
         const int sh = beta * (S - 1 - s);
-        da[s] = (int)(ua >> sh);
-        db[s] = (int)(ub >> sh);
-        if (s > 0) {
-          da[s] &= (int)mask;
-          db[s] &= (int)mask;
+        int xa, xb;
+        if (s == 0) {
+          xa = (int)(qa2 >> sh);
+          xb = (int)(qb2 >> sh);
+        } else {
+          xa = (int)((qa2 >> sh) & mask) - (int)half;
+          xb = (int)((qb2 >> sh) & mask) - (int)half;
         }
-      }
-#pragma unroll
-      for (int s = S - 1; s >= 1; --s) {
-        if (da[s] >= (int)half) {
-          da[s] -= (int)(mask + 1);
-          da[s - 1] += 1;
-        }
-        if (db[s] >= (int)half) {
-          db[s] -= (int)(mask + 1);
-          db[s - 1] += 1;
-        }
-      }
-#pragma unroll
-      for (int s = 0; s < S; ++s) {
-        const int xa = qa < 0 ? -da[s] : da[s];
-        const int xb = qb < 0 ? -db[s] : db[s];
         // small integer -> bf16 bits (exact): 1.5*2^23 magic
         const unsigned ba = __float_as_uint(__int_as_float(0x4B400000 + xa) - 12582912.0f) >> 16;
         const unsigned bb = __float_as_uint(__int_as_float(0x4B400000 + xb) - 12582912.0f) >> 16;
