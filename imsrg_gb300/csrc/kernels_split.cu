@@ -29,7 +29,8 @@
 //    output (the rectangular products of the scalar-tensor commutator).
 //
 // Kernel layout (persistent, one CTA per SM, 320 threads):
-//   warp 0: TMA producer (cp.async.bulk.tensor, 64B swizzle, mbarrier pipeline)
+//   warp 0: TMA producer (cp.async.bulk.tensor, 64B swizzle, mbarrier pipeline;
+//           one 3-D box per operand and stage, holding every digit plane)
 //   warp 1: TMEM allocator + single-thread MMA issuer
 //   warps 2-9: epilogue (two warps per TMEM lane quarter, each on half the columns)
 // Every mbarrier wait is bounded; a timeout sets the status word and the CTA
@@ -69,9 +70,9 @@ struct SplitJob {
   int kidx_off, w_off, phase_off;
   int bsel, sign, accumulate;
   double bscale;
-  // slice layout
-  long long row_base;  // first row of this job in the slice arrays (slice s at row_base + s * m_pad)
-  long long exp_base;  // first row of this job in the exponent arrays
+  // slice layout: digit s of row i of this job is row exp_base + i of digit
+  // plane s (every slice array is S planes of the same row count)
+  long long exp_base;  // first row of this job in the exponent arrays and in each digit plane
   int m_pad, K_pad, nkb;
   int nosym, n;        // plain product: B rows (n = m for the symmetrised form)
   int nkt;             // K blocks per tile: nkb (plain) or 2 nkb (K doubled)
@@ -87,7 +88,7 @@ struct SplitPlan {
   int family = 0;
   int S = 6, beta = 6;
   int K_stride = 0;
-  long long total_rows = 0, total_exp_rows = 0;
+  long long total_exp_rows = 0;   // rows of one digit plane (and of the exponent arrays)
   int njobs = 0, ntiles = 0;
   std::vector<SplitJob> jobs;
   SplitJob* d_jobs = nullptr;
@@ -100,7 +101,9 @@ struct SplitPlan {
   int4* d_rblk = nullptr;   // exponent blocks (job, 32-row group, 256-column chunk)
   int4* d_dblk = nullptr;   // digit blocks (job, 32-row group, KB-column chunk), jobs in reverse order
   int n_rblk = 0, n_dblk = 0;
-  CUtensorMap maps[4];
+  // 3-D maps (K, plane row, digit): A-operand role (TILE_M-row boxes) of
+  // alpha, beta, gamma, then B-operand role (tn-row boxes) of alpha, beta, delta
+  CUtensorMap maps[6];
   int grid = 0;
   size_t smem = 0;
   int nstages = 0;
@@ -154,12 +157,13 @@ __device__ __forceinline__ bool mbar_wait(unsigned a, unsigned parity, unsigned 
   return false;
 }
 
-__device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap* map, int x, int y, unsigned bar)
+// one box of all S digit planes: coordinates (K element, plane row, digit 0)
+__device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap* map, int x, int y, unsigned bar)
 {
   asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          dst),
-      "l"((unsigned long long)map), "r"(x), "r"(y), "r"(bar)
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(dst),
+      "l"((unsigned long long)map), "r"(x), "r"(y), "r"(0), "r"(bar)
       : "memory");
 }
 
@@ -396,7 +400,7 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
                                                      const int* __restrict__ phase, double gbscale, int gsign,
                                                      const int* __restrict__ rexpA, const int* __restrict__ rexpB,
                                                      const int* __restrict__ jobmax, const int* __restrict__ flags,
-                                                     int beta, int K_stride,
+                                                     int beta, int K_stride, long long plane_rows,
                                                      __nv_bfloat16* __restrict__ alpha, __nv_bfloat16* __restrict__ bet,
                                                      __nv_bfloat16* __restrict__ gam, __nv_bfloat16* __restrict__ del)
 {
@@ -504,7 +508,7 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
   // stores: each thread one 16-byte vector (8 digits) of one row of one slice
   for (int e = threadIdx.x; e < S * 32 * (KB / 8); e += 256) {
     const int v = e % (KB / 8), r = (e / (KB / 8)) & 31, s = e / (32 * (KB / 8));
-    const long long row = jb.row_base + (long long)s * jb.m_pad + r0 + r;
+    const long long row = (long long)s * plane_rows + jb.exp_base + r0 + r;
     const long long o = row * K_stride + t0 + v * 8;
     const unsigned* qa = &dA[s][r][v * 4];
     const unsigned* qb = &dB[s][r][v * 4];
@@ -550,11 +554,16 @@ struct GemmArgs {
 // TN: tile columns (UMMA N); NACC: TMEM accumulator sets (2 lets the
 // epilogue of one tile overlap the MMAs of the next); EPIW: epilogue warps
 // (4 or 8; with 8, two warps share a TMEM lane quarter and split the columns).
+// The maps: the A-operand role (TILE_M-row boxes) of alpha, beta, gamma and
+// the B-operand role (TN-row boxes) of alpha, beta, delta; each box holds all
+// S digit planes, so one stage is two TMA loads.
 template <int S, int TN, int NACC, int EPIW>
-__global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_constant__ CUtensorMap mAlpha,
-                                                                 const __grid_constant__ CUtensorMap mBeta,
-                                                                 const __grid_constant__ CUtensorMap mGamma,
-                                                                 const __grid_constant__ CUtensorMap mDelta,
+__global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_constant__ CUtensorMap mAlphaA,
+                                                                 const __grid_constant__ CUtensorMap mBetaA,
+                                                                 const __grid_constant__ CUtensorMap mGammaA,
+                                                                 const __grid_constant__ CUtensorMap mAlphaB,
+                                                                 const __grid_constant__ CUtensorMap mBetaB,
+                                                                 const __grid_constant__ CUtensorMap mDeltaB,
                                                                  GemmArgs g)
 {
   static_assert(NACC * S * TN <= 512, "TMEM accumulators exceed 512 columns");
@@ -617,11 +626,17 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
       const int tend = g.cta_first[blockIdx.x + 1];
       for (int tix = g.cta_first[blockIdx.x]; tix < tend && !s_err; ++tix) {
         const SplitTile tl = g.tiles[tix];
-        const SplitJob& jb = g.jobs[tl.job];
+        // the job's fields are copied to registers: the TMA and MMA asm
+        // statements clobber memory, which would reload them from global
+        const SplitJob* jp = g.jobs + tl.job;
+        const long long exp_base = jp->exp_base;
+        const int nkt = jp->nkt, nkb = jp->nkb;
         const bool useG = g.flags[2 * tl.job] != 0, useD = g.flags[2 * tl.job + 1] != 0;
-        const CUtensorMap* mA2 = useG ? &mGamma : &mBeta;
-        const CUtensorMap* mB2 = useD ? &mDelta : &mAlpha;
-        for (int kb = 0; kb < jb.nkt; ++kb, ++it) {
+        const CUtensorMap* mA2 = useG ? &mGammaA : &mBetaA;
+        const CUtensorMap* mB2 = useD ? &mDeltaB : &mAlphaB;
+        const int rowA = (int)(exp_base + tl.I * TILE_M);
+        const int rowB = (int)(exp_base + tl.J * TN);
+        for (int kb = 0; kb < nkt; ++kb, ++it) {
           int st = it % NST;
           unsigned ph = (unsigned)((it / NST) & 1);
           if (!mbar_wait(empty_bar(st), ph ^ 1u)) {
@@ -630,21 +645,16 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
             break;
           }
           mbar_expect_tx(full_bar(st), STAGE);
-          const bool second = kb >= jb.nkb;
-          const int k = (second ? kb - jb.nkb : kb) * KB;
-          const CUtensorMap* ma = second ? mA2 : &mAlpha;
-          const CUtensorMap* mb = second ? mB2 : &mBeta;
-          unsigned sA = sbase + st * STAGE;
-          unsigned sB = sA + S * A_SLICE;
-          for (int s = 0; s < S; ++s) {
-            int rowA = (int)(jb.row_base + (long long)s * jb.m_pad + tl.I * TILE_M);
-            int rowB = (int)(jb.row_base + (long long)s * jb.m_pad + tl.J * TN);
-            // the maps load TN-row boxes: an A tile is TILE_M / TN of them
-#pragma unroll
-            for (int h = 0; h < TILE_M / TN; ++h)
-              tma_load_2d(sA + s * A_SLICE + h * TN * KB * 2, ma, k, rowA + h * TN, full_bar(st));
-            tma_load_2d(sB + s * B_SLICE, mb, k, rowB, full_bar(st));
-          }
+          const bool second = kb >= nkb;
+          const int k = (second ? kb - nkb : kb) * KB;
+          const CUtensorMap* ma = second ? mA2 : &mAlphaA;
+          const CUtensorMap* mb = second ? mB2 : &mBetaB;
+          // digit plane s of a box lands s slices after the box start: the A
+          // digit tiles at sA + s A_SLICE, the B digit tiles at sB + t B_SLICE
+          const unsigned sA = sbase + st * STAGE;
+          const unsigned sB = sA + S * A_SLICE;
+          tma_load_3d(sA, ma, k, rowA, full_bar(st));
+          tma_load_3d(sB, mb, k, rowB, full_bar(st));
         }
       }
     }
@@ -655,7 +665,7 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
       int it = 0, tc = 0;
       const int tend = g.cta_first[blockIdx.x + 1];
       for (int tix = g.cta_first[blockIdx.x]; tix < tend && !s_err; ++tix, ++tc) {
-        const SplitJob& jb = g.jobs[g.tiles[tix].job];
+        const int nkt = g.jobs[g.tiles[tix].job].nkt;
         const int b = tc % NACC;
         if (!mbar_wait(acc_empty(b), (unsigned)(((tc / NACC) & 1) ^ 1))) {
           set_status(g.status, 102);
@@ -665,7 +675,7 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
         tc_fence_after();
         const unsigned dbase = tmem + (unsigned)(b * S * TN);
         bool ok = true;
-        for (int kb = 0; kb < jb.nkt; ++kb, ++it) {
+        for (int kb = 0; kb < nkt; ++kb, ++it) {
           int st = it % NST;
           unsigned ph = (unsigned)((it / NST) & 1);
           if (!mbar_wait(full_bar(st), ph)) {
@@ -716,7 +726,12 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
     const int tend = g.cta_first[blockIdx.x + 1];
     for (int tix = g.cta_first[blockIdx.x]; tix < tend; ++tix, ++tc) {
       const SplitTile tl = g.tiles[tix];
-      const SplitJob& jb = g.jobs[tl.job];
+      // the job's fields in registers (a reference would be re-read after
+      // every store to the output, which the compiler cannot tell apart)
+      const SplitJob* jp = g.jobs + tl.job;
+      const int jm = jp->m, jn = jp->n, ldo = jp->ldo, nosym = jp->nosym, phase_off = jp->phase_off;
+      const int jsign = jp->sign, jacc = jp->accumulate;
+      const long long exp_base = jp->exp_base, out_off = jp->out_off;
       const int b = tc % NACC;
       // the epilogue warps decide together (named barrier 1), so a timeout
       // never leaves one of them waiting at a barrier alone
@@ -724,16 +739,16 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
         set_status(g.status, 104);
         s_epi_err = 1;
       }
-      const int c = jb.nosym ? 0 : job_c(g.jobmax, tl.job);
-      const int* ph = jb.phase_off >= 0 ? g.phase + jb.phase_off : nullptr;
+      const int c = nosym ? 0 : job_c(g.jobmax, tl.job);
+      const int* ph = phase_off >= 0 ? g.phase + phase_off : nullptr;
       // column exponents and phases of this tile (a plain job's columns are
       // B rows with their own exponents)
       if (et < TN) {
         const int j = tl.J * TN + et;
-        const bool ok = j < jb.n;
+        const bool ok = j < jn;
         s_colexp[tc & 1][et] = !ok ? EXP_NONE
-                               : jb.nosym ? own_exp(g.rexpB[jb.exp_base + j])
-                                          : row_exp(g.rexpA[jb.exp_base + j], g.rexpB[jb.exp_base + j], c);
+                               : nosym ? own_exp(g.rexpB[exp_base + j])
+                                          : row_exp(g.rexpA[exp_base + j], g.rexpB[exp_base + j], c);
         s_colph[tc & 1][et] = (ph && ok) ? ph[j] : 1;
       }
       asm volatile("bar.sync 1, %0;" ::"r"(EPI_T) : "memory");
@@ -742,16 +757,16 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
         break;
       }
       tc_fence_after();
-      const int sign = jb.sign != 0 ? jb.sign : g.gsign;
+      const int sign = jsign != 0 ? jsign : g.gsign;
       const int i = tl.I * TILE_M + q * 32 + lane;
-      const bool rowok = i < jb.m;
+      const bool rowok = i < jm;
       const int ai = !rowok   ? EXP_NONE
-                     : jb.nosym ? own_exp(g.rexpA[jb.exp_base + i])
-                                : row_exp(g.rexpA[jb.exp_base + i], g.rexpB[jb.exp_base + i], c);
+                     : nosym ? own_exp(g.rexpA[exp_base + i])
+                                : row_exp(g.rexpA[exp_base + i], g.rexpB[exp_base + i], c);
       const int phi_i = (ph && rowok) ? ph[i] : 1;
-      double* O = g.out + jb.out_off;
+      double* O = g.out + out_off;
       const int Xi = ai + c - g.beta * (S + 1);
-      const bool accumulate = g.accum > 0 || (g.accum < 0 && jb.accumulate);
+      const bool accumulate = g.accum > 0 || (g.accum < 0 && jacc);
       const unsigned tbase = tmem + ((unsigned)(q * 32) << 16) + (unsigned)(b * S * TN);
       for (int c0 = cbeg; c0 < cbeg + COLS_W; c0 += EPI_COLS) {
         unsigned r[MAX_S][EPI_COLS];
@@ -765,8 +780,8 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
 #pragma unroll
         for (int cc = 0; cc < EPI_COLS; ++cc) {
           const int j = tl.J * TN + c0 + cc;
-          wd[cc] = rowok && j < jb.n && !(tl.diag && i > j);
-          wm[cc] = wd[cc] && i != j && !jb.nosym && !g.nomirror;
+          wd[cc] = rowok && j < jn && !(tl.diag && i > j);
+          wm[cc] = wd[cc] && i != j && !nosym && !g.nomirror;
           // exact merge of the weight groups: Horner in base 2^beta
           long long I64 = __float2int_rn(__uint_as_float(r[0][cc]));
 #pragma unroll
@@ -783,22 +798,22 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
 #pragma unroll
           for (int cc = 0; cc < EPI_COLS; ++cc) {
             const long long j = tl.J * TN + c0 + cc;
-            if (wd[cc]) od[cc] = __ldcg(O + j * jb.ldo + i);
-            if (wm[cc]) om[cc] = __ldcg(O + (long long)i * jb.ldo + j);
+            if (wd[cc]) od[cc] = __ldcg(O + j * ldo + i);
+            if (wm[cc]) om[cc] = __ldcg(O + (long long)i * ldo + j);
           }
 #pragma unroll
           for (int cc = 0; cc < EPI_COLS; ++cc) {
             const long long j = tl.J * TN + c0 + cc;
-            if (wd[cc]) O[j * jb.ldo + i] = od[cc] + v[cc];
-            if (wm[cc]) O[(long long)i * jb.ldo + j] = om[cc] + mv[cc];
+            if (wd[cc]) O[j * ldo + i] = od[cc] + v[cc];
+            if (wm[cc]) O[(long long)i * ldo + j] = om[cc] + mv[cc];
           }
         } else {
           // overwrite: no FP64 add (the FP64 pipe is the slow one on this part)
 #pragma unroll
           for (int cc = 0; cc < EPI_COLS; ++cc) {
             const long long j = tl.J * TN + c0 + cc;
-            if (wd[cc]) O[j * jb.ldo + i] = v[cc];
-            if (wm[cc]) O[(long long)i * jb.ldo + j] = mv[cc];
+            if (wd[cc]) O[j * ldo + i] = v[cc];
+            if (wm[cc]) O[(long long)i * ldo + j] = mv[cc];
           }
         }
       }
@@ -862,13 +877,15 @@ static PFN_encodeTiled get_encode()
   return fn;
 }
 
-static void encode_map(CUtensorMap* m, void* base, long long rows, int K_stride, int box_rows)
+// a slice array as (K element, plane row, digit plane); a box is KB elements
+// x box_rows rows x all S planes
+static void encode_map(CUtensorMap* m, void* base, long long plane_rows, int S, int K_stride, int box_rows)
 {
-  cuuint64_t dims[2] = {(cuuint64_t)K_stride, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)K_stride * 2};
-  cuuint32_t box[2] = {(cuuint32_t)KB, (cuuint32_t)box_rows};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = get_encode()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+  cuuint64_t dims[3] = {(cuuint64_t)K_stride, (cuuint64_t)plane_rows, (cuuint64_t)S};
+  cuuint64_t strides[2] = {(cuuint64_t)K_stride * 2, (cuuint64_t)K_stride * 2 * (cuuint64_t)plane_rows};
+  cuuint32_t box[3] = {(cuuint32_t)KB, (cuuint32_t)box_rows, (cuuint32_t)S};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = get_encode()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed");
@@ -952,7 +969,7 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
     }
     p->S = opts.digits;
   }
-  long long row = 0, erow = 0;
+  long long erow = 0;
   int kstride = KB;
   std::vector<SplitTile> tiles;
   std::vector<int> order(jobs_in.size());
@@ -983,9 +1000,7 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
     sj.nkt = sj.nosym ? sj.nkb : 2 * sj.nkb;
     if (sj.nosym && (sj.sign != 0 || sj.phase_off >= 0))
       throw std::invalid_argument("a plain split job takes no sign or phases (fold a sign into bscale)");
-    sj.row_base = row;
     sj.exp_base = erow;
-    row += (long long)p->S * sj.m_pad;
     erow += sj.m_pad;
     kstride = std::max(kstride, sj.K_pad);
     p->jobs.push_back(sj);
@@ -1005,9 +1020,10 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
         for (int J = per * I; J < nJ; ++J) tiles.push_back({jix, I, J, J < per * (I + 1) ? 1 : 0});
     }
   }
-  if (row > (1ll << 31) - TILE_M) throw std::runtime_error("split slice arrays exceed 2^31 rows");
+  if (erow > (1ll << 31) - TILE_M) throw std::runtime_error("split digit planes exceed 2^31 rows");
+  // every nonempty job pads to TILE_M rows, so a plane has at least TILE_M
+  erow = std::max(erow, (long long)TILE_M);
   p->K_stride = kstride;
-  p->total_rows = row;
   p->total_exp_rows = erow;
   p->njobs = (int)p->jobs.size();
   p->ntiles = (int)tiles.size();
@@ -1066,7 +1082,7 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
     cudaMemcpy(p->d_jobs, p->jobs.data(), sizeof(SplitJob) * p->njobs, cudaMemcpyHostToDevice);
     cudaMemcpy(p->d_tiles, tiles.data(), sizeof(SplitTile) * p->ntiles, cudaMemcpyHostToDevice);
     cudaMemcpy(p->d_cta, cta_first.data(), sizeof(int) * cta_first.size(), cudaMemcpyHostToDevice);
-    size_t abytes = (size_t)std::max(row, (long long)TILE_M) * kstride * 2;
+    size_t abytes = (size_t)p->S * erow * kstride * 2;
     // gamma / delta (the second half of a doubled K) only for symmetrised jobs
     bool any_sym = false, any_plain = false;
     for (const SplitJob& sj : p->jobs) {
@@ -1120,10 +1136,11 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
     p->d_dblk = (int4*)dm(sizeof(int4) * std::max<size_t>(1, db.size()));
     cudaMemcpy(p->d_rblk, rb.data(), sizeof(int4) * rb.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(p->d_dblk, db.data(), sizeof(int4) * db.size(), cudaMemcpyHostToDevice);
-    long long rows_map = std::max(row, (long long)TILE_M);
-    // every operand tile is loaded in 64-row boxes (an A tile is two of them),
-    // so one map per array serves both operand roles
-    for (int a = 0; a < 4; ++a) encode_map(&p->maps[a], p->arr[a], rows_map, kstride, p->tn);
+    // A-operand role of alpha, beta, gamma (TILE_M-row boxes); B-operand
+    // role of alpha, beta, delta (tn-row boxes)
+    for (int a = 0; a < 3; ++a) encode_map(&p->maps[a], p->arr[a], erow, p->S, kstride, TILE_M);
+    const int brole[3] = {0, 1, 3};
+    for (int a = 0; a < 3; ++a) encode_map(&p->maps[3 + a], p->arr[brole[a]], erow, p->S, kstride, p->tn);
   } catch (...) {
     split_plan_destroy(p);
     throw;
@@ -1187,8 +1204,8 @@ static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, con
       auto kd = p->plain ? k_split_digits<S, true> : k_split_digits<S, false>;
       kd<<<p->n_dblk, 256, 0, st>>>(p->d_jobs, p->d_dblk, A, B0, B1, kidx, kw, phase, gbscale, gsign,
                                                     p->d_rexpA, p->d_rexpB, p->d_jobmax, flags_for(p, gsign),
-                                                    p->beta, p->K_stride, p->arr[0], p->arr[1], p->arr[2],
-                                                    p->arr[3]);
+                                                    p->beta, p->K_stride, p->total_exp_rows, p->arr[0],
+                                                    p->arr[1], p->arr[2], p->arr[3]);
       count_launch();
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
@@ -1217,12 +1234,14 @@ static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, con
       auto kern = k_split_gemm<S, 64, 1, 8>;
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
       if (e != cudaSuccess) return e;
-      kern<<<p->grid, 64 + 32 * 8, p->smem, st>>>(p->maps[0], p->maps[1], p->maps[2], p->maps[3], ga);
+      kern<<<p->grid, 64 + 32 * 8, p->smem, st>>>(p->maps[0], p->maps[1], p->maps[2], p->maps[3], p->maps[4],
+                                                   p->maps[5], ga);
     } else {
       auto kern = k_split_gemm<S, 32, 2, 8>;
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
       if (e != cudaSuccess) return e;
-      kern<<<p->grid, 64 + 32 * 8, p->smem, st>>>(p->maps[0], p->maps[1], p->maps[2], p->maps[3], ga);
+      kern<<<p->grid, 64 + 32 * 8, p->smem, st>>>(p->maps[0], p->maps[1], p->maps[2], p->maps[3], p->maps[4],
+                                                   p->maps[5], ga);
     }
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
