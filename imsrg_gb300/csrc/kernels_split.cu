@@ -23,7 +23,8 @@
 //    that the FP32 sums of the leading groups stay exact integers.
 //  * Recombination.  The epilogue reads the S group sums (tcgen05.ld), merges
 //    them exactly as int64, converts once to FP64 and applies the power-of-two
-//    scale by exponent arithmetic.
+//    scale by exponent arithmetic.  Tensor memory is a ring of accumulator
+//    blocks, so the next tile's products run while the epilogue drains a tile.
 //  * Plain jobs (nosym): Out (+)= A B^T with A m x K, B n x K, each row of A
 //    and of B with its own exponent, K not doubled, every tile of the m x n
 //    output (the rectangular products of the scalar-tensor commutator).
@@ -109,7 +110,7 @@ struct SplitPlan {
   int nstages = 0;
   int accum_override = -1;
   int mirror = 1;  // 0: symmetrised jobs write only their upper triangle
-  int tn = 64, nacc = 1, epiw = 4;  // tile columns, accumulator sets, epilogue warps
+  int tn = 64, nacc = 1, epiw = 4;  // tile columns, tuning label of the tile (64 x 1 or 32 x 2), epilogue warps
   int stages_opt = 0, sched = 0;    // requested pipeline stages (0: most that fit), tile schedule
   int* d_cta = nullptr;             // [grid + 1]: each CTA's tiles are tiles[d_cta[b] .. d_cta[b + 1])
   bool shared_gd = false;           // gamma / delta alias beta / alpha (plain jobs only)
@@ -551,14 +552,34 @@ struct GemmArgs {
   int nomirror;  // 1: symmetrised jobs skip the mirror (lower-triangle) stores
 };
 
-// TN: tile columns (UMMA N); NACC: TMEM accumulator sets (2 lets the
-// epilogue of one tile overlap the MMAs of the next); EPIW: epilogue warps
-// (4 or 8; with 8, two warps share a TMEM lane quarter and split the columns).
+// Accumulators in tensor memory: NB = 512 / TN blocks of TN columns, one
+// block per weight group (S groups a tile).  Even tiles (counted per CTA)
+// keep group g in block g, odd tiles in block NB - S + g, so consecutive
+// tiles share OV = 2S - NB blocks (none when 2S <= NB): the last OV groups of
+// an even tile, the first OV groups of an odd one.  The epilogue folds those
+// groups into a per-column int64 partial sum first and releases them, and the
+// next tile's MMAs run under the rest of the epilogue.
+template <int S, int TN>
+struct AccPair {
+  static constexpr int NB = 512 / TN;
+  static constexpr int OV = 2 * S - NB > 0 ? 2 * S - NB : 0;
+  static_assert(S <= NB, "a tile's groups exceed tensor memory");
+  __device__ static unsigned base(int tc) { return (unsigned)((tc & 1) ? TN * (NB - S) : 0); }
+  // first group the next tile overwrites (the early ones: [early_lo, early_lo + OV))
+  __device__ static int early_lo(int tc) { return (tc & 1) ? 0 : S - OV; }
+};
+
+// TN: tile columns (UMMA N); EPIW: epilogue warps (4 or 8; with 8, two warps
+// share a TMEM lane quarter and split the columns).
 // The maps: the A-operand role (TILE_M-row boxes) of alpha, beta, gamma and
 // the B-operand role (TN-row boxes) of alpha, beta, delta; each box holds all
 // S digit planes, so one stage is two TMA loads.
-template <int S, int TN, int NACC, int EPIW>
-__global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_constant__ CUtensorMap mAlphaA,
+// Registers are capped at 128 a thread (41k for the CTA), so the kernels of
+// a second stream still fit beside the product on every SM; uncapped, the
+// epilogue's per-column partial sums take it to 168 and the commutator's two
+// streams stop overlapping.
+template <int S, int TN, int EPIW>
+__global__ void __maxnreg__(128) k_split_gemm(const __grid_constant__ CUtensorMap mAlphaA,
                                                                  const __grid_constant__ CUtensorMap mBetaA,
                                                                  const __grid_constant__ CUtensorMap mGammaA,
                                                                  const __grid_constant__ CUtensorMap mAlphaB,
@@ -566,7 +587,8 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
                                                                  const __grid_constant__ CUtensorMap mDeltaB,
                                                                  GemmArgs g)
 {
-  static_assert(NACC * S * TN <= 512, "TMEM accumulators exceed 512 columns");
+  using Acc = AccPair<S, TN>;
+  constexpr int OV = Acc::OV;
   static_assert(TILE_M % TN == 0 && TN % 16 == 0, "tile shape");
   constexpr int EPI_T = 32 * EPIW;          // epilogue threads
   constexpr int COLS_W = TN / (EPIW / 4);   // columns per epilogue warp
@@ -578,8 +600,8 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
   const unsigned B_SLICE = TN * KB * 2;
   const unsigned STAGE = S * (A_SLICE + B_SLICE);
   unsigned long long* bars = (unsigned long long*)(smem + NST * STAGE);
-  // bars: full[NST], empty[NST], acc_full[NACC], acc_empty[NACC]; then tmem slot
-  unsigned* tmem_slot = (unsigned*)(bars + 2 * NST + 2 * NACC);
+  // bars: full[NST], empty[NST], acc_full[2], done[2], early[1]; then the tmem slot
+  unsigned* tmem_slot = (unsigned*)(bars + 2 * NST + 5);
   __shared__ int s_err_;
   __shared__ int s_colexp[2][TN];  // indexed by tile parity: warps run at most one tile apart
   __shared__ int s_colph[2][TN];
@@ -593,7 +615,8 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
   auto full_bar = [&](int s) { return bar0 + 8u * s; };
   auto empty_bar = [&](int s) { return bar0 + 8u * (NST + s); };
   auto acc_full = [&](int b) { return bar0 + 8u * (2 * NST + b); };
-  auto acc_empty = [&](int b) { return bar0 + 8u * (2 * NST + NACC + b); };
+  auto acc_done = [&](int b) { return bar0 + 8u * (2 * NST + 2 + b); };  // epilogue finished the tile
+  const unsigned acc_early = bar0 + 8u * (2 * NST + 4);                  // shared blocks read
 
   if (threadIdx.x == 0) {
     s_err = 0;
@@ -602,10 +625,11 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
       mbar_init(full_bar(s), 1);
       mbar_init(empty_bar(s), 1);
     }
-    for (int b = 0; b < NACC; ++b) {
-      mbar_init(acc_full(b), 1);
-      mbar_init(acc_empty(b), EPI_T);
-    }
+    mbar_init(acc_full(0), 1);
+    mbar_init(acc_full(1), 1);
+    mbar_init(acc_done(0), EPI_T);
+    mbar_init(acc_done(1), EPI_T);
+    mbar_init(acc_early, EPI_T);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -666,14 +690,19 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
       const int tend = g.cta_first[blockIdx.x + 1];
       for (int tix = g.cta_first[blockIdx.x]; tix < tend && !s_err; ++tix, ++tc) {
         const int nkt = g.jobs[g.tiles[tix].job].nkt;
-        const int b = tc % NACC;
-        if (!mbar_wait(acc_empty(b), (unsigned)(((tc / NACC) & 1) ^ 1))) {
+        // the blocks of this tile are free: the tile before last is done, and
+        // the shared blocks of the previous tile have been read (the
+        // epilogue works through the tiles in order, so the second implies
+        // the first)
+        const bool waited = OV > 0 ? mbar_wait(acc_early, (unsigned)((tc & 1) ^ 1))
+                                   : mbar_wait(acc_done(tc & 1), (unsigned)(((tc >> 1) & 1) ^ 1));
+        if (!waited) {
           set_status(g.status, 102);
           s_err = 1;
           break;
         }
         tc_fence_after();
-        const unsigned dbase = tmem + (unsigned)(b * S * TN);
+        const unsigned dbase = tmem + Acc::base(tc);
         bool ok = true;
         for (int kb = 0; kb < nkt; ++kb, ++it) {
           int st = it % NST;
@@ -714,7 +743,7 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
           tc_commit(empty_bar(st));
         }
         if (!ok) break;
-        tc_commit(acc_full(b));
+        tc_commit(acc_full(tc & 1));
       }
     }
   } else {
@@ -732,10 +761,9 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
       const int jm = jp->m, jn = jp->n, ldo = jp->ldo, nosym = jp->nosym, phase_off = jp->phase_off;
       const int jsign = jp->sign, jacc = jp->accumulate;
       const long long exp_base = jp->exp_base, out_off = jp->out_off;
-      const int b = tc % NACC;
       // the epilogue warps decide together (named barrier 1), so a timeout
       // never leaves one of them waiting at a barrier alone
-      if (!mbar_wait(acc_full(b), (unsigned)((tc / NACC) & 1))) {
+      if (!mbar_wait(acc_full(tc & 1), (unsigned)((tc >> 1) & 1))) {
         set_status(g.status, 104);
         s_epi_err = 1;
       }
@@ -767,11 +795,42 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
       double* O = g.out + out_off;
       const int Xi = ai + c - g.beta * (S + 1);
       const bool accumulate = g.accum > 0 || (g.accum < 0 && jacc);
-      const unsigned tbase = tmem + ((unsigned)(q * 32) << 16) + (unsigned)(b * S * TN);
-      for (int c0 = cbeg; c0 < cbeg + COLS_W; c0 += EPI_COLS) {
-        unsigned r[MAX_S][EPI_COLS];
+      const unsigned lane_base = tmem + ((unsigned)(q * 32) << 16) + Acc::base(tc);
+      // exact merge of the weight groups: Horner in base 2^beta, per column,
+      // in two parts.  The groups the next tile overwrites (e0 .. e0+OV-1)
+      // are read first for all this warp's columns into P, then released;
+      // per chunk of columns the other groups (l0 .. l0+S-OV-1) give the rest:
+      //   odd tile  (e0 = 0, the leading groups):  I = P 2^(beta (S-OV)) + L
+      //   even tile (e0 = S-OV, the trailing ones): I = L 2^(beta OV) + P
+      const int e0 = Acc::early_lo(tc);
+      const int l0 = (tc & 1) ? OV : 0;
+      const long long mulP = (tc & 1) ? (1ll << (g.beta * (S - OV))) : 1ll;
+      const long long mulL = (tc & 1) ? 1ll : (1ll << (g.beta * OV));
+      long long P[COLS_W];
 #pragma unroll
-        for (int gidx = 0; gidx < S; ++gidx) tmem_ld8(tbase + (unsigned)(gidx * TN + c0), r[gidx]);
+      for (int cc = 0; cc < COLS_W; ++cc) P[cc] = 0;
+      if (OV > 0) {
+#pragma unroll
+        for (int c0 = 0; c0 < COLS_W; c0 += EPI_COLS) {
+          unsigned r[OV > 0 ? OV : 1][EPI_COLS];
+#pragma unroll
+          for (int gi = 0; gi < OV; ++gi)
+            tmem_ld8(lane_base + (unsigned)((e0 + gi) * TN + cbeg + c0), r[gi]);
+          tmem_wait_ld();
+#pragma unroll
+          for (int gi = 0; gi < OV; ++gi)
+#pragma unroll
+            for (int cc = 0; cc < EPI_COLS; ++cc)
+              P[c0 + cc] = P[c0 + cc] * (1ll << g.beta) + __float2int_rn(__uint_as_float(r[gi][cc]));
+        }
+        tc_fence_before();
+        mbar_arrive(acc_early);
+      }
+#pragma unroll
+      for (int c0 = 0; c0 < COLS_W; c0 += EPI_COLS) {
+        unsigned r[S - OV][EPI_COLS];
+#pragma unroll
+        for (int gi = 0; gi < S - OV; ++gi) tmem_ld8(lane_base + (unsigned)((l0 + gi) * TN + cbeg + c0), r[gi]);
         tmem_wait_ld();
         // values of this chunk, then all old values (accumulate), then the
         // stores: the loads of one chunk are in flight together
@@ -779,17 +838,17 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
         bool wd[EPI_COLS], wm[EPI_COLS];
 #pragma unroll
         for (int cc = 0; cc < EPI_COLS; ++cc) {
-          const int j = tl.J * TN + c0 + cc;
+          const int jc = cbeg + c0 + cc;  // column within the tile
+          const int j = tl.J * TN + jc;
           wd[cc] = rowok && j < jn && !(tl.diag && i > j);
           wm[cc] = wd[cc] && i != j && !nosym && !g.nomirror;
-          // exact merge of the weight groups: Horner in base 2^beta
-          long long I64 = __float2int_rn(__uint_as_float(r[0][cc]));
+          long long L = 0;
 #pragma unroll
-          for (int gidx = 1; gidx < S; ++gidx)
-            I64 = I64 * (1ll << g.beta) + __float2int_rn(__uint_as_float(r[gidx][cc]));
-          v[cc] = i64_ldexp(I64, Xi + s_colexp[tc & 1][c0 + cc]);
+          for (int gi = 0; gi < S - OV; ++gi) L = L * (1ll << g.beta) + __float2int_rn(__uint_as_float(r[gi][cc]));
+          const long long I64 = P[c0 + cc] * mulP + L * mulL;
+          v[cc] = i64_ldexp(I64, Xi + s_colexp[tc & 1][jc]);
           mv[cc] = __longlong_as_double(__double_as_longlong(v[cc]) ^
-                                        ((sign * phi_i * s_colph[tc & 1][c0 + cc]) < 0 ? (long long)0x8000000000000000ull
+                                        ((sign * phi_i * s_colph[tc & 1][jc]) < 0 ? (long long)0x8000000000000000ull
                                                                                    : 0ll));
           od[cc] = 0.0;
           om[cc] = 0.0;
@@ -797,13 +856,13 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
         if (accumulate) {
 #pragma unroll
           for (int cc = 0; cc < EPI_COLS; ++cc) {
-            const long long j = tl.J * TN + c0 + cc;
+            const long long j = tl.J * TN + cbeg + c0 + cc;
             if (wd[cc]) od[cc] = __ldcg(O + j * ldo + i);
             if (wm[cc]) om[cc] = __ldcg(O + (long long)i * ldo + j);
           }
 #pragma unroll
           for (int cc = 0; cc < EPI_COLS; ++cc) {
-            const long long j = tl.J * TN + c0 + cc;
+            const long long j = tl.J * TN + cbeg + c0 + cc;
             if (wd[cc]) O[j * ldo + i] = od[cc] + v[cc];
             if (wm[cc]) O[(long long)i * ldo + j] = om[cc] + mv[cc];
           }
@@ -811,14 +870,15 @@ __global__ void __launch_bounds__(64 + 32 * EPIW, 1) k_split_gemm(const __grid_c
           // overwrite: no FP64 add (the FP64 pipe is the slow one on this part)
 #pragma unroll
           for (int cc = 0; cc < EPI_COLS; ++cc) {
-            const long long j = tl.J * TN + c0 + cc;
+            const long long j = tl.J * TN + cbeg + c0 + cc;
             if (wd[cc]) O[j * ldo + i] = v[cc];
             if (wm[cc]) O[(long long)i * ldo + j] = mv[cc];
           }
         }
       }
+      // every TMEM load of this tile has completed (tcgen05.wait::ld)
       tc_fence_before();
-      mbar_arrive(acc_empty(b));
+      mbar_arrive(acc_done(tc & 1));
     }
   }
   // every role has left its loop: all MMAs this CTA issued have been drained
@@ -931,9 +991,10 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
   SplitPlan* p = new SplitPlan();
   p->family = family;
   // defaults: the ladder products have long K (MMA-bound tiles): 64-column
-  // tiles, one accumulator set; the Pandya-space products have short K
-  // (epilogue-bound tiles): 32-column tiles and two accumulator sets; eight
-  // epilogue warps
+  // tiles; the Pandya-space products have short K (epilogue-bound tiles):
+  // 32-column tiles; eight epilogue warps.  (The second number of a tile
+  // shape, 1 or 2, is its name in the tuning tables: the accumulator ring
+  // sizes itself from the tile width.)
   p->tn = family == 0 ? 64 : 32;
   p->nacc = family == 0 ? 1 : 2;
   if (opts.tn == 64 && (opts.nacc == 0 || opts.nacc == 1)) {
@@ -1155,7 +1216,7 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
     split_plan_destroy(p);
     throw std::runtime_error("not enough shared memory for the split GEMM pipeline (or fewer than 2 stages asked)");
   }
-  p->smem = 1024 + p->nstages * stage + (2 * p->nstages + 2 * p->nacc) * 8 + 16;
+  p->smem = 1024 + p->nstages * stage + (2 * p->nstages + 5) * 8 + 16;
   return p;
 }
 
@@ -1231,13 +1292,13 @@ static cudaError_t launch_s(SplitPlan* p, const double* A, const double* B0, con
     ga.accum = p->accum_override;
     ga.nomirror = p->mirror ? 0 : 1;
     if (p->tn == 64) {
-      auto kern = k_split_gemm<S, 64, 1, 8>;
+      auto kern = k_split_gemm<S, 64, 8>;
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
       if (e != cudaSuccess) return e;
       kern<<<p->grid, 64 + 32 * 8, p->smem, st>>>(p->maps[0], p->maps[1], p->maps[2], p->maps[3], p->maps[4],
                                                    p->maps[5], ga);
     } else {
-      auto kern = k_split_gemm<S, 32, 2, 8>;
+      auto kern = k_split_gemm<S, 32, 8>;
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
       if (e != cudaSuccess) return e;
       kern<<<p->grid, 64 + 32 * 8, p->smem, st>>>(p->maps[0], p->maps[1], p->maps[2], p->maps[3], p->maps[4],
