@@ -200,6 +200,7 @@ __device__ __forceinline__ unsigned long long sdesc_sw64(unsigned addr)
 }
 
 // instruction descriptor, kind::f16: BF16 x BF16 -> F32, both K-major
+// (bit 13, set by the caller where needed, negates the A operand)
 __host__ __device__ constexpr unsigned idesc_bf16(int M, int N)
 {
   return (1u << 4)                   // D format F32
@@ -505,7 +506,7 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
     }
   }
   __syncthreads();
-  const bool need_g = flags[2 * job] != 0, need_d = flags[2 * job + 1] != 0;
+  const bool need_g = flags[2 * job] == 1, need_d = flags[2 * job + 1] != 0;
   // stores: each thread one 16-byte vector (8 digits) of one row of one slice
   for (int e = threadIdx.x; e < S * 32 * (KB / 8); e += 256) {
     const int v = e % (KB / 8), r = (e / (KB / 8)) & 31, s = e / (32 * (KB / 8));
@@ -543,7 +544,7 @@ struct GemmArgs {
   const int* rexpA;
   const int* rexpB;
   const int* jobmax;
-  const int* flags;   // [2*job]: gamma used, delta used
+  const int* flags;   // [2*job]: second-half A operand (0 beta, 1 gamma, 2 beta negated by the MMA); [2*job+1]: delta used
   const int* phase;
   double* out;
   int* status;
@@ -655,7 +656,7 @@ __global__ void __maxnreg__(128) k_split_gemm(const __grid_constant__ CUtensorMa
         const SplitJob* jp = g.jobs + tl.job;
         const long long exp_base = jp->exp_base;
         const int nkt = jp->nkt, nkb = jp->nkb;
-        const bool useG = g.flags[2 * tl.job] != 0, useD = g.flags[2 * tl.job + 1] != 0;
+        const bool useG = g.flags[2 * tl.job] == 1, useD = g.flags[2 * tl.job + 1] != 0;
         const CUtensorMap* mA2 = useG ? &mGammaA : &mBetaA;
         const CUtensorMap* mB2 = useD ? &mDeltaB : &mAlphaB;
         const int rowA = (int)(exp_base + tl.I * TILE_M);
@@ -689,7 +690,9 @@ __global__ void __maxnreg__(128) k_split_gemm(const __grid_constant__ CUtensorMa
       int it = 0, tc = 0;
       const int tend = g.cta_first[blockIdx.x + 1];
       for (int tix = g.cta_first[blockIdx.x]; tix < tend && !s_err; ++tix, ++tc) {
-        const int nkt = g.jobs[g.tiles[tix].job].nkt;
+        const int job = g.tiles[tix].job;
+        const int nkt = g.jobs[job].nkt, nkb = g.jobs[job].nkb;
+        const unsigned neg2 = g.flags[2 * job] == 2 ? (1u << 13) : 0u;  // negate A in the second K half
         // the blocks of this tile are free: the tile before last is done, and
         // the shared blocks of the previous tile have been read (the
         // epilogue works through the tiles in order, so the second implies
@@ -722,6 +725,7 @@ __global__ void __maxnreg__(128) k_split_gemm(const __grid_constant__ CUtensorMa
           const unsigned sA = sbase + st * STAGE;
           const unsigned long long a0 = sdesc_sw64(sA), b0 = sdesc_sw64(sA + S * A_SLICE);
           const unsigned first = kb == 0 ? 0u : 1u;
+          const unsigned neg = kb >= nkb ? neg2 : 0u;
           // The products (s, t) of one A digit s go to the weight groups s + t,
           // which are consecutive TN-column blocks of tensor memory, and the B
           // digit tiles t are consecutive TN-row blocks of shared memory with
@@ -736,7 +740,7 @@ __global__ void __maxnreg__(128) k_split_gemm(const __grid_constant__ CUtensorMa
               for (int t0 = 0; t0 < S - s; t0 += MAXT) {
                 const int nt = (S - s - t0) < MAXT ? (S - s - t0) : MAXT;
                 const unsigned long long bd = b0 + (unsigned long long)((t0 * B_SLICE + sub * 32) >> 4);
-                tc_mma(dbase + (s + t0) * TN, ad, bd, idesc_bf16(TILE_M, nt * TN), (sub == 0 && s == 0) ? first : 1u);
+                tc_mma(dbase + (s + t0) * TN, ad, bd, idesc_bf16(TILE_M, nt * TN) | neg, (sub == 0 && s == 0) ? first : 1u);
               }
             }
           }
@@ -1170,8 +1174,10 @@ SplitPlan* split_plan_create(const Space& s, const std::vector<GemmJobDev>& jobs
       for (int j = 0; j < p->njobs; ++j) {
         const SplitJob& sj = p->jobs[j];
         int sign = sj.sign != 0 ? sj.sign : (gs == 0 ? 1 : -1);
-        // plain jobs have no second K half: gamma / delta stay unwritten
-        flags[2 * p->njobs * gs + 2 * j] = !sj.nosym && (sign != 1 || sj.phase_off >= 0) ? 1 : 0;
+        // plain jobs have no second K half: gamma / delta stay unwritten.
+        // Without row phases gamma is beta or -beta: the MMA reads beta and,
+        // for -beta, negates its A operand (instruction descriptor bit 13)
+        flags[2 * p->njobs * gs + 2 * j] = sj.nosym ? 0 : sj.phase_off >= 0 ? 1 : sign != 1 ? 2 : 0;
         flags[2 * p->njobs * gs + 2 * j + 1] = !sj.nosym && sj.phase_off >= 0 ? 1 : 0;
       }
     cudaMemcpy(p->d_flags, flags.data(), sizeof(int) * flags.size(), cudaMemcpyHostToDevice);
