@@ -319,26 +319,44 @@ __global__ void k_sym_subtract_ff(DevSpace S, const float2* __restrict__ W2, dou
     if (r < n && c < n) v = W2[off + (long long)c * n + r];
     tt[yy][tx] = v;
   }
-  __syncthreads();
-  for (int yy = ty; yy < 32; yy += 8) {
-    int r = ti * 32 + tx, c = tj * 32 + yy;
+  // the direct W2 values and the old Z values of this thread's four
+  // elements are all requested before the first store (loads in flight
+  // together; the kernel is bound by their latency)
+  float2 w[4];
+  double zo4[4];
+  const int r = ti * 32 + tx;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int c = tj * 32 + ty + 8 * k;
+    w[k] = make_float2(0.f, 0.f);
+    zo4[k] = 0.0;
     if (r < n && c < n) {
-      const float2 w = W2[off + (long long)c * n + r];
+      w[k] = W2[off + (long long)c * n + r];
+      zo4[k] = Z[off + (long long)c * n + r];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int yy = ty + 8 * k, c = tj * 32 + yy;
+    if (r < n && c < n) {
       float2 u = tt[tx][yy];
       if (hZ < 0) {
         u.x = -u.x;
         u.y = -u.y;
       }
       float hi, lo;
-      df_add(w.x, w.y, u.x, u.y, hi, lo);
-      Z[off + (long long)c * n + r] -= ff2d(hi, lo);
+      df_add(w[k].x, w[k].y, u.x, u.y, hi, lo);
+      Z[off + (long long)c * n + r] = zo4[k] - ff2d(hi, lo);
     }
   }
 }
 
 // Same one-body part when Mpp - Mhh is already in Mz (the ladder product added
-// to a zeroed Z): one warp per (i <= j) pair, lanes over c; each lane forms the
-// short Mhh dot products (hh kets only) itself, so the warp reduces once.
+// to a zeroed Z): one block of 128 threads per (i <= j) pair, threads over c;
+// each thread forms the short Mhh dot products (hh kets only) itself, and the
+// block reduces once.  (A warp per pair left 5% of the warps of the GPU
+// active: there are only a few hundred pairs.)
 __global__ void k_comm221_1b_mz(DevSpace S, DevWork W, const double* __restrict__ X, const double* __restrict__ Y,
                                 double* __restrict__ Z, int hX, int hZ, const double* __restrict__ Mz,
                                 const long long* __restrict__ zo)
@@ -347,14 +365,15 @@ __global__ void k_comm221_1b_mz(DevSpace S, DevWork W, const double* __restrict_
   Y = zsh(Y, zo, ZR_Y);
   Z = zsh(Z, zo, ZR_Z);
   Mz = zsh(Mz, zo, ZR_Z);
-  int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  int lane = threadIdx.x & 31;
+  __shared__ double red[4];
+  const int item = blockIdx.x;
+  const int lane = threadIdx.x & 31;
   if (item >= W.npairs1b) return;
   const int i = W.pairs1b[2 * item], j = W.pairs1b[2 * item + 1];
   const int N = S.norb;
   const int ji = S.j2[i], jj = S.j2[j];
   double z = 0.0;
-  for (int c = lane; c < N; c += 32) {
+  for (int c = threadIdx.x; c < N; c += blockDim.x) {
     const double nc = S.occ[c], nbarc = 1.0 - nc;
     const bool need_pp = fabs(nc) > 1e-9, need_hh = fabs(nbarc) > 1e-9;
     const int jc = S.j2[c];
@@ -396,7 +415,10 @@ __global__ void k_comm221_1b_mz(DevSpace S, DevWork W, const double* __restrict_
     }
   }
   z = warp_sum(z);
-  if (lane == 0) {
+  if (lane == 0) red[threadIdx.x >> 5] = z;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    z = red[0] + red[1] + red[2] + red[3];
     double v = z / (ji + 1.0);
     Z[32 + (size_t)j * N + i] += v;
     if (i != j) Z[32 + (size_t)i * N + j] += hZ * v;
@@ -1276,7 +1298,7 @@ cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, 
   int wpb = 8;
   if (Mz) {
     // no other kernel writes Z1 concurrently: plain stores per (i, j) pair
-    k_comm221_1b_mz<<<dim3((s.work.npairs1b + 3) / 4, 1, nz), 128, 0, st>>>(s.dev, s.work, X, Y, Z, hX, hZ, Mz, zo);
+    k_comm221_1b_mz<<<dim3(s.work.npairs1b, 1, nz), 128, 0, st>>>(s.dev, s.work, X, Y, Z, hX, hZ, Mz, zo);
     count_launch();
     return cudaGetLastError();
   }
