@@ -147,7 +147,7 @@ void setup_device_lists(imsrg_space* sp)
   sp->n_zbar_pairs = (int)zp.size() / 3;
   sp->d_zbar_pairs = sp->track(dcopy(zp));
   // comm122 symmetrisation tiles (all 32x32 tiles of every block)
-  std::vector<int> t122, tinv, tfwd;
+  std::vector<int> t122, tinv;
   for (int c = 0; c < s.nch; ++c) {
     int n = s.ch[c].n();
     int nt = (n + 31) / 32;
@@ -197,16 +197,7 @@ void setup_device_lists(imsrg_space* sp)
     int ncc = s.cc[c].n();
     int K = 2 * s.cc_nph[c];
     if (ncc == 0) continue;
-    if (K == 0) {
-      sp->zbar_zero.push_back({s.zb_off[c], (int64_t)ncc * 2 * ncc});
-      continue;
-    }
-    for (int r0 = 0; r0 < ncc; r0 += 64)
-      for (int t0 = 0; t0 < K; t0 += 4) {
-        tfwd.push_back(c);
-        tfwd.push_back(r0);
-        tfwd.push_back(t0);
-      }
+    if (K == 0) sp->zbar_zero.push_back({s.zb_off[c], (int64_t)ncc * 2 * ncc});
   }
   sp->n_sym122 = (int)t122.size() / 3;
   sp->d_sym122 = sp->track(dcopy(t122));
@@ -233,8 +224,6 @@ void setup_device_lists(imsrg_space* sp)
   sp->d_cls_list = sp->track(dcopy(s.cls_list));
   sp->d_cls_off = sp->track(dcopy(s.cls_off));
   sp->d_cls_sort = sp->track(dcopy(s.cls_sort));
-  sp->n_pfwd = (int)tfwd.size() / 3;
-  sp->d_pfwd = sp->track(dcopy(tfwd));
   // norm chunks: every 2b block in pieces of <= 65536 elements, weight (2J+1)^2
   std::vector<long long> no;
   std::vector<int> nl;
@@ -674,7 +663,7 @@ int prep_ph(const imsrg_op* X, const imsrg_op* Y, cudaStream_t st)
   int rc = ensure_scratch(sp, true, false);
   if (rc) return rc;
   ProfScope ps("Pandya transform of X, Y", st);
-  CUDA_TRY(launch_pandya_fwd(s, X->d, Y->d, Y->herm, sp->d_xb, sp->d_yt, sp->d_yf, sp->d_pfwd, sp->n_pfwd, st));
+  CUDA_TRY(launch_pandya_fwd(s, X->d, Y->d, Y->herm, sp->d_xb, sp->d_yt, sp->d_yf, st));
   for (auto& zr : sp->zbar_zero) CUDA_TRY(cudaMemsetAsync(sp->d_zb + zr.first, 0, zr.second * sizeof(double), st));
   return IMSRG_OK;
 }
@@ -1585,7 +1574,7 @@ int group_pre(GroupedProducts* g, cudaStream_t st)
     CUDA_TRY(launch_to_ff(s, X->d, sp->d_xf, st, zo, nz, ZR_X, ZR_XF));
     CUDA_TRY(launch_to_ff(s, Y->d, sp->d_yff, st, zo, nz, ZR_Y, ZR_YF));
   }
-  CUDA_TRY(launch_pandya_fwd(s, X->d, Y->d, Y->herm, sp->d_xb, sp->d_yt, sp->d_yf, sp->d_pfwd, sp->n_pfwd, st, zo, nz));
+  CUDA_TRY(launch_pandya_fwd(s, X->d, Y->d, Y->herm, sp->d_xb, sp->d_yt, sp->d_yf, st, zo, nz));
   CUDA_TRY(launch_comm111_110(s, X->d, Y->d, Z->d, true, X->herm != Y->herm, st, zo, nz));
   if (X->herm != Y->herm) CUDA_TRY(launch_comm220(s, X->d, Y->d, Z->d, X->herm, st, zo, nz));
   CUDA_TRY(launch_comm121(s, sp->d_holes, X->d, Y->d, Z->d, Z->herm, st, zo, nz));

@@ -81,8 +81,6 @@ struct imsrg_space {
   int n_sym122 = 0;
   int* d_sym122u = nullptr;  // tile pairs a <= b (fused split-form comm122ss)
   int n_sym122u = 0;
-  int* d_pfwd = nullptr;
-  int n_pfwd = 0;
   int* d_pinv = nullptr;
   int n_pinv = 0;
   int* d_invq = nullptr;  // quadruple blocks of the split-form inverse Pandya transform

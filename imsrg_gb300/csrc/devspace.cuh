@@ -44,6 +44,18 @@ struct DevSpace {
 };
 
 // Device copies of the per-kernel work lists (built once per space).
+// One output of the Pandya transform of X and Y (an (ik, t) element of the
+// Xbar / Ybar panels of a cross-coupled channel), from per-space descriptors:
+// its terms pf_e[beg .. beg+nterm) (arena indices) and pf_w (the signed
+// (2J+1) 6j weights), its panel position and factors.
+struct PfOut {
+  int dest;        // Xbar / YbarT element (into the panel arrays)
+  int dyf;         // YflipT element - dest
+  int beg;
+  unsigned code;   // nterm | (factors of sqrt 2 in normfactor) << 16 | (phi_bra phi_ik < 0) << 18
+  double xs;       // normfactor * (n_a - n_b)
+};
+
 struct DevWork {
   const double* ket_wpp;  // flat over 2b channel kets (ch_kofs order)
   const double* ket_nn;
@@ -66,6 +78,9 @@ struct DevWork {
   const long long* xb_off;
   const long long* zb_off;
   const int* cc_phase_off;
+  const PfOut* pf_out; int n_pfout;  // Pandya transform of X and Y, from descriptors
+  const int* pf_e;
+  const double* pf_w;
 };
 
 // global index of ket (p, q), p <= q: ModelSpace::Index2 (src/ModelSpace.cc:1108-1118)

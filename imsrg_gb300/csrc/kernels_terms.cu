@@ -492,78 +492,36 @@ __global__ void k_sym_subtract(DevSpace S, const double* __restrict__ W2, double
 //   Xb(ik, t)  = Xbar(ik, t) * normfactor * (n_a - n_b)
 //   Yt(ik, t)  = Ybar(t, ik) * normfactor
 //   Yf(ik, t') = Ybar(t, ik) * normfactor * phi_bra phi_ik hY, t' = t with halves swapped
-// One thread per (ik, t); blocks over a (channel, tile) list.
-__global__ void k_pandya_fwd(DevSpace S, DevWork W, const double* __restrict__ X, const double* __restrict__ Y,
-                             int hY, double* __restrict__ Xb, double* __restrict__ Yt, double* __restrict__ Yf,
-                             const int* __restrict__ tiles, int ntiles, const long long* __restrict__ zo)
+// One thread per (ik, t), from the space's descriptors (build_pandya_fwd,
+// space.cpp): the J sum is one gather of X and of Y and two FMAs per term.
+__global__ void __launch_bounds__(256) k_pandya_fwd(DevWork W, const double* __restrict__ X,
+                                                    const double* __restrict__ Y, int hY, double* __restrict__ Xb,
+                                                    double* __restrict__ Yt, double* __restrict__ Yf,
+                                                    const long long* __restrict__ zo)
 {
   X = zsh(X, zo, ZR_X);
   Y = zsh(Y, zo, ZR_Y);
   Xb = zsh(Xb, zo, ZR_XB);
   Yt = zsh(Yt, zo, ZR_YT);
   Yf = zsh(Yf, zo, ZR_YFL);
-  int tix = blockIdx.x;
-  if (tix >= ntiles) return;
-  int cc = tiles[3 * tix], row0 = tiles[3 * tix + 1], t0 = tiles[3 * tix + 2];
-  int ncc = S.cc_n[cc];
-  int nph = W.cc_nph[cc];
-  int ik = row0 + (threadIdx.x & 63);
-  int t = t0 + (threadIdx.x >> 6);
-  if (ik >= ncc || t >= 2 * nph) return;
-  int Jcc = cc / 6;
-  int ibra = t < nph ? t : t - nph;
-  int ab_case = t < nph ? 0 : 1;
-  int kb = W.cc_ph[W.cc_ph_off[cc] + ibra];
-  int bp = S.cc_p[S.cc_kofs[cc] + kb], bq = S.cc_q[S.cc_kofs[cc] + kb];
-  int a = ab_case ? bq : bp, b = ab_case ? bp : bq;
-  int c = S.cc_p[S.cc_kofs[cc] + ik], d = S.cc_q[S.cc_kofs[cc] + ik];
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= W.n_pfout) return;
+  const PfOut m = W.pf_out[o];
+  const int nterm = (int)(m.code & 0xFFFFu), nsq = (int)((m.code >> 16) & 3u);
+  // normfactor as the reference forms it: 1, sqrt 2 or sqrt 2 * sqrt 2
+  const double ys = nsq == 0 ? 1.0 : nsq == 1 ? kSqrt2 : kSqrt2 * kSqrt2;
+  const double yfs = (m.code >> 18) & 1u ? -1.0 : 1.0;
   double xbar = 0.0, ybar = 0.0;
-  double nf = 1.0;
-  if (S.tz2[a] + S.tz2[d] == S.tz2[b] + S.tz2[c]) {
-    if (a == d) nf *= kSqrt2;
-    if (c == b) nf *= kSqrt2;
-    int ja = S.j2[a], jb = S.j2[b], jc = S.j2[c], jd = S.j2[d];
-    int jmin = max(abs(ja - jd), abs(jc - jb)) / 2;
-    int jmax = min(ja + jd, jc + jb) / 2;
-    int dJ = 1;
-    if (a == d || c == b) {
-      dJ = 2;
-      jmin += jmin & 1;
-    }
-    // GetTBME_J_norm_twoOps(Y, J, J, c, b, a, d): same element of X and Y
-    int lc = S.l[c], lb = S.l[b], la = S.l[a], ld = S.l[d];
-    bool ok = (((lc + lb + la + ld) & 1) == 0) && (S.tz2[c] + S.tz2[b] == S.tz2[a] + S.tz2[d]);
-    if (ok) {
-      int k1 = ket_index(S.norb, min(c, b), max(c, b));
-      int k2 = ket_index(S.norb, min(a, d), max(a, d));
-      int par = (lc + lb) & 1, tz = (S.tz2[c] + S.tz2[b]) / 2;
-      // (2J+1) 6j from the weighted table (0 where the reference skips |6j| < 1e-8);
-      // the swap phases are sign flips: one FP64 FMA per operand and J
-      const int pcb = (c > b) ? ((S.j2[c] + S.j2[b]) / 2 + 1) : 0;
-      const int pad = (a > d) ? ((S.j2[a] + S.j2[d]) / 2 + 1) : 0;
-      for (int J = jmin; J <= jmax; J += dJ) {
-        double w = dev_sixj_w(S, ja, jb, Jcc, jc, jd, J);
-        if (dzero(w)) continue;
-        int bi = S.ketJ_loc[J * S.nkets + k1], ki = S.ketJ_loc[J * S.nkets + k2];
-        if (bi < 0 || ki < 0) continue;
-        int ch = chan_index(J, par, tz);
-        int n = S.ch_n[ch];
-        long long e = S.ch_off[ch] + (long long)ki * n + bi;
-        bool neg = ((c > b) && ((pcb + J) & 1)) != ((a > d) && ((pad + J) & 1));
-        double wx = dneg_if(w, !neg);  // accumulate -(2J+1) 6j ph
-        xbar = fma(wx, X[e], xbar);
-        ybar = fma(wx, Y[e], ybar);
-      }
-    }
+  for (int k = m.beg; k < m.beg + nterm; ++k) {
+    const int e = __ldg(W.pf_e + k);
+    const double w = __ldg(W.pf_w + k);
+    xbar = fma(w, X[e], xbar);
+    ybar = fma(w, Y[e], ybar);
   }
-  double na_nb = S.occ[a] - S.occ[b];
-  long long base = W.xb_off[cc];
-  Xb[base + (long long)t * ncc + ik] = xbar * (nf * na_nb);
-  double yv = dneg_if(ybar * nf, hY < 0);
-  Yt[base + (long long)t * ncc + ik] = yv;
-  const int* phi = W.phase_tab + W.cc_phase_off[cc];
-  int tf = t < nph ? t + nph : t - nph;
-  Yf[base + (long long)tf * ncc + ik] = yv * phi[kb] * phi[ik] * hY;
+  Xb[m.dest] = xbar * m.xs;
+  const double yv = dneg_if(ybar * ys, hY < 0);
+  Yt[m.dest] = yv;
+  Yf[m.dest + m.dyf] = yv * yfs * hY;
 }
 
 // ------------------------------------------------------------ Pandya inverse
@@ -1473,10 +1431,10 @@ cudaError_t launch_comm122_df(const Space& s, const double* X, const double* Y, 
 }
 
 cudaError_t launch_pandya_fwd(const Space& s, const double* X, const double* Y, int hY, double* Xb, double* Yt,
-                              double* Yf, const int* tiles, int ntiles, cudaStream_t st, const long long* zo, int nz)
+                              double* Yf, cudaStream_t st, const long long* zo, int nz)
 {
-  if (ntiles == 0) return cudaSuccess;
-  k_pandya_fwd<<<dim3(ntiles, 1, nz), 256, 0, st>>>(s.dev, s.work, X, Y, hY, Xb, Yt, Yf, tiles, ntiles, zo);
+  if (s.work.n_pfout == 0) return cudaSuccess;
+  k_pandya_fwd<<<dim3((s.work.n_pfout + 255) / 256, 1, nz), 256, 0, st>>>(s.work, X, Y, hY, Xb, Yt, Yf, zo);
   count_launch();
   return cudaGetLastError();
 }

@@ -10,6 +10,7 @@
 #include "tensor.hpp"
 
 #include <algorithm>
+#include <cstdint>
 #include <cmath>
 #include <cstdlib>
 #include <map>
@@ -66,6 +67,119 @@ void reference_orbits(int emax, int A, int Z, std::vector<int>& n, std::vector<i
           occ.push_back(it == filled.end() ? 0.0 : it->second);
         }
     }
+}
+
+// Descriptors of the Pandya transform of X and Y
+// (DoPandyaTransformation_SingleChannel_XandY, src/Commutator.cc:1392-1485, and
+// the flipped Ybar of comm222_phss, src/Commutator.cc:1766-1788).  For every
+// element (ik, t) of a cross-coupled channel's panels, t over its hh and ph
+// bras and their swapped copies:
+//   Xbar(ik, t) = normfactor (n_a - n_b) sum_J w_J X(e_J),
+//   Ybar(t, ik) = normfactor             sum_J w_J Y(e_J),
+// with w_J = -(2J+1) {j_a j_b J_cc; j_c j_d J} and the swap phases of
+// GetTBME_J_norm folded into its sign, and e_J the arena index of the
+// normalised J-coupled element (c b | a d).  Everything but X and Y is a
+// property of the space, so it is listed once: the kernel is then one gather
+// and FMA per term, in the same order as the J loop it replaces.
+static void build_pandya_fwd(Space& s)
+{
+  constexpr double kSqrt2 = 1.4142135623730950488;
+  // one task per (channel, bra column t): a run of n_cc consecutive outputs
+  std::vector<std::pair<int, int>> tasks;
+  for (int cc = 0; cc < s.nch; ++cc)
+    if (s.cc[cc].n() > 0)
+      for (int t = 0; t < 2 * s.cc_nph[cc]; ++t) tasks.push_back({cc, t});
+  const int ntask = (int)tasks.size();
+  std::vector<std::vector<PfOut>> outs(ntask);
+  std::vector<std::vector<int>> es(ntask);
+  std::vector<std::vector<double>> ws(ntask);
+  bool too_big = false;
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int task = 0; task < ntask; ++task) {
+    const int cc = tasks[task].first, t = tasks[task].second;
+    const Chan& K = s.cc[cc];
+    const int ncc = K.n(), nph = s.cc_nph[cc];
+    const int Jcc = cc / 6;
+    const int* phi = s.phase_tab.data() + s.cc_phase_off[cc];
+    const int ibra = t < nph ? t : t - nph;
+    const int kb = s.cc_ph[s.cc_ph_off[cc] + ibra];
+    const int a = t < nph ? K.p[kb] : K.q[kb], b = t < nph ? K.q[kb] : K.p[kb];
+    const int tf = t < nph ? t + nph : t - nph;
+    std::vector<PfOut>& out = outs[task];
+    std::vector<int>& te = es[task];
+    std::vector<double>& tw = ws[task];
+    out.reserve(ncc);
+    for (int ik = 0; ik < ncc; ++ik) {
+      const int c = K.p[ik], d = K.q[ik];
+      PfOut o{};
+      const int64_t dest = s.xb_off[cc] + (int64_t)t * ncc + ik;
+      if (dest > INT32_MAX) too_big = true;
+      o.dest = (int)dest;
+      o.dyf = (tf - t) * ncc;
+      o.beg = (int)te.size();
+      double nf = 1.0;
+      unsigned nsq = 0;
+      if (s.tz2[a] + s.tz2[d] == s.tz2[b] + s.tz2[c]) {
+        if (a == d) nf *= kSqrt2, ++nsq;
+        if (c == b) nf *= kSqrt2, ++nsq;
+        const int ja = s.j2[a], jb = s.j2[b], jc = s.j2[c], jd = s.j2[d];
+        int jmin = std::max(std::abs(ja - jd), std::abs(jc - jb)) / 2;
+        const int jmax = std::min(ja + jd, jc + jb) / 2;
+        int dJ = 1;
+        if (a == d || c == b) {
+          dJ = 2;
+          jmin += jmin & 1;
+        }
+        const int lc = s.l[c], lb = s.l[b], la = s.l[a], ld = s.l[d];
+        const bool ok = (((lc + lb + la + ld) & 1) == 0) && (s.tz2[c] + s.tz2[b] == s.tz2[a] + s.tz2[d]);
+        if (ok) {
+          const int k1 = ket_index(s.norb, std::min(c, b), std::max(c, b));
+          const int k2 = ket_index(s.norb, std::min(a, d), std::max(a, d));
+          const int par = (lc + lb) & 1, tz = (s.tz2[c] + s.tz2[b]) / 2;
+          const int pcb = (c > b) ? ((jc + jb) / 2 + 1) : 0;
+          const int pad = (a > d) ? ((ja + jd) / 2 + 1) : 0;
+          for (int J = jmin; J <= jmax && J < s.NJ; J += dJ) {
+            const int slot = sixj_slot(s.d1, s.sixj_base.data(), ja, jb, Jcc, jc, jd, J);
+            const double w = slot < 0 ? 0.0 : s.sixj_wval[slot];
+            if (w == 0.0) continue;
+            const int bi = s.ketJ_loc[(size_t)J * s.nkets + k1], ki = s.ketJ_loc[(size_t)J * s.nkets + k2];
+            if (bi < 0 || ki < 0) continue;
+            const Chan& C = s.ch[chan_index(J, par, tz)];
+            const int64_t e = C.off + (int64_t)ki * C.n() + bi;
+            if (e > INT32_MAX) too_big = true;
+            const bool neg = ((c > b) && ((pcb + J) & 1)) != ((a > d) && ((pad + J) & 1));
+            te.push_back((int)e);
+            tw.push_back(neg ? w : -w);  // -(2J+1) 6j with the swap phases
+          }
+        }
+      }
+      o.code = (unsigned)(te.size() - o.beg) | nsq << 16 | (phi[kb] * phi[ik] < 0 ? 1u : 0u) << 18;
+      o.xs = nf * (s.occ[a] - s.occ[b]);
+      out.push_back(o);
+    }
+  }
+  if (too_big) throw std::runtime_error("Pandya transform descriptors: arena index beyond 2^31");
+  size_t nout = 0, nterm = 0;
+  for (int task = 0; task < ntask; ++task) {
+    nout += outs[task].size();
+    nterm += es[task].size();
+  }
+  if (nterm > (size_t)INT32_MAX) throw std::runtime_error("Pandya transform descriptors: more than 2^31 terms");
+  s.pf_out.clear();
+  s.pf_out.reserve(nout);
+  s.pf_e.clear();
+  s.pf_e.reserve(nterm);
+  s.pf_w.clear();
+  s.pf_w.reserve(nterm);
+  for (int task = 0; task < ntask; ++task) {
+    const int base = (int)s.pf_e.size();
+    for (PfOut o : outs[task]) {
+      o.beg += base;
+      s.pf_out.push_back(o);
+    }
+    s.pf_e.insert(s.pf_e.end(), es[task].begin(), es[task].end());
+    s.pf_w.insert(s.pf_w.end(), ws[task].begin(), ws[task].end());
+  }
 }
 
 Space* build_space(int emax, const std::vector<int>& n, const std::vector<int>& l, const std::vector<int>& j2,
@@ -223,6 +337,7 @@ Space* build_space(int emax, const std::vector<int>& n, const std::vector<int>& 
   }
   s.xb_total = xb;
   s.zb_total = zb;
+  build_pandya_fwd(s);
 
   // ---- small-term work lists
   s.hh_off.assign(s.nch + 1, 0);
@@ -386,6 +501,10 @@ void upload_space(Space& s)
   w.xb_off = dev_copy(s, xo);
   w.zb_off = dev_copy(s, zo);
   w.cc_phase_off = dev_copy(s, s.cc_phase_off);
+  w.pf_out = dev_copy(s, s.pf_out);
+  w.n_pfout = (int)s.pf_out.size();
+  w.pf_e = dev_copy(s, s.pf_e);
+  w.pf_w = dev_copy(s, s.pf_w);
 }
 
 // Blocks of the quadruple-ordered inverse Pandya transform (split form).

@@ -70,6 +70,9 @@ struct Space {
   int64_t xb_total = 0, zb_total = 0;
   std::vector<int> cc_phase_off;         // phi of each CC ket (into phase_tab)
   std::vector<SymGemmJob> zbar_jobs;     // head + tail per CC channel
+  std::vector<PfOut> pf_out;             // Pandya transform of X and Y: one per panel element
+  std::vector<int> pf_e;                 // its terms: arena index and signed (2J+1) 6j weight
+  std::vector<double> pf_w;
 
   // ---- small-term work lists
   std::vector<double> ket_wpp, ket_nn;  // per 2b channel ket (flat, channel-major): Mpp / Mhh weights
