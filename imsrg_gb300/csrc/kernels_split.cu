@@ -457,7 +457,7 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
   for (int e = threadIdx.x; e < 32 * (KB / 2); e += 256) {
     const int r = e & 31, tp = e >> 5;
     const int i = r0 + r;
-    unsigned wa[S], wb[S];
+    long long qa2[2], qb2[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int tt = 2 * tp + h, t = t0 + tt;
@@ -480,24 +480,28 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
       // the rest (bias = half * sum_{s >= 1} 2^(beta (S-1-s)), so the digits
       // still sum to q): |d| <= 2^(beta-1) below the top digit,
       // |d_1| <= 2^beta + 1
-      const long long qa2 = qa + bias, qb2 = qb + bias;
+      qa2[h] = qa + bias;
+      qb2[h] = qb + bias;
+    }
+    // small integer -> bf16 bits (exact): the float 1.5*2^23 + x minus
+    // 1.5*2^23, whose upper 16 bits are the bf16 of x; for a lower digit the
+    // "- half" rides in the magic constant.  The two columns' upper halves
+    // are packed into one word by a byte permute.
+    unsigned wa[S], wb[S];
 #pragma unroll
-      for (int s = 0; s < S; ++s) {
-        const int sh = beta * (S - 1 - s);
-        int xa, xb;
-        if (s == 0) {
-          xa = (int)(qa2 >> sh);
-          xb = (int)(qb2 >> sh);
-        } else {
-          xa = (int)((qa2 >> sh) & mask) - (int)half;
-          xb = (int)((qb2 >> sh) & mask) - (int)half;
-        }
-        // small integer -> bf16 bits (exact): 1.5*2^23 magic
-        const unsigned ba = __float_as_uint(__int_as_float(0x4B400000 + xa) - 12582912.0f) >> 16;
-        const unsigned bb = __float_as_uint(__int_as_float(0x4B400000 + xb) - 12582912.0f) >> 16;
-        wa[s] = h ? (wa[s] | (ba << 16)) : ba;
-        wb[s] = h ? (wb[s] | (bb << 16)) : bb;
+    for (int s = 0; s < S; ++s) {
+      const int sh = beta * (S - 1 - s);
+      const int mg = s == 0 ? 0x4B400000 : 0x4B400000 - (int)half;
+      float fa[2], fb[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int xa = s == 0 ? (int)(qa2[h] >> sh) : (int)((unsigned)(qa2[h] >> sh) & (unsigned)mask);
+        const int xb = s == 0 ? (int)(qb2[h] >> sh) : (int)((unsigned)(qb2[h] >> sh) & (unsigned)mask);
+        fa[h] = __int_as_float(mg + xa) - 12582912.0f;
+        fb[h] = __int_as_float(mg + xb) - 12582912.0f;
       }
+      wa[s] = __byte_perm(__float_as_uint(fa[0]), __float_as_uint(fa[1]), 0x7632);
+      wb[s] = __byte_perm(__float_as_uint(fb[0]), __float_as_uint(fb[1]), 0x7632);
     }
 #pragma unroll
     for (int s = 0; s < S; ++s) {
