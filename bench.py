@@ -613,7 +613,10 @@ def run_gb300(args):
     hZ = torch.empty(A, dtype=torch.float64, pin_memory=True)
     dX.download_ptr(hX.data_ptr())
     dY.download_ptr(hY.data_ptr())
-    ne = max(1, min(args.steps, 10))
+    # as many steps as the device-resident timing: the streamed pipeline's
+    # fill (the first upload) and drain (the last download) are inside the
+    # timed region, spread over the same step count
+    ne = max(1, args.steps)
 
     def serial_step():
         dX.upload_ptr(hX.data_ptr())
