@@ -363,27 +363,28 @@ print(json.dumps({"t": t, "threads": o.num_threads()}))
     print(json.dumps(out))
 
 
-def e2e_streamed(ig, ms, prec, hX, hY, hZ, steps, barrier, max_ms):
+def e2e_streamed(ig, ms, prec, hX, hY, hZ, steps, barrier, max_ms, nsets=3):
     """Wall time (ms) of `steps` independent host-to-host commutators through
     the C ABI with copies overlapped: uploads on one stream, commutators on a
     second, downloads on a third (issued from a worker thread, since a
     download returns only when its copy is done).  Events keep each operator
-    set's upload, commutator and download in order across the two sets."""
+    set's upload, commutator and download in order; with `nsets` sets a step's
+    upload may run up to nsets - 1 commutators ahead."""
     import concurrent.futures
     import torch
-    sets = [(ig.DeviceOperator(ms, 1), ig.DeviceOperator(ms, -1), ig.DeviceOperator(ms, 1)) for _ in range(2)]
+    sets = [(ig.DeviceOperator(ms, 1), ig.DeviceOperator(ms, -1), ig.DeviceOperator(ms, 1)) for _ in range(nsets)]
     sH, sC, sD = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
     ptr = {s: ctypes.c_void_p(s.cuda_stream) for s in (sH, sC, sD)}
-    up = [torch.cuda.Event() for _ in range(2)]
-    comp = [torch.cuda.Event() for _ in range(2)]
-    down = [torch.cuda.Event() for _ in range(2)]
-    for b in range(2):
+    up = [torch.cuda.Event() for _ in range(nsets)]
+    comp = [torch.cuda.Event() for _ in range(nsets)]
+    down = [torch.cuda.Event() for _ in range(nsets)]
+    for b in range(nsets):
         for e in (comp[b], down[b]):
             e.record(sC)
     pool = concurrent.futures.ThreadPoolExecutor(max_workers=1)
 
     def upload(k):
-        b = k % 2
+        b = k % nsets
         sH.wait_event(comp[b])  # the commutator that last read this set
         sets[b][0].upload_ptr(hX.data_ptr(), ptr[sH])
         sets[b][1].upload_ptr(hY.data_ptr(), ptr[sH])
@@ -395,19 +396,20 @@ def e2e_streamed(ig, ms, prec, hX, hY, hZ, steps, barrier, max_ms):
 
     barrier()
     t0 = time.perf_counter()
-    upload(0)
+    for k in range(min(nsets - 1, steps)):
+        upload(k)
     pending = []
     for k in range(steps):
-        b = k % 2
-        if k + 1 < steps:
-            upload(k + 1)
+        b = k % nsets
+        if k + nsets - 1 < steps:
+            upload(k + nsets - 1)
         sC.wait_event(up[b])
         sC.wait_event(down[b])  # the download that last read this set's Z
         ig.Commutator.device_commutator(sets[b][0], sets[b][1], sets[b][2], prec, ptr[sC])
         comp[b].record(sC)
         sD.wait_event(comp[b])
         pending.append(pool.submit(download, b))
-        if len(pending) > 1:
+        if len(pending) > nsets - 1:
             pending.pop(0).result()
     for f in pending:
         f.result()
@@ -624,8 +626,9 @@ def run_gb300(args):
         step()
         dZ.download_ptr(hZ.data_ptr())
     serial_ms, _ = timed_steps(serial_step, ne, barrier, max_ms)
-    # streamed: independent commutators with two operator sets; step k+1's
-    # upload and step k-1's download overlap step k's commutator
+    # streamed: independent commutators with three operator sets; the next
+    # steps' uploads and the previous steps' downloads overlap step k's
+    # commutator
     pipe_ms = e2e_streamed(ig, ms, prec, hX, hY, hZ, ne, barrier, max_ms)
     ms.check_status()
     ems = min(serial_ms, pipe_ms)
@@ -635,7 +638,7 @@ def run_gb300(args):
            "serial": {"value": world * ne / (serial_ms / 1000.0), "ms_per_step": serial_ms / ne},
            "streamed": {"value": world * ne / (pipe_ms / 1000.0), "ms_per_step": pipe_ms / ne},
            "note": "per step: H2D of X and Y from pinned host memory, the commutator, D2H of Z, through the C ABI; "
-                   "streamed = uploads / downloads on their own streams, two device operator sets"}
+                   "streamed = uploads / downloads on their own streams, three device operator sets"}
     # ---- the 64-pair batch (emax 2..6, one CUDA graph, both forms)
     batch = None
     if not args.no_batch:
