@@ -518,10 +518,14 @@ __global__ void __launch_bounds__(256) k_pandya_fwd(DevWork W, const double* __r
     xbar = fma(w, X[e], xbar);
     ybar = fma(w, Y[e], ybar);
   }
-  Xb[m.dest] = xbar * m.xs;
-  const double yv = dneg_if(ybar * ys, hY < 0);
+  // the FP64 pipe is this kernel's bound: factors of +-1 (every phase, the
+  // usual normfactor and occupation difference) are sign flips, not
+  // multiplies; the results are the same numbers
+  const double xs = m.xs;
+  Xb[m.dest] = (xs == 1.0 || xs == -1.0) ? dneg_if(xbar, xs < 0.0) : xbar * xs;
+  const double yv = dneg_if(nsq == 0 ? ybar : ybar * ys, hY < 0);
   Yt[m.dest] = yv;
-  Yf[m.dest + m.dyf] = yv * yfs * hY;
+  Yf[m.dest + m.dyf] = dneg_if(yv, (yfs < 0.0) != (hY < 0));
 }
 
 // ------------------------------------------------------------ Pandya inverse
