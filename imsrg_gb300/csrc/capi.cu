@@ -656,14 +656,14 @@ int do_ladder(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaS
 
 // comm222_phss, first half: the Pandya-transformed operands (X bar, Y bar,
 // Y bar flipped) and the zero blocks of Z bar
-int prep_ph(const imsrg_op* X, const imsrg_op* Y, cudaStream_t st)
+int prep_ph(const imsrg_op* X, const imsrg_op* Y, int prec, cudaStream_t st)
 {
   imsrg_space* sp = X->sp;
   Space& s = *sp->s;
   int rc = ensure_scratch(sp, true, false);
   if (rc) return rc;
   ProfScope ps("Pandya transform of X, Y", st);
-  CUDA_TRY(launch_pandya_fwd(s, X->d, Y->d, Y->herm, sp->d_xb, sp->d_yt, sp->d_yf, st));
+  CUDA_TRY(launch_pandya_fwd(s, X->d, Y->d, Y->herm, sp->d_xb, sp->d_yt, sp->d_yf, prec == IMSRG_PREC_SPLIT, st));
   for (auto& zr : sp->zbar_zero) CUDA_TRY(cudaMemsetAsync(sp->d_zb + zr.first, 0, zr.second * sizeof(double), st));
   return IMSRG_OK;
 }
@@ -675,7 +675,7 @@ int do_ph(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStrea
   Space& s = *sp->s;
   int rc = ensure_scratch(sp, true, false);
   if (rc) return rc;
-  if (!prepared && (rc = prep_ph(X, Y, st))) return rc;
+  if (!prepared && (rc = prep_ph(X, Y, prec, st))) return rc;
   ProfScope ps("comm222_phss", st);
   int slot = prof_begin("Build Z_bar", st);
   if (prec == IMSRG_PREC_SPLIT) {
@@ -734,7 +734,7 @@ int commutator_impl(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec,
   CUDA_TRY(cudaStreamWaitEvent(sd, sp->ev_fork, 0));
   const bool split = prec == IMSRG_PREC_SPLIT;
   if (on[T122] && split && (rc = prep_122_df(X, Y, sd))) return rc;
-  if (on[T222PH] && (rc = prep_ph(X, Y, sd))) return rc;
+  if (on[T222PH] && (rc = prep_ph(X, Y, prec, sd))) return rc;
   if ((rc = do_111_110(X, Y, Z, on[T111], on[T110], sd))) return rc;
   if (on[T220] && (rc = do_220(X, Y, Z, sd))) return rc;
   if (on[T121] && (rc = do_121(X, Y, Z, sd))) return rc;
@@ -1574,7 +1574,8 @@ int group_pre(GroupedProducts* g, cudaStream_t st)
     CUDA_TRY(launch_to_ff(s, X->d, sp->d_xf, st, zo, nz, ZR_X, ZR_XF));
     CUDA_TRY(launch_to_ff(s, Y->d, sp->d_yff, st, zo, nz, ZR_Y, ZR_YF));
   }
-  CUDA_TRY(launch_pandya_fwd(s, X->d, Y->d, Y->herm, sp->d_xb, sp->d_yt, sp->d_yf, st, zo, nz));
+  CUDA_TRY(launch_pandya_fwd(s, X->d, Y->d, Y->herm, sp->d_xb, sp->d_yt, sp->d_yf, g->prec == IMSRG_PREC_SPLIT, st,
+                             zo, nz));
   CUDA_TRY(launch_comm111_110(s, X->d, Y->d, Z->d, true, X->herm != Y->herm, st, zo, nz));
   if (X->herm != Y->herm) CUDA_TRY(launch_comm220(s, X->d, Y->d, Z->d, X->herm, st, zo, nz));
   CUDA_TRY(launch_comm121(s, sp->d_holes, X->d, Y->d, Z->d, Z->herm, st, zo, nz));

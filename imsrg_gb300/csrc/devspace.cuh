@@ -81,6 +81,7 @@ struct DevWork {
   const PfOut* pf_out; int n_pfout;  // Pandya transform of X and Y, from descriptors
   const int* pf_e;
   const double* pf_w;
+  const float2* pf_wf;  // pf_w as (hi, lo) float pairs (the split form's double-float sums)
 };
 
 // global index of ket (p, q), p <= q: ModelSpace::Index2 (src/ModelSpace.cc:1108-1118)

@@ -64,7 +64,7 @@ cudaError_t launch_comm122_fused_df(const Space& s, const double* X, const doubl
                                     const long long* zo = nullptr, int nz = 1);
 // (grouped)
 cudaError_t launch_pandya_fwd(const Space& s, const double* X, const double* Y, int hY, double* Xb, double* Yt,
-                              double* Yf, cudaStream_t st, const long long* zo = nullptr, int nz = 1);
+                              double* Yf, bool df, cudaStream_t st, const long long* zo = nullptr, int nz = 1);
 cudaError_t launch_pandya_inv(const Space& s, const double* Zb, double* Z, int hZ, const int* tiles, int ntiles,
                               cudaStream_t st);
 // split form: blocks of orbit quadruples (Space::invq_tasks), double-float sums

@@ -494,6 +494,9 @@ __global__ void k_sym_subtract(DevSpace S, const double* __restrict__ W2, double
 //   Yf(ik, t') = Ybar(t, ik) * normfactor * phi_bra phi_ik hY, t' = t with halves swapped
 // One thread per (ik, t), from the space's descriptors (build_pandya_fwd,
 // space.cpp): the J sum is one gather of X and of Y and two FMAs per term.
+// DF: the J sums in double-float on the FP32 pipe (the split form, whose
+// Z-bar product takes 42-bit digits of these panels); otherwise FP64.
+template <bool DF>
 __global__ void __launch_bounds__(256) k_pandya_fwd(DevWork W, const double* __restrict__ X,
                                                     const double* __restrict__ Y, int hY, double* __restrict__ Xb,
                                                     double* __restrict__ Yt, double* __restrict__ Yf,
@@ -512,11 +515,25 @@ __global__ void __launch_bounds__(256) k_pandya_fwd(DevWork W, const double* __r
   const double ys = nsq == 0 ? 1.0 : nsq == 1 ? kSqrt2 : kSqrt2 * kSqrt2;
   const double yfs = (m.code >> 18) & 1u ? -1.0 : 1.0;
   double xbar = 0.0, ybar = 0.0;
-  for (int k = m.beg; k < m.beg + nterm; ++k) {
-    const int e = __ldg(W.pf_e + k);
-    const double w = __ldg(W.pf_w + k);
-    xbar = fma(w, X[e], xbar);
-    ybar = fma(w, Y[e], ybar);
+  if (DF) {
+    float sx = 0.f, cx = 0.f, sy = 0.f, cy = 0.f;
+    for (int k = m.beg; k < m.beg + nterm; ++k) {
+      const int e = __ldg(W.pf_e + k);
+      const float2 w = __ldg(W.pf_wf + k);
+      df_fma(w, d2ff(X[e]), sx, cx);
+      df_fma(w, d2ff(Y[e]), sy, cy);
+    }
+    float hi = __fadd_rn(sx, cx);
+    xbar = ff2d(hi, __fsub_rn(cx, __fsub_rn(hi, sx)));
+    hi = __fadd_rn(sy, cy);
+    ybar = ff2d(hi, __fsub_rn(cy, __fsub_rn(hi, sy)));
+  } else {
+    for (int k = m.beg; k < m.beg + nterm; ++k) {
+      const int e = __ldg(W.pf_e + k);
+      const double w = __ldg(W.pf_w + k);
+      xbar = fma(w, X[e], xbar);
+      ybar = fma(w, Y[e], ybar);
+    }
   }
   // the FP64 pipe is this kernel's bound: factors of +-1 (every phase, the
   // usual normfactor and occupation difference) are sign flips, not
@@ -1435,10 +1452,11 @@ cudaError_t launch_comm122_df(const Space& s, const double* X, const double* Y, 
 }
 
 cudaError_t launch_pandya_fwd(const Space& s, const double* X, const double* Y, int hY, double* Xb, double* Yt,
-                              double* Yf, cudaStream_t st, const long long* zo, int nz)
+                              double* Yf, bool df, cudaStream_t st, const long long* zo, int nz)
 {
   if (s.work.n_pfout == 0) return cudaSuccess;
-  k_pandya_fwd<<<dim3((s.work.n_pfout + 255) / 256, 1, nz), 256, 0, st>>>(s.work, X, Y, hY, Xb, Yt, Yf, zo);
+  auto kern = df ? k_pandya_fwd<true> : k_pandya_fwd<false>;
+  kern<<<dim3((s.work.n_pfout + 255) / 256, 1, nz), 256, 0, st>>>(s.work, X, Y, hY, Xb, Yt, Yf, zo);
   count_launch();
   return cudaGetLastError();
 }

@@ -505,6 +505,12 @@ void upload_space(Space& s)
   w.n_pfout = (int)s.pf_out.size();
   w.pf_e = dev_copy(s, s.pf_e);
   w.pf_w = dev_copy(s, s.pf_w);
+  std::vector<float2> wf(s.pf_w.size());
+  for (size_t k = 0; k < wf.size(); ++k) {
+    const float hi = (float)s.pf_w[k];
+    wf[k] = make_float2(hi, (float)(s.pf_w[k] - (double)hi));
+  }
+  w.pf_wf = dev_copy(s, wf);
 }
 
 // Blocks of the quadruple-ordered inverse Pandya transform (split form).

@@ -203,6 +203,28 @@ def test_commutator_with_every_tuning(prec):
                             "inverse.desc_results": 2048, "inverse.desc_ilp": 1}[k])
 
 
+def test_seven_digit_ladder_product_vs_fp64():
+    """The split commutator with 7-digit ladder operands (42 bits: the ladder's
+    digit width is 6 bits at emax 8) against the FP64 form on the same
+    operators; exercises the 7-digit product kernel."""
+    emax = 8
+    ms = ig.ModelSpace(emax, "O16", "O16")
+    r = ref_space(emax)
+    with ig.DeviceOperator(ms, 1) as dX, ig.DeviceOperator(ms, -1) as dY, ig.DeviceOperator(ms, 1) as dZ:
+        dX.fill_random(871)
+        dY.fill_random(872)
+        ig.Commutator.device_commutator(dX, dY, dZ, "fp64")
+        ref = dZ.download()
+        try:
+            ms.set_tuning("ladder.digits", 7)
+            ig.Commutator.device_commutator(dX, dY, dZ, "split")
+            out = dZ.download()
+        finally:
+            ms.set_tuning("ladder.digits", 0)
+    errs = rel_errors(r, out, ref)
+    assert max(errs) < TOL["split"], errs
+
+
 @pytest.mark.parametrize("fused", [0, 1])
 def test_comm122_double_float_vs_fp64(fused):
     emax = 8
