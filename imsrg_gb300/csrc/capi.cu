@@ -484,6 +484,9 @@ int ensure_invd(imsrg_space* sp)
     sp->invd.dA = up(plan.dA);
     sp->invd.dB = up(plan.dB);
     sp->invd.nblocks = (int)plan.blocks.size();
+    long long upper = 0;  // upper-triangle elements (diagonal included) of every two-body block
+    for (const Chan& C : sp->s->ch) upper += (long long)C.n() * (C.n() + 1) / 2;
+    sp->invd.covers_all = (long long)plan.dA.size() == upper;
     sp->invd.stage_max = plan.stage_max;
     sp->invd.staged_weights = sp->invd_weights != 0;
   } catch (std::exception& e) {
@@ -497,7 +500,7 @@ int ensure_invd(imsrg_space* sp)
 // AddInversePandyaTransformation of zb into Z with the kernel the space's
 // tuning selects for the form (grouped: nz pairs at the offsets zo)
 int inverse_pandya(imsrg_space* sp, const double* zb, double* Z, int hZ, int prec, cudaStream_t st,
-                   const long long* zo = nullptr, int nz = 1)
+                   const long long* zo = nullptr, int nz = 1, const void* w2 = nullptr, int w2mode = 0)
 {
   Space& s = *sp->s;
   const int variant = prec == IMSRG_PREC_SPLIT ? sp->inv_split : (sp->inv_fp64 ? 2 : 0);
@@ -505,9 +508,10 @@ int inverse_pandya(imsrg_space* sp, const double* zb, double* Z, int hZ, int pre
     int rc = ensure_invd(sp);
     if (rc) return rc;
     sp->invd.ilp = sp->invd_ilp;
-    CUDA_TRY(launch_pandya_inv_desc(s, sp->invd, variant == 1, zb, Z, hZ, st, zo, nz));
+    CUDA_TRY(launch_pandya_inv_desc(s, sp->invd, variant == 1, zb, Z, hZ, st, zo, nz, w2, w2mode));
     return IMSRG_OK;
   }
+  if (w2mode) return fail(IMSRG_ERR_ARG, "comm122ss's update folds only into the descriptor inverse kernel");
   if (prec == IMSRG_PREC_SPLIT && sp->n_invq > 0) {
     CUDA_TRY(launch_pandya_inv_ff(s, zb, Z, hZ, sp->d_invq, sp->n_invq, sp->d_cls_list, sp->d_cls_off, sp->d_cls_sort,
                                   s.invq_smem, st, zo, nz));
@@ -579,8 +583,9 @@ int prep_122_df(const imsrg_op* X, const imsrg_op* Y, cudaStream_t st)
 // FP64 form: FP64 gathers (the plain form keeps every term in FP64).
 // Split form: the same gathers in double-float on the FP32 pipe (prepared:
 // the float-pair copies are already made, on a stream ordered before st).
+// fold_sym: only W2 here; the inverse Pandya kernel applies Z -= W2 + hZ W2^T
 int do_122(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st, int prec = IMSRG_PREC_FP64,
-           bool prepared = false)
+           bool prepared = false, bool fold_sym = false)
 {
   imsrg_space* sp = X->sp;
   int rc = ensure_scratch(sp, false, true);
@@ -593,11 +598,12 @@ int do_122(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, cudaStream_t st, i
                                        sp->n_sym122u, st));
     else
       CUDA_TRY(launch_comm122_df(*sp->s, X->d, Y->d, Z->d, sp->d_xf, sp->d_yff, (float2*)sp->d_w2, Z->herm,
-                                 sp->d_sym122, sp->n_sym122, st));
+                                 sp->d_sym122, sp->n_sym122, st, nullptr, 1, !fold_sym));
     return IMSRG_OK;
   }
   ProfScope ps("comm122ss", st);
-  CUDA_TRY(launch_comm122(*sp->s, X->d, Y->d, Z->d, sp->d_w2, Z->herm, sp->d_sym122, sp->n_sym122, st));
+  CUDA_TRY(launch_comm122(*sp->s, X->d, Y->d, Z->d, sp->d_w2, Z->herm, sp->d_sym122, sp->n_sym122, st, nullptr, 1,
+                          !fold_sym));
   return IMSRG_OK;
 }
 
@@ -669,7 +675,9 @@ int prep_ph(const imsrg_op* X, const imsrg_op* Y, int prec, cudaStream_t st)
 }
 
 // prepared: prep_ph already ran, on a stream ordered before st
-int do_ph(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStream_t st, bool prepared = false)
+// fold_w2: also apply comm122ss's Z -= W2 + hZ W2^T (W2 already computed on st)
+int do_ph(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStream_t st, bool prepared = false,
+          bool fold_w2 = false)
 {
   imsrg_space* sp = X->sp;
   Space& s = *sp->s;
@@ -693,7 +701,8 @@ int do_ph(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec, cudaStrea
   }
   prof_end(slot, st);
   ProfScope pinv("InversePandyaTransformation", st);
-  return inverse_pandya(sp, sp->d_zb, Z->d, Z->herm, prec, st);
+  return inverse_pandya(sp, sp->d_zb, Z->d, Z->herm, prec, st, nullptr, 1, fold_w2 ? (const void*)sp->d_w2 : nullptr,
+                        fold_w2 ? (prec == IMSRG_PREC_SPLIT ? 1 : 2) : 0);
 }
 
 int z_herm(int hx, int hy) { return (hx == hy) ? -1 : 1; }
@@ -743,8 +752,19 @@ int commutator_impl(const imsrg_op* X, const imsrg_op* Y, imsrg_op* Z, int prec,
   if (ladder_first && (rc = do_ladder(X, Y, Z, prec, st, true))) return rc;
   CUDA_TRY(cudaStreamWaitEvent(st, sp->ev_join, 0));
   if (on[T221] && (rc = do_221_1b(X, Y, Z, st, ladder_first ? Z->d : nullptr))) return rc;
-  if (on[T122] && (rc = do_122(X, Y, Z, st, prec, split))) return rc;
-  if (on[T222PH] && (rc = do_ph(X, Y, Z, prec, st, true))) return rc;
+  // comm122ss's final Z -= W2 + hZ W2^T rides in the inverse Pandya kernel,
+  // which reads and writes every upper-triangle element of Z and its mirror
+  // anyway, when that kernel is the descriptor one and lists every element
+  bool fold = false;
+  if (on[T122] && on[T222PH] && !(split && sp->comm122_fused)) {
+    const int variant = split ? sp->inv_split : (sp->inv_fp64 ? 2 : 0);
+    if (variant == 1 || variant == 2) {
+      if ((rc = ensure_invd(sp))) return rc;
+      fold = sp->invd.covers_all;
+    }
+  }
+  if (on[T122] && (rc = do_122(X, Y, Z, st, prec, split, fold))) return rc;
+  if (on[T222PH] && (rc = do_ph(X, Y, Z, prec, st, true, fold))) return rc;
   return IMSRG_OK;
 }
 

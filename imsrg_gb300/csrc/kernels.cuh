@@ -43,7 +43,7 @@ cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, 
 // (grouped)
 cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, double* Z, double* W2, int hZ,
                            const int* sym_tiles, int nsym_tiles, cudaStream_t st, const long long* zo = nullptr,
-                           int nz = 1);
+                           int nz = 1, bool sym = true);
 // loads launch_comm122's kernels on the current device (they are otherwise
 // loaded at their first launch under lazy module loading)
 cudaError_t load_comm122_kernels();
@@ -53,9 +53,10 @@ cudaError_t launch_to_ff(const Space& s, const double* A, float2* Af, cudaStream
                          int nz = 1, int rsrc = ZR_X, int rdst = ZR_XF);
 // split-form comm122ss from the (hi, lo) copies Xf, Yf of X and Y
 // (grouped)
+// sym = false: W2 only (the Z update is folded into the inverse Pandya kernel)
 cudaError_t launch_comm122_df(const Space& s, const double* X, const double* Y, double* Z, const float2* Xf,
                               const float2* Yf, float2* W2, int hZ, const int* sym_tiles, int nsym_tiles,
-                              cudaStream_t st, const long long* zo = nullptr, int nz = 1);
+                              cudaStream_t st, const long long* zo = nullptr, int nz = 1, bool sym = true);
 // the same without the W2 round trip: tile pairs (ch, a, b), a <= b, each
 // forming both W2 tiles in shared memory and updating Z(a, b) and Z(b, a)
 // (grouped)
@@ -98,13 +99,17 @@ struct InvdDev {
   int nblocks = 0, stage_max = 0;
   bool staged_weights = false;  // the 6j weight rows are staged per block (else read from the table)
   int ilp = 1;                  // results each thread keeps in flight (1, 2 or 4)
+  bool covers_all = false;      // one result per upper-triangle Z element (comm122ss's W2 can be folded in)
 };
 // blocks of at most stage_max staged values (and, staging weights, as many
 // weights) and res_max results
 void build_invd(const Space& s, InvdPlan& out, int stage_max, int res_max, bool stage_weights);
 // (grouped)
+// W2 / w2mode: comm122ss's W2 folded into the same update (Z -= W2 + hZ W2^T;
+// 1: (hi, lo) float pairs, 2: FP64), only when d.covers_all and not grouped
 cudaError_t launch_pandya_inv_desc(const Space& s, const InvdDev& d, bool df, const double* Zb, double* Z, int hZ,
-                                   cudaStream_t st, const long long* zo = nullptr, int nz = 1);
+                                   cudaStream_t st, const long long* zo = nullptr, int nz = 1,
+                                   const void* W2 = nullptr, int w2mode = 0);
 // single-operator Pandya transform into the Xbar panel layout (xb_off)
 cudaError_t launch_pandya_single(const Space& s, const double* Z, int herm, int transpose, double* out,
                                  cudaStream_t st);

@@ -196,7 +196,10 @@ void build_invd_part(const Space& s, int i, const std::vector<int> (&cls)[4], In
                 }
                 if (n2 == 0) c2 = 0;
               }
-              if ((c1 == 0 || n1 == 0) && c2 == 0) continue;
+              // an element whose sums vanish by symmetry still gets a result
+              // (z = 0): every upper-triangle element of Z has exactly one, so
+              // the kernel can also apply comm122ss's W2 + h_Z W2^T there
+              if ((c1 == 0 || n1 == 0) && c2 == 0) c1 = 0;
               const int scale = (i == j && k == l) ? 1 : (ev ? 2 : 0);
               const int ib = s.ketJ_loc[(size_t)J * nk + ket_index(N, i, j)];
               const int ik = s.ketJ_loc[(size_t)J * nk + ket_index(N, k, l)];
@@ -411,7 +414,8 @@ __global__ void __launch_bounds__(kThreads) k_pandya_inv_desc(const int4* __rest
                                                               const double* __restrict__ wval,
                                                               const float2* __restrict__ wf,
                                                               const double* __restrict__ Zb, double* __restrict__ Z,
-                                                              int hZ, const long long* __restrict__ zo)
+                                                              int hZ, const long long* __restrict__ zo,
+                                                              const void* __restrict__ W2, int w2mode)
 {
   if (zo) {
     Zb = (const double*)((const char*)Zb + zo[blockIdx.z * kZRoles + ZR_ZB]);
@@ -478,19 +482,39 @@ __global__ void __launch_bounds__(kThreads) k_pandya_inv_desc(const int4* __rest
         ok[u] = !(((b[u].x >> kDiagBit) & 1) && hZ < 0);
       }
     }
+    // comm122ss's Z -= W2 + h_Z W2^T at the same two elements, when the
+    // commutator folds it in here (w2mode 1: W2 as (hi, lo) float pairs,
+    // 2: FP64); W2 has Z's layout
+    double w1[R], w2[R];
 #pragma unroll
     for (int u = 0; u < R; ++u) {
+      w1[u] = 0.0;
+      w2[u] = 0.0;
       if (ok[u]) {
         o1[u] = Z[a[u].z];
         o2[u] = a[u].w >= 0 ? Z[a[u].w] : 0.0;
+        const int q = a[u].w >= 0 ? a[u].w : a[u].z;
+        if (w2mode == 2) {
+          const double wp = __ldg((const double*)W2 + a[u].z), wq = __ldg((const double*)W2 + q);
+          w1[u] = wp + hZ * wq;
+          w2[u] = wq + hZ * wp;
+        } else if (w2mode == 1) {
+          const float2 wp = __ldg((const float2*)W2 + a[u].z), wq = __ldg((const float2*)W2 + q);
+          const float sg = hZ < 0 ? -1.f : 1.f;
+          float hi, lo;
+          df_add(wp.x, wp.y, sg * wq.x, sg * wq.y, hi, lo);
+          w1[u] = ff2d(hi, lo);
+          df_add(wq.x, wq.y, sg * wp.x, sg * wp.y, hi, lo);
+          w2[u] = ff2d(hi, lo);
+        }
       }
     }
 #pragma unroll
     for (int u = 0; u < R; ++u) {
       if (!ok[u]) continue;
       const double z = invd_value<DF, SW>(a[u], b[u], hZ, smem, bk.y, wval, wf);
-      Z[a[u].z] = o1[u] + z;
-      if (a[u].w >= 0) Z[a[u].w] = o2[u] + (hZ > 0 ? z : -z);
+      Z[a[u].z] = w2mode ? (o1[u] + z) - w1[u] : o1[u] + z;
+      if (a[u].w >= 0) Z[a[u].w] = w2mode ? (o2[u] + (hZ > 0 ? z : -z)) - w2[u] : o2[u] + (hZ > 0 ? z : -z);
     }
   }
 }
@@ -498,12 +522,14 @@ __global__ void __launch_bounds__(kThreads) k_pandya_inv_desc(const int4* __rest
 }  // namespace
 
 cudaError_t launch_pandya_inv_desc(const Space& s, const InvdDev& d, bool df, const double* Zb, double* Z, int hZ,
-                                   cudaStream_t st, const long long* zo, int nz)
+                                   cudaStream_t st, const long long* zo, int nz, const void* W2, int w2mode)
 {
+  if (w2mode && (zo || !d.covers_all)) return cudaErrorInvalidValue;
   if (d.nblocks == 0) return cudaSuccess;
   const size_t smem = (size_t)d.stage_max * 8;
   using Kern = void (*)(const int4*, const int2*, const int2*, const int*, const unsigned short*, const int4*,
-                       const int2*, const double*, const float2*, const double*, double*, int, const long long*);
+                       const int2*, const double*, const float2*, const double*, double*, int, const long long*,
+                       const void*, int);
   // [df][staged weights][results in flight: 1, 2, 4]
   static const Kern kerns[2][2][3] = {
       {{k_pandya_inv_desc<false, false, 1>, k_pandya_inv_desc<false, false, 2>, k_pandya_inv_desc<false, false, 4>},
@@ -515,7 +541,7 @@ cudaError_t launch_pandya_inv_desc(const Space& s, const InvdDev& d, bool df, co
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   kern<<<dim3(d.nblocks, 1, nz), kThreads, smem, st>>>(d.blocks, d.wblk, d.wrow, d.sidx, d.sslot, d.dA, d.dB,
-                                                       s.dev.sixj_wval, s.dev.sixj_wf, Zb, Z, hZ, zo);
+                                                       s.dev.sixj_wval, s.dev.sixj_wf, Zb, Z, hZ, zo, W2, w2mode);
   count_launch();
   return cudaGetLastError();
 }

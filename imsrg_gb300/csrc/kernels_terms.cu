@@ -1287,13 +1287,13 @@ cudaError_t launch_comm221_1b(const Space& s, const double* X, const double* Y, 
 }
 
 cudaError_t launch_comm122(const Space& s, const double* X, const double* Y, double* Z, double* W2, int hZ,
-                           const int* sym_tiles, int nsym_tiles, cudaStream_t st, const long long* zo, int nz)
+                           const int* sym_tiles, int nsym_tiles, cudaStream_t st, const long long* zo, int nz, bool sym)
 {
   if (s.work.ncols122 == 0) return cudaSuccess;
   k_comm122_w<<<dim3(s.work.ncols122, 1, nz), 128, 0, st>>>(s.dev, s.work, X, Y, W2, zo);
   count_launch();
   cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  if (e != cudaSuccess || !sym) return e;
   k_sym_subtract<<<dim3(nsym_tiles, 1, nz), 256, 0, st>>>(s.dev, W2, Z, hZ, sym_tiles, nsym_tiles, zo);
   count_launch();
   return cudaGetLastError();
@@ -1439,13 +1439,13 @@ cudaError_t launch_comm122_fused_df(const Space& s, const double* X, const doubl
 
 cudaError_t launch_comm122_df(const Space& s, const double* X, const double* Y, double* Z, const float2* Xf,
                               const float2* Yf, float2* W2, int hZ, const int* sym_tiles, int nsym_tiles,
-                              cudaStream_t st, const long long* zo, int nz)
+                              cudaStream_t st, const long long* zo, int nz, bool sym)
 {
   if (s.work.ncols122 == 0) return cudaSuccess;
   k_comm122_w_df<<<dim3(s.work.ncols122, 1, nz), 128, 0, st>>>(s.dev, s.work, X, Y, Xf, Yf, W2, zo);
   count_launch();
   cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  if (e != cudaSuccess || !sym) return e;
   k_sym_subtract_ff<<<dim3(nsym_tiles, 1, nz), 256, 0, st>>>(s.dev, W2, Z, hZ, sym_tiles, nsym_tiles, zo);
   count_launch();
   return cudaGetLastError();
