@@ -769,12 +769,11 @@ __global__ void __maxnreg__(128) k_split_gemm(const __grid_constant__ CUtensorMa
       const int jm = jp->m, jn = jp->n, ldo = jp->ldo, nosym = jp->nosym, phase_off = jp->phase_off;
       const int jsign = jp->sign, jacc = jp->accumulate;
       const long long exp_base = jp->exp_base, out_off = jp->out_off;
-      // the epilogue warps decide together (named barrier 1), so a timeout
-      // never leaves one of them waiting at a barrier alone
-      if (!mbar_wait(acc_full(tc & 1), (unsigned)((tc >> 1) & 1))) {
-        set_status(g.status, 104);
-        s_epi_err = 1;
-      }
+      // the tile's row and column exponents and phases come from the
+      // exponent pass (before this kernel), not from the MMAs: they are read
+      // while the tile's products still run.  (s_colexp[tc & 1] was last read
+      // for tile tc - 2, which every epilogue warp finished before the
+      // barrier of tile tc - 1.)
       const int c = nosym ? 0 : job_c(g.jobmax, tl.job);
       const int* ph = phase_off >= 0 ? g.phase + phase_off : nullptr;
       // column exponents and phases of this tile (a plain job's columns are
@@ -787,12 +786,6 @@ __global__ void __maxnreg__(128) k_split_gemm(const __grid_constant__ CUtensorMa
                                           : row_exp(g.rexpA[exp_base + j], g.rexpB[exp_base + j], c);
         s_colph[tc & 1][et] = (ph && ok) ? ph[j] : 1;
       }
-      asm volatile("bar.sync 1, %0;" ::"r"(EPI_T) : "memory");
-      if (s_epi_err) {
-        s_err = 1;
-        break;
-      }
-      tc_fence_after();
       const int sign = jsign != 0 ? jsign : g.gsign;
       const int i = tl.I * TILE_M + q * 32 + lane;
       const bool rowok = i < jm;
@@ -800,6 +793,18 @@ __global__ void __maxnreg__(128) k_split_gemm(const __grid_constant__ CUtensorMa
                      : nosym ? own_exp(g.rexpA[exp_base + i])
                                 : row_exp(g.rexpA[exp_base + i], g.rexpB[exp_base + i], c);
       const int phi_i = (ph && rowok) ? ph[i] : 1;
+      // the epilogue warps decide together (named barrier 1), so a timeout
+      // never leaves one of them waiting at a barrier alone
+      if (!mbar_wait(acc_full(tc & 1), (unsigned)((tc >> 1) & 1))) {
+        set_status(g.status, 104);
+        s_epi_err = 1;
+      }
+      asm volatile("bar.sync 1, %0;" ::"r"(EPI_T) : "memory");
+      if (s_epi_err) {
+        s_err = 1;
+        break;
+      }
+      tc_fence_after();
       double* O = g.out + out_off;
       const int Xi = ai + c - g.beta * (S + 1);
       const bool accumulate = g.accum > 0 || (g.accum < 0 && jacc);
