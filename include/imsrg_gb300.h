@@ -342,8 +342,9 @@ int imsrg_batch_info(const imsrg_batch* batch, int* n_pairs, int* n_branches, in
 /* Tuning of a space's kernels: tile shapes, pipeline depth and tile-to-CTA
  * schedules of the split products, and the inverse Pandya kernel and its
  * block sizes.  Parameters (value 0 = the built-in default where allowed):
- *   "ladder.tile", "zbar.tile"          64 (64 columns, one accumulator set)
- *                                       or 32 (32 columns, two sets)
+ *   "ladder.tile", "zbar.tile"          64 (64-column tiles; consecutive
+ *                                       tiles share part of tensor memory) or
+ *                                       32 (32-column tiles, sharing none)
  *   "ladder.stages", "zbar.stages"      pipeline stages, 2..6 (0: most that fit)
  *   "ladder.schedule", "zbar.schedule"  0: tiles dealt round-robin to the
  *                                       persistent CTAs in size order, 1:
