@@ -1406,12 +1406,25 @@ int imsrg_bch_transform(const imsrg_op* OpIn, const imsrg_op* Omega, imsrg_op* O
     std::swap(nested.d, next.d);
     std::swap(nested.herm, next.herm);
     fden /= i;
-    CUDA_TRY(launch_axpy(OpOut->d, nested.d, fden, sp->s->arena, st));
+    // OpOut += fden nested and the norm of nested in one pass, then one
+    // host sync for the norm and (split form) the kernels' status word
+    CUDA_TRY(launch_axpy_norm(*sp->s, OpOut->d, nested.d, fden, sp->d_norm_off, sp->d_norm_len, sp->d_norm_w,
+                              sp->n_norm, sp->d_norm_partial, st));
     if (n_nested) *n_nested = i;
     epsilon *= i + 1;
-    double nn = 0;
-    if ((rc = norm_impl(&nested, &nn, st))) return rc;
-    if (precision == IMSRG_PREC_SPLIT && (rc = check_status(sp, st))) return rc;
+    CUDA_TRY(cudaMemcpyAsync(sp->h_norm_partial.data(), sp->d_norm_partial, (sp->n_norm + 1) * sizeof(double),
+                             cudaMemcpyDeviceToHost, st));
+    int hstat = 0;
+    if (precision == IMSRG_PREC_SPLIT)
+      CUDA_TRY(cudaMemcpyAsync(&hstat, sp->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (hstat != 0) {
+      cudaMemsetAsync(sp->d_status, 0, sizeof(int), st);
+      return fail(IMSRG_ERR_KERNEL, "a kernel reported error status " + std::to_string(hstat));
+    }
+    double n2 = 0.0;
+    for (int c = 0; c < sp->n_norm; ++c) n2 += sp->h_norm_partial[c];
+    const double nn = std::sqrt(sp->h_norm_partial[sp->n_norm] + n2);
     if (nn < epsilon) break;
   }
   return IMSRG_OK;

@@ -129,6 +129,11 @@ cudaError_t launch_generator(const Space& s, const double* H, double* Eta, doubl
                              cudaStream_t st);
 cudaError_t launch_axpy(double* y, const double* x, double a, long long n, cudaStream_t st);
 cudaError_t launch_scale(double* y, double a, long long n, cudaStream_t st);
+// y += a x and the norm pieces of x (as launch_norm: partial[0..nchunks) the
+// two-body chunks, partial[nchunks] the one-body part); x must have zero padding
+cudaError_t launch_axpy_norm(const Space& s, double* y, const double* x, double a, const long long* chunk_off,
+                             const int* chunk_len, const double* chunk_w, int nchunks, double* partial,
+                             cudaStream_t st);
 cudaError_t launch_norm(const Space& s, const double* A, const long long* chunk_off, const int* chunk_len,
                         const double* chunk_w, int nchunks, double* partial, cudaStream_t st);
 

@@ -1216,6 +1216,46 @@ __global__ void k_norm_chunks(const double* __restrict__ A, const long long* __r
   }
 }
 
+// y += a x together with the pieces of x's norm (the BCH loop adds each
+// nested commutator and tests its norm): block c < nchunks does norm chunk c
+// of the two-body blocks, block nchunks the zero- and one-body parts.  x is a
+// commutator result, whose padding between blocks is zero, so those words of
+// y are left as they are.
+__global__ void k_axpy_norm(DevSpace S, double* __restrict__ y, const double* __restrict__ x, double a,
+                            const long long* __restrict__ chunk_off, const int* __restrict__ chunk_len,
+                            const double* __restrict__ chunk_w, double* __restrict__ partial, int nchunks)
+{
+  __shared__ double red[32];
+  const int c = blockIdx.x;
+  double s = 0.0;
+  if (c < nchunks) {
+    const long long off = chunk_off[c];
+    const int len = chunk_len[c];
+    for (int t = threadIdx.x; t < len; t += blockDim.x) {
+      const double v = x[off + t];
+      y[off + t] = fma(a, v, y[off + t]);
+      s = fma(v, v, s);
+    }
+  } else {
+    const int N = S.norb;
+    if (threadIdx.x == 0) y[0] = fma(a, x[0], y[0]);
+    for (int t = threadIdx.x; t < N * N; t += blockDim.x) {
+      const int p = t % N, q = t / N;
+      const double v = x[32 + t];
+      y[32 + t] = fma(a, v, y[32 + t]);
+      if (S.l[p] == S.l[q] && S.j2[p] == S.j2[q] && S.tz2[p] == S.tz2[q]) s += v * v * (S.j2[p] + 1);
+    }
+  }
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) partial[c] = c < nchunks ? v * chunk_w[c] : v;
+  }
+}
+
 // one-body norm: sum over p, q in one channel of (2 j_p + 1) O_pq^2
 __global__ void k_norm_onebody(DevSpace S, const double* __restrict__ A, double* __restrict__ out)
 {
@@ -1525,6 +1565,16 @@ cudaError_t launch_axpy(double* y, const double* x, double a, long long n, cudaS
 cudaError_t launch_scale(double* y, double a, long long n, cudaStream_t st)
 {
   k_scale<<<stride_grid(n, 1216), 256, 0, st>>>(y, a, n);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_axpy_norm(const Space& s, double* y, const double* x, double a, const long long* chunk_off,
+                             const int* chunk_len, const double* chunk_w, int nchunks, double* partial,
+                             cudaStream_t st)
+{
+  // the one-body block first: it is the longest
+  k_axpy_norm<<<nchunks + 1, 256, 0, st>>>(s.dev, y, x, a, chunk_off, chunk_len, chunk_w, partial, nchunks);
   count_launch();
   return cudaGetLastError();
 }
