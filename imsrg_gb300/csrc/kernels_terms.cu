@@ -285,16 +285,30 @@ __global__ void __launch_bounds__(128) k_comm122_w_df(DevSpace S, DevWork W, con
     cl[t] = W.it122_loc[first + t];
   }
   __syncthreads();
-  for (int r = threadIdx.x; r < n; r += blockDim.x) {
-    float s = 0.f, c = 0.f;
+  // two rows per thread and pass (r and r + blockDim.x): the item's
+  // coefficients and column address are read once for both
+  for (int r0 = threadIdx.x; r0 < n; r0 += 2 * blockDim.x) {
+    const int r1 = r0 + blockDim.x;
+    const bool two = r1 < n;
+    float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
     for (int t = 0; t < cnt; ++t) {
-      long long e = off + (long long)cl[t] * n + r;
-      df_fma(cx[t], Yf[e], s, c);
-      df_fma(cy[t], Xf[e], s, c);
+      const long long e = off + (long long)cl[t] * n + r0;
+      const float2 ax = cx[t], ay = cy[t];
+      df_fma(ax, Yf[e], s0, c0);
+      df_fma(ay, Xf[e], s0, c0);
+      if (two) {
+        df_fma(ax, Yf[e + blockDim.x], s1, c1);
+        df_fma(ay, Xf[e + blockDim.x], s1, c1);
+      }
     }
-    float hi = __fadd_rn(s, c);
-    float lo = __fsub_rn(c, __fsub_rn(hi, s));
-    W2[off + (long long)ij * n + r] = make_float2(hi, lo);
+    float hi = __fadd_rn(s0, c0);
+    float lo = __fsub_rn(c0, __fsub_rn(hi, s0));
+    W2[off + (long long)ij * n + r0] = make_float2(hi, lo);
+    if (two) {
+      hi = __fadd_rn(s1, c1);
+      lo = __fsub_rn(c1, __fsub_rn(hi, s1));
+      W2[off + (long long)ij * n + r1] = make_float2(hi, lo);
+    }
   }
 }
 
