@@ -453,26 +453,45 @@ __global__ void __launch_bounds__(256) k_split_digits(const SplitJob* __restrict
 #pragma unroll
   for (int s = 1; s < S; ++s) bias += half << (beta * (S - 1 - s));
   // column pair (tt, tt + 1) of row r: thread layout r fastest (coalesced
-  // column reads), the two digits of a pair packed in one 32-bit word
-  for (int e = threadIdx.x; e < 32 * (KB / 2); e += 256) {
+  // column reads), the two digits of a pair packed in one 32-bit word.  Every
+  // operand value of the thread's pairs is requested before the first is
+  // converted (the pass is bound by those loads)
+  constexpr int NIT = 32 * (KB / 2) / 256;
+  double va[NIT][2], vb[NIT][2];
+#pragma unroll
+  for (int u = 0; u < NIT; ++u) {
+    const int e = threadIdx.x + u * 256;
     const int r = e & 31, tp = e >> 5;
     const int i = r0 + r;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int tt = 2 * tp + h, t = t0 + tt;
+      va[u][h] = 0.0;
+      vb[u][h] = 0.0;
+      if (!PLAIN ? (i < jb.m && t < jb.K) : (t < jb.K && (i < jb.m || i < jb.n))) {
+        const int col = s_col[tt];
+        if (!PLAIN || i < jb.m) va[u][h] = A[(long long)col * jb.lda + i];
+        if (!PLAIN || i < jb.n) vb[u][h] = B[(long long)col * jb.ldb + i];
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < NIT; ++u) {
+    const int e = threadIdx.x + u * 256;
+    const int r = e & 31, tp = e >> 5;
     long long qa2[2], qb2[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int tt = 2 * tp + h, t = t0 + tt;
       long long qa = 0, qb = 0;
-      if (!PLAIN ? (i < jb.m && t < jb.K) : (t < jb.K && (i < jb.m || i < jb.n))) {
-        const int col = s_col[tt], code = s_code[tt];
-        if (!PLAIN || i < jb.m) qa = to_fixed(A[(long long)col * jb.lda + i], rowA[r], P);
-        if (!PLAIN || i < jb.n) {
-          const double vb = B[(long long)col * jb.ldb + i];
-          if (code == SC_GENERAL) {
-            qb = to_fixed(vb * s_sc[tt], rowB[r], P);
-          } else {
-            qb = to_fixed(vb, rowB[r] - (code >> 1), P);
-            if (code & 1) qb = -qb;
-          }
+      if (t < jb.K) {  // the values outside the job are 0.0 and give 0
+        const int code = s_code[tt];
+        qa = to_fixed(va[u][h], rowA[r], P);
+        if (code == SC_GENERAL) {
+          qb = to_fixed(vb[u][h] * s_sc[tt], rowB[r], P);
+        } else {
+          qb = to_fixed(vb[u][h], rowB[r] - (code >> 1), P);
+          if (code & 1) qb = -qb;
         }
       }
       // balanced digits by one biased add: the lower digits are the beta-bit
