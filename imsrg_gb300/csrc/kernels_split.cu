@@ -311,7 +311,23 @@ __global__ void __launch_bounds__(256) k_split_rowexp(const SplitJob* __restrict
   const double* B = (jb.bsel ? B1 : B0) + jb.b_off;
   if (!PLAIN) {
     if (i < jb.m) {
-      for (int t = t0 + ty; t < tend; t += 8) {
+      // four columns' loads in flight per thread (the pass is bound by them)
+      int t = t0 + ty;
+      for (; t + 24 < tend; t += 32) {
+        double a[4], b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int col = s_col[t + 8 * u - t0];
+          a[u] = A[(long long)col * jb.lda + i];
+          b[u] = B[(long long)col * jb.ldb + i];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          ea = max(ea, dexp(a[u]));
+          eb = max(eb, dexp_scaled(b[u], s_code[t + 8 * u - t0], s_sc[t + 8 * u - t0]));
+        }
+      }
+      for (; t < tend; t += 8) {
         const int col = s_col[t - t0];
         ea = max(ea, dexp(A[(long long)col * jb.lda + i]));
         eb = max(eb, dexp_scaled(B[(long long)col * jb.ldb + i], s_code[t - t0], s_sc[t - t0]));
