@@ -248,7 +248,15 @@ __global__ void k_to_ff(const double* __restrict__ src, float2* __restrict__ dst
   src = zsh(src, zo, rsrc);
   dst = zsh(dst, zo, rdst);
   long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  long long stride = (long long)gridDim.x * blockDim.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  // four loads in flight per thread, then the conversions and stores
+  for (; i + 3 * stride < n; i += 4 * stride) {
+    double v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = src[i + u * stride];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) dst[i + u * stride] = d2ff(v[u]);
+  }
   for (; i < n; i += stride) dst[i] = d2ff(src[i]);
 }
 
