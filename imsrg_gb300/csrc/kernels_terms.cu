@@ -1253,7 +1253,22 @@ __global__ void k_axpy_norm(DevSpace S, double* __restrict__ y, const double* __
   if (c < nchunks) {
     const long long off = chunk_off[c];
     const int len = chunk_len[c];
-    for (int t = threadIdx.x; t < len; t += blockDim.x) {
+    int t = threadIdx.x;
+    // four elements' loads in flight per thread
+    for (; t + 3 * (int)blockDim.x < len; t += 4 * blockDim.x) {
+      double v[4], w[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        v[u] = x[off + t + u * blockDim.x];
+        w[u] = y[off + t + u * blockDim.x];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        y[off + t + u * blockDim.x] = fma(a, v[u], w[u]);
+        s = fma(v[u], v[u], s);
+      }
+    }
+    for (; t < len; t += blockDim.x) {
       const double v = x[off + t];
       y[off + t] = fma(a, v, y[off + t]);
       s = fma(v, v, s);
