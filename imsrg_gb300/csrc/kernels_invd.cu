@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(kThreads) k_pandya_inv_desc(const int4* __rest
   const int2 wb = wblk[blockIdx.x];
   const int tid = threadIdx.x;
   // 1. staging: the block's 6j weight rows, then its Zbar values (in address
-  //    order, each to its slot), four loads in flight per thread
+  //    order, each to its slot), eight loads in flight per thread
   for (int r = tid; SW && r < wb.y; r += kThreads) {
     const int2 row = __ldg(wrow + wb.x + r);
     const int o = bk.y + (row.y & 0xFFFFF), n = row.y >> 20;
@@ -440,17 +440,17 @@ __global__ void __launch_bounds__(kThreads) k_pandya_inv_desc(const int4* __rest
   {
     const int* si = sidx + bk.x;
     const unsigned short* sl = sslot + bk.x;
-    for (int e0 = tid; e0 < bk.y; e0 += 4 * kThreads) {
-      double v[4];
-      int w[4];
+    for (int e0 = tid; e0 < bk.y; e0 += 8 * kThreads) {
+      double v[8];
+      int w[8];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < 8; ++u) {
         const int e = e0 + u * kThreads;
         w[u] = e < bk.y ? __ldg(si + e) : 0;
         v[u] = e < bk.y ? __ldg(Zb + (w[u] & kIdxMask)) : 0.0;
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < 8; ++u) {
         const int e = e0 + u * kThreads;
         const bool neg = ((w[u] >> kNegBit) & 1) != (((w[u] >> kHzBit) & 1) && hZ < 0);
         if (neg) v[u] = -v[u];
